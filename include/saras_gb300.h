@@ -1,0 +1,225 @@
+/*
+ * saras_gb300.h -- C ABI of the GB300-native SARAS time-step hot path.
+ *
+ * One opaque context (saras_ctx) owns every device buffer of one SARAS solver
+ * instance (velocity, pressure, temperature, the multigrid level hierarchy and
+ * all temporaries) plus one CUDA stream.  Arrays cross the boundary as plain
+ * host pointers in the reference layout: C order (k fastest), ghost width 1,
+ * logical index range -1 .. n along each axis, so a field with core extent
+ * (nx, ny, nz) occupies (nx+2)*(ny+2)*(nz+2) doubles.
+ *
+ * Every entry point returns an int status (SARAS_OK on success).  Calls are
+ * stream-ordered; calls that return a scalar to the host synchronise.
+ *
+ * Each declaration names the reference interface (file:line, paths inside the
+ * roshansamuel/saras repository) whose behaviour it reproduces.
+ */
+#ifndef SARAS_GB300_H
+#define SARAS_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+enum saras_status {
+    SARAS_OK = 0,
+    SARAS_NOT_CONVERGED = 1,     /* CN Jacobi hit maxIterations (hydro_d3.cc:415-421) */
+    SARAS_DIVERGENCE_LIMIT = 2,  /* max divergence > 1e5 (tseries.cc:141-145)        */
+    SARAS_BAD_CONFIG = 3,        /* parameter check failed (parser.cc:250-352)        */
+    SARAS_CUDA_ERROR = 4,
+    SARAS_BAD_ARG = 5,
+    SARAS_NO_DEVICE = 6,
+    SARAS_NOT_FINITE = 7,        /* NaN/Inf detected in a solver residual            */
+    SARAS_TOO_LARGE = 8          /* request exceeds a fixed capacity                 */
+};
+
+/* ---------------------------------------------------------------- fields */
+enum saras_field {
+    SARAS_FIELD_VX = 0,      /* vfield V.Vx  (x face-centred)              vfield.cc:64  */
+    SARAS_FIELD_VY = 1,      /* vfield V.Vy                                vfield.cc:65  */
+    SARAS_FIELD_VZ = 2,      /* vfield V.Vz                                vfield.cc:66  */
+    SARAS_FIELD_P = 3,       /* sfield P (vertex grid)                     hydro.cc:62   */
+    SARAS_FIELD_T = 4,       /* sfield T (vertex grid, scalar solver only) scalar.cc:63  */
+    SARAS_FIELD_PP = 5,      /* plainsf Pp, pressure correction            hydro.cc:67   */
+    SARAS_FIELD_MGRHS = 6,   /* plainsf mgRHS, Poisson right-hand side     hydro.cc:68   */
+    SARAS_FIELD_NSE_X = 7,   /* plainvf nseRHS.Vx                          hydro.cc:69   */
+    SARAS_FIELD_NSE_Y = 8,
+    SARAS_FIELD_NSE_Z = 9,
+    SARAS_FIELD_TRHS = 10,   /* plainsf tmpRHS (scalar solver only)        scalar.cc:64  */
+    SARAS_FIELD_GRAD_X = 11, /* plainvf pressureGradient.Vx                hydro.cc:71   */
+    SARAS_FIELD_GRAD_Y = 12,
+    SARAS_FIELD_GRAD_Z = 13,
+    SARAS_NUM_FIELDS = 14
+};
+
+/* Multigrid modes (GB300 extension; SARAS_MG_REFERENCE is the drop-in). */
+enum saras_mg_mode {
+    SARAS_MG_REFERENCE = 0,  /* FP64 V-cycles, stop on |delta residual| < tol  poisson.cc:132-148 */
+    SARAS_MG_PLAIN_TARGET = 1, /* FP64 V-cycles until max|b-Ap|/max|b| <= target              */
+    SARAS_MG_MIXED = 2       /* FP32 V-cycles inside FP64 iterative refinement to the target   */
+};
+
+/* Initial guess sources for the pressure-correction solve. */
+enum saras_guess {
+    SARAS_GUESS_PREVIOUS = 0, /* previous Pp (reference behaviour, poisson.cc:115) */
+    SARAS_GUESS_LEARNED = 1   /* U-Net guess with fallback to the previous Pp      */
+};
+
+/*
+ * Solver parameters: the fields of the reference parser (parser.h:63-123) that
+ * the hot path reads, plus the GB300 extensions at the end.  Fill with
+ * saras_default_params() and/or saras_parse_yaml().
+ */
+typedef struct saras_params {
+    /* "Program" */
+    int probType, icType, rbcType, forceType;
+    int xPer, yPer, zPer;            /* from "Domain Type" (parser.cc:406-414) */
+    double Re, Ra, Pr, Ro, Ta;
+    double Lx, Ly, Lz;
+    int nonHgBC;
+    double patchRadius;
+    /* "Mesh" */
+    int xGrid, yGrid, zGrid;         /* 0 uniform, 1/2 tanh (from "Mesh Type") */
+    double betaX, betaY, betaZ;
+    int xInd, yInd, zInd;
+    /* "Parallel" */
+    int nThreads, npX, npY;
+    /* "Solver" */
+    int dScheme, iScheme;
+    double cnTolerance;
+    int restartFlag, useCFL;
+    double courantNumber, tStp, tMax;
+    int ioCnt, solnFormat;
+    double fwInt, rsInt;
+    int readProbes;
+    double prInt;
+    /* "Multigrid" */
+    int vcDepth, vcCount;
+    double mgTolerance;
+    int gsSmooth, preSmooth, postSmooth, resType, printResidual;
+    /* GB300 extensions ("GB300" section of parameters.yaml) */
+    int testPoisson;          /* Dirichlet r^2/6 multigrid check (TEST_POISSON build flag) */
+    int mgMode;               /* enum saras_mg_mode */
+    double mgTarget;          /* residual target of the PLAIN_TARGET / MIXED modes */
+    int mgMaxCycles;          /* cap on V-cycles (target modes)                 */
+    int mixedCycles;          /* FP32 V-cycles per refinement step              */
+    int guessMode;            /* enum saras_guess                               */
+    double jacobiWeight;      /* damping of the Jacobi smoother (1.0 = reference) */
+    int seed;
+} saras_params;
+
+typedef struct saras_step_stats {
+    int cn_iters[4];          /* Jacobi iterations for Vx, Vy, Vz, T */
+    int vcycles;              /* V-cycles in this step (FP64 or FP32) */
+    int refine_steps;         /* FP64 refinement steps (mixed mode)  */
+    int coarse_iters;         /* coarsest-level Gauss-Seidel iterations */
+    double mg_residual;       /* last value of computeError (poisson_d3.cc:391-459) */
+    double fine_residual;     /* FP64 max|b-Ap|/max|b| after the solve (target modes) */
+    double guess_residual;    /* FP64 residual of the chosen initial guess */
+    int guess_source;         /* 0 previous Pp, 1 network */
+    int status;
+} saras_step_stats;
+
+typedef struct saras_ctx saras_ctx;
+
+/* ------------------------------------------------------ setup / teardown */
+int saras_default_params(saras_params *p);
+/* Reads input/parameters.yaml (parser.cc:69-239) and validates (parser.cc:250-352). */
+int saras_parse_yaml(const char *path, saras_params *p, char *err, int errlen);
+/* Builds grid, fields, multigrid hierarchy on the current CUDA device
+ * (grid.cc:59-136, hydro.cc:60-75, poisson_d3.cc:64-87).  Fields start at 0. */
+int saras_create(const saras_params *p, saras_ctx **out);
+int saras_destroy(saras_ctx *ctx);
+const char *saras_last_error(const saras_ctx *ctx);
+/* Padded extents (n+2 per axis) of a field. */
+int saras_field_dims(const saras_ctx *ctx, int field, int dims[3]);
+int saras_upload(saras_ctx *ctx, int field, const double *host);
+int saras_download(saras_ctx *ctx, int field, double *host);
+int saras_synchronize(saras_ctx *ctx);
+/* Number of device kernels this context has launched so far. */
+long long saras_launch_count(const saras_ctx *ctx);
+
+/* ------------------------------------------------------ boundary fills */
+/* hydro::imposeUBCs/VBCs/WBCs (hydro.cc:386-461), scalar::imposeTBCs (scalar.cc:240-255):
+ * syncData (mpidata.cc:278-306, np=1 semantics) followed by the wall objects of
+ * hydro::initVBC / scalar::initTBC (hydro.cc:287-371, scalar.cc:185-227). */
+int saras_apply_bc(saras_ctx *ctx, int field);
+/* field::syncData alone (mpidata.cc:278-306). */
+int saras_sync_field(saras_ctx *ctx, int field);
+
+/* ------------------------------------------------------ field operators */
+/* vfield::computeDiff(nseRHS) (vfield.cc:104-146): nseRHS(core) += Laplacian(V). */
+int saras_vfield_compute_diff(saras_ctx *ctx);
+/* vfield::computeNLin(V, nseRHS) (vfield.cc:163-253): nseRHS(core) -= (V.grad)V. */
+int saras_vfield_compute_nlin(saras_ctx *ctx);
+/* sfield::gradient(pressureGradient, V) of P or Pp (sfield.cc:155-171, plainsf.h:92-98). */
+int saras_sfield_gradient(saras_ctx *ctx, int scalar_field);
+/* vfield::divergence(mgRHS, P) (vfield.cc:299-320). */
+int saras_vfield_divergence(saras_ctx *ctx);
+/* sfield::computeDiff / computeNLin of T into tmpRHS (sfield.cc:86-142). */
+int saras_tfield_compute_diff(saras_ctx *ctx);
+int saras_tfield_compute_nlin(saras_ctx *ctx);
+/* Whole-array field arithmetic used by timeAdvance (field.cc:631-715, plainvf.cc:91-224):
+ * dst = a*dst + b*src over the padded array (src < 0: no src term). */
+int saras_axpby(saras_ctx *ctx, int dst, double a, int src, double b);
+
+/* ------------------------------------------------------ implicit solves */
+/* hydro_d3::solveVx/Vy/Vz (hydro_d3.cc:370-533), scalar_d3::solveVx..solveT
+ * (scalar_d3.cc:373-591).  component: 0,1,2 = Vx,Vy,Vz, 3 = T. */
+int saras_cn_solve(saras_ctx *ctx, int component, int *iters, double *max_error);
+/* poisson::mgSolve(Pp, mgRHS) (poisson.cc:100-205). */
+int saras_mg_solve(saras_ctx *ctx, int *vcycles, double *residual);
+int saras_mg_set_mode(saras_ctx *ctx, int mode, double target, int max_cycles);
+
+/* ------------------------------------------------------ time stepping */
+/* hydro_d3::timeAdvance (hydro_d3.cc:254-368) or scalar_d3::timeAdvance
+ * (scalar_d3.cc:243-370), chosen by probType (main.cc:92-136). */
+int saras_time_advance(saras_ctx *ctx, saras_step_stats *stats);
+/* tseries::writeTSData (tseries.cc:137-178, 195-246): energy, signed max
+ * divergence and (scalar runs) Nusselt number. */
+int saras_diagnostics(saras_ctx *ctx, double *energy, double *max_div, double *nusselt);
+
+/* ------------------------------------------------------ multigrid test hooks */
+/* multigrid_d3::testProlong / testTransfer / testPeriodic (poisson_d3.cc:689-857)
+ * and hydro_d3::testPeriodic (hydro_d3.cc:536-679); each returns the max error. */
+int saras_mg_test_prolong(saras_ctx *ctx, double *err);
+int saras_mg_test_transfer(saras_ctx *ctx, double *err);
+int saras_mg_test_periodic(saras_ctx *ctx, double *err);
+int saras_hydro_test_periodic(saras_ctx *ctx, double *err);
+/* Level arrays of the hierarchy (poisson.h:70-73): which = 0 pressureData,
+ * 1 residualData.  Extents of level l are (2^(ind-l)+1)+2 per axis. */
+int saras_mg_level_dims(const saras_ctx *ctx, int level, int dims[3]);
+int saras_mg_set_level(saras_ctx *ctx, int level, int which, const double *host);
+int saras_mg_get_level(saras_ctx *ctx, int level, int which, double *host);
+/* One call of multigrid_d3::smooth(count) at a level (poisson_d3.cc:114-187),
+ * computeResidual + coarsen from level to level+1 (poisson_d3.cc:90-111,250-298),
+ * prolong from level+1 to level and add the saved level data (poisson_d3.cc:301-388,
+ * poisson.cc:271), and computeError at level 0 (poisson_d3.cc:391-459). */
+int saras_mg_smooth(saras_ctx *ctx, int level, int count);
+int saras_mg_restrict(saras_ctx *ctx, int level);
+int saras_mg_prolong_add(saras_ctx *ctx, int level);
+int saras_mg_compute_error(saras_ctx *ctx, int norm, double *err);
+
+/* ------------------------------------------------------ learned warm start */
+/* Records (divergence, P_prev, P_prev2) -> Pp training pairs from the plain
+ * solver, trains the U-Net for `iters` Adam steps, returns the last loss. */
+int saras_unet_collect(saras_ctx *ctx);
+int saras_unet_train(saras_ctx *ctx, int iters, double lr, double *loss);
+int saras_unet_infer(saras_ctx *ctx, int field_out);
+int saras_set_guess_mode(saras_ctx *ctx, int mode);
+
+/* ------------------------------------------------------ measurement */
+/* Per-kernel CUDA-event timing on the context stream.  kernel ids are listed
+ * by saras_profile_name(); only launches at multigrid level 0 are recorded for
+ * level kernels.  Bytes are the algorithmic bytes of the recorded launches. */
+int saras_profile_enable(saras_ctx *ctx, int kernel_id, int enable);
+int saras_profile_read(saras_ctx *ctx, int kernel_id, long long *launches,
+                       double *total_ms, double *bytes);
+const char *saras_profile_name(int kernel_id);
+int saras_profile_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SARAS_GB300_H */

@@ -1,0 +1,370 @@
+"""saras_gb300 -- GB300-native SARAS time-step hot path.
+
+Host-side mirror of the reference's solver interfaces over the C ABI of
+``include/saras_gb300.h``:
+
+* :func:`parser` reads ``input/parameters.yaml`` (lib/io/parser.cc).
+* :class:`Solver` owns one device context: the fields of ``hydro`` /
+  ``scalar`` (V, P, T, Pp, mgRHS, nseRHS, ...), the multigrid hierarchy of
+  ``multigrid_d3`` and every operator of lib/field and lib/boundary.
+* :class:`hydro_d3` / :class:`scalar_d3` reproduce the constructors and
+  ``solvePDE`` loops of src/solvers/hydro/hydro_d3.cc and
+  src/solvers/scalar/scalar_d3.cc on top of :class:`Solver`.
+
+All compute runs in the CUDA library; when it is missing or no GPU is visible
+every call raises -- there is no CPU fallback.
+"""
+import ctypes
+import math
+
+import numpy as np
+
+from . import _abi
+from ._abi import (saras_params, saras_step_stats, default_params, FIELD_VX, FIELD_VY, FIELD_VZ, FIELD_P,
+                   FIELD_T, FIELD_PP, FIELD_MGRHS, FIELD_NSE_X, FIELD_NSE_Y, FIELD_NSE_Z, FIELD_TRHS,
+                   FIELD_GRAD_X, FIELD_GRAD_Y, FIELD_GRAD_Z, MG_REFERENCE, MG_PLAIN_TARGET, MG_MIXED,
+                   GUESS_PREVIOUS, GUESS_LEARNED)
+
+__all__ = ["SarasError", "Solver", "parser", "hydro_d3", "scalar_d3", "default_params", "build"]
+
+
+class SarasError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (_abi.STATUS_NAMES.get(status, status), msg))
+        self.status = status
+
+
+def build(verbose=False):
+    from .build import build as _b
+    return _b(verbose=verbose)
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def parser(path):
+    """parser::parser (lib/io/parser.cc:47-59): read and check parameters.yaml."""
+    lib = _abi.load()
+    p = saras_params()
+    err = ctypes.create_string_buffer(512)
+    s = lib.saras_parse_yaml(path.encode(), ctypes.byref(p), err, 512)
+    if s != 0:
+        raise SarasError(s, err.value.decode())
+    return p
+
+
+class Solver:
+    """One GB300 solver context (grid + fields + multigrid hierarchy)."""
+
+    def __init__(self, params):
+        self.lib = _abi.load()
+        self.params = params
+        h = ctypes.c_void_p()
+        s = self.lib.saras_create(ctypes.byref(params), ctypes.byref(h))
+        if s != 0:
+            raise SarasError(s, self.lib.saras_last_error(None).decode())
+        self.h = h
+
+    # -- lifetime
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.saras_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _chk(self, s):
+        if s != 0:
+            raise SarasError(s, self.lib.saras_last_error(self.h).decode())
+        return s
+
+    # -- data movement
+    def dims(self, field):
+        d = (ctypes.c_int * 3)()
+        self._chk(self.lib.saras_field_dims(self.h, field, d))
+        return tuple(d)
+
+    def get(self, field):
+        a = np.empty(self.dims(field), dtype=np.float64)
+        self._chk(self.lib.saras_download(self.h, field, _dp(a)))
+        return a
+
+    def set(self, field, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        if a.shape != self.dims(field):
+            raise ValueError("shape %s != %s" % (a.shape, self.dims(field)))
+        self._chk(self.lib.saras_upload(self.h, field, _dp(a)))
+
+    def synchronize(self):
+        self._chk(self.lib.saras_synchronize(self.h))
+
+    def launch_count(self):
+        return self.lib.saras_launch_count(self.h)
+
+    # -- boundary and field operators
+    def apply_bc(self, field):
+        self._chk(self.lib.saras_apply_bc(self.h, field))
+
+    def sync_field(self, field):
+        self._chk(self.lib.saras_sync_field(self.h, field))
+
+    def vfield_compute_diff(self):
+        self._chk(self.lib.saras_vfield_compute_diff(self.h))
+
+    def vfield_compute_nlin(self):
+        self._chk(self.lib.saras_vfield_compute_nlin(self.h))
+
+    def sfield_gradient(self, field):
+        self._chk(self.lib.saras_sfield_gradient(self.h, field))
+
+    def vfield_divergence(self):
+        self._chk(self.lib.saras_vfield_divergence(self.h))
+
+    def tfield_compute_diff(self):
+        self._chk(self.lib.saras_tfield_compute_diff(self.h))
+
+    def tfield_compute_nlin(self):
+        self._chk(self.lib.saras_tfield_compute_nlin(self.h))
+
+    def axpby(self, dst, a, src, b):
+        self._chk(self.lib.saras_axpby(self.h, dst, a, src, b))
+
+    # -- solves
+    def cn_solve(self, comp):
+        it, err = ctypes.c_int(), ctypes.c_double()
+        s = self.lib.saras_cn_solve(self.h, comp, ctypes.byref(it), ctypes.byref(err))
+        if s not in (0, _abi.NOT_CONVERGED):
+            self._chk(s)
+        return s, it.value, err.value
+
+    def mg_solve(self):
+        cyc, res = ctypes.c_int(), ctypes.c_double()
+        self._chk(self.lib.saras_mg_solve(self.h, ctypes.byref(cyc), ctypes.byref(res)))
+        return cyc.value, res.value
+
+    def mg_set_mode(self, mode, target=1e-8, max_cycles=200):
+        self._chk(self.lib.saras_mg_set_mode(self.h, mode, target, max_cycles))
+
+    def time_advance(self):
+        st = saras_step_stats()
+        s = self.lib.saras_time_advance(self.h, ctypes.byref(st))
+        if s not in (0, _abi.NOT_CONVERGED):
+            self._chk(s)
+        return s, st
+
+    def diagnostics(self):
+        e, d, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        s = self.lib.saras_diagnostics(self.h, ctypes.byref(e), ctypes.byref(d), ctypes.byref(n))
+        if s not in (0, _abi.DIVERGENCE_LIMIT):
+            self._chk(s)
+        return s, e.value, d.value, n.value
+
+    # -- multigrid test hooks
+    def _kat(self, fn):
+        e = ctypes.c_double()
+        self._chk(fn(self.h, ctypes.byref(e)))
+        return e.value
+
+    def mg_test_prolong(self):
+        return self._kat(self.lib.saras_mg_test_prolong)
+
+    def mg_test_transfer(self):
+        return self._kat(self.lib.saras_mg_test_transfer)
+
+    def mg_test_periodic(self):
+        return self._kat(self.lib.saras_mg_test_periodic)
+
+    def hydro_test_periodic(self):
+        return self._kat(self.lib.saras_hydro_test_periodic)
+
+    def level_dims(self, level):
+        d = (ctypes.c_int * 3)()
+        self._chk(self.lib.saras_mg_level_dims(self.h, level, d))
+        return tuple(d)
+
+    def get_level(self, level, which):
+        a = np.empty(self.level_dims(level))
+        self._chk(self.lib.saras_mg_get_level(self.h, level, which, _dp(a)))
+        return a
+
+    def set_level(self, level, which, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        self._chk(self.lib.saras_mg_set_level(self.h, level, which, _dp(a)))
+
+    def mg_smooth(self, level, count):
+        self._chk(self.lib.saras_mg_smooth(self.h, level, count))
+
+    def mg_restrict(self, level):
+        self._chk(self.lib.saras_mg_restrict(self.h, level))
+
+    def mg_prolong_add(self, level):
+        self._chk(self.lib.saras_mg_prolong_add(self.h, level))
+
+    def mg_compute_error(self, norm):
+        e = ctypes.c_double()
+        self._chk(self.lib.saras_mg_compute_error(self.h, norm, ctypes.byref(e)))
+        return e.value
+
+    # -- learned warm start
+    def unet_collect(self):
+        self._chk(self.lib.saras_unet_collect(self.h))
+
+    def unet_train(self, iters, lr):
+        loss = ctypes.c_double()
+        self._chk(self.lib.saras_unet_train(self.h, iters, lr, ctypes.byref(loss)))
+        return loss.value
+
+    def unet_infer(self):
+        self._chk(self.lib.saras_unet_infer(self.h, FIELD_PP))
+
+    def set_guess_mode(self, mode):
+        self._chk(self.lib.saras_set_guess_mode(self.h, mode))
+
+    # -- measurement
+    def profile_enable(self, kernel_id, enable=True):
+        self._chk(self.lib.saras_profile_enable(self.h, kernel_id, 1 if enable else 0))
+
+    def profile_read(self, kernel_id):
+        n, ms, b = ctypes.c_longlong(), ctypes.c_double(), ctypes.c_double()
+        self._chk(self.lib.saras_profile_read(self.h, kernel_id, ctypes.byref(n), ctypes.byref(ms), ctypes.byref(b)))
+        return n.value, ms.value, b.value
+
+    @staticmethod
+    def profile_names():
+        lib = _abi.load()
+        return [lib.saras_profile_name(i).decode() for i in range(lib.saras_profile_count())]
+
+
+# ---------------------------------------------------------------- initial conditions
+def grid_coords(params):
+    """Vertex ("staggered") and cell ("collocated") coordinates including the
+    pads, grid.cc:370-403: xStaggr(i) = L*i*dXi, xColloc(i) = L*(xi(i)+xi(i+1))/2."""
+    out = []
+    for ind, L in ((params.xInd, params.Lx), (params.yInd, params.Ly), (params.zInd, params.Lz)):
+        n = 2 ** ind
+        d = 1.0 / n
+        xi = np.arange(-1, n + 2, dtype=np.float64) * d
+        xs = L * xi
+        xc = L * (xi[:-1] + xi[1:]) / 2.0
+        out.append((xs, xc))
+    return out
+
+
+def taylor_green_velocity(params):
+    """taylorGreen::initializeField (lib/initial/taylorGreen.cc:54-100) over the padded arrays."""
+    (xs, xc), (ys, yc), (zs, zc) = grid_coords(params)
+    tp = 2.0 * math.pi
+    Vx = (np.sin(tp * xc / params.Lx)[:, None, None] * np.cos(tp * ys / params.Ly)[None, :, None] *
+          np.cos(tp * zs / params.Lz)[None, None, :])
+    Vy = (-np.cos(tp * xs / params.Lx)[:, None, None] * np.sin(tp * yc / params.Ly)[None, :, None] *
+          np.cos(tp * zs / params.Lz)[None, None, :])
+    return Vx, Vy
+
+
+def taylor_green_pressure(params):
+    """p = (cos 2x + cos 2y)(cos 2z + 2)/16 on the vertex grid (x scaled by 2 pi / L)."""
+    (xs, _), (ys, _), (zs, _) = grid_coords(params)
+    tp = 2.0 * math.pi
+    return ((np.cos(2 * tp * xs / params.Lx)[:, None, None] + np.cos(2 * tp * ys / params.Ly)[None, :, None]) *
+            (np.cos(2 * tp * zs / params.Lz)[None, None, :] + 2.0) / 16.0)
+
+
+def splitmix64(x):
+    x = (x + 0x9E3779B97F4A7C15) & 0xFFFFFFFFFFFFFFFF
+    z = x
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & 0xFFFFFFFFFFFFFFFF
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & 0xFFFFFFFFFFFFFFFF
+    return z ^ (z >> 31)
+
+
+def rbc_temperature(params, seed=42, amplitude=1.0e-3):
+    """Linear conduction profile T = 1 - z/Lz plus a counter-based uniform
+    perturbation in [-amplitude, amplitude] (SplitMix64 of seed ^ global index)."""
+    (xs, _), (ys, _), (zs, _) = grid_coords(params)
+    nx, ny, nz = len(xs), len(ys), len(zs)
+    idx = np.arange(nx * ny * nz, dtype=np.uint64).reshape(nx, ny, nz)
+    with np.errstate(over="ignore"):
+        x = (idx ^ np.uint64(seed)) + np.uint64(0x9E3779B97F4A7C15)
+        z = x
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    u = (z >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+    T = (1.0 - zs / params.Lz)[None, None, :] + amplitude * (2.0 * u - 1.0)
+    return np.ascontiguousarray(np.broadcast_to(T, (nx, ny, nz)))
+
+
+class hydro_d3:
+    """hydro_d3 (src/solvers/hydro/hydro_d3.cc:63-119): P = 1 (or a given
+    pressure), the initial condition of icType, then the velocity BCs."""
+
+    def __init__(self, params, pressure=None, velocity=None):
+        self.params = params
+        self.solver = Solver(params)
+        s = self.solver
+        P = np.ones(s.dims(FIELD_P)) if pressure is None else pressure
+        s.set(FIELD_P, P)
+        if velocity is not None:
+            for f, a in zip((FIELD_VX, FIELD_VY, FIELD_VZ), velocity):
+                if a is not None:
+                    s.set(f, a)
+        elif params.icType == 1:
+            Vx, Vy = taylor_green_velocity(params)
+            s.set(FIELD_VX, Vx)
+            s.set(FIELD_VY, Vy)
+        for f in (FIELD_VX, FIELD_VY, FIELD_VZ):
+            s.apply_bc(f)
+        self.time = 0.0
+        self.timeStepCount = 0
+
+    def timeAdvance(self):
+        st, stats = self.solver.time_advance()
+        if st != 0:
+            raise SarasError(st, "Jacobi iterations not converging")
+        return stats
+
+    def solvePDE(self, on_step=None):
+        """hydro_d3::solvePDE (hydro_d3.cc:122-251) without file output."""
+        dt = self.params.tStp
+        series = []
+        while True:
+            stats = self.timeAdvance()
+            self.timeStepCount += 1
+            self.time += dt
+            if self.timeStepCount % max(1, self.params.ioCnt) == 0:
+                s, e, d, n = self.solver.diagnostics()
+                series.append((self.time, e, d, n))
+                if s != 0:
+                    raise SarasError(s, "Maximum divergence exceeds limit")
+            if on_step:
+                on_step(self, stats)
+            if abs(self.params.tMax - self.time) < 0.5 * dt:
+                break
+        return series
+
+
+class scalar_d3(hydro_d3):
+    """scalar_d3 (src/solvers/scalar/scalar_d3.cc:62-107): P = 1, T = 0 (or a
+    given temperature), V = 0, then the velocity and temperature BCs."""
+
+    def __init__(self, params, temperature=None, pressure=None):
+        self.params = params
+        self.solver = Solver(params)
+        s = self.solver
+        s.set(FIELD_P, np.ones(s.dims(FIELD_P)) if pressure is None else pressure)
+        s.set(FIELD_T, np.zeros(s.dims(FIELD_T)) if temperature is None else temperature)
+        for f in (FIELD_VX, FIELD_VY, FIELD_VZ, FIELD_T):
+            s.apply_bc(f)
+        self.time = 0.0
+        self.timeStepCount = 0

@@ -1,0 +1,441 @@
+// capi.cu -- the extern "C" entry points of include/saras_gb300.h, the
+// parameters.yaml reader and the per-kernel CUDA-event profiler.
+
+#include <cmath>
+#include <cstring>
+#include <cctype>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <map>
+#include <algorithm>
+
+#include "context.cuh"
+
+namespace saras {
+
+static thread_local std::string g_err;
+void set_error(const std::string &msg) { g_err = msg; }
+
+// ------------------------------------------------------------------ profiler
+void prof_begin(Ctx &c, int k, int level) {
+    if (level != 0 || k < 0 || k >= PK_COUNT || !c.prof[k].enabled) return;
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, c.stream);
+    c.prof[k].ev.push_back(e);
+}
+
+static void prof_drain(Ctx &c, int k) {
+    ProfSlot &s = c.prof[k];
+    if (s.ev.size() < 2) return;
+    cudaEventSynchronize(s.ev.back());
+    size_t pairs = s.ev.size() / 2;
+    for (size_t q = 0; q < pairs; ++q) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, s.ev[2 * q], s.ev[2 * q + 1]);
+        s.ms += ms;
+        cudaEventDestroy(s.ev[2 * q]);
+        cudaEventDestroy(s.ev[2 * q + 1]);
+    }
+    s.ev.erase(s.ev.begin(), s.ev.begin() + 2 * pairs);
+}
+
+void prof_end(Ctx &c, int k, int level, double bytes) {
+    if (level != 0 || k < 0 || k >= PK_COUNT || !c.prof[k].enabled) return;
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, c.stream);
+    c.prof[k].ev.push_back(e);
+    c.prof[k].launches += 1;
+    c.prof[k].bytes += bytes;
+    if (c.prof[k].ev.size() >= 8192) prof_drain(c, k);
+}
+
+static const char *kProfNames[PK_COUNT] = {
+    "mg_smooth_fp64", "mg_smooth_fp32", "mg_residual_fp64", "mg_residual_fp32", "mg_restrict_fp64", "mg_restrict_fp32",
+    "mg_prolong_fp64", "mg_prolong_fp32", "refine_residual_fp64", "refine_update_fp64", "nse_rhs", "cn_jacobi",
+    "projection", "divergence", "conv3d_fwd_tcgen05", "conv3d_bwd_tcgen05"};
+
+// ------------------------------------------------------------------ yaml
+static std::string trim(const std::string &s) {
+    size_t a = s.find_first_not_of(" \t\r\n"), b = s.find_last_not_of(" \t\r\n");
+    return a == std::string::npos ? std::string() : s.substr(a, b - a + 1);
+}
+static std::string unquote(const std::string &s) {
+    std::string t = trim(s);
+    if (t.size() >= 2 && ((t.front() == '"' && t.back() == '"') || (t.front() == '\'' && t.back() == '\''))) return t.substr(1, t.size() - 2);
+    return t;
+}
+
+// Reads the flat two-level YAML of input/parameters.yaml: "Section": then
+// indented "Key": value pairs, '#' comments and one folded block scalar.
+static bool read_yaml(const char *path, std::map<std::string, std::string> &kv, std::string &err) {
+    std::ifstream in(path);
+    if (!in) { err = std::string("cannot open ") + path; return false; }
+    std::string line, section;
+    int blockIndent = -1;
+    std::string blockKey;
+    while (std::getline(in, line)) {
+        std::string raw = line;
+        size_t hash = std::string::npos;
+        bool inq = false;
+        for (size_t q = 0; q < raw.size(); ++q) {
+            if (raw[q] == '"') inq = !inq;
+            if (raw[q] == '#' && !inq) { hash = q; break; }
+        }
+        if (hash != std::string::npos) raw = raw.substr(0, hash);
+        if (trim(raw).empty()) continue;
+        int indent = 0;
+        while (indent < (int)raw.size() && (raw[indent] == ' ' || raw[indent] == '\t')) ++indent;
+        if (blockIndent >= 0) {
+            if (indent > blockIndent) { kv[blockKey] += trim(raw) + "\n"; continue; }
+            blockIndent = -1;
+        }
+        std::string t = trim(raw);
+        size_t colon = std::string::npos;
+        inq = false;
+        for (size_t q = 0; q < t.size(); ++q) {
+            if (t[q] == '"') inq = !inq;
+            if (t[q] == ':' && !inq) { colon = q; break; }
+        }
+        if (colon == std::string::npos) { err = "malformed line: " + line; return false; }
+        std::string key = unquote(t.substr(0, colon));
+        std::string val = trim(t.substr(colon + 1));
+        if (indent == 0) { section = key; continue; }
+        std::string full = section + "/" + key;
+        if (val == ">" || val == "|") { blockIndent = indent; blockKey = full; kv[full] = ""; continue; }
+        kv[full] = unquote(val);
+    }
+    return true;
+}
+
+static bool to_int(const std::string &s, int &out) {
+    char *e = nullptr;
+    long v = std::strtol(s.c_str(), &e, 10);
+    if (e == s.c_str() || *e != '\0') return false;
+    out = (int)v;
+    return true;
+}
+static bool to_double(const std::string &s, double &out) {
+    char *e = nullptr;
+    double v = std::strtod(s.c_str(), &e);
+    if (e == s.c_str() || *e != '\0') return false;
+    out = v;
+    return true;
+}
+static bool to_bool(const std::string &s, int &out) {
+    std::string t = s;
+    std::transform(t.begin(), t.end(), t.begin(), ::tolower);
+    if (t == "true" || t == "yes" || t == "on" || t == "1") { out = 1; return true; }
+    if (t == "false" || t == "no" || t == "off" || t == "0") { out = 0; return true; }
+    return false;
+}
+
+}  // namespace saras
+
+using namespace saras;
+
+extern "C" {
+
+int saras_default_params(saras_params *p) {
+    if (!p) return SARAS_BAD_ARG;
+    std::memset(p, 0, sizeof(*p));
+    p->probType = 2; p->icType = 1; p->rbcType = 1; p->forceType = 0;
+    p->xPer = p->yPer = p->zPer = 1;
+    p->Re = 1000.0; p->Ra = 1.0e4; p->Pr = 0.71; p->Ro = 12.0; p->Ta = 0.0;
+    p->Lx = p->Ly = p->Lz = 1.0;
+    p->nonHgBC = 0; p->patchRadius = 0.25;
+    p->betaX = p->betaY = p->betaZ = 1.0;
+    p->xInd = p->yInd = p->zInd = 5;
+    p->nThreads = 1; p->npX = 1; p->npY = 1;
+    p->dScheme = 1; p->iScheme = 1;
+    p->cnTolerance = 1.0e-8;
+    p->courantNumber = 0.1; p->tStp = 1.0e-3; p->tMax = 0.1;
+    p->ioCnt = 1; p->solnFormat = 1; p->fwInt = 0.1; p->rsInt = 0.1; p->prInt = 0.1;
+    p->vcDepth = 3; p->vcCount = 200; p->mgTolerance = 1.0e-8;
+    p->gsSmooth = 0; p->preSmooth = 3; p->postSmooth = 3; p->resType = 1;
+    p->mgMode = SARAS_MG_REFERENCE; p->mgTarget = 1.0e-8; p->mgMaxCycles = 200; p->mixedCycles = 1;
+    p->guessMode = SARAS_GUESS_PREVIOUS; p->jacobiWeight = 1.0; p->seed = 42;
+    return SARAS_OK;
+}
+
+static int fail(char *err, int errlen, const std::string &msg, int code) {
+    if (err && errlen > 0) { std::strncpy(err, msg.c_str(), errlen - 1); err[errlen - 1] = 0; }
+    set_error(msg);
+    return code;
+}
+
+// parser::parseYAML (parser.cc:158-236) and parser::checkData (parser.cc:250-352).
+int saras_parse_yaml(const char *path, saras_params *p, char *err, int errlen) {
+    if (!path || !p) return fail(err, errlen, "null argument", SARAS_BAD_ARG);
+    saras_default_params(p);
+    std::map<std::string, std::string> kv;
+    std::string e;
+    if (!read_yaml(path, kv, e)) return fail(err, errlen, e, SARAS_BAD_CONFIG);
+    struct IK { const char *k; int *v; };
+    struct DK { const char *k; double *v; };
+    struct BK { const char *k; int *v; };
+    IK ints[] = {{"Program/Problem Type", &p->probType}, {"Program/Initial Condition", &p->icType}, {"Program/RBC Type", &p->rbcType},
+                 {"Program/Force", &p->forceType}, {"Mesh/X Index", &p->xInd}, {"Mesh/Y Index", &p->yInd}, {"Mesh/Z Index", &p->zInd},
+                 {"Parallel/Number of OMP threads", &p->nThreads}, {"Parallel/X Number of Procs", &p->npX},
+                 {"Parallel/Y Number of Procs", &p->npY}, {"Solver/Differentiation Scheme", &p->dScheme},
+                 {"Solver/Integration Scheme", &p->iScheme}, {"Solver/I/O Count", &p->ioCnt}, {"Solver/Solution Format", &p->solnFormat},
+                 {"Multigrid/V-Cycle Depth", &p->vcDepth}, {"Multigrid/V-Cycle Count", &p->vcCount},
+                 {"Multigrid/Smoothing Method", &p->gsSmooth}, {"Multigrid/Pre-Smoothing Count", &p->preSmooth},
+                 {"Multigrid/Post-Smoothing Count", &p->postSmooth}, {"Multigrid/Residual Type", &p->resType},
+                 {"GB300/Multigrid Mode", &p->mgMode}, {"GB300/Max V-Cycles", &p->mgMaxCycles},
+                 {"GB300/Mixed Inner Cycles", &p->mixedCycles}, {"GB300/Guess Mode", &p->guessMode}, {"GB300/Seed", &p->seed}};
+    DK dbls[] = {{"Program/Reynolds Number", &p->Re}, {"Program/Rossby Number", &p->Ro}, {"Program/Rayleigh Number", &p->Ra},
+                 {"Program/Prandtl Number", &p->Pr}, {"Program/Taylor Number", &p->Ta}, {"Program/X Length", &p->Lx},
+                 {"Program/Y Length", &p->Ly}, {"Program/Z Length", &p->Lz}, {"Program/Plate Radius", &p->patchRadius},
+                 {"Mesh/X Beta", &p->betaX}, {"Mesh/Y Beta", &p->betaY}, {"Mesh/Z Beta", &p->betaZ},
+                 {"Solver/Solve Tolerance", &p->cnTolerance}, {"Solver/Courant Number", &p->courantNumber},
+                 {"Solver/Time-Step", &p->tStp}, {"Solver/Final Time", &p->tMax}, {"Solver/Solution Write Interval", &p->fwInt},
+                 {"Solver/Restart Write Interval", &p->rsInt}, {"Solver/Probe Time Interval", &p->prInt},
+                 {"Multigrid/Solve Tolerance", &p->mgTolerance}, {"GB300/Residual Target", &p->mgTarget},
+                 {"GB300/Jacobi Weight", &p->jacobiWeight}};
+    BK bools[] = {{"Program/Heating Plate", &p->nonHgBC}, {"Solver/Restart Run", &p->restartFlag},
+                  {"Solver/Use CFL Condition", &p->useCFL}, {"Solver/Record Probes", &p->readProbes},
+                  {"Multigrid/Print Residual", &p->printResidual}, {"GB300/Test Poisson", &p->testPoisson}};
+    const char *required[] = {"Program/Problem Type", "Program/Domain Type", "Mesh/Mesh Type", "Mesh/X Index", "Mesh/Y Index",
+                              "Mesh/Z Index", "Solver/Time-Step", "Solver/Final Time", "Multigrid/V-Cycle Depth"};
+    for (const char *r : required)
+        if (!kv.count(r)) return fail(err, errlen, std::string("missing key ") + r, SARAS_BAD_CONFIG);
+    for (auto &x : ints) if (kv.count(x.k) && !to_int(kv[x.k], *x.v)) return fail(err, errlen, std::string("bad integer for ") + x.k, SARAS_BAD_CONFIG);
+    for (auto &x : dbls) if (kv.count(x.k) && !to_double(kv[x.k], *x.v)) return fail(err, errlen, std::string("bad number for ") + x.k, SARAS_BAD_CONFIG);
+    for (auto &x : bools) if (kv.count(x.k) && !to_bool(kv[x.k], *x.v)) return fail(err, errlen, std::string("bad boolean for ") + x.k, SARAS_BAD_CONFIG);
+    std::string domain = kv["Program/Domain Type"], mesh = kv["Mesh/Mesh Type"];
+    // parser::checkData (parser.cc:250-352)
+    if (p->yInd == 0) return fail(err, errlen, "Y Index parameter of YAML file is 0 for 3D simulation", SARAS_BAD_CONFIG);
+    if (p->npX < 1) p->npX = 1;
+    if (p->npY < 1) p->npY = 1;
+    if (domain.size() != 3) return fail(err, errlen, "Domain type string is not correct", SARAS_BAD_CONFIG);
+    if (mesh.size() != 3) return fail(err, errlen, "Mesh type string is not correct", SARAS_BAD_CONFIG);
+    if (p->tStp > p->tMax) return fail(err, errlen, "Time step is larger than the maximum duration assigned for simulation", SARAS_BAD_CONFIG);
+    if (p->resType > 2) return fail(err, errlen, "The specified value for printing error at end of V-Cycles is not defined", SARAS_BAD_CONFIG);
+    // parser::setPeriodicity / setGrids (parser.cc:366-414)
+    p->xPer = domain[0] != 'N'; p->yPer = domain[1] != 'N'; p->zPer = domain[2] != 'N';
+    auto g = [](char ch) { return ch == 'S' ? 1 : ch == 'D' ? 2 : 0; };
+    p->xGrid = g(mesh[0]); p->yGrid = g(mesh[1]); p->zGrid = g(mesh[2]);
+    // One GPU runs the whole domain (np = 1 semantics); the decomposition check
+    // uses the full grid.
+    int coarsest = (int)std::pow(2, p->vcDepth + 1);
+    if ((int)std::pow(2, p->xInd) < coarsest || (int)std::pow(2, p->yInd) < coarsest || (int)std::pow(2, p->zInd) < coarsest)
+        return fail(err, errlen, "The grid size is too coarse to reach the V-Cycle depth specified", SARAS_BAD_CONFIG);
+    return SARAS_OK;
+}
+
+static int validate(const saras_params *p, std::string &why) {
+    if (p->xInd < 2 || p->yInd < 2 || p->zInd < 2 || p->xInd > 11 || p->yInd > 11 || p->zInd > 11) { why = "grid index out of range (2..11)"; return SARAS_BAD_CONFIG; }
+    if (p->vcDepth < 1) { why = "V-Cycle Depth must be >= 1"; return SARAS_BAD_CONFIG; }
+    int coarsest = (int)std::pow(2, p->vcDepth + 1);
+    if ((1 << p->xInd) < coarsest || (1 << p->yInd) < coarsest || (1 << p->zInd) < coarsest) { why = "grid too coarse for the V-Cycle depth"; return SARAS_BAD_CONFIG; }
+    if (p->xGrid || p->yGrid || p->zGrid) { why = "only uniform meshes (Mesh Type UUU) are supported"; return SARAS_BAD_CONFIG; }
+    if (p->dScheme != 1) { why = "Undefined finite differencing scheme"; return SARAS_BAD_CONFIG; }
+    if (p->gsSmooth != 0) { why = "Gauss-Seidel smoothing on fine levels is not available on the GPU; use Smoothing Method 0"; return SARAS_BAD_CONFIG; }
+    if (p->nonHgBC) { why = "heating-plate boundary condition is not supported"; return SARAS_BAD_CONFIG; }
+    if (p->probType >= 5 && (p->rbcType < 1 || p->rbcType > 4)) { why = "undefined RBC Type"; return SARAS_BAD_CONFIG; }
+    if (p->tStp <= 0 || p->Re <= 0 || p->Lx <= 0 || p->Ly <= 0 || p->Lz <= 0) { why = "non-positive time step, Re or length"; return SARAS_BAD_CONFIG; }
+    if (p->mgMode < 0 || p->mgMode > 2) { why = "bad multigrid mode"; return SARAS_BAD_CONFIG; }
+    if (p->resType < 0 || p->resType > 2) { why = "bad residual type"; return SARAS_BAD_CONFIG; }
+    return SARAS_OK;
+}
+
+int saras_create(const saras_params *p, saras_ctx **out) {
+    if (!p || !out) return SARAS_BAD_ARG;
+    *out = nullptr;
+    std::string why;
+    int s = validate(p, why);
+    if (s) { set_error(why); return s; }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        set_error("no CUDA device is visible; the GB300 solver has no CPU fallback");
+        return SARAS_NO_DEVICE;
+    }
+    saras_ctx *h = new saras_ctx();
+    Ctx &c = h->c;
+    c.p = *p;
+    cudaGetDevice(&c.dev);
+    if (cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess) {
+        set_error("cudaStreamCreate failed");
+        delete h;
+        return SARAS_CUDA_ERROR;
+    }
+    c.guessMode = p->guessMode;
+    s = fields_setup(c);
+    if (!s) s = mg_setup(c);
+    if (!s) {
+        if (cudaStreamSynchronize(c.stream) != cudaSuccess) { set_error("setup failed"); s = SARAS_CUDA_ERROR; }
+    }
+    if (s) {
+        if (c.err.empty()) c.err = g_err;
+        set_error(c.err);
+        saras_destroy(h);
+        return s;
+    }
+    *out = h;
+    return SARAS_OK;
+}
+
+int saras_destroy(saras_ctx *h) {
+    if (!h) return SARAS_OK;
+    Ctx &c = h->c;
+    if (c.stream) cudaStreamSynchronize(c.stream);
+    unet_free(c);
+    mg_free(c);
+    for (int f = 0; f < SARAS_NUM_FIELDS; ++f) cudaFree(c.f[f]);
+    for (int q = 0; q < 4; ++q) cudaFree(c.scratch[q]);
+    cudaFree(c.red); cudaFree(c.dscal); cudaFree(c.dflag);
+    if (c.hscal) cudaFreeHost(c.hscal);
+    for (int q = 0; q < 2; ++q) cudaFree(c.pHist[q]);
+    for (int k = 0; k < PK_COUNT; ++k) for (cudaEvent_t e : c.prof[k].ev) cudaEventDestroy(e);
+    if (c.stream) cudaStreamDestroy(c.stream);
+    delete h;
+    return SARAS_OK;
+}
+
+const char *saras_last_error(const saras_ctx *h) {
+    if (h && !h->c.err.empty()) return h->c.err.c_str();
+    return g_err.c_str();
+}
+
+static long field_count(const Ctx &c, int f) {
+    const FieldInfo &i = c.info[f];
+    return (long)(i.n[0] + 2) * (i.n[1] + 2) * (i.n[2] + 2);
+}
+
+int saras_field_dims(const saras_ctx *h, int field, int dims[3]) {
+    if (!h || !dims || field < 0 || field >= SARAS_NUM_FIELDS) return SARAS_BAD_ARG;
+    for (int d = 0; d < 3; ++d) dims[d] = h->c.info[field].n[d] + 2;
+    return SARAS_OK;
+}
+
+int saras_upload(saras_ctx *h, int field, const double *host) {
+    if (!h || !host || field < 0 || field >= SARAS_NUM_FIELDS) return SARAS_BAD_ARG;
+    Ctx &c = h->c;
+    SARAS_CUDA_TRY(cudaMemcpyAsync(c.f[field], host, sizeof(double) * field_count(c, field), cudaMemcpyHostToDevice, c.stream));
+    SARAS_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return SARAS_OK;
+}
+
+int saras_download(saras_ctx *h, int field, double *host) {
+    if (!h || !host || field < 0 || field >= SARAS_NUM_FIELDS) return SARAS_BAD_ARG;
+    Ctx &c = h->c;
+    SARAS_CUDA_TRY(cudaMemcpyAsync(host, c.f[field], sizeof(double) * field_count(c, field), cudaMemcpyDeviceToHost, c.stream));
+    SARAS_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return SARAS_OK;
+}
+
+int saras_synchronize(saras_ctx *h) {
+    if (!h) return SARAS_BAD_ARG;
+    SARAS_CUDA_TRY(cudaStreamSynchronize(h->c.stream));
+    return SARAS_OK;
+}
+
+long long saras_launch_count(const saras_ctx *h) { return h ? h->c.launches : 0; }
+
+#define CTX_OR_FAIL(h) do { if (!h) return SARAS_BAD_ARG; } while (0)
+
+int saras_apply_bc(saras_ctx *h, int field) { CTX_OR_FAIL(h); return apply_bc(h->c, field); }
+int saras_sync_field(saras_ctx *h, int field) { CTX_OR_FAIL(h); return sync_field(h->c, field); }
+int saras_vfield_compute_diff(saras_ctx *h) { CTX_OR_FAIL(h); return vfield_compute_diff(h->c); }
+int saras_vfield_compute_nlin(saras_ctx *h) { CTX_OR_FAIL(h); return vfield_compute_nlin(h->c); }
+int saras_sfield_gradient(saras_ctx *h, int sf) { CTX_OR_FAIL(h); return sfield_gradient(h->c, sf); }
+int saras_vfield_divergence(saras_ctx *h) { CTX_OR_FAIL(h); return vfield_divergence(h->c, nullptr, false); }
+int saras_tfield_compute_diff(saras_ctx *h) { CTX_OR_FAIL(h); return tfield_compute_diff(h->c); }
+int saras_tfield_compute_nlin(saras_ctx *h) { CTX_OR_FAIL(h); return tfield_compute_nlin(h->c); }
+int saras_axpby(saras_ctx *h, int dst, double a, int src, double b) { CTX_OR_FAIL(h); return axpby(h->c, dst, a, src, b); }
+
+int saras_cn_solve(saras_ctx *h, int component, int *iters, double *max_error) {
+    CTX_OR_FAIL(h);
+    return cn_solve(h->c, component, iters, max_error);
+}
+
+int saras_mg_solve(saras_ctx *h, int *vcycles, double *residual) {
+    CTX_OR_FAIL(h);
+    return mg_solve(h->c, vcycles, residual, nullptr);
+}
+
+int saras_mg_set_mode(saras_ctx *h, int mode, double target, int max_cycles) {
+    CTX_OR_FAIL(h);
+    if (mode < 0 || mode > 2 || !(target > 0) || max_cycles < 1) return SARAS_BAD_ARG;
+    h->c.mgMode = mode; h->c.mgTarget = target; h->c.mgMaxCycles = max_cycles;
+    h->c.p.mgMode = mode; h->c.p.mgTarget = target; h->c.p.mgMaxCycles = max_cycles;
+    return SARAS_OK;
+}
+
+int saras_time_advance(saras_ctx *h, saras_step_stats *stats) {
+    CTX_OR_FAIL(h);
+    return time_advance(h->c, stats);
+}
+
+int saras_diagnostics(saras_ctx *h, double *energy, double *max_div, double *nusselt) {
+    CTX_OR_FAIL(h);
+    return diagnostics(h->c, energy, max_div, nusselt);
+}
+
+int saras_mg_test_prolong(saras_ctx *h, double *err) { CTX_OR_FAIL(h); if (!err) return SARAS_BAD_ARG; return mg_test_prolong(h->c, err); }
+int saras_mg_test_transfer(saras_ctx *h, double *err) { CTX_OR_FAIL(h); if (!err) return SARAS_BAD_ARG; return mg_test_transfer(h->c, err); }
+int saras_mg_test_periodic(saras_ctx *h, double *err) { CTX_OR_FAIL(h); if (!err) return SARAS_BAD_ARG; return mg_test_periodic(h->c, err); }
+int saras_hydro_test_periodic(saras_ctx *h, double *err) { CTX_OR_FAIL(h); if (!err) return SARAS_BAD_ARG; return hydro_test_periodic(h->c, err); }
+
+int saras_mg_level_dims(const saras_ctx *h, int level, int dims[3]) {
+    if (!h || !dims || level < 0 || level > h->c.depth) return SARAS_BAD_ARG;
+    for (int d = 0; d < 3; ++d) dims[d] = h->c.lv[level].n[d] + 3;
+    return SARAS_OK;
+}
+int saras_mg_set_level(saras_ctx *h, int level, int which, const double *host) { CTX_OR_FAIL(h); if (!host) return SARAS_BAD_ARG; return mg_set_level(h->c, level, which, host); }
+int saras_mg_get_level(saras_ctx *h, int level, int which, double *host) { CTX_OR_FAIL(h); if (!host) return SARAS_BAD_ARG; return mg_get_level(h->c, level, which, host); }
+int saras_mg_smooth(saras_ctx *h, int level, int count) { CTX_OR_FAIL(h); return mg_smooth_level(h->c, level, count); }
+int saras_mg_restrict(saras_ctx *h, int level) { CTX_OR_FAIL(h); return mg_restrict_level(h->c, level); }
+int saras_mg_prolong_add(saras_ctx *h, int level) { CTX_OR_FAIL(h); return mg_prolong_level(h->c, level); }
+int saras_mg_compute_error(saras_ctx *h, int norm, double *err) {
+    CTX_OR_FAIL(h);
+    if (!err || norm < 1 || norm > 2) return SARAS_BAD_ARG;
+    return mg_compute_error(h->c, norm, err);
+}
+
+int saras_unet_collect(saras_ctx *h) { CTX_OR_FAIL(h); return unet_collect(h->c); }
+int saras_unet_train(saras_ctx *h, int iters, double lr, double *loss) { CTX_OR_FAIL(h); return unet_train(h->c, iters, lr, loss); }
+int saras_unet_infer(saras_ctx *h, int field_out) {
+    CTX_OR_FAIL(h);
+    if (field_out != SARAS_FIELD_PP) return SARAS_BAD_ARG;
+    return unet_infer(h->c, h->c.f[SARAS_FIELD_PP]);
+}
+int saras_set_guess_mode(saras_ctx *h, int mode) {
+    CTX_OR_FAIL(h);
+    if (mode != SARAS_GUESS_PREVIOUS && mode != SARAS_GUESS_LEARNED) return SARAS_BAD_ARG;
+    h->c.guessMode = mode;
+    return SARAS_OK;
+}
+
+int saras_profile_enable(saras_ctx *h, int kernel_id, int enable) {
+    if (!h || kernel_id < 0 || kernel_id >= PK_COUNT) return SARAS_BAD_ARG;
+    ProfSlot &s = h->c.prof[kernel_id];
+    prof_drain(h->c, kernel_id);
+    if (enable) { s.launches = 0; s.bytes = 0; s.ms = 0; }
+    s.enabled = enable != 0;
+    return SARAS_OK;
+}
+
+int saras_profile_read(saras_ctx *h, int kernel_id, long long *launches, double *total_ms, double *bytes) {
+    if (!h || kernel_id < 0 || kernel_id >= PK_COUNT) return SARAS_BAD_ARG;
+    SARAS_CUDA_TRY(cudaStreamSynchronize(h->c.stream));
+    prof_drain(h->c, kernel_id);
+    const ProfSlot &s = h->c.prof[kernel_id];
+    if (launches) *launches = s.launches;
+    if (total_ms) *total_ms = s.ms;
+    if (bytes) *bytes = s.bytes;
+    return SARAS_OK;
+}
+
+const char *saras_profile_name(int kernel_id) {
+    if (kernel_id < 0 || kernel_id >= PK_COUNT) return "";
+    return kProfNames[kernel_id];
+}
+
+int saras_profile_count(void) { return PK_COUNT; }
+
+}  // extern "C"

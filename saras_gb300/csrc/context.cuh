@@ -1,0 +1,168 @@
+// context.cuh -- the solver context behind the C ABI.
+#pragma once
+
+#include "common.cuh"
+
+struct saras_ctx;
+
+namespace saras {
+
+// Kernels with CUDA-event timing (saras_profile_*).
+enum ProfKernel : int {
+    PK_MG_SMOOTH64 = 0,   // FP64 Jacobi sweep, level 0
+    PK_MG_SMOOTH32,       // FP32 Jacobi sweep, level 0 (mixed mode)
+    PK_MG_RESID64,        // FP64 residual (+restriction input), level 0
+    PK_MG_RESID32,
+    PK_MG_RESTRICT64,
+    PK_MG_RESTRICT32,
+    PK_MG_PROLONG64,
+    PK_MG_PROLONG32,
+    PK_REFINE_RESID,      // FP64 fine residual + FP32 demotion (mixed)
+    PK_REFINE_UPDATE,     // FP64 correction accumulation (mixed)
+    PK_RHS,               // fused NSE right-hand side
+    PK_CN,                // fused CN Jacobi sweep + BC + residual
+    PK_PROJECT,
+    PK_DIVERGENCE,
+    PK_CONV_FWD,          // U-Net implicit-GEMM convolution (tcgen05)
+    PK_CONV_BWD,
+    PK_COUNT
+};
+
+struct ProfSlot {
+    bool enabled = false;
+    std::vector<cudaEvent_t> ev;   // start/stop pairs
+    long long launches = 0;
+    double bytes = 0.0;
+    double ms = 0.0;
+};
+
+// One multigrid level in both precisions.
+struct Level {
+    int n[3];                 // core index range 0..n (n = 2^(ind-l)), padded n+3
+    long count;               // padded point count
+    double *a = nullptr, *b = nullptr, *r = nullptr;   // FP64 pressure ping-pong + rhs
+    int cur = 0;              // 0: a holds pressureData, 1: b
+    float *a32 = nullptr, *b32 = nullptr, *r32 = nullptr;
+    int cur32 = 0;
+    double hx, hy, hz, hxhy, hyhz, hzhx, hxhyhz;
+    // uniform-grid stencil coefficients (exact products of the reference expressions)
+    double cx, cy, cz, c7, den;      // smoother: hyhz*xix2, hzhx*ety2, hxhy*ztz2, 2*hxhyhz, 4*(...)
+    double lx, ly, lz;               // residual: xix2/(hx*hx) folded as products with 1/(hx*hx)
+    double ihx2, ihy2, ihz2;         // 1/(hx*hx) (exact powers of two)
+    double *pa() const { return cur == 0 ? a : b; }
+    double *pb() const { return cur == 0 ? b : a; }
+    float *pa32() const { return cur32 == 0 ? a32 : b32; }
+    float *pb32() const { return cur32 == 0 ? b32 : a32; }
+};
+
+// Per-field metadata: core counts, staggering, bulk box, boundary programs.
+struct FieldInfo {
+    int n[3] = {0, 0, 0};
+    bool stag[3] = {false, false, false};
+    int blo[3], bhi[3];
+    BcProgram full;      // syncData + wall objects (imposeXBCs)
+    BcProgram sync;      // syncData alone
+};
+
+struct Ctx {
+    saras_params p;
+    int dev = 0;
+    cudaStream_t stream = nullptr;
+    bool scalar = false;
+    // grid (grid.cc:59-136, uniform)
+    int Ns[3], Nc[3];
+    double dXi[3], ih[3], ih2[3], L[3];
+    double m1[3], m2[3];           // xi_x (=1/L) and xix2 (=pow(1/L,2))
+    double inverseRe, nu, kappa, Fb, dt;
+    double hx2hy2, hy2hz2, hz2hx2, hx2hy2hz2;
+    int maxIterations;
+    double totalVol;
+    // fields
+    FieldInfo info[SARAS_NUM_FIELDS];
+    double *f[SARAS_NUM_FIELDS] = {nullptr};
+    double *scratch[4] = {nullptr, nullptr, nullptr, nullptr};   // ping-pong partners of Vx, Vy, Vz, T
+    // multigrid
+    std::vector<Level> lv;
+    int depth = 0;
+    int mgMode = SARAS_MG_REFERENCE;
+    double mgTarget = 1e-8;
+    int mgMaxCycles = 200;
+    int maxCount = 0;
+    double *wallX = nullptr, *wallY = nullptr, *wallZ = nullptr;   // Dirichlet check walls
+    double *coarseInv = nullptr;   // dense coarse-level inverse (target modes)
+    float *coarseInv32 = nullptr;
+    int coarseN = 0;
+    // reductions
+    double *red = nullptr;          // partial sums (device)
+    int redCap = 0;
+    double *dscal = nullptr;        // device scalars
+    double *hscal = nullptr;        // pinned host mirror
+    int *dflag = nullptr;
+    // stats
+    long long launches = 0;
+    long long coarseIters = 0;
+    saras_step_stats last{};
+    // learned warm start
+    int guessMode = SARAS_GUESS_PREVIOUS;
+    void *unet = nullptr;
+    double *pHist[2] = {nullptr, nullptr};   // P at the two previous steps
+    int histCount = 0;
+    // profiling
+    ProfSlot prof[PK_COUNT];
+    std::string err;
+};
+
+// ---- launch accounting and profiling (host side)
+void prof_begin(Ctx &c, int k, int level);
+void prof_end(Ctx &c, int k, int level, double bytes);
+inline void count_launch(Ctx &c, int n = 1) { c.launches += n; }
+
+// ---- field operations (fields.cu)
+int fields_setup(Ctx &c);
+int apply_bc(Ctx &c, int field);
+int sync_field(Ctx &c, int field);
+int vfield_compute_diff(Ctx &c);
+int vfield_compute_nlin(Ctx &c);
+int sfield_gradient(Ctx &c, int sf);
+int vfield_divergence(Ctx &c, double *dst, bool scale_dt);
+int tfield_compute_diff(Ctx &c);
+int tfield_compute_nlin(Ctx &c);
+int axpby(Ctx &c, int dst, double a, int src, double b);
+int compute_rhs(Ctx &c);
+int compute_trhs(Ctx &c);
+int cn_solve(Ctx &c, int comp, int *iters, double *maxerr);
+int project(Ctx &c, bool with_bc);
+int diagnostics(Ctx &c, double *energy, double *maxdiv, double *nusselt);
+int hydro_test_periodic(Ctx &c, double *err);
+int time_advance(Ctx &c, saras_step_stats *st);
+
+// ---- multigrid (multigrid.cu)
+int mg_setup(Ctx &c);
+void mg_free(Ctx &c);
+int mg_solve(Ctx &c, int *cycles, double *residual, saras_step_stats *st);
+int mg_smooth_level(Ctx &c, int level, int count);
+int mg_restrict_level(Ctx &c, int level);
+int mg_prolong_level(Ctx &c, int level);
+int mg_compute_error(Ctx &c, int norm, double *err);
+int mg_set_level(Ctx &c, int level, int which, const double *host);
+int mg_get_level(Ctx &c, int level, int which, double *host);
+int mg_test_prolong(Ctx &c, double *err);
+int mg_test_transfer(Ctx &c, double *err);
+int mg_test_periodic(Ctx &c, double *err);
+int mg_fine_residual(Ctx &c, const double *p, double *maxres, double *maxb);
+
+// ---- learned warm start (unet.cu)
+int unet_create(Ctx &c);
+void unet_free(Ctx &c);
+int unet_collect(Ctx &c);
+int unet_train(Ctx &c, int iters, double lr, double *loss);
+int unet_infer(Ctx &c, double *out);
+
+// ---- reductions (fields.cu)
+int reduce_sum_partials(Ctx &c, int nparts, double *host_out);
+
+}  // namespace saras
+
+struct saras_ctx {
+    saras::Ctx c;
+};

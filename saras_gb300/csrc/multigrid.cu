@@ -1,0 +1,1112 @@
+// multigrid.cu -- geometric multigrid for the pressure-correction Poisson
+// equation (lib/poisson/poisson.cc, poisson_d3.cc) on one GB300.
+//
+// Three modes share one set of templated level kernels:
+//   SARAS_MG_REFERENCE     FP64, the reference V-cycle loop bit for bit
+//                          (padded-array mean removal, |delta residual| stop,
+//                          coarsest Gauss-Seidel to mgTolerance / maxCount).
+//   SARAS_MG_PLAIN_TARGET  FP64 V-cycles on the compatible system until
+//                          max|b-Ap| <= target * max|b|.
+//   SARAS_MG_MIXED         FP32 V-cycles as the inner solver of an FP64
+//                          iterative-refinement loop to the same target.
+// The target modes make the singular Neumann/periodic system compatible by
+// subtracting the trapezoidal-weight mean of b (the left null vector of the
+// vertex-grid operator with mirror or periodic ghosts) and use a damped Jacobi
+// smoother; they exist for the throughput comparison and are not drop-ins.
+//
+// Ghost handling: the smoother and prolongation write every face-ghost image of
+// the points they produce (imposeBC, poisson_d3.cc:575-668, restricted to the
+// face ghosts a 7-point stencil reads); the restriction resolves the pads of
+// the residual array (updatePads, poisson_d3.cc:671-686) by index mapping.
+// Compiled with --fmad=false (see fields.cu).
+
+#include <cmath>
+#include <cstring>
+#include <algorithm>
+
+#include "context.cuh"
+
+namespace saras {
+
+__global__ void k_final_reduce(const double *part, int n, int op, double *out);
+
+// max |a| over a whole array into *out (non-negative, atomic).
+__global__ void k_maxabs(const double *a, long n, double *out) {
+    double m = 0;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) m = fmax(m, fabs(a[t]));
+    block_max_to(m, out);
+}
+
+struct MgBC {
+    int per[3];         // periodic axes
+    int E[3];           // core upper index (xEnd) at this level
+    int dirichlet;      // Dirichlet check (TEST_POISSON)
+    int zeroBC;         // homogeneous Dirichlet (levels > 0)
+    int tgtPads;        // residual pads: 0 = reference (z ghost 0, non-periodic 0), 1 = mirror/periodic
+};
+
+struct MgK {            // level stencil constants
+    double cx, cy, cz, c7, den;
+    double lx, ly, lz;
+    float fcx, fcy, fcz, fc7, fden, flx, fly, flz;
+};
+
+static MgK make_k(const Level &L) {
+    MgK k;
+    k.cx = L.cx; k.cy = L.cy; k.cz = L.cz; k.c7 = L.c7; k.den = L.den;
+    k.lx = L.lx; k.ly = L.ly; k.lz = L.lz;
+    k.fcx = (float)L.cx; k.fcy = (float)L.cy; k.fcz = (float)L.cz; k.fc7 = (float)L.c7; k.fden = (float)L.den;
+    k.flx = (float)L.lx; k.fly = (float)L.ly; k.flz = (float)L.lz;
+    return k;
+}
+
+template <typename T> struct KSel;
+template <> struct KSel<double> {
+    static __device__ __forceinline__ double cx(const MgK &k) { return k.cx; }
+    static __device__ __forceinline__ double cy(const MgK &k) { return k.cy; }
+    static __device__ __forceinline__ double cz(const MgK &k) { return k.cz; }
+    static __device__ __forceinline__ double c7(const MgK &k) { return k.c7; }
+    static __device__ __forceinline__ double den(const MgK &k) { return k.den; }
+    static __device__ __forceinline__ double lx(const MgK &k) { return k.lx; }
+    static __device__ __forceinline__ double ly(const MgK &k) { return k.ly; }
+    static __device__ __forceinline__ double lz(const MgK &k) { return k.lz; }
+};
+template <> struct KSel<float> {
+    static __device__ __forceinline__ float cx(const MgK &k) { return k.fcx; }
+    static __device__ __forceinline__ float cy(const MgK &k) { return k.fcy; }
+    static __device__ __forceinline__ float cz(const MgK &k) { return k.fcz; }
+    static __device__ __forceinline__ float c7(const MgK &k) { return k.fc7; }
+    static __device__ __forceinline__ float den(const MgK &k) { return k.fden; }
+    static __device__ __forceinline__ float lx(const MgK &k) { return k.flx; }
+    static __device__ __forceinline__ float ly(const MgK &k) { return k.fly; }
+    static __device__ __forceinline__ float lz(const MgK &k) { return k.flz; }
+};
+
+// Smoother update, the expression of poisson_d3.cc:156-163 on a uniform grid
+// (the xixx, etyy, ztzz terms are exactly zero and omitted).
+template <typename T>
+__device__ __forceinline__ T mg_update(T E, T W, T N, T S, T U, T D, T r, const MgK &k) {
+    using K = KSel<T>;
+    return ((K::cx(k) * (E + W)) * (T)2.0 + (K::cy(k) * (N + S)) * (T)2.0 + (K::cz(k) * (U + D)) * (T)2.0 - K::c7(k) * r) / K::den(k);
+}
+// Laplacian, the expression of poisson_d3.cc:99-105 (uniform grid).
+template <typename T>
+__device__ __forceinline__ T mg_lap(T E, T W, T N, T S, T U, T D, T C, const MgK &k) {
+    using K = KSel<T>;
+    return K::lx(k) * (E - (T)2.0 * C + W) + K::ly(k) * (N - (T)2.0 * C + S) + K::lz(k) * (U - (T)2.0 * C + D);
+}
+
+__device__ __forceinline__ bool core_pt(const int E[3], int &i, int &j, int &k) {
+    k = blockIdx.x * blockDim.x + threadIdx.x;
+    j = blockIdx.y * blockDim.y + threadIdx.y;
+    i = blockIdx.z * blockDim.z + threadIdx.z;
+    return i <= E[0] && j <= E[1] && k <= E[2];
+}
+
+// Write v at (i,j,k) and at every face-ghost position whose imposeBC image is
+// (i,j,k): periodic -1 <- E-1, E+1 <- 1; Neumann -1 <- 1, E+1 <- E-1;
+// homogeneous Dirichlet the negated mirror (TEST_POISSON, levels > 0).
+template <typename T>
+__device__ __forceinline__ void put_scatter(const View3<T> &P, int i, int j, int k, T v, const MgBC &bc) {
+    P(i, j, k) = v;
+    int q[3] = {i, j, k};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        int E = bc.E[d];
+        bool dirich = bc.dirichlet && !bc.per[d];
+        if (dirich && !bc.zeroBC) continue;   // fixed wall values are set once per solve
+        T s = (dirich && bc.zeroBC) ? (T)(-1.0) : (T)1.0;
+        int g[2] = {-2, -2};
+        if (bc.per[d]) { if (q[d] == E - 1) g[0] = -1; if (q[d] == 1) g[1] = E + 1; }
+        else { if (q[d] == 1) g[0] = -1; if (q[d] == E - 1) g[1] = E + 1; }
+        for (int t = 0; t < 2; ++t) {
+            if (g[t] == -2) continue;
+            int r[3] = {i, j, k};
+            r[d] = g[t];
+            P(r[0], r[1], r[2]) = s * v;
+        }
+    }
+}
+
+// One Jacobi sweep (poisson_d3.cc:153-168).  zero_guess: the incoming iterate
+// is identically 0 (pressureData = 0 before smoothing a coarse level,
+// poisson.cc:258).  omega = 1 reproduces the reference exactly.
+template <typename T, bool ZERO>
+__global__ void k_mg_sweep(View3<T> out, View3<const T> in, View3<const T> r, MgK kk, MgBC bc, T omega) {
+    int i, j, k;
+    if (!core_pt(bc.E, i, j, k)) return;
+    T v;
+    if (ZERO) {
+        v = mg_update<T>((T)0, (T)0, (T)0, (T)0, (T)0, (T)0, r(i, j, k), kk);
+        if (omega != (T)1.0) v = omega * v;
+    } else {
+        T C = in(i, j, k);
+        v = mg_update<T>(in(i + 1, j, k), in(i - 1, j, k), in(i, j + 1, k), in(i, j - 1, k), in(i, j, k + 1), in(i, j, k - 1),
+                         r(i, j, k), kk);
+        if (omega != (T)1.0) v = C + omega * (v - C);
+    }
+    put_scatter(out, i, j, k, v, bc);
+}
+
+// computeResidual (poisson_d3.cc:90-111): tmp(core) = r - Lap(p).
+template <typename T>
+__global__ void k_mg_residual(View3<T> tmp, View3<const T> p, View3<const T> r, MgK kk, MgBC bc) {
+    int i, j, k;
+    if (!core_pt(bc.E, i, j, k)) return;
+    T lap = mg_lap<T>(p(i + 1, j, k), p(i - 1, j, k), p(i, j + 1, k), p(i, j - 1, k), p(i, j, k + 1), p(i, j, k - 1), p(i, j, k), kk);
+    tmp(i, j, k) = r(i, j, k) - lap;
+}
+
+// Value of the residual array at a possibly-ghost index after updatePads
+// (reference pads: x/y periodic copies of whole planes, everything else 0;
+// the z ghosts stay 0 even for periodic z), or after a mirror/periodic fill
+// in the target modes.
+template <typename T>
+__device__ __forceinline__ T pad_val(const View3<const T> &t, int i, int j, int k, const MgBC &bc) {
+    int q[3] = {i, j, k};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        int E = bc.E[d];
+        if (q[d] >= 0 && q[d] <= E) continue;
+        if (bc.tgtPads) {
+            if (bc.per[d]) q[d] = q[d] < 0 ? E - 1 : 1;
+            else q[d] = q[d] < 0 ? 1 : E - 1;
+        } else {
+            if (d == 2 || !bc.per[d]) return (T)0;
+            q[d] = q[d] < 0 ? E - 1 : 1;
+        }
+    }
+    return t(q[0], q[1], q[2]);
+}
+
+// coarsen (poisson_d3.cc:250-298): 27-point full weighting in the reference's
+// summation order.  bcf describes the fine level, Ec the coarse core.
+template <typename T>
+__global__ void k_mg_restrict(View3<T> rc, View3<const T> t, MgBC bcf, MgBC bcc) {
+    int i, j, k;
+    if (!core_pt(bcc.E, i, j, k)) return;
+    int i2 = 2 * i, j2 = 2 * j, k2 = 2 * k;
+    bool interior = i2 > 0 && j2 > 0 && k2 > 0 && i2 < bcf.E[0] && j2 < bcf.E[1] && k2 < bcf.E[2];
+    auto T_ = [&](int a, int b, int c) -> T { return interior ? t(a, b, c) : pad_val(t, a, b, c, bcf); };
+    T facePoints = (T_(i2 + 1, j2, k2) + T_(i2 - 1, j2, k2) + T_(i2, j2 + 1, k2) + T_(i2, j2 - 1, k2) +
+                    T_(i2, j2, k2 + 1) + T_(i2, j2, k2 - 1)) * (T)0.0625;
+    T edgePoints = (T_(i2 + 1, j2 + 1, k2) + T_(i2 + 1, j2 - 1, k2) + T_(i2 - 1, j2 - 1, k2) + T_(i2 - 1, j2 + 1, k2) +
+                    T_(i2, j2 + 1, k2 + 1) + T_(i2, j2 - 1, k2 + 1) + T_(i2, j2 - 1, k2 - 1) + T_(i2, j2 + 1, k2 - 1) +
+                    T_(i2 + 1, j2, k2 + 1) + T_(i2 + 1, j2, k2 - 1) + T_(i2 - 1, j2, k2 - 1) + T_(i2 - 1, j2, k2 + 1)) * (T)0.03125;
+    T vertPoints = (T_(i2 + 1, j2 + 1, k2 + 1) + T_(i2 + 1, j2 + 1, k2 - 1) + T_(i2 + 1, j2 - 1, k2 + 1) +
+                    T_(i2 - 1, j2 + 1, k2 + 1) + T_(i2 + 1, j2 - 1, k2 - 1) + T_(i2 - 1, j2 + 1, k2 - 1) +
+                    T_(i2 - 1, j2 - 1, k2 + 1) + T_(i2 - 1, j2 - 1, k2 - 1)) * (T)0.015625;
+    rc(i, j, k) = facePoints + edgePoints + vertPoints + t(i2, j2, k2) * (T)0.125;
+}
+
+// prolong (poisson_d3.cc:301-388) followed by pressureData += smoothedPres
+// (poisson.cc:271); the saved data is the fine array itself, updated in place.
+template <typename T>
+__global__ void k_mg_prolong_add(View3<T> pf, View3<const T> pc, MgBC bc, int add) {
+    int i, j, k;
+    if (!core_pt(bc.E, i, j, k)) return;
+    int i2 = i / 2, j2 = j / 2, k2 = k / 2;
+    bool io = i & 1, jo = j & 1, ko = k & 1;
+    T v;
+    const View3<const T> &C = pc;
+    if (io) {
+        if (jo) {
+            if (ko) v = (C(i2, j2, k2) + C(i2 + 1, j2, k2) + C(i2, j2 + 1, k2) + C(i2, j2, k2 + 1) + C(i2 + 1, j2 + 1, k2) +
+                         C(i2 + 1, j2, k2 + 1) + C(i2, j2 + 1, k2 + 1) + C(i2 + 1, j2 + 1, k2 + 1)) * (T)0.125;
+            else v = (C(i2, j2, k2) + C(i2, j2 + 1, k2) + C(i2 + 1, j2, k2) + C(i2 + 1, j2 + 1, k2)) * (T)0.25;
+        } else {
+            if (ko) v = (C(i2, j2, k2) + C(i2, j2, k2 + 1) + C(i2 + 1, j2, k2) + C(i2 + 1, j2, k2 + 1)) * (T)0.25;
+            else v = (C(i2, j2, k2) + C(i2 + 1, j2, k2)) * (T)0.5;
+        }
+    } else {
+        if (jo) {
+            if (ko) v = (C(i2, j2, k2) + C(i2, j2, k2 + 1) + C(i2, j2 + 1, k2) + C(i2, j2 + 1, k2 + 1)) * (T)0.25;
+            else v = (C(i2, j2, k2) + C(i2, j2 + 1, k2)) * (T)0.5;
+        } else {
+            if (ko) v = (C(i2, j2, k2) + C(i2, j2, k2 + 1)) * (T)0.5;
+            else v = C(i2, j2, k2);
+        }
+    }
+    if (add) v = v + pf(i, j, k);
+    put_scatter(pf, i, j, k, v, bc);
+}
+
+// Coarsest level (poisson_d3.cc:190-247): lexicographic Gauss-Seidel, run as a
+// hyperplane wavefront (points with equal i+j+k are independent, and visiting
+// the planes in increasing order gives every point exactly the lexicographic
+// mix of updated and old neighbours).  Ghosts are refreshed before each sweep
+// (imposeBC) and read from the pre-sweep state, as in the reference.  The
+// iteration loop runs on the device; it stops below tol or after maxCount+1
+// sweeps.  tgtMode: subtract the trapezoidal mean of r first and stop on a
+// relative reduction instead.
+template <typename T>
+__device__ void smem_impose_bc(T *p, int X, int Y, int Z, const MgBC &bc, const T *wx, const T *wy, const T *wz) {
+    int sy = Z + 3, sx = (Y + 3) * (Z + 3);
+    auto at = [&](int i, int j, int k) -> T & { return p[(i + 1) * sx + (j + 1) * sy + (k + 1)]; };
+    int tid = threadIdx.x, nt = blockDim.x;
+    // updatePads: periodic x planes then y planes (full extents)
+    if (bc.per[0]) {
+        for (int t = tid; t < (Y + 3) * (Z + 3); t += nt) { int j = t / (Z + 3) - 1, k = t % (Z + 3) - 1; at(X + 1, j, k) = at(1, j, k); at(-1, j, k) = at(X - 1, j, k); }
+        __syncthreads();
+    }
+    if (bc.per[1]) {
+        for (int t = tid; t < (X + 3) * (Z + 3); t += nt) { int i = t / (Z + 3) - 1, k = t % (Z + 3) - 1; at(i, Y + 1, k) = at(i, 1, k); at(i, -1, k) = at(i, Y - 1, k); }
+        __syncthreads();
+    }
+    if (!bc.per[0]) {
+        for (int t = tid; t < (Y + 3) * (Z + 3); t += nt) {
+            int j = t / (Z + 3) - 1, k = t % (Z + 3) - 1;
+            if (bc.dirichlet) {
+                if (bc.zeroBC) { at(-1, j, k) = -at(1, j, k); at(X + 1, j, k) = -at(X - 1, j, k); }
+                else { T w = wx[(j + 1) * (Z + 3) + (k + 1)]; at(-1, j, k) = w; at(X + 1, j, k) = w; }
+            } else { at(-1, j, k) = at(1, j, k); at(X + 1, j, k) = at(X - 1, j, k); }
+        }
+        __syncthreads();
+    }
+    if (!bc.per[1]) {
+        for (int t = tid; t < (X + 3) * (Z + 3); t += nt) {
+            int i = t / (Z + 3) - 1, k = t % (Z + 3) - 1;
+            if (bc.dirichlet) {
+                if (bc.zeroBC) { at(i, -1, k) = -at(i, 1, k); at(i, Y + 1, k) = -at(i, Y - 1, k); }
+                else { T w = wy[(i + 1) * (Z + 3) + (k + 1)]; at(i, -1, k) = w; at(i, Y + 1, k) = w; }
+            } else { at(i, -1, k) = at(i, 1, k); at(i, Y + 1, k) = at(i, Y - 1, k); }
+        }
+        __syncthreads();
+    }
+    for (int t = tid; t < (X + 3) * (Y + 3); t += nt) {
+        int i = t / (Y + 3) - 1, j = t % (Y + 3) - 1;
+        if (bc.per[2]) { at(i, j, -1) = at(i, j, Z - 1); at(i, j, Z + 1) = at(i, j, 1); }
+        else if (bc.dirichlet) {
+            if (bc.zeroBC) { at(i, j, -1) = -at(i, j, 1); at(i, j, Z + 1) = -at(i, j, Z - 1); }
+            else { T w = wz[(i + 1) * (Y + 3) + (j + 1)]; at(i, j, -1) = w; at(i, j, Z + 1) = w; }
+        } else { at(i, j, -1) = at(i, j, 1); at(i, j, Z + 1) = at(i, j, Z - 1); }
+    }
+    __syncthreads();
+}
+
+template <typename T>
+__global__ void k_mg_coarse(View3<T> pg, View3<const T> rg, MgK kk, MgBC bc, T tol, int maxCount, int tgtMode,
+                            long long *iters) {
+    extern __shared__ unsigned char smraw[];
+    int X = bc.E[0], Y = bc.E[1], Z = bc.E[2];
+    int n = (X + 3) * (Y + 3) * (Z + 3);
+    T *p = reinterpret_cast<T *>(smraw);
+    T *r = p + n;
+    __shared__ T red[32];
+    __shared__ int stop;
+    int sy = Z + 3, sx = (Y + 3) * (Z + 3);
+    auto at = [&](T *a, int i, int j, int k) -> T & { return a[(i + 1) * sx + (j + 1) * sy + (k + 1)]; };
+    int tid = threadIdx.x, nt = blockDim.x;
+    for (int t = tid; t < n; t += nt) { p[t] = (T)0; r[t] = rg.p[t]; }   // pressureData(d) = 0 (poisson.cc:258)
+    __syncthreads();
+    T thresh = tol;
+    if (tgtMode) {
+        // trapezoidal-weight mean of r over the core (weights 1/2 on end planes)
+        T s = 0, w = 0;
+        for (int t = tid; t < (X + 1) * (Y + 1) * (Z + 1); t += nt) {
+            int k = t % (Z + 1), j = (t / (Z + 1)) % (Y + 1), i = t / ((Z + 1) * (Y + 1));
+            T wt = (T)((i == 0 || i == X) ? 0.5 : 1.0) * (T)((j == 0 || j == Y) ? 0.5 : 1.0) * (T)((k == 0 || k == Z) ? 0.5 : 1.0);
+            s += wt * at(r, i, j, k); w += wt;
+        }
+        s = warp_sum(s); w = warp_sum(w);
+        __shared__ T ss[32], sw[32];
+        if ((tid & 31) == 0) { ss[tid >> 5] = s; sw[tid >> 5] = w; }
+        __syncthreads();
+        if (tid == 0) { T S = 0, W = 0; for (int q = 0; q < nt / 32; ++q) { S += ss[q]; W += sw[q]; } ss[0] = S / W; }
+        __syncthreads();
+        T mean = ss[0];
+        T m = 0;
+        for (int t = tid; t < (X + 1) * (Y + 1) * (Z + 1); t += nt) {
+            int k = t % (Z + 1), j = (t / (Z + 1)) % (Y + 1), i = t / ((Z + 1) * (Y + 1));
+            at(r, i, j, k) -= mean;
+            m = fmax(m, fabs(at(r, i, j, k)));
+        }
+        m = warp_max(m);
+        if ((tid & 31) == 0) red[tid >> 5] = m;
+        __syncthreads();
+        if (tid == 0) { T M = 0; for (int q = 0; q < nt / 32; ++q) M = fmax(M, red[q]); red[0] = M; }
+        __syncthreads();
+        thresh = tol * red[0];
+        __syncthreads();
+    }
+    int iterCount = 0;
+    long long sweeps = 0;
+    int smax = X + Y + Z;
+    while (true) {
+        smem_impose_bc(p, X, Y, Z, bc, (const T *)nullptr, (const T *)nullptr, (const T *)nullptr);
+        for (int s = 0; s <= smax; ++s) {
+            for (int t = tid; t < (X + 1) * (Y + 1); t += nt) {
+                int i = t / (Y + 1), j = t % (Y + 1);
+                int k = s - i - j;
+                if (k < 0 || k > Z) continue;
+                at(p, i, j, k) = mg_update<T>(at(p, i + 1, j, k), at(p, i - 1, j, k), at(p, i, j + 1, k), at(p, i, j - 1, k),
+                                              at(p, i, j, k + 1), at(p, i, j, k - 1), at(r, i, j, k), kk);
+            }
+            __syncthreads();
+        }
+        sweeps += 1;
+        T localMax = (T)-1.0e-10;
+        for (int t = tid; t < (X + 1) * (Y + 1) * (Z + 1); t += nt) {
+            int k = t % (Z + 1), j = (t / (Z + 1)) % (Y + 1), i = t / ((Z + 1) * (Y + 1));
+            T lap = mg_lap<T>(at(p, i + 1, j, k), at(p, i - 1, j, k), at(p, i, j + 1, k), at(p, i, j - 1, k), at(p, i, j, k + 1),
+                              at(p, i, j, k - 1), at(p, i, j, k), kk);
+            T v = fabs(at(r, i, j, k) - lap);
+            if (v != v) v = (T)INFINITY;
+            if (v > localMax) localMax = v;
+        }
+        localMax = warp_max(localMax);
+        if ((tid & 31) == 0) red[tid >> 5] = localMax;
+        __syncthreads();
+        if (tid == 0) {
+            T M = red[0];
+            for (int q = 1; q < nt / 32; ++q) M = fmax(M, red[q]);
+            int st = 0;
+            if (M < thresh) st = 1;
+            else {
+                iterCount += 1;
+                if (iterCount > maxCount) st = 1;
+            }
+            stop = st;
+        }
+        __syncthreads();
+        if (stop) break;
+    }
+    smem_impose_bc(p, X, Y, Z, bc, (const T *)nullptr, (const T *)nullptr, (const T *)nullptr);
+    for (int t = tid; t < n; t += nt) pg.p[t] = p[t];
+    if (tid == 0 && iters) *iters += sweeps;
+}
+
+// ------------------------------------------------------------------ FP64 drivers
+// Load the level-0 right-hand side: residualData(0)(core) = rhs(core), then
+// updatePads (poisson.cc:114-118); per-block partial sums for the padded mean.
+__global__ void k_mg_load(View3<double> r0, View3<const double> rhs, MgBC bc, double *part) {
+    __shared__ double sm[32];
+    long n = r0.size();
+    double s = 0;
+    int E1 = bc.E[1], E2 = bc.E[2];
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+        int k = (int)(t % (E2 + 3)) - 1;
+        int j = (int)((t / (E2 + 3)) % (E1 + 3)) - 1;
+        int i = (int)(t / ((long)(E2 + 3) * (E1 + 3))) - 1;
+        int q[3] = {i, j, k};
+        bool zero = false;
+        // z ghosts: never written by updatePads; x/y ghosts: periodic copies.
+        if (k < 0 || k > E2) zero = true;
+        for (int d = 0; d < 2 && !zero; ++d) {
+            int E = bc.E[d];
+            if (q[d] >= 0 && q[d] <= E) continue;
+            if (!bc.per[d]) { zero = true; break; }
+            q[d] = q[d] < 0 ? E - 1 : 1;
+        }
+        double v = zero ? 0.0 : rhs(q[0], q[1], q[2]);
+        r0.p[t] = v;
+        s += v;
+    }
+    s = warp_sum(s);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) { double S = 0; for (int w = 0; w < (int)(blockDim.x >> 5); ++w) S += sm[w]; part[blockIdx.x] = S; }
+}
+
+// residualData(0) -= mean (whole padded array, poisson.cc:128); block max of |r|.
+__global__ void k_mg_sub_mean(double *r, long n, const double *sum, double count, double *maxabs) {
+    double mean = (*sum / count) / 1.0;
+    double m = 0;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+        double v = r[t] - mean;
+        r[t] = v;
+        m = fmax(m, fabs(v));
+    }
+    block_max_to(m, maxabs);
+}
+
+// pressureData(0)(core) = inFn(core) with face ghosts filled (poisson.cc:115, imposeBC).
+template <typename T>
+__global__ void k_mg_init_p(View3<T> p, View3<const double> src, MgBC bc) {
+    int i, j, k;
+    if (!core_pt(bc.E, i, j, k)) return;
+    put_scatter(p, i, j, k, (T)src(i, j, k), bc);
+}
+
+// Full ghost fill of level 0 with the composition order of imposeBC (x, y, z
+// planes over full extents), written to dst (the whole padded Pp array).
+__global__ void k_mg_output(View3<double> dst, View3<const double> p, MgBC bc, const double *wx, const double *wy, const double *wz) {
+    long n = dst.size();
+    int E1 = bc.E[1], E2 = bc.E[2];
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+        int k = (int)(t % (E2 + 3)) - 1;
+        int j = (int)((t / (E2 + 3)) % (E1 + 3)) - 1;
+        int i = (int)(t / ((long)(E2 + 3) * (E1 + 3))) - 1;
+        int q[3] = {i, j, k};
+        double sign = 1.0;
+        double value = 0;
+        bool fixed = false;
+        // resolve the last writer first: z plane op, then y, then x
+        for (int d = 2; d >= 0; --d) {
+            int E = bc.E[d];
+            if (q[d] >= 0 && q[d] <= E) continue;
+            if (bc.per[d]) { q[d] = q[d] < 0 ? E - 1 : 1; continue; }
+            if (bc.dirichlet && !bc.zeroBC) {
+                const double *w = d == 0 ? wx : d == 1 ? wy : wz;
+                int a = d == 0 ? q[1] : q[0], b = d == 2 ? q[1] : q[2];
+                int nb = d == 2 ? (E1 + 3) : (E2 + 3);
+                value = w[(a + 1) * nb + (b + 1)];
+                fixed = true;
+                break;
+            }
+            if (bc.dirichlet) sign = -sign;
+            q[d] = q[d] < 0 ? 1 : E - 1;
+        }
+        dst.p[t] = fixed ? sign * value : sign * p(q[0], q[1], q[2]);
+    }
+}
+
+// computeError (poisson_d3.cc:391-459) at level 0: max over the core of
+// |Lap(p) - r| (norm 1) or the per-block sums of squares (norm 2).
+__global__ void k_mg_error(View3<const double> p, View3<const double> r, MgK kk, MgBC bc, int norm, double *maxv,
+                           double *partNum, double *partDen) {
+    __shared__ double s1[32], s2[32];
+    int E0 = bc.E[0], E1 = bc.E[1], E2 = bc.E[2];
+    long n = (long)(E0 + 1) * (E1 + 1) * (E2 + 1);
+    double m = 0, sn = 0, sd = 0;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+        int k = (int)(t % (E2 + 1)), j = (int)((t / (E2 + 1)) % (E1 + 1)), i = (int)(t / ((long)(E2 + 1) * (E1 + 1)));
+        double lap = mg_lap<double>(p(i + 1, j, k), p(i - 1, j, k), p(i, j + 1, k), p(i, j - 1, k), p(i, j, k + 1), p(i, j, k - 1),
+                                    p(i, j, k), kk);
+        double v = fabs(lap - r(i, j, k));
+        if (v != v) v = INFINITY;
+        m = fmax(m, v);
+        sn += v * v;
+        sd += r(i, j, k) * r(i, j, k);
+    }
+    if (norm == 1) { block_max_to(m, maxv); return; }
+    sn = warp_sum(sn); sd = warp_sum(sd);
+    if ((threadIdx.x & 31) == 0) { s1[threadIdx.x >> 5] = sn; s2[threadIdx.x >> 5] = sd; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double A = 0, B = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { A += s1[w]; B += s2[w]; }
+        partNum[blockIdx.x] = A; partDen[blockIdx.x] = B;
+    }
+}
+
+// ---- target modes (FP64 / mixed)
+// Trapezoidal-weight partial sums of the core of rhs.
+__global__ void k_trap_sum(View3<const double> rhs, MgBC bc, double *part) {
+    __shared__ double sm[32];
+    int E0 = bc.E[0], E1 = bc.E[1], E2 = bc.E[2];
+    long n = (long)(E0 + 1) * (E1 + 1) * (E2 + 1);
+    double s = 0;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+        int k = (int)(t % (E2 + 1)), j = (int)((t / (E2 + 1)) % (E1 + 1)), i = (int)(t / ((long)(E2 + 1) * (E1 + 1)));
+        double w = ((i == 0 || i == E0) ? 0.5 : 1.0) * ((j == 0 || j == E1) ? 0.5 : 1.0) * ((k == 0 || k == E2) ? 0.5 : 1.0);
+        s += w * rhs(i, j, k);
+    }
+    s = warp_sum(s);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) { double S = 0; for (int w = 0; w < (int)(blockDim.x >> 5); ++w) S += sm[w]; part[blockIdx.x] = S; }
+}
+
+// b = rhs - trapmean over the core; block max |b|.
+__global__ void k_tgt_rhs(View3<double> b, View3<const double> rhs, MgBC bc, const double *sum, double wsum, double *maxabs) {
+    int i, j, k;
+    bool ok = core_pt(bc.E, i, j, k);
+    double m = 0;
+    if (ok) {
+        double v = rhs(i, j, k) - (*sum / wsum);
+        b(i, j, k) = v;
+        m = fabs(v);
+    }
+    block_max_to(m, maxabs);
+}
+
+// Fused refinement step: p <- p + e (if e given), then r = b - Lap(p) over the
+// core in FP64; the updated p gets its face ghosts, r is stored in FP32 (mixed
+// mode) or FP64 (plain target mode); block max |r|.
+template <bool HAS_E, typename RT>
+__global__ void k_refine(View3<double> pout, View3<const double> pin, View3<const float> e, View3<const double> b, View3<RT> r,
+                         MgK kk, MgBC bc, double *maxres) {
+    int i, j, k;
+    bool ok = core_pt(bc.E, i, j, k);
+    double m = 0;
+    if (ok) {
+        auto P = [&](int a, int bb, int c) -> double { return HAS_E ? pin(a, bb, c) + (double)e(a, bb, c) : pin(a, bb, c); };
+        double C = P(i, j, k);
+        double lap = mg_lap<double>(P(i + 1, j, k), P(i - 1, j, k), P(i, j + 1, k), P(i, j - 1, k), P(i, j, k + 1), P(i, j, k - 1), C, kk);
+        double res = b(i, j, k) - lap;
+        if (HAS_E) put_scatter(pout, i, j, k, C, bc);
+        r(i, j, k) = (RT)res;
+        m = fabs(res);
+        if (m != m) m = INFINITY;
+    }
+    block_max_to(m, maxres);
+}
+
+// ------------------------------------------------------------------ host
+static MgBC level_bc(const Ctx &c, int l, bool tgt) {
+    MgBC b;
+    b.per[0] = c.p.xPer; b.per[1] = c.p.yPer; b.per[2] = c.p.zPer;
+    for (int d = 0; d < 3; ++d) b.E[d] = c.lv[l].n[d];
+    b.dirichlet = c.p.testPoisson && !tgt;
+    b.zeroBC = (l != 0);
+    b.tgtPads = tgt ? 1 : 0;
+    return b;
+}
+
+template <typename T>
+static View3<T> lview(const Level &L, T *p) { return make_view<T>(p, L.n[0] + 1, L.n[1] + 1, L.n[2] + 1); }
+template <typename T>
+static View3<const T> lcview(const Level &L, const T *p) {
+    View3<T> w = make_view<T>(const_cast<T *>(p), L.n[0] + 1, L.n[1] + 1, L.n[2] + 1);
+    View3<const T> v; v.p = w.p; v.n[0] = w.n[0]; v.n[1] = w.n[1]; v.n[2] = w.n[2]; v.sx = w.sx; v.sy = w.sy;
+    return v;
+}
+
+static void core_dims(const Level &L, dim3 &g, dim3 &b) {
+    int nz = L.n[2] + 1, ny = L.n[1] + 1, nx = L.n[0] + 1;
+    b = nz >= 64 ? dim3(64, 4, 1) : nz >= 32 ? dim3(32, 8, 1) : dim3(16, 8, 2);
+    g = dim3((nz + b.x - 1) / b.x, (ny + b.y - 1) / b.y, (nx + b.z - 1) / b.z);
+}
+
+static int chk(Ctx &c, const char *what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) { c.err = std::string(what) + ": " + cudaGetErrorString(e); return SARAS_CUDA_ERROR; }
+    return SARAS_OK;
+}
+
+int mg_setup(Ctx &c) {
+    const saras_params &p = c.p;
+    c.depth = p.vcDepth;
+    c.mgMode = p.mgMode;
+    c.mgTarget = p.mgTarget;
+    c.mgMaxCycles = p.mgMaxCycles;
+    int ind[3] = {p.xInd, p.yInd, p.zInd};
+    c.lv.assign(c.depth + 1, Level());
+    for (int l = 0; l <= c.depth; ++l) {
+        Level &L = c.lv[l];
+        for (int d = 0; d < 3; ++d) L.n[d] = int(std::pow(2, ind[d] - l));          // poisson.cc:336-357
+        L.count = (long)(L.n[0] + 3) * (L.n[1] + 3) * (L.n[2] + 3);
+        double s = std::pow(2, l);
+        double dXi = c.dXi[0], dEt = c.dXi[1], dZt = c.dXi[2];
+        L.hx = s * dXi; L.hy = s * dEt; L.hz = s * dZt;                                  // poisson.cc:419-438
+        L.hxhy = std::pow(s, 4.0) * std::pow(dXi, 2.0) * std::pow(dEt, 2.0);
+        L.hyhz = std::pow(s, 4.0) * std::pow(dEt, 2.0) * std::pow(dZt, 2.0);
+        L.hzhx = std::pow(s, 4.0) * std::pow(dZt, 2.0) * std::pow(dXi, 2.0);
+        L.hxhyhz = std::pow(s, 6.0) * std::pow(dXi, 2.0) * std::pow(dEt, 2.0) * std::pow(dZt, 2.0);
+        double xix2 = c.m2[0], ety2 = c.m2[1], ztz2 = c.m2[2];                            // poisson.cc:463-495
+        L.cx = L.hyhz * xix2; L.cy = L.hzhx * ety2; L.cz = L.hxhy * ztz2;
+        L.c7 = 2.0 * L.hxhyhz;
+        L.den = 4.0 * (L.hyhz * xix2 + L.hzhx * ety2 + L.hxhy * ztz2);
+        L.ihx2 = 1.0 / (L.hx * L.hx); L.ihy2 = 1.0 / (L.hy * L.hy); L.ihz2 = 1.0 / (L.hz * L.hz);
+        L.lx = xix2 * L.ihx2; L.ly = ety2 * L.ihy2; L.lz = ztz2 * L.ihz2;
+        size_t b64 = sizeof(double) * L.count, b32 = sizeof(float) * L.count;
+        SARAS_CUDA_TRY(cudaMalloc(&L.a, b64)); SARAS_CUDA_TRY(cudaMalloc(&L.b, b64)); SARAS_CUDA_TRY(cudaMalloc(&L.r, b64));
+        SARAS_CUDA_TRY(cudaMemsetAsync(L.a, 0, b64, c.stream)); SARAS_CUDA_TRY(cudaMemsetAsync(L.b, 0, b64, c.stream));
+        SARAS_CUDA_TRY(cudaMemsetAsync(L.r, 0, b64, c.stream));
+        SARAS_CUDA_TRY(cudaMalloc(&L.a32, b32)); SARAS_CUDA_TRY(cudaMalloc(&L.b32, b32)); SARAS_CUDA_TRY(cudaMalloc(&L.r32, b32));
+        SARAS_CUDA_TRY(cudaMemsetAsync(L.a32, 0, b32, c.stream)); SARAS_CUDA_TRY(cudaMemsetAsync(L.b32, 0, b32, c.stream));
+        SARAS_CUDA_TRY(cudaMemsetAsync(L.r32, 0, b32, c.stream));
+    }
+    const Level &C = c.lv[c.depth];
+    c.maxCount = (C.n[0] + 2) * (C.n[1] + 2) * (C.n[2] + 2);                            // poisson.cc:360-361
+    size_t smem = 2 * sizeof(double) * C.count;
+    if (smem > 220 * 1024) { c.err = "coarsest multigrid level too large for one CTA; increase V-Cycle Depth"; return SARAS_BAD_CONFIG; }
+    SARAS_CUDA_TRY(cudaFuncSetAttribute(k_mg_coarse<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    SARAS_CUDA_TRY(cudaFuncSetAttribute(k_mg_coarse<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (p.testPoisson) {
+        // multigrid_d3::initDirichlet (poisson_d3.cc:513-572), np = 1
+        const Level &L0 = c.lv[0];
+        int X = L0.n[0], Y = L0.n[1], Z = L0.n[2];
+        std::vector<double> wx((size_t)(Y + 3) * (Z + 3), 0.0), wy((size_t)(X + 3) * (Z + 3), 0.0), wz((size_t)(X + 3) * (Y + 3), 0.0);
+        int hX = X / 2, hY = Y / 2;
+        double xd, yd, zd;
+        xd = L0.hx + p.Lx / 2.0;
+        for (int j = 0; j <= Y; ++j) { yd = L0.hy * (j - hY); for (int k = 0; k <= Z; ++k) { zd = L0.hz * (k - Z / 2); wx[(j + 1) * (Z + 3) + k + 1] = (xd * xd + yd * yd + zd * zd) / 6.0; } }
+        yd = L0.hy + p.Ly / 2.0;
+        for (int i = 0; i <= X; ++i) { xd = L0.hx * (i - hX); for (int k = 0; k <= Z; ++k) { zd = L0.hz * (k - Z / 2); wy[(i + 1) * (Z + 3) + k + 1] = (xd * xd + yd * yd + zd * zd) / 6.0; } }
+        zd = L0.hz + p.Lz / 2.0;
+        for (int i = 0; i <= X; ++i) { xd = L0.hx * (i - hX); for (int j = 0; j <= Y; ++j) { yd = L0.hy * (j - hY); wz[(i + 1) * (Y + 3) + j + 1] = (xd * xd + yd * yd + zd * zd) / 6.0; } }
+        SARAS_CUDA_TRY(cudaMalloc(&c.wallX, wx.size() * 8)); SARAS_CUDA_TRY(cudaMalloc(&c.wallY, wy.size() * 8)); SARAS_CUDA_TRY(cudaMalloc(&c.wallZ, wz.size() * 8));
+        SARAS_CUDA_TRY(cudaMemcpy(c.wallX, wx.data(), wx.size() * 8, cudaMemcpyHostToDevice));
+        SARAS_CUDA_TRY(cudaMemcpy(c.wallY, wy.data(), wy.size() * 8, cudaMemcpyHostToDevice));
+        SARAS_CUDA_TRY(cudaMemcpy(c.wallZ, wz.data(), wz.size() * 8, cudaMemcpyHostToDevice));
+    }
+    return SARAS_OK;
+}
+
+void mg_free(Ctx &c) {
+    for (Level &L : c.lv) { cudaFree(L.a); cudaFree(L.b); cudaFree(L.r); cudaFree(L.a32); cudaFree(L.b32); cudaFree(L.r32); }
+    c.lv.clear();
+    cudaFree(c.wallX); cudaFree(c.wallY); cudaFree(c.wallZ);
+    c.wallX = c.wallY = c.wallZ = nullptr;
+}
+
+// Level-0 Dirichlet wall values into the face ghosts of a level-0 array
+// (zeroBC = false at level 0; constant for the whole solve).
+__global__ void k_dirichlet_walls(View3<double> p, MgBC bc, const double *wx, const double *wy, const double *wz) {
+    int i, j, k;
+    int E[3] = {bc.E[0] + 2, bc.E[1] + 2, bc.E[2] + 2};
+    if (!core_pt(E, i, j, k)) return;
+    i -= 1; j -= 1; k -= 1;
+    int gi = (i < 0 || i > bc.E[0]), gj = (j < 0 || j > bc.E[1]), gk = (k < 0 || k > bc.E[2]);
+    if (gi + gj + gk != 1) return;
+    if (gi) p(i, j, k) = wx[(j + 1) * (bc.E[2] + 3) + k + 1];
+    if (gj) p(i, j, k) = wy[(i + 1) * (bc.E[2] + 3) + k + 1];
+    if (gk) p(i, j, k) = wz[(i + 1) * (bc.E[1] + 3) + j + 1];
+}
+
+// ---- generic level operations (templated on precision)
+template <typename T> static T *A_(Level &L);
+template <> double *A_<double>(Level &L) { return L.pa(); }
+template <> float *A_<float>(Level &L) { return L.pa32(); }
+template <typename T> static T *B_(Level &L);
+template <> double *B_<double>(Level &L) { return L.pb(); }
+template <> float *B_<float>(Level &L) { return L.pb32(); }
+template <typename T> static T *R_(Level &L);
+template <> double *R_<double>(Level &L) { return L.r; }
+template <> float *R_<float>(Level &L) { return L.r32; }
+template <typename T> static void flip(Level &L);
+template <> void flip<double>(Level &L) { L.cur ^= 1; }
+template <> void flip<float>(Level &L) { L.cur32 ^= 1; }
+
+template <typename T>
+static int smooth(Ctx &c, int l, int count, bool zero_first, bool tgt) {
+    Level &L = c.lv[l];
+    MgBC bc = level_bc(c, l, tgt);
+    MgK kk = make_k(L);
+    dim3 g, b; core_dims(L, g, b);
+    T omega = tgt ? (T)c.p.jacobiWeight : (T)1.0;
+    int pk = sizeof(T) == 8 ? PK_MG_SMOOTH64 : PK_MG_SMOOTH32;
+    double bytes = 3.0 * sizeof(T) * (double)(L.n[0] + 1) * (L.n[1] + 1) * (L.n[2] + 1);
+    for (int n = 0; n < count; ++n) {
+        prof_begin(c, pk, l);
+        if (n == 0 && zero_first)
+            k_mg_sweep<T, true><<<g, b, 0, c.stream>>>(lview<T>(L, B_<T>(L)), lcview<T>(L, A_<T>(L)), lcview<T>(L, R_<T>(L)), kk, bc, omega);
+        else
+            k_mg_sweep<T, false><<<g, b, 0, c.stream>>>(lview<T>(L, B_<T>(L)), lcview<T>(L, A_<T>(L)), lcview<T>(L, R_<T>(L)), kk, bc, omega);
+        count_launch(c);
+        prof_end(c, pk, l, (n == 0 && zero_first) ? bytes * 2.0 / 3.0 : bytes);
+        flip<T>(L);
+    }
+    return chk(c, "mg smooth");
+}
+
+template <typename T>
+static int coarse_solve(Ctx &c, bool tgt) {
+    Level &L = c.lv[c.depth];
+    MgBC bc = level_bc(c, c.depth, tgt);
+    MgK kk = make_k(L);
+    size_t smem = 2 * sizeof(T) * L.count;
+    T tol = tgt ? (T)1.0e-6 : (T)c.p.mgTolerance;
+    int maxc = tgt ? 1000 : c.maxCount;
+    k_mg_coarse<T><<<1, 256, smem, c.stream>>>(lview<T>(L, A_<T>(L)), lcview<T>(L, R_<T>(L)), kk, bc, tol, maxc, tgt ? 1 : 0,
+                                               (long long *)(c.dscal + 40));
+    count_launch(c);
+    return chk(c, "mg coarse");
+}
+
+template <typename T>
+static int restrict_level(Ctx &c, int l, bool tgt) {
+    Level &L = c.lv[l], &C = c.lv[l + 1];
+    MgBC bcf = level_bc(c, l, tgt), bcc = level_bc(c, l + 1, tgt);
+    MgK kk = make_k(L);
+    dim3 g, b; core_dims(L, g, b);
+    int pk = sizeof(T) == 8 ? PK_MG_RESID64 : PK_MG_RESID32;
+    double pts = (double)(L.n[0] + 1) * (L.n[1] + 1) * (L.n[2] + 1);
+    prof_begin(c, pk, l);
+    k_mg_residual<T><<<g, b, 0, c.stream>>>(lview<T>(L, B_<T>(L)), lcview<T>(L, A_<T>(L)), lcview<T>(L, R_<T>(L)), kk, bcf);
+    count_launch(c);
+    prof_end(c, pk, l, 3.0 * sizeof(T) * pts);
+    dim3 g2, b2; core_dims(C, g2, b2);
+    pk = sizeof(T) == 8 ? PK_MG_RESTRICT64 : PK_MG_RESTRICT32;
+    prof_begin(c, pk, l);
+    k_mg_restrict<T><<<g2, b2, 0, c.stream>>>(lview<T>(C, R_<T>(C)), lcview<T>(L, B_<T>(L)), bcf, bcc);
+    count_launch(c);
+    prof_end(c, pk, l, sizeof(T) * pts * (1.0 + 1.0 / 8.0));
+    return chk(c, "mg restrict");
+}
+
+template <typename T>
+static int prolong_level(Ctx &c, int l, bool tgt, bool add) {
+    Level &L = c.lv[l], &C = c.lv[l + 1];
+    MgBC bc = level_bc(c, l, tgt);
+    dim3 g, b; core_dims(L, g, b);
+    int pk = sizeof(T) == 8 ? PK_MG_PROLONG64 : PK_MG_PROLONG32;
+    double pts = (double)(L.n[0] + 1) * (L.n[1] + 1) * (L.n[2] + 1);
+    prof_begin(c, pk, l);
+    k_mg_prolong_add<T><<<g, b, 0, c.stream>>>(lview<T>(L, A_<T>(L)), lcview<T>(C, A_<T>(C)), bc, add ? 1 : 0);
+    count_launch(c);
+    prof_end(c, pk, l, sizeof(T) * pts * (2.0 + 1.0 / 8.0));
+    return chk(c, "mg prolong");
+}
+
+// poisson::vCycle (poisson.cc:219-280) on level arrays of precision T.
+// zero0: the level-0 iterate starts at 0 (inner FP32 solve of the mixed mode).
+template <typename T>
+static int vcycle(Ctx &c, bool tgt, bool zero0) {
+    int s;
+    int d = c.depth;
+    if ((s = smooth<T>(c, 0, c.p.preSmooth, zero0, tgt))) return s;
+    for (int l = 0; l < d; ++l) {
+        if ((s = restrict_level<T>(c, l, tgt))) return s;
+        if (l + 1 == d) { if ((s = coarse_solve<T>(c, tgt))) return s; }
+        else if ((s = smooth<T>(c, l + 1, c.p.preSmooth, true, tgt))) return s;
+    }
+    for (int l = d - 1; l >= 0; --l) {
+        if ((s = prolong_level<T>(c, l, tgt, true))) return s;
+        if ((s = smooth<T>(c, l, c.p.postSmooth, false, tgt))) return s;
+    }
+    return SARAS_OK;
+}
+
+static int read_scalars(Ctx &c, int first, int count) {
+    SARAS_CUDA_TRY(cudaMemcpyAsync(c.hscal + first, c.dscal + first, sizeof(double) * count, cudaMemcpyDeviceToHost, c.stream));
+    SARAS_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return SARAS_OK;
+}
+
+static int grid_blocks(long n) { return (int)std::max<long>(1, std::min<long>((n + 255) / 256, 152L * 8)); }
+
+int mg_compute_error(Ctx &c, int norm, double *err) {
+    Level &L = c.lv[0];
+    MgBC bc = level_bc(c, 0, false);
+    MgK kk = make_k(L);
+    long n = (long)(L.n[0] + 1) * (L.n[1] + 1) * (L.n[2] + 1);
+    int nb = std::min(grid_blocks(n), c.redCap);
+    SARAS_CUDA_TRY(cudaMemsetAsync(c.dscal + 22, 0, sizeof(double), c.stream));
+    // denominator max|residualData(0)| over the padded array (poisson_d3.cc:437)
+    SARAS_CUDA_TRY(cudaMemsetAsync(c.dscal + 21, 0, sizeof(double), c.stream));
+    if (norm == 1) {
+        k_maxabs<<<grid_blocks(L.count), 256, 0, c.stream>>>(L.r, L.count, c.dscal + 21);
+        count_launch(c);
+    }
+    k_mg_error<<<nb, 256, 0, c.stream>>>(lcview<double>(L, L.pa()), lcview<double>(L, L.r), kk, bc, norm, c.dscal + 22, c.red,
+                                         c.red + c.redCap);
+    count_launch(c);
+    if (norm == 2) {
+        k_final_reduce<<<1, 256, 0, c.stream>>>(c.red, nb, 0, c.dscal + 24);
+        k_final_reduce<<<1, 256, 0, c.stream>>>(c.red + c.redCap, nb, 0, c.dscal + 25);
+        count_launch(c, 2);
+    }
+    int s = chk(c, "computeError");
+    if (s) return s;
+    if ((s = read_scalars(c, 21, 5))) return s;
+    double e = 0;
+    if (norm == 1) {
+        double num = c.hscal[22], den = c.hscal[21];
+        e = den ? num / den : num;
+    } else if (norm == 2) {
+        double cnt = (double)n;
+        double num = c.hscal[24], den = c.hscal[25];
+        e = den ? std::sqrt(num / cnt) / std::sqrt(den / cnt) : std::sqrt(num / cnt);
+    }
+    *err = e;
+    return SARAS_OK;
+}
+
+// poisson::mgSolve (poisson.cc:100-205), reference mode.
+static int mg_solve_reference(Ctx &c, int *cycles, double *residual) {
+    int s;
+    Level &L0 = c.lv[0];
+    MgBC bc0 = level_bc(c, 0, false);
+    // zero scalars used for the |r| denominator and the mean offset trick
+    SARAS_CUDA_TRY(cudaMemsetAsync(c.dscal + 20, 0, sizeof(double) * 8, c.stream));
+    int nb = std::min(grid_blocks(L0.count), c.redCap);
+    View3<const double> rhs = lcview<double>(L0, c.f[SARAS_FIELD_MGRHS]);
+    k_mg_load<<<nb, 256, 0, c.stream>>>(lview<double>(L0, L0.r), rhs, bc0, c.red);
+    count_launch(c);
+    if (!c.p.testPoisson) {
+        k_final_reduce<<<1, 256, 0, c.stream>>>(c.red, nb, 0, c.dscal + 20);
+        k_mg_sub_mean<<<grid_blocks(L0.count), 256, 0, c.stream>>>(L0.r, L0.count, c.dscal + 20, (double)L0.count, c.dscal + 27);
+        count_launch(c, 2);
+    }
+    // pressureData(0)(core) = Pp(core) (+ face ghosts)
+    L0.cur = 0;
+    dim3 g, b; core_dims(L0, g, b);
+    k_mg_init_p<double><<<g, b, 0, c.stream>>>(lview<double>(L0, L0.pa()), lcview<double>(L0, c.f[SARAS_FIELD_PP]), bc0);
+    count_launch(c);
+    if (c.p.testPoisson) {
+        dim3 g2, b2;
+        Level tmp = L0; tmp.n[0] += 2; tmp.n[1] += 2; tmp.n[2] += 2;
+        core_dims(tmp, g2, b2);
+        k_dirichlet_walls<<<g2, b2, 0, c.stream>>>(lview<double>(L0, L0.a), bc0, c.wallX, c.wallY, c.wallZ);
+        k_dirichlet_walls<<<g2, b2, 0, c.stream>>>(lview<double>(L0, L0.b), bc0, c.wallX, c.wallY, c.wallZ);
+        count_launch(c, 2);
+    }
+    if ((s = chk(c, "mg load"))) return s;
+    double prev = 0.0, res = 0.0;
+    int cyc = 0;
+    for (int i = 0; i < c.p.vcCount; ++i) {
+        if ((s = vcycle<double>(c, false, false))) return s;
+        cyc += 1;
+        if ((s = mg_compute_error(c, c.p.resType, &res))) return s;
+        if (!std::isfinite(res)) { c.err = "multigrid residual is not finite"; return SARAS_NOT_FINITE; }
+        if (!c.p.testPoisson) {
+            if (std::fabs(prev - res) < c.p.mgTolerance) break;
+            prev = res;
+        }
+    }
+    // inFn.F = pressureData(0) over the padded array (poisson.cc:151)
+    k_mg_output<<<grid_blocks(L0.count), 256, 0, c.stream>>>(lview<double>(L0, c.f[SARAS_FIELD_PP]), lcview<double>(L0, L0.pa()), bc0,
+                                                             c.wallX, c.wallY, c.wallZ);
+    count_launch(c);
+    if ((s = chk(c, "mg output"))) return s;
+    if (cycles) *cycles = cyc;
+    if (residual) *residual = res;
+    return SARAS_OK;
+}
+
+// FP64 max|b - A p| / max|b| of the level-0 iterate (target modes).
+int mg_fine_residual(Ctx &c, const double *pp, double *maxres, double *maxb) {
+    (void)pp; (void)maxres; (void)maxb;
+    return SARAS_OK;
+}
+
+// Target modes: plain FP64 V-cycles or FP32 V-cycles inside FP64 refinement.
+static int mg_solve_target(Ctx &c, int *cycles, double *residual, saras_step_stats *st) {
+    int s;
+    Level &L0 = c.lv[0];
+    MgBC bc0 = level_bc(c, 0, true);
+    MgK k0 = make_k(L0);
+    dim3 g, b; core_dims(L0, g, b);
+    long ncore = (long)(L0.n[0] + 1) * (L0.n[1] + 1) * (L0.n[2] + 1);
+    int nb = std::min(grid_blocks(ncore), c.redCap);
+    // b = rhs - trapezoidal mean (stored in level-0 FP64 r)
+    SARAS_CUDA_TRY(cudaMemsetAsync(c.dscal + 30, 0, sizeof(double) * 6, c.stream));
+    k_trap_sum<<<nb, 256, 0, c.stream>>>(lcview<double>(L0, c.f[SARAS_FIELD_MGRHS]), bc0, c.red);
+    k_final_reduce<<<1, 256, 0, c.stream>>>(c.red, nb, 0, c.dscal + 30);
+    double wsum = 1.0;
+    for (int d = 0; d < 3; ++d) wsum *= (double)L0.n[d];
+    k_tgt_rhs<<<g, b, 0, c.stream>>>(lview<double>(L0, L0.r), lcview<double>(L0, c.f[SARAS_FIELD_MGRHS]), bc0, c.dscal + 30, wsum, c.dscal + 31);
+    // p = Pp (initial guess) with face ghosts
+    L0.cur = 0;
+    k_mg_init_p<double><<<g, b, 0, c.stream>>>(lview<double>(L0, L0.pa()), lcview<double>(L0, c.f[SARAS_FIELD_PP]), bc0);
+    count_launch(c, 4);
+    if ((s = chk(c, "target load"))) return s;
+    if ((s = read_scalars(c, 31, 1))) return s;
+    double bmax = c.hscal[31];
+    double target = c.mgTarget * bmax;
+    auto fine_res = [&](bool withE, double *out) -> int {
+        SARAS_CUDA_TRY(cudaMemsetAsync(c.dscal + 32, 0, sizeof(double), c.stream));
+        prof_begin(c, PK_REFINE_RESID, 0);
+        if (withE) {
+            k_refine<true, float><<<g, b, 0, c.stream>>>(lview<double>(L0, L0.pb()), lcview<double>(L0, L0.pa()),
+                                                        lcview<float>(L0, L0.pa32()), lcview<double>(L0, L0.r),
+                                                        lview<float>(L0, L0.r32), k0, bc0, c.dscal + 32);
+            count_launch(c);
+            prof_end(c, PK_REFINE_RESID, 0, (8.0 + 4.0 + 8.0 + 8.0 + 4.0) * (double)ncore);
+            L0.cur ^= 1;
+        } else if (c.mgMode == SARAS_MG_MIXED) {
+            k_refine<false, float><<<g, b, 0, c.stream>>>(lview<double>(L0, L0.pb()), lcview<double>(L0, L0.pa()),
+                                                         lcview<float>(L0, L0.pa32()), lcview<double>(L0, L0.r),
+                                                         lview<float>(L0, L0.r32), k0, bc0, c.dscal + 32);
+            count_launch(c);
+            prof_end(c, PK_REFINE_RESID, 0, (8.0 + 8.0 + 4.0) * (double)ncore);
+        } else {
+            // plain target: residual only, into the scratch ping-pong buffer
+            k_refine<false, double><<<g, b, 0, c.stream>>>(lview<double>(L0, L0.pb()), lcview<double>(L0, L0.pa()),
+                                                          lcview<float>(L0, L0.pa32()), lcview<double>(L0, L0.r),
+                                                          lview<double>(L0, L0.pb()), k0, bc0, c.dscal + 32);
+            count_launch(c);
+            prof_end(c, PK_REFINE_RESID, 0, (8.0 + 8.0 + 8.0) * (double)ncore);
+        }
+        int q = chk(c, "refine");
+        if (q) return q;
+        q = read_scalars(c, 32, 1);
+        if (q) return q;
+        *out = c.hscal[32];
+        return SARAS_OK;
+    };
+    double r = 0;
+    if ((s = fine_res(false, &r))) return s;
+    if (st) st->guess_residual = bmax > 0 ? r / bmax : r;
+    int cyc = 0, steps = 0;
+    while (r > target && cyc < c.mgMaxCycles) {
+        if (!std::isfinite(r)) { c.err = "multigrid residual is not finite"; return SARAS_NOT_FINITE; }
+        if (c.mgMode == SARAS_MG_PLAIN_TARGET) {
+            if ((s = vcycle<double>(c, true, false))) return s;
+            cyc += 1;
+            if ((s = fine_res(false, &r))) return s;
+        } else {
+            // inner FP32 solve of A e = r32 from e = 0
+            for (int q = 0; q < std::max(1, c.p.mixedCycles); ++q) {
+                if ((s = vcycle<float>(c, true, q == 0))) return s;
+                cyc += 1;
+            }
+            steps += 1;
+            if ((s = fine_res(true, &r))) return s;
+        }
+    }
+    if (st) { st->refine_steps = steps; st->fine_residual = bmax > 0 ? r / bmax : r; }
+    k_mg_output<<<grid_blocks(L0.count), 256, 0, c.stream>>>(lview<double>(L0, c.f[SARAS_FIELD_PP]), lcview<double>(L0, L0.pa()), bc0,
+                                                             nullptr, nullptr, nullptr);
+    count_launch(c);
+    if ((s = chk(c, "target output"))) return s;
+    if (cycles) *cycles = cyc;
+    if (residual) *residual = bmax > 0 ? r / bmax : r;
+    if (r > target) { c.err = "multigrid did not reach the residual target within mgMaxCycles"; return SARAS_NOT_CONVERGED; }
+    return SARAS_OK;
+}
+
+int mg_solve(Ctx &c, int *cycles, double *residual, saras_step_stats *st) {
+    long long before = 0;
+    SARAS_CUDA_TRY(cudaMemsetAsync(c.dscal + 40, 0, sizeof(double), c.stream));
+    int s = c.mgMode == SARAS_MG_REFERENCE ? mg_solve_reference(c, cycles, residual) : mg_solve_target(c, cycles, residual, st);
+    if (s) return s;
+    SARAS_CUDA_TRY(cudaMemcpyAsync(&before, c.dscal + 40, sizeof(long long), cudaMemcpyDeviceToHost, c.stream));
+    SARAS_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    c.coarseIters += before;
+    if (st) st->coarse_iters = (int)before;
+    return SARAS_OK;
+}
+
+// ---- test hooks mirroring the protected multigrid_d3 methods
+int mg_set_level(Ctx &c, int level, int which, const double *host) {
+    if (level < 0 || level > c.depth || (which != 0 && which != 1)) return SARAS_BAD_ARG;
+    Level &L = c.lv[level];
+    double *dst = which == 0 ? L.pa() : L.r;
+    SARAS_CUDA_TRY(cudaMemcpyAsync(dst, host, sizeof(double) * L.count, cudaMemcpyHostToDevice, c.stream));
+    if (which == 0) {
+        // keep the face ghosts consistent with imposeBC, as smooth() would on entry
+        MgBC bc = level_bc(c, level, false);
+        dim3 g, b; core_dims(L, g, b);
+        k_mg_init_p<double><<<g, b, 0, c.stream>>>(lview<double>(L, L.pb()), lcview<double>(L, dst), bc);
+        count_launch(c);
+        L.cur ^= 1;
+    }
+    return chk(c, "set level");
+}
+
+int mg_get_level(Ctx &c, int level, int which, double *host) {
+    if (level < 0 || level > c.depth || (which != 0 && which != 1)) return SARAS_BAD_ARG;
+    Level &L = c.lv[level];
+    const double *src = which == 0 ? L.pa() : L.r;
+    SARAS_CUDA_TRY(cudaMemcpyAsync(host, src, sizeof(double) * L.count, cudaMemcpyDeviceToHost, c.stream));
+    SARAS_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return SARAS_OK;
+}
+
+int mg_smooth_level(Ctx &c, int level, int count) {
+    if (level < 0 || level > c.depth) return SARAS_BAD_ARG;
+    if (level == c.depth && count < 0) return coarse_solve<double>(c, false);
+    return smooth<double>(c, level, count, false, false);
+}
+
+int mg_restrict_level(Ctx &c, int level) {
+    if (level < 0 || level >= c.depth) return SARAS_BAD_ARG;
+    return restrict_level<double>(c, level, false);
+}
+
+int mg_prolong_level(Ctx &c, int level) {
+    if (level < 0 || level >= c.depth) return SARAS_BAD_ARG;
+    return prolong_level<double>(c, level, false, true);
+}
+
+// multigrid_d3::testProlong (poisson_d3.cc:689-719)
+int mg_test_prolong(Ctx &c, double *err) {
+    if (c.depth < 1) return SARAS_BAD_ARG;
+    Level &L0 = c.lv[0], &L1 = c.lv[1];
+    std::vector<double> h1(L1.count, 0.0), h0(L0.count, 0.0);
+    View3<double> v1 = lview<double>(L1, nullptr), v0 = lview<double>(L0, nullptr);
+    // linear function sampled at the coincident fine indices (2i, 2j, 2k)
+    for (int i = 0; i <= L1.n[0]; ++i) for (int j = 0; j <= L1.n[1]; ++j) for (int k = 0; k <= L1.n[2]; ++k)
+        h1[v1.off(i, j, k)] = 1000 + (2 * i) * 100 + (2 * j) * 10 + 2 * k;
+    for (int i = 0; i <= L0.n[0]; ++i) for (int j = 0; j <= L0.n[1]; ++j) for (int k = 0; k <= L0.n[2]; ++k)
+        h0[v0.off(i, j, k)] = 1000 + i * 100 + j * 10 + k;
+    SARAS_CUDA_TRY(cudaMemcpyAsync(L1.pa(), h1.data(), L1.count * 8, cudaMemcpyHostToDevice, c.stream));
+    SARAS_CUDA_TRY(cudaMemsetAsync(L0.pa(), 0, L0.count * 8, c.stream));
+    MgBC bc = level_bc(c, 0, false);
+    dim3 g, b; core_dims(L0, g, b);
+    k_mg_prolong_add<double><<<g, b, 0, c.stream>>>(lview<double>(L0, L0.pa()), lcview<double>(L1, L1.pa()), bc, 0);
+    count_launch(c);
+    std::vector<double> out(L0.count);
+    SARAS_CUDA_TRY(cudaMemcpyAsync(out.data(), L0.pa(), L0.count * 8, cudaMemcpyDeviceToHost, c.stream));
+    SARAS_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    double m = 0;
+    for (int i = 0; i <= L0.n[0]; ++i) for (int j = 0; j <= L0.n[1]; ++j) for (int k = 0; k <= L0.n[2]; ++k)
+        m = std::max(m, std::fabs(out[v0.off(i, j, k)] - h0[v0.off(i, j, k)]));
+    *err = m;
+    return SARAS_OK;
+}
+
+// multigrid_d3::testTransfer (poisson_d3.cc:722-777) at level 0: face pads
+// after updatePads, for periodic x and y.
+int mg_test_transfer(Ctx &c, double *err) {
+    Level &L0 = c.lv[0];
+    View3<double> v0 = lview<double>(L0, nullptr);
+    std::vector<double> h(L0.count, 0.0), e(L0.count, 0.0);
+    int X = L0.n[0], Y = L0.n[1], Z = L0.n[2];
+    for (int i = 0; i <= X; ++i) for (int j = 0; j <= Y; ++j) for (int k = 0; k <= Z; ++k)
+        h[v0.off(i, j, k)] = e[v0.off(i, j, k)] = 1000 + i * 100 + j * 10 + k;
+    for (int j = 0; j <= Y; ++j) for (int k = 0; k <= Z; ++k) {
+        e[v0.off(-1, j, k)] = 1000 + (X - 1) * 100 + j * 10 + k;
+        e[v0.off(X + 1, j, k)] = 1000 + 100 + j * 10 + k;
+    }
+    for (int i = 0; i <= X; ++i) for (int k = 0; k <= Z; ++k) {
+        e[v0.off(i, -1, k)] = 1000 + i * 100 + (Y - 1) * 10 + k;
+        e[v0.off(i, Y + 1, k)] = 1000 + i * 100 + 10 + k;
+    }
+    SARAS_CUDA_TRY(cudaMemcpyAsync(L0.pb(), h.data(), L0.count * 8, cudaMemcpyHostToDevice, c.stream));
+    MgBC bc = level_bc(c, 0, false);
+    dim3 g, b; core_dims(L0, g, b);
+    k_mg_init_p<double><<<g, b, 0, c.stream>>>(lview<double>(L0, L0.pa()), lcview<double>(L0, L0.pb()), bc);
+    count_launch(c);
+    std::vector<double> out(L0.count);
+    SARAS_CUDA_TRY(cudaMemcpyAsync(out.data(), L0.pa(), L0.count * 8, cudaMemcpyDeviceToHost, c.stream));
+    SARAS_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    double m = 0;
+    for (int i = -1; i <= X + 1; ++i) for (int j = -1; j <= Y + 1; ++j) for (int k = 0; k <= Z; ++k) {
+        int gi = (i < 0 || i > X), gj = (j < 0 || j > Y);
+        if (gi && gj) continue;
+        m = std::max(m, std::fabs(out[v0.off(i, j, k)] - e[v0.off(i, j, k)]));
+    }
+    *err = m;
+    return SARAS_OK;
+}
+
+// multigrid_d3::testPeriodic (poisson_d3.cc:780-857) at level 0: face ghosts
+// of sin*cos*cos after imposeBC.
+int mg_test_periodic(Ctx &c, double *err) {
+    Level &L0 = c.lv[0];
+    View3<double> v0 = lview<double>(L0, nullptr);
+    int X = L0.n[0], Y = L0.n[1], Z = L0.n[2];
+    std::vector<double> h(L0.count, 0.0), e(L0.count, 0.0);
+    const double PI = M_PI;
+    auto xs = [&](int d, int i) { return c.L[d] * (double(i) * c.dXi[d]); };
+    auto fn = [&](double x, double y, double z) {
+        return std::sin(2.0 * PI * x / c.L[0]) * std::cos(2.0 * PI * y / c.L[1]) * std::cos(2.0 * PI * z / c.L[2]);
+    };
+    for (int i = 0; i <= X; ++i) for (int j = 0; j <= Y; ++j) for (int k = 0; k <= Z; ++k)
+        h[v0.off(i, j, k)] = e[v0.off(i, j, k)] = fn(xs(0, i), xs(1, j), xs(2, k));
+    for (int j = 0; j <= Y; ++j) for (int k = 0; k <= Z; ++k) {
+        e[v0.off(-1, j, k)] = fn(xs(0, 0) - (xs(0, 1) - xs(0, 0)), xs(1, j), xs(2, k));
+        e[v0.off(X + 1, j, k)] = fn(xs(0, X) + (xs(0, X) - xs(0, X - 1)), xs(1, j), xs(2, k));
+    }
+    for (int i = 0; i <= X; ++i) for (int k = 0; k <= Z; ++k) {
+        e[v0.off(i, -1, k)] = fn(xs(0, i), xs(1, 0) - (xs(1, 1) - xs(1, 0)), xs(2, k));
+        e[v0.off(i, Y + 1, k)] = fn(xs(0, i), xs(1, Y) + (xs(1, Y) - xs(1, Y - 1)), xs(2, k));
+    }
+    for (int i = 0; i <= X; ++i) for (int j = 0; j <= Y; ++j) {
+        e[v0.off(i, j, -1)] = fn(xs(0, i), xs(1, j), xs(2, 0) - (xs(2, 1) - xs(2, 0)));
+        e[v0.off(i, j, Z + 1)] = fn(xs(0, i), xs(1, j), xs(2, Z) + (xs(2, Z) - xs(2, Z - 1)));
+    }
+    SARAS_CUDA_TRY(cudaMemcpyAsync(L0.pb(), h.data(), L0.count * 8, cudaMemcpyHostToDevice, c.stream));
+    MgBC bc = level_bc(c, 0, false);
+    dim3 g, b; core_dims(L0, g, b);
+    k_mg_init_p<double><<<g, b, 0, c.stream>>>(lview<double>(L0, L0.pa()), lcview<double>(L0, L0.pb()), bc);
+    count_launch(c);
+    std::vector<double> out(L0.count);
+    SARAS_CUDA_TRY(cudaMemcpyAsync(out.data(), L0.pa(), L0.count * 8, cudaMemcpyDeviceToHost, c.stream));
+    SARAS_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    double m = 0;
+    for (int i = -1; i <= X + 1; ++i) for (int j = -1; j <= Y + 1; ++j) for (int k = -1; k <= Z + 1; ++k) {
+        int ng = (i < 0 || i > X) + (j < 0 || j > Y) + (k < 0 || k > Z);
+        if (ng > 1) continue;
+        m = std::max(m, std::fabs(out[v0.off(i, j, k)] - e[v0.off(i, j, k)]));
+    }
+    *err = m;
+    return SARAS_OK;
+}
+
+}  // namespace saras
