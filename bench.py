@@ -1,0 +1,404 @@
+#!/usr/bin/env python
+"""Throughput of the SARAS time step on GB300.
+
+Workload: 3D Taylor-Green vortex, 257^3 vertex grid on [0, 2 pi]^3, Re 1600,
+dt 5e-4 (the precision-form / learned-warm-start configuration).  A "step" is
+one hydro_d3::timeAdvance: NSE right-hand side, three Crank-Nicolson Jacobi
+solves, divergence, the pressure-correction solve to the FP64 residual target
+max|b - Ap| / max|b| <= 1e-8, projection and boundary fills.
+
+Our arm runs the pressure solve as FP32 V-cycles inside FP64 iterative
+refinement (optionally warm-started by the U-Net); the same run also times the
+plain FP64 V-cycle solve to the same residual target and reports both.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Multi-GPU: the path does not shard (one GPU owns the whole domain), so N > 1
+runs N independent replicas and `value` sums their steps.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+GRID_INDEX = 8          # 2^8 + 1 = 257 points per axis
+DEPTH = 6
+DT = 5.0e-4
+TARGET = 1.0e-8
+METRIC = "steps/s at 257^3: learned+mixed MG vs plain FP64 MG at equal 1e-8 residual"
+
+
+def tgv_params(mode, guess=0, ind=GRID_INDEX, depth=DEPTH):
+    from saras_gb300 import _abi
+    p = _abi.default_params()
+    p.probType, p.icType = 2, 1
+    p.xPer = p.yPer = p.zPer = 1
+    p.Lx = p.Ly = p.Lz = 2.0 * math.pi
+    p.xInd = p.yInd = p.zInd = ind
+    p.vcDepth = depth
+    p.Re = 1600.0
+    p.tStp = DT
+    p.cnTolerance = 1.0e-8
+    p.mgTolerance = 1.0e-8
+    p.preSmooth = p.postSmooth = 3
+    p.mgMode = mode
+    p.mgTarget = TARGET
+    p.mgMaxCycles = 100
+    p.mixedCycles = 1
+    p.jacobiWeight = 6.0 / 7.0 if mode != _abi.MG_REFERENCE else 1.0
+    p.guessMode = guess
+    return p
+
+
+def init_tgv(solver, p):
+    import saras_gb300 as S
+    from saras_gb300 import _abi as F
+    Vx, Vy = S.taylor_green_velocity(p)
+    solver.set(F.FIELD_VX, Vx)
+    solver.set(F.FIELD_VY, Vy)
+    solver.set(F.FIELD_P, S.taylor_green_pressure(p))
+    for f in (F.FIELD_VX, F.FIELD_VY, F.FIELD_VZ):
+        solver.apply_bc(f)
+
+
+# ------------------------------------------------------------------ distributed
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo", init_method="env://")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x):
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ------------------------------------------------------------------ clocks
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        if not self.proc:
+            return out
+        self.proc.terminate()
+        try:
+            self.proc.wait(5)
+        except Exception:
+            self.proc.kill()
+        try:
+            rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
+            sm = [float(r[1]) for r in rows if len(r) >= 9]
+            mx = [float(r[2]) for r in rows if len(r) >= 9]
+            reasons = set()
+            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+            for r in rows:
+                if len(r) < 9:
+                    continue
+                for n, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(n)
+            out = {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                   "reasons": sorted(reasons), "samples": len(sm)}
+        except Exception:
+            pass
+        try:
+            os.unlink(self.path)
+        except Exception:
+            pass
+        return out
+
+
+def measured_peak_hbm():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel):
+    """Per-launch DRAM traffic of `kernel` at this workload from the committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
+            return json.load(f).get(kernel)
+    except Exception:
+        return None
+
+
+# ------------------------------------------------------------------ arms
+def run_ours(args, dist):
+    import saras_gb300 as S
+    from saras_gb300 import _abi as F
+    S._abi.load()
+    gpu = dist.local
+    try:
+        import torch
+        torch.cuda.set_device(gpu)
+    except Exception:
+        torch = None
+    guess = F.GUESS_LEARNED if args.learned else F.GUESS_PREVIOUS
+    p = tgv_params(F.MG_MIXED, guess)
+    g = S.Solver(p)
+    init_tgv(g, p)
+    names = S.Solver.profile_names()
+    # --- warm-up (also trains the warm-start network when enabled)
+    warm_stats = []
+    for k in range(args.warmup):
+        s, st = g.time_advance()
+        if s != 0:
+            raise RuntimeError("warm-up step failed: %d" % s)
+        warm_stats.append(st.vcycles)
+    # pick the dominant kernel from one profiled step
+    for k in range(len(names)):
+        g.profile_enable(k, True)
+    s, st = g.time_advance()
+    totals = []
+    for k in range(len(names)):
+        n, ms, b = g.profile_read(k)
+        totals.append((ms, k, n, b))
+        g.profile_enable(k, False)
+    dom = max(totals)[1]
+    g.profile_enable(dom, True)
+    # --- timed region
+    clocks = Clocks(gpu)
+    clocks.start()
+    dist.barrier()
+    g.synchronize()
+    launches0 = g.launch_count()
+    g.event_record(0)
+    vc, rs, fine = [], [], []
+    for k in range(args.steps):
+        s, st = g.time_advance()
+        if s != 0:
+            raise RuntimeError("timed step failed: %d" % s)
+        vc.append(st.vcycles)
+        rs.append(st.refine_steps)
+        fine.append(st.fine_residual)
+    g.event_record(1)
+    g.synchronize()
+    dist.barrier()
+    ms = g.event_elapsed(0, 1)
+    clk = clocks.stop()
+    launches = g.launch_count() - launches0
+    n_dom, ms_dom, b_dom = g.profile_read(dom)
+    g.profile_enable(dom, False)
+    ms_max = dist.max(ms)
+    value = dist.world * args.steps / (ms_max / 1e3)
+    # --- plain FP64 multigrid on the same workload (same residual target)
+    plain = None
+    if not args.no_plain and dist.rank == 0:
+        q = tgv_params(F.MG_PLAIN_TARGET, F.GUESS_PREVIOUS)
+        h = S.Solver(q)
+        init_tgv(h, q)
+        for k in range(args.warmup):
+            h.time_advance()
+        steps_p = max(2, min(args.steps, 5))
+        h.synchronize()
+        h.event_record(0)
+        pvc = []
+        for k in range(steps_p):
+            s2, st2 = h.time_advance()
+            pvc.append(st2.vcycles)
+        h.event_record(1)
+        h.synchronize()
+        pms = h.event_elapsed(0, 1)
+        plain = {"steps_per_s": steps_p / (pms / 1e3), "vcycles_per_step": sum(pvc) / len(pvc), "steps": steps_p}
+        # error of the mixed solve against the plain FP64 solve after equal step counts
+        m = S.Solver(tgv_params(F.MG_MIXED, F.GUESS_PREVIOUS))
+        init_tgv(m, q)
+        for k in range(args.warmup + steps_p):
+            m.time_advance()
+        errs = {}
+        for f, name in ((F.FIELD_VX, "Vx"), (F.FIELD_VY, "Vy"), (F.FIELD_VZ, "Vz"), (F.FIELD_P, "P")):
+            a, b = m.get(f), h.get(f)
+            import numpy as np
+            errs[name] = float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+        plain["max_rel_err_mixed_vs_plain"] = errs
+        m.close()
+        h.close()
+    # --- end to end through the C ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        import numpy as np
+        fields = (F.FIELD_VX, F.FIELD_VY, F.FIELD_VZ, F.FIELD_P)
+        host = {}
+        if torch is not None:
+            for f in fields:
+                t = torch.empty(g.dims(f), dtype=torch.float64, pin_memory=True)
+                host[f] = (t, t.data_ptr())
+        else:
+            for f in fields:
+                a = np.empty(g.dims(f))
+                host[f] = (a, a.ctypes.data)
+        for f in fields:
+            g.download_ptr(f, host[f][1])
+        h2d = sum(8 * int(np.prod(g.dims(f))) for f in fields)
+        d2h = h2d
+        steps_e = max(2, min(args.steps, 5))
+        g.synchronize()
+        t0 = time.perf_counter()
+        for k in range(steps_e):
+            for f in fields:
+                g.upload_ptr(f, host[f][1])
+            s, st = g.time_advance()
+            for f in fields:
+                g.download_ptr(f, host[f][1])
+        g.synchronize()
+        el = dist.max(time.perf_counter() - t0)
+        e2e = {"value": dist.world * steps_e / el, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+               "steps": steps_e}
+    # --- roofline of the dominant kernel
+    peak, peak_kind = measured_peak_hbm()
+    bpl = b_dom / n_dom if n_dom else 0.0
+    avg_ms = ms_dom / n_dom if n_dom else 0.0
+    achieved = bpl / (avg_ms * 1e-3) / 1e9 if avg_ms > 0 else 0.0
+    roof = {"kernel": names[dom], "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+            "traffic": ncu_traffic(names[dom]), "launches": n_dom, "avg_ms": round(avg_ms, 4),
+            "share_of_step": round(ms_dom / ms, 4) if ms > 0 else None}
+    out = {
+        "metric": METRIC, "value": round(value, 4), "unit": "steps/s", "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic (Taylor-Green initial condition)",
+        "config": {
+            "workload": "Taylor-Green vortex 257^3 (2^8+1 vertex points per axis), [0,2pi]^3 PPP, Re 1600, dt 5e-4; "
+                        "pressure solve: FP32 V(3,3) cycles inside FP64 iterative refinement to max|b-Ap|/max|b| <= 1e-8",
+            "grid": [257, 257, 257], "vcycle_depth": DEPTH, "mg_mode": "mixed_fp32_in_fp64",
+            "warm_start": "unet" if args.learned else "previous_pressure",
+            "residual_target": TARGET, "vcycles_per_step": sum(vc) / len(vc),
+            "refine_steps_per_step": sum(rs) / len(rs), "max_fine_residual": max(fine),
+            "plain_fp64": plain,
+            "speedup_vs_plain_fp64": round(value / dist.world / plain["steps_per_s"], 3) if plain else None,
+            "l2": "inputs larger than L2: every FP64 field is 259^3*8 B = 139 MB > 129 MB L2",
+            "parallelism": "replicas" if dist.world > 1 else "single GPU",
+        },
+        "roofline": roof, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
+    }
+    if dist.rank == 0 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
+    g.close()
+    return out
+
+
+def cpu_baseline(budget_s=30.0, ind=GRID_INDEX, depth=DEPTH, vc_cap=2):
+    """The oracle (CPU restatement of the reference algorithm) on the host
+    cores: one reference time step of the same workload with the V-cycle loop
+    capped at `vc_cap` cycles (a bounded sample; the uncapped step needs the
+    cycles of the reference stopping rule on top)."""
+    from oracle.oracle import Oracle
+    from saras_gb300 import _abi as F
+    threads = int(os.environ.get("OMP_NUM_THREADS", str(os.cpu_count() or 1)))
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    p = tgv_params(F.MG_REFERENCE, F.GUESS_PREVIOUS, ind, depth)
+    p.vcCount = vc_cap
+    o = Oracle(p)
+    init_tgv(o, p)
+    t0 = time.perf_counter()
+    s, st = o.time_advance()
+    el = time.perf_counter() - t0
+    o.close()
+    return {"value": round(1.0 / el, 6), "unit": "steps/s", "cores": threads, "kind": "port",
+            "sample": "one reference time step of TGV %d^3 with the V-cycle loop capped at %d cycles (%.1f s on %d threads)"
+                      % (2 ** ind + 1, vc_cap, el, threads)}
+
+
+def run_reference(args, dist):
+    """The reference algorithm on the host cores: the CPU oracle (the reference
+    is C++ with MPI/Blitz++/yaml-cpp/HDF5, none of which is installed, so the
+    oracle's strict restatement stands in for it), each step a bounded sample."""
+    if dist.rank != 0:
+        return None
+    from oracle.oracle import Oracle
+    from saras_gb300 import _abi as F
+    threads = int(os.environ.get("OMP_NUM_THREADS", str(os.cpu_count() or 1)))
+    p = tgv_params(F.MG_REFERENCE, F.GUESS_PREVIOUS)
+    p.vcCount = 2
+    o = Oracle(p)
+    init_tgv(o, p)
+    for k in range(args.warmup):
+        o.time_advance()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        o.time_advance()
+    el = time.perf_counter() - t0
+    v = args.steps / el
+    return {
+        "impl": "reference", "metric": METRIC, "value": round(v, 6), "unit": "steps/s", "n_gpus": dist.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * el / args.steps, 1), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (Taylor-Green initial condition)",
+        "config": {"workload": "Taylor-Green vortex 257^3, Re 1600, dt 5e-4; reference multigrid (Jacobi V(3,3), "
+                               "V-cycle loop capped at 2 cycles per step as the bounded sample)",
+                   "grid": [257, 257, 257], "implementation": "CPU oracle (strict restatement of the reference), OpenMP"},
+        "cpu_baseline": {"value": round(v, 6), "unit": "steps/s", "cores": threads, "kind": "port",
+                         "sample": "%d reference steps of TGV 257^3, V-cycle loop capped at 2 cycles" % args.steps},
+        "e2e": {"value": round(v, 6), "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--learned", type=int, default=0)
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=30.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    dist = Dist()
+    try:
+        out = run_reference(args, dist) if args.impl == "reference" else run_ours(args, dist)
+        if dist.rank == 0 and out is not None:
+            print(json.dumps(out), flush=True)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -218,6 +218,10 @@ int saras_profile_read(saras_ctx *ctx, int kernel_id, long long *launches,
                        double *total_ms, double *bytes);
 const char *saras_profile_name(int kernel_id);
 int saras_profile_count(void);
+/* CUDA events on the context stream for whole-step timing: record event
+ * `slot` (0..15) now; elapsed milliseconds between two recorded slots. */
+int saras_event_record(saras_ctx *ctx, int slot);
+int saras_event_elapsed(saras_ctx *ctx, int slot_start, int slot_stop, double *ms);
 
 #ifdef __cplusplus
 }

@@ -18,7 +18,9 @@ SRC = os.path.join(_HERE, "saras_oracle.cc")
 LIB = os.path.join(_HERE, "_build", "libsaras_oracle.so")
 # Strict IEEE: no FMA contraction, no fast-math, so every expression is
 # evaluated in the order the reference writes it.
-CXXFLAGS = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-std=c++17", "-fPIC", "-shared"]
+# OpenMP parallelises only loops whose iterations write disjoint points (and
+# exact max reductions), so results do not depend on the thread count.
+CXXFLAGS = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-std=c++17", "-fPIC", "-shared", "-fopenmp"]
 
 
 def build(force=False):

@@ -64,6 +64,23 @@ struct A1 {  // 1D array with lower bound
     inline double operator()(int i) const { return v[(size_t)(i - lb)]; }
 };
 
+// Sum of a sequence in fixed 4096-element chunks: each chunk is summed in
+// index order, then the chunk sums are summed in chunk order.  The GPU
+// reduction of the same sums follows exactly this order, so both sides agree
+// bit for bit (the reference's one-pass Blitz sum differs from it by rounding).
+static const long kChunk = 4096;
+template <class Get>
+static double chunked_sum(long n, Get get) {
+    double total = 0.0;
+    for (long c0 = 0; c0 < n; c0 += kChunk) {
+        double s = 0.0;
+        long c1 = std::min(n, c0 + kChunk);
+        for (long t = c0; t < c1; ++t) s += get(t);
+        total += s;
+    }
+    return total;
+}
+
 // Blitz++ stencil operators (see header comment).
 static inline double central12n(double fm, double fp) { return (fp - fm) * 0.5; }
 static inline double central22n(double fm, double f0, double fp) { return fm - 2.0 * f0 + fp; }
@@ -398,6 +415,7 @@ struct Multigrid {
     void computeResidual() {
         int l = vLevel;
         tmpDataArray[l].fill(0.0);
+#pragma omp parallel for schedule(static)
         for (int i = 0; i <= xEnd[l]; ++i) for (int j = 0; j <= yEnd[l]; ++j) for (int k = 0; k <= zEnd[l]; ++k)
             tmpDataArray[l](i, j, k) = residualData[l](i, j, k) - lap(pressureData[l], l, i, j, k);
         updatePads(tmpDataArray);
@@ -415,6 +433,7 @@ struct Multigrid {
                 for (int i = 0; i <= xEnd[l]; ++i) for (int j = 0; j <= yEnd[l]; ++j) for (int k = 0; k <= zEnd[l]; ++k)
                     P(i, j, k) = update(P, residualData[l], l, i, j, k);
             } else {
+#pragma omp parallel for schedule(static)
                 for (int i = 0; i <= xEnd[l]; ++i) for (int j = 0; j <= yEnd[l]; ++j) for (int k = 0; k <= zEnd[l]; ++k)
                     tmpDataArray[l](i, j, k) = update(pressureData[l], residualData[l], l, i, j, k);
                 std::swap(tmpDataArray, pressureData);
@@ -454,6 +473,7 @@ struct Multigrid {
         vLevel += 1;
         const A3 &T = tmpDataArray[pLevel];
         A3 &R = residualData[vLevel];
+#pragma omp parallel for schedule(static)
         for (int i = 0; i <= xEnd[vLevel]; ++i) {
             int i2 = i * 2;
             for (int j = 0; j <= yEnd[vLevel]; ++j) {
@@ -490,6 +510,7 @@ struct Multigrid {
         A3 &F = pressureData[vLevel];
         const A3 &C = pressureData[pLevel];
         F.fill(0.0);
+#pragma omp parallel for schedule(static)
         for (int i = 0; i <= xEnd[vLevel]; ++i) {
             int i2 = i / 2;
             for (int j = 0; j <= yEnd[vLevel]; ++j) {
@@ -529,17 +550,21 @@ struct Multigrid {
         int valCountLoc = 0;
         const A3 &P = pressureData[0];
         const A3 &R = residualData[0];
-        for (int i = 0; i <= xEnd[0]; ++i) for (int j = 0; j <= yEnd[0]; ++j) for (int k = 0; k <= zEnd[0]; ++k) {
-            // hx(vLevel) with vLevel = 0 at this point
-            tempValue = std::fabs(lap(P, 0, i, j, k) - R(i, j, k));
-            switch (normOrder) {
-            case 1: if (tempValue > numValLoc) numValLoc = tempValue; break;
-            case 2:
-                numValLoc += tempValue * tempValue;
-                denValLoc += R(i, j, k) * R(i, j, k);
-                valCountLoc += 1;
-                break;
+        int X = xEnd[0], Y = yEnd[0], Z = zEnd[0];
+        long ncore = (long)(X + 1) * (Y + 1) * (Z + 1);
+        auto pt = [&](long t, int &i, int &j, int &k) { k = (int)(t % (Z + 1)); j = (int)((t / (Z + 1)) % (Y + 1)); i = (int)(t / ((long)(Z + 1) * (Y + 1))); };
+        if (normOrder == 1) {
+#pragma omp parallel for schedule(static) reduction(max : numValLoc) private(tempValue)
+            for (int i = 0; i <= X; ++i) for (int j = 0; j <= Y; ++j) for (int k = 0; k <= Z; ++k) {
+                // hx(vLevel) with vLevel = 0 at this point
+                tempValue = std::fabs(lap(P, 0, i, j, k) - R(i, j, k));
+                if (tempValue > numValLoc) numValLoc = tempValue;
             }
+        } else if (normOrder == 2) {
+            // sums in the chunked order shared with the GPU (see chunked_sum)
+            numValLoc = chunked_sum(ncore, [&](long t) { int i, j, k; pt(t, i, j, k); double v = std::fabs(lap(P, 0, i, j, k) - R(i, j, k)); return v * v; });
+            denValLoc = chunked_sum(ncore, [&](long t) { int i, j, k; pt(t, i, j, k); return R(i, j, k) * R(i, j, k); });
+            valCountLoc = (int)ncore;
         }
         switch (normOrder) {
         case 1: {
@@ -593,9 +618,9 @@ struct Multigrid {
         updatePads(residualData);
         updatePads(pressureData);
         if (!p.testPoisson) {
-            // blitz::mean over the padded array: sequential sum / count
-            double s = 0.0;
-            for (double x : residualData[0].v) s += x;
+            // blitz::mean over the padded array: sum / count (chunked order)
+            const std::vector<double> &rv = residualData[0].v;
+            double s = chunked_sum((long)rv.size(), [&](long t) { return rv[(size_t)t]; });
             double localMean = s / double(residualData[0].v.size());
             double globalAvg = localMean / 1.0;   // MPI_Allreduce / nProc at np = 1
             for (double &x : residualData[0].v) x -= globalAvg;
@@ -933,9 +958,11 @@ struct Solver {
 
     // vfield::computeDiff (vfield.cc:104-146) / sfield::computeDiff (sfield.cc:86-100)
     void computeDiff(const Field &f, A3 &H) {
-        for (int d = 0; d < 3; ++d)
+        for (int d = 0; d < 3; ++d) {
+#pragma omp parallel for schedule(static)
             for (int i = 0; i < f.cnt[0]; ++i) for (int j = 0; j < f.cnt[1]; ++j) for (int k = 0; k < f.cnt[2]; ++k)
                 H(i, j, k) += d2(f, d, i, j, k);
+        }
     }
 
     // vfield::computeNLin (vfield.cc:163-253) / sfield::computeNLin (sfield.cc:113-142)
@@ -945,6 +972,7 @@ struct Solver {
             int sh[4][3];
             int ns = slices(f, d, sh);
             const A3 &S = vsrc[d]->F;
+#pragma omp parallel for schedule(static)
             for (int i = 0; i < f.cnt[0]; ++i) for (int j = 0; j < f.cnt[1]; ++j) for (int k = 0; k < f.cnt[2]; ++k) {
                 double inter = 0.0;
                 for (int s = 0; s < ns; ++s) inter += S(i + sh[s][0], j + sh[s][1], k + sh[s][2]);
@@ -1007,6 +1035,7 @@ struct Solver {
         int iterCount = 0;
         double maxError = 0.0;
         while (true) {
+#pragma omp parallel for schedule(static)
             for (int iX = f.blb[0]; iX <= f.bub[0]; iX++) for (int iY = f.blb[1]; iY <= f.bub[1]; iY++) for (int iZ = f.blb[2]; iZ <= f.bub[2]; iZ++) {
                 double A = hy2hz2 * (*mx)(iX) * (V(iX + 1, iY, iZ) + V(iX - 1, iY, iZ)) +
                            hz2hx2 * (*my)(iY) * (V(iX, iY + 1, iZ) + V(iX, iY - 1, iZ)) +
@@ -1021,6 +1050,7 @@ struct Solver {
             }
             V.v = guess.v;
             imposeBCs(c);
+#pragma omp parallel for schedule(static)
             for (int iX = f.blb[0]; iX <= f.bub[0]; iX++) for (int iY = f.blb[1]; iY <= f.bub[1]; iY++) for (int iZ = f.blb[2]; iZ <= f.bub[2]; iZ++) {
                 double L = (*mx)(iX) * (V(iX + 1, iY, iZ) - 2.0 * V(iX, iY, iZ) + V(iX - 1, iY, iZ)) / (hx * hx) +
                            (*my)(iY) * (V(iX, iY + 1, iZ) - 2.0 * V(iX, iY, iZ) + V(iX, iY - 1, iZ)) / (hy * hy) +

@@ -240,6 +240,21 @@ class Solver:
         self._chk(self.lib.saras_profile_read(self.h, kernel_id, ctypes.byref(n), ctypes.byref(ms), ctypes.byref(b)))
         return n.value, ms.value, b.value
 
+    def event_record(self, slot):
+        self._chk(self.lib.saras_event_record(self.h, slot))
+
+    def event_elapsed(self, a, b):
+        ms = ctypes.c_double()
+        self._chk(self.lib.saras_event_elapsed(self.h, a, b, ctypes.byref(ms)))
+        return ms.value
+
+    def upload_ptr(self, field, ptr):
+        """Upload from a raw host pointer (e.g. pinned memory)."""
+        self._chk(self.lib.saras_upload(self.h, field, ctypes.cast(ptr, ctypes.POINTER(ctypes.c_double))))
+
+    def download_ptr(self, field, ptr):
+        self._chk(self.lib.saras_download(self.h, field, ctypes.cast(ptr, ctypes.POINTER(ctypes.c_double))))
+
     @staticmethod
     def profile_names():
         lib = _abi.load()

@@ -291,6 +291,7 @@ int saras_destroy(saras_ctx *h) {
     if (c.hscal) cudaFreeHost(c.hscal);
     for (int q = 0; q < 2; ++q) cudaFree(c.pHist[q]);
     for (int k = 0; k < PK_COUNT; ++k) for (cudaEvent_t e : c.prof[k].ev) cudaEventDestroy(e);
+    for (int k = 0; k < 16; ++k) if (c.userEv[k]) cudaEventDestroy(c.userEv[k]);
     if (c.stream) cudaStreamDestroy(c.stream);
     delete h;
     return SARAS_OK;
@@ -437,5 +438,24 @@ const char *saras_profile_name(int kernel_id) {
 }
 
 int saras_profile_count(void) { return PK_COUNT; }
+
+int saras_event_record(saras_ctx *h, int slot) {
+    if (!h || slot < 0 || slot >= 16) return SARAS_BAD_ARG;
+    Ctx &c = h->c;
+    if (!c.userEv[slot]) SARAS_CUDA_TRY(cudaEventCreate(&c.userEv[slot]));
+    SARAS_CUDA_TRY(cudaEventRecord(c.userEv[slot], c.stream));
+    return SARAS_OK;
+}
+
+int saras_event_elapsed(saras_ctx *h, int a, int b, double *ms) {
+    if (!h || !ms || a < 0 || a >= 16 || b < 0 || b >= 16) return SARAS_BAD_ARG;
+    Ctx &c = h->c;
+    if (!c.userEv[a] || !c.userEv[b]) return SARAS_BAD_ARG;
+    SARAS_CUDA_TRY(cudaEventSynchronize(c.userEv[b]));
+    float f = 0;
+    SARAS_CUDA_TRY(cudaEventElapsedTime(&f, c.userEv[a], c.userEv[b]));
+    *ms = f;
+    return SARAS_OK;
+}
 
 }  // extern "C"

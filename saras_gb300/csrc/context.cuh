@@ -109,6 +109,7 @@ struct Ctx {
     int histCount = 0;
     // profiling
     ProfSlot prof[PK_COUNT];
+    cudaEvent_t userEv[16] = {nullptr};
     std::string err;
 };
 

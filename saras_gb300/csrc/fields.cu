@@ -411,6 +411,7 @@ __global__ void k_final_reduce(const double *part, int n, int op, double *out) {
 
 // ------------------------------------------------------------------ host side
 static void add_op(BcProgram &pg, int kind, const int lo[3], const int hi[3], const int sh[3], double cst) {
+    if (pg.nops >= kMaxBcOps) return;   // at most 4 faces + 4 edges + 6 walls are ever added
     BcOp &o = pg.op[pg.nops++];
     o.kind = kind; o.c = cst;
     for (int d = 0; d < 3; ++d) { o.lo[d] = lo[d]; o.hi[d] = hi[d]; o.shift[d] = sh[d]; }
@@ -582,7 +583,7 @@ int fields_setup(Ctx &c) {
         SARAS_CUDA_TRY(cudaMalloc(&c.scratch[q], bytes));
         SARAS_CUDA_TRY(cudaMemsetAsync(c.scratch[q], 0, bytes, c.stream));
     }
-    c.redCap = 4096;
+    c.redCap = 1 << 16;
     SARAS_CUDA_TRY(cudaMalloc(&c.red, sizeof(double) * c.redCap * 3));
     SARAS_CUDA_TRY(cudaMalloc(&c.dscal, sizeof(double) * 64));
     SARAS_CUDA_TRY(cudaMalloc(&c.dflag, sizeof(int) * 16));
@@ -836,6 +837,12 @@ int cn_solve(Ctx &c, int comp, int *iters, double *maxerr) {
         SARAS_CUDA_TRY(cudaMemcpyAsync(c.hscal, c.dscal, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
         SARAS_CUDA_TRY(cudaStreamSynchronize(c.stream));
         res = c.hscal[0];
+        if (!std::isfinite(res)) {
+            c.err = "Jacobi residual is not finite";
+            if (iters) *iters = sweeps;
+            if (maxerr) *maxerr = res;
+            return SARAS_NOT_FINITE;
+        }
         if (res < c.p.cnTolerance) break;      // V_sweeps (the current field) is the answer
         failed += 1;
         if (failed > c.maxIterations) {

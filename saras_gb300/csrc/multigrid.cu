@@ -37,6 +37,28 @@ __global__ void k_maxabs(const double *a, long n, double *out) {
     block_max_to(m, out);
 }
 
+// Deterministic sums in the oracle's chunked order: thread t sums elements
+// [t*4096, (t+1)*4096) in index order; one thread then sums the chunk sums in
+// chunk order.  mode 0: a[t] over a flat array; mode 1/2: |Lap(p)-r|^2 / r^2
+// over the level-0 core (computeError norm 2).
+constexpr long kChunk = 4096;
+__global__ void k_seq_sum(const double *part, long n, double *out) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        double s = 0.0;
+        for (long t = 0; t < n; ++t) s += part[t];
+        *out = s;
+    }
+}
+__global__ void k_chunk_sum_flat(const double *a, long n, double *part) {
+    long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    long c0 = c * kChunk;
+    if (c0 >= n) return;
+    long c1 = min(n, c0 + kChunk);
+    double s = 0.0;
+    for (long t = c0; t < c1; ++t) s += a[t];
+    part[c] = s;
+}
+
 struct MgBC {
     int per[3];         // periodic axes
     int E[3];           // core upper index (xEnd) at this level
@@ -463,6 +485,26 @@ __global__ void k_mg_output(View3<double> dst, View3<const double> p, MgBC bc, c
 
 // computeError (poisson_d3.cc:391-459) at level 0: max over the core of
 // |Lap(p) - r| (norm 1) or the per-block sums of squares (norm 2).
+__global__ void k_mg_error_sq(View3<const double> p, View3<const double> r, MgK kk, MgBC bc, double *partNum, double *partDen) {
+    int E1 = bc.E[1], E2 = bc.E[2];
+    long n = (long)(bc.E[0] + 1) * (E1 + 1) * (E2 + 1);
+    long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    long c0 = c * kChunk;
+    if (c0 >= n) return;
+    long c1 = min(n, c0 + kChunk);
+    double sn = 0.0, sd = 0.0;
+    for (long t = c0; t < c1; ++t) {
+        int k = (int)(t % (E2 + 1)), j = (int)((t / (E2 + 1)) % (E1 + 1)), i = (int)(t / ((long)(E2 + 1) * (E1 + 1)));
+        double lap = mg_lap<double>(p(i + 1, j, k), p(i - 1, j, k), p(i, j + 1, k), p(i, j - 1, k), p(i, j, k + 1), p(i, j, k - 1),
+                                    p(i, j, k), kk);
+        double v = fabs(lap - r(i, j, k));
+        sn += v * v;
+        sd += r(i, j, k) * r(i, j, k);
+    }
+    partNum[c] = sn;
+    partDen[c] = sd;
+}
+
 __global__ void k_mg_error(View3<const double> p, View3<const double> r, MgK kk, MgBC bc, int norm, double *maxv,
                            double *partNum, double *partDen) {
     __shared__ double s1[32], s2[32];
@@ -781,13 +823,18 @@ int mg_compute_error(Ctx &c, int norm, double *err) {
         k_maxabs<<<grid_blocks(L.count), 256, 0, c.stream>>>(L.r, L.count, c.dscal + 21);
         count_launch(c);
     }
-    k_mg_error<<<nb, 256, 0, c.stream>>>(lcview<double>(L, L.pa()), lcview<double>(L, L.r), kk, bc, norm, c.dscal + 22, c.red,
-                                         c.red + c.redCap);
-    count_launch(c);
-    if (norm == 2) {
-        k_final_reduce<<<1, 256, 0, c.stream>>>(c.red, nb, 0, c.dscal + 24);
-        k_final_reduce<<<1, 256, 0, c.stream>>>(c.red + c.redCap, nb, 0, c.dscal + 25);
-        count_launch(c, 2);
+    if (norm == 1) {
+        k_mg_error<<<nb, 256, 0, c.stream>>>(lcview<double>(L, L.pa()), lcview<double>(L, L.r), kk, bc, norm, c.dscal + 22, c.red,
+                                             c.red + c.redCap);
+        count_launch(c);
+    } else {
+        long nch = (n + kChunk - 1) / kChunk;
+        if (nch > c.redCap) { c.err = "reduction buffer too small"; return SARAS_TOO_LARGE; }
+        k_mg_error_sq<<<(int)((nch + 127) / 128), 128, 0, c.stream>>>(lcview<double>(L, L.pa()), lcview<double>(L, L.r), kk, bc,
+                                                                      c.red, c.red + c.redCap);
+        k_seq_sum<<<1, 32, 0, c.stream>>>(c.red, nch, c.dscal + 24);
+        k_seq_sum<<<1, 32, 0, c.stream>>>(c.red + c.redCap, nch, c.dscal + 25);
+        count_launch(c, 3);
     }
     int s = chk(c, "computeError");
     if (s) return s;
@@ -817,9 +864,12 @@ static int mg_solve_reference(Ctx &c, int *cycles, double *residual) {
     k_mg_load<<<nb, 256, 0, c.stream>>>(lview<double>(L0, L0.r), rhs, bc0, c.red);
     count_launch(c);
     if (!c.p.testPoisson) {
-        k_final_reduce<<<1, 256, 0, c.stream>>>(c.red, nb, 0, c.dscal + 20);
+        long nch = (L0.count + kChunk - 1) / kChunk;
+        if (nch > c.redCap) { c.err = "reduction buffer too small"; return SARAS_TOO_LARGE; }
+        k_chunk_sum_flat<<<(int)((nch + 127) / 128), 128, 0, c.stream>>>(L0.r, L0.count, c.red);
+        k_seq_sum<<<1, 32, 0, c.stream>>>(c.red, nch, c.dscal + 20);
         k_mg_sub_mean<<<grid_blocks(L0.count), 256, 0, c.stream>>>(L0.r, L0.count, c.dscal + 20, (double)L0.count, c.dscal + 27);
-        count_launch(c, 2);
+        count_launch(c, 3);
     }
     // pressureData(0)(core) = Pp(core) (+ face ghosts)
     L0.cur = 0;

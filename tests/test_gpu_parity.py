@@ -111,24 +111,31 @@ def test_cn_solve(kind):
 
 @pytest.mark.parametrize("kind", ["ldc", "tgv", "rbc"])
 def test_multigrid_level_operators(kind):
-    """smooth / residual+restriction / coarsest GS / prolongation+add / computeError."""
+    """smooth / residual+restriction / coarsest GS / prolongation+add / computeError,
+    fed level by level the way vCycle feeds them (poisson.cc:219-280).  Level
+    data is set right before use: the reference's Jacobi swap exchanges the
+    arrays of every level at once (poisson_d3.cc:168), so data parked on other
+    levels does not survive a smoothing call."""
     p, g, o = pair(kind, depth=2)
     rng = np.random.default_rng(3)
-    for lvl in range(p.vcDepth + 1):
-        for which in (0, 1):
-            a = rng.standard_normal(g.level_dims(lvl))
-            g.set_level(lvl, which, a); o.set_level(lvl, which, a)
+
+    def put(lvl, which, a):
+        g.set_level(lvl, which, a); o.set_level(lvl, which, a)
 
     def core(a):
         return a[1:-1, 1:-1, 1:-1]
+    put(0, 0, rng.standard_normal(g.level_dims(0)))
+    put(0, 1, rng.standard_normal(g.level_dims(0)))
     g.mg_smooth(0, 3); o.mg_smooth(0, 3)
     assert np.array_equal(core(g.get_level(0, 0)), core(o.get_level(0, 0)))
     g.mg_restrict(0); o.mg_restrict(0)
     assert np.array_equal(core(g.get_level(1, 1)), core(o.get_level(1, 1)))
+    put(1, 0, 0.1 * rng.standard_normal(g.level_dims(1)))
     g.mg_smooth(1, 2); o.mg_smooth(1, 2)
     assert np.array_equal(core(g.get_level(1, 0)), core(o.get_level(1, 0)))
     g.mg_restrict(1); o.mg_restrict(1)
     assert np.array_equal(core(g.get_level(2, 1)), core(o.get_level(2, 1)))
+    put(2, 0, np.zeros(g.level_dims(2)))
     g.mg_smooth(2, -1); o.mg_smooth(2, -1)       # coarsest Gauss-Seidel solve
     assert_close(core(g.get_level(2, 0)), core(o.get_level(2, 0)), "coarsest solve", 0.0)
     g.mg_prolong_add(1); o.mg_prolong_add(1)
@@ -137,7 +144,7 @@ def test_multigrid_level_operators(kind):
     assert np.array_equal(core(g.get_level(0, 0)), core(o.get_level(0, 0)))
     for norm in (1, 2):
         eg, eo = g.mg_compute_error(norm), o.mg_compute_error(norm)
-        assert abs(eg - eo) <= 1e-12 * max(abs(eo), 1e-300), (norm, eg, eo)
+        assert eg == eo, (norm, eg, eo)
 
 
 @pytest.mark.parametrize("kind", ["ldc", "tgv", "rbc"])
@@ -162,13 +169,14 @@ def test_time_advance(kind, steps):
     """hydro_d3 / scalar_d3 timeAdvance: equal iteration counts every step and
     V, P (and T) within 1e-10 after the run."""
     p, g, o = pair(kind)
+    fields = [F.FIELD_VX, F.FIELD_VY, F.FIELD_VZ, F.FIELD_P, F.FIELD_PP] + ([F.FIELD_T] if kind == "rbc" else [])
     for step in range(steps):
         sg, stg = g.time_advance()
         so, sto = o.time_advance()
         assert sg == so == 0
-        assert list(stg.cn_iters) == list(sto.cn_iters), step
-        assert stg.vcycles == sto.vcycles, step
-    fields = [F.FIELD_VX, F.FIELD_VY, F.FIELD_VZ, F.FIELD_P, F.FIELD_PP] + ([F.FIELD_T] if kind == "rbc" else [])
+        errs = {F.FIELD_NAMES[f]: C.rel_err(g.get(f), o.get(f)) for f in fields}
+        assert list(stg.cn_iters) == list(sto.cn_iters), (step, errs)
+        assert stg.vcycles == sto.vcycles, (step, stg.vcycles, sto.vcycles, errs)
     for f in fields:
         assert_close(g.get(f), o.get(f), F.FIELD_NAMES[f])
     _, eg, dg, ng = g.diagnostics()
