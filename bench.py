@@ -54,6 +54,7 @@ def tgv_params(mode, guess=0, ind=GRID_INDEX, depth=DEPTH):
     p.mgMaxCycles = 100
     p.mixedCycles = 1
     p.jacobiWeight = 6.0 / 7.0 if mode != _abi.MG_REFERENCE else 1.0
+    p.fastKernels = 1 if mode != _abi.MG_REFERENCE else 0
     p.guessMode = guess
     return p
 

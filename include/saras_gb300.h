@@ -107,6 +107,9 @@ typedef struct saras_params {
     int guessMode;            /* enum saras_guess                               */
     double jacobiWeight;      /* damping of the Jacobi smoother (1.0 = reference) */
     int seed;
+    int fastKernels;          /* 1: fused multiply-add / reciprocal forms of the CN and
+                                 RHS kernels (not bit-identical to the reference);
+                                 0: reference arithmetic (the drop-in)          */
 } saras_params;
 
 typedef struct saras_step_stats {

@@ -57,6 +57,7 @@ class saras_params(ctypes.Structure):
         ("mgMaxCycles", _I), ("mixedCycles", _I), ("guessMode", _I),
         ("jacobiWeight", _D),
         ("seed", _I),
+        ("fastKernels", _I),
     ]
 
     def to_dict(self):
@@ -96,6 +97,7 @@ def default_params():
     p.testPoisson, p.mgMode = 0, MG_REFERENCE
     p.mgTarget, p.mgMaxCycles, p.mixedCycles, p.guessMode = 1.0e-8, 200, 1, GUESS_PREVIOUS
     p.jacobiWeight, p.seed = 1.0, 42
+    p.fastKernels = 0
     return p
 
 

@@ -185,7 +185,8 @@ int saras_parse_yaml(const char *path, saras_params *p, char *err, int errlen) {
                  {"Multigrid/Smoothing Method", &p->gsSmooth}, {"Multigrid/Pre-Smoothing Count", &p->preSmooth},
                  {"Multigrid/Post-Smoothing Count", &p->postSmooth}, {"Multigrid/Residual Type", &p->resType},
                  {"GB300/Multigrid Mode", &p->mgMode}, {"GB300/Max V-Cycles", &p->mgMaxCycles},
-                 {"GB300/Mixed Inner Cycles", &p->mixedCycles}, {"GB300/Guess Mode", &p->guessMode}, {"GB300/Seed", &p->seed}};
+                 {"GB300/Mixed Inner Cycles", &p->mixedCycles}, {"GB300/Guess Mode", &p->guessMode}, {"GB300/Seed", &p->seed},
+                 {"GB300/Fast Kernels", &p->fastKernels}};
     DK dbls[] = {{"Program/Reynolds Number", &p->Re}, {"Program/Rossby Number", &p->Ro}, {"Program/Rayleigh Number", &p->Ra},
                  {"Program/Prandtl Number", &p->Pr}, {"Program/Taylor Number", &p->Ta}, {"Program/X Length", &p->Lx},
                  {"Program/Y Length", &p->Ly}, {"Program/Z Length", &p->Lz}, {"Program/Plate Radius", &p->patchRadius},

@@ -252,6 +252,50 @@ __global__ void k_rhs(RhsArgs a) {
     a.H(i, j, k) = h;
 }
 
+// Fast form (fastKernels = 1) of the same right-hand side: constants folded,
+// fused multiply-adds; not bit-identical to the reference order.
+struct RhsFast {
+    double K2[3];     // visc * m2h * ih2 (second derivatives)
+    double K1[3];     // 0.5 * ih * m1 (first derivatives)
+    double G[3];      // gm * ih (gradient)
+    double Fb2;       // Fb / 2
+    double dt;
+};
+template <int C>
+__global__ void __launch_bounds__(256) k_rhs_fast(RhsArgs a, RhsFast q) {
+    int i, j, k;
+    if (!box_point(a.b, i, j, k)) return;
+    const View3<const double> &F = a.F;
+    double f0 = F(i, j, k);
+    double sx = fma(-2.0, f0, F(i - 1, j, k) + F(i + 1, j, k));
+    double sy = fma(-2.0, f0, F(i, j - 1, k) + F(i, j + 1, k));
+    double sz = fma(-2.0, f0, F(i, j, k - 1) + F(i, j, k + 1));
+    double h = fma(q.K2[0], sx, fma(q.K2[1], sy, q.K2[2] * sz));
+    double dx = (F(i + 1, j, k) - F(i - 1, j, k)) * q.K1[0];
+    double dy = (F(i, j + 1, k) - F(i, j - 1, k)) * q.K1[1];
+    double dz = (F(i, j, k + 1) - F(i, j, k - 1)) * q.K1[2];
+    h = fma(-interp<C, 0>(a.V.v[0], i, j, k), dx * (1.0 / Slices<C, 0>::n), h);
+    h = fma(-interp<C, 1>(a.V.v[1], i, j, k), dy * (1.0 / Slices<C, 1>::n), h);
+    h = fma(-interp<C, 2>(a.V.v[2], i, j, k), dz * (1.0 / Slices<C, 2>::n), h);
+    if (C == 2 && a.buoyancy) h = fma(q.Fb2, a.T(i, j, k) + a.T(i, j, k + 1), h);
+    double sp = C == 0 ? a.P(i + 1, j, k) : C == 1 ? a.P(i, j + 1, k) : a.P(i, j, k + 1);
+    h = fma(-q.G[C], sp - a.P(i, j, k), h);
+    a.H(i, j, k) = fma(h, q.dt, f0);
+}
+
+static RhsFast make_rhs_fast(const Ctx &c, double visc) {
+    RhsFast q;
+    for (int d = 0; d < 3; ++d) {
+        double m2h = (c.p.iScheme == 1) ? 0.5 * c.m2[d] : c.m2[d];
+        q.K2[d] = visc * m2h * c.ih2[d];
+        q.K1[d] = 0.5 * c.ih[d] * c.m1[d];
+        q.G[d] = c.m1[d] * c.ih[d];
+    }
+    q.Fb2 = 0.5 * c.Fb;
+    q.dt = c.dt;
+    return q;
+}
+
 // scalar_d3::timeAdvance lines 344-355: tmpRHS for T (vertex field).
 __global__ void k_trhs(RhsArgs a) {
     int i, j, k;
@@ -330,6 +374,51 @@ __global__ void k_cn(CnArgs a) {
         } else {
             a.out(i, j, k) = bc_resolve(a.prog, i, j, k, [&](int x, int y, int z) -> double {
                 return in_box(a.prog.blo, a.prog.bhi, x, y, z) ? cn_guess(a, x, y, z) : 0.0;
+            });
+        }
+    }
+    if (a.withResidual) block_max_to(res, a.resMax);
+}
+
+// Fast form of the same Jacobi iteration (fastKernels = 1): the two divisions
+// become multiplications by precomputed reciprocals and the sums are fused
+// multiply-adds.  Same fixed point and stopping rule, not bit-identical.
+struct CnFast {
+    View3<double> out;
+    View3<const double> in, rhs;
+    BcProgram prog;
+    Box full;
+    double c1, c2, c3, k1, invDn;   // guess = fma(A, k1, rhs) * invDn
+    double lx, ly, lz, lc, k2;      // residual value = C - k2 * Lap(C)
+    int withResidual;
+    double *resMax;
+};
+
+__device__ __forceinline__ double cn_guess_fast(const CnFast &a, int i, int j, int k) {
+    const View3<const double> &V = a.in;
+    double A = fma(a.c1, V(i + 1, j, k) + V(i - 1, j, k), fma(a.c2, V(i, j + 1, k) + V(i, j - 1, k), a.c3 * (V(i, j, k + 1) + V(i, j, k - 1))));
+    return fma(A, a.k1, a.rhs(i, j, k)) * a.invDn;
+}
+
+__global__ void __launch_bounds__(256) k_cn_fast(CnFast a) {
+    int i, j, k;
+    bool ok = box_point(a.full, i, j, k);
+    double res = 0.0;
+    if (ok) {
+        if (in_box(a.prog.blo, a.prog.bhi, i, j, k)) {
+            const View3<const double> &V = a.in;
+            double C = V(i, j, k);
+            double ew = V(i + 1, j, k) + V(i - 1, j, k), ns = V(i, j + 1, k) + V(i, j - 1, k), ud = V(i, j, k + 1) + V(i, j, k - 1);
+            if (a.withResidual) {
+                double L = fma(a.lx, ew, fma(a.ly, ns, fma(a.lz, ud, a.lc * C)));
+                res = fabs(fma(-a.k2, L, C) - a.rhs(i, j, k));
+                if (res != res) res = INFINITY;
+            }
+            double A = fma(a.c1, ew, fma(a.c2, ns, a.c3 * ud));
+            a.out(i, j, k) = fma(A, a.k1, a.rhs(i, j, k)) * a.invDn;
+        } else {
+            a.out(i, j, k) = bc_resolve(a.prog, i, j, k, [&](int x, int y, int z) -> double {
+                return in_box(a.prog.blo, a.prog.bhi, x, y, z) ? cn_guess_fast(a, x, y, z) : 0.0;
             });
         }
     }
@@ -741,14 +830,22 @@ int compute_rhs(Ctx &c) {
     a.buoyancy = (c.scalar && c.p.forceType == 3) ? 1 : 0;
     double bytes = 0;
     prof_begin(c, PK_RHS, 0);
+    RhsFast qf = make_rhs_fast(c, a.visc);
+    bool fast = c.p.fastKernels != 0;
     for (int q = 0; q < 3; ++q) {
         a.H = mview(c, SARAS_FIELD_NSE_X + q);
         a.F = cview(c, SARAS_FIELD_VX + q);
         a.b = core_box(c.info[SARAS_FIELD_VX + q]);
         dim3 g, bl; box_launch_dims(a.b, g, bl);
-        if (q == 0) k_rhs<0><<<g, bl, 0, c.stream>>>(a);
-        if (q == 1) k_rhs<1><<<g, bl, 0, c.stream>>>(a);
-        if (q == 2) k_rhs<2><<<g, bl, 0, c.stream>>>(a);
+        if (fast) {
+            if (q == 0) k_rhs_fast<0><<<g, bl, 0, c.stream>>>(a, qf);
+            if (q == 1) k_rhs_fast<1><<<g, bl, 0, c.stream>>>(a, qf);
+            if (q == 2) k_rhs_fast<2><<<g, bl, 0, c.stream>>>(a, qf);
+        } else {
+            if (q == 0) k_rhs<0><<<g, bl, 0, c.stream>>>(a);
+            if (q == 1) k_rhs<1><<<g, bl, 0, c.stream>>>(a);
+            if (q == 2) k_rhs<2><<<g, bl, 0, c.stream>>>(a);
+        }
         count_launch(c);
         bytes += 8.0 * (double)a.H.size();
     }
@@ -812,24 +909,43 @@ int cn_solve(Ctx &c, int comp, int *iters, double *maxerr) {
     dim3 g, bl; box_launch_dims(a.full, g, bl);
     int slot = scratch_slot(field);
     double bytes = 3.0 * 8.0 * (double)make_view<double>(nullptr, f.n[0], f.n[1], f.n[2]).size();
+    CnFast fa;
+    bool fast = c.p.fastKernels != 0;
+    if (fast) {
+        fa.rhs = a.rhs; fa.prog = a.prog; fa.full = a.full;
+        fa.c1 = a.c1; fa.c2 = a.c2; fa.c3 = a.c3;
+        fa.k1 = a.scalarForm ? (a.dt * a.coef) / a.X : a.dt / a.X;
+        fa.invDn = 1.0 / a.Dn;
+        fa.lx = a.lx; fa.ly = a.ly; fa.lz = a.lz;
+        fa.lc = -2.0 * (a.lx + a.ly + a.lz);
+        fa.k2 = 0.5 * a.dt * a.resCoef;
+        fa.resMax = a.resMax;
+    }
+    auto launch = [&](int withRes) {
+        if (fast) {
+            fa.in = cview(c, field);
+            fa.out = mview_ptr(c, field, c.scratch[slot]);
+            fa.withResidual = withRes;
+            k_cn_fast<<<g, bl, 0, c.stream>>>(fa);
+        } else {
+            a.in = cview(c, field);
+            a.out = mview_ptr(c, field, c.scratch[slot]);
+            a.withResidual = withRes;
+            k_cn<<<g, bl, 0, c.stream>>>(a);
+        }
+    };
     // first sweep (no residual check precedes it)
-    a.in = cview(c, field);
-    a.out = mview_ptr(c, field, c.scratch[slot]);
-    a.withResidual = 0;
     prof_begin(c, PK_CN, 0);
-    k_cn<<<g, bl, 0, c.stream>>>(a);
+    launch(0);
     count_launch(c);
     prof_end(c, PK_CN, 0, bytes);
     std::swap(c.f[field], c.scratch[slot]);
     int sweeps = 1, failed = 0;
     double res = 0;
     while (true) {
-        a.in = cview(c, field);
-        a.out = mview_ptr(c, field, c.scratch[slot]);
-        a.withResidual = 1;
         SARAS_CUDA_TRY(cudaMemsetAsync(c.dscal, 0, sizeof(double), c.stream));
         prof_begin(c, PK_CN, 0);
-        k_cn<<<g, bl, 0, c.stream>>>(a);
+        launch(1);
         count_launch(c);
         prof_end(c, PK_CN, 0, bytes);
         int s = check_launch(c, "cn");

@@ -532,6 +532,96 @@ __global__ void k_mg_error(View3<const double> p, View3<const double> r, MgK kk,
     }
 }
 
+// ---- target-mode level kernels
+// Folded constants of the damped Jacobi update and of the Laplacian:
+//   v   = om1*C + ax*(E+W) + ay*(N+S) + az*(U+D) + ar*r
+//   lap = lx*(E+W) + ly*(N+S) + lz*(U+D) + lc*C
+// evaluated with fused multiply-adds; 32-bit offsets (the largest padded level
+// array, 515^3 points, is far below 2^31).
+template <typename T>
+struct TgK {
+    T ax, ay, az, ar, om1;
+    T lx, ly, lz, lc;
+};
+
+template <typename T>
+static TgK<T> make_tgk(const Level &L, double omega) {
+    TgK<T> k;
+    k.ax = (T)(omega * 2.0 * L.cx / L.den);
+    k.ay = (T)(omega * 2.0 * L.cy / L.den);
+    k.az = (T)(omega * 2.0 * L.cz / L.den);
+    k.ar = (T)(-omega * L.c7 / L.den);
+    k.om1 = (T)(1.0 - omega);
+    k.lx = (T)L.lx; k.ly = (T)L.ly; k.lz = (T)L.lz;
+    k.lc = (T)(-2.0 * (L.lx + L.ly + L.lz));
+    return k;
+}
+
+__device__ __forceinline__ bool near_face(int i, int j, int k, const MgBC &bc) {
+    return i <= 1 || j <= 1 || k <= 1 || i >= bc.E[0] - 1 || j >= bc.E[1] - 1 || k >= bc.E[2] - 1;
+}
+
+template <typename T>
+__device__ __noinline__ void scatter_slow(T *P, int sx, int sy, int i, int j, int k, T v, const MgBC &bc) {
+    View3<T> V; V.p = P; V.sx = sx; V.sy = sy;
+    put_scatter(V, i, j, k, v, bc);
+}
+
+template <typename T, bool ZERO>
+__global__ void __launch_bounds__(256) k_tgt_sweep(T *__restrict__ out, const T *__restrict__ in, const T *__restrict__ r,
+                                                   int sx, int sy, MgBC bc, TgK<T> c) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y * blockDim.y + threadIdx.y;
+    int i = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i > bc.E[0] || j > bc.E[1] || k > bc.E[2]) return;
+    int o = (i + 1) * sx + (j + 1) * sy + (k + 1);
+    T v;
+    if (ZERO) {
+        v = c.ar * r[o];
+    } else {
+        T C = in[o];
+        T ew = in[o + sx] + in[o - sx], ns = in[o + sy] + in[o - sy], ud = in[o + 1] + in[o - 1];
+        v = fma(c.ax, ew, fma(c.ay, ns, fma(c.az, ud, fma(c.ar, r[o], c.om1 * C))));
+    }
+    out[o] = v;
+    if (near_face(i, j, k, bc)) scatter_slow(out, sx, sy, i, j, k, v, bc);
+}
+
+// r_out = b - Lap(p) over the core; optional max |r| (FP64 accumulation).
+template <typename T, typename OT, bool MAXRED>
+__global__ void __launch_bounds__(256) k_tgt_residual(OT *__restrict__ out, const T *__restrict__ p, const T *__restrict__ b,
+                                                      int sx, int sy, MgBC bc, TgK<T> c, double *maxres) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y * blockDim.y + threadIdx.y;
+    int i = blockIdx.z * blockDim.z + threadIdx.z;
+    double m = 0.0;
+    if (i <= bc.E[0] && j <= bc.E[1] && k <= bc.E[2]) {
+        int o = (i + 1) * sx + (j + 1) * sy + (k + 1);
+        T C = p[o];
+        T ew = p[o + sx] + p[o - sx], ns = p[o + sy] + p[o - sy], ud = p[o + 1] + p[o - 1];
+        T lap = fma(c.lx, ew, fma(c.ly, ns, fma(c.lz, ud, c.lc * C)));
+        T res = b[o] - lap;
+        if (out) out[o] = (OT)res;
+        if (MAXRED) {
+            m = fabs((double)res);
+            if (m != m) m = INFINITY;
+        }
+    }
+    if (MAXRED) block_max_to(m, maxres);
+}
+
+// p64 += e32 over the core (FP64 correction accumulation) with face ghosts.
+__global__ void __launch_bounds__(256) k_tgt_update(double *__restrict__ p, const float *__restrict__ e, int sx, int sy, MgBC bc) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y * blockDim.y + threadIdx.y;
+    int i = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i > bc.E[0] || j > bc.E[1] || k > bc.E[2]) return;
+    int o = (i + 1) * sx + (j + 1) * sy + (k + 1);
+    double v = p[o] + (double)e[o];
+    p[o] = v;
+    if (near_face(i, j, k, bc)) scatter_slow(p, sx, sy, i, j, k, v, bc);
+}
+
 // ---- target modes (FP64 / mixed)
 // Trapezoidal-weight partial sums of the core of rhs.
 __global__ void k_trap_sum(View3<const double> rhs, MgBC bc, double *part) {
@@ -561,28 +651,6 @@ __global__ void k_tgt_rhs(View3<double> b, View3<const double> rhs, MgBC bc, con
         m = fabs(v);
     }
     block_max_to(m, maxabs);
-}
-
-// Fused refinement step: p <- p + e (if e given), then r = b - Lap(p) over the
-// core in FP64; the updated p gets its face ghosts, r is stored in FP32 (mixed
-// mode) or FP64 (plain target mode); block max |r|.
-template <bool HAS_E, typename RT>
-__global__ void k_refine(View3<double> pout, View3<const double> pin, View3<const float> e, View3<const double> b, View3<RT> r,
-                         MgK kk, MgBC bc, double *maxres) {
-    int i, j, k;
-    bool ok = core_pt(bc.E, i, j, k);
-    double m = 0;
-    if (ok) {
-        auto P = [&](int a, int bb, int c) -> double { return HAS_E ? pin(a, bb, c) + (double)e(a, bb, c) : pin(a, bb, c); };
-        double C = P(i, j, k);
-        double lap = mg_lap<double>(P(i + 1, j, k), P(i - 1, j, k), P(i, j + 1, k), P(i, j - 1, k), P(i, j, k + 1), P(i, j, k - 1), C, kk);
-        double res = b(i, j, k) - lap;
-        if (HAS_E) put_scatter(pout, i, j, k, C, bc);
-        r(i, j, k) = (RT)res;
-        m = fabs(res);
-        if (m != m) m = INFINITY;
-    }
-    block_max_to(m, maxres);
 }
 
 // ------------------------------------------------------------------ host
@@ -721,9 +789,14 @@ static int smooth(Ctx &c, int l, int count, bool zero_first, bool tgt) {
     T omega = tgt ? (T)c.p.jacobiWeight : (T)1.0;
     int pk = sizeof(T) == 8 ? PK_MG_SMOOTH64 : PK_MG_SMOOTH32;
     double bytes = 3.0 * sizeof(T) * (double)(L.n[0] + 1) * (L.n[1] + 1) * (L.n[2] + 1);
+    TgK<T> tk = make_tgk<T>(L, c.p.jacobiWeight);
+    int sx = (L.n[1] + 3) * (L.n[2] + 3), sy = L.n[2] + 3;
     for (int n = 0; n < count; ++n) {
         prof_begin(c, pk, l);
-        if (n == 0 && zero_first)
+        if (tgt) {
+            if (n == 0 && zero_first) k_tgt_sweep<T, true><<<g, b, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
+            else k_tgt_sweep<T, false><<<g, b, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
+        } else if (n == 0 && zero_first)
             k_mg_sweep<T, true><<<g, b, 0, c.stream>>>(lview<T>(L, B_<T>(L)), lcview<T>(L, A_<T>(L)), lcview<T>(L, R_<T>(L)), kk, bc, omega);
         else
             k_mg_sweep<T, false><<<g, b, 0, c.stream>>>(lview<T>(L, B_<T>(L)), lcview<T>(L, A_<T>(L)), lcview<T>(L, R_<T>(L)), kk, bc, omega);
@@ -757,7 +830,11 @@ static int restrict_level(Ctx &c, int l, bool tgt) {
     int pk = sizeof(T) == 8 ? PK_MG_RESID64 : PK_MG_RESID32;
     double pts = (double)(L.n[0] + 1) * (L.n[1] + 1) * (L.n[2] + 1);
     prof_begin(c, pk, l);
-    k_mg_residual<T><<<g, b, 0, c.stream>>>(lview<T>(L, B_<T>(L)), lcview<T>(L, A_<T>(L)), lcview<T>(L, R_<T>(L)), kk, bcf);
+    if (tgt) {
+        int sx = (L.n[1] + 3) * (L.n[2] + 3), sy = L.n[2] + 3;
+        k_tgt_residual<T, T, false><<<g, b, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bcf, make_tgk<T>(L, 1.0), nullptr);
+    } else
+        k_mg_residual<T><<<g, b, 0, c.stream>>>(lview<T>(L, B_<T>(L)), lcview<T>(L, A_<T>(L)), lcview<T>(L, R_<T>(L)), kk, bcf);
     count_launch(c);
     prof_end(c, pk, l, 3.0 * sizeof(T) * pts);
     dim3 g2, b2; core_dims(C, g2, b2);
@@ -918,7 +995,6 @@ static int mg_solve_target(Ctx &c, int *cycles, double *residual, saras_step_sta
     int s;
     Level &L0 = c.lv[0];
     MgBC bc0 = level_bc(c, 0, true);
-    MgK k0 = make_k(L0);
     dim3 g, b; core_dims(L0, g, b);
     long ncore = (long)(L0.n[0] + 1) * (L0.n[1] + 1) * (L0.n[2] + 1);
     int nb = std::min(grid_blocks(ncore), c.redCap);
@@ -937,30 +1013,25 @@ static int mg_solve_target(Ctx &c, int *cycles, double *residual, saras_step_sta
     if ((s = read_scalars(c, 31, 1))) return s;
     double bmax = c.hscal[31];
     double target = c.mgTarget * bmax;
+    int sx0 = (L0.n[1] + 3) * (L0.n[2] + 3), sy0 = L0.n[2] + 3;
+    TgK<double> t0 = make_tgk<double>(L0, 1.0);
     auto fine_res = [&](bool withE, double *out) -> int {
         SARAS_CUDA_TRY(cudaMemsetAsync(c.dscal + 32, 0, sizeof(double), c.stream));
-        prof_begin(c, PK_REFINE_RESID, 0);
         if (withE) {
-            k_refine<true, float><<<g, b, 0, c.stream>>>(lview<double>(L0, L0.pb()), lcview<double>(L0, L0.pa()),
-                                                        lcview<float>(L0, L0.pa32()), lcview<double>(L0, L0.r),
-                                                        lview<float>(L0, L0.r32), k0, bc0, c.dscal + 32);
+            prof_begin(c, PK_REFINE_UPDATE, 0);
+            k_tgt_update<<<g, b, 0, c.stream>>>(L0.pa(), L0.pa32(), sx0, sy0, bc0);
             count_launch(c);
-            prof_end(c, PK_REFINE_RESID, 0, (8.0 + 4.0 + 8.0 + 8.0 + 4.0) * (double)ncore);
-            L0.cur ^= 1;
-        } else if (c.mgMode == SARAS_MG_MIXED) {
-            k_refine<false, float><<<g, b, 0, c.stream>>>(lview<double>(L0, L0.pb()), lcview<double>(L0, L0.pa()),
-                                                         lcview<float>(L0, L0.pa32()), lcview<double>(L0, L0.r),
-                                                         lview<float>(L0, L0.r32), k0, bc0, c.dscal + 32);
-            count_launch(c);
+            prof_end(c, PK_REFINE_UPDATE, 0, (8.0 + 4.0 + 8.0) * (double)ncore);
+        }
+        prof_begin(c, PK_REFINE_RESID, 0);
+        if (c.mgMode == SARAS_MG_MIXED) {
+            k_tgt_residual<double, float, true><<<g, b, 0, c.stream>>>(L0.r32, L0.pa(), L0.r, sx0, sy0, bc0, t0, c.dscal + 32);
             prof_end(c, PK_REFINE_RESID, 0, (8.0 + 8.0 + 4.0) * (double)ncore);
         } else {
-            // plain target: residual only, into the scratch ping-pong buffer
-            k_refine<false, double><<<g, b, 0, c.stream>>>(lview<double>(L0, L0.pb()), lcview<double>(L0, L0.pa()),
-                                                          lcview<float>(L0, L0.pa32()), lcview<double>(L0, L0.r),
-                                                          lview<double>(L0, L0.pb()), k0, bc0, c.dscal + 32);
-            count_launch(c);
-            prof_end(c, PK_REFINE_RESID, 0, (8.0 + 8.0 + 8.0) * (double)ncore);
+            k_tgt_residual<double, double, true><<<g, b, 0, c.stream>>>(nullptr, L0.pa(), L0.r, sx0, sy0, bc0, t0, c.dscal + 32);
+            prof_end(c, PK_REFINE_RESID, 0, (8.0 + 8.0) * (double)ncore);
         }
+        count_launch(c);
         int q = chk(c, "refine");
         if (q) return q;
         q = read_scalars(c, 32, 1);

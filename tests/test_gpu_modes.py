@@ -1,0 +1,107 @@
+"""GPU checks of the GB300 extensions: the residual-target multigrid modes
+(plain FP64 and FP32-in-FP64 refinement), the fused-multiply-add kernel forms,
+and failure reporting (status codes, never a GPU fault)."""
+import math
+
+import numpy as np
+import pytest
+
+import saras_gb300 as S
+from saras_gb300 import _abi as F
+from tests import _cases as C
+
+pytestmark = pytest.mark.gpu
+
+
+def target_case(mode, fast=1, ind=5, depth=3):
+    p = C.tgv(ind=ind, depth=depth, dt=5e-4)
+    p.mgMode = mode
+    p.mgTarget = 1e-8
+    p.mgMaxCycles = 100
+    p.jacobiWeight = 6.0 / 7.0
+    p.fastKernels = fast
+    g = S.Solver(p)
+    C.initialise(g, p, "tgv")
+    return p, g
+
+
+@pytest.mark.parametrize("mode", [F.MG_PLAIN_TARGET, F.MG_MIXED])
+def test_target_modes_reach_residual(mode):
+    p, g = target_case(mode)
+    for _ in range(3):
+        s, st = g.time_advance()
+        assert s == 0
+        assert st.fine_residual <= 1e-8
+        assert 0 < st.vcycles < 100
+
+
+def test_mixed_matches_plain_fp64():
+    """Every result of the precision form states its error against the plain FP64 solve."""
+    _, a = target_case(F.MG_PLAIN_TARGET)
+    _, b = target_case(F.MG_MIXED)
+    for _ in range(4):
+        a.time_advance()
+        b.time_advance()
+    for f in (F.FIELD_VX, F.FIELD_VY, F.FIELD_VZ, F.FIELD_P):
+        assert C.rel_err(b.get(f), a.get(f)) < 1e-8, F.FIELD_NAMES[f]
+
+
+def test_fast_kernels_match_reference_arithmetic():
+    """fastKernels=1 changes rounding only: both solve the same CN and Poisson systems."""
+    _, a = target_case(F.MG_PLAIN_TARGET, fast=0)
+    _, b = target_case(F.MG_PLAIN_TARGET, fast=1)
+    for _ in range(3):
+        a.time_advance()
+        b.time_advance()
+    for f in (F.FIELD_VX, F.FIELD_VY, F.FIELD_VZ):
+        assert C.rel_err(b.get(f), a.get(f)) < 1e-8, F.FIELD_NAMES[f]
+
+
+def test_nan_input_reports_not_finite():
+    """A NaN in the velocity is reported by the Jacobi solve, not hung on."""
+    p = C.ldc(ind=3, depth=1)
+    g = S.Solver(p)
+    C.initialise(g, p, "ldc")
+    V = g.get(F.FIELD_VX)
+    V[4, 4, 4] = float("nan")
+    g.set(F.FIELD_VX, V)
+    with pytest.raises(S.SarasError) as e:
+        g.time_advance()
+    assert e.value.status == F.NOT_FINITE
+    # the context stays usable after the error
+    C.initialise(g, p, "ldc")
+    g.set(F.FIELD_VX, np.zeros(g.dims(F.FIELD_VX)))
+    g.apply_bc(F.FIELD_VX)
+    s, st = g.time_advance()
+    assert s == 0
+
+
+def test_unreachable_cn_tolerance_reports_not_converged():
+    """hydro_d3.cc:415-421 aborts after maxIterations; the C ABI returns a status instead."""
+    p = C.ldc(ind=3, depth=1)
+    p.cnTolerance = 0.0
+    g = S.Solver(p)
+    C.initialise(g, p, "ldc")
+    s, st = g.time_advance()
+    assert s == F.NOT_CONVERGED
+
+
+def test_cycle_cap_reports_not_converged():
+    p, g = target_case(F.MG_PLAIN_TARGET)
+    g.mg_set_mode(F.MG_PLAIN_TARGET, 1e-14, 1)
+    with pytest.raises(S.SarasError) as e:
+        g.time_advance()
+    assert e.value.status == F.NOT_CONVERGED
+
+
+def test_solvepde_ldc_runs_and_stays_bounded():
+    """hydro_d3::solvePDE on the LDC case: energy grows from the lid, divergence stays small."""
+    p = C.ldc(ind=4, depth=2)
+    p.tMax = 0.02
+    p.ioCnt = 5
+    solver = S.hydro_d3(p)
+    series = solver.solvePDE()
+    assert solver.timeStepCount == 20
+    assert len(series) == 4
+    assert all(0.0 < e < 1.0 for _, e, _, _ in series)
+    assert all(abs(d) < 1.0 for _, _, d, _ in series)

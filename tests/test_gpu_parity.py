@@ -142,6 +142,8 @@ def test_multigrid_level_operators(kind):
     assert np.array_equal(core(g.get_level(1, 0)), core(o.get_level(1, 0)))
     g.mg_prolong_add(0); o.mg_prolong_add(0)
     assert np.array_equal(core(g.get_level(0, 0)), core(o.get_level(0, 0)))
+    g.mg_smooth(0, 3); o.mg_smooth(0, 3)          # post-smoothing ends with imposeBC
+    assert np.array_equal(core(g.get_level(0, 0)), core(o.get_level(0, 0)))
     for norm in (1, 2):
         eg, eo = g.mg_compute_error(norm), o.mg_compute_error(norm)
         assert eg == eo, (norm, eg, eo)
