@@ -179,18 +179,31 @@ def run_ours(args, dist):
         torch.cuda.set_device(gpu)
     except Exception:
         torch = None
-    guess = F.GUESS_LEARNED if args.learned else F.GUESS_PREVIOUS
-    p = tgv_params(F.MG_MIXED, guess)
+    p = tgv_params(F.MG_MIXED, F.GUESS_PREVIOUS)
     g = S.Solver(p)
     init_tgv(g, p)
     names = S.Solver.profile_names()
-    # --- warm-up (also trains the warm-start network when enabled)
-    warm_stats = []
-    for k in range(args.warmup):
+    # --- warm-up: the solver's own steps; with the learned warm start they
+    # also yield the (input, solution) pairs the U-Net is trained on
+    warm_steps = max(args.warmup, args.collect) if args.learned else args.warmup
+    learn = None
+    if args.learned:
+        g.unet_collect()
+    warm_vc = []
+    for k in range(warm_steps):
         s, st = g.time_advance()
         if s != 0:
             raise RuntimeError("warm-up step failed: %d" % s)
-        warm_stats.append(st.vcycles)
+        warm_vc.append(st.vcycles)
+    if args.learned:
+        t0 = time.perf_counter()
+        loss = g.unet_train(args.train_iters, args.lr)
+        g.synchronize()
+        learn = {"pairs": max(0, warm_steps - 2), "train_iters": args.train_iters, "lr": args.lr,
+                 "final_loss": loss, "train_seconds": round(time.perf_counter() - t0, 3),
+                 "vcycles_per_step_warmup_previous_guess": sum(warm_vc[-5:]) / len(warm_vc[-5:])}
+        g.set_guess_mode(F.GUESS_LEARNED)
+        s, st = g.time_advance()
     # pick the dominant kernel from one profiled step
     for k in range(len(names)):
         g.profile_enable(k, True)
@@ -209,7 +222,7 @@ def run_ours(args, dist):
     g.synchronize()
     launches0 = g.launch_count()
     g.event_record(0)
-    vc, rs, fine = [], [], []
+    vc, rs, fine, src = [], [], [], []
     for k in range(args.steps):
         s, st = g.time_advance()
         if s != 0:
@@ -217,6 +230,7 @@ def run_ours(args, dist):
         vc.append(st.vcycles)
         rs.append(st.refine_steps)
         fine.append(st.fine_residual)
+        src.append(st.guess_source)
     g.event_record(1)
     g.synchronize()
     dist.barrier()
@@ -307,7 +321,10 @@ def run_ours(args, dist):
             "workload": "Taylor-Green vortex 257^3 (2^8+1 vertex points per axis), [0,2pi]^3 PPP, Re 1600, dt 5e-4; "
                         "pressure solve: FP32 V(3,3) cycles inside FP64 iterative refinement to max|b-Ap|/max|b| <= 1e-8",
             "grid": [257, 257, 257], "vcycle_depth": DEPTH, "mg_mode": "mixed_fp32_in_fp64",
-            "warm_start": "unet" if args.learned else "previous_pressure",
+            "warm_start": "unet (3-level 16/32/64, tcgen05 BF16 convs) with fallback to the previous pressure"
+                          if args.learned else "previous_pressure",
+            "learned": learn,
+            "guess_sources_timed": {"network": src.count(1), "previous": src.count(0)},
             "residual_target": TARGET, "vcycles_per_step": sum(vc) / len(vc),
             "refine_steps_per_step": sum(rs) / len(rs), "max_fine_residual": max(fine),
             "plain_fp64": plain,
@@ -384,7 +401,10 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--learned", type=int, default=0)
+    ap.add_argument("--learned", type=int, default=1)
+    ap.add_argument("--collect", type=int, default=14)
+    ap.add_argument("--train-iters", type=int, default=200)
+    ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")

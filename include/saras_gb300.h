@@ -63,7 +63,8 @@ enum saras_mg_mode {
 /* Initial guess sources for the pressure-correction solve. */
 enum saras_guess {
     SARAS_GUESS_PREVIOUS = 0, /* previous Pp (reference behaviour, poisson.cc:115) */
-    SARAS_GUESS_LEARNED = 1   /* U-Net guess with fallback to the previous Pp      */
+    SARAS_GUESS_LEARNED = 1,  /* U-Net guess with fallback to the previous Pp      */
+    SARAS_GUESS_EXTRAPOLATE = 2 /* 2 Pp(n-1) - Pp(n-2) with the same fallback (ablation) */
 };
 
 /*
@@ -211,6 +212,14 @@ int saras_unet_collect(saras_ctx *ctx);
 int saras_unet_train(saras_ctx *ctx, int iters, double lr, double *loss);
 int saras_unet_infer(saras_ctx *ctx, int field_out);
 int saras_set_guess_mode(saras_ctx *ctx, int mode);
+/* Stand-alone check of the tensor-core 3x3x3 convolution (no context needed).
+ * Channels-last BF16 activations (x: D*H*W*cin, dy: D*H*W*cout as raw bf16
+ * bits), FP32 weights w[cout][27][cin], bias[cout].  mode 0: forward,
+ * out = conv(x) (+bias, ReLU if relu), D*H*W*cout; mode 1: input gradient,
+ * out = conv^T(dy), D*H*W*cin; mode 2: weight gradient, out = dW[cout][27][cin]
+ * followed by db[cout].  Allocates its own device buffers. */
+int saras_conv3d_check(int mode, int D, int H, int W, int cin, int cout, const unsigned short *x,
+                       const unsigned short *dy, const float *w, const float *bias, int relu, float *out);
 
 /* ------------------------------------------------------ measurement */
 /* Per-kernel CUDA-event timing on the context stream.  kernel ids are listed

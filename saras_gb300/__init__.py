@@ -261,6 +261,44 @@ class Solver:
         return [lib.saras_profile_name(i).decode() for i in range(lib.saras_profile_count())]
 
 
+def to_bf16_bits(a):
+    """Round an FP32 array to BF16 (round to nearest even) and return the raw bits."""
+    f = np.ascontiguousarray(a, dtype=np.float32)
+    u = f.view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16).astype(np.uint16)
+    return r
+
+
+def from_bf16_bits(b):
+    return (b.astype(np.uint32) << 16).view(np.float32)
+
+
+def conv3d_check(mode, x_bits, dy_bits, w, bias, relu, dims, cin, cout):
+    """Run the tensor-core 3x3x3 convolution stand-alone (saras_conv3d_check).
+    x_bits / dy_bits: channels-last BF16 bit arrays; w: FP32 [cout][27][cin]."""
+    lib = _abi.load()
+    D, H, W = dims
+    nv = D * H * W
+    if mode == 0:
+        out = np.empty(nv * cout, dtype=np.float32)
+    elif mode == 1:
+        out = np.empty(nv * cin, dtype=np.float32)
+    else:
+        out = np.empty(27 * cin * cout + cout, dtype=np.float32)
+    wd = np.ascontiguousarray(w, dtype=np.float64).astype(np.float32)
+    bd = None if bias is None else np.ascontiguousarray(bias, dtype=np.float32)
+    xp = None if x_bits is None else np.ascontiguousarray(x_bits, dtype=np.uint16)
+    dp = None if dy_bits is None else np.ascontiguousarray(dy_bits, dtype=np.uint16)
+    fp = ctypes.POINTER(ctypes.c_float)
+    s = lib.saras_conv3d_check(mode, D, H, W, cin, cout,
+                               None if xp is None else xp.ctypes.data, None if dp is None else dp.ctypes.data,
+                               wd.ctypes.data, None if bd is None else bd.ctypes.data,
+                               relu, out.ctypes.data_as(fp))
+    if s != 0:
+        raise SarasError(s, lib.saras_last_error(None).decode())
+    return out
+
+
 # ---------------------------------------------------------------- initial conditions
 def grid_coords(params):
     """Vertex ("staggered") and cell ("collocated") coordinates including the

@@ -24,7 +24,7 @@ FIELD_NAMES = ["Vx", "Vy", "Vz", "P", "T", "Pp", "mgRHS", "nseRHS.Vx", "nseRHS.V
                "tmpRHS", "pressureGradient.Vx", "pressureGradient.Vy", "pressureGradient.Vz"]
 
 MG_REFERENCE, MG_PLAIN_TARGET, MG_MIXED = 0, 1, 2
-GUESS_PREVIOUS, GUESS_LEARNED = 0, 1
+GUESS_PREVIOUS, GUESS_LEARNED, GUESS_EXTRAPOLATE = 0, 1, 2
 
 _I, _D = ctypes.c_int, ctypes.c_double
 
@@ -156,6 +156,8 @@ def load():
         "saras_unet_train": (_I, [vp, _I, _D, dp]),
         "saras_unet_infer": (_I, [vp, _I]),
         "saras_set_guess_mode": (_I, [vp, _I]),
+        "saras_conv3d_check": (_I, [_I, _I, _I, _I, _I, _I, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _I,
+                                    ctypes.POINTER(ctypes.c_float)]),
         "saras_profile_enable": (_I, [vp, _I, _I]),
         "saras_profile_read": (_I, [vp, _I, ctypes.POINTER(ctypes.c_longlong), dp, dp]),
         "saras_profile_name": (cp, [_I]),

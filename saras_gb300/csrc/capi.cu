@@ -408,7 +408,7 @@ int saras_unet_infer(saras_ctx *h, int field_out) {
 }
 int saras_set_guess_mode(saras_ctx *h, int mode) {
     CTX_OR_FAIL(h);
-    if (mode != SARAS_GUESS_PREVIOUS && mode != SARAS_GUESS_LEARNED) return SARAS_BAD_ARG;
+    if (mode != SARAS_GUESS_PREVIOUS && mode != SARAS_GUESS_LEARNED && mode != SARAS_GUESS_EXTRAPOLATE) return SARAS_BAD_ARG;
     h->c.guessMode = mode;
     return SARAS_OK;
 }

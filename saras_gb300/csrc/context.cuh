@@ -107,6 +107,7 @@ struct Ctx {
     void *unet = nullptr;
     double *pHist[2] = {nullptr, nullptr};   // P at the two previous steps
     int histCount = 0;
+    bool collecting = false;
     // profiling
     ProfSlot prof[PK_COUNT];
     cudaEvent_t userEv[16] = {nullptr};
@@ -158,6 +159,11 @@ void unet_free(Ctx &c);
 int unet_collect(Ctx &c);
 int unet_train(Ctx &c, int iters, double lr, double *loss);
 int unet_infer(Ctx &c, double *out);
+int unet_begin_solve(Ctx &c);
+int unet_guess(Ctx &c, const double *b, double *dst, bool use_net);
+int unet_collect_sample(Ctx &c, const double *b);
+int conv3d_check(int mode, int D, int H, int W, int cin, int cout, const unsigned short *x, const unsigned short *dy,
+                 const float *w, const float *bias, int relu, float *out);
 
 // ---- reductions (fields.cu)
 int reduce_sum_partials(Ctx &c, int nparts, double *host_out);

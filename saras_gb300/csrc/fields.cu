@@ -1100,9 +1100,9 @@ int time_advance(Ctx &c, saras_step_stats *st) {
     if (s) return s;
     int cyc = 0; double res = 0;
     s = mg_solve(c, &cyc, &res, &local);
-    if (s) { local.status = s; if (st) *st = local; return s; }
     local.vcycles = cyc;
     local.mg_residual = res;
+    if (s) { local.status = s; if (st) *st = local; return s; }
     s = sync_field(c, SARAS_FIELD_PP);
     if (s) return s;
     s = project(c, !c.scalar);

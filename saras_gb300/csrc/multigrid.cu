@@ -557,54 +557,78 @@ static TgK<T> make_tgk(const Level &L, double omega) {
     return k;
 }
 
-__device__ __forceinline__ bool near_face(int i, int j, int k, const MgBC &bc) {
-    return i <= 1 || j <= 1 || k <= 1 || i >= bc.E[0] - 1 || j >= bc.E[1] - 1 || k >= bc.E[2] - 1;
-}
-
 template <typename T>
 __device__ __noinline__ void scatter_slow(T *P, int sx, int sy, int i, int j, int k, T v, const MgBC &bc) {
     View3<T> V; V.p = P; V.sx = sx; V.sy = sy;
     put_scatter(V, i, j, k, v, bc);
 }
 
+// The target-mode kernels march along x: a (32 k) x (8 j) thread tile walks
+// kIch consecutive x planes, keeping the x-1 / x / x+1 values of its column in
+// registers, so each point costs one new x-neighbour load plus the four
+// in-plane neighbours and the right-hand side.
+constexpr int kIch = 8;
+
+static void march_dims(const Level &L, dim3 &g, dim3 &b) {
+    b = dim3(32, 8, 1);
+    g = dim3((L.n[2] + 1 + 31) / 32, (L.n[1] + 1 + 7) / 8, (L.n[0] + 1 + kIch - 1) / kIch);
+}
+
 template <typename T, bool ZERO>
 __global__ void __launch_bounds__(256) k_tgt_sweep(T *__restrict__ out, const T *__restrict__ in, const T *__restrict__ r,
                                                    int sx, int sy, MgBC bc, TgK<T> c) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    int j = blockIdx.y * blockDim.y + threadIdx.y;
-    int i = blockIdx.z * blockDim.z + threadIdx.z;
-    if (i > bc.E[0] || j > bc.E[1] || k > bc.E[2]) return;
-    int o = (i + 1) * sx + (j + 1) * sy + (k + 1);
-    T v;
-    if (ZERO) {
-        v = c.ar * r[o];
-    } else {
-        T C = in[o];
-        T ew = in[o + sx] + in[o - sx], ns = in[o + sy] + in[o - sy], ud = in[o + 1] + in[o - 1];
-        v = fma(c.ax, ew, fma(c.ay, ns, fma(c.az, ud, fma(c.ar, r[o], c.om1 * C))));
+    int k = blockIdx.x * 32 + threadIdx.x;
+    int j = blockIdx.y * 8 + threadIdx.y;
+    int i0 = blockIdx.z * kIch;
+    if (j > bc.E[1] || k > bc.E[2]) return;
+    int iend = min(i0 + kIch - 1, bc.E[0]);
+    int o = (i0 + 1) * sx + (j + 1) * sy + (k + 1);
+    bool edge_jk = j <= 1 || k <= 1 || j >= bc.E[1] - 1 || k >= bc.E[2] - 1;
+    T cm = (T)0, cc = (T)0;
+    if (!ZERO) { cm = in[o - sx]; cc = in[o]; }
+#pragma unroll 4
+    for (int i = i0; i <= iend; ++i, o += sx) {
+        T v;
+        if (ZERO) {
+            v = c.ar * r[o];
+        } else {
+            T cp = in[o + sx];
+            T ns = in[o + sy] + in[o - sy], ud = in[o + 1] + in[o - 1];
+            v = fma(c.ax, cm + cp, fma(c.ay, ns, fma(c.az, ud, fma(c.ar, r[o], c.om1 * cc))));
+            cm = cc;
+            cc = cp;
+        }
+        out[o] = v;
+        if (edge_jk || i <= 1 || i >= bc.E[0] - 1) scatter_slow(out, sx, sy, i, j, k, v, bc);
     }
-    out[o] = v;
-    if (near_face(i, j, k, bc)) scatter_slow(out, sx, sy, i, j, k, v, bc);
 }
 
 // r_out = b - Lap(p) over the core; optional max |r| (FP64 accumulation).
 template <typename T, typename OT, bool MAXRED>
 __global__ void __launch_bounds__(256) k_tgt_residual(OT *__restrict__ out, const T *__restrict__ p, const T *__restrict__ b,
                                                       int sx, int sy, MgBC bc, TgK<T> c, double *maxres) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    int j = blockIdx.y * blockDim.y + threadIdx.y;
-    int i = blockIdx.z * blockDim.z + threadIdx.z;
+    int k = blockIdx.x * 32 + threadIdx.x;
+    int j = blockIdx.y * 8 + threadIdx.y;
+    int i0 = blockIdx.z * kIch;
     double m = 0.0;
-    if (i <= bc.E[0] && j <= bc.E[1] && k <= bc.E[2]) {
-        int o = (i + 1) * sx + (j + 1) * sy + (k + 1);
-        T C = p[o];
-        T ew = p[o + sx] + p[o - sx], ns = p[o + sy] + p[o - sy], ud = p[o + 1] + p[o - 1];
-        T lap = fma(c.lx, ew, fma(c.ly, ns, fma(c.lz, ud, c.lc * C)));
-        T res = b[o] - lap;
-        if (out) out[o] = (OT)res;
-        if (MAXRED) {
-            m = fabs((double)res);
-            if (m != m) m = INFINITY;
+    if (j <= bc.E[1] && k <= bc.E[2]) {
+        int iend = min(i0 + kIch - 1, bc.E[0]);
+        int o = (i0 + 1) * sx + (j + 1) * sy + (k + 1);
+        T cm = p[o - sx], cc = p[o];
+#pragma unroll 4
+        for (int i = i0; i <= iend; ++i, o += sx) {
+            T cp = p[o + sx];
+            T ns = p[o + sy] + p[o - sy], ud = p[o + 1] + p[o - 1];
+            T lap = fma(c.lx, cm + cp, fma(c.ly, ns, fma(c.lz, ud, c.lc * cc)));
+            T res = b[o] - lap;
+            if (out) out[o] = (OT)res;
+            if (MAXRED) {
+                double a = fabs((double)res);
+                if (a != a) a = INFINITY;
+                m = fmax(m, a);
+            }
+            cm = cc;
+            cc = cp;
         }
     }
     if (MAXRED) block_max_to(m, maxres);
@@ -612,14 +636,19 @@ __global__ void __launch_bounds__(256) k_tgt_residual(OT *__restrict__ out, cons
 
 // p64 += e32 over the core (FP64 correction accumulation) with face ghosts.
 __global__ void __launch_bounds__(256) k_tgt_update(double *__restrict__ p, const float *__restrict__ e, int sx, int sy, MgBC bc) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    int j = blockIdx.y * blockDim.y + threadIdx.y;
-    int i = blockIdx.z * blockDim.z + threadIdx.z;
-    if (i > bc.E[0] || j > bc.E[1] || k > bc.E[2]) return;
-    int o = (i + 1) * sx + (j + 1) * sy + (k + 1);
-    double v = p[o] + (double)e[o];
-    p[o] = v;
-    if (near_face(i, j, k, bc)) scatter_slow(p, sx, sy, i, j, k, v, bc);
+    int k = blockIdx.x * 32 + threadIdx.x;
+    int j = blockIdx.y * 8 + threadIdx.y;
+    int i0 = blockIdx.z * kIch;
+    if (j > bc.E[1] || k > bc.E[2]) return;
+    int iend = min(i0 + kIch - 1, bc.E[0]);
+    int o = (i0 + 1) * sx + (j + 1) * sy + (k + 1);
+    bool edge_jk = j <= 1 || k <= 1 || j >= bc.E[1] - 1 || k >= bc.E[2] - 1;
+#pragma unroll 4
+    for (int i = i0; i <= iend; ++i, o += sx) {
+        double v = p[o] + (double)e[o];
+        p[o] = v;
+        if (edge_jk || i <= 1 || i >= bc.E[0] - 1) scatter_slow(p, sx, sy, i, j, k, v, bc);
+    }
 }
 
 // ---- target modes (FP64 / mixed)
@@ -791,11 +820,12 @@ static int smooth(Ctx &c, int l, int count, bool zero_first, bool tgt) {
     double bytes = 3.0 * sizeof(T) * (double)(L.n[0] + 1) * (L.n[1] + 1) * (L.n[2] + 1);
     TgK<T> tk = make_tgk<T>(L, c.p.jacobiWeight);
     int sx = (L.n[1] + 3) * (L.n[2] + 3), sy = L.n[2] + 3;
+    dim3 gm, bm; march_dims(L, gm, bm);
     for (int n = 0; n < count; ++n) {
         prof_begin(c, pk, l);
         if (tgt) {
-            if (n == 0 && zero_first) k_tgt_sweep<T, true><<<g, b, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
-            else k_tgt_sweep<T, false><<<g, b, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
+            if (n == 0 && zero_first) k_tgt_sweep<T, true><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
+            else k_tgt_sweep<T, false><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
         } else if (n == 0 && zero_first)
             k_mg_sweep<T, true><<<g, b, 0, c.stream>>>(lview<T>(L, B_<T>(L)), lcview<T>(L, A_<T>(L)), lcview<T>(L, R_<T>(L)), kk, bc, omega);
         else
@@ -832,7 +862,8 @@ static int restrict_level(Ctx &c, int l, bool tgt) {
     prof_begin(c, pk, l);
     if (tgt) {
         int sx = (L.n[1] + 3) * (L.n[2] + 3), sy = L.n[2] + 3;
-        k_tgt_residual<T, T, false><<<g, b, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bcf, make_tgk<T>(L, 1.0), nullptr);
+        dim3 gm, bm; march_dims(L, gm, bm);
+        k_tgt_residual<T, T, false><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bcf, make_tgk<T>(L, 1.0), nullptr);
     } else
         k_mg_residual<T><<<g, b, 0, c.stream>>>(lview<T>(L, B_<T>(L)), lcview<T>(L, A_<T>(L)), lcview<T>(L, R_<T>(L)), kk, bcf);
     count_launch(c);
@@ -1005,6 +1036,11 @@ static int mg_solve_target(Ctx &c, int *cycles, double *residual, saras_step_sta
     double wsum = 1.0;
     for (int d = 0; d < 3; ++d) wsum *= (double)L0.n[d];
     k_tgt_rhs<<<g, b, 0, c.stream>>>(lview<double>(L0, L0.r), lcview<double>(L0, c.f[SARAS_FIELD_MGRHS]), bc0, c.dscal + 30, wsum, c.dscal + 31);
+    // pressure history for the learned / extrapolated guess
+    bool wantGuess = c.guessMode != SARAS_GUESS_PREVIOUS;
+    if (wantGuess || c.collecting) {
+        if ((s = unet_begin_solve(c))) return s;
+    }
     // p = Pp (initial guess) with face ghosts
     L0.cur = 0;
     k_mg_init_p<double><<<g, b, 0, c.stream>>>(lview<double>(L0, L0.pa()), lcview<double>(L0, c.f[SARAS_FIELD_PP]), bc0);
@@ -1015,20 +1051,21 @@ static int mg_solve_target(Ctx &c, int *cycles, double *residual, saras_step_sta
     double target = c.mgTarget * bmax;
     int sx0 = (L0.n[1] + 3) * (L0.n[2] + 3), sy0 = L0.n[2] + 3;
     TgK<double> t0 = make_tgk<double>(L0, 1.0);
+    dim3 gm0, bm0; march_dims(L0, gm0, bm0);
     auto fine_res = [&](bool withE, double *out) -> int {
         SARAS_CUDA_TRY(cudaMemsetAsync(c.dscal + 32, 0, sizeof(double), c.stream));
         if (withE) {
             prof_begin(c, PK_REFINE_UPDATE, 0);
-            k_tgt_update<<<g, b, 0, c.stream>>>(L0.pa(), L0.pa32(), sx0, sy0, bc0);
+            k_tgt_update<<<gm0, bm0, 0, c.stream>>>(L0.pa(), L0.pa32(), sx0, sy0, bc0);
             count_launch(c);
             prof_end(c, PK_REFINE_UPDATE, 0, (8.0 + 4.0 + 8.0) * (double)ncore);
         }
         prof_begin(c, PK_REFINE_RESID, 0);
         if (c.mgMode == SARAS_MG_MIXED) {
-            k_tgt_residual<double, float, true><<<g, b, 0, c.stream>>>(L0.r32, L0.pa(), L0.r, sx0, sy0, bc0, t0, c.dscal + 32);
+            k_tgt_residual<double, float, true><<<gm0, bm0, 0, c.stream>>>(L0.r32, L0.pa(), L0.r, sx0, sy0, bc0, t0, c.dscal + 32);
             prof_end(c, PK_REFINE_RESID, 0, (8.0 + 8.0 + 4.0) * (double)ncore);
         } else {
-            k_tgt_residual<double, double, true><<<g, b, 0, c.stream>>>(nullptr, L0.pa(), L0.r, sx0, sy0, bc0, t0, c.dscal + 32);
+            k_tgt_residual<double, double, true><<<gm0, bm0, 0, c.stream>>>(nullptr, L0.pa(), L0.r, sx0, sy0, bc0, t0, c.dscal + 32);
             prof_end(c, PK_REFINE_RESID, 0, (8.0 + 8.0) * (double)ncore);
         }
         count_launch(c);
@@ -1041,7 +1078,26 @@ static int mg_solve_target(Ctx &c, int *cycles, double *residual, saras_step_sta
     };
     double r = 0;
     if ((s = fine_res(false, &r))) return s;
-    if (st) st->guess_residual = bmax > 0 ? r / bmax : r;
+    int source = 0;
+    if (wantGuess && c.histCount >= 2) {
+        bool net = c.guessMode == SARAS_GUESS_LEARNED;
+        int gs = unet_guess(c, L0.r, L0.pb(), net);
+        if (gs == SARAS_OK) {
+            L0.cur ^= 1;
+            double rg = 0;
+            if ((s = fine_res(false, &rg))) return s;
+            if (rg < r) {
+                r = rg;
+                source = net ? 1 : 2;
+            } else {
+                L0.cur ^= 1;   // keep the previous pressure (and recompute its FP32 residual)
+                if ((s = fine_res(false, &r))) return s;
+            }
+        } else if (gs != SARAS_BAD_CONFIG) {
+            return gs;
+        }
+    }
+    if (st) { st->guess_residual = bmax > 0 ? r / bmax : r; st->guess_source = source; }
     int cyc = 0, steps = 0;
     while (r > target && cyc < c.mgMaxCycles) {
         if (!std::isfinite(r)) { c.err = "multigrid residual is not finite"; return SARAS_NOT_FINITE; }
@@ -1064,6 +1120,9 @@ static int mg_solve_target(Ctx &c, int *cycles, double *residual, saras_step_sta
                                                              nullptr, nullptr, nullptr);
     count_launch(c);
     if ((s = chk(c, "target output"))) return s;
+    if (c.collecting && r <= target) {
+        if ((s = unet_collect_sample(c, L0.r))) return s;
+    }
     if (cycles) *cycles = cyc;
     if (residual) *residual = bmax > 0 ? r / bmax : r;
     if (r > target) { c.err = "multigrid did not reach the residual target within mgMaxCycles"; return SARAS_NOT_CONVERGED; }

@@ -1,22 +1,826 @@
 // unet.cu -- learned warm start for the pressure-correction solve.
-// (The implicit-GEMM tcgen05 convolutions land in this file.)
+//
+// A three-level 3D U-Net (16/32/64 channels, 3x3x3 convolutions, BF16
+// activations and weights, FP32 accumulation on tcgen05 tensor cores) maps
+//   (b / s_b, P_{n-1} / s_p, P_{n-2} / s_p)   at multigrid level 1
+// to a correction d of the linear extrapolation 2 P_{n-1} - P_{n-2}; the guess
+// handed to the multigrid solve is
+//   P_guess = 2 P_{n-1} - P_{n-2} + s_p * prolong(d),
+// and the solver keeps the previous pressure instead whenever the guess has the
+// larger FP64 residual.  The network is trained on (input, solution) pairs that
+// the solver itself produces during the run's warm-up, with Adam on FP32
+// master weights; forward and input-gradient convolutions run on the tensor
+// cores (k_conv3d_tc), weight gradients reduce over voxels on the CUDA cores.
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+#include <algorithm>
 
 #include "context.cuh"
+#include "tc_conv.cuh"
 
 namespace saras {
 
-int unet_create(Ctx &c) { (void)c; return SARAS_OK; }
-void unet_free(Ctx &c) { (void)c; }
-int unet_collect(Ctx &c) { c.err = "U-Net warm start not available in this build"; return SARAS_BAD_CONFIG; }
-int unet_train(Ctx &c, int iters, double lr, double *loss) {
-    (void)iters; (void)lr; (void)loss;
-    c.err = "U-Net warm start not available in this build";
-    return SARAS_BAD_CONFIG;
+__global__ void k_final_reduce(const double *part, int n, int op, double *out);
+typedef __nv_bfloat16 bf16;
+
+// ------------------------------------------------------------------ element kernels
+struct Grid3 {
+    int D, H, W;
+    __host__ __device__ long n() const { return (long)D * H * W; }
+};
+
+__device__ __forceinline__ float fw1(int d) { return d == 0 ? 0.5f : 0.25f; }
+
+// Full-weighting restriction of a channels-last tensor (vertex grids, coarse
+// point i sits on fine point 2i; zero outside the fine grid), times `scale`.
+__global__ void k_pool_down(const bf16 *__restrict__ in, bf16 *__restrict__ out, int C, Grid3 f, Grid3 c, float scale) {
+    long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    long total = c.n() * C;
+    if (t >= total) return;
+    int ch = (int)(t % C);
+    long v = t / C;
+    int x = (int)(v % c.W), y = (int)((v / c.W) % c.H), z = (int)(v / ((long)c.W * c.H));
+    float s = 0.0f;
+    for (int dz = -1; dz <= 1; ++dz) {
+        int zz = 2 * z + dz;
+        if (zz < 0 || zz >= f.D) continue;
+        for (int dy = -1; dy <= 1; ++dy) {
+            int yy = 2 * y + dy;
+            if (yy < 0 || yy >= f.H) continue;
+            for (int dx = -1; dx <= 1; ++dx) {
+                int xx = 2 * x + dx;
+                if (xx < 0 || xx >= f.W) continue;
+                s += fw1(dz) * fw1(dy) * fw1(dx) * __bfloat162float(in[(((long)zz * f.H + yy) * f.W + xx) * C + ch]);
+            }
+        }
+    }
+    out[t] = __float2bfloat16(s * scale);
 }
-int unet_infer(Ctx &c, double *out) {
-    (void)out;
-    c.err = "U-Net warm start not available in this build";
-    return SARAS_BAD_CONFIG;
+
+// Trilinear vertex prolongation of a channels-last tensor, times `scale`.
+__global__ void k_pool_up(const bf16 *__restrict__ in, bf16 *__restrict__ out, int C, Grid3 c, Grid3 f, float scale) {
+    long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    long total = f.n() * C;
+    if (t >= total) return;
+    int ch = (int)(t % C);
+    long v = t / C;
+    int x = (int)(v % f.W), y = (int)((v / f.W) % f.H), z = (int)(v / ((long)f.W * f.H));
+    int x0 = x >> 1, y0 = y >> 1, z0 = z >> 1;
+    int x1 = min(x0 + (x & 1), c.W - 1), y1 = min(y0 + (y & 1), c.H - 1), z1 = min(z0 + (z & 1), c.D - 1);
+    auto at = [&](int a, int b, int d) { return __bfloat162float(in[(((long)a * c.H + b) * c.W + d) * C + ch]); };
+    float s = at(z0, y0, x0) + at(z0, y0, x1) + at(z0, y1, x0) + at(z0, y1, x1) + at(z1, y0, x0) + at(z1, y0, x1) +
+              at(z1, y1, x0) + at(z1, y1, x1);
+    out[t] = __float2bfloat16(0.125f * s * scale);
+}
+
+// out = (a + b) where mask > 0, else 0  (b and mask optional).
+__global__ void k_add_mask(const bf16 *a, const bf16 *b, const bf16 *mask, bf16 *out, long n) {
+    long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    float v = __bfloat162float(a[t]) + (b ? __bfloat162float(b[t]) : 0.0f);
+    if (mask && !(__bfloat162float(mask[t]) > 0.0f)) v = 0.0f;
+    out[t] = __float2bfloat16(v);
+}
+
+// Pack FP32 master weights W[cout][27][cin] into the per-K-step tensor-core
+// tiles of k_conv3d_tc.  transposed = 0: forward tiles (N = cout, K = cin);
+// transposed = 1: input-gradient tiles (N = cin, K = cout, taps mirrored).
+__global__ void k_pack_weights(const float *__restrict__ w, bf16 *__restrict__ pk, int cin, int cout, int transposed) {
+    int N = transposed ? cin : cout, KC = transposed ? cout : cin;
+    int nch = KC / 16;
+    long total = 27L * nch * N * 16;
+    long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    int k = (int)(t % 16);
+    int n = (int)((t / 16) % N);
+    long s = t / (16L * N);
+    int tap = (int)(s / nch), ch = (int)(s % nch);
+    int kk = ch * 16 + k;
+    float val = transposed ? w[((long)kk * 27 + (26 - tap)) * cin + n] : w[((long)n * 27 + tap) * cin + kk];
+    long byte = s * (long)N * 32 + (n >> 3) * 256 + (k >> 3) * 128 + (n & 7) * 16 + (k & 7) * 2;
+    pk[byte / 2] = __float2bfloat16(val);
+}
+
+// Weight and bias gradients: dW[n][tap][c] += sum_v dY[v][n] X[v + off(tap)][c],
+// db[n] += sum_v dY[v][n].  blockIdx.y = tap; each block reduces a voxel chunk.
+constexpr int kDwChunk = 2048;
+constexpr int kDwSub = 32;
+__global__ void __launch_bounds__(256) k_conv_dw(const bf16 *x0, const bf16 *x1, int c0, int c1, const bf16 *dy, int cout, Grid3 g,
+                                                  float *dw, float *db) {
+    extern __shared__ float sh[];
+    int cin = c0 + c1;
+    float *sx = sh;                   // kDwSub x cin
+    float *sy = sh + kDwSub * cin;    // kDwSub x cout
+    int tap = blockIdx.y;
+    int dz = tap / 9 - 1, dyy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+    long v0 = (long)blockIdx.x * kDwChunk;
+    long nv = g.n();
+    int pairs = cin * cout;
+    constexpr int MAXP = 24;
+    float acc[MAXP];
+    float bacc = 0.0f;
+#pragma unroll
+    for (int q = 0; q < MAXP; ++q) acc[q] = 0.0f;
+    for (long vb = v0; vb < min(v0 + kDwChunk, nv); vb += kDwSub) {
+        __syncthreads();
+        for (int t = threadIdx.x; t < kDwSub * cin; t += blockDim.x) {
+            int r = t / cin, cc = t % cin;
+            long v = vb + r;
+            float val = 0.0f;
+            if (v < nv) {
+                int x = (int)(v % g.W), y = (int)((v / g.W) % g.H), z = (int)(v / ((long)g.W * g.H));
+                int zz = z + dz, yy = y + dyy, xx = x + dx;
+                if (zz >= 0 && zz < g.D && yy >= 0 && yy < g.H && xx >= 0 && xx < g.W) {
+                    long sv = ((long)zz * g.H + yy) * g.W + xx;
+                    val = cc < c0 ? __bfloat162float(x0[sv * c0 + cc]) : __bfloat162float(x1[sv * c1 + (cc - c0)]);
+                }
+            }
+            sx[t] = val;
+        }
+        for (int t = threadIdx.x; t < kDwSub * cout; t += blockDim.x) {
+            int r = t / cout, n = t % cout;
+            long v = vb + r;
+            sy[t] = v < nv ? __bfloat162float(dy[v * cout + n]) : 0.0f;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < MAXP; ++q) {
+            int pr = threadIdx.x + q * blockDim.x;
+            if (pr < pairs) {
+                int n = pr / cin, cc = pr % cin;
+                float a = acc[q];
+                for (int r = 0; r < kDwSub; ++r) a = fmaf(sy[r * cout + n], sx[r * cin + cc], a);
+                acc[q] = a;
+            }
+        }
+        if (tap == 13 && (int)threadIdx.x < cout)
+            for (int r = 0; r < kDwSub; ++r) bacc += sy[r * cout + threadIdx.x];
+    }
+#pragma unroll
+    for (int q = 0; q < MAXP; ++q) {
+        int pr = threadIdx.x + q * blockDim.x;
+        if (pr < pairs) {
+            int n = pr / cin, cc = pr % cin;
+            atomicAdd(&dw[((long)n * 27 + tap) * cin + cc], acc[q]);
+        }
+    }
+    if (tap == 13 && (int)threadIdx.x < cout) atomicAdd(&db[threadIdx.x], bacc);
+}
+
+// Adam on the flat FP32 parameter vector.
+__global__ void k_adam(float *p, const float *g, float *m, float *v, long n, float lr, float b1, float b2, float eps, float c1, float c2) {
+    long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    float gr = g[t];
+    float mm = b1 * m[t] + (1.0f - b1) * gr;
+    float vv = b2 * v[t] + (1.0f - b2) * gr * gr;
+    m[t] = mm;
+    v[t] = vv;
+    p[t] -= lr * (mm / c1) / (sqrtf(vv / c2) + eps);
+}
+
+// ---- FP64 <-> network features
+struct L0View {
+    const double *p;
+    int n[3];     // core upper index (E) per axis; padded extent E+3
+    __device__ double at(int i, int j, int k) const {
+        return p[((long)(i + 1) * (n[1] + 3) + (j + 1)) * (n[2] + 3) + (k + 1)];
+    }
+};
+
+// Full weighting of a level-0 core field at the level-1 point (z, y, x).
+__device__ __forceinline__ double fw_restrict(const L0View &f, int z, int y, int x) {
+    double s = 0.0;
+    for (int dz = -1; dz <= 1; ++dz) {
+        int zz = 2 * z + dz;
+        if (zz < 0 || zz > f.n[0]) continue;
+        for (int dy = -1; dy <= 1; ++dy) {
+            int yy = 2 * y + dy;
+            if (yy < 0 || yy > f.n[1]) continue;
+            for (int dx = -1; dx <= 1; ++dx) {
+                int xx = 2 * x + dx;
+                if (xx < 0 || xx > f.n[2]) continue;
+                s += (double)(fw1(dz) * fw1(dy) * fw1(dx)) * f.at(zz, yy, xx);
+            }
+        }
+    }
+    return s;
+}
+
+// Sample features (3 FP32 channels) and, with `target`, the training target
+// d* = R(P_new - 2 P1 + P2) / s_p.
+__global__ void k_features(L0View b, L0View p1, L0View p2, L0View pnew, Grid3 g1, const double *scales, float *feat, float *target) {
+    long v = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (v >= g1.n()) return;
+    int x = (int)(v % g1.W), y = (int)((v / g1.W) % g1.H), z = (int)(v / ((long)g1.W * g1.H));
+    double sb = scales[0], sp = scales[1];
+    double rb = fw_restrict(b, z, y, x), r1 = fw_restrict(p1, z, y, x), r2 = fw_restrict(p2, z, y, x);
+    feat[v * 3 + 0] = (float)(rb / sb);
+    feat[v * 3 + 1] = (float)(r1 / sp);
+    feat[v * 3 + 2] = (float)(r2 / sp);
+    if (target) target[v] = (float)((fw_restrict(pnew, z, y, x) - 2.0 * r1 + r2) / sp);
+}
+
+// Expand 3-channel FP32 features into the 16-channel BF16 network input.
+__global__ void k_expand(const float *feat, bf16 *x0, long nv) {
+    long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (t >= nv * 16) return;
+    long v = t / 16;
+    int c = (int)(t % 16);
+    x0[t] = __float2bfloat16(c < 3 ? feat[v * 3 + c] : 0.0f);
+}
+
+// Loss 0.5 * mean (d - d*)^2 and the output gradient (channel 0 of a 16-channel BF16 tensor).
+__global__ void k_loss(const float *d, const float *dstar, bf16 *gout, long nv, double *part) {
+    __shared__ double sm[32];
+    long v = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    double e = 0.0;
+    if (v < nv) {
+        float r = d[v] - dstar[v];
+        e = 0.5 * (double)r * r;
+        float gr = r / (float)nv;
+#pragma unroll
+        for (int c = 0; c < 16; ++c) gout[v * 16 + c] = __float2bfloat16(c == 0 ? gr : 0.0f);
+    }
+    e = warp_sum(e);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = e;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += sm[w];
+        part[blockIdx.x] = s;
+    }
+}
+
+// Guess on level 0: 2 P1 - P2 + s_p * prolong(d), core points, with face ghosts.
+__global__ void k_apply_guess(double *out, L0View p1, L0View p2, const float *d, Grid3 g1, const double *scales, int use_net,
+                              int per0, int per1, int per2) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y * blockDim.y + threadIdx.y;
+    int i = blockIdx.z;
+    if (i > p1.n[0] || j > p1.n[1] || k > p1.n[2]) return;
+    double v = 2.0 * p1.at(i, j, k) - p2.at(i, j, k);
+    if (use_net) {
+        int z0 = i >> 1, y0 = j >> 1, x0 = k >> 1;
+        int z1 = min(z0 + (i & 1), g1.D - 1), y1 = min(y0 + (j & 1), g1.H - 1), x1 = min(x0 + (k & 1), g1.W - 1);
+        auto at = [&](int a, int b, int c) { return (double)d[((long)a * g1.H + b) * g1.W + c]; };
+        double s = at(z0, y0, x0) + at(z0, y0, x1) + at(z0, y1, x0) + at(z0, y1, x1) + at(z1, y0, x0) + at(z1, y0, x1) +
+                   at(z1, y1, x0) + at(z1, y1, x1);
+        v += scales[1] * 0.125 * s;
+    }
+    long sy = p1.n[2] + 3, sx = (long)(p1.n[1] + 3) * sy;
+    auto put = [&](int a, int b, int c) { out[(long)(a + 1) * sx + (long)(b + 1) * sy + (c + 1)] = v; };
+    put(i, j, k);
+    int q[3] = {i, j, k};
+    int per[3] = {per0, per1, per2};
+    for (int dd = 0; dd < 3; ++dd) {
+        int E = p1.n[dd];
+        int g0 = -2, g1v = -2;
+        if (per[dd]) { if (q[dd] == E - 1) g0 = -1; if (q[dd] == 1) g1v = E + 1; }
+        else { if (q[dd] == 1) g0 = -1; if (q[dd] == E - 1) g1v = E + 1; }
+        int r[3] = {i, j, k};
+        if (g0 != -2) { r[dd] = g0; put(r[0], r[1], r[2]); }
+        if (g1v != -2) { r[dd] = g1v; put(r[0], r[1], r[2]); }
+    }
+}
+
+__global__ void k_maxabs_core(L0View f, double *out) {
+    long n = (long)(f.n[0] + 1) * (f.n[1] + 1) * (f.n[2] + 1);
+    double m = 0.0;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+        int k = (int)(t % (f.n[2] + 1)), j = (int)((t / (f.n[2] + 1)) % (f.n[1] + 1)), i = (int)(t / ((long)(f.n[2] + 1) * (f.n[1] + 1)));
+        m = fmax(m, fabs(f.at(i, j, k)));
+    }
+    block_max_to(m, out);
+}
+
+__global__ void k_floor_scale(double *s, double floor_) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        if (!(s[0] > floor_)) s[0] = floor_;
+        if (!(s[1] > floor_)) s[1] = floor_;
+    }
+}
+
+// ------------------------------------------------------------------ host: network
+struct ConvLayer {
+    int cin0, cin1, cout, level;
+    bool relu;
+    long woff, boff;   // offsets of W and b in the flat parameter vector
+    bf16 *wf = nullptr, *wt = nullptr;   // packed forward / transposed tiles
+};
+
+struct UNet {
+    Grid3 g[3];                      // level-1, 2, 3 grids
+    std::vector<ConvLayer> L;
+    long nparam = 0;
+    float *param = nullptr, *grad = nullptr, *adam_m = nullptr, *adam_v = nullptr;
+    long adam_t = 0;
+    std::vector<bf16 *> act;          // activations
+    std::vector<bf16 *> grd;          // gradient buffers
+    bf16 *x0 = nullptr;
+    float *out = nullptr, *feat = nullptr;
+    double *scales = nullptr;         // s_b, s_p (device)
+    // training samples: 3 feature channels + target per voxel
+    std::vector<float *> samples;
+    int nsamples = 0, cap = 0, next = 0;
+    int *err = nullptr;
+    double *part = nullptr;
+    bool trained = false;
+    long flops_fwd = 0;
+};
+
+static int ucheck(Ctx &c, const char *what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) { c.err = std::string(what) + ": " + cudaGetErrorString(e); return SARAS_CUDA_ERROR; }
+    return SARAS_OK;
+}
+
+template <int N>
+static void launch_conv_n(const ConvArgs &a, cudaStream_t s) {
+    int blocks = (a.nvox + 127) / 128;
+    k_conv3d_tc<N><<<blocks, 128, conv_smem_bytes<N>(), s>>>(a);
+}
+
+static int launch_conv(Ctx &c, int N, const ConvArgs &a) {
+    switch (N) {
+    case 16: launch_conv_n<16>(a, c.stream); break;
+    case 32: launch_conv_n<32>(a, c.stream); break;
+    case 48: launch_conv_n<48>(a, c.stream); break;
+    case 64: launch_conv_n<64>(a, c.stream); break;
+    case 96: launch_conv_n<96>(a, c.stream); break;
+    default: c.err = "unsupported convolution width"; return SARAS_BAD_ARG;
+    }
+    count_launch(c);
+    return ucheck(c, "k_conv3d_tc");
+}
+
+// Activation / gradient slot indices.
+enum { A_X0 = 0, A_0, A_E1, A_P1, A_2, A_E2, A_P2, A_4, A_E3, A_U2, A_6, A_F2, A_U1, A_8, A_F1, A_COUNT };
+
+static UNet *U(Ctx &c) { return reinterpret_cast<UNet *>(c.unet); }
+
+static int unet_alloc(Ctx &c) {
+    if (c.unet) return SARAS_OK;
+    UNet *u = new UNet();
+    c.unet = u;
+    const Level &L1 = c.lv[1];
+    const Level &L2 = c.lv[std::min(2, c.depth)];
+    const Level &L3 = c.lv[std::min(3, c.depth)];
+    if (c.depth < 3) { c.err = "the U-Net needs a multigrid depth of at least 3"; return SARAS_BAD_CONFIG; }
+    u->g[0] = Grid3{L1.n[0] + 1, L1.n[1] + 1, L1.n[2] + 1};
+    u->g[1] = Grid3{L2.n[0] + 1, L2.n[1] + 1, L2.n[2] + 1};
+    u->g[2] = Grid3{L3.n[0] + 1, L3.n[1] + 1, L3.n[2] + 1};
+    struct Spec { int c0, c1, co, lvl; bool relu; };
+    const Spec spec[11] = {{16, 0, 16, 0, true},  {16, 0, 16, 0, true},  {16, 0, 32, 1, true}, {32, 0, 32, 1, true},
+                           {32, 0, 64, 2, true},  {64, 0, 64, 2, true},  {64, 32, 32, 1, true}, {32, 0, 32, 1, true},
+                           {32, 16, 16, 0, true}, {16, 0, 16, 0, true},  {16, 0, 16, 0, false}};
+    long off = 0;
+    for (const Spec &s : spec) {
+        ConvLayer l;
+        l.cin0 = s.c0; l.cin1 = s.c1; l.cout = s.co; l.level = s.lvl; l.relu = s.relu;
+        l.woff = off; off += 27L * (s.c0 + s.c1) * s.co;
+        l.boff = off; off += s.co;
+        u->flops_fwd += 2L * 27 * (s.c0 + s.c1) * s.co * u->g[s.lvl].n();
+        u->L.push_back(l);
+    }
+    u->nparam = off;
+    size_t pb = sizeof(float) * off;
+    SARAS_CUDA_TRY(cudaMalloc(&u->param, pb)); SARAS_CUDA_TRY(cudaMalloc(&u->grad, pb));
+    SARAS_CUDA_TRY(cudaMalloc(&u->adam_m, pb)); SARAS_CUDA_TRY(cudaMalloc(&u->adam_v, pb));
+    SARAS_CUDA_TRY(cudaMemset(u->adam_m, 0, pb)); SARAS_CUDA_TRY(cudaMemset(u->adam_v, 0, pb));
+    // Kaiming-uniform initialisation from a counter-based generator (seeded);
+    // the output layer starts at zero so the untrained guess is the extrapolation.
+    std::vector<float> h(off, 0.0f);
+    uint64_t seed = (uint64_t)c.p.seed * 0x9E3779B97F4A7C15ull + 12345;
+    auto rnd = [&](uint64_t i) {
+        uint64_t z = seed + i * 0x9E3779B97F4A7C15ull;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+    };
+    for (size_t q = 0; q < u->L.size(); ++q) {
+        const ConvLayer &l = u->L[q];
+        int fan = 27 * (l.cin0 + l.cin1);
+        float bound = (q + 1 == u->L.size()) ? 0.0f : (float)std::sqrt(6.0 / fan);
+        for (long t = 0; t < 27L * (l.cin0 + l.cin1) * l.cout; ++t) h[l.woff + t] = (float)((2.0 * rnd(l.woff + t) - 1.0) * bound);
+    }
+    SARAS_CUDA_TRY(cudaMemcpy(u->param, h.data(), pb, cudaMemcpyHostToDevice));
+    for (ConvLayer &l : u->L) {
+        size_t tiles = 27L * (l.cin0 + l.cin1) * l.cout * sizeof(bf16);
+        SARAS_CUDA_TRY(cudaMalloc(&l.wf, tiles));
+        SARAS_CUDA_TRY(cudaMalloc(&l.wt, tiles));
+    }
+    // activations (channels of each slot, level)
+    const int chs[A_COUNT] = {16, 16, 16, 16, 32, 32, 32, 64, 64, 64, 32, 32, 32, 16, 16};
+    const int lvl[A_COUNT] = {0, 0, 0, 1, 1, 1, 2, 2, 2, 1, 1, 1, 0, 0, 0};
+    u->act.assign(A_COUNT, nullptr);
+    u->grd.assign(A_COUNT, nullptr);
+    for (int s = 0; s < A_COUNT; ++s) {
+        size_t bytes = sizeof(bf16) * (size_t)chs[s] * u->g[lvl[s]].n();
+        SARAS_CUDA_TRY(cudaMalloc(&u->act[s], bytes));
+        SARAS_CUDA_TRY(cudaMalloc(&u->grd[s], bytes));
+        SARAS_CUDA_TRY(cudaMemset(u->act[s], 0, bytes));
+        SARAS_CUDA_TRY(cudaMemset(u->grd[s], 0, bytes));
+    }
+    u->x0 = u->act[A_X0];
+    long n1 = u->g[0].n();
+    SARAS_CUDA_TRY(cudaMalloc(&u->out, sizeof(float) * n1));
+    SARAS_CUDA_TRY(cudaMalloc(&u->feat, sizeof(float) * 4 * n1));
+    SARAS_CUDA_TRY(cudaMalloc(&u->scales, sizeof(double) * 4));
+    SARAS_CUDA_TRY(cudaMalloc(&u->err, sizeof(int)));
+    SARAS_CUDA_TRY(cudaMemset(u->err, 0, sizeof(int)));
+    SARAS_CUDA_TRY(cudaMalloc(&u->part, sizeof(double) * ((n1 + 255) / 256 + 1)));
+    u->cap = 32;
+    return SARAS_OK;
+}
+
+void unet_free(Ctx &c) {
+    UNet *u = U(c);
+    if (!u) return;
+    cudaFree(u->param); cudaFree(u->grad); cudaFree(u->adam_m); cudaFree(u->adam_v);
+    for (ConvLayer &l : u->L) { cudaFree(l.wf); cudaFree(l.wt); }
+    for (bf16 *p : u->act) cudaFree(p);
+    for (bf16 *p : u->grd) cudaFree(p);
+    for (float *p : u->samples) cudaFree(p);
+    cudaFree(u->out); cudaFree(u->feat); cudaFree(u->scales); cudaFree(u->err); cudaFree(u->part);
+    delete u;
+    c.unet = nullptr;
+}
+
+int unet_create(Ctx &c) { return unet_alloc(c); }
+
+static int pack_all(Ctx &c) {
+    UNet *u = U(c);
+    for (ConvLayer &l : u->L) {
+        int cin = l.cin0 + l.cin1;
+        long total = 27L * cin * l.cout;
+        int blocks = (int)((total + 255) / 256);
+        k_pack_weights<<<blocks, 256, 0, c.stream>>>(u->param + l.woff, l.wf, cin, l.cout, 0);
+        k_pack_weights<<<blocks, 256, 0, c.stream>>>(u->param + l.woff, l.wt, cin, l.cout, 1);
+        count_launch(c, 2);
+    }
+    return ucheck(c, "pack weights");
+}
+
+static ConvArgs conv_args(UNet *u, const Grid3 &g) {
+    ConvArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.D = g.D; a.H = g.H; a.W = g.W;
+    a.nvox = (int)g.n();
+    a.err = u->err;
+    return a;
+}
+
+static int pool(Ctx &c, const bf16 *in, bf16 *out, int C, const Grid3 &from, const Grid3 &to, bool down, float scale) {
+    long total = to.n() * C;
+    int blocks = (int)((total + 255) / 256);
+    if (down) k_pool_down<<<blocks, 256, 0, c.stream>>>(in, out, C, from, to, scale);
+    else k_pool_up<<<blocks, 256, 0, c.stream>>>(in, out, C, from, to, scale);
+    count_launch(c);
+    return ucheck(c, "pool");
+}
+
+// Forward pass from u->x0 to u->out (FP32 d at level 1).
+static int unet_forward(Ctx &c) {
+    UNet *u = U(c);
+    int s;
+    auto fwd = [&](int li, const bf16 *in0, const bf16 *in1, bf16 *out, float *out32) -> int {
+        const ConvLayer &l = u->L[li];
+        ConvArgs a = conv_args(u, u->g[l.level]);
+        a.in0 = in0; a.in1 = in1; a.c0 = l.cin0; a.c1 = l.cin1;
+        a.wpk = l.wf; a.bias = u->param + l.boff;
+        a.out0 = out; a.split = l.cout; a.out32 = out32; a.relu = l.relu ? 1 : 0;
+        prof_begin(c, PK_CONV_FWD, l.level == 0 ? 0 : 1);
+        int r = launch_conv(c, l.cout, a);
+        prof_end(c, PK_CONV_FWD, l.level == 0 ? 0 : 1,
+                 (double)u->g[l.level].n() * 2.0 * (l.cin0 + l.cin1 + l.cout));
+        return r;
+    };
+    auto A = [&](int q) { return u->act[q]; };
+    if ((s = fwd(0, A(A_X0), nullptr, A(A_0), nullptr))) return s;
+    if ((s = fwd(1, A(A_0), nullptr, A(A_E1), nullptr))) return s;
+    if ((s = pool(c, A(A_E1), A(A_P1), 16, u->g[0], u->g[1], true, 1.0f))) return s;
+    if ((s = fwd(2, A(A_P1), nullptr, A(A_2), nullptr))) return s;
+    if ((s = fwd(3, A(A_2), nullptr, A(A_E2), nullptr))) return s;
+    if ((s = pool(c, A(A_E2), A(A_P2), 32, u->g[1], u->g[2], true, 1.0f))) return s;
+    if ((s = fwd(4, A(A_P2), nullptr, A(A_4), nullptr))) return s;
+    if ((s = fwd(5, A(A_4), nullptr, A(A_E3), nullptr))) return s;
+    if ((s = pool(c, A(A_E3), A(A_U2), 64, u->g[2], u->g[1], false, 1.0f))) return s;
+    if ((s = fwd(6, A(A_U2), A(A_E2), A(A_6), nullptr))) return s;
+    if ((s = fwd(7, A(A_6), nullptr, A(A_F2), nullptr))) return s;
+    if ((s = pool(c, A(A_F2), A(A_U1), 32, u->g[1], u->g[0], false, 1.0f))) return s;
+    if ((s = fwd(8, A(A_U1), A(A_E1), A(A_8), nullptr))) return s;
+    if ((s = fwd(9, A(A_8), nullptr, A(A_F1), nullptr))) return s;
+    if ((s = fwd(10, A(A_F1), nullptr, nullptr, u->out))) return s;
+    return SARAS_OK;
+}
+
+static int add_mask(Ctx &c, const bf16 *a, const bf16 *b, const bf16 *mask, bf16 *out, long n) {
+    k_add_mask<<<(int)((n + 255) / 256), 256, 0, c.stream>>>(a, b, mask, out, n);
+    count_launch(c);
+    return ucheck(c, "add_mask");
+}
+
+static int conv_dw(Ctx &c, int li, const bf16 *x0, const bf16 *x1, const bf16 *dy) {
+    UNet *u = U(c);
+    const ConvLayer &l = u->L[li];
+    const Grid3 &g = u->g[l.level];
+    int cin = l.cin0 + l.cin1;
+    dim3 grid((unsigned)((g.n() + kDwChunk - 1) / kDwChunk), 27);
+    size_t sm = sizeof(float) * kDwSub * (cin + l.cout);
+    k_conv_dw<<<grid, 256, sm, c.stream>>>(x0, x1, l.cin0, l.cin1, dy, l.cout, g, u->grad + l.woff, u->grad + l.boff);
+    count_launch(c);
+    return ucheck(c, "conv_dw");
+}
+
+// Input gradient of layer li: conv of dY with the mirrored, transposed weights.
+static int conv_dx(Ctx &c, int li, const bf16 *dy, bf16 *out0, bf16 *out1, const bf16 *mask0) {
+    UNet *u = U(c);
+    const ConvLayer &l = u->L[li];
+    ConvArgs a = conv_args(u, u->g[l.level]);
+    a.in0 = dy; a.c0 = l.cout; a.in1 = nullptr; a.c1 = 0;
+    a.wpk = l.wt; a.bias = nullptr; a.relu = 0;
+    a.out0 = out0; a.out1 = out1; a.split = l.cin1 ? l.cin0 : l.cin0;
+    a.mask0 = mask0;
+    prof_begin(c, PK_CONV_BWD, l.level == 0 ? 0 : 1);
+    int s = launch_conv(c, l.cin0 + l.cin1, a);
+    prof_end(c, PK_CONV_BWD, l.level == 0 ? 0 : 1, (double)u->g[l.level].n() * 2.0 * (l.cin0 + l.cin1 + l.cout));
+    return s;
+}
+
+// Backward pass from the output gradient in grd[A_F1]-shaped buffer `gout`.
+static int unet_backward(Ctx &c, const bf16 *gout) {
+    UNet *u = U(c);
+    int s;
+    auto A = [&](int q) { return u->act[q]; };
+    auto G = [&](int q) { return u->grd[q]; };
+    long n1 = u->g[0].n(), n2 = u->g[1].n(), n3 = u->g[2].n();
+    SARAS_CUDA_TRY(cudaMemsetAsync(u->grad, 0, sizeof(float) * u->nparam, c.stream));
+    // layer 10 (no ReLU): dW, dX masked by f1 > 0 -> dY9
+    if ((s = conv_dw(c, 10, A(A_F1), nullptr, gout))) return s;
+    if ((s = conv_dx(c, 10, gout, G(A_F1), nullptr, A(A_F1)))) return s;
+    if ((s = conv_dw(c, 9, A(A_8), nullptr, G(A_F1)))) return s;
+    if ((s = conv_dx(c, 9, G(A_F1), G(A_8), nullptr, A(A_8)))) return s;
+    // layer 8: input concat(u1 32, e1 16)
+    if ((s = conv_dw(c, 8, A(A_U1), A(A_E1), G(A_8)))) return s;
+    if ((s = conv_dx(c, 8, G(A_8), G(A_U1), G(A_0), nullptr))) return s;   // G(A_0) holds de1 (skip path)
+    // up1 backward: dF2 = 8 * down(dU1), masked by f2
+    if ((s = pool(c, G(A_U1), G(A_F2), 32, u->g[0], u->g[1], true, 8.0f))) return s;
+    if ((s = add_mask(c, G(A_F2), nullptr, A(A_F2), G(A_F2), n2 * 32))) return s;
+    if ((s = conv_dw(c, 7, A(A_6), nullptr, G(A_F2)))) return s;
+    if ((s = conv_dx(c, 7, G(A_F2), G(A_6), nullptr, A(A_6)))) return s;
+    // layer 6: input concat(u2 64, e2 32)
+    if ((s = conv_dw(c, 6, A(A_U2), A(A_E2), G(A_6)))) return s;
+    if ((s = conv_dx(c, 6, G(A_6), G(A_U2), G(A_2), nullptr))) return s;    // G(A_2) holds de2 (skip path)
+    // up2 backward: dE3 = 8 * down(dU2), masked by e3
+    if ((s = pool(c, G(A_U2), G(A_E3), 64, u->g[1], u->g[2], true, 8.0f))) return s;
+    if ((s = add_mask(c, G(A_E3), nullptr, A(A_E3), G(A_E3), n3 * 64))) return s;
+    if ((s = conv_dw(c, 5, A(A_4), nullptr, G(A_E3)))) return s;
+    if ((s = conv_dx(c, 5, G(A_E3), G(A_4), nullptr, A(A_4)))) return s;
+    if ((s = conv_dw(c, 4, A(A_P2), nullptr, G(A_4)))) return s;
+    if ((s = conv_dx(c, 4, G(A_4), G(A_P2), nullptr, nullptr))) return s;
+    // pool2 backward: dE2 += up(dP2) / 8; then mask by e2
+    if ((s = pool(c, G(A_P2), G(A_E2), 32, u->g[2], u->g[1], false, 0.125f))) return s;
+    if ((s = add_mask(c, G(A_E2), G(A_2), A(A_E2), G(A_E2), n2 * 32))) return s;
+    if ((s = conv_dw(c, 3, A(A_2), nullptr, G(A_E2)))) return s;
+    if ((s = conv_dx(c, 3, G(A_E2), G(A_2), nullptr, A(A_2)))) return s;
+    if ((s = conv_dw(c, 2, A(A_P1), nullptr, G(A_2)))) return s;
+    if ((s = conv_dx(c, 2, G(A_2), G(A_P1), nullptr, nullptr))) return s;
+    // pool1 backward: dE1 = up(dP1) / 8 + de1 (skip), masked by e1
+    if ((s = pool(c, G(A_P1), G(A_E1), 16, u->g[1], u->g[0], false, 0.125f))) return s;
+    if ((s = add_mask(c, G(A_E1), G(A_0), A(A_E1), G(A_E1), n1 * 16))) return s;
+    if ((s = conv_dw(c, 1, A(A_0), nullptr, G(A_E1)))) return s;
+    if ((s = conv_dx(c, 1, G(A_E1), G(A_0), nullptr, A(A_0)))) return s;
+    if ((s = conv_dw(c, 0, A(A_X0), nullptr, G(A_0)))) return s;
+    return SARAS_OK;
+}
+
+static L0View l0view(const Ctx &c, const double *p) {
+    L0View v;
+    v.p = p;
+    for (int d = 0; d < 3; ++d) v.n[d] = c.lv[0].n[d];
+    return v;
+}
+
+static int ensure_hist(Ctx &c) {
+    if (c.pHist[0]) return SARAS_OK;
+    size_t bytes = sizeof(double) * c.lv[0].count;
+    for (int q = 0; q < 2; ++q) {
+        SARAS_CUDA_TRY(cudaMalloc(&c.pHist[q], bytes));
+        SARAS_CUDA_TRY(cudaMemsetAsync(c.pHist[q], 0, bytes, c.stream));
+    }
+    return SARAS_OK;
+}
+
+// Scales s_b = max|b|, s_p = max|P_{n-1}| of the current solve (device).
+static int compute_scales(Ctx &c, const double *b) {
+    UNet *u = U(c);
+    SARAS_CUDA_TRY(cudaMemsetAsync(u->scales, 0, sizeof(double) * 2, c.stream));
+    k_maxabs_core<<<304, 256, 0, c.stream>>>(l0view(c, b), u->scales);
+    k_maxabs_core<<<304, 256, 0, c.stream>>>(l0view(c, c.pHist[0]), u->scales + 1);
+    k_floor_scale<<<1, 32, 0, c.stream>>>(u->scales, 1e-300);
+    count_launch(c, 3);
+    return ucheck(c, "scales");
 }
 
 }  // namespace saras
+
+// ------------------------------------------------------------------ solver hooks
+namespace saras {
+
+// Called at the start of a target-mode solve: rotate the pressure history.
+int unet_begin_solve(Ctx &c) {
+    int s = ensure_hist(c);
+    if (s) return s;
+    std::swap(c.pHist[0], c.pHist[1]);
+    SARAS_CUDA_TRY(cudaMemcpyAsync(c.pHist[0], c.f[SARAS_FIELD_PP], sizeof(double) * c.lv[0].count, cudaMemcpyDeviceToDevice, c.stream));
+    c.histCount += 1;
+    return SARAS_OK;
+}
+
+// Build the learned (or extrapolated) guess for the level-0 iterate into `dst`;
+// b is the compatible right-hand side.  Returns BAD_CONFIG if unavailable.
+int unet_guess(Ctx &c, const double *b, double *dst, bool use_net) {
+    if (c.histCount < 2) return SARAS_BAD_CONFIG;
+    int s;
+    if (use_net) {
+        if (!c.unet || !U(c)->trained) return SARAS_BAD_CONFIG;
+        UNet *u = U(c);
+        if ((s = compute_scales(c, b))) return s;
+        long n1 = u->g[0].n();
+        k_features<<<(int)((n1 + 255) / 256), 256, 0, c.stream>>>(l0view(c, b), l0view(c, c.pHist[0]), l0view(c, c.pHist[1]),
+                                                                  l0view(c, c.pHist[0]), u->g[0], u->scales, u->feat, nullptr);
+        k_expand<<<(int)((n1 * 16 + 255) / 256), 256, 0, c.stream>>>(u->feat, u->x0, n1);
+        count_launch(c, 2);
+        if ((s = unet_forward(c))) return s;
+    }
+    UNet *u = U(c);
+    const Level &L0 = c.lv[0];
+    dim3 b2(64, 4), g2((L0.n[2] + 1 + 63) / 64, (L0.n[1] + 1 + 3) / 4, L0.n[0] + 1);
+    Grid3 g1 = u ? u->g[0] : Grid3{1, 1, 1};
+    k_apply_guess<<<g2, b2, 0, c.stream>>>(dst, l0view(c, c.pHist[0]), l0view(c, c.pHist[1]), use_net ? u->out : nullptr, g1,
+                                           use_net ? u->scales : nullptr, use_net ? 1 : 0, c.p.xPer, c.p.yPer, c.p.zPer);
+    count_launch(c);
+    return ucheck(c, "guess");
+}
+
+int unet_collect_sample(Ctx &c, const double *b) {
+    int s = unet_alloc(c);
+    if (s) return s;
+    if (c.histCount < 2) return SARAS_OK;
+    UNet *u = U(c);
+    long n1 = u->g[0].n();
+    float *dst;
+    if (u->nsamples < u->cap) {
+        SARAS_CUDA_TRY(cudaMalloc(&dst, sizeof(float) * 4 * n1));
+        u->samples.push_back(dst);
+        u->nsamples += 1;
+    } else {
+        dst = u->samples[u->next];
+        u->next = (u->next + 1) % u->cap;
+    }
+    if ((s = compute_scales(c, b))) return s;
+    k_features<<<(int)((n1 + 255) / 256), 256, 0, c.stream>>>(l0view(c, b), l0view(c, c.pHist[0]), l0view(c, c.pHist[1]),
+                                                              l0view(c, c.f[SARAS_FIELD_PP]), u->g[0], u->scales, dst, dst + 3 * n1);
+    count_launch(c);
+    return ucheck(c, "collect");
+}
+
+int unet_collect(Ctx &c) {
+    int s = unet_alloc(c);
+    if (s) return s;
+    c.collecting = true;
+    return SARAS_OK;
+}
+
+int unet_train(Ctx &c, int iters, double lr, double *loss) {
+    int s = unet_alloc(c);
+    if (s) return s;
+    UNet *u = U(c);
+    c.collecting = false;
+    if (u->nsamples == 0) { c.err = "no training pairs collected"; return SARAS_BAD_CONFIG; }
+    long n1 = u->g[0].n();
+    int nb = (int)((n1 + 255) / 256);
+    double last = 0.0;
+    SARAS_CUDA_TRY(cudaMemsetAsync(u->err, 0, sizeof(int), c.stream));
+    for (int it = 0; it < iters; ++it) {
+        if ((s = pack_all(c))) return s;
+        const float *smp = u->samples[it % u->nsamples];
+        k_expand<<<(int)((n1 * 16 + 255) / 256), 256, 0, c.stream>>>(smp, u->x0, n1);
+        count_launch(c);
+        if ((s = unet_forward(c))) return s;
+        k_loss<<<nb, 256, 0, c.stream>>>(u->out, smp + 3 * n1, u->grd[A_X0], n1, u->part);
+        count_launch(c);
+        if (it == iters - 1) {
+            k_final_reduce<<<1, 256, 0, c.stream>>>(u->part, nb, 0, u->scales + 2);
+            count_launch(c);
+        }
+        if ((s = unet_backward(c, u->grd[A_X0]))) return s;
+        u->adam_t += 1;
+        float b1 = 0.9f, b2 = 0.999f;
+        float c1 = 1.0f - std::pow(b1, (float)u->adam_t), c2 = 1.0f - std::pow(b2, (float)u->adam_t);
+        k_adam<<<(int)((u->nparam + 255) / 256), 256, 0, c.stream>>>(u->param, u->grad, u->adam_m, u->adam_v, u->nparam, (float)lr, b1, b2,
+                                                                      1e-8f, c1, c2);
+        count_launch(c);
+    }
+    if ((s = pack_all(c))) return s;
+    int herr = 0;
+    SARAS_CUDA_TRY(cudaMemcpyAsync(&herr, u->err, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    SARAS_CUDA_TRY(cudaMemcpyAsync(&last, u->scales + 2, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    SARAS_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    if (herr) { c.err = "tensor-core convolution timed out waiting on an mbarrier"; return SARAS_CUDA_ERROR; }
+    u->trained = true;
+    if (loss) *loss = last;
+    return SARAS_OK;
+}
+
+int unet_infer(Ctx &c, double *out) {
+    return unet_guess(c, c.lv[0].r, out, true);
+}
+
+}  // namespace saras
+
+// ------------------------------------------------------------------ stand-alone convolution check
+namespace saras {
+
+__global__ void k_bf16_to_f32(const bf16 *a, float *b, long n) {
+    long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (t < n) b[t] = __bfloat162float(a[t]);
+}
+
+int conv3d_check(int mode, int D, int H, int W, int cin, int cout, const unsigned short *x, const unsigned short *dy,
+                 const float *w, const float *bias, int relu, float *out) {
+    if (D < 1 || H < 1 || W < 1 || cin % 16 || cout % 16 || cin < 16 || cout < 16 || cin > 96 || cout > 96) return SARAS_BAD_ARG;
+    if ((long)D * H * W > (1L << 24)) return SARAS_TOO_LARGE;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { cudaGetLastError(); set_error("no CUDA device"); return SARAS_NO_DEVICE; }
+    Ctx c;   // scratch context: stream + launch accounting only
+    c.stream = 0;
+    long nv = (long)D * H * W;
+    bf16 *dx = nullptr, *ddy = nullptr, *dout = nullptr, *wf = nullptr, *wt = nullptr;
+    float *dw = nullptr, *dbias = nullptr, *dgrad = nullptr, *dout32 = nullptr;
+    int *derr = nullptr;
+    int s = SARAS_OK;
+    auto fail = [&](cudaError_t e) { set_error(cudaGetErrorString(e)); s = SARAS_CUDA_ERROR; };
+    cudaError_t e;
+    size_t wbytes = sizeof(float) * 27L * cin * cout;
+    if ((e = cudaMalloc(&dx, sizeof(bf16) * nv * cin)) || (e = cudaMalloc(&ddy, sizeof(bf16) * nv * cout)) ||
+        (e = cudaMalloc(&dout, sizeof(bf16) * nv * std::max(cin, cout))) || (e = cudaMalloc(&wf, sizeof(bf16) * 27L * cin * cout)) ||
+        (e = cudaMalloc(&wt, sizeof(bf16) * 27L * cin * cout)) || (e = cudaMalloc(&dw, wbytes)) || (e = cudaMalloc(&dbias, sizeof(float) * cout)) ||
+        (e = cudaMalloc(&dgrad, wbytes + sizeof(float) * cout)) || (e = cudaMalloc(&dout32, sizeof(float) * nv * std::max(cin, cout))) ||
+        (e = cudaMalloc(&derr, sizeof(int)))) {
+        fail(e);
+    }
+    if (!s) {
+        cudaMemset(derr, 0, sizeof(int));
+        if (x) cudaMemcpy(dx, x, sizeof(bf16) * nv * cin, cudaMemcpyHostToDevice);
+        else cudaMemset(dx, 0, sizeof(bf16) * nv * cin);
+        if (dy) cudaMemcpy(ddy, dy, sizeof(bf16) * nv * cout, cudaMemcpyHostToDevice);
+        else cudaMemset(ddy, 0, sizeof(bf16) * nv * cout);
+        cudaMemcpy(dw, w, wbytes, cudaMemcpyHostToDevice);
+        if (bias) cudaMemcpy(dbias, bias, sizeof(float) * cout, cudaMemcpyHostToDevice);
+        else cudaMemset(dbias, 0, sizeof(float) * cout);
+        long total = 27L * cin * cout;
+        k_pack_weights<<<(int)((total + 255) / 256), 256>>>(dw, wf, cin, cout, 0);
+        k_pack_weights<<<(int)((total + 255) / 256), 256>>>(dw, wt, cin, cout, 1);
+        ConvArgs a;
+        std::memset(&a, 0, sizeof(a));
+        a.D = D; a.H = H; a.W = W; a.nvox = (int)nv; a.err = derr;
+        if (mode == 0) {
+            a.in0 = dx; a.c0 = cin; a.wpk = wf; a.bias = dbias; a.out0 = dout; a.split = cout; a.relu = relu;
+            s = launch_conv(c, cout, a);
+            if (!s) k_bf16_to_f32<<<(int)((nv * cout + 255) / 256), 256>>>(dout, dout32, nv * cout);
+            if (!s && (e = cudaMemcpy(out, dout32, sizeof(float) * nv * cout, cudaMemcpyDeviceToHost))) fail(e);
+        } else if (mode == 1) {
+            a.in0 = ddy; a.c0 = cout; a.wpk = wt; a.out0 = dout; a.split = cin;
+            s = launch_conv(c, cin, a);
+            if (!s) k_bf16_to_f32<<<(int)((nv * cin + 255) / 256), 256>>>(dout, dout32, nv * cin);
+            if (!s && (e = cudaMemcpy(out, dout32, sizeof(float) * nv * cin, cudaMemcpyDeviceToHost))) fail(e);
+        } else if (mode == 2) {
+            cudaMemset(dgrad, 0, wbytes + sizeof(float) * cout);
+            Grid3 g{D, H, W};
+            dim3 grid((unsigned)((nv + kDwChunk - 1) / kDwChunk), 27);
+            k_conv_dw<<<grid, 256, sizeof(float) * kDwSub * (cin + cout)>>>(dx, nullptr, cin, 0, ddy, cout, g, dgrad, dgrad + 27L * cin * cout);
+            if ((e = cudaGetLastError()) || (e = cudaMemcpy(out, dgrad, wbytes + sizeof(float) * cout, cudaMemcpyDeviceToHost))) fail(e);
+        } else {
+            s = SARAS_BAD_ARG;
+        }
+        int herr = 0;
+        if (!s && (e = cudaMemcpy(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost))) fail(e);
+        if (!s && herr) { set_error("tensor-core convolution timed out on an mbarrier"); s = SARAS_CUDA_ERROR; }
+        if (!s && (e = cudaDeviceSynchronize())) fail(e);
+    }
+    cudaFree(dx); cudaFree(ddy); cudaFree(dout); cudaFree(wf); cudaFree(wt); cudaFree(dw); cudaFree(dbias);
+    cudaFree(dgrad); cudaFree(dout32); cudaFree(derr);
+    return s;
+}
+
+}  // namespace saras
+
+extern "C" int saras_conv3d_check(int mode, int D, int H, int W, int cin, int cout, const unsigned short *x,
+                                  const unsigned short *dy, const float *w, const float *bias, int relu, float *out) {
+    return saras::conv3d_check(mode, D, H, W, cin, cout, x, dy, w, bias, relu, out);
+}
