@@ -209,18 +209,24 @@ __device__ __forceinline__ double fw_restrict(const L0View &f, int z, int y, int
     return s;
 }
 
-// Sample features (3 FP32 channels) and, with `target`, the training target
-// d* = R(P_new - 2 P1 + P2) / s_p.
-__global__ void k_features(L0View b, L0View p1, L0View p2, L0View pnew, Grid3 g1, const double *scales, float *feat, float *target) {
+// Sample features at level 1 (3 FP32 channels), all derived from the
+// divergence b and the previous two pressures P1, P2:
+//   0: R(r_ex) / s_r   residual of the extrapolated guess 2 P1 - P2
+//   1: R(P1 - P2) / s_d
+//   2: R(b) / s_b
+// and, with `target`, the training target d* = R(P_new - (2 P1 - P2)) / s_d.
+// scales = {s_b, s_d, s_r}.
+__global__ void k_features(L0View b, L0View p1, L0View p2, L0View rex, L0View pnew, Grid3 g1, const double *scales, float *feat,
+                           float *target) {
     long v = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (v >= g1.n()) return;
     int x = (int)(v % g1.W), y = (int)((v / g1.W) % g1.H), z = (int)(v / ((long)g1.W * g1.H));
-    double sb = scales[0], sp = scales[1];
-    double rb = fw_restrict(b, z, y, x), r1 = fw_restrict(p1, z, y, x), r2 = fw_restrict(p2, z, y, x);
-    feat[v * 3 + 0] = (float)(rb / sb);
-    feat[v * 3 + 1] = (float)(r1 / sp);
-    feat[v * 3 + 2] = (float)(r2 / sp);
-    if (target) target[v] = (float)((fw_restrict(pnew, z, y, x) - 2.0 * r1 + r2) / sp);
+    double sb = scales[0], sd = scales[1], sr = scales[2];
+    double r1 = fw_restrict(p1, z, y, x), r2 = fw_restrict(p2, z, y, x);
+    feat[v * 3 + 0] = (float)(fw_restrict(rex, z, y, x) / sr);
+    feat[v * 3 + 1] = (float)((r1 - r2) / sd);
+    feat[v * 3 + 2] = (float)(fw_restrict(b, z, y, x) / sb);
+    if (target) target[v] = (float)((fw_restrict(pnew, z, y, x) - (2.0 * r1 - r2)) / sd);
 }
 
 // Expand 3-channel FP32 features into the 16-channel BF16 network input.
@@ -286,6 +292,33 @@ __global__ void k_apply_guess(double *out, L0View p1, L0View p2, const float *d,
     }
 }
 
+// Binomial low-pass filter ([1,2,1]/4 per axis, weights renormalised at the
+// domain edge) of the network output: multigrid removes high-frequency error
+// by itself, and BF16 rounding noise in the correction would otherwise show up
+// amplified by the Laplacian in the residual of the guess.
+__global__ void k_lowpass(const float *in, float *out, Grid3 g) {
+    long v = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (v >= g.n()) return;
+    int x = (int)(v % g.W), y = (int)((v / g.W) % g.H), z = (int)(v / ((long)g.W * g.H));
+    float s = 0.0f, w = 0.0f;
+    for (int dz = -1; dz <= 1; ++dz) {
+        int zz = z + dz;
+        if (zz < 0 || zz >= g.D) continue;
+        for (int dy = -1; dy <= 1; ++dy) {
+            int yy = y + dy;
+            if (yy < 0 || yy >= g.H) continue;
+            for (int dx = -1; dx <= 1; ++dx) {
+                int xx = x + dx;
+                if (xx < 0 || xx >= g.W) continue;
+                float wt = fw1(dz) * fw1(dy) * fw1(dx);
+                s += wt * in[((long)zz * g.H + yy) * g.W + xx];
+                w += wt;
+            }
+        }
+    }
+    out[v] = s / w;
+}
+
 __global__ void k_maxabs_core(L0View f, double *out) {
     long n = (long)(f.n[0] + 1) * (f.n[1] + 1) * (f.n[2] + 1);
     double m = 0.0;
@@ -296,11 +329,33 @@ __global__ void k_maxabs_core(L0View f, double *out) {
     block_max_to(m, out);
 }
 
-__global__ void k_floor_scale(double *s, double floor_) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        if (!(s[0] > floor_)) s[0] = floor_;
-        if (!(s[1] > floor_)) s[1] = floor_;
+__global__ void k_maxabs_diff(L0View a, L0View b, double *out) {
+    long n = (long)(a.n[0] + 1) * (a.n[1] + 1) * (a.n[2] + 1);
+    double m = 0.0;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+        int k = (int)(t % (a.n[2] + 1)), j = (int)((t / (a.n[2] + 1)) % (a.n[1] + 1)), i = (int)(t / ((long)(a.n[2] + 1) * (a.n[1] + 1)));
+        m = fmax(m, fabs(a.at(i, j, k) - b.at(i, j, k)));
     }
+    block_max_to(m, out);
+}
+
+__global__ void k_floor_scale(double *s, double floor_) {
+    if (threadIdx.x == 0 && blockIdx.x == 0)
+        for (int q = 0; q < 3; ++q)
+            if (!(s[q] > floor_)) s[q] = floor_;
+}
+
+// r = b - Lap(p) over the level-0 core (FP64), uniform-grid Laplacian.
+__global__ void k_residual64(double *r, L0View p, L0View b, double lx, double ly, double lz) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y * blockDim.y + threadIdx.y;
+    int i = blockIdx.z;
+    if (i > p.n[0] || j > p.n[1] || k > p.n[2]) return;
+    double C = p.at(i, j, k);
+    double lap = lx * (p.at(i + 1, j, k) + p.at(i - 1, j, k)) + ly * (p.at(i, j + 1, k) + p.at(i, j - 1, k)) +
+                 lz * (p.at(i, j, k + 1) + p.at(i, j, k - 1)) - 2.0 * (lx + ly + lz) * C;
+    long sy = p.n[2] + 3, sx = (long)(p.n[1] + 3) * sy;
+    r[(long)(i + 1) * sx + (long)(j + 1) * sy + (k + 1)] = b.at(i, j, k) - lap;
 }
 
 // ------------------------------------------------------------------ host: network
@@ -321,7 +376,8 @@ struct UNet {
     std::vector<bf16 *> grd;          // gradient buffers
     bf16 *x0 = nullptr;
     float *out = nullptr, *feat = nullptr;
-    double *scales = nullptr;         // s_b, s_p (device)
+    double *scales = nullptr;         // s_b, s_d, s_r, last loss (device)
+    double *ext = nullptr, *rex = nullptr;   // level-0 extrapolated guess and its residual
     // training samples: 3 feature channels + target per voxel
     std::vector<float *> samples;
     int nsamples = 0, cap = 0, next = 0;
@@ -430,6 +486,10 @@ static int unet_alloc(Ctx &c) {
     SARAS_CUDA_TRY(cudaMalloc(&u->out, sizeof(float) * n1));
     SARAS_CUDA_TRY(cudaMalloc(&u->feat, sizeof(float) * 4 * n1));
     SARAS_CUDA_TRY(cudaMalloc(&u->scales, sizeof(double) * 4));
+    SARAS_CUDA_TRY(cudaMalloc(&u->ext, sizeof(double) * c.lv[0].count));
+    SARAS_CUDA_TRY(cudaMalloc(&u->rex, sizeof(double) * c.lv[0].count));
+    SARAS_CUDA_TRY(cudaMemset(u->ext, 0, sizeof(double) * c.lv[0].count));
+    SARAS_CUDA_TRY(cudaMemset(u->rex, 0, sizeof(double) * c.lv[0].count));
     SARAS_CUDA_TRY(cudaMalloc(&u->err, sizeof(int)));
     SARAS_CUDA_TRY(cudaMemset(u->err, 0, sizeof(int)));
     SARAS_CUDA_TRY(cudaMalloc(&u->part, sizeof(double) * ((n1 + 255) / 256 + 1)));
@@ -446,6 +506,7 @@ void unet_free(Ctx &c) {
     for (bf16 *p : u->grd) cudaFree(p);
     for (float *p : u->samples) cudaFree(p);
     cudaFree(u->out); cudaFree(u->feat); cudaFree(u->scales); cudaFree(u->err); cudaFree(u->part);
+    cudaFree(u->ext); cudaFree(u->rex);
     delete u;
     c.unet = nullptr;
 }
@@ -615,15 +676,26 @@ static int ensure_hist(Ctx &c) {
     return SARAS_OK;
 }
 
-// Scales s_b = max|b|, s_p = max|P_{n-1}| of the current solve (device).
-static int compute_scales(Ctx &c, const double *b) {
+// Extrapolated guess 2 P1 - P2, its FP64 residual against b, and the scales
+// s_b = max|b|, s_d = max|P1 - P2|, s_r = max|r_ex| (device).
+static int prepare_features(Ctx &c, const double *b, const double *pnew, float *feat, float *target) {
     UNet *u = U(c);
-    SARAS_CUDA_TRY(cudaMemsetAsync(u->scales, 0, sizeof(double) * 2, c.stream));
+    const Level &L0 = c.lv[0];
+    dim3 b2(64, 4), g2((L0.n[2] + 1 + 63) / 64, (L0.n[1] + 1 + 3) / 4, L0.n[0] + 1);
+    k_apply_guess<<<g2, b2, 0, c.stream>>>(u->ext, l0view(c, c.pHist[0]), l0view(c, c.pHist[1]), nullptr, u->g[0], nullptr, 0,
+                                           c.p.xPer, c.p.yPer, c.p.zPer);
+    k_residual64<<<g2, b2, 0, c.stream>>>(u->rex, l0view(c, u->ext), l0view(c, b), L0.lx, L0.ly, L0.lz);
+    SARAS_CUDA_TRY(cudaMemsetAsync(u->scales, 0, sizeof(double) * 3, c.stream));
     k_maxabs_core<<<304, 256, 0, c.stream>>>(l0view(c, b), u->scales);
-    k_maxabs_core<<<304, 256, 0, c.stream>>>(l0view(c, c.pHist[0]), u->scales + 1);
+    k_maxabs_diff<<<304, 256, 0, c.stream>>>(l0view(c, c.pHist[0]), l0view(c, c.pHist[1]), u->scales + 1);
+    k_maxabs_core<<<304, 256, 0, c.stream>>>(l0view(c, u->rex), u->scales + 2);
     k_floor_scale<<<1, 32, 0, c.stream>>>(u->scales, 1e-300);
-    count_launch(c, 3);
-    return ucheck(c, "scales");
+    long n1 = u->g[0].n();
+    k_features<<<(int)((n1 + 255) / 256), 256, 0, c.stream>>>(l0view(c, b), l0view(c, c.pHist[0]), l0view(c, c.pHist[1]),
+                                                              l0view(c, u->rex), l0view(c, pnew ? pnew : c.pHist[0]), u->g[0],
+                                                              u->scales, feat, target);
+    count_launch(c, 7);
+    return ucheck(c, "features");
 }
 
 }  // namespace saras
@@ -649,13 +721,15 @@ int unet_guess(Ctx &c, const double *b, double *dst, bool use_net) {
     if (use_net) {
         if (!c.unet || !U(c)->trained) return SARAS_BAD_CONFIG;
         UNet *u = U(c);
-        if ((s = compute_scales(c, b))) return s;
+        if ((s = prepare_features(c, b, nullptr, u->feat, nullptr))) return s;
         long n1 = u->g[0].n();
-        k_features<<<(int)((n1 + 255) / 256), 256, 0, c.stream>>>(l0view(c, b), l0view(c, c.pHist[0]), l0view(c, c.pHist[1]),
-                                                                  l0view(c, c.pHist[0]), u->g[0], u->scales, u->feat, nullptr);
         k_expand<<<(int)((n1 * 16 + 255) / 256), 256, 0, c.stream>>>(u->feat, u->x0, n1);
-        count_launch(c, 2);
+        count_launch(c);
         if ((s = unet_forward(c))) return s;
+        // two low-pass passes (out -> feat -> out; feat is free after the forward pass)
+        k_lowpass<<<(int)((n1 + 255) / 256), 256, 0, c.stream>>>(u->out, u->feat, u->g[0]);
+        k_lowpass<<<(int)((n1 + 255) / 256), 256, 0, c.stream>>>(u->feat, u->out, u->g[0]);
+        count_launch(c, 2);
     }
     UNet *u = U(c);
     const Level &L0 = c.lv[0];
@@ -670,7 +744,9 @@ int unet_guess(Ctx &c, const double *b, double *dst, bool use_net) {
 int unet_collect_sample(Ctx &c, const double *b) {
     int s = unet_alloc(c);
     if (s) return s;
-    if (c.histCount < 2) return SARAS_OK;
+    // the first solves of a run are the start-up transient of the pressure
+    // correction; pairs are taken once two earlier corrections exist beyond it
+    if (c.histCount < 4) return SARAS_OK;
     UNet *u = U(c);
     long n1 = u->g[0].n();
     float *dst;
@@ -682,10 +758,7 @@ int unet_collect_sample(Ctx &c, const double *b) {
         dst = u->samples[u->next];
         u->next = (u->next + 1) % u->cap;
     }
-    if ((s = compute_scales(c, b))) return s;
-    k_features<<<(int)((n1 + 255) / 256), 256, 0, c.stream>>>(l0view(c, b), l0view(c, c.pHist[0]), l0view(c, c.pHist[1]),
-                                                              l0view(c, c.f[SARAS_FIELD_PP]), u->g[0], u->scales, dst, dst + 3 * n1);
-    count_launch(c);
+    if ((s = prepare_features(c, b, c.f[SARAS_FIELD_PP], dst, dst + 3 * n1))) return s;
     return ucheck(c, "collect");
 }
 
@@ -715,7 +788,7 @@ int unet_train(Ctx &c, int iters, double lr, double *loss) {
         k_loss<<<nb, 256, 0, c.stream>>>(u->out, smp + 3 * n1, u->grd[A_X0], n1, u->part);
         count_launch(c);
         if (it == iters - 1) {
-            k_final_reduce<<<1, 256, 0, c.stream>>>(u->part, nb, 0, u->scales + 2);
+            k_final_reduce<<<1, 256, 0, c.stream>>>(u->part, nb, 0, u->scales + 3);
             count_launch(c);
         }
         if ((s = unet_backward(c, u->grd[A_X0]))) return s;
@@ -729,7 +802,7 @@ int unet_train(Ctx &c, int iters, double lr, double *loss) {
     if ((s = pack_all(c))) return s;
     int herr = 0;
     SARAS_CUDA_TRY(cudaMemcpyAsync(&herr, u->err, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
-    SARAS_CUDA_TRY(cudaMemcpyAsync(&last, u->scales + 2, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    SARAS_CUDA_TRY(cudaMemcpyAsync(&last, u->scales + 3, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     SARAS_CUDA_TRY(cudaStreamSynchronize(c.stream));
     if (herr) { c.err = "tensor-core convolution timed out waiting on an mbarrier"; return SARAS_CUDA_ERROR; }
     u->trained = true;
