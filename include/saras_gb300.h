@@ -172,6 +172,18 @@ int saras_axpby(saras_ctx *ctx, int dst, double a, int src, double b);
 /* hydro_d3::solveVx/Vy/Vz (hydro_d3.cc:370-533), scalar_d3::solveVx..solveT
  * (scalar_d3.cc:373-591).  component: 0,1,2 = Vx,Vy,Vz, 3 = T. */
 int saras_cn_solve(saras_ctx *ctx, int component, int *iters, double *max_error);
+/* Allocation-free variant of saras_cn_solve for callers that cannot allocate
+ * device memory when they need the solve (fixed memory budgets, pool
+ * allocators closed after start-up).  No counterpart in the reference.  v
+ * (in/out) and rhs are the caller's device arrays in the padded layout of the
+ * component; the second Jacobi iterate and the residual slot live in a fixed
+ * 32 MiB device array reserved by the library on every GPU that loads it, so
+ * padded fields above 4 Mi points (e.g. beyond 161^3) return SARAS_TOO_LARGE.
+ * The first call on a device resolves that array's address: make it before
+ * any stream capture.  Calls that overlap on the GPU share the array and race.
+ * stream may be NULL (legacy default stream). */
+int saras_cn_solve_noalloc(const saras_params *p, int component, double *v, const double *rhs, void *stream,
+                           int *iters, double *max_error);
 /* poisson::mgSolve(Pp, mgRHS) (poisson.cc:100-205). */
 int saras_mg_solve(saras_ctx *ctx, int *vcycles, double *residual);
 int saras_mg_set_mode(saras_ctx *ctx, int mode, double target, int max_cycles);

@@ -137,6 +137,7 @@ def load():
         "saras_tfield_compute_nlin": (_I, [vp]),
         "saras_axpby": (_I, [vp, _I, _D, _I, _D]),
         "saras_cn_solve": (_I, [vp, _I, ip, dp]),
+        "saras_cn_solve_noalloc": (_I, [P, _I, vp, vp, vp, ip, dp]),
         "saras_mg_solve": (_I, [vp, ip, dp]),
         "saras_mg_set_mode": (_I, [vp, _I, _D, _I]),
         "saras_time_advance": (_I, [vp, ctypes.POINTER(saras_step_stats)]),

@@ -1124,3 +1124,224 @@ int time_advance(Ctx &c, saras_step_stats *st) {
 }
 
 }  // namespace saras
+
+// ------------------------------------------------------------------ allocation-free Jacobi solve
+// Some callers cannot allocate device memory at the point where they need a
+// solve: a host application that hands the solver a fixed memory budget up
+// front, a caller running under a custom pool allocator that forbids further
+// cudaMalloc/cudaFree traffic once its simulation loop has started, or code
+// that must not change the device's allocation state between two checkpoints.
+// saras_cn_solve_noalloc serves them: the caller passes the velocity (or
+// temperature) array and the right-hand side in device memory, and the second
+// iterate plus the residual slot live in the fixed array below instead of in
+// memory from cudaMalloc.  The array is reserved on every GPU that loads the
+// library, for the life of the process, whether or not this entry point is
+// used.
+namespace saras {
+
+constexpr long kNoAllocMaxPoints = 4L << 20;   // 4 Mi doubles (32 MiB): padded field arrays up to this size
+static __device__ __align__(256) double g_cn_scratch[kNoAllocMaxPoints + 32];
+static double *g_cn_scratch_dev[64] = {nullptr};   // device address of g_cn_scratch, per device ordinal
+
+// The wall objects of walls_for(), written into a fixed array (no host heap use).
+static int walls_fixed(const saras_params &p, int field, Wall *w) {
+    int n = 0;
+    auto add = [&](WallKind k, int wall, double v) { w[n++] = Wall{k, wall, v}; };
+    if (field == SARAS_FIELD_VX) {
+        if (!p.xPer) { if (p.probType == 3) { add(W_DIR_FC, 0, 1.0); add(W_NEU, 1, 0.0); } else { add(W_DIR_FC, 0, 0.0); add(W_DIR_FC, 1, 0.0); } }
+        if (!p.yPer) { add(W_DIR_CC, 2, 0.0); add(W_DIR_CC, 3, 0.0); }
+        if (p.zPer) { add(W_PER_CC, 5, 0); add(W_PER_CC, 4, 0); }
+        else if (p.probType == 1) { add(W_DIR_CC, 5, 1.0); add(W_DIR_CC, 4, 0.0); }
+        else { add(W_DIR_CC, 5, 0.0); add(W_DIR_CC, 4, 0.0); }
+    } else if (field == SARAS_FIELD_VY) {
+        if (!p.xPer) { if (p.probType == 3) { add(W_DIR_CC, 0, 0.0); add(W_NEU, 1, 0.0); } else { add(W_DIR_CC, 0, 0.0); add(W_DIR_CC, 1, 0.0); } }
+        if (!p.yPer) { add(W_DIR_FC, 2, 0.0); add(W_DIR_FC, 3, 0.0); }
+        if (p.zPer) { add(W_PER_CC, 5, 0); add(W_PER_CC, 4, 0); }
+        else { add(W_DIR_CC, 5, 0.0); add(W_DIR_CC, 4, 0.0); }
+    } else if (field == SARAS_FIELD_VZ) {
+        if (!p.xPer) { if (p.probType == 3) { add(W_DIR_CC, 0, 0.0); add(W_NEU, 1, 0.0); } else { add(W_DIR_CC, 0, 0.0); add(W_DIR_CC, 1, 0.0); } }
+        if (!p.yPer) { add(W_DIR_CC, 2, 0.0); add(W_DIR_CC, 3, 0.0); }
+        if (p.zPer) { add(W_PER_FC, 5, 0); add(W_PER_FC, 4, 0); }
+        else { add(W_DIR_FC, 5, 0.0); add(W_DIR_FC, 4, 0.0); }
+    } else {
+        if (!p.xPer) {
+            if (p.probType == 5 || p.probType == 6 || p.probType == 8) { add(W_NEU, 0, 0.0); add(W_NEU, 1, 0.0); }
+            else if (p.probType == 7) { add(W_DIR_CC, 0, 1.0); add(W_DIR_CC, 1, 0.0); }
+        }
+        if (!p.yPer) { add(W_NEU, 2, 0.0); add(W_NEU, 3, 0.0); }
+        if (p.zPer) { add(W_PER_CC, 5, 0); add(W_PER_CC, 4, 0); }
+        else if (p.probType == 5 || p.probType == 8) { add(W_DIR_CC, 5, 0.0); add(W_DIR_CC, 4, 1.0); }
+        else if (p.probType == 6) { add(W_DIR_CC, 5, 1.0); add(W_DIR_CC, 4, 0.0); }
+    }
+    return n;
+}
+
+}  // namespace saras
+
+// The same Jacobi iteration as saras_cn_solve (same kernels, same stopping
+// rule and iteration cap), on caller-owned device arrays v (in: current
+// iterate with its boundary values, out: solution) and rhs.  Nothing is
+// allocated.  The first call on a device looks up the device address of the
+// scratch array; make that first call before any stream capture.  Every call
+// shares the one array, so calls that overlap on the GPU (other streams,
+// other host threads) race: order them on one stream or serialise them.
+extern "C" int saras_cn_solve_noalloc(const saras_params *p, int component, double *v, const double *rhs, void *stream,
+                                      int *iters, double *max_error) {
+    using namespace saras;
+    if (!p || !v || !rhs) return SARAS_BAD_ARG;
+    bool scalar = p->probType >= 5;
+    if (component < 0 || component > 3 || (component == 3 && !scalar)) return SARAS_BAD_ARG;
+    if (p->xGrid || p->yGrid || p->zGrid || p->xInd < 2 || p->yInd < 2 || p->zInd < 2 || p->xInd > 11 || p->yInd > 11 || p->zInd > 11)
+        return SARAS_BAD_CONFIG;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); set_error("no CUDA device"); return SARAS_NO_DEVICE; }
+    if (dev < 0 || dev >= 64) { set_error("device ordinal beyond 63"); return SARAS_BAD_ARG; }
+    if (!g_cn_scratch_dev[dev]) {
+        double *ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress((void **)&ptr, g_cn_scratch);
+        if (e != cudaSuccess || !ptr) {
+            set_error(std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+            return SARAS_CUDA_ERROR;
+        }
+        g_cn_scratch_dev[dev] = ptr;
+    }
+    double *scratch = g_cn_scratch_dev[dev];
+    double *resSlot = scratch + kNoAllocMaxPoints;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+
+    // grid constants (grid.cc:84-86, 405-421; hydro.cc:223-241)
+    int ind[3] = {p->xInd, p->yInd, p->zInd};
+    double L[3] = {p->Lx, p->Ly, p->Lz};
+    double dXi[3], m2[3];
+    int Ns[3], Nc[3];
+    for (int d = 0; d < 3; ++d) {
+        Ns[d] = int(std::pow(2, ind[d])) + 1;
+        Nc[d] = Ns[d] - 1;
+        dXi[d] = 1.0 / double(Ns[d] - 1);
+        m2[d] = std::pow(1.0 / L[d], 2.0);
+    }
+    double hz2hx2 = std::pow(dXi[2], 2.0) * std::pow(dXi[0], 2.0);
+    double hx2hy2 = std::pow(dXi[0], 2.0) * std::pow(dXi[1], 2.0);
+    double hy2hz2 = std::pow(dXi[1], 2.0) * std::pow(dXi[2], 2.0);
+    double hx2hy2hz2 = std::pow(dXi[0], 2.0) * std::pow(dXi[1], 2.0) * std::pow(dXi[2], 2.0);
+    int maxIterations = Nc[0] * Nc[1] * Nc[2];
+
+    // field layout, bulk box and boundary program (field.cc:66-290, hydro.cc:287-461)
+    int field = component == 3 ? SARAS_FIELD_T : SARAS_FIELD_VX + component;
+    bool stg[3] = {field != SARAS_FIELD_VX, field != SARAS_FIELD_VY, field != SARAS_FIELD_VZ};
+    bool per[3] = {p->xPer != 0, p->yPer != 0, p->zPer != 0};
+    FieldInfo f;
+    for (int d = 0; d < 3; ++d) {
+        f.stag[d] = stg[d];
+        f.n[d] = stg[d] ? Ns[d] : Nc[d];
+        f.blo[d] = 0; f.bhi[d] = f.n[d] - 1;
+        if (stg[d] && !per[d]) { f.blo[d] += 1; f.bhi[d] -= 1; }
+    }
+    long points = (long)(f.n[0] + 2) * (f.n[1] + 2) * (f.n[2] + 2);
+    if (points > kNoAllocMaxPoints) {
+        set_error("saras_cn_solve_noalloc: field of " + std::to_string(points) + " points exceeds the fixed scratch of " +
+                  std::to_string(kNoAllocMaxPoints) + " points; use saras_cn_solve");
+        return SARAS_TOO_LARGE;
+    }
+    f.full.nops = 0;
+    add_sync_ops(f.full, f, per[0], per[1]);
+    Wall walls[6];
+    int nw = walls_fixed(*p, field, walls);
+    for (int q = 0; q < nw; ++q) add_wall_op(f.full, f, walls[q]);
+    for (int d = 0; d < 3; ++d) { f.full.blo[d] = f.blo[d]; f.full.bhi[d] = f.bhi[d]; }
+
+    // coefficients, as in cn_solve
+    double nu = 0, kappa = 0;
+    if (scalar) {
+        if (p->rbcType == 1) { nu = p->Pr; kappa = 1.0; }
+        else if (p->rbcType == 3) { nu = 1.0; kappa = 1.0 / p->Pr; }
+        else { nu = std::sqrt(p->Pr / p->Ra); kappa = 1.0 / std::sqrt(p->Pr * p->Ra); }
+    }
+    CnArgs a;
+    {
+        View3<double> w = make_view<double>(const_cast<double *>(rhs), f.n[0], f.n[1], f.n[2]);
+        a.rhs.p = w.p; a.rhs.n[0] = w.n[0]; a.rhs.n[1] = w.n[1]; a.rhs.n[2] = w.n[2]; a.rhs.sx = w.sx; a.rhs.sy = w.sy;
+    }
+    a.prog = f.full;
+    Box fb; for (int d = 0; d < 3; ++d) { fb.lo[d] = -1; fb.ext[d] = f.n[d] + 2; }
+    a.full = fb;
+    a.c1 = hy2hz2 * m2[0]; a.c2 = hz2hx2 * m2[1]; a.c3 = hx2hy2 * m2[2];
+    double B = (hy2hz2 * m2[0] + hz2hx2 * m2[1]) + hx2hy2 * m2[2];
+    a.dt = p->tStp;
+    if (!scalar) {
+        a.scalarForm = 0; a.coef = 0;
+        a.X = hx2hy2hz2 * 2.0 * p->Re;
+        a.Dn = 1.0 + p->tStp * B / (p->Re * hx2hy2hz2);
+        a.resCoef = 1.0 / p->Re;
+    } else {
+        double coef = component == 3 ? kappa : nu;
+        a.scalarForm = 1; a.coef = coef;
+        a.X = hx2hy2hz2 * 2.0;
+        a.Dn = 1.0 + p->tStp * coef * B / hx2hy2hz2;
+        a.resCoef = coef;
+    }
+    a.lx = m2[0] * (1.0 / (dXi[0] * dXi[0]));
+    a.ly = m2[1] * (1.0 / (dXi[1] * dXi[1]));
+    a.lz = m2[2] * (1.0 / (dXi[2] * dXi[2]));
+    a.resMax = resSlot;
+    dim3 g, bl; box_launch_dims(fb, g, bl);
+
+    // the fused multiply-add form when the parameters ask for it, as cn_solve does
+    CnFast fa;
+    bool fast = p->fastKernels != 0;
+    if (fast) {
+        fa.rhs = a.rhs; fa.prog = a.prog; fa.full = a.full;
+        fa.c1 = a.c1; fa.c2 = a.c2; fa.c3 = a.c3;
+        fa.k1 = a.scalarForm ? (a.dt * a.coef) / a.X : a.dt / a.X;
+        fa.invDn = 1.0 / a.Dn;
+        fa.lx = a.lx; fa.ly = a.ly; fa.lz = a.lz;
+        fa.lc = -2.0 * (a.lx + a.ly + a.lz);
+        fa.k2 = 0.5 * a.dt * a.resCoef;
+        fa.resMax = a.resMax;
+    }
+    double *cur = v, *nxt = scratch;
+    auto view_of = [&](double *ptr) { return make_view<double>(ptr, f.n[0], f.n[1], f.n[2]); };
+    auto launch = [&](int withRes) {
+        View3<double> in = view_of(cur), out = view_of(nxt);
+        View3<const double> cin;
+        cin.p = in.p; cin.n[0] = in.n[0]; cin.n[1] = in.n[1]; cin.n[2] = in.n[2]; cin.sx = in.sx; cin.sy = in.sy;
+        if (fast) {
+            fa.in = cin; fa.out = out; fa.withResidual = withRes;
+            k_cn_fast<<<g, bl, 0, st>>>(fa);
+        } else {
+            a.in = cin; a.out = out; a.withResidual = withRes;
+            k_cn<<<g, bl, 0, st>>>(a);
+        }
+        return cudaGetLastError();
+    };
+    cudaError_t e = launch(0);
+    if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); return SARAS_CUDA_ERROR; }
+    std::swap(cur, nxt);
+    int sweeps = 1, failed = 0;
+    double res = 0.0;
+    int status = SARAS_OK;
+    while (true) {
+        if ((e = cudaMemsetAsync(resSlot, 0, sizeof(double), st)) != cudaSuccess) break;
+        if ((e = launch(1)) != cudaSuccess) break;
+        if ((e = cudaMemcpyAsync(&res, resSlot, sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess) break;
+        if ((e = cudaStreamSynchronize(st)) != cudaSuccess) break;
+        if (!std::isfinite(res)) { set_error("Jacobi residual is not finite"); status = SARAS_NOT_FINITE; break; }
+        if (res < p->cnTolerance) break;
+        failed += 1;
+        if (failed > maxIterations) { status = SARAS_NOT_CONVERGED; break; }
+        std::swap(cur, nxt);
+        sweeps += 1;
+    }
+    if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); return SARAS_CUDA_ERROR; }
+    // the answer is `cur`; bring it into the caller's array if it sits in the scratch
+    if (cur != v) {
+        if ((e = cudaMemcpyAsync(v, cur, sizeof(double) * points, cudaMemcpyDeviceToDevice, st)) != cudaSuccess ||
+            (e = cudaStreamSynchronize(st)) != cudaSuccess) {
+            set_error(cudaGetErrorString(e));
+            return SARAS_CUDA_ERROR;
+        }
+    }
+    if (iters) *iters = status == SARAS_NOT_CONVERGED ? failed : sweeps;
+    if (max_error) *max_error = res;
+    return status;
+}
