@@ -54,7 +54,7 @@ def tgv_params(mode, guess=0, ind=GRID_INDEX, depth=DEPTH):
     p.mgMaxCycles = 100
     p.mixedCycles = 1
     p.jacobiWeight = 6.0 / 7.0 if mode != _abi.MG_REFERENCE else 1.0
-    p.fastKernels = 1 if mode != _abi.MG_REFERENCE else 0
+    p.fastKernels = 2 if mode != _abi.MG_REFERENCE else 0
     p.guessMode = guess
     return p
 
@@ -204,6 +204,10 @@ def run_ours(args, dist):
                  "vcycles_per_step_warmup_previous_guess": sum(warm_vc[-5:]) / len(warm_vc[-5:])}
         g.set_guess_mode(F.GUESS_LEARNED)
         s, st = g.time_advance()
+    elif args.guess != "previous":
+        g.set_guess_mode({"extrapolate": F.GUESS_EXTRAPOLATE, "quadratic": F.GUESS_QUADRATIC}[args.guess])
+        for k in range(3):
+            g.time_advance()
     # pick the dominant kernel from one profiled step
     for k in range(len(names)):
         g.profile_enable(k, True)
@@ -321,10 +325,12 @@ def run_ours(args, dist):
             "workload": "Taylor-Green vortex 257^3 (2^8+1 vertex points per axis), [0,2pi]^3 PPP, Re 1600, dt 5e-4; "
                         "pressure solve: FP32 V(3,3) cycles inside FP64 iterative refinement to max|b-Ap|/max|b| <= 1e-8",
             "grid": [257, 257, 257], "vcycle_depth": DEPTH, "mg_mode": "mixed_fp32_in_fp64",
-            "warm_start": "unet (3-level 16/32/64, tcgen05 BF16 convs) with fallback to the previous pressure"
-                          if args.learned else "previous_pressure",
+            "warm_start": "unet (3-level 16/32/64, tcgen05 BF16 convs) correcting 2 Pp(n-1) - Pp(n-2), "
+                          "least-squares step length, fallback to the previous pressure"
+                          if args.learned else args.guess,
             "learned": learn,
-            "guess_sources_timed": {"network": src.count(1), "previous": src.count(0)},
+            "guess_sources_timed": {"previous": src.count(0), "network": src.count(1), "extrapolation": src.count(2),
+                                    "quadratic": src.count(3)},
             "residual_target": TARGET, "vcycles_per_step": sum(vc) / len(vc),
             "refine_steps_per_step": sum(rs) / len(rs), "max_fine_residual": max(fine),
             "plain_fp64": plain,
@@ -401,7 +407,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--learned", type=int, default=1)
+    ap.add_argument("--guess", default="learned", choices=["learned", "extrapolate", "quadratic", "previous"],
+                    help="initial guess of the pressure-correction solve in the timed steps")
     ap.add_argument("--collect", type=int, default=14)
     ap.add_argument("--train-iters", type=int, default=200)
     ap.add_argument("--lr", type=float, default=2e-3)
@@ -412,6 +419,7 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    args.learned = args.guess == "learned"
     dist = Dist()
     try:
         out = run_reference(args, dist) if args.impl == "reference" else run_ours(args, dist)

@@ -64,7 +64,8 @@ enum saras_mg_mode {
 enum saras_guess {
     SARAS_GUESS_PREVIOUS = 0, /* previous Pp (reference behaviour, poisson.cc:115) */
     SARAS_GUESS_LEARNED = 1,  /* U-Net guess with fallback to the previous Pp      */
-    SARAS_GUESS_EXTRAPOLATE = 2 /* 2 Pp(n-1) - Pp(n-2) with the same fallback (ablation) */
+    SARAS_GUESS_EXTRAPOLATE = 2, /* 2 Pp(n-1) - Pp(n-2) with the same fallback (ablation) */
+    SARAS_GUESS_QUADRATIC = 3    /* 3 Pp(n-1) - 3 Pp(n-2) + Pp(n-3), same fallback (ablation) */
 };
 
 /*
@@ -108,8 +109,11 @@ typedef struct saras_params {
     int guessMode;            /* enum saras_guess                               */
     double jacobiWeight;      /* damping of the Jacobi smoother (1.0 = reference) */
     int seed;
-    int fastKernels;          /* 1: fused multiply-add / reciprocal forms of the CN and
-                                 RHS kernels (not bit-identical to the reference);
+    int fastKernels;          /* 1: fused multiply-add / reciprocal forms of the CN,
+                                 RHS, divergence and projection kernels (not
+                                 bit-identical to the reference); 2: as 1, with the
+                                 CN Jacobi update in split-FP64 form (FP64 values
+                                 carried in float pairs, about 1e-14 relative);
                                  0: reference arithmetic (the drop-in)          */
 } saras_params;
 
@@ -121,7 +125,7 @@ typedef struct saras_step_stats {
     double mg_residual;       /* last value of computeError (poisson_d3.cc:391-459) */
     double fine_residual;     /* FP64 max|b-Ap|/max|b| after the solve (target modes) */
     double guess_residual;    /* FP64 residual of the chosen initial guess */
-    int guess_source;         /* 0 previous Pp, 1 network */
+    int guess_source;         /* guess used: 0 previous Pp, else the saras_guess mode that won */
     int status;
 } saras_step_stats;
 

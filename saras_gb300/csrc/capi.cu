@@ -239,6 +239,8 @@ static int validate(const saras_params *p, std::string &why) {
     if (p->probType >= 5 && (p->rbcType < 1 || p->rbcType > 4)) { why = "undefined RBC Type"; return SARAS_BAD_CONFIG; }
     if (p->tStp <= 0 || p->Re <= 0 || p->Lx <= 0 || p->Ly <= 0 || p->Lz <= 0) { why = "non-positive time step, Re or length"; return SARAS_BAD_CONFIG; }
     if (p->mgMode < 0 || p->mgMode > 2) { why = "bad multigrid mode"; return SARAS_BAD_CONFIG; }
+    if (p->guessMode < SARAS_GUESS_PREVIOUS || p->guessMode > SARAS_GUESS_QUADRATIC) { why = "bad guess mode"; return SARAS_BAD_CONFIG; }
+    if (p->fastKernels < 0 || p->fastKernels > 2) { why = "Fast Kernels must be 0, 1 or 2"; return SARAS_BAD_CONFIG; }
     if (p->resType < 0 || p->resType > 2) { why = "bad residual type"; return SARAS_BAD_CONFIG; }
     return SARAS_OK;
 }
@@ -290,7 +292,8 @@ int saras_destroy(saras_ctx *h) {
     for (int q = 0; q < 4; ++q) cudaFree(c.scratch[q]);
     cudaFree(c.red); cudaFree(c.dscal); cudaFree(c.dflag);
     if (c.hscal) cudaFreeHost(c.hscal);
-    for (int q = 0; q < 2; ++q) cudaFree(c.pHist[q]);
+    for (int q = 0; q < 3; ++q) cudaFree(c.pHist[q]);
+    cudaFree(c.cnp);
     for (int k = 0; k < PK_COUNT; ++k) for (cudaEvent_t e : c.prof[k].ev) cudaEventDestroy(e);
     for (int k = 0; k < 16; ++k) if (c.userEv[k]) cudaEventDestroy(c.userEv[k]);
     if (c.stream) cudaStreamDestroy(c.stream);
@@ -408,7 +411,7 @@ int saras_unet_infer(saras_ctx *h, int field_out) {
 }
 int saras_set_guess_mode(saras_ctx *h, int mode) {
     CTX_OR_FAIL(h);
-    if (mode != SARAS_GUESS_PREVIOUS && mode != SARAS_GUESS_LEARNED && mode != SARAS_GUESS_EXTRAPOLATE) return SARAS_BAD_ARG;
+    if (mode < SARAS_GUESS_PREVIOUS || mode > SARAS_GUESS_QUADRATIC) return SARAS_BAD_ARG;
     h->c.guessMode = mode;
     return SARAS_OK;
 }

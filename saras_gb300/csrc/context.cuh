@@ -105,7 +105,10 @@ struct Ctx {
     // learned warm start
     int guessMode = SARAS_GUESS_PREVIOUS;
     void *unet = nullptr;
-    double *pHist[2] = {nullptr, nullptr};   // P at the two previous steps
+    double *pHist[3] = {nullptr, nullptr, nullptr};   // Pp of the three previous steps (newest first)
+    long long *fx[3] = {nullptr, nullptr, nullptr};   // level-0 fixed-point iterate ping-pong + rhs (mixed mode)
+    float *cnp = nullptr;      // split-FP64 Jacobi solve: N0 and the D ping-pong as float pairs
+    long cnpCount = 0;
     int histCount = 0;
     bool collecting = false;
     // profiling
@@ -160,7 +163,7 @@ int unet_collect(Ctx &c);
 int unet_train(Ctx &c, int iters, double lr, double *loss);
 int unet_infer(Ctx &c, double *out);
 int unet_begin_solve(Ctx &c);
-int unet_guess(Ctx &c, const double *b, double *dst, bool use_net);
+int unet_guess(Ctx &c, const double *b, double *dst, int mode);
 int unet_collect_sample(Ctx &c, const double *b);
 int conv3d_check(int mode, int D, int H, int W, int cin, int cout, const unsigned short *x, const unsigned short *dy,
                  const float *w, const float *bias, int relu, float *out);

@@ -1,0 +1,165 @@
+// df64.cuh -- FP64 values carried through FP32/INT32 arithmetic.
+//
+// GB300 executes FP64 at 1/64 of its FP32 rate (2 FP64 operations per SM
+// clock), so an FP64 stencil there is bound by the FP64 pipe long before it
+// reaches HBM.  The fast kernels (fastKernels = 2) therefore read the FP64
+// fields, split each value into two floats with integer operations only, do
+// the arithmetic in float pairs where cancellation needs it (Knuth's TwoSum,
+// the classical double-float technique of Dekker 1971), and spend one FP64
+// addition per output point to form the FP64 result.
+//
+// dsplit(x) -> (hi, lo):  hi = x with the low 29 of its 52 fraction bits
+//   cleared (exact in float when 2^-126 <= |x| < 2^128), lo = the cleared
+//   bits, kept to their top 23 bits: |x - hi - lo| <= 2^-46 |x|.
+//   |x| < 2^-126 gives hi = 0 (and lo = 0 below 2^-104); NaN and Inf give a
+//   NaN / Inf hi, so they reach every result computed from the split.
+// f2d(f): the float f as an exact double, built from its bits.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace saras {
+
+__device__ __forceinline__ void dsplit(double x, float &hi, float &lo) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    unsigned h = (unsigned)(b >> 32), l = (unsigned)b;
+    unsigned sign = h & 0x80000000u;
+    int e = (int)((h >> 20) & 0x7ffu);
+    int fe = e - 896;   // float biased exponent of hi (1023 - 127 = 896)
+    unsigned fr = ((h & 0xfffffu) << 3) | (l >> 29);
+    unsigned hb;
+    if (fe >= 1 && fe <= 254) hb = sign | ((unsigned)fe << 23) | fr;
+    else if (e == 2047) hb = ((h & 0xfffffu) | l) ? 0x7fc00000u : (sign | 0x7f800000u);
+    else if (fe > 254) hb = sign | 0x7f800000u;
+    else hb = sign;
+    hi = __uint_as_float(hb);
+    // lo = (l mod 2^29) 2^(e-1075): its top 23 bits m as a float by the
+    // magic-number conversion (2^(E-127) (1 + m 2^-23) - 2^(E-127) = m 2^(E-150),
+    // exact), with E - 150 = e - 1069, i.e. E = e - 919.
+    int me = e - 919;
+    unsigned m23 = (l & 0x1fffffffu) >> 6;
+    float mag = 0.0f;
+    if (me >= 1 && me <= 254) mag = __uint_as_float(((unsigned)me << 23) | m23) - __uint_as_float((unsigned)me << 23);
+    lo = sign ? -mag : mag;
+}
+
+// The high part of dsplit alone (x truncated to a float).
+__device__ __forceinline__ float dhi(double x) {
+    unsigned h = (unsigned)((unsigned long long)__double_as_longlong(x) >> 32);
+    unsigned sign = h & 0x80000000u;
+    int e = (int)((h >> 20) & 0x7ffu);
+    int fe = e - 896;
+    unsigned fr = ((h & 0xfffffu) << 3) | ((unsigned)__double_as_longlong(x) >> 29);
+    unsigned hb;
+    if (fe >= 1 && fe <= 254) hb = sign | ((unsigned)fe << 23) | fr;
+    else if (e == 2047) hb = 0x7fc00000u | sign;
+    else if (fe > 254) hb = sign | 0x7f800000u;
+    else hb = sign;
+    return __uint_as_float(hb);
+}
+
+__device__ __forceinline__ double f2d(float f) {
+    unsigned u = __float_as_uint(f);
+    unsigned sign = u & 0x80000000u;
+    int fe = (int)((u >> 23) & 0xffu);
+    unsigned fr = u & 0x7fffffu;
+    unsigned hw, lw;
+    if (fe == 0) { hw = sign; lw = 0u; }   // zero (float subnormals are flushed)
+    else if (fe == 255) { hw = sign | 0x7ff00000u | (fr ? 0x80000u : 0u); lw = 0u; }
+    else { hw = sign | ((unsigned)(fe + 896) << 20) | (fr >> 3); lw = (fr & 7u) << 29; }
+    return __longlong_as_double((long long)(((unsigned long long)hw << 32) | lw));
+}
+
+// Knuth's TwoSum: s + t == a + b exactly, s = fl(a + b).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &t) {
+    s = a + b;
+    float bb = s - a;
+    t = (a - (s - bb)) + (b - bb);
+}
+
+// Float pairs: value h + l with |l| <= ulp(h) / 2 after each operation
+// (Dekker's FastTwoSum renormalises), about 44 significant bits.
+struct fpair {
+    float h, l;
+};
+
+__device__ __forceinline__ fpair fp_norm(float s, float t) {
+    float h = s + t;
+    return fpair{h, t - (h - s)};
+}
+
+__device__ __forceinline__ fpair fp_add(fpair a, fpair b) {
+    float s, t;
+    two_sum(a.h, b.h, s, t);
+    return fp_norm(s, t + (a.l + b.l));
+}
+
+__device__ __forceinline__ fpair fp_neg(fpair a) { return fpair{-a.h, -a.l}; }
+
+// Product through the exact FMA residual of the high parts.
+__device__ __forceinline__ fpair fp_mul(fpair a, fpair b) {
+    float p = a.h * b.h;
+    float e = fmaf(a.h, b.h, -p);
+    e = fmaf(a.h, b.l, fmaf(a.l, b.h, e));
+    return fp_norm(p, e);
+}
+
+__device__ __forceinline__ fpair fp_of(double x) {
+    fpair r;
+    dsplit(x, r.h, r.l);
+    return r;
+}
+
+// |f| < 2^128 and not NaN, from the bits (keeps the check off the FP64 pipe).
+__device__ __forceinline__ bool f_finite(float f) { return (__float_as_uint(f) & 0x7fffffffu) < 0x7f800000u; }
+
+// ---- 64-bit fixed point (the exact residual of the mixed-precision refinement)
+// v = round(x 2^s) to nearest (ties away from zero) from the bits of x; sets
+// `bad` for NaN / Inf or when |v| would reach 2^62.  Integer operations only.
+__device__ __forceinline__ long long d2fx(double x, int s, bool &bad) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    int e = (int)((b >> 52) & 0x7ffu);
+    if (e == 0) return 0;
+    if (e == 2047) { bad = true; return 0; }
+    unsigned long long m = (b & 0xfffffffffffffull) | 0x10000000000000ull;   // |x| = m 2^(e-1075)
+    int sh = e - 1075 + s;
+    unsigned long long a;
+    if (sh >= 0) {
+        if (sh > 9) { bad = true; return 0; }
+        a = m << sh;
+    } else if (sh >= -53) {
+        a = (m >> (-sh)) + ((m >> (-sh - 1)) & 1ull);
+    } else {
+        return 0;
+    }
+    long long v = (long long)a;
+    return (b >> 63) ? -v : v;
+}
+
+__device__ __forceinline__ long long f2fx(float f, int s, bool &bad) {
+    unsigned u = __float_as_uint(f);
+    int e = (int)((u >> 23) & 0xffu);
+    if (e == 0) return 0;
+    if (e == 255) { bad = true; return 0; }
+    unsigned long long m = (u & 0x7fffffu) | 0x800000u;   // |f| = m 2^(e-150)
+    int sh = e - 150 + s;
+    unsigned long long a;
+    if (sh >= 0) {
+        if (sh > 38) { bad = true; return 0; }
+        a = m << sh;
+    } else if (sh >= -24) {
+        a = (m >> (-sh)) + ((m >> (-sh - 1)) & 1ull);
+    } else {
+        return 0;
+    }
+    long long v = (long long)a;
+    return (u >> 31) ? -v : v;
+}
+
+// A 64-bit integer as a float (to within a few float ulps) from two 32-bit
+// conversions: the 64-bit conversion instruction runs on GB300's FP64 pipe.
+__device__ __forceinline__ float fx2f(long long r) {
+    return fmaf((float)(int)(r >> 32), 4294967296.0f, (float)(unsigned)r);
+}
+
+}  // namespace saras

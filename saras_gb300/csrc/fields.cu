@@ -17,6 +17,7 @@
 #include <algorithm>
 
 #include "context.cuh"
+#include "df64.cuh"
 
 namespace saras {
 
@@ -73,12 +74,18 @@ template <int T, int S> struct Slices;
         __device__ static __forceinline__ double sum(const View3<const double> &V, int i, int j, int k) { \
             return V(i, j, k);                                                                 \
         }                                                                                      \
+        __device__ static __forceinline__ fpair sump(const View3<const double> &V, int i, int j, int k) { \
+            return fp_of(V(i, j, k));                                                          \
+        }                                                                                      \
     };
 #define SARAS_SLICE2(T_, S_, a, b, c)                                                          \
     template <> struct Slices<T_, S_> {                                                        \
         static constexpr int n = 2;                                                            \
         __device__ static __forceinline__ double sum(const View3<const double> &V, int i, int j, int k) { \
             return V(i, j, k) + V(i + (a), j + (b), k + (c));                                  \
+        }                                                                                      \
+        __device__ static __forceinline__ fpair sump(const View3<const double> &V, int i, int j, int k) { \
+            return fp_add(fp_of(V(i, j, k)), fp_of(V(i + (a), j + (b), k + (c))));            \
         }                                                                                      \
     };
 #define SARAS_SLICE4(T_, S_, a1, b1, c1, a2, b2, c2, a3, b3, c3)                                \
@@ -87,6 +94,10 @@ template <int T, int S> struct Slices;
         __device__ static __forceinline__ double sum(const View3<const double> &V, int i, int j, int k) { \
             return V(i, j, k) + V(i + (a1), j + (b1), k + (c1)) + V(i + (a2), j + (b2), k + (c2)) + \
                    V(i + (a3), j + (b3), k + (c3));                                             \
+        }                                                                                      \
+        __device__ static __forceinline__ fpair sump(const View3<const double> &V, int i, int j, int k) { \
+            return fp_add(fp_add(fp_of(V(i, j, k)), fp_of(V(i + (a1), j + (b1), k + (c1)))),   \
+                          fp_add(fp_of(V(i + (a2), j + (b2), k + (c2))), fp_of(V(i + (a3), j + (b3), k + (c3))))); \
         }                                                                                      \
     };
 SARAS_SLICE1(0, 0)
@@ -189,15 +200,31 @@ __global__ void k_gradient(View3<double> G, View3<const double> S, Box b, UC u) 
 
 // vfield::divergence (vfield.cc:299-320), then optionally mgRHS *= 1/dt
 // (hydro_d3.cc:326-327).  Writes the whole padded array (ghosts = 0).
-__global__ void k_divergence(View3<double> D, Vel V, Box full, UC u, double scale, int do_scale, int force_one) {
+// Folded per-axis factors of the fast forms (fastKernels = 1).
+struct Fold3 {
+    double k[3];
+};
+
+// fast != 0: the same divergence with gm * ih * scale folded into one factor
+// per axis and the sum as fused multiply-adds (6 FP64 operations a point
+// instead of 12; GB300's FP64 pipe, not HBM, bounds this kernel).
+__global__ void k_divergence(View3<double> D, Vel V, Box full, UC u, double scale, int do_scale, int force_one, int fast,
+                             Fold3 fk) {
     int i, j, k;
     if (!box_point(full, i, j, k)) return;
     double out = 0.0;
     if (force_one) { D(i, j, k) = 1.0; return; }
     if (i >= 0 && j >= 0 && k >= 0 && i < D.n[0] && j < D.n[1] && k < D.n[2]) {
-        double tx = (u.gm[0] * (V.v[0](i, j, k) - V.v[0](i - 1, j, k))) * u.ih[0];
-        double ty = (u.gm[1] * (V.v[1](i, j, k) - V.v[1](i, j - 1, k))) * u.ih[1];
-        double tz = (u.gm[2] * (V.v[2](i, j, k) - V.v[2](i, j, k - 1))) * u.ih[2];
+        double dx = V.v[0](i, j, k) - V.v[0](i - 1, j, k);
+        double dy = V.v[1](i, j, k) - V.v[1](i, j - 1, k);
+        double dz = V.v[2](i, j, k) - V.v[2](i, j, k - 1);
+        if (fast) {
+            D(i, j, k) = fma(fk.k[0], dx, fma(fk.k[1], dy, fk.k[2] * dz));
+            return;
+        }
+        double tx = (u.gm[0] * dx) * u.ih[0];
+        double ty = (u.gm[1] * dy) * u.ih[1];
+        double tz = (u.gm[2] * dz) * u.ih[2];
         out = tx + ty + tz;
     }
     if (do_scale) out = out * scale;
@@ -281,6 +308,42 @@ __global__ void __launch_bounds__(256) k_rhs_fast(RhsArgs a, RhsFast q) {
     double sp = C == 0 ? a.P(i + 1, j, k) : C == 1 ? a.P(i, j + 1, k) : a.P(i, j, k + 1);
     h = fma(-q.G[C], sp - a.P(i, j, k), h);
     a.H(i, j, k) = fma(h, q.dt, f0);
+}
+
+// Split-FP64 form (fastKernels = 2) of the same right-hand side,
+//   H = F + dt (visc Lap F - (V.grad) F [+ Fb avg T] - grad P),
+// evaluated in float-pair arithmetic (df64.cuh) from split values: every
+// intermediate keeps about 44 bits, so H is good to about 2^-44 of the
+// largest term (about 1e-13 for O(1) fields).  FP64 work per point: the two
+// additions that form F + dt h.
+struct RhsDf {
+    fpair k2[3];     // visc m2h ih2
+    fpair k1n[3];    // 0.5 ih m1 / (number of velocity values averaged along that axis)
+    fpair g[3];      // gm ih (pressure gradient)
+    fpair fb2, dt;
+};
+
+template <int C>
+__global__ void __launch_bounds__(256) k_rhs_df(RhsArgs a, RhsDf q) {
+    int i, j, k;
+    if (!box_point(a.b, i, j, k)) return;
+    const View3<const double> &F = a.F;
+    double f0 = F(i, j, k);
+    fpair c = fp_of(f0), c2 = fpair{-2.0f * c.h, -2.0f * c.l};
+    fpair ex = fp_of(F(i + 1, j, k)), wx = fp_of(F(i - 1, j, k));
+    fpair ey = fp_of(F(i, j + 1, k)), wy = fp_of(F(i, j - 1, k));
+    fpair ez = fp_of(F(i, j, k + 1)), wz = fp_of(F(i, j, k - 1));
+    fpair h = fp_mul(q.k2[0], fp_add(fp_add(ex, wx), c2));
+    h = fp_add(h, fp_mul(q.k2[1], fp_add(fp_add(ey, wy), c2)));
+    h = fp_add(h, fp_mul(q.k2[2], fp_add(fp_add(ez, wz), c2)));
+    h = fp_add(h, fp_neg(fp_mul(Slices<C, 0>::sump(a.V.v[0], i, j, k), fp_mul(fp_add(ex, fp_neg(wx)), q.k1n[0]))));
+    h = fp_add(h, fp_neg(fp_mul(Slices<C, 1>::sump(a.V.v[1], i, j, k), fp_mul(fp_add(ey, fp_neg(wy)), q.k1n[1]))));
+    h = fp_add(h, fp_neg(fp_mul(Slices<C, 2>::sump(a.V.v[2], i, j, k), fp_mul(fp_add(ez, fp_neg(wz)), q.k1n[2]))));
+    if (C == 2 && a.buoyancy) h = fp_add(h, fp_mul(q.fb2, fp_add(fp_of(a.T(i, j, k)), fp_of(a.T(i, j, k + 1)))));
+    double sp = C == 0 ? a.P(i + 1, j, k) : C == 1 ? a.P(i, j + 1, k) : a.P(i, j, k + 1);
+    h = fp_add(h, fp_neg(fp_mul(q.g[C], fp_add(fp_of(sp), fp_neg(fp_of(a.P(i, j, k)))))));
+    h = fp_mul(h, q.dt);
+    a.H(i, j, k) = (f0 + f2d(h.h)) + f2d(h.l);
 }
 
 static RhsFast make_rhs_fast(const Ctx &c, double visc) {
@@ -382,16 +445,18 @@ __global__ void k_cn(CnArgs a) {
 
 // Fast form of the same Jacobi iteration (fastKernels = 1): the two divisions
 // become multiplications by precomputed reciprocals and the sums are fused
-// multiply-adds.  Same fixed point and stopping rule, not bit-identical.
+// multiply-adds.  The residual of the input C, C - k2 Lap(C) - rhs, equals
+// Dn (C - J(C)) for the Jacobi image J(C) = (rhs + k2 offdiag(C)) / Dn, so the
+// kernel reports max |C - J(C)| and the host multiplies by Dn: no second
+// stencil evaluation.  Same fixed point and stopping rule, not bit-identical.
 struct CnFast {
     View3<double> out;
     View3<const double> in, rhs;
     BcProgram prog;
     Box full;
     double c1, c2, c3, k1, invDn;   // guess = fma(A, k1, rhs) * invDn
-    double lx, ly, lz, lc, k2;      // residual value = C - k2 * Lap(C)
     int withResidual;
-    double *resMax;
+    double *resMax;                 // max |C - guess| (times Dn on the host)
 };
 
 __device__ __forceinline__ double cn_guess_fast(const CnFast &a, int i, int j, int k) {
@@ -409,13 +474,13 @@ __global__ void __launch_bounds__(256) k_cn_fast(CnFast a) {
             const View3<const double> &V = a.in;
             double C = V(i, j, k);
             double ew = V(i + 1, j, k) + V(i - 1, j, k), ns = V(i, j + 1, k) + V(i, j - 1, k), ud = V(i, j, k + 1) + V(i, j, k - 1);
+            double A = fma(a.c1, ew, fma(a.c2, ns, a.c3 * ud));
+            double o = fma(A, a.k1, a.rhs(i, j, k)) * a.invDn;
+            a.out(i, j, k) = o;
             if (a.withResidual) {
-                double L = fma(a.lx, ew, fma(a.ly, ns, fma(a.lz, ud, a.lc * C)));
-                res = fabs(fma(-a.k2, L, C) - a.rhs(i, j, k));
+                res = fabs(C - o);
                 if (res != res) res = INFINITY;
             }
-            double A = fma(a.c1, ew, fma(a.c2, ns, a.c3 * ud));
-            a.out(i, j, k) = fma(A, a.k1, a.rhs(i, j, k)) * a.invDn;
         } else {
             a.out(i, j, k) = bc_resolve(a.prog, i, j, k, [&](int x, int y, int z) -> double {
                 return in_box(a.prog.blo, a.prog.bhi, x, y, z) ? cn_guess_fast(a, x, y, z) : 0.0;
@@ -425,18 +490,151 @@ __global__ void __launch_bounds__(256) k_cn_fast(CnFast a) {
     if (a.withResidual) block_max_to(res, a.resMax);
 }
 
+// Split-FP64 form of the same Jacobi iteration (fastKernels = 2), in delta
+// form.  With Dn = 1 + 2 k1 (c1 + c2 + c3) the Jacobi image of an iterate C is
+//   J(C) = C + corr,  corr = (rhs - C + k1 (c1 S_x(C) + c2 S_y(C) + c3 S_z(C))) / Dn,
+// S_d(C) = C(+d) + C(-d) - 2C.  Writing C = C0 + D for the field C0 at the
+// start of the solve,
+//   corr = (N0 - D + k1 sum_d c_d S_d(D)) / Dn,  N0 = rhs - C0 + k1 sum_d c_d S_d(C0),
+// so N0 is formed once per solve (k_cn_pack, float-pair arithmetic from split
+// FP64 values) and every sweep (k_cn_delta) works on the small correction D,
+// held as a float pair: the sweep reads and writes 8 bytes per point like the
+// FP64 form but does no FP64 arithmetic at all, and k_cn_unpack forms
+// C0 + D in FP64 at the end, so C0 keeps all its bits.  Accuracy: about 2^-44
+// of the largest of |rhs|, |C0| in N0, and of |D| in the sweeps (the Jacobi
+// tolerance is 1e-8).  Boundary points: the field's boundary program resolved
+// on C0 + D in float pairs (constant -> value, copy -> copy, reflect -> 2c - v),
+// then minus C0 there, as the FP64 form resolves it on C.
+struct CnDf {
+    fpair kc[3];     // k1 c1, k1 c2, k1 c3 as float pairs (N0)
+    float kf[3];     // the same as floats (sweeps: S_d(D) is small)
+    fpair invDn;     // 1 / Dn
+};
+
+static CnDf cn_df_consts(const CnFast &fa) {
+    CnDf d;
+    auto pr = [](double x) { fpair r; r.h = (float)x; r.l = (float)(x - (double)r.h); return r; };
+    d.kc[0] = pr(fa.k1 * fa.c1);
+    d.kc[1] = pr(fa.k1 * fa.c2);
+    d.kc[2] = pr(fa.k1 * fa.c3);
+    for (int q = 0; q < 3; ++q) d.kf[q] = d.kc[q].h;
+    d.invDn = pr(fa.invDn);
+    return d;
+}
+
+// N0 at the bulk points of the field's full box.
+__global__ void __launch_bounds__(256) k_cn_pack(View3<const double> V, View3<const double> rhs, BcProgram prog, Box full, CnDf f,
+                                                 float *n0h, float *n0l) {
+    int i, j, k;
+    if (!box_point(full, i, j, k) || !in_box(prog.blo, prog.bhi, i, j, k)) return;
+    fpair c = fp_of(V(i, j, k)), c2 = fpair{-2.0f * c.h, -2.0f * c.l};
+    fpair sx = fp_add(fp_add(fp_of(V(i + 1, j, k)), fp_of(V(i - 1, j, k))), c2);
+    fpair sy = fp_add(fp_add(fp_of(V(i, j + 1, k)), fp_of(V(i, j - 1, k))), c2);
+    fpair sz = fp_add(fp_add(fp_of(V(i, j, k + 1)), fp_of(V(i, j, k - 1))), c2);
+    fpair q = fp_add(fp_add(fp_mul(f.kc[0], sx), fp_mul(f.kc[1], sy)), fp_mul(f.kc[2], sz));
+    fpair n = fp_add(fp_add(fp_of(rhs(i, j, k)), fp_neg(c)), q);
+    long o = V.off(i, j, k);
+    n0h[o] = n.h;
+    n0l[o] = n.l;
+}
+
+struct CnDelta {
+    const double *C0;
+    const float *n0h, *n0l;
+    const float *dh, *dl;      // D in
+    float *oh, *ol;            // D out
+    long sx, sy;               // strides of the padded layout (k stride 1)
+    BcProgram prog;
+    Box full;
+    CnDf f;
+    int withResidual;
+    double *resMax;            // max |corr| (times Dn on the host)
+    __device__ long off(int i, int j, int k) const { return (long)(i + 1) * sx + (long)(j + 1) * sy + (k + 1); }
+};
+
+// D + corr at bulk point o.
+__device__ __forceinline__ fpair cn_delta_image(const CnDelta &a, long o, fpair &corr) {
+    fpair D = fpair{a.dh[o], a.dl[o]};
+    float d2 = 2.0f * D.h;
+    float q = fmaf(a.f.kf[0], (a.dh[o + a.sx] + a.dh[o - a.sx]) - d2,
+                   fmaf(a.f.kf[1], (a.dh[o + a.sy] + a.dh[o - a.sy]) - d2, a.f.kf[2] * ((a.dh[o + 1] + a.dh[o - 1]) - d2)));
+    fpair num = fp_add(fp_add(fpair{a.n0h[o], a.n0l[o]}, fp_neg(D)), fpair{q, 0.0f});
+    corr = fp_mul(num, a.f.invDn);
+    return fp_add(D, corr);
+}
+
+__device__ __forceinline__ fpair fp_of_c(double x) {
+    fpair r;
+    r.h = __double2float_rn(x);
+    r.l = __double2float_rn(x - (double)r.h);
+    return r;
+}
+
+__global__ void __launch_bounds__(256) k_cn_delta(CnDelta a) {
+    int i, j, k;
+    bool ok = box_point(a.full, i, j, k);
+    double res = 0.0;
+    if (ok) {
+        long o = a.off(i, j, k);
+        fpair out;
+        if (in_box(a.prog.blo, a.prog.bhi, i, j, k)) {
+            fpair corr;
+            out = cn_delta_image(a, o, corr);
+            if (a.withResidual) res = f_finite(corr.h) ? f2d(fabsf(corr.h)) : INFINITY;
+        } else {
+            // bc_resolve on C0 + D in float pairs (the FP64 form's bc_resolve with
+            // base = Jacobi image at bulk points, 0 elsewhere), then minus C0 here
+            const BcProgram &prog = a.prog;
+            int chain[kMaxBcOps];
+            int nchain = 0;
+            fpair value = fpair{0.0f, 0.0f};
+            bool haveConst = false;
+            int q[3] = {i, j, k};
+            for (int op = prog.nops - 1; op >= 0; --op) {
+                const BcOp &b = prog.op[op];
+                if (q[0] < b.lo[0] || q[0] > b.hi[0] || q[1] < b.lo[1] || q[1] > b.hi[1] || q[2] < b.lo[2] || q[2] > b.hi[2]) continue;
+                if (b.kind == OP_CONST) { value = fp_of_c(b.c); haveConst = true; break; }
+                chain[nchain++] = op;
+                q[0] += b.shift[0]; q[1] += b.shift[1]; q[2] += b.shift[2];
+            }
+            if (!haveConst && in_box(prog.blo, prog.bhi, q[0], q[1], q[2])) {
+                long os = a.off(q[0], q[1], q[2]);
+                fpair corr;
+                value = fp_add(fp_of(a.C0[os]), cn_delta_image(a, os, corr));
+            }
+            for (int cix = nchain - 1; cix >= 0; --cix) {
+                const BcOp &b = prog.op[chain[cix]];
+                if (b.kind == OP_REFLECT) value = fp_add(fp_of_c(2.0 * b.c), fp_neg(value));
+            }
+            out = fp_add(value, fp_neg(fp_of(a.C0[o])));
+        }
+        a.oh[o] = out.h;
+        a.ol[o] = out.l;
+    }
+    if (a.withResidual) block_max_to(res, a.resMax);
+}
+
+// C0 + D in FP64 over the whole padded array (in place on the field).
+__global__ void k_cn_unpack(double *V, const float *dh, const float *dl, long n) {
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x)
+        V[t] = (V[t] + f2d(dh[t])) + f2d(dl[t]);
+}
+
 // ------------------------------------------------------------------ projection
 // hydro_d3.cc:357-367: V -= dt*grad(Pp) on the component core (gradient = 0
 // elsewhere), optionally followed by the component's boundary program.
-template <int C>
+// FAST (fastKernels = 1): V - fastDt * (Pp(+1) - Pp) as one fused
+// multiply-add, fastDt = gm * ih * dt folded on the host.
+template <int C, bool FAST>
 __global__ void k_project(View3<double> out, View3<const double> in, View3<const double> Pp, BcProgram prog, Box full,
-                          UC u, double dt, int with_bc) {
+                          UC u, double dt, int with_bc, double fastDt) {
     int i, j, k;
     if (!box_point(full, i, j, k)) return;
     auto base = [&](int x, int y, int z) -> double {
         double v = in(x, y, z);
         if (x >= 0 && y >= 0 && z >= 0 && x < in.n[0] && y < in.n[1] && z < in.n[2]) {
             double sp = C == 0 ? Pp(x + 1, y, z) : C == 1 ? Pp(x, y + 1, z) : Pp(x, y, z + 1);
+            if (FAST) return fma(-fastDt, sp - Pp(x, y, z), v);
             double g = (u.gm[C] * (sp - Pp(x, y, z))) * u.ih[C];
             v = v - g * dt;
         }
@@ -797,8 +995,10 @@ int vfield_divergence(Ctx &c, double *dst, bool scale_dt) {
     dim3 g, bl; box_launch_dims(fb, g, bl);
     View3<double> D = mview_ptr(c, SARAS_FIELD_MGRHS, dst ? dst : c.f[SARAS_FIELD_MGRHS]);
     prof_begin(c, PK_DIVERGENCE, 0);
+    Fold3 fk;
+    for (int d = 0; d < 3; ++d) fk.k[d] = u.gm[d] * u.ih[d] * (scale_dt ? 1.0 / c.dt : 1.0);
     k_divergence<<<g, bl, 0, c.stream>>>(D, make_vel(c), fb, u, 1.0 / c.dt, scale_dt ? 1 : 0,
-                                         (scale_dt && c.p.testPoisson) ? 1 : 0);
+                                         (scale_dt && c.p.testPoisson) ? 1 : 0, c.p.fastKernels != 0, fk);
     count_launch(c);
     prof_end(c, PK_DIVERGENCE, 0, 5.0 * 8.0 * (double)D.size());
     return check_launch(c, "divergence");
@@ -837,7 +1037,20 @@ int compute_rhs(Ctx &c) {
         a.F = cview(c, SARAS_FIELD_VX + q);
         a.b = core_box(c.info[SARAS_FIELD_VX + q]);
         dim3 g, bl; box_launch_dims(a.b, g, bl);
-        if (fast) {
+        if (c.p.fastKernels == 2) {
+            RhsDf qd;
+            auto pr = [](double x) { fpair r; r.h = (float)x; r.l = (float)(x - (double)r.h); return r; };
+            for (int d = 0; d < 3; ++d) {
+                qd.k2[d] = pr(qf.K2[d]);
+                qd.k1n[d] = pr(qf.K1[d] / (q == d ? 1.0 : 4.0));   // Slices<q, d>::n
+                qd.g[d] = pr(qf.G[d]);
+            }
+            qd.fb2 = pr(qf.Fb2);
+            qd.dt = pr(qf.dt);
+            if (q == 0) k_rhs_df<0><<<g, bl, 0, c.stream>>>(a, qd);
+            if (q == 1) k_rhs_df<1><<<g, bl, 0, c.stream>>>(a, qd);
+            if (q == 2) k_rhs_df<2><<<g, bl, 0, c.stream>>>(a, qd);
+        } else if (fast) {
             if (q == 0) k_rhs_fast<0><<<g, bl, 0, c.stream>>>(a, qf);
             if (q == 1) k_rhs_fast<1><<<g, bl, 0, c.stream>>>(a, qf);
             if (q == 2) k_rhs_fast<2><<<g, bl, 0, c.stream>>>(a, qf);
@@ -867,6 +1080,72 @@ int compute_trhs(Ctx &c) {
     k_trhs<<<g, bl, 0, c.stream>>>(a);
     count_launch(c);
     return check_launch(c, "trhs");
+}
+
+// fastKernels = 2: the delta-form split-FP64 Jacobi solve (k_cn_pack,
+// k_cn_delta sweeps, k_cn_unpack), with the stopping rule and the sweep
+// semantics of cn_solve: each sweep also reports the residual of its input,
+// and the input of the first sweep whose input residual is below the
+// tolerance is the answer.
+static int cn_solve_delta(Ctx &c, int field, const CnFast &fa, double Dn, dim3 g, dim3 bl, double bytes, int *iters, double *maxerr) {
+    const FieldInfo &f = c.info[field];
+    View3<double> V = mview(c, field);
+    long n = V.size();
+    if (c.cnpCount < n) {
+        cudaFree(c.cnp);
+        c.cnp = nullptr;
+        SARAS_CUDA_TRY(cudaMalloc(&c.cnp, sizeof(float) * 6 * (size_t)n));
+        c.cnpCount = n;
+    }
+    float *n0h = c.cnp, *n0l = n0h + n, *dA = n0l + n, *dAl = dA + n, *dB = dAl + n, *dBl = dB + n;
+    CnDf fd = cn_df_consts(fa);
+    k_cn_pack<<<g, bl, 0, c.stream>>>(cview(c, field), fa.rhs, f.full, fa.full, fd, n0h, n0l);
+    SARAS_CUDA_TRY(cudaMemsetAsync(dA, 0, sizeof(float) * 2 * (size_t)n, c.stream));
+    count_launch(c);
+    CnDelta d;
+    d.C0 = V.p;
+    d.n0h = n0h; d.n0l = n0l;
+    d.sx = V.sx; d.sy = V.sy;
+    d.prog = f.full;
+    d.full = fa.full;
+    d.f = fd;
+    d.resMax = c.dscal;
+    float *cur[2] = {dA, dAl}, *nxt[2] = {dB, dBl};
+    auto launch = [&](int withRes) {
+        d.dh = cur[0]; d.dl = cur[1]; d.oh = nxt[0]; d.ol = nxt[1];
+        d.withResidual = withRes;
+        prof_begin(c, PK_CN, 0);
+        k_cn_delta<<<g, bl, 0, c.stream>>>(d);
+        count_launch(c);
+        prof_end(c, PK_CN, 0, bytes);
+    };
+    launch(0);
+    std::swap(cur, nxt);
+    int sweeps = 1, failed = 0, status = SARAS_OK;
+    double res = 0;
+    while (true) {
+        SARAS_CUDA_TRY(cudaMemsetAsync(c.dscal, 0, sizeof(double), c.stream));
+        launch(1);
+        int s = check_launch(c, "cn");
+        if (s) return s;
+        SARAS_CUDA_TRY(cudaMemcpyAsync(c.hscal, c.dscal, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        SARAS_CUDA_TRY(cudaStreamSynchronize(c.stream));
+        res = c.hscal[0] * Dn;
+        if (!std::isfinite(res)) { c.err = "Jacobi residual is not finite"; status = SARAS_NOT_FINITE; break; }
+        if (res < c.p.cnTolerance) break;     // cur is the answer
+        failed += 1;
+        if (failed > c.maxIterations) { status = SARAS_NOT_CONVERGED; break; }
+        std::swap(cur, nxt);
+        sweeps += 1;
+    }
+    // the field becomes C0 + D (also on failure, as the FP64 form leaves its last iterate)
+    k_cn_unpack<<<std::min<long>((n + 255) / 256, 152L * 16), 256, 0, c.stream>>>(V.p, cur[0], cur[1], n);
+    count_launch(c);
+    int s = check_launch(c, "cn unpack");
+    if (s) return s;
+    if (iters) *iters = status == SARAS_NOT_CONVERGED ? failed : sweeps;
+    if (maxerr) *maxerr = res;
+    return status;
 }
 
 int cn_solve(Ctx &c, int comp, int *iters, double *maxerr) {
@@ -916,11 +1195,10 @@ int cn_solve(Ctx &c, int comp, int *iters, double *maxerr) {
         fa.c1 = a.c1; fa.c2 = a.c2; fa.c3 = a.c3;
         fa.k1 = a.scalarForm ? (a.dt * a.coef) / a.X : a.dt / a.X;
         fa.invDn = 1.0 / a.Dn;
-        fa.lx = a.lx; fa.ly = a.ly; fa.lz = a.lz;
-        fa.lc = -2.0 * (a.lx + a.ly + a.lz);
-        fa.k2 = 0.5 * a.dt * a.resCoef;
         fa.resMax = a.resMax;
     }
+    const double resScale = fast ? a.Dn : 1.0;
+    if (c.p.fastKernels == 2) return cn_solve_delta(c, field, fa, a.Dn, g, bl, bytes, iters, maxerr);
     auto launch = [&](int withRes) {
         if (fast) {
             fa.in = cview(c, field);
@@ -952,7 +1230,7 @@ int cn_solve(Ctx &c, int comp, int *iters, double *maxerr) {
         if (s) return s;
         SARAS_CUDA_TRY(cudaMemcpyAsync(c.hscal, c.dscal, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
         SARAS_CUDA_TRY(cudaStreamSynchronize(c.stream));
-        res = c.hscal[0];
+        res = c.hscal[0] * resScale;
         if (!std::isfinite(res)) {
             c.err = "Jacobi residual is not finite";
             if (iters) *iters = sweeps;
@@ -996,9 +1274,17 @@ int project(Ctx &c, bool with_bc) {
         dim3 g, bl; box_launch_dims(fb, g, bl);
         View3<double> out = mview_ptr(c, field, c.scratch[q]);
         View3<const double> in = cview(c, field), Pp = cview(c, SARAS_FIELD_PP);
-        if (q == 0) k_project<0><<<g, bl, 0, c.stream>>>(out, in, Pp, f.full, fb, u, c.dt, with_bc ? 1 : 0);
-        if (q == 1) k_project<1><<<g, bl, 0, c.stream>>>(out, in, Pp, f.full, fb, u, c.dt, with_bc ? 1 : 0);
-        if (q == 2) k_project<2><<<g, bl, 0, c.stream>>>(out, in, Pp, f.full, fb, u, c.dt, with_bc ? 1 : 0);
+        double fdt = u.gm[q] * u.ih[q] * c.dt;
+        int wb = with_bc ? 1 : 0;
+        if (c.p.fastKernels) {
+            if (q == 0) k_project<0, true><<<g, bl, 0, c.stream>>>(out, in, Pp, f.full, fb, u, c.dt, wb, fdt);
+            if (q == 1) k_project<1, true><<<g, bl, 0, c.stream>>>(out, in, Pp, f.full, fb, u, c.dt, wb, fdt);
+            if (q == 2) k_project<2, true><<<g, bl, 0, c.stream>>>(out, in, Pp, f.full, fb, u, c.dt, wb, fdt);
+        } else {
+            if (q == 0) k_project<0, false><<<g, bl, 0, c.stream>>>(out, in, Pp, f.full, fb, u, c.dt, wb, fdt);
+            if (q == 1) k_project<1, false><<<g, bl, 0, c.stream>>>(out, in, Pp, f.full, fb, u, c.dt, wb, fdt);
+            if (q == 2) k_project<2, false><<<g, bl, 0, c.stream>>>(out, in, Pp, f.full, fb, u, c.dt, wb, fdt);
+        }
         count_launch(c);
         std::swap(c.f[field], c.scratch[q]);
         bytes += 3.0 * 8.0 * (double)out.size();
@@ -1294,11 +1580,9 @@ extern "C" int saras_cn_solve_noalloc(const saras_params *p, int component, doub
         fa.c1 = a.c1; fa.c2 = a.c2; fa.c3 = a.c3;
         fa.k1 = a.scalarForm ? (a.dt * a.coef) / a.X : a.dt / a.X;
         fa.invDn = 1.0 / a.Dn;
-        fa.lx = a.lx; fa.ly = a.ly; fa.lz = a.lz;
-        fa.lc = -2.0 * (a.lx + a.ly + a.lz);
-        fa.k2 = 0.5 * a.dt * a.resCoef;
         fa.resMax = a.resMax;
     }
+    const double resScale = fast ? a.Dn : 1.0;
     double *cur = v, *nxt = scratch;
     auto view_of = [&](double *ptr) { return make_view<double>(ptr, f.n[0], f.n[1], f.n[2]); };
     auto launch = [&](int withRes) {
@@ -1307,7 +1591,7 @@ extern "C" int saras_cn_solve_noalloc(const saras_params *p, int component, doub
         cin.p = in.p; cin.n[0] = in.n[0]; cin.n[1] = in.n[1]; cin.n[2] = in.n[2]; cin.sx = in.sx; cin.sy = in.sy;
         if (fast) {
             fa.in = cin; fa.out = out; fa.withResidual = withRes;
-            k_cn_fast<<<g, bl, 0, st>>>(fa);
+            k_cn_fast<<<g, bl, 0, st>>>(fa);   // both fast forms: the split-FP64 one needs more scratch
         } else {
             a.in = cin; a.out = out; a.withResidual = withRes;
             k_cn<<<g, bl, 0, st>>>(a);
@@ -1325,6 +1609,7 @@ extern "C" int saras_cn_solve_noalloc(const saras_params *p, int component, doub
         if ((e = launch(1)) != cudaSuccess) break;
         if ((e = cudaMemcpyAsync(&res, resSlot, sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess) break;
         if ((e = cudaStreamSynchronize(st)) != cudaSuccess) break;
+        res *= resScale;
         if (!std::isfinite(res)) { set_error("Jacobi residual is not finite"); status = SARAS_NOT_FINITE; break; }
         if (res < p->cnTolerance) break;
         failed += 1;

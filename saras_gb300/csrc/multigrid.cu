@@ -7,8 +7,10 @@
 //                          coarsest Gauss-Seidel to mgTolerance / maxCount).
 //   SARAS_MG_PLAIN_TARGET  FP64 V-cycles on the compatible system until
 //                          max|b-Ap| <= target * max|b|.
-//   SARAS_MG_MIXED         FP32 V-cycles as the inner solver of an FP64
-//                          iterative-refinement loop to the same target.
+//   SARAS_MG_MIXED         FP32 V-cycles as the inner solver of an
+//                          iterative-refinement loop to the same target; the
+//                          outer residual is FP64, or exact 64-bit fixed point
+//                          when the level-0 stencil is isotropic (k_fx_refine).
 // The target modes make the singular Neumann/periodic system compatible by
 // subtracting the trapezoidal-weight mean of b (the left null vector of the
 // vertex-grid operator with mirror or periodic ghosts) and use a damped Jacobi
@@ -25,6 +27,7 @@
 #include <algorithm>
 
 #include "context.cuh"
+#include "df64.cuh"
 
 namespace saras {
 
@@ -651,17 +654,121 @@ __global__ void __launch_bounds__(256) k_tgt_update(double *__restrict__ p, cons
     }
 }
 
+// ---- exact fixed-point refinement (SARAS_MG_MIXED, isotropic level 0)
+// With lx = ly = lz = l the level-0 residual is r = b - l (sum of the six
+// neighbours - 6 centre).  Holding the iterate as integers P = round(p 2^s) and
+// the right-hand side as B = round(b 2^s / l) makes it
+//     r = l 2^-s (B - (sum of the six neighbours of P - 6 P)),
+// evaluated exactly in 64-bit integer arithmetic: no rounding at all, where an
+// FP64 residual loses the digits the stencil cancels (about log10 of
+// (N / pi)^2 of them for smooth fields).  s is chosen per solve so that
+// |P|, |B| <= 2^55; sums of seven terms stay below 2^59.  GB300 runs these
+// integer operations at the FP32 rate, 64 times its FP64 rate, so the
+// residual is bound by HBM.
+//
+// WITH_E: the iterate is first advanced by the FP32 correction e of the inner
+// V-cycle, P_out = P_in + round(e 2^s) (face-ghost images included), and the
+// residual is that of P_out.  r32 receives r in FP32 (the next V-cycle's
+// right-hand side), maxr the block maxima of |B - ...| in integer units, flag
+// any value outside the fixed-point range.
+template <bool WITH_E>
+__global__ void __launch_bounds__(256) k_fx_refine(long long *__restrict__ pout, const long long *__restrict__ pin,
+                                                   const float *__restrict__ e, const long long *__restrict__ bfx,
+                                                   float *__restrict__ r32, int sx, int sy, MgBC bc, int s, float rscale,
+                                                   unsigned long long *maxr, int *flag) {
+    int k = blockIdx.x * 32 + threadIdx.x;
+    int j = blockIdx.y * 8 + threadIdx.y;
+    int i0 = blockIdx.z * kIch;
+    unsigned long long m = 0;
+    bool bad = false;
+    if (j <= bc.E[1] && k <= bc.E[2]) {
+        int iend = min(i0 + kIch - 1, bc.E[0]);
+        int o = (i0 + 1) * sx + (j + 1) * sy + (k + 1);
+        bool edge_jk = j <= 1 || k <= 1 || j >= bc.E[1] - 1 || k >= bc.E[2] - 1;
+        auto val = [&](int q) -> long long {
+            long long v = pin[q];
+            if (WITH_E) v += f2fx(e[q], s, bad);
+            return v;
+        };
+        long long cm = val(o - sx), cc = val(o);
+        for (int i = i0; i <= iend; ++i, o += sx) {
+            long long cp = val(o + sx);
+            long long nb = (cm + cp) + (val(o + sy) + val(o - sy)) + (val(o + 1) + val(o - 1));
+            long long r = bfx[o] - (nb - 6 * cc);
+            r32[o] = fx2f(r) * rscale;
+            unsigned long long a = (unsigned long long)(r < 0 ? -r : r);
+            m = a > m ? a : m;
+            if (WITH_E) {
+                pout[o] = cc;
+                unsigned long long ac = (unsigned long long)(cc < 0 ? -cc : cc);
+                if (ac > (1ull << 59)) bad = true;
+                if (edge_jk || i <= 1 || i >= bc.E[0] - 1) scatter_slow(pout, sx, sy, i, j, k, cc, bc);
+            }
+            cm = cc;
+            cc = cp;
+        }
+    }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+        unsigned long long o2 = __shfl_xor_sync(0xffffffffu, m, off);
+        m = o2 > m ? o2 : m;
+    }
+    __shared__ unsigned long long sm[8];
+    if (threadIdx.x == 0) sm[threadIdx.y] = m;
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        unsigned long long b = 0;
+        for (int q = 0; q < 8; ++q) b = sm[q] > b ? sm[q] : b;
+        atomicMax(maxr, b);
+    }
+    if (bad) atomicExch(flag, 1);
+}
+
+// dst = round(src 2^s) over a whole padded array (face-ghost images included).
+__global__ void k_fx_from(long long *__restrict__ dst, const double *__restrict__ src, long n, int s, int *flag) {
+    bool bad = false;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) dst[t] = d2fx(src[t], s, bad);
+    if (bad) atomicExch(flag, 1);
+}
+
+// B = round(b mul) over the core (mul = 2^s / l; the residual reads b only there).
+__global__ void k_fx_rhs(long long *__restrict__ dst, const double *__restrict__ b, int sx, int sy, MgBC bc, double mul, int *flag) {
+    int i, j, k;
+    if (!core_pt(bc.E, i, j, k)) return;
+    long o = (long)(i + 1) * sx + (long)(j + 1) * sy + (k + 1);
+    bool bad = false;
+    dst[o] = d2fx(b[o] * mul, 0, bad);
+    if (bad) atomicExch(flag, 1);
+}
+
+// p = P 2^-s (FP64, rounded once) over the whole padded array; with chk, also
+// chk = round(p 2^s): the FP64 result back in fixed point, whose exact residual
+// is the residual of what the solve returns.
+__global__ void k_fx_to(double *__restrict__ dst, long long *__restrict__ chk, const long long *__restrict__ src, long n, double inv2s,
+                        int s, int *flag) {
+    bool bad = false;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+        double x = __ll2double_rn(src[t]) * inv2s;
+        dst[t] = x;
+        if (chk) chk[t] = d2fx(x, s, bad);
+    }
+    if (bad) atomicExch(flag, 1);
+}
+
 // ---- target modes (FP64 / mixed)
 // Trapezoidal-weight partial sums of the core of rhs.
 __global__ void k_trap_sum(View3<const double> rhs, MgBC bc, double *part) {
     __shared__ double sm[32];
     int E0 = bc.E[0], E1 = bc.E[1], E2 = bc.E[2];
     long n = (long)(E0 + 1) * (E1 + 1) * (E2 + 1);
+    // weight 2^-(number of axes on which the point is an end point), as one
+    // table lookup: the product of three halves costs GB300's FP64 pipe
+    const double wt[4] = {1.0, 0.5, 0.25, 0.125};
     double s = 0;
     for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
         int k = (int)(t % (E2 + 1)), j = (int)((t / (E2 + 1)) % (E1 + 1)), i = (int)(t / ((long)(E2 + 1) * (E1 + 1)));
-        double w = ((i == 0 || i == E0) ? 0.5 : 1.0) * ((j == 0 || j == E1) ? 0.5 : 1.0) * ((k == 0 || k == E2) ? 0.5 : 1.0);
-        s += w * rhs(i, j, k);
+        int ends = (i == 0 || i == E0) + (j == 0 || j == E1) + (k == 0 || k == E2);
+        s = fma(wt[ends], rhs(i, j, k), s);
     }
     s = warp_sum(s);
     if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
@@ -669,13 +776,14 @@ __global__ void k_trap_sum(View3<const double> rhs, MgBC bc, double *part) {
     if (threadIdx.x == 0) { double S = 0; for (int w = 0; w < (int)(blockDim.x >> 5); ++w) S += sm[w]; part[blockIdx.x] = S; }
 }
 
-// b = rhs - trapmean over the core; block max |b|.
-__global__ void k_tgt_rhs(View3<double> b, View3<const double> rhs, MgBC bc, const double *sum, double wsum, double *maxabs) {
+// b = rhs - trapmean over the core; block max |b|.  The mean is one product
+// with 1/wsum (wsum = product of the interval counts).
+__global__ void k_tgt_rhs(View3<double> b, View3<const double> rhs, MgBC bc, const double *sum, double inv_wsum, double *maxabs) {
     int i, j, k;
     bool ok = core_pt(bc.E, i, j, k);
     double m = 0;
     if (ok) {
-        double v = rhs(i, j, k) - (*sum / wsum);
+        double v = rhs(i, j, k) - *sum * inv_wsum;
         b(i, j, k) = v;
         m = fabs(v);
     }
@@ -776,6 +884,7 @@ int mg_setup(Ctx &c) {
 
 void mg_free(Ctx &c) {
     for (Level &L : c.lv) { cudaFree(L.a); cudaFree(L.b); cudaFree(L.r); cudaFree(L.a32); cudaFree(L.b32); cudaFree(L.r32); }
+    for (long long *&q : c.fx) { cudaFree(q); q = nullptr; }
     c.lv.clear();
     cudaFree(c.wallX); cudaFree(c.wallY); cudaFree(c.wallZ);
     c.wallX = c.wallY = c.wallZ = nullptr;
@@ -843,8 +952,10 @@ static int coarse_solve(Ctx &c, bool tgt) {
     MgBC bc = level_bc(c, c.depth, tgt);
     MgK kk = make_k(L);
     size_t smem = 2 * sizeof(T) * L.count;
-    T tol = tgt ? (T)1.0e-6 : (T)c.p.mgTolerance;
-    int maxc = tgt ? 1000 : c.maxCount;
+    // target modes: the coarsest correction only has to be small against the
+    // V-cycle's own error reduction (about 0.1), so 1e-3 of the initial residual
+    T tol = tgt ? (T)1.0e-3 : (T)c.p.mgTolerance;
+    int maxc = tgt ? 500 : c.maxCount;
     k_mg_coarse<T><<<1, 256, smem, c.stream>>>(lview<T>(L, A_<T>(L)), lcview<T>(L, R_<T>(L)), kk, bc, tol, maxc, tgt ? 1 : 0,
                                                (long long *)(c.dscal + 40));
     count_launch(c);
@@ -1021,6 +1132,127 @@ int mg_fine_residual(Ctx &c, const double *pp, double *maxres, double *maxb) {
     return SARAS_OK;
 }
 
+// SARAS_MG_MIXED on an isotropic level 0: FP32 V-cycles inside the exact
+// fixed-point refinement (k_fx_refine).  On entry L0.r holds b, L0.pa() the
+// previous Pp with its face ghosts.  On return with done = true, L0.pa() holds
+// the FP64 result, r its residual max|b - A p| (evaluated exactly on the FP64
+// values), and the counters are set.  done = false (a value left the
+// fixed-point range, which takes a diverging iterate) leaves L0.pa() holding
+// the previous Pp again for the FP64 refinement loop.
+static int mixed_fixed(Ctx &c, double bmax, double target, bool wantGuess, double &r, int &source, int &cyc, int &steps, bool &done,
+                       saras_step_stats *st) {
+    int s;
+    Level &L0 = c.lv[0];
+    MgBC bc0 = level_bc(c, 0, true);
+    done = false;
+    for (long long *&q : c.fx)
+        if (!q) {
+            SARAS_CUDA_TRY(cudaMalloc(&q, sizeof(long long) * L0.count));
+            SARAS_CUDA_TRY(cudaMemsetAsync(q, 0, sizeof(long long) * L0.count, c.stream));
+        }
+    long long *B = c.fx[2];
+    unsigned long long *dmax = reinterpret_cast<unsigned long long *>(c.dscal + 34);
+    int *dflag = reinterpret_cast<int *>(c.dscal + 35);
+    // scale: |P|, |B| <= 2^55 for the largest of max|p| (padded array) and max|b| / l
+    SARAS_CUDA_TRY(cudaMemsetAsync(c.dscal + 33, 0, sizeof(double) * 3, c.stream));
+    k_maxabs<<<grid_blocks(L0.count), 256, 0, c.stream>>>(L0.pa(), L0.count, c.dscal + 33);
+    count_launch(c);
+    if ((s = chk(c, "fixed-point scale"))) return s;
+    if ((s = read_scalars(c, 33, 1))) return s;
+    double l = L0.lx;
+    double M = std::max(c.hscal[33], bmax / l);
+    if (!(M > 0.0) || !std::isfinite(M)) return SARAS_OK;   // nothing to scale (or not finite): FP64 path
+    int sc = 54 - std::ilogb(M);
+    sc = std::max(-900, std::min(900, sc));
+    double inv2s = std::ldexp(1.0, -sc);
+    double rs = l * inv2s;   // residual units -> value
+    int sx0 = (L0.n[1] + 3) * (L0.n[2] + 3), sy0 = L0.n[2] + 3;
+    dim3 gm0, bm0; march_dims(L0, gm0, bm0);
+    dim3 gc, bcd; core_dims(L0, gc, bcd);
+    int nbF = grid_blocks(L0.count);
+    k_fx_rhs<<<gc, bcd, 0, c.stream>>>(B, L0.r, sx0, sy0, bc0, std::ldexp(1.0, sc) / l, dflag);
+    count_launch(c);
+    // residual of fixed iterate q (with e: advanced into q ^ 1 first); returns the max in value units
+    auto refine = [&](int q, bool withE, double &out, bool &bad) -> int {
+        SARAS_CUDA_TRY(cudaMemsetAsync(c.dscal + 34, 0, sizeof(double), c.stream));
+        if (withE) {
+            prof_begin(c, PK_REFINE_UPDATE, 0);
+            k_fx_refine<true><<<gm0, bm0, 0, c.stream>>>(c.fx[q ^ 1], c.fx[q], L0.pa32(), B, L0.r32, sx0, sy0, bc0, sc, (float)rs, dmax, dflag);
+            prof_end(c, PK_REFINE_UPDATE, 0, (8.0 + 4.0 + 8.0 + 8.0 + 4.0) * (double)L0.count);
+        } else {
+            prof_begin(c, PK_REFINE_RESID, 0);
+            k_fx_refine<false><<<gm0, bm0, 0, c.stream>>>(nullptr, c.fx[q], nullptr, B, L0.r32, sx0, sy0, bc0, sc, (float)rs, dmax, dflag);
+            prof_end(c, PK_REFINE_RESID, 0, (8.0 + 8.0 + 4.0) * (double)L0.count);
+        }
+        count_launch(c);
+        int e = chk(c, "fixed-point refinement");
+        if (e) return e;
+        unsigned long long mx = 0;
+        int fl = 0;
+        SARAS_CUDA_TRY(cudaMemcpyAsync(&mx, dmax, sizeof(mx), cudaMemcpyDeviceToHost, c.stream));
+        SARAS_CUDA_TRY(cudaMemcpyAsync(&fl, dflag, sizeof(fl), cudaMemcpyDeviceToHost, c.stream));
+        SARAS_CUDA_TRY(cudaStreamSynchronize(c.stream));
+        out = (double)mx * rs;
+        bad = fl != 0;
+        return SARAS_OK;
+    };
+    bool bad = false;
+    k_fx_from<<<nbF, 256, 0, c.stream>>>(c.fx[0], L0.pa(), L0.count, sc, dflag);
+    count_launch(c);
+    if ((s = refine(0, false, r, bad))) return s;
+    if (bad) return SARAS_OK;
+    int cur = 0;
+    if (wantGuess && c.histCount >= 2) {
+        int gs = unet_guess(c, L0.r, L0.pb(), c.guessMode);
+        if (gs == SARAS_OK) {
+            double rg = 0;
+            k_fx_from<<<nbF, 256, 0, c.stream>>>(c.fx[1], L0.pb(), L0.count, sc, dflag);
+            count_launch(c);
+            if ((s = refine(1, false, rg, bad))) return s;
+            if (bad) return SARAS_OK;
+            if (rg < r) {
+                r = rg;
+                source = c.guessMode;
+                cur = 1;
+            } else if ((s = refine(0, false, r, bad))) {   // the previous Pp's FP32 residual back into r32
+                return s;
+            }
+        } else if (gs != SARAS_BAD_CONFIG) {
+            return gs;
+        }
+    }
+    if (st) { st->guess_residual = bmax > 0 ? r / bmax : r; st->guess_source = source; }
+    while (true) {
+        while (r > target && cyc < c.mgMaxCycles) {
+            if (!std::isfinite(r)) { c.err = "multigrid residual is not finite"; return SARAS_NOT_FINITE; }
+            for (int q = 0; q < std::max(1, c.p.mixedCycles); ++q) {
+                if ((s = vcycle<float>(c, true, q == 0))) return s;
+                cyc += 1;
+            }
+            steps += 1;
+            if ((s = refine(cur, true, r, bad))) return s;
+            if (bad) break;
+            cur ^= 1;
+        }
+        if (bad) break;
+        // the FP64 result, and the exact residual of those FP64 values
+        k_fx_to<<<nbF, 256, 0, c.stream>>>(L0.pa(), c.fx[cur ^ 1], c.fx[cur], L0.count, inv2s, sc, dflag);
+        count_launch(c);
+        double rf = 0;
+        if ((s = refine(cur ^ 1, false, rf, bad))) return s;
+        if (bad) break;
+        r = rf;
+        cur ^= 1;
+        if (r <= target || cyc >= c.mgMaxCycles) { done = true; return SARAS_OK; }
+    }
+    // out of range: restart from the previous Pp in FP64
+    L0.cur = 0;
+    k_mg_init_p<double><<<gc, bcd, 0, c.stream>>>(lview<double>(L0, L0.pa()), lcview<double>(L0, c.f[SARAS_FIELD_PP]), bc0);
+    count_launch(c);
+    r = 0; source = 0; cyc = 0; steps = 0;
+    return chk(c, "fixed-point fallback");
+}
+
 // Target modes: plain FP64 V-cycles or FP32 V-cycles inside FP64 refinement.
 static int mg_solve_target(Ctx &c, int *cycles, double *residual, saras_step_stats *st) {
     int s;
@@ -1035,7 +1267,7 @@ static int mg_solve_target(Ctx &c, int *cycles, double *residual, saras_step_sta
     k_final_reduce<<<1, 256, 0, c.stream>>>(c.red, nb, 0, c.dscal + 30);
     double wsum = 1.0;
     for (int d = 0; d < 3; ++d) wsum *= (double)L0.n[d];
-    k_tgt_rhs<<<g, b, 0, c.stream>>>(lview<double>(L0, L0.r), lcview<double>(L0, c.f[SARAS_FIELD_MGRHS]), bc0, c.dscal + 30, wsum, c.dscal + 31);
+    k_tgt_rhs<<<g, b, 0, c.stream>>>(lview<double>(L0, L0.r), lcview<double>(L0, c.f[SARAS_FIELD_MGRHS]), bc0, c.dscal + 30, 1.0 / wsum, c.dscal + 31);
     // pressure history for the learned / extrapolated guess
     bool wantGuess = c.guessMode != SARAS_GUESS_PREVIOUS;
     if (wantGuess || c.collecting) {
@@ -1077,18 +1309,22 @@ static int mg_solve_target(Ctx &c, int *cycles, double *residual, saras_step_sta
         return SARAS_OK;
     };
     double r = 0;
+    int source = 0, cyc = 0, steps = 0;
+    bool fixedDone = false;
+    if (c.mgMode == SARAS_MG_MIXED && L0.lx == L0.ly && L0.ly == L0.lz) {
+        if ((s = mixed_fixed(c, bmax, target, wantGuess, r, source, cyc, steps, fixedDone, st))) return s;
+    }
+    if (!fixedDone) {
     if ((s = fine_res(false, &r))) return s;
-    int source = 0;
     if (wantGuess && c.histCount >= 2) {
-        bool net = c.guessMode == SARAS_GUESS_LEARNED;
-        int gs = unet_guess(c, L0.r, L0.pb(), net);
+        int gs = unet_guess(c, L0.r, L0.pb(), c.guessMode);
         if (gs == SARAS_OK) {
             L0.cur ^= 1;
             double rg = 0;
             if ((s = fine_res(false, &rg))) return s;
             if (rg < r) {
                 r = rg;
-                source = net ? 1 : 2;
+                source = c.guessMode;
             } else {
                 L0.cur ^= 1;   // keep the previous pressure (and recompute its FP32 residual)
                 if ((s = fine_res(false, &r))) return s;
@@ -1098,7 +1334,6 @@ static int mg_solve_target(Ctx &c, int *cycles, double *residual, saras_step_sta
         }
     }
     if (st) { st->guess_residual = bmax > 0 ? r / bmax : r; st->guess_source = source; }
-    int cyc = 0, steps = 0;
     while (r > target && cyc < c.mgMaxCycles) {
         if (!std::isfinite(r)) { c.err = "multigrid residual is not finite"; return SARAS_NOT_FINITE; }
         if (c.mgMode == SARAS_MG_PLAIN_TARGET) {
@@ -1114,6 +1349,7 @@ static int mg_solve_target(Ctx &c, int *cycles, double *residual, saras_step_sta
             steps += 1;
             if ((s = fine_res(true, &r))) return s;
         }
+    }
     }
     if (st) { st->refine_steps = steps; st->fine_residual = bmax > 0 ? r / bmax : r; }
     k_mg_output<<<grid_blocks(L0.count), 256, 0, c.stream>>>(lview<double>(L0, c.f[SARAS_FIELD_PP]), lcview<double>(L0, L0.pa()), bc0,

@@ -214,8 +214,10 @@ __device__ __forceinline__ double fw_restrict(const L0View &f, int z, int y, int
 //   0: R(r_ex) / s_r   residual of the extrapolated guess 2 P1 - P2
 //   1: R(P1 - P2) / s_d
 //   2: R(b) / s_b
-// and, with `target`, the training target d* = R(P_new - (2 P1 - P2)) / s_d.
-// scales = {s_b, s_d, s_r}.
+// and, with `target`, the training target d* = R(P_new - (2 P1 - P2)) / s_t,
+// the error of the extrapolation in units of s_t = s_r L^2 / (4 pi^2) (the
+// size A^-1 gives a residual of size s_r made of the domain's lowest modes).
+// scales = {s_b, s_d, s_r, -, -, s_t}.
 __global__ void k_features(L0View b, L0View p1, L0View p2, L0View rex, L0View pnew, Grid3 g1, const double *scales, float *feat,
                            float *target) {
     long v = blockIdx.x * (long)blockDim.x + threadIdx.x;
@@ -226,7 +228,7 @@ __global__ void k_features(L0View b, L0View p1, L0View p2, L0View rex, L0View pn
     feat[v * 3 + 0] = (float)(fw_restrict(rex, z, y, x) / sr);
     feat[v * 3 + 1] = (float)((r1 - r2) / sd);
     feat[v * 3 + 2] = (float)(fw_restrict(b, z, y, x) / sb);
-    if (target) target[v] = (float)((fw_restrict(pnew, z, y, x) - (2.0 * r1 - r2)) / sd);
+    if (target) target[v] = (float)((fw_restrict(pnew, z, y, x) - (2.0 * r1 - r2)) / scales[5]);
 }
 
 // Expand 3-channel FP32 features into the 16-channel BF16 network input.
@@ -260,21 +262,22 @@ __global__ void k_loss(const float *d, const float *dstar, bf16 *gout, long nv, 
     }
 }
 
-// Guess on level 0: 2 P1 - P2 + s_p * prolong(d), core points, with face ghosts.
+// Guess on level 0: 2 P1 - P2 (quad: 3 P1 - 3 P2 + P3) + alpha s_t prolong(d),
+// core points, with face ghosts.
 __global__ void k_apply_guess(double *out, L0View p1, L0View p2, const float *d, Grid3 g1, const double *scales, int use_net,
-                              int per0, int per1, int per2) {
+                              int per0, int per1, int per2, const double *alpha, L0View p3, int quad) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y * blockDim.y + threadIdx.y;
     int i = blockIdx.z;
     if (i > p1.n[0] || j > p1.n[1] || k > p1.n[2]) return;
-    double v = 2.0 * p1.at(i, j, k) - p2.at(i, j, k);
+    double v = quad ? 3.0 * (p1.at(i, j, k) - p2.at(i, j, k)) + p3.at(i, j, k) : 2.0 * p1.at(i, j, k) - p2.at(i, j, k);
     if (use_net) {
         int z0 = i >> 1, y0 = j >> 1, x0 = k >> 1;
         int z1 = min(z0 + (i & 1), g1.D - 1), y1 = min(y0 + (j & 1), g1.H - 1), x1 = min(x0 + (k & 1), g1.W - 1);
         auto at = [&](int a, int b, int c) { return (double)d[((long)a * g1.H + b) * g1.W + c]; };
         double s = at(z0, y0, x0) + at(z0, y0, x1) + at(z0, y1, x0) + at(z0, y1, x1) + at(z1, y0, x0) + at(z1, y0, x1) +
                    at(z1, y1, x0) + at(z1, y1, x1);
-        v += scales[1] * 0.125 * s;
+        v += (alpha ? *alpha : 1.0) * scales[5] * 0.125 * s;
     }
     long sy = p1.n[2] + 3, sx = (long)(p1.n[1] + 3) * sy;
     auto put = [&](int a, int b, int c) { out[(long)(a + 1) * sx + (long)(b + 1) * sy + (c + 1)] = v; };
@@ -339,10 +342,54 @@ __global__ void k_maxabs_diff(L0View a, L0View b, double *out) {
     block_max_to(m, out);
 }
 
-__global__ void k_floor_scale(double *s, double floor_) {
-    if (threadIdx.x == 0 && blockIdx.x == 0)
+__global__ void k_floor_scale(double *s, double floor_, double lfac) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
         for (int q = 0; q < 3; ++q)
             if (!(s[q] > floor_)) s[q] = floor_;
+        s[5] = s[2] * lfac;
+    }
+}
+
+constexpr int kAlphaBlocks = 304;   // 2 blocks per SM for the step-length reduction
+
+// Step length of the network correction c = g - e (g: extrapolation plus the
+// full correction, e: extrapolation alone).  With r_e = b - A e and
+// r_g = b - A g, A c = r_e - r_g =: q, and alpha = <r_e, q> / <q, q> minimises
+// |b - A (e + alpha c)|_2.  Per-block partial sums of <r_e, q> and <q, q>.
+__global__ void k_alpha_dots(L0View g, L0View b, L0View rex, double lx, double ly, double lz, double *part) {
+    __shared__ double sm[2][32];
+    long n = (long)(g.n[0] + 1) * (g.n[1] + 1) * (g.n[2] + 1);
+    double rq = 0.0, qq = 0.0;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+        int k = (int)(t % (g.n[2] + 1)), j = (int)((t / (g.n[2] + 1)) % (g.n[1] + 1)), i = (int)(t / ((long)(g.n[2] + 1) * (g.n[1] + 1)));
+        double C = g.at(i, j, k);
+        double lap = lx * (g.at(i + 1, j, k) + g.at(i - 1, j, k)) + ly * (g.at(i, j + 1, k) + g.at(i, j - 1, k)) +
+                     lz * (g.at(i, j, k + 1) + g.at(i, j, k - 1)) - 2.0 * (lx + ly + lz) * C;
+        double re = rex.at(i, j, k);
+        double q = re - (b.at(i, j, k) - lap);
+        rq += re * q;
+        qq += q * q;
+    }
+    rq = warp_sum(rq);
+    qq = warp_sum(qq);
+    if ((threadIdx.x & 31) == 0) { sm[0][threadIdx.x >> 5] = rq; sm[1][threadIdx.x >> 5] = qq; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, c = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { a += sm[0][w]; c += sm[1][w]; }
+        part[2 * blockIdx.x] = a;
+        part[2 * blockIdx.x + 1] = c;
+    }
+}
+
+// alpha from the partial sums (fixed order), limited to [0, 1.5]; 0 when the
+// correction has no effect on the residual or the sums are not finite.
+__global__ void k_alpha_final(const double *part, int nb, double *alpha) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double a = 0.0, c = 0.0;
+    for (int q = 0; q < nb; ++q) { a += part[2 * q]; c += part[2 * q + 1]; }
+    double al = (c > 0.0 && isfinite(a) && isfinite(c)) ? a / c : 0.0;
+    *alpha = fmin(fmax(al, 0.0), 1.5);
 }
 
 // r = b - Lap(p) over the level-0 core (FP64), uniform-grid Laplacian.
@@ -376,7 +423,7 @@ struct UNet {
     std::vector<bf16 *> grd;          // gradient buffers
     bf16 *x0 = nullptr;
     float *out = nullptr, *feat = nullptr;
-    double *scales = nullptr;         // s_b, s_d, s_r, last loss (device)
+    double *scales = nullptr;         // s_b, s_d, s_r, last loss, step length alpha (device)
     double *ext = nullptr, *rex = nullptr;   // level-0 extrapolated guess and its residual
     // training samples: 3 feature channels + target per voxel
     std::vector<float *> samples;
@@ -485,14 +532,14 @@ static int unet_alloc(Ctx &c) {
     long n1 = u->g[0].n();
     SARAS_CUDA_TRY(cudaMalloc(&u->out, sizeof(float) * n1));
     SARAS_CUDA_TRY(cudaMalloc(&u->feat, sizeof(float) * 4 * n1));
-    SARAS_CUDA_TRY(cudaMalloc(&u->scales, sizeof(double) * 4));
+    SARAS_CUDA_TRY(cudaMalloc(&u->scales, sizeof(double) * 8));
     SARAS_CUDA_TRY(cudaMalloc(&u->ext, sizeof(double) * c.lv[0].count));
     SARAS_CUDA_TRY(cudaMalloc(&u->rex, sizeof(double) * c.lv[0].count));
     SARAS_CUDA_TRY(cudaMemset(u->ext, 0, sizeof(double) * c.lv[0].count));
     SARAS_CUDA_TRY(cudaMemset(u->rex, 0, sizeof(double) * c.lv[0].count));
     SARAS_CUDA_TRY(cudaMalloc(&u->err, sizeof(int)));
     SARAS_CUDA_TRY(cudaMemset(u->err, 0, sizeof(int)));
-    SARAS_CUDA_TRY(cudaMalloc(&u->part, sizeof(double) * ((n1 + 255) / 256 + 1)));
+    SARAS_CUDA_TRY(cudaMalloc(&u->part, sizeof(double) * std::max((n1 + 255) / 256 + 1, 2L * kAlphaBlocks)));
     u->cap = 32;
     return SARAS_OK;
 }
@@ -669,7 +716,7 @@ static L0View l0view(const Ctx &c, const double *p) {
 static int ensure_hist(Ctx &c) {
     if (c.pHist[0]) return SARAS_OK;
     size_t bytes = sizeof(double) * c.lv[0].count;
-    for (int q = 0; q < 2; ++q) {
+    for (int q = 0; q < 3; ++q) {
         SARAS_CUDA_TRY(cudaMalloc(&c.pHist[q], bytes));
         SARAS_CUDA_TRY(cudaMemsetAsync(c.pHist[q], 0, bytes, c.stream));
     }
@@ -683,13 +730,14 @@ static int prepare_features(Ctx &c, const double *b, const double *pnew, float *
     const Level &L0 = c.lv[0];
     dim3 b2(64, 4), g2((L0.n[2] + 1 + 63) / 64, (L0.n[1] + 1 + 3) / 4, L0.n[0] + 1);
     k_apply_guess<<<g2, b2, 0, c.stream>>>(u->ext, l0view(c, c.pHist[0]), l0view(c, c.pHist[1]), nullptr, u->g[0], nullptr, 0,
-                                           c.p.xPer, c.p.yPer, c.p.zPer);
+                                           c.p.xPer, c.p.yPer, c.p.zPer, nullptr, l0view(c, c.pHist[2]), 0);
     k_residual64<<<g2, b2, 0, c.stream>>>(u->rex, l0view(c, u->ext), l0view(c, b), L0.lx, L0.ly, L0.lz);
     SARAS_CUDA_TRY(cudaMemsetAsync(u->scales, 0, sizeof(double) * 3, c.stream));
     k_maxabs_core<<<304, 256, 0, c.stream>>>(l0view(c, b), u->scales);
     k_maxabs_diff<<<304, 256, 0, c.stream>>>(l0view(c, c.pHist[0]), l0view(c, c.pHist[1]), u->scales + 1);
     k_maxabs_core<<<304, 256, 0, c.stream>>>(l0view(c, u->rex), u->scales + 2);
-    k_floor_scale<<<1, 32, 0, c.stream>>>(u->scales, 1e-300);
+    double lfac = (c.p.Lx * c.p.Lx + c.p.Ly * c.p.Ly + c.p.Lz * c.p.Lz) / (3.0 * 4.0 * M_PI * M_PI);
+    k_floor_scale<<<1, 32, 0, c.stream>>>(u->scales, 1e-300, lfac);
     long n1 = u->g[0].n();
     k_features<<<(int)((n1 + 255) / 256), 256, 0, c.stream>>>(l0view(c, b), l0view(c, c.pHist[0]), l0view(c, c.pHist[1]),
                                                               l0view(c, u->rex), l0view(c, pnew ? pnew : c.pHist[0]), u->g[0],
@@ -707,7 +755,10 @@ namespace saras {
 int unet_begin_solve(Ctx &c) {
     int s = ensure_hist(c);
     if (s) return s;
-    std::swap(c.pHist[0], c.pHist[1]);
+    double *oldest = c.pHist[2];
+    c.pHist[2] = c.pHist[1];
+    c.pHist[1] = c.pHist[0];
+    c.pHist[0] = oldest;
     SARAS_CUDA_TRY(cudaMemcpyAsync(c.pHist[0], c.f[SARAS_FIELD_PP], sizeof(double) * c.lv[0].count, cudaMemcpyDeviceToDevice, c.stream));
     c.histCount += 1;
     return SARAS_OK;
@@ -715,8 +766,10 @@ int unet_begin_solve(Ctx &c) {
 
 // Build the learned (or extrapolated) guess for the level-0 iterate into `dst`;
 // b is the compatible right-hand side.  Returns BAD_CONFIG if unavailable.
-int unet_guess(Ctx &c, const double *b, double *dst, bool use_net) {
-    if (c.histCount < 2) return SARAS_BAD_CONFIG;
+int unet_guess(Ctx &c, const double *b, double *dst, int mode) {
+    bool use_net = mode == SARAS_GUESS_LEARNED;
+    int quad = mode == SARAS_GUESS_QUADRATIC ? 1 : 0;
+    if (c.histCount < 2 + quad) return SARAS_BAD_CONFIG;
     int s;
     if (use_net) {
         if (!c.unet || !U(c)->trained) return SARAS_BAD_CONFIG;
@@ -735,8 +788,17 @@ int unet_guess(Ctx &c, const double *b, double *dst, bool use_net) {
     const Level &L0 = c.lv[0];
     dim3 b2(64, 4), g2((L0.n[2] + 1 + 63) / 64, (L0.n[1] + 1 + 3) / 4, L0.n[0] + 1);
     Grid3 g1 = u ? u->g[0] : Grid3{1, 1, 1};
+    if (use_net) {
+        // full correction first, then its least-squares step length, then the guess with that step
+        k_apply_guess<<<g2, b2, 0, c.stream>>>(dst, l0view(c, c.pHist[0]), l0view(c, c.pHist[1]), u->out, g1, u->scales, 1,
+                                               c.p.xPer, c.p.yPer, c.p.zPer, nullptr, l0view(c, c.pHist[2]), 0);
+        k_alpha_dots<<<kAlphaBlocks, 256, 0, c.stream>>>(l0view(c, dst), l0view(c, b), l0view(c, u->rex), L0.lx, L0.ly, L0.lz, u->part);
+        k_alpha_final<<<1, 32, 0, c.stream>>>(u->part, kAlphaBlocks, u->scales + 4);
+        count_launch(c, 3);
+    }
     k_apply_guess<<<g2, b2, 0, c.stream>>>(dst, l0view(c, c.pHist[0]), l0view(c, c.pHist[1]), use_net ? u->out : nullptr, g1,
-                                           use_net ? u->scales : nullptr, use_net ? 1 : 0, c.p.xPer, c.p.yPer, c.p.zPer);
+                                           use_net ? u->scales : nullptr, use_net ? 1 : 0, c.p.xPer, c.p.yPer, c.p.zPer,
+                                           use_net ? u->scales + 4 : nullptr, l0view(c, c.pHist[2]), quad);
     count_launch(c);
     return ucheck(c, "guess");
 }

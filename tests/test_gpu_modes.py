@@ -46,15 +46,48 @@ def test_mixed_matches_plain_fp64():
         assert C.rel_err(b.get(f), a.get(f)) < 1e-8, F.FIELD_NAMES[f]
 
 
-def test_fast_kernels_match_reference_arithmetic():
-    """fastKernels=1 changes rounding only: both solve the same CN and Poisson systems."""
+@pytest.mark.parametrize("fast", [1, 2])
+def test_fast_kernels_match_reference_arithmetic(fast):
+    """fastKernels=1 (fused forms) and 2 (split-FP64 CN update) change rounding
+    only: all solve the same CN and Poisson systems."""
     _, a = target_case(F.MG_PLAIN_TARGET, fast=0)
-    _, b = target_case(F.MG_PLAIN_TARGET, fast=1)
+    _, b = target_case(F.MG_PLAIN_TARGET, fast=fast)
     for _ in range(3):
         a.time_advance()
         b.time_advance()
     for f in (F.FIELD_VX, F.FIELD_VY, F.FIELD_VZ):
         assert C.rel_err(b.get(f), a.get(f)) < 1e-8, F.FIELD_NAMES[f]
+
+
+@pytest.mark.parametrize("kind", ["ldc", "rbc"])
+def test_split_fp64_cn_matches_fp64(kind):
+    """One CN Jacobi solve per component with the split-FP64 update
+    (fastKernels=2) against the FP64 fused form (fastKernels=1): same
+    iteration counts, fields within 1e-11 (the Jacobi tolerance is 1e-8)."""
+    mk = C.ldc if kind == "ldc" else C.rbc
+    rng = np.random.default_rng(11)
+    out = {}
+    for fast in (1, 2):
+        p = mk(ind=5, depth=3) if kind == "ldc" else mk(ind=(5, 5, 4), depth=3)
+        p.fastKernels = fast
+        g = S.Solver(p)
+        C.initialise(g, p, kind)
+        r = np.random.default_rng(11)
+        comps = [0, 1, 2] + ([3] if kind == "rbc" else [])
+        res = []
+        for c in comps:
+            f = F.FIELD_T if c == 3 else F.FIELD_VX + c
+            rf = F.FIELD_TRHS if c == 3 else F.FIELD_NSE_X + c
+            V = g.get(f)
+            g.set(rf, V + 1e-3 * r.standard_normal(V.shape))
+            s, it, err = g.cn_solve(c)
+            assert s == 0
+            res.append((it, g.get(f)))
+        out[fast] = res
+        g.close()
+    for (ia, a), (ib, b) in zip(out[1], out[2]):
+        assert ia == ib
+        assert np.max(np.abs(a - b)) < 1e-11
 
 
 def test_nan_input_reports_not_finite():
