@@ -355,6 +355,7 @@ int saras_axpby(saras_ctx *h, int dst, double a, int src, double b) { CTX_OR_FAI
 
 int saras_cn_solve(saras_ctx *h, int component, int *iters, double *max_error) {
     CTX_OR_FAIL(h);
+    for (int &q : h->c.n0Fresh) q = 0;   // nseRHS may have been set by the caller
     return cn_solve(h->c, component, iters, max_error);
 }
 

@@ -105,20 +105,55 @@ __device__ __forceinline__ T warp_sum(T v) {
     return v;
 }
 
-// Block-wide max of non-negative values into *out (atomic).
-__device__ __forceinline__ void block_max_to(double v, double *out) {
-    __shared__ double sm[32];
-    v = warp_max(v);
+// Block-wide max of non-negative values into *out (atomic), exact, on the
+// 64-bit patterns (integer pipe; NaN stays above Inf).
+__device__ __forceinline__ void block_max_bits_to(unsigned long long u, double *out) {
+    __shared__ unsigned long long sm[32];
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long x = __shfl_xor_sync(0xffffffffu, u, o);
+        u = x > u ? x : u;
+    }
     int nw = (blockDim.x * blockDim.y * blockDim.z + 31) >> 5;
     int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
     int lane = tid & 31, w = tid >> 5;
     __syncthreads();
-    if (lane == 0) sm[w] = v;
+    if (lane == 0) sm[w] = u;
     __syncthreads();
     if (w == 0) {
-        double x = lane < nw ? sm[lane] : 0.0;
-        x = warp_max(x);
-        if (lane == 0 && x > 0.0) atomic_max_nonneg(out, x);
+        unsigned long long x = lane < nw ? sm[lane] : 0ull;
+        for (int o = 16; o > 0; o >>= 1) {
+            unsigned long long y = __shfl_xor_sync(0xffffffffu, x, o);
+            x = y > x ? y : x;
+        }
+        if (lane == 0 && x > 0ull) atomicMax(reinterpret_cast<unsigned long long *>(out), x);
+    }
+}
+
+// |v| as the integer that orders like it (for running maxima off the FP64 pipe).
+__device__ __forceinline__ unsigned long long abs_bits(double v) {
+    return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+}
+
+__device__ __forceinline__ void block_max_to(double v, double *out) { block_max_bits_to(abs_bits(v), out); }
+
+// Block-wide max of |v| for float values into the double *out (atomic), on
+// the integer bits: non-negative floats order like their bit patterns, NaN
+// above Inf, so a NaN anywhere reaches *out as NaN.  redux.sync does the warp
+// step in one instruction; a warp max in FP64 would cost GB300's FP64 pipe
+// about as much as a stencil.
+__device__ __forceinline__ void block_maxf_to(float v, double *out) {
+    __shared__ unsigned smf[32];
+    unsigned u = __reduce_max_sync(0xffffffffu, __float_as_uint(v) & 0x7fffffffu);
+    int nw = (blockDim.x * blockDim.y * blockDim.z + 31) >> 5;
+    int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    int lane = tid & 31, w = tid >> 5;
+    __syncthreads();
+    if (lane == 0) smf[w] = u;
+    __syncthreads();
+    if (w == 0) {
+        unsigned x = lane < nw ? smf[lane] : 0u;
+        x = __reduce_max_sync(0xffffffffu, x);
+        if (lane == 0 && x > 0u) atomic_max_nonneg(out, (double)__uint_as_float(x));
     }
 }
 

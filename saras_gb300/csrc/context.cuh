@@ -107,8 +107,9 @@ struct Ctx {
     void *unet = nullptr;
     double *pHist[3] = {nullptr, nullptr, nullptr};   // Pp of the three previous steps (newest first)
     long long *fx[3] = {nullptr, nullptr, nullptr};   // level-0 fixed-point iterate ping-pong + rhs (mixed mode)
-    float *cnp = nullptr;      // split-FP64 Jacobi solve: N0 and the D ping-pong as float pairs
+    float *cnp = nullptr;      // split-FP64 Jacobi solve: N0 of each component and the D ping-pong (float pairs)
     long cnpCount = 0;
+    int n0Fresh[4] = {0, 0, 0, 0};   // N0 of component q written by this step's right-hand side
     int histCount = 0;
     bool collecting = false;
     // profiling

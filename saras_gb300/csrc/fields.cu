@@ -22,6 +22,13 @@
 namespace saras {
 
 // ------------------------------------------------------------------ constants
+// Constants of the split-FP64 Jacobi solve (see k_cn_delta).
+struct CnDf {
+    fpair kc[3];     // k1 c1, k1 c2, k1 c3 as float pairs (N0)
+    float kf[3];     // the same as floats (sweeps: S_d(D) is small)
+    fpair invDn;     // 1 / Dn
+};
+
 struct UC {                 // uniform-grid stencil constants
     double ih[3], ih2[3];   // 1/dXi and pow(1/dXi, 2)                 (derivative.cc:67-69)
     double m1[3];           // first-derivative metric xi_x = 1/L        (derivative.cc:77-105)
@@ -324,7 +331,7 @@ struct RhsDf {
 };
 
 template <int C>
-__global__ void __launch_bounds__(256) k_rhs_df(RhsArgs a, RhsDf q) {
+__global__ void __launch_bounds__(256) k_rhs_df(RhsArgs a, RhsDf q, CnDf cf, float *n0h, float *n0l) {
     int i, j, k;
     if (!box_point(a.b, i, j, k)) return;
     const View3<const double> &F = a.F;
@@ -333,9 +340,8 @@ __global__ void __launch_bounds__(256) k_rhs_df(RhsArgs a, RhsDf q) {
     fpair ex = fp_of(F(i + 1, j, k)), wx = fp_of(F(i - 1, j, k));
     fpair ey = fp_of(F(i, j + 1, k)), wy = fp_of(F(i, j - 1, k));
     fpair ez = fp_of(F(i, j, k + 1)), wz = fp_of(F(i, j, k - 1));
-    fpair h = fp_mul(q.k2[0], fp_add(fp_add(ex, wx), c2));
-    h = fp_add(h, fp_mul(q.k2[1], fp_add(fp_add(ey, wy), c2)));
-    h = fp_add(h, fp_mul(q.k2[2], fp_add(fp_add(ez, wz), c2)));
+    fpair Sx = fp_add(fp_add(ex, wx), c2), Sy = fp_add(fp_add(ey, wy), c2), Sz = fp_add(fp_add(ez, wz), c2);
+    fpair h = fp_add(fp_add(fp_mul(q.k2[0], Sx), fp_mul(q.k2[1], Sy)), fp_mul(q.k2[2], Sz));
     h = fp_add(h, fp_neg(fp_mul(Slices<C, 0>::sump(a.V.v[0], i, j, k), fp_mul(fp_add(ex, fp_neg(wx)), q.k1n[0]))));
     h = fp_add(h, fp_neg(fp_mul(Slices<C, 1>::sump(a.V.v[1], i, j, k), fp_mul(fp_add(ey, fp_neg(wy)), q.k1n[1]))));
     h = fp_add(h, fp_neg(fp_mul(Slices<C, 2>::sump(a.V.v[2], i, j, k), fp_mul(fp_add(ez, fp_neg(wz)), q.k1n[2]))));
@@ -344,6 +350,12 @@ __global__ void __launch_bounds__(256) k_rhs_df(RhsArgs a, RhsDf q) {
     h = fp_add(h, fp_neg(fp_mul(q.g[C], fp_add(fp_of(sp), fp_neg(fp_of(a.P(i, j, k)))))));
     h = fp_mul(h, q.dt);
     a.H(i, j, k) = (f0 + f2d(h.h)) + f2d(h.l);
+    // N0 = H - F + k1 sum_d c_d S_d(F) of the Jacobi solve that follows (k_cn_pack's
+    // quantity, from the same split values)
+    fpair n0 = fp_add(h, fp_add(fp_add(fp_mul(cf.kc[0], Sx), fp_mul(cf.kc[1], Sy)), fp_mul(cf.kc[2], Sz)));
+    long o = F.off(i, j, k);
+    n0h[o] = n0.h;
+    n0l[o] = n0.l;
 }
 
 static RhsFast make_rhs_fast(const Ctx &c, double visc) {
@@ -477,10 +489,7 @@ __global__ void __launch_bounds__(256) k_cn_fast(CnFast a) {
             double A = fma(a.c1, ew, fma(a.c2, ns, a.c3 * ud));
             double o = fma(A, a.k1, a.rhs(i, j, k)) * a.invDn;
             a.out(i, j, k) = o;
-            if (a.withResidual) {
-                res = fabs(C - o);
-                if (res != res) res = INFINITY;
-            }
+            if (a.withResidual) res = C - o;   // |.| and NaN ordering in block_max_to (integer pipe)
         } else {
             a.out(i, j, k) = bc_resolve(a.prog, i, j, k, [&](int x, int y, int z) -> double {
                 return in_box(a.prog.blo, a.prog.bhi, x, y, z) ? cn_guess_fast(a, x, y, z) : 0.0;
@@ -505,12 +514,6 @@ __global__ void __launch_bounds__(256) k_cn_fast(CnFast a) {
 // tolerance is 1e-8).  Boundary points: the field's boundary program resolved
 // on C0 + D in float pairs (constant -> value, copy -> copy, reflect -> 2c - v),
 // then minus C0 there, as the FP64 form resolves it on C.
-struct CnDf {
-    fpair kc[3];     // k1 c1, k1 c2, k1 c3 as float pairs (N0)
-    float kf[3];     // the same as floats (sweeps: S_d(D) is small)
-    fpair invDn;     // 1 / Dn
-};
-
 static CnDf cn_df_consts(const CnFast &fa) {
     CnDf d;
     auto pr = [](double x) { fpair r; r.h = (float)x; r.l = (float)(x - (double)r.h); return r; };
@@ -570,48 +573,62 @@ __device__ __forceinline__ fpair fp_of_c(double x) {
     return r;
 }
 
-__global__ void __launch_bounds__(256) k_cn_delta(CnDelta a) {
-    int i, j, k;
-    bool ok = box_point(a.full, i, j, k);
-    double res = 0.0;
-    if (ok) {
-        long o = a.off(i, j, k);
-        fpair out;
-        if (in_box(a.prog.blo, a.prog.bhi, i, j, k)) {
-            fpair corr;
-            out = cn_delta_image(a, o, corr);
-            if (a.withResidual) res = f_finite(corr.h) ? f2d(fabsf(corr.h)) : INFINITY;
-        } else {
-            // bc_resolve on C0 + D in float pairs (the FP64 form's bc_resolve with
-            // base = Jacobi image at bulk points, 0 elsewhere), then minus C0 here
-            const BcProgram &prog = a.prog;
-            int chain[kMaxBcOps];
-            int nchain = 0;
-            fpair value = fpair{0.0f, 0.0f};
-            bool haveConst = false;
-            int q[3] = {i, j, k};
-            for (int op = prog.nops - 1; op >= 0; --op) {
-                const BcOp &b = prog.op[op];
-                if (q[0] < b.lo[0] || q[0] > b.hi[0] || q[1] < b.lo[1] || q[1] > b.hi[1] || q[2] < b.lo[2] || q[2] > b.hi[2]) continue;
-                if (b.kind == OP_CONST) { value = fp_of_c(b.c); haveConst = true; break; }
-                chain[nchain++] = op;
-                q[0] += b.shift[0]; q[1] += b.shift[1]; q[2] += b.shift[2];
-            }
-            if (!haveConst && in_box(prog.blo, prog.bhi, q[0], q[1], q[2])) {
-                long os = a.off(q[0], q[1], q[2]);
-                fpair corr;
-                value = fp_add(fp_of(a.C0[os]), cn_delta_image(a, os, corr));
-            }
-            for (int cix = nchain - 1; cix >= 0; --cix) {
-                const BcOp &b = prog.op[chain[cix]];
-                if (b.kind == OP_REFLECT) value = fp_add(fp_of_c(2.0 * b.c), fp_neg(value));
-            }
-            out = fp_add(value, fp_neg(fp_of(a.C0[o])));
-        }
-        a.oh[o] = out.h;
-        a.ol[o] = out.l;
+// Boundary point (i, j, k): the program resolved on C0 + D in float pairs (the
+// FP64 form's bc_resolve with base = Jacobi image at bulk points, 0 elsewhere),
+// minus C0 there.
+__device__ __noinline__ fpair cn_delta_boundary(const CnDelta &a, int i, int j, int k, long o) {
+    const BcProgram &prog = a.prog;
+    int chain[kMaxBcOps];
+    int nchain = 0;
+    fpair value = fpair{0.0f, 0.0f};
+    bool haveConst = false;
+    int q[3] = {i, j, k};
+    for (int op = prog.nops - 1; op >= 0; --op) {
+        const BcOp &b = prog.op[op];
+        if (q[0] < b.lo[0] || q[0] > b.hi[0] || q[1] < b.lo[1] || q[1] > b.hi[1] || q[2] < b.lo[2] || q[2] > b.hi[2]) continue;
+        if (b.kind == OP_CONST) { value = fp_of_c(b.c); haveConst = true; break; }
+        chain[nchain++] = op;
+        q[0] += b.shift[0]; q[1] += b.shift[1]; q[2] += b.shift[2];
     }
-    if (a.withResidual) block_max_to(res, a.resMax);
+    if (!haveConst && in_box(prog.blo, prog.bhi, q[0], q[1], q[2])) {
+        long os = a.off(q[0], q[1], q[2]);
+        fpair corr;
+        value = fp_add(fp_of(a.C0[os]), cn_delta_image(a, os, corr));
+    }
+    for (int cix = nchain - 1; cix >= 0; --cix) {
+        const BcOp &b = prog.op[chain[cix]];
+        if (b.kind == OP_REFLECT) value = fp_add(fp_of_c(2.0 * b.c), fp_neg(value));
+    }
+    return fp_add(value, fp_neg(fp_of(a.C0[o])));
+}
+
+// One thread per (j, k) column of the full box, marching kCnMarch points
+// along i (block 32 x 8): the index work is paid once per column segment.
+constexpr int kCnMarch = 8;
+
+__global__ void __launch_bounds__(256) k_cn_delta(CnDelta a) {
+    int k = a.full.lo[2] + blockIdx.x * 32 + threadIdx.x;
+    int j = a.full.lo[1] + blockIdx.y * 8 + threadIdx.y;
+    int i0 = a.full.lo[0] + blockIdx.z * kCnMarch;
+    unsigned m = 0u;
+    if (k < a.full.lo[2] + a.full.ext[2] && j < a.full.lo[1] + a.full.ext[1]) {
+        int iend = min(i0 + kCnMarch, a.full.lo[0] + a.full.ext[0]);
+        bool bulkJK = j >= a.prog.blo[1] && j <= a.prog.bhi[1] && k >= a.prog.blo[2] && k <= a.prog.bhi[2];
+        for (int i = i0; i < iend; ++i) {
+            long o = a.off(i, j, k);
+            fpair out;
+            if (bulkJK && i >= a.prog.blo[0] && i <= a.prog.bhi[0]) {
+                fpair corr;
+                out = cn_delta_image(a, o, corr);
+                m = max(m, __float_as_uint(corr.h) & 0x7fffffffu);   // |corr| bits; NaN stays above Inf
+            } else {
+                out = cn_delta_boundary(a, i, j, k, o);
+            }
+            a.oh[o] = out.h;
+            a.ol[o] = out.l;
+        }
+    }
+    if (a.withResidual) block_maxf_to(__uint_as_float(m), a.resMax);
 }
 
 // C0 + D in FP64 over the whole padded array (in place on the field).
@@ -1017,6 +1034,63 @@ int axpby(Ctx &c, int dst, double a, int src, double b) {
     return check_launch(c, "axpby");
 }
 
+// Constants of the Jacobi solve of component comp (hydro_d3.cc:370-533,
+// scalar_d3.cc:373-591): the reference form in a, the fused forms in fa.
+static void cn_setup(Ctx &c, int comp, CnArgs &a, CnFast &fa) {
+    int field = comp == 3 ? SARAS_FIELD_T : SARAS_FIELD_VX + comp;
+    int rhsField = comp == 3 ? SARAS_FIELD_TRHS : SARAS_FIELD_NSE_X + comp;
+    const FieldInfo &f = c.info[field];
+    a.rhs = cview(c, rhsField);
+    a.prog = f.full;
+    a.full = full_box(f);
+    // Metrics: every component's xix2/ety2/ztz2 equal pow(1/L,2) on uniform grids
+    // (the T solve's ztz2Colloc of scalar_d3.cc:551,570 has the same value).
+    double xix2 = c.m2[0], ety2 = c.m2[1], ztz2 = c.m2[2];
+    a.c1 = c.hy2hz2 * xix2;
+    a.c2 = c.hz2hx2 * ety2;
+    a.c3 = c.hx2hy2 * ztz2;
+    double B = (c.hy2hz2 * xix2 + c.hz2hx2 * ety2) + c.hx2hy2 * ztz2;
+    a.dt = c.dt;
+    if (!c.scalar) {
+        a.scalarForm = 0;
+        a.coef = 0;
+        a.X = c.hx2hy2hz2 * 2.0 * c.p.Re;
+        a.Dn = 1.0 + c.dt * B / (c.p.Re * c.hx2hy2hz2);
+        a.resCoef = c.inverseRe;
+    } else {
+        double coef = comp == 3 ? c.kappa : c.nu;
+        a.scalarForm = 1;
+        a.coef = coef;
+        a.X = c.hx2hy2hz2 * 2.0;
+        a.Dn = 1.0 + c.dt * coef * B / c.hx2hy2hz2;
+        a.resCoef = coef;
+    }
+    // residual: metric*(...)/(h*h); h*h is a power of two, so /(h*h) == *(1/(h*h))
+    a.lx = xix2 * (1.0 / (c.dXi[0] * c.dXi[0]));
+    a.ly = ety2 * (1.0 / (c.dXi[1] * c.dXi[1]));
+    a.lz = ztz2 * (1.0 / (c.dXi[2] * c.dXi[2]));
+    a.resMax = c.dscal;
+    fa.rhs = a.rhs; fa.prog = a.prog; fa.full = a.full;
+    fa.c1 = a.c1; fa.c2 = a.c2; fa.c3 = a.c3;
+    fa.k1 = a.scalarForm ? (a.dt * a.coef) / a.X : a.dt / a.X;
+    fa.invDn = 1.0 / a.Dn;
+    fa.resMax = a.resMax;
+}
+
+// Split-FP64 solve buffers: N0 of components 0..3 and the D ping-pong, as
+// float pairs of the largest padded component size.
+static int cnp_ensure(Ctx &c) {
+    if (c.cnp) return SARAS_OK;
+    long n = 0;
+    for (int fld : {SARAS_FIELD_VX, SARAS_FIELD_VY, SARAS_FIELD_VZ, SARAS_FIELD_T}) {
+        const FieldInfo &f = c.info[fld];
+        n = std::max(n, make_view<double>(nullptr, f.n[0], f.n[1], f.n[2]).size());
+    }
+    SARAS_CUDA_TRY(cudaMalloc(&c.cnp, sizeof(float) * 12 * (size_t)n));
+    c.cnpCount = n;
+    return SARAS_OK;
+}
+
 int compute_rhs(Ctx &c) {
     UC u = make_uc(c);
     RhsArgs a;
@@ -1047,9 +1121,17 @@ int compute_rhs(Ctx &c) {
             }
             qd.fb2 = pr(qf.Fb2);
             qd.dt = pr(qf.dt);
-            if (q == 0) k_rhs_df<0><<<g, bl, 0, c.stream>>>(a, qd);
-            if (q == 1) k_rhs_df<1><<<g, bl, 0, c.stream>>>(a, qd);
-            if (q == 2) k_rhs_df<2><<<g, bl, 0, c.stream>>>(a, qd);
+            CnArgs ca;
+            CnFast cfa;
+            cn_setup(c, q, ca, cfa);
+            CnDf cf = cn_df_consts(cfa);
+            int e = cnp_ensure(c);
+            if (e) return e;
+            float *n0h = c.cnp + (size_t)2 * q * c.cnpCount, *n0l = n0h + c.cnpCount;
+            if (q == 0) k_rhs_df<0><<<g, bl, 0, c.stream>>>(a, qd, cf, n0h, n0l);
+            if (q == 1) k_rhs_df<1><<<g, bl, 0, c.stream>>>(a, qd, cf, n0h, n0l);
+            if (q == 2) k_rhs_df<2><<<g, bl, 0, c.stream>>>(a, qd, cf, n0h, n0l);
+            c.n0Fresh[q] = 1;
         } else if (fast) {
             if (q == 0) k_rhs_fast<0><<<g, bl, 0, c.stream>>>(a, qf);
             if (q == 1) k_rhs_fast<1><<<g, bl, 0, c.stream>>>(a, qf);
@@ -1087,21 +1169,23 @@ int compute_trhs(Ctx &c) {
 // semantics of cn_solve: each sweep also reports the residual of its input,
 // and the input of the first sweep whose input residual is below the
 // tolerance is the answer.
-static int cn_solve_delta(Ctx &c, int field, const CnFast &fa, double Dn, dim3 g, dim3 bl, double bytes, int *iters, double *maxerr) {
+static int cn_solve_delta(Ctx &c, int comp, int field, const CnFast &fa, double Dn, double bytes, int *iters, double *maxerr) {
     const FieldInfo &f = c.info[field];
     View3<double> V = mview(c, field);
     long n = V.size();
-    if (c.cnpCount < n) {
-        cudaFree(c.cnp);
-        c.cnp = nullptr;
-        SARAS_CUDA_TRY(cudaMalloc(&c.cnp, sizeof(float) * 6 * (size_t)n));
-        c.cnpCount = n;
-    }
-    float *n0h = c.cnp, *n0l = n0h + n, *dA = n0l + n, *dAl = dA + n, *dB = dAl + n, *dBl = dB + n;
+    int e = cnp_ensure(c);
+    if (e) return e;
+    long N = c.cnpCount;
+    float *n0h = c.cnp + (size_t)2 * comp * N, *n0l = n0h + N;
+    float *dA = c.cnp + (size_t)8 * N, *dAl = dA + N, *dB = dAl + N, *dBl = dB + N;
     CnDf fd = cn_df_consts(fa);
-    k_cn_pack<<<g, bl, 0, c.stream>>>(cview(c, field), fa.rhs, f.full, fa.full, fd, n0h, n0l);
-    SARAS_CUDA_TRY(cudaMemsetAsync(dA, 0, sizeof(float) * 2 * (size_t)n, c.stream));
-    count_launch(c);
+    if (!c.n0Fresh[comp]) {   // N0 not already written by the right-hand-side kernel
+        dim3 g, bl; box_launch_dims(fa.full, g, bl);
+        k_cn_pack<<<g, bl, 0, c.stream>>>(cview(c, field), fa.rhs, f.full, fa.full, fd, n0h, n0l);
+        count_launch(c);
+    }
+    c.n0Fresh[comp] = 0;
+    SARAS_CUDA_TRY(cudaMemsetAsync(dA, 0, sizeof(float) * 2 * (size_t)N, c.stream));
     CnDelta d;
     d.C0 = V.p;
     d.n0h = n0h; d.n0l = n0l;
@@ -1111,11 +1195,12 @@ static int cn_solve_delta(Ctx &c, int field, const CnFast &fa, double Dn, dim3 g
     d.f = fd;
     d.resMax = c.dscal;
     float *cur[2] = {dA, dAl}, *nxt[2] = {dB, dBl};
+    dim3 gm((fa.full.ext[2] + 31) / 32, (fa.full.ext[1] + 7) / 8, (fa.full.ext[0] + kCnMarch - 1) / kCnMarch), bm(32, 8, 1);
     auto launch = [&](int withRes) {
         d.dh = cur[0]; d.dl = cur[1]; d.oh = nxt[0]; d.ol = nxt[1];
         d.withResidual = withRes;
         prof_begin(c, PK_CN, 0);
-        k_cn_delta<<<g, bl, 0, c.stream>>>(d);
+        k_cn_delta<<<gm, bm, 0, c.stream>>>(d);
         count_launch(c);
         prof_end(c, PK_CN, 0, bytes);
     };
@@ -1152,53 +1237,16 @@ int cn_solve(Ctx &c, int comp, int *iters, double *maxerr) {
     if (comp < 0 || comp > 3) return SARAS_BAD_ARG;
     if (comp == 3 && !c.scalar) return SARAS_BAD_ARG;
     int field = comp == 3 ? SARAS_FIELD_T : SARAS_FIELD_VX + comp;
-    int rhsField = comp == 3 ? SARAS_FIELD_TRHS : SARAS_FIELD_NSE_X + comp;
     const FieldInfo &f = c.info[field];
     CnArgs a;
-    a.rhs = cview(c, rhsField);
-    a.prog = f.full;
-    a.full = full_box(f);
-    // Metrics: every component's xix2/ety2/ztz2 equal pow(1/L,2) on uniform grids
-    // (the T solve's ztz2Colloc of scalar_d3.cc:551,570 has the same value).
-    double xix2 = c.m2[0], ety2 = c.m2[1], ztz2 = c.m2[2];
-    a.c1 = c.hy2hz2 * xix2;
-    a.c2 = c.hz2hx2 * ety2;
-    a.c3 = c.hx2hy2 * ztz2;
-    double B = (c.hy2hz2 * xix2 + c.hz2hx2 * ety2) + c.hx2hy2 * ztz2;
-    a.dt = c.dt;
-    if (!c.scalar) {
-        a.scalarForm = 0;
-        a.coef = 0;
-        a.X = c.hx2hy2hz2 * 2.0 * c.p.Re;
-        a.Dn = 1.0 + c.dt * B / (c.p.Re * c.hx2hy2hz2);
-        a.resCoef = c.inverseRe;
-    } else {
-        double coef = comp == 3 ? c.kappa : c.nu;
-        a.scalarForm = 1;
-        a.coef = coef;
-        a.X = c.hx2hy2hz2 * 2.0;
-        a.Dn = 1.0 + c.dt * coef * B / c.hx2hy2hz2;
-        a.resCoef = coef;
-    }
-    // residual: metric*(...)/(h*h); h*h is a power of two, so /(h*h) == *(1/(h*h))
-    a.lx = xix2 * (1.0 / (c.dXi[0] * c.dXi[0]));
-    a.ly = ety2 * (1.0 / (c.dXi[1] * c.dXi[1]));
-    a.lz = ztz2 * (1.0 / (c.dXi[2] * c.dXi[2]));
-    a.resMax = c.dscal;
+    CnFast fa;
+    cn_setup(c, comp, a, fa);
     dim3 g, bl; box_launch_dims(a.full, g, bl);
     int slot = scratch_slot(field);
     double bytes = 3.0 * 8.0 * (double)make_view<double>(nullptr, f.n[0], f.n[1], f.n[2]).size();
-    CnFast fa;
     bool fast = c.p.fastKernels != 0;
-    if (fast) {
-        fa.rhs = a.rhs; fa.prog = a.prog; fa.full = a.full;
-        fa.c1 = a.c1; fa.c2 = a.c2; fa.c3 = a.c3;
-        fa.k1 = a.scalarForm ? (a.dt * a.coef) / a.X : a.dt / a.X;
-        fa.invDn = 1.0 / a.Dn;
-        fa.resMax = a.resMax;
-    }
     const double resScale = fast ? a.Dn : 1.0;
-    if (c.p.fastKernels == 2) return cn_solve_delta(c, field, fa, a.Dn, g, bl, bytes, iters, maxerr);
+    if (c.p.fastKernels == 2) return cn_solve_delta(c, comp, field, fa, a.Dn, bytes, iters, maxerr);
     auto launch = [&](int withRes) {
         if (fast) {
             fa.in = cview(c, field);
@@ -1375,12 +1423,12 @@ int time_advance(Ctx &c, saras_step_stats *st) {
     saras_step_stats local;
     std::memset(&local, 0, sizeof(local));
     int s = compute_rhs(c);
-    if (s) return s;
+    if (s) { for (int &q : c.n0Fresh) q = 0; return s; }
     for (int q = 0; q < 3; ++q) {
         int it = 0; double e = 0;
         s = cn_solve(c, q, &it, &e);
         local.cn_iters[q] = it;
-        if (s) { local.status = s; if (st) *st = local; return s; }
+        if (s) { for (int &r : c.n0Fresh) r = 0; local.status = s; if (st) *st = local; return s; }
     }
     s = vfield_divergence(c, nullptr, true);
     if (s) return s;

@@ -584,13 +584,11 @@ __global__ void __launch_bounds__(256) k_tgt_sweep(T *__restrict__ out, const T 
     int j = blockIdx.y * 8 + threadIdx.y;
     int i0 = blockIdx.z * kIch;
     if (j > bc.E[1] || k > bc.E[2]) return;
-    int iend = min(i0 + kIch - 1, bc.E[0]);
-    int o = (i0 + 1) * sx + (j + 1) * sy + (k + 1);
-    bool edge_jk = j <= 1 || k <= 1 || j >= bc.E[1] - 1 || k >= bc.E[2] - 1;
+    int n = min(kIch, bc.E[0] - i0 + 1);
+    const int o0 = (i0 + 1) * sx + (j + 1) * sy + (k + 1);
     T cm = (T)0, cc = (T)0;
-    if (!ZERO) { cm = in[o - sx]; cc = in[o]; }
-#pragma unroll 4
-    for (int i = i0; i <= iend; ++i, o += sx) {
+    if (!ZERO) { cm = in[o0 - sx]; cc = in[o0]; }
+    auto point = [&](int o) {
         T v;
         if (ZERO) {
             v = c.ar * r[o];
@@ -602,7 +600,21 @@ __global__ void __launch_bounds__(256) k_tgt_sweep(T *__restrict__ out, const T 
             cc = cp;
         }
         out[o] = v;
-        if (edge_jk || i <= 1 || i >= bc.E[0] - 1) scatter_slow(out, sx, sy, i, j, k, v, bc);
+    };
+    // the column segment without branches (all loads of a full segment can be
+    // in flight together), then the face-ghost images of its boundary points
+    if (n == kIch) {
+#pragma unroll
+        for (int q = 0; q < kIch; ++q) point(o0 + q * sx);
+    } else {
+        for (int q = 0; q < n; ++q) point(o0 + q * sx);
+    }
+    bool edge_jk = j <= 1 || k <= 1 || j >= bc.E[1] - 1 || k >= bc.E[2] - 1;
+    if (edge_jk || i0 <= 1 || i0 + n - 1 >= bc.E[0] - 1) {
+        for (int q = 0; q < n; ++q) {
+            int i = i0 + q;
+            if (edge_jk || i <= 1 || i >= bc.E[0] - 1) scatter_slow(out, sx, sy, i, j, k, out[o0 + q * sx], bc);
+        }
     }
 }
 
@@ -613,7 +625,7 @@ __global__ void __launch_bounds__(256) k_tgt_residual(OT *__restrict__ out, cons
     int k = blockIdx.x * 32 + threadIdx.x;
     int j = blockIdx.y * 8 + threadIdx.y;
     int i0 = blockIdx.z * kIch;
-    double m = 0.0;
+    unsigned long long m = 0ull;
     if (j <= bc.E[1] && k <= bc.E[2]) {
         int iend = min(i0 + kIch - 1, bc.E[0]);
         int o = (i0 + 1) * sx + (j + 1) * sy + (k + 1);
@@ -626,15 +638,14 @@ __global__ void __launch_bounds__(256) k_tgt_residual(OT *__restrict__ out, cons
             T res = b[o] - lap;
             if (out) out[o] = (OT)res;
             if (MAXRED) {
-                double a = fabs((double)res);
-                if (a != a) a = INFINITY;
-                m = fmax(m, a);
+                unsigned long long a = sizeof(T) == 8 ? abs_bits((double)res) : abs_bits(f2d((float)res));
+                m = a > m ? a : m;
             }
             cm = cc;
             cc = cp;
         }
     }
-    if (MAXRED) block_max_to(m, maxres);
+    if (MAXRED) block_max_bits_to(m, maxres);
 }
 
 // p64 += e32 over the core (FP64 correction accumulation) with face ghosts.
@@ -720,6 +731,73 @@ __global__ void __launch_bounds__(256) k_fx_refine(long long *__restrict__ pout,
         unsigned long long b = 0;
         for (int q = 0; q < 8; ++q) b = sm[q] > b ? sm[q] : b;
         atomicMax(maxr, b);
+    }
+    if (bad) atomicExch(flag, 1);
+}
+
+// The WITH_E step of k_fx_refine with the in-plane neighbours shared through
+// shared memory: each advanced value P + round(e 2^s) is formed once per
+// block (the tile's halo adds a third), instead of once per stencil use.
+// Block 32 (k) x 8 (j) marching kIch planes along i; the plane tile is double
+// buffered, and the column's own i-1 / i+1 values stay in registers.
+__global__ void __launch_bounds__(256) k_fx_update(long long *__restrict__ pout, const long long *__restrict__ pin,
+                                                   const float *__restrict__ e, const long long *__restrict__ bfx,
+                                                   float *__restrict__ r32, int sx, int sy, MgBC bc, int s, float rscale,
+                                                   unsigned long long *maxr, int *flag) {
+    __shared__ long long tile[2][10][34];
+    int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
+    int k0 = blockIdx.x * 32, j0 = blockIdx.y * 8, i0 = blockIdx.z * kIch;
+    int k = k0 + tx, j = j0 + ty;
+    int iend = min(i0 + kIch - 1, bc.E[0]);
+    bool bad = false;
+    auto val = [&](long q) -> long long { return pin[q] + f2fx(e[q], s, bad); };
+    // plane i of the tile: points (j0 - 1 .. j0 + 8, k0 - 1 .. k0 + 32), inside the padded box
+    auto load_plane = [&](int i, int buf) {
+        for (int t = tid; t < 340; t += 256) {
+            int jj = t / 34, kk = t - jj * 34;
+            int jg = j0 + jj - 1, kg = k0 + kk - 1;
+            long long v = 0;
+            if (jg <= bc.E[1] + 1 && kg <= bc.E[2] + 1) v = val((long)(i + 1) * sx + (long)(jg + 1) * sy + (kg + 1));
+            tile[buf][jj][kk] = v;
+        }
+    };
+    bool active = j <= bc.E[1] && k <= bc.E[2];
+    bool edge_jk = j <= 1 || k <= 1 || j >= bc.E[1] - 1 || k >= bc.E[2] - 1;
+    long o = (long)(i0 + 1) * sx + (long)(j + 1) * sy + (k + 1);
+    long long cm = active ? val(o - sx) : 0;
+    unsigned long long m = 0;
+    load_plane(i0, 0);
+    for (int i = i0; i <= iend; ++i, o += sx) {
+        int b = (i - i0) & 1;
+        load_plane(i + 1, b ^ 1);
+        __syncthreads();
+        if (active) {
+            long long cc = tile[b][ty + 1][tx + 1], cp = tile[b ^ 1][ty + 1][tx + 1];
+            long long nb = (cm + cp) + (tile[b][ty][tx + 1] + tile[b][ty + 2][tx + 1]) + (tile[b][ty + 1][tx] + tile[b][ty + 1][tx + 2]);
+            long long r = bfx[o] - (nb - 6 * cc);
+            r32[o] = fx2f(r) * rscale;
+            unsigned long long a = (unsigned long long)(r < 0 ? -r : r);
+            m = a > m ? a : m;
+            pout[o] = cc;
+            unsigned long long ac = (unsigned long long)(cc < 0 ? -cc : cc);
+            if (ac > (1ull << 59)) bad = true;
+            if (edge_jk || i <= 1 || i >= bc.E[0] - 1) scatter_slow(pout, sx, sy, i, j, k, cc, bc);
+            cm = cc;
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+        unsigned long long o2 = __shfl_xor_sync(0xffffffffu, m, off);
+        m = o2 > m ? o2 : m;
+    }
+    __shared__ unsigned long long sm[8];
+    if (tx == 0) sm[ty] = m;
+    __syncthreads();
+    if (tid == 0) {
+        unsigned long long bm = 0;
+        for (int q = 0; q < 8; ++q) bm = sm[q] > bm ? sm[q] : bm;
+        atomicMax(maxr, bm);
     }
     if (bad) atomicExch(flag, 1);
 }
@@ -1177,7 +1255,7 @@ static int mixed_fixed(Ctx &c, double bmax, double target, bool wantGuess, doubl
         SARAS_CUDA_TRY(cudaMemsetAsync(c.dscal + 34, 0, sizeof(double), c.stream));
         if (withE) {
             prof_begin(c, PK_REFINE_UPDATE, 0);
-            k_fx_refine<true><<<gm0, bm0, 0, c.stream>>>(c.fx[q ^ 1], c.fx[q], L0.pa32(), B, L0.r32, sx0, sy0, bc0, sc, (float)rs, dmax, dflag);
+            k_fx_update<<<gm0, bm0, 0, c.stream>>>(c.fx[q ^ 1], c.fx[q], L0.pa32(), B, L0.r32, sx0, sy0, bc0, sc, (float)rs, dmax, dflag);
             prof_end(c, PK_REFINE_UPDATE, 0, (8.0 + 4.0 + 8.0 + 8.0 + 4.0) * (double)L0.count);
         } else {
             prof_begin(c, PK_REFINE_RESID, 0);
