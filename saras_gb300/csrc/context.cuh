@@ -110,6 +110,10 @@ struct Ctx {
     float *cnp = nullptr;      // split-FP64 Jacobi solve: N0 of each component and the D ping-pong (float pairs)
     long cnpCount = 0;
     int n0Fresh[4] = {0, 0, 0, 0};   // N0 of component q written by this step's right-hand side
+    // target-mode V-cycles replayed as CUDA graphs: [FP32?][zero start?]
+    cudaGraphExec_t vgraph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    long long vgraphLaunches[2][2] = {{0, 0}, {0, 0}};
+    std::vector<int> vgraphState[2][2];
     int histCount = 0;
     bool collecting = false;
     // profiling
@@ -165,6 +169,9 @@ int unet_train(Ctx &c, int iters, double lr, double *loss);
 int unet_infer(Ctx &c, double *out);
 int unet_begin_solve(Ctx &c);
 int unet_guess(Ctx &c, const double *b, double *dst, int mode);
+void vgraph_reset(Ctx &c);
+int unet_pick(Ctx &c);
+void unet_record(Ctx &c, int built, int cycles);
 int unet_collect_sample(Ctx &c, const double *b);
 int conv3d_check(int mode, int D, int H, int W, int cin, int cout, const unsigned short *x, const unsigned short *dy,
                  const float *w, const float *bias, int relu, float *out);

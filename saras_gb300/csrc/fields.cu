@@ -614,6 +614,29 @@ __global__ void __launch_bounds__(256) k_cn_delta(CnDelta a) {
     if (k < a.full.lo[2] + a.full.ext[2] && j < a.full.lo[1] + a.full.ext[1]) {
         int iend = min(i0 + kCnMarch, a.full.lo[0] + a.full.ext[0]);
         bool bulkJK = j >= a.prog.blo[1] && j <= a.prog.bhi[1] && k >= a.prog.blo[2] && k <= a.prog.bhi[2];
+        if (bulkJK && iend == i0 + kCnMarch && i0 >= a.prog.blo[0] && iend - 1 <= a.prog.bhi[0]) {
+            // a whole segment of bulk points: branch-free, the column's own i-1 / i / i+1
+            // high parts carried in registers, every load of the segment in flight together
+            long o = a.off(i0, j, k);
+            float hm = a.dh[o - a.sx], hc = a.dh[o];
+#pragma unroll
+            for (int q = 0; q < kCnMarch; ++q, o += a.sx) {
+                float hp = a.dh[o + a.sx];
+                fpair D = fpair{hc, a.dl[o]};
+                float d2 = 2.0f * hc;
+                float qq = fmaf(a.f.kf[0], (hp + hm) - d2,
+                                fmaf(a.f.kf[1], (a.dh[o + a.sy] + a.dh[o - a.sy]) - d2, a.f.kf[2] * ((a.dh[o + 1] + a.dh[o - 1]) - d2)));
+                fpair num = fp_add(fp_add(fpair{a.n0h[o], a.n0l[o]}, fp_neg(D)), fpair{qq, 0.0f});
+                fpair corr = fp_mul(num, a.f.invDn);
+                fpair out = fp_add(D, corr);
+                m = max(m, __float_as_uint(corr.h) & 0x7fffffffu);
+                a.oh[o] = out.h;
+                a.ol[o] = out.l;
+                hm = hc;
+                hc = hp;
+            }
+            iend = i0;   // segment done (the generic loop below runs no iteration)
+        }
         for (int i = i0; i < iend; ++i) {
             long o = a.off(i, j, k);
             fpair out;

@@ -961,6 +961,7 @@ int mg_setup(Ctx &c) {
 }
 
 void mg_free(Ctx &c) {
+    vgraph_reset(c);
     for (Level &L : c.lv) { cudaFree(L.a); cudaFree(L.b); cudaFree(L.r); cudaFree(L.a32); cudaFree(L.b32); cudaFree(L.r32); }
     for (long long *&q : c.fx) { cudaFree(q); q = nullptr; }
     c.lv.clear();
@@ -1096,6 +1097,74 @@ static int vcycle(Ctx &c, bool tgt, bool zero0) {
         if ((s = prolong_level<T>(c, l, tgt, true))) return s;
         if ((s = smooth<T>(c, l, c.p.postSmooth, false, tgt))) return s;
     }
+    return SARAS_OK;
+}
+
+// The target-mode V-cycle issues about ten kernels per level, most of them
+// microseconds long on the coarse levels, where the host's launch rate rather
+// than the GPU bounds the cycle.  It is captured once as a CUDA graph and
+// replayed: the kernels, their arguments and the level buffers they use are
+// the same every cycle, because every level's ping-pong flips an even number
+// of times per cycle (pre + post smoothing) and so returns to its starting
+// state.  The graph is rebuilt when the level states differ from the ones it
+// was captured with; with kernel profiling on, the cycle runs uncaptured.
+static std::vector<int> level_state(const Ctx &c) {
+    std::vector<int> st;
+    for (const Level &L : c.lv) { st.push_back(L.cur); st.push_back(L.cur32); }
+    return st;
+}
+
+void vgraph_reset(Ctx &c) {
+    for (auto &row : c.vgraph)
+        for (cudaGraphExec_t &g : row) {
+            if (g) cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+}
+
+template <typename T>
+static int vcycle_tgt(Ctx &c, bool zero0) {
+    bool profiling = false;
+    for (const ProfSlot &ps : c.prof) profiling = profiling || ps.enabled;
+    if (profiling) return vcycle<T>(c, true, zero0);
+    int a = sizeof(T) == 4 ? 1 : 0, b = zero0 ? 1 : 0;
+    cudaGraphExec_t &ge = c.vgraph[a][b];
+    std::vector<int> st = level_state(c);
+    if (ge && c.vgraphState[a][b] != st) {
+        cudaGraphExecDestroy(ge);
+        ge = nullptr;
+    }
+    if (!ge) {
+        long long l0 = c.launches;
+        SARAS_CUDA_TRY(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+        int s = vcycle<T>(c, true, zero0);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(c.stream, &g);
+        if (s || e != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            if (s) return s;
+            c.err = std::string("V-cycle capture: ") + cudaGetErrorString(e);
+            return SARAS_CUDA_ERROR;
+        }
+        e = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            ge = nullptr;
+            c.err = std::string("V-cycle graph: ") + cudaGetErrorString(e);
+            return SARAS_CUDA_ERROR;
+        }
+        c.vgraphLaunches[a][b] = c.launches - l0;
+        c.launches = l0;
+        c.vgraphState[a][b] = st;
+        if (level_state(c) != st) {   // a cycle that does not restore the level states is never replayed
+            cudaGraphExecDestroy(ge);
+            ge = nullptr;
+            return vcycle<T>(c, true, zero0);
+        }
+    }
+    SARAS_CUDA_TRY(cudaGraphLaunch(ge, c.stream));
+    c.launches += c.vgraphLaunches[a][b];
     return SARAS_OK;
 }
 
@@ -1275,13 +1344,15 @@ static int mixed_fixed(Ctx &c, double bmax, double target, bool wantGuess, doubl
         return SARAS_OK;
     };
     bool bad = false;
+    int built = 0;
     k_fx_from<<<nbF, 256, 0, c.stream>>>(c.fx[0], L0.pa(), L0.count, sc, dflag);
     count_launch(c);
     if ((s = refine(0, false, r, bad))) return s;
     if (bad) return SARAS_OK;
     int cur = 0;
     if (wantGuess && c.histCount >= 2) {
-        int gs = unet_guess(c, L0.r, L0.pb(), c.guessMode);
+        built = unet_pick(c);
+        int gs = unet_guess(c, L0.r, L0.pb(), built);
         if (gs == SARAS_OK) {
             double rg = 0;
             k_fx_from<<<nbF, 256, 0, c.stream>>>(c.fx[1], L0.pb(), L0.count, sc, dflag);
@@ -1290,7 +1361,7 @@ static int mixed_fixed(Ctx &c, double bmax, double target, bool wantGuess, doubl
             if (bad) return SARAS_OK;
             if (rg < r) {
                 r = rg;
-                source = c.guessMode;
+                source = built;
                 cur = 1;
             } else if ((s = refine(0, false, r, bad))) {   // the previous Pp's FP32 residual back into r32
                 return s;
@@ -1304,7 +1375,7 @@ static int mixed_fixed(Ctx &c, double bmax, double target, bool wantGuess, doubl
         while (r > target && cyc < c.mgMaxCycles) {
             if (!std::isfinite(r)) { c.err = "multigrid residual is not finite"; return SARAS_NOT_FINITE; }
             for (int q = 0; q < std::max(1, c.p.mixedCycles); ++q) {
-                if ((s = vcycle<float>(c, true, q == 0))) return s;
+                if ((s = vcycle_tgt<float>(c, q == 0))) return s;
                 cyc += 1;
             }
             steps += 1;
@@ -1321,7 +1392,11 @@ static int mixed_fixed(Ctx &c, double bmax, double target, bool wantGuess, doubl
         if (bad) break;
         r = rf;
         cur ^= 1;
-        if (r <= target || cyc >= c.mgMaxCycles) { done = true; return SARAS_OK; }
+        if (r <= target || cyc >= c.mgMaxCycles) {
+            if (built) unet_record(c, built, cyc);
+            done = true;
+            return SARAS_OK;
+        }
     }
     // out of range: restart from the previous Pp in FP64
     L0.cur = 0;
@@ -1387,7 +1462,7 @@ static int mg_solve_target(Ctx &c, int *cycles, double *residual, saras_step_sta
         return SARAS_OK;
     };
     double r = 0;
-    int source = 0, cyc = 0, steps = 0;
+    int source = 0, cyc = 0, steps = 0, built = 0;
     bool fixedDone = false;
     if (c.mgMode == SARAS_MG_MIXED && L0.lx == L0.ly && L0.ly == L0.lz) {
         if ((s = mixed_fixed(c, bmax, target, wantGuess, r, source, cyc, steps, fixedDone, st))) return s;
@@ -1395,14 +1470,15 @@ static int mg_solve_target(Ctx &c, int *cycles, double *residual, saras_step_sta
     if (!fixedDone) {
     if ((s = fine_res(false, &r))) return s;
     if (wantGuess && c.histCount >= 2) {
-        int gs = unet_guess(c, L0.r, L0.pb(), c.guessMode);
+        built = unet_pick(c);
+        int gs = unet_guess(c, L0.r, L0.pb(), built);
         if (gs == SARAS_OK) {
             L0.cur ^= 1;
             double rg = 0;
             if ((s = fine_res(false, &rg))) return s;
             if (rg < r) {
                 r = rg;
-                source = c.guessMode;
+                source = built;
             } else {
                 L0.cur ^= 1;   // keep the previous pressure (and recompute its FP32 residual)
                 if ((s = fine_res(false, &r))) return s;
@@ -1415,13 +1491,13 @@ static int mg_solve_target(Ctx &c, int *cycles, double *residual, saras_step_sta
     while (r > target && cyc < c.mgMaxCycles) {
         if (!std::isfinite(r)) { c.err = "multigrid residual is not finite"; return SARAS_NOT_FINITE; }
         if (c.mgMode == SARAS_MG_PLAIN_TARGET) {
-            if ((s = vcycle<double>(c, true, false))) return s;
+            if ((s = vcycle_tgt<double>(c, false))) return s;
             cyc += 1;
             if ((s = fine_res(false, &r))) return s;
         } else {
             // inner FP32 solve of A e = r32 from e = 0
             for (int q = 0; q < std::max(1, c.p.mixedCycles); ++q) {
-                if ((s = vcycle<float>(c, true, q == 0))) return s;
+                if ((s = vcycle_tgt<float>(c, q == 0))) return s;
                 cyc += 1;
             }
             steps += 1;
@@ -1429,6 +1505,7 @@ static int mg_solve_target(Ctx &c, int *cycles, double *residual, saras_step_sta
         }
     }
     }
+    if (!fixedDone && built) unet_record(c, built, cyc);
     if (st) { st->refine_steps = steps; st->fine_residual = bmax > 0 ? r / bmax : r; }
     k_mg_output<<<grid_blocks(L0.count), 256, 0, c.stream>>>(lview<double>(L0, c.f[SARAS_FIELD_PP]), lcview<double>(L0, L0.pa()), bc0,
                                                              nullptr, nullptr, nullptr);

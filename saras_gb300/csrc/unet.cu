@@ -19,6 +19,7 @@
 
 #include "context.cuh"
 #include "tc_conv.cuh"
+#include "df64.cuh"
 
 namespace saras {
 
@@ -182,6 +183,9 @@ __global__ void k_adam(float *p, const float *g, float *m, float *v, long n, flo
 }
 
 // ---- FP64 <-> network features
+// The network works on multigrid level lb (the first level with at most 65
+// points per axis, so its cost does not grow with the grid), fed by full-
+// weighting restrictions of the divergence b and of the pressure history.
 struct L0View {
     const double *p;
     int n[3];     // core upper index (E) per axis; padded extent E+3
@@ -190,9 +194,15 @@ struct L0View {
     }
 };
 
-// Full weighting of a level-0 core field at the level-1 point (z, y, x).
-__device__ __forceinline__ double fw_restrict(const L0View &f, int z, int y, int x) {
-    double s = 0.0;
+// Level-0 padded field -> level-1 core array: full weighting (coarse point i on
+// fine point 2i, taps outside the grid skipped).  The weights are powers of
+// two, so every weighted term of a split value is exact and the sum is kept in
+// float-pair arithmetic (no FP64 pipe work but the final addition).
+__global__ void k_restrict0(L0View f, Grid3 g1, double *out) {
+    long v = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (v >= g1.n()) return;
+    int x = (int)(v % g1.W), y = (int)((v / g1.W) % g1.H), z = (int)(v / ((long)g1.W * g1.H));
+    fpair s = fpair{0.0f, 0.0f};
     for (int dz = -1; dz <= 1; ++dz) {
         int zz = 2 * z + dz;
         if (zz < 0 || zz > f.n[0]) continue;
@@ -202,33 +212,69 @@ __device__ __forceinline__ double fw_restrict(const L0View &f, int z, int y, int
             for (int dx = -1; dx <= 1; ++dx) {
                 int xx = 2 * x + dx;
                 if (xx < 0 || xx > f.n[2]) continue;
-                s += (double)(fw1(dz) * fw1(dy) * fw1(dx)) * f.at(zz, yy, xx);
+                float w = fw1(dz) * fw1(dy) * fw1(dx);
+                fpair t = fp_of(f.at(zz, yy, xx));
+                s = fp_add(s, fpair{t.h * w, t.l * w});
             }
         }
     }
-    return s;
+    out[v] = f2d(s.h) + f2d(s.l);
 }
 
-// Sample features at level 1 (3 FP32 channels), all derived from the
-// divergence b and the previous two pressures P1, P2:
-//   0: R(r_ex) / s_r   residual of the extrapolated guess 2 P1 - P2
-//   1: R(P1 - P2) / s_d
-//   2: R(b) / s_b
-// and, with `target`, the training target d* = R(P_new - (2 P1 - P2)) / s_t,
-// the error of the extrapolation in units of s_t = s_r L^2 / (4 pi^2) (the
-// size A^-1 gives a residual of size s_r made of the domain's lowest modes).
-// scales = {s_b, s_d, s_r, -, -, s_t}.
-__global__ void k_features(L0View b, L0View p1, L0View p2, L0View rex, L0View pnew, Grid3 g1, const double *scales, float *feat,
-                           float *target) {
+// Level-l core array -> level-l+1 core array, the same weights (FP64; these
+// levels are small).
+__global__ void k_restrict(const double *f, Grid3 gf, Grid3 gc, double *out) {
     long v = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (v >= g1.n()) return;
-    int x = (int)(v % g1.W), y = (int)((v / g1.W) % g1.H), z = (int)(v / ((long)g1.W * g1.H));
-    double sb = scales[0], sd = scales[1], sr = scales[2];
-    double r1 = fw_restrict(p1, z, y, x), r2 = fw_restrict(p2, z, y, x);
-    feat[v * 3 + 0] = (float)(fw_restrict(rex, z, y, x) / sr);
-    feat[v * 3 + 1] = (float)((r1 - r2) / sd);
-    feat[v * 3 + 2] = (float)(fw_restrict(b, z, y, x) / sb);
-    if (target) target[v] = (float)((fw_restrict(pnew, z, y, x) - (2.0 * r1 - r2)) / scales[5]);
+    if (v >= gc.n()) return;
+    int x = (int)(v % gc.W), y = (int)((v / gc.W) % gc.H), z = (int)(v / ((long)gc.W * gc.H));
+    double s = 0.0;
+    for (int dz = -1; dz <= 1; ++dz) {
+        int zz = 2 * z + dz;
+        if (zz < 0 || zz >= gf.D) continue;
+        for (int dy = -1; dy <= 1; ++dy) {
+            int yy = 2 * y + dy;
+            if (yy < 0 || yy >= gf.H) continue;
+            for (int dx = -1; dx <= 1; ++dx) {
+                int xx = 2 * x + dx;
+                if (xx < 0 || xx >= gf.W) continue;
+                s = fma((double)(fw1(dz) * fw1(dy) * fw1(dx)), f[((long)zz * gf.H + yy) * gf.W + xx], s);
+            }
+        }
+    }
+    out[v] = s;
+}
+
+// Scales of the features at level lb: s_b = max|R b|, s_d = max|R(P1 - P2)|,
+// s_r = max|R r_ex| with R r_ex = R b - 2 R b1 + R b2 (the residual of the
+// extrapolation 2 P1 - P2 is b - 2 b1 + b2 up to the previous solves'
+// residuals, which the target keeps below 1e-8 of max|b|).
+__global__ void k_feat_scales(const double *rb0, const double *rb1, const double *rb2, const double *rp0, const double *rp1, long n,
+                              double *scales) {
+    unsigned long long mb = 0, md = 0, mr = 0;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+        unsigned long long a = abs_bits(rb0[t]), d = abs_bits(rp0[t] - rp1[t]), r = abs_bits(rb0[t] - 2.0 * rb1[t] + rb2[t]);
+        mb = a > mb ? a : mb;
+        md = d > md ? d : md;
+        mr = r > mr ? r : mr;
+    }
+    block_max_bits_to(mb, scales);
+    block_max_bits_to(md, scales + 1);
+    block_max_bits_to(mr, scales + 2);
+}
+
+// Network input (3 FP32 channels per level-lb point) and, with `target`, the
+// training target d* = R(P_new - (2 P1 - P2)) / s_t:
+//   0: R r_ex / s_r   1: R(P1 - P2) / s_d   2: R b / s_b
+// with s_t = s_r L^2 / (4 pi^2) (the size A^-1 gives a residual of size s_r
+// made of the domain's lowest modes).  scales = {s_b, s_d, s_r, -, -, s_t}.
+__global__ void k_features(const double *rb0, const double *rb1, const double *rb2, const double *rp0, const double *rp1,
+                           const double *rpnew, long n, const double *scales, float *feat, float *target) {
+    long v = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    feat[v * 3 + 0] = (float)((rb0[v] - 2.0 * rb1[v] + rb2[v]) / scales[2]);
+    feat[v * 3 + 1] = (float)((rp0[v] - rp1[v]) / scales[1]);
+    feat[v * 3 + 2] = (float)(rb0[v] / scales[0]);
+    if (target) target[v] = (float)((rpnew[v] - (2.0 * rp0[v] - rp1[v])) / scales[5]);
 }
 
 // Expand 3-channel FP32 features into the 16-channel BF16 network input.
@@ -262,22 +308,30 @@ __global__ void k_loss(const float *d, const float *dstar, bf16 *gout, long nv, 
     }
 }
 
-// Guess on level 0: 2 P1 - P2 (quad: 3 P1 - 3 P2 + P3) + alpha s_t prolong(d),
-// core points, with face ghosts.
-__global__ void k_apply_guess(double *out, L0View p1, L0View p2, const float *d, Grid3 g1, const double *scales, int use_net,
-                              int per0, int per1, int per2, const double *alpha, L0View p3, int quad) {
+// Guess on level 0: 2 P1 - P2 (quad: 3 P1 - 3 P2 + P3) plus, with d, the
+// network correction alpha s_t P(d), P the trilinear interpolation from level
+// lb (repeated linear prolongation of vertex grids), at core points with the
+// face-ghost images.
+__global__ void k_apply_guess(double *out, L0View p1, L0View p2, L0View p3, int quad, const float *d, Grid3 g, int lb,
+                              const double *scales, const double *alpha, int per0, int per1, int per2) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y * blockDim.y + threadIdx.y;
     int i = blockIdx.z;
     if (i > p1.n[0] || j > p1.n[1] || k > p1.n[2]) return;
     double v = quad ? 3.0 * (p1.at(i, j, k) - p2.at(i, j, k)) + p3.at(i, j, k) : 2.0 * p1.at(i, j, k) - p2.at(i, j, k);
-    if (use_net) {
-        int z0 = i >> 1, y0 = j >> 1, x0 = k >> 1;
-        int z1 = min(z0 + (i & 1), g1.D - 1), y1 = min(y0 + (j & 1), g1.H - 1), x1 = min(x0 + (k & 1), g1.W - 1);
-        auto at = [&](int a, int b, int c) { return (double)d[((long)a * g1.H + b) * g1.W + c]; };
-        double s = at(z0, y0, x0) + at(z0, y0, x1) + at(z0, y1, x0) + at(z0, y1, x1) + at(z1, y0, x0) + at(z1, y0, x1) +
-                   at(z1, y1, x0) + at(z1, y1, x1);
-        v += (alpha ? *alpha : 1.0) * scales[5] * 0.125 * s;
+    if (d) {
+        int m = (1 << lb) - 1;
+        float inv = 1.0f / (float)(1 << lb);
+        int z0 = i >> lb, y0 = j >> lb, x0 = k >> lb;
+        float fz = (float)(i & m) * inv, fy = (float)(j & m) * inv, fx = (float)(k & m) * inv;
+        int z1 = min(z0 + 1, g.D - 1), y1 = min(y0 + 1, g.H - 1), x1 = min(x0 + 1, g.W - 1);
+        auto at = [&](int a, int b, int c) { return d[((long)a * g.H + b) * g.W + c]; };
+        float c00 = at(z0, y0, x0) + fx * (at(z0, y0, x1) - at(z0, y0, x0));
+        float c01 = at(z0, y1, x0) + fx * (at(z0, y1, x1) - at(z0, y1, x0));
+        float c10 = at(z1, y0, x0) + fx * (at(z1, y0, x1) - at(z1, y0, x0));
+        float c11 = at(z1, y1, x0) + fx * (at(z1, y1, x1) - at(z1, y1, x0));
+        float c0 = c00 + fy * (c01 - c00), c1 = c10 + fy * (c11 - c10);
+        v += (*alpha * scales[5]) * (double)(c0 + fz * (c1 - c0));
     }
     long sy = p1.n[2] + 3, sx = (long)(p1.n[1] + 3) * sy;
     auto put = [&](int a, int b, int c) { out[(long)(a + 1) * sx + (long)(b + 1) * sy + (c + 1)] = v; };
@@ -322,26 +376,6 @@ __global__ void k_lowpass(const float *in, float *out, Grid3 g) {
     out[v] = s / w;
 }
 
-__global__ void k_maxabs_core(L0View f, double *out) {
-    long n = (long)(f.n[0] + 1) * (f.n[1] + 1) * (f.n[2] + 1);
-    double m = 0.0;
-    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
-        int k = (int)(t % (f.n[2] + 1)), j = (int)((t / (f.n[2] + 1)) % (f.n[1] + 1)), i = (int)(t / ((long)(f.n[2] + 1) * (f.n[1] + 1)));
-        m = fmax(m, fabs(f.at(i, j, k)));
-    }
-    block_max_to(m, out);
-}
-
-__global__ void k_maxabs_diff(L0View a, L0View b, double *out) {
-    long n = (long)(a.n[0] + 1) * (a.n[1] + 1) * (a.n[2] + 1);
-    double m = 0.0;
-    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
-        int k = (int)(t % (a.n[2] + 1)), j = (int)((t / (a.n[2] + 1)) % (a.n[1] + 1)), i = (int)(t / ((long)(a.n[2] + 1) * (a.n[1] + 1)));
-        m = fmax(m, fabs(a.at(i, j, k) - b.at(i, j, k)));
-    }
-    block_max_to(m, out);
-}
-
 __global__ void k_floor_scale(double *s, double floor_, double lfac) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         for (int q = 0; q < 3; ++q)
@@ -350,23 +384,34 @@ __global__ void k_floor_scale(double *s, double floor_, double lfac) {
     }
 }
 
-constexpr int kAlphaBlocks = 304;   // 2 blocks per SM for the step-length reduction
+constexpr int kAlphaBlocks = 152;   // one block per SM for the step-length reduction
 
-// Step length of the network correction c = g - e (g: extrapolation plus the
-// full correction, e: extrapolation alone).  With r_e = b - A e and
-// r_g = b - A g, A c = r_e - r_g =: q, and alpha = <r_e, q> / <q, q> minimises
-// |b - A (e + alpha c)|_2.  Per-block partial sums of <r_e, q> and <q, q>.
-__global__ void k_alpha_dots(L0View g, L0View b, L0View rex, double lx, double ly, double lz, double *part) {
+// Step length of the network correction c = s_t d at level lb: with the
+// restricted residual of the extrapolation R r_ex and q = A_lb c (the level's
+// 7-point operator; mirror or periodic neighbours at the walls),
+// alpha = <R r_ex, q> / <q, q> minimises |R r_ex - alpha q|_2, the residual the
+// corrected guess leaves on the smooth modes the correction can change.
+// per0 / l0 belong to the slowest axis (D, the reference's x), per2 / l2 to the fastest (W).
+__global__ void k_alpha_coarse(const float *d, const double *rb0, const double *rb1, const double *rb2, Grid3 g, int per0, int per1,
+                               int per2, double l0, double l1, double l2, const double *scales, double *part) {
     __shared__ double sm[2][32];
-    long n = (long)(g.n[0] + 1) * (g.n[1] + 1) * (g.n[2] + 1);
     double rq = 0.0, qq = 0.0;
-    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
-        int k = (int)(t % (g.n[2] + 1)), j = (int)((t / (g.n[2] + 1)) % (g.n[1] + 1)), i = (int)(t / ((long)(g.n[2] + 1) * (g.n[1] + 1)));
-        double C = g.at(i, j, k);
-        double lap = lx * (g.at(i + 1, j, k) + g.at(i - 1, j, k)) + ly * (g.at(i, j + 1, k) + g.at(i, j - 1, k)) +
-                     lz * (g.at(i, j, k + 1) + g.at(i, j, k - 1)) - 2.0 * (lx + ly + lz) * C;
-        double re = rex.at(i, j, k);
-        double q = re - (b.at(i, j, k) - lap);
+    double st = scales[5];
+    auto nb = [](int q, int E, int per, int dir) {   // neighbour index along one axis (E = last index)
+        int r = q + dir;
+        if (r < 0) r = per ? E - 1 : 1;
+        if (r > E) r = per ? 1 : E - 1;
+        return r;
+    };
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < g.n(); t += (long)gridDim.x * blockDim.x) {
+        int x = (int)(t % g.W), y = (int)((t / g.W) % g.H), z = (int)(t / ((long)g.W * g.H));
+        auto at = [&](int a, int b, int c) { return (double)d[((long)a * g.H + b) * g.W + c]; };
+        double C = at(z, y, x);
+        double lap = l0 * (at(nb(z, g.D - 1, per0, 1), y, x) + at(nb(z, g.D - 1, per0, -1), y, x) - 2.0 * C) +
+                     l1 * (at(z, nb(y, g.H - 1, per1, 1), x) + at(z, nb(y, g.H - 1, per1, -1), x) - 2.0 * C) +
+                     l2 * (at(z, y, nb(x, g.W - 1, per2, 1)) + at(z, y, nb(x, g.W - 1, per2, -1)) - 2.0 * C);
+        double q = st * lap;
+        double re = rb0[t] - 2.0 * rb1[t] + rb2[t];
         rq += re * q;
         qq += q * q;
     }
@@ -392,19 +437,6 @@ __global__ void k_alpha_final(const double *part, int nb, double *alpha) {
     *alpha = fmin(fmax(al, 0.0), 1.5);
 }
 
-// r = b - Lap(p) over the level-0 core (FP64), uniform-grid Laplacian.
-__global__ void k_residual64(double *r, L0View p, L0View b, double lx, double ly, double lz) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    int j = blockIdx.y * blockDim.y + threadIdx.y;
-    int i = blockIdx.z;
-    if (i > p.n[0] || j > p.n[1] || k > p.n[2]) return;
-    double C = p.at(i, j, k);
-    double lap = lx * (p.at(i + 1, j, k) + p.at(i - 1, j, k)) + ly * (p.at(i, j + 1, k) + p.at(i, j - 1, k)) +
-                 lz * (p.at(i, j, k + 1) + p.at(i, j, k - 1)) - 2.0 * (lx + ly + lz) * C;
-    long sy = p.n[2] + 3, sx = (long)(p.n[1] + 3) * sy;
-    r[(long)(i + 1) * sx + (long)(j + 1) * sy + (k + 1)] = b.at(i, j, k) - lap;
-}
-
 // ------------------------------------------------------------------ host: network
 struct ConvLayer {
     int cin0, cin1, cout, level;
@@ -414,7 +446,8 @@ struct ConvLayer {
 };
 
 struct UNet {
-    Grid3 g[3];                      // level-1, 2, 3 grids
+    int lb = 1;                      // multigrid level of the network's finest grid
+    Grid3 g[3];                      // levels lb, lb + 1, lb + 2
     std::vector<ConvLayer> L;
     long nparam = 0;
     float *param = nullptr, *grad = nullptr, *adam_m = nullptr, *adam_v = nullptr;
@@ -424,7 +457,16 @@ struct UNet {
     bf16 *x0 = nullptr;
     float *out = nullptr, *feat = nullptr;
     double *scales = nullptr;         // s_b, s_d, s_r, last loss, step length alpha (device)
-    double *ext = nullptr, *rex = nullptr;   // level-0 extrapolated guess and its residual
+    // restrictions to level lb: b of this and the two previous solves, Pp of
+    // the three previous solves (newest first), R(P_new) for training targets
+    double *rb[3] = {nullptr, nullptr, nullptr}, *rp[3] = {nullptr, nullptr, nullptr}, *rpnew = nullptr;
+    double *tmp[2] = {nullptr, nullptr};     // intermediate levels 1 .. lb-1 of a restriction
+    int nb = 0, np = 0;                      // consecutive solves with rb / rp pushed
+    bool bPushed = false;                    // rb[0] holds this solve's b
+    // V-cycles per solve with the network's guess and with plain extrapolation
+    // (moving averages), the basis of the choice between them
+    double cycNet = 0.0, cycExt = 0.0;
+    int usesNet = 0, usesExt = 0, solves = 0;
     // training samples: 3 feature channels + target per voxel
     std::vector<float *> samples;
     int nsamples = 0, cap = 0, next = 0;
@@ -468,13 +510,16 @@ static int unet_alloc(Ctx &c) {
     if (c.unet) return SARAS_OK;
     UNet *u = new UNet();
     c.unet = u;
-    const Level &L1 = c.lv[1];
-    const Level &L2 = c.lv[std::min(2, c.depth)];
-    const Level &L3 = c.lv[std::min(3, c.depth)];
     if (c.depth < 3) { c.err = "the U-Net needs a multigrid depth of at least 3"; return SARAS_BAD_CONFIG; }
-    u->g[0] = Grid3{L1.n[0] + 1, L1.n[1] + 1, L1.n[2] + 1};
-    u->g[1] = Grid3{L2.n[0] + 1, L2.n[1] + 1, L2.n[2] + 1};
-    u->g[2] = Grid3{L3.n[0] + 1, L3.n[1] + 1, L3.n[2] + 1};
+    // finest network level: the first with at most 64 intervals per axis (at
+    // least level 1), keeping two coarser levels for the U-Net's depth
+    int lb = 1;
+    while (lb + 2 < c.depth && std::max(c.lv[lb].n[0], std::max(c.lv[lb].n[1], c.lv[lb].n[2])) > 64) ++lb;
+    u->lb = lb;
+    for (int q = 0; q < 3; ++q) {
+        const Level &L = c.lv[lb + q];
+        u->g[q] = Grid3{L.n[0] + 1, L.n[1] + 1, L.n[2] + 1};
+    }
     struct Spec { int c0, c1, co, lvl; bool relu; };
     const Spec spec[11] = {{16, 0, 16, 0, true},  {16, 0, 16, 0, true},  {16, 0, 32, 1, true}, {32, 0, 32, 1, true},
                            {32, 0, 64, 2, true},  {64, 0, 64, 2, true},  {64, 32, 32, 1, true}, {32, 0, 32, 1, true},
@@ -533,10 +578,16 @@ static int unet_alloc(Ctx &c) {
     SARAS_CUDA_TRY(cudaMalloc(&u->out, sizeof(float) * n1));
     SARAS_CUDA_TRY(cudaMalloc(&u->feat, sizeof(float) * 4 * n1));
     SARAS_CUDA_TRY(cudaMalloc(&u->scales, sizeof(double) * 8));
-    SARAS_CUDA_TRY(cudaMalloc(&u->ext, sizeof(double) * c.lv[0].count));
-    SARAS_CUDA_TRY(cudaMalloc(&u->rex, sizeof(double) * c.lv[0].count));
-    SARAS_CUDA_TRY(cudaMemset(u->ext, 0, sizeof(double) * c.lv[0].count));
-    SARAS_CUDA_TRY(cudaMemset(u->rex, 0, sizeof(double) * c.lv[0].count));
+    for (int q = 0; q < 3; ++q) {
+        SARAS_CUDA_TRY(cudaMalloc(&u->rb[q], sizeof(double) * n1));
+        SARAS_CUDA_TRY(cudaMalloc(&u->rp[q], sizeof(double) * n1));
+    }
+    SARAS_CUDA_TRY(cudaMalloc(&u->rpnew, sizeof(double) * n1));
+    for (int q = 1; q < lb && q <= 2; ++q) {
+        const Level &L = c.lv[q];
+        SARAS_CUDA_TRY(cudaMalloc(&u->tmp[q - 1], sizeof(double) * (size_t)(L.n[0] + 1) * (L.n[1] + 1) * (L.n[2] + 1)));
+    }
+    if (lb > 3) { c.err = "grid too fine for the U-Net's restriction chain"; return SARAS_BAD_CONFIG; }
     SARAS_CUDA_TRY(cudaMalloc(&u->err, sizeof(int)));
     SARAS_CUDA_TRY(cudaMemset(u->err, 0, sizeof(int)));
     SARAS_CUDA_TRY(cudaMalloc(&u->part, sizeof(double) * std::max((n1 + 255) / 256 + 1, 2L * kAlphaBlocks)));
@@ -553,7 +604,8 @@ void unet_free(Ctx &c) {
     for (bf16 *p : u->grd) cudaFree(p);
     for (float *p : u->samples) cudaFree(p);
     cudaFree(u->out); cudaFree(u->feat); cudaFree(u->scales); cudaFree(u->err); cudaFree(u->part);
-    cudaFree(u->ext); cudaFree(u->rex);
+    for (int q = 0; q < 3; ++q) { cudaFree(u->rb[q]); cudaFree(u->rp[q]); }
+    cudaFree(u->rpnew); cudaFree(u->tmp[0]); cudaFree(u->tmp[1]);
     delete u;
     c.unet = nullptr;
 }
@@ -723,26 +775,49 @@ static int ensure_hist(Ctx &c) {
     return SARAS_OK;
 }
 
-// Extrapolated guess 2 P1 - P2, its FP64 residual against b, and the scales
-// s_b = max|b|, s_d = max|P1 - P2|, s_r = max|r_ex| (device).
-static int prepare_features(Ctx &c, const double *b, const double *pnew, float *feat, float *target) {
+// R^lb of a level-0 padded field into dst (a level-lb core array).
+static int restrict_to_base(Ctx &c, const double *src, double *dst) {
     UNet *u = U(c);
-    const Level &L0 = c.lv[0];
-    dim3 b2(64, 4), g2((L0.n[2] + 1 + 63) / 64, (L0.n[1] + 1 + 3) / 4, L0.n[0] + 1);
-    k_apply_guess<<<g2, b2, 0, c.stream>>>(u->ext, l0view(c, c.pHist[0]), l0view(c, c.pHist[1]), nullptr, u->g[0], nullptr, 0,
-                                           c.p.xPer, c.p.yPer, c.p.zPer, nullptr, l0view(c, c.pHist[2]), 0);
-    k_residual64<<<g2, b2, 0, c.stream>>>(u->rex, l0view(c, u->ext), l0view(c, b), L0.lx, L0.ly, L0.lz);
+    const Level &L1 = c.lv[1];
+    Grid3 g1{L1.n[0] + 1, L1.n[1] + 1, L1.n[2] + 1};
+    double *first = u->lb == 1 ? dst : u->tmp[0];
+    k_restrict0<<<(int)((g1.n() + 255) / 256), 256, 0, c.stream>>>(l0view(c, src), g1, first);
+    count_launch(c);
+    Grid3 gf = g1;
+    for (int l = 2; l <= u->lb; ++l) {
+        const Level &L = c.lv[l];
+        Grid3 gc{L.n[0] + 1, L.n[1] + 1, L.n[2] + 1};
+        const double *in = u->tmp[l - 2];
+        double *out = l == u->lb ? dst : u->tmp[l - 1];
+        k_restrict<<<(int)((gc.n() + 255) / 256), 256, 0, c.stream>>>(in, gf, gc, out);
+        count_launch(c);
+        gf = gc;
+    }
+    return ucheck(c, "restrict");
+}
+
+// rb ring: this solve's R b (once per solve).
+static int push_b(Ctx &c, const double *b) {
+    UNet *u = U(c);
+    if (u->bPushed) return SARAS_OK;
+    std::swap(u->rb[2], u->rb[1]);
+    std::swap(u->rb[1], u->rb[0]);
+    u->nb += 1;
+    u->bPushed = true;
+    return restrict_to_base(c, b, u->rb[0]);
+}
+
+// Scales and features of this solve at level lb (target from rpnew when given).
+static int features(Ctx &c, float *feat, float *target) {
+    UNet *u = U(c);
+    long n = u->g[0].n();
     SARAS_CUDA_TRY(cudaMemsetAsync(u->scales, 0, sizeof(double) * 3, c.stream));
-    k_maxabs_core<<<304, 256, 0, c.stream>>>(l0view(c, b), u->scales);
-    k_maxabs_diff<<<304, 256, 0, c.stream>>>(l0view(c, c.pHist[0]), l0view(c, c.pHist[1]), u->scales + 1);
-    k_maxabs_core<<<304, 256, 0, c.stream>>>(l0view(c, u->rex), u->scales + 2);
+    k_feat_scales<<<152, 256, 0, c.stream>>>(u->rb[0], u->rb[1], u->rb[2], u->rp[0], u->rp[1], n, u->scales);
     double lfac = (c.p.Lx * c.p.Lx + c.p.Ly * c.p.Ly + c.p.Lz * c.p.Lz) / (3.0 * 4.0 * M_PI * M_PI);
     k_floor_scale<<<1, 32, 0, c.stream>>>(u->scales, 1e-300, lfac);
-    long n1 = u->g[0].n();
-    k_features<<<(int)((n1 + 255) / 256), 256, 0, c.stream>>>(l0view(c, b), l0view(c, c.pHist[0]), l0view(c, c.pHist[1]),
-                                                              l0view(c, u->rex), l0view(c, pnew ? pnew : c.pHist[0]), u->g[0],
-                                                              u->scales, feat, target);
-    count_launch(c, 7);
+    k_features<<<(int)((n + 255) / 256), 256, 0, c.stream>>>(u->rb[0], u->rb[1], u->rb[2], u->rp[0], u->rp[1], u->rpnew, n, u->scales,
+                                                             feat, target);
+    count_launch(c, 3);
     return ucheck(c, "features");
 }
 
@@ -751,7 +826,8 @@ static int prepare_features(Ctx &c, const double *b, const double *pnew, float *
 // ------------------------------------------------------------------ solver hooks
 namespace saras {
 
-// Called at the start of a target-mode solve: rotate the pressure history.
+// Called at the start of a target-mode solve: rotate the pressure history
+// (and, with the network in use, its restriction to level lb).
 int unet_begin_solve(Ctx &c) {
     int s = ensure_hist(c);
     if (s) return s;
@@ -761,7 +837,50 @@ int unet_begin_solve(Ctx &c) {
     c.pHist[0] = oldest;
     SARAS_CUDA_TRY(cudaMemcpyAsync(c.pHist[0], c.f[SARAS_FIELD_PP], sizeof(double) * c.lv[0].count, cudaMemcpyDeviceToDevice, c.stream));
     c.histCount += 1;
+    UNet *u = U(c);
+    if (u && (c.collecting || c.guessMode == SARAS_GUESS_LEARNED)) {
+        std::swap(u->rp[2], u->rp[1]);
+        std::swap(u->rp[1], u->rp[0]);
+        u->np += 1;
+        u->bPushed = false;
+        if ((s = restrict_to_base(c, c.pHist[0], u->rp[0]))) return s;
+    } else if (u) {
+        u->np = u->nb = 0;   // the restricted histories are no longer consecutive
+    }
     return SARAS_OK;
+}
+
+// SARAS_GUESS_LEARNED picks, per solve, between the network's guess and plain
+// extrapolation by the V-cycles each has needed (moving averages over its
+// recent solves): the cheaper one is used, and the other is tried every
+// kProbe-th solve so that its average stays current.  A network that does not
+// beat extrapolation on the running problem is thus only evaluated on probe
+// solves, and one that does is used throughout.
+constexpr int kProbe = 8;
+
+int unet_pick(Ctx &c) {
+    if (c.guessMode != SARAS_GUESS_LEARNED) return c.guessMode;
+    UNet *u = U(c);
+    if (!u || !u->trained || u->nb < 2 || u->np < 2) return SARAS_GUESS_EXTRAPOLATE;   // R b ring completed by this solve's push
+    u->solves += 1;
+    if (u->usesNet < 2) return SARAS_GUESS_LEARNED;
+    if (u->usesExt < 2) return SARAS_GUESS_EXTRAPOLATE;
+    bool netBetter = u->cycNet <= u->cycExt;
+    if (u->solves % kProbe == 0) netBetter = !netBetter;
+    return netBetter ? SARAS_GUESS_LEARNED : SARAS_GUESS_EXTRAPOLATE;
+}
+
+void unet_record(Ctx &c, int built, int cycles) {
+    UNet *u = U(c);
+    if (!u || c.guessMode != SARAS_GUESS_LEARNED) return;
+    const double w = 0.3;
+    if (built == SARAS_GUESS_LEARNED) {
+        u->cycNet = u->usesNet ? (1.0 - w) * u->cycNet + w * cycles : cycles;
+        u->usesNet += 1;
+    } else if (built == SARAS_GUESS_EXTRAPOLATE) {
+        u->cycExt = u->usesExt ? (1.0 - w) * u->cycExt + w * cycles : cycles;
+        u->usesExt += 1;
+    }
 }
 
 // Build the learned (or extrapolated) guess for the level-0 iterate into `dst`;
@@ -771,56 +890,59 @@ int unet_guess(Ctx &c, const double *b, double *dst, int mode) {
     int quad = mode == SARAS_GUESS_QUADRATIC ? 1 : 0;
     if (c.histCount < 2 + quad) return SARAS_BAD_CONFIG;
     int s;
+    UNet *u = U(c);
+    if (c.guessMode == SARAS_GUESS_LEARNED && u && u->trained && (s = push_b(c, b))) return s;
     if (use_net) {
-        if (!c.unet || !U(c)->trained) return SARAS_BAD_CONFIG;
-        UNet *u = U(c);
-        if ((s = prepare_features(c, b, nullptr, u->feat, nullptr))) return s;
-        long n1 = u->g[0].n();
-        k_expand<<<(int)((n1 * 16 + 255) / 256), 256, 0, c.stream>>>(u->feat, u->x0, n1);
+        if (!u || !u->trained) return SARAS_BAD_CONFIG;
+        if (u->nb < 3 || u->np < 2) use_net = false;   // histories not yet consecutive: plain extrapolation
+    }
+    if (use_net) {
+        long n = u->g[0].n();
+        if ((s = features(c, u->feat, nullptr))) return s;
+        k_expand<<<(int)((n * 16 + 255) / 256), 256, 0, c.stream>>>(u->feat, u->x0, n);
         count_launch(c);
         if ((s = unet_forward(c))) return s;
         // two low-pass passes (out -> feat -> out; feat is free after the forward pass)
-        k_lowpass<<<(int)((n1 + 255) / 256), 256, 0, c.stream>>>(u->out, u->feat, u->g[0]);
-        k_lowpass<<<(int)((n1 + 255) / 256), 256, 0, c.stream>>>(u->feat, u->out, u->g[0]);
-        count_launch(c, 2);
+        k_lowpass<<<(int)((n + 255) / 256), 256, 0, c.stream>>>(u->out, u->feat, u->g[0]);
+        k_lowpass<<<(int)((n + 255) / 256), 256, 0, c.stream>>>(u->feat, u->out, u->g[0]);
+        const Level &Lb = c.lv[u->lb];
+        k_alpha_coarse<<<kAlphaBlocks, 256, 0, c.stream>>>(u->out, u->rb[0], u->rb[1], u->rb[2], u->g[0], c.p.xPer, c.p.yPer, c.p.zPer,
+                                                           Lb.lx, Lb.ly, Lb.lz, u->scales, u->part);
+        k_alpha_final<<<1, 32, 0, c.stream>>>(u->part, kAlphaBlocks, u->scales + 4);
+        count_launch(c, 4);
     }
-    UNet *u = U(c);
     const Level &L0 = c.lv[0];
     dim3 b2(64, 4), g2((L0.n[2] + 1 + 63) / 64, (L0.n[1] + 1 + 3) / 4, L0.n[0] + 1);
-    Grid3 g1 = u ? u->g[0] : Grid3{1, 1, 1};
-    if (use_net) {
-        // full correction first, then its least-squares step length, then the guess with that step
-        k_apply_guess<<<g2, b2, 0, c.stream>>>(dst, l0view(c, c.pHist[0]), l0view(c, c.pHist[1]), u->out, g1, u->scales, 1,
-                                               c.p.xPer, c.p.yPer, c.p.zPer, nullptr, l0view(c, c.pHist[2]), 0);
-        k_alpha_dots<<<kAlphaBlocks, 256, 0, c.stream>>>(l0view(c, dst), l0view(c, b), l0view(c, u->rex), L0.lx, L0.ly, L0.lz, u->part);
-        k_alpha_final<<<1, 32, 0, c.stream>>>(u->part, kAlphaBlocks, u->scales + 4);
-        count_launch(c, 3);
-    }
-    k_apply_guess<<<g2, b2, 0, c.stream>>>(dst, l0view(c, c.pHist[0]), l0view(c, c.pHist[1]), use_net ? u->out : nullptr, g1,
-                                           use_net ? u->scales : nullptr, use_net ? 1 : 0, c.p.xPer, c.p.yPer, c.p.zPer,
-                                           use_net ? u->scales + 4 : nullptr, l0view(c, c.pHist[2]), quad);
+    k_apply_guess<<<g2, b2, 0, c.stream>>>(dst, l0view(c, c.pHist[0]), l0view(c, c.pHist[1]), l0view(c, c.pHist[2]), quad,
+                                           use_net ? u->out : nullptr, use_net ? u->g[0] : Grid3{1, 1, 1}, use_net ? u->lb : 0,
+                                           use_net ? u->scales : nullptr, use_net ? u->scales + 4 : nullptr, c.p.xPer, c.p.yPer,
+                                           c.p.zPer);
     count_launch(c);
     return ucheck(c, "guess");
 }
 
+// After a solve that reached the target: one training pair (features of this
+// solve, target R(P_new - (2 P1 - P2))).
 int unet_collect_sample(Ctx &c, const double *b) {
     int s = unet_alloc(c);
     if (s) return s;
+    UNet *u = U(c);
+    if ((s = push_b(c, b))) return s;
     // the first solves of a run are the start-up transient of the pressure
     // correction; pairs are taken once two earlier corrections exist beyond it
-    if (c.histCount < 4) return SARAS_OK;
-    UNet *u = U(c);
-    long n1 = u->g[0].n();
+    if (c.histCount < 4 || u->nb < 3 || u->np < 2) return SARAS_OK;
+    long n = u->g[0].n();
     float *dst;
     if (u->nsamples < u->cap) {
-        SARAS_CUDA_TRY(cudaMalloc(&dst, sizeof(float) * 4 * n1));
+        SARAS_CUDA_TRY(cudaMalloc(&dst, sizeof(float) * 4 * n));
         u->samples.push_back(dst);
         u->nsamples += 1;
     } else {
         dst = u->samples[u->next];
         u->next = (u->next + 1) % u->cap;
     }
-    if ((s = prepare_features(c, b, c.f[SARAS_FIELD_PP], dst, dst + 3 * n1))) return s;
+    if ((s = restrict_to_base(c, c.f[SARAS_FIELD_PP], u->rpnew))) return s;
+    if ((s = features(c, dst, dst + 3 * n))) return s;
     return ucheck(c, "collect");
 }
 
@@ -872,8 +994,10 @@ int unet_train(Ctx &c, int iters, double lr, double *loss) {
     return SARAS_OK;
 }
 
+// The learned guess for the current right-hand side into `out` (history and
+// the level-lb rings as the next solve would see them; no rotation).
 int unet_infer(Ctx &c, double *out) {
-    return unet_guess(c, c.lv[0].r, out, true);
+    return unet_guess(c, c.lv[0].r, out, SARAS_GUESS_LEARNED);
 }
 
 }  // namespace saras
