@@ -52,7 +52,7 @@ def tgv_params(mode, guess=0, ind=GRID_INDEX, depth=DEPTH):
     p.mgMode = mode
     p.mgTarget = TARGET
     p.mgMaxCycles = 100
-    p.mixedCycles = 1
+    p.mixedCycles = 2
     p.jacobiWeight = 6.0 / 7.0 if mode != _abi.MG_REFERENCE else 1.0
     p.fastKernels = 2 if mode != _abi.MG_REFERENCE else 0
     p.guessMode = guess
@@ -160,12 +160,17 @@ def measured_peak_hbm():
 
 
 def ncu_traffic(kernel):
-    """Per-launch DRAM traffic of `kernel` at this workload from the committed ncu summary."""
+    """Per-launch DRAM traffic (bytes) of profile slot `kernel` at this workload, from
+    the table in the committed ncu summary profiles/ncu_traffic.md (None if absent)."""
     try:
-        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
-            return json.load(f).get(kernel)
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.md")) as f:
+            for line in f:
+                cells = [x.strip() for x in line.strip().strip("|").split("|")]
+                if len(cells) >= 3 and cells[0] == kernel:
+                    return float(cells[2])
     except Exception:
-        return None
+        pass
+    return None
 
 
 # ------------------------------------------------------------------ arms
@@ -323,7 +328,7 @@ def run_ours(args, dist):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic (Taylor-Green initial condition)",
         "config": {
             "workload": "Taylor-Green vortex 257^3 (2^8+1 vertex points per axis), [0,2pi]^3 PPP, Re 1600, dt 5e-4; "
-                        "pressure solve: FP32 V(3,3) cycles inside FP64 iterative refinement to max|b-Ap|/max|b| <= 1e-8",
+                        "pressure solve: FP32 V(3,3) cycles (two per refinement step) inside iterative refinement with an exact fixed-point residual, to max|b-Ap|/max|b| <= 1e-8",
             "grid": [257, 257, 257], "vcycle_depth": DEPTH, "mg_mode": "mixed_fp32_in_fp64",
             "warm_start": "unet (3-level 16/32/64, tcgen05 BF16 convs) correcting 2 Pp(n-1) - Pp(n-2), "
                           "least-squares step length, fallback to the previous pressure"

@@ -601,11 +601,29 @@ __global__ void __launch_bounds__(256) k_tgt_sweep(T *__restrict__ out, const T 
         }
         out[o] = v;
     };
-    // the column segment without branches (all loads of a full segment can be
-    // in flight together), then the face-ghost images of its boundary points
+    // a full column segment: every load of the segment issued before the first
+    // store (the loads are independent of the stores, and issuing them together
+    // keeps enough bytes in flight for HBM), then the updates; afterwards the
+    // face-ghost images of the segment's boundary points
     if (n == kIch) {
+        T nc[kIch + 1], ns[kIch], ud[kIch], rr[kIch];
 #pragma unroll
-        for (int q = 0; q < kIch; ++q) point(o0 + q * sx);
+        for (int q = 0; q < kIch; ++q) {
+            int o = o0 + q * sx;
+            nc[q + 1] = ZERO ? (T)0 : in[o + sx];
+            ns[q] = ZERO ? (T)0 : in[o + sy] + in[o - sy];
+            ud[q] = ZERO ? (T)0 : in[o + 1] + in[o - 1];
+            rr[q] = r[o];
+        }
+        nc[0] = cc;
+#pragma unroll
+        for (int q = 0; q < kIch; ++q) {
+            T v;
+            if (ZERO) v = c.ar * rr[q];
+            else v = fma(c.ax, cm + nc[q + 1], fma(c.ay, ns[q], fma(c.az, ud[q], fma(c.ar, rr[q], c.om1 * nc[q]))));
+            cm = nc[q];
+            out[o0 + q * sx] = v;
+        }
     } else {
         for (int q = 0; q < n; ++q) point(o0 + q * sx);
     }
