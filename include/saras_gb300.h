@@ -65,7 +65,9 @@ enum saras_guess {
     SARAS_GUESS_PREVIOUS = 0, /* previous Pp (reference behaviour, poisson.cc:115) */
     SARAS_GUESS_LEARNED = 1,  /* U-Net guess with fallback to the previous Pp      */
     SARAS_GUESS_EXTRAPOLATE = 2, /* 2 Pp(n-1) - Pp(n-2) with the same fallback (ablation) */
-    SARAS_GUESS_QUADRATIC = 3    /* 3 Pp(n-1) - 3 Pp(n-2) + Pp(n-3), same fallback (ablation) */
+    SARAS_GUESS_QUADRATIC = 3,   /* 3 Pp(n-1) - 3 Pp(n-2) + Pp(n-3), same fallback (ablation) */
+    SARAS_GUESS_PARITY = 4       /* Pp(n-1) + Pp(n-2) - Pp(n-3): exact for a linear trend plus a
+                                    period-2 oscillation, same fallback (ablation) */
 };
 
 /*

@@ -576,7 +576,7 @@ __device__ __forceinline__ fpair fp_of_c(double x) {
 // Boundary point (i, j, k): the program resolved on C0 + D in float pairs (the
 // FP64 form's bc_resolve with base = Jacobi image at bulk points, 0 elsewhere),
 // minus C0 there.
-__device__ __noinline__ fpair cn_delta_boundary(const CnDelta &a, int i, int j, int k, long o) {
+__device__ __forceinline__ fpair cn_delta_boundary(const CnDelta &a, int i, int j, int k, long o) {
     const BcProgram &prog = a.prog;
     int chain[kMaxBcOps];
     int nchain = 0;
@@ -638,20 +638,39 @@ __global__ void __launch_bounds__(256) k_cn_delta(CnDelta a) {
             iend = i0;   // segment done (the generic loop below runs no iteration)
         }
         for (int i = i0; i < iend; ++i) {
+            if (!(bulkJK && i >= a.prog.blo[0] && i <= a.prog.bhi[0])) continue;   // boundary points: k_cn_delta_shell
             long o = a.off(i, j, k);
-            fpair out;
-            if (bulkJK && i >= a.prog.blo[0] && i <= a.prog.bhi[0]) {
-                fpair corr;
-                out = cn_delta_image(a, o, corr);
-                m = max(m, __float_as_uint(corr.h) & 0x7fffffffu);   // |corr| bits; NaN stays above Inf
-            } else {
-                out = cn_delta_boundary(a, i, j, k, o);
-            }
+            fpair corr;
+            fpair out = cn_delta_image(a, o, corr);
+            m = max(m, __float_as_uint(corr.h) & 0x7fffffffu);   // |corr| bits; NaN stays above Inf
             a.oh[o] = out.h;
             a.ol[o] = out.l;
         }
     }
     if (a.withResidual) block_maxf_to(__uint_as_float(m), a.resMax);
+}
+
+// The non-bulk points of the full box (the boundary program's targets), as six
+// disjoint slabs: along axis d the points below / above the bulk range, with the
+// axes before d restricted to the bulk range and the axes after d full.
+__global__ void k_cn_delta_shell(CnDelta a) {
+    int s = blockIdx.y, d = s >> 1;
+    int lo[3], hi[3];
+    for (int e = 0; e < 3; ++e) {
+        if (e < d) { lo[e] = a.prog.blo[e]; hi[e] = a.prog.bhi[e]; }
+        else { lo[e] = a.full.lo[e]; hi[e] = a.full.lo[e] + a.full.ext[e] - 1; }
+    }
+    if (s & 1) lo[d] = a.prog.bhi[d] + 1;
+    else hi[d] = a.prog.blo[d] - 1;
+    if (lo[0] > hi[0] || lo[1] > hi[1] || lo[2] > hi[2]) return;
+    long n1 = hi[1] - lo[1] + 1, n2 = hi[2] - lo[2] + 1, n = (long)(hi[0] - lo[0] + 1) * n1 * n2;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+        int k = lo[2] + (int)(t % n2), j = lo[1] + (int)((t / n2) % n1), i = lo[0] + (int)(t / (n1 * n2));
+        long o = a.off(i, j, k);
+        fpair out = cn_delta_boundary(a, i, j, k, o);
+        a.oh[o] = out.h;
+        a.ol[o] = out.l;
+    }
 }
 
 // C0 + D in FP64 over the whole padded array (in place on the field).
@@ -1224,7 +1243,8 @@ static int cn_solve_delta(Ctx &c, int comp, int field, const CnFast &fa, double 
         d.withResidual = withRes;
         prof_begin(c, PK_CN, 0);
         k_cn_delta<<<gm, bm, 0, c.stream>>>(d);
-        count_launch(c);
+        k_cn_delta_shell<<<dim3(64, 6), 256, 0, c.stream>>>(d);
+        count_launch(c, 2);
         prof_end(c, PK_CN, 0, bytes);
     };
     launch(0);

@@ -627,12 +627,25 @@ __global__ void __launch_bounds__(256) k_tgt_sweep(T *__restrict__ out, const T 
     } else {
         for (int q = 0; q < n; ++q) point(o0 + q * sx);
     }
-    bool edge_jk = j <= 1 || k <= 1 || j >= bc.E[1] - 1 || k >= bc.E[2] - 1;
-    if (edge_jk || i0 <= 1 || i0 + n - 1 >= bc.E[0] - 1) {
-        for (int q = 0; q < n; ++q) {
-            int i = i0 + q;
-            if (edge_jk || i <= 1 || i >= bc.E[0] - 1) scatter_slow(out, sx, sy, i, j, k, out[o0 + q * sx], bc);
-        }
+}
+
+// Face-ghost images (put_scatter) of the boundary points of a level array,
+// after a sweep that wrote the core only.  The points that have images are
+// those with a coordinate 1 or E-1 on some axis (periodic: E-1 -> -1, 1 -> E+1;
+// mirror: 1 -> -1, E-1 -> E+1): blockIdx.y picks one of those six planes.
+template <typename T>
+__global__ void k_tgt_ghosts(T *__restrict__ p, int sx, int sy, MgBC bc) {
+    int plane = blockIdx.y, d = plane >> 1;
+    int v = (plane & 1) ? bc.E[d] - 1 : 1;
+    int a1 = d == 0 ? 1 : 0, a2 = d == 2 ? 1 : 2;   // the other two axes
+    long n = (long)(bc.E[a1] + 1) * (bc.E[a2] + 1);
+    View3<T> V; V.p = p; V.sx = sx; V.sy = sy;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+        int q[3];
+        q[d] = v;
+        q[a1] = (int)(t / (bc.E[a2] + 1));
+        q[a2] = (int)(t % (bc.E[a2] + 1));
+        put_scatter(V, q[0], q[1], q[2], V(q[0], q[1], q[2]), bc);
     }
 }
 
@@ -753,6 +766,7 @@ __global__ void __launch_bounds__(256) k_fx_refine(long long *__restrict__ pout,
     if (bad) atomicExch(flag, 1);
 }
 
+// (k_fx_update writes the core; the face-ghost images follow with k_tgt_ghosts.)
 // The WITH_E step of k_fx_refine with the in-plane neighbours shared through
 // shared memory: each advanced value P + round(e 2^s) is formed once per
 // block (the tile's halo adds a third), instead of once per stencil use.
@@ -780,7 +794,6 @@ __global__ void __launch_bounds__(256) k_fx_update(long long *__restrict__ pout,
         }
     };
     bool active = j <= bc.E[1] && k <= bc.E[2];
-    bool edge_jk = j <= 1 || k <= 1 || j >= bc.E[1] - 1 || k >= bc.E[2] - 1;
     long o = (long)(i0 + 1) * sx + (long)(j + 1) * sy + (k + 1);
     long long cm = active ? val(o - sx) : 0;
     unsigned long long m = 0;
@@ -799,7 +812,6 @@ __global__ void __launch_bounds__(256) k_fx_update(long long *__restrict__ pout,
             pout[o] = cc;
             unsigned long long ac = (unsigned long long)(cc < 0 ? -cc : cc);
             if (ac > (1ull << 59)) bad = true;
-            if (edge_jk || i <= 1 || i >= bc.E[0] - 1) scatter_slow(pout, sx, sy, i, j, k, cc, bc);
             cm = cc;
         }
         __syncthreads();
@@ -1032,6 +1044,10 @@ static int smooth(Ctx &c, int l, int count, bool zero_first, bool tgt) {
         if (tgt) {
             if (n == 0 && zero_first) k_tgt_sweep<T, true><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
             else k_tgt_sweep<T, false><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
+            long face = (long)(L.n[0] + 1) * (L.n[1] + 1);
+            face = std::max(face, std::max((long)(L.n[0] + 1) * (L.n[2] + 1), (long)(L.n[1] + 1) * (L.n[2] + 1)));
+            k_tgt_ghosts<T><<<dim3((unsigned)std::min<long>((face + 255) / 256, 64), 6), 256, 0, c.stream>>>(B_<T>(L), sx, sy, bc);
+            count_launch(c);
         } else if (n == 0 && zero_first)
             k_mg_sweep<T, true><<<g, b, 0, c.stream>>>(lview<T>(L, B_<T>(L)), lcview<T>(L, A_<T>(L)), lcview<T>(L, R_<T>(L)), kk, bc, omega);
         else
@@ -1343,6 +1359,8 @@ static int mixed_fixed(Ctx &c, double bmax, double target, bool wantGuess, doubl
         if (withE) {
             prof_begin(c, PK_REFINE_UPDATE, 0);
             k_fx_update<<<gm0, bm0, 0, c.stream>>>(c.fx[q ^ 1], c.fx[q], L0.pa32(), B, L0.r32, sx0, sy0, bc0, sc, (float)rs, dmax, dflag);
+            k_tgt_ghosts<long long><<<dim3(64, 6), 256, 0, c.stream>>>(c.fx[q ^ 1], sx0, sy0, bc0);
+            count_launch(c);
             prof_end(c, PK_REFINE_UPDATE, 0, (8.0 + 4.0 + 8.0 + 8.0 + 4.0) * (double)L0.count);
         } else {
             prof_begin(c, PK_REFINE_RESID, 0);

@@ -308,17 +308,19 @@ __global__ void k_loss(const float *d, const float *dstar, bf16 *gout, long nv, 
     }
 }
 
-// Guess on level 0: 2 P1 - P2 (quad: 3 P1 - 3 P2 + P3) plus, with d, the
+// Guess on level 0: 2 P1 - P2 (kind 1: 3 P1 - 3 P2 + P3, kind 2: P1 + P2 - P3) plus, with d, the
 // network correction alpha s_t P(d), P the trilinear interpolation from level
 // lb (repeated linear prolongation of vertex grids), at core points with the
 // face-ghost images.
-__global__ void k_apply_guess(double *out, L0View p1, L0View p2, L0View p3, int quad, const float *d, Grid3 g, int lb,
+__global__ void k_apply_guess(double *out, L0View p1, L0View p2, L0View p3, int kind, const float *d, Grid3 g, int lb,
                               const double *scales, const double *alpha, int per0, int per1, int per2) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y * blockDim.y + threadIdx.y;
     int i = blockIdx.z;
     if (i > p1.n[0] || j > p1.n[1] || k > p1.n[2]) return;
-    double v = quad ? 3.0 * (p1.at(i, j, k) - p2.at(i, j, k)) + p3.at(i, j, k) : 2.0 * p1.at(i, j, k) - p2.at(i, j, k);
+    double v = kind == 1 ? 3.0 * (p1.at(i, j, k) - p2.at(i, j, k)) + p3.at(i, j, k)
+             : kind == 2 ? (p1.at(i, j, k) + p2.at(i, j, k)) - p3.at(i, j, k)
+                         : 2.0 * p1.at(i, j, k) - p2.at(i, j, k);
     if (d) {
         int m = (1 << lb) - 1;
         float inv = 1.0f / (float)(1 << lb);
@@ -887,8 +889,8 @@ void unet_record(Ctx &c, int built, int cycles) {
 // b is the compatible right-hand side.  Returns BAD_CONFIG if unavailable.
 int unet_guess(Ctx &c, const double *b, double *dst, int mode) {
     bool use_net = mode == SARAS_GUESS_LEARNED;
-    int quad = mode == SARAS_GUESS_QUADRATIC ? 1 : 0;
-    if (c.histCount < 2 + quad) return SARAS_BAD_CONFIG;
+    int quad = mode == SARAS_GUESS_QUADRATIC ? 1 : mode == SARAS_GUESS_PARITY ? 2 : 0;
+    if (c.histCount < 2 + (quad ? 1 : 0)) return SARAS_BAD_CONFIG;
     int s;
     UNet *u = U(c);
     if (c.guessMode == SARAS_GUESS_LEARNED && u && u->trained && (s = push_b(c, b))) return s;
