@@ -330,32 +330,86 @@ struct RhsDf {
     fpair fb2, dt;
 };
 
+// One thread per (j, k) column of the component's core box marching kRhsMarch
+// points along i: the split values of F(i-1), F(i), F(i+1), of P along i (Vx)
+// and the in-plane pair sums of the velocity slices that step in i (the
+// Slices patterns with an i offset) are carried from point to point, so each
+// of those values is split once per column instead of at every stencil use.
+constexpr int kRhsMarch = 8;
+
 template <int C>
 __global__ void __launch_bounds__(256) k_rhs_df(RhsArgs a, RhsDf q, CnDf cf, float *n0h, float *n0l) {
-    int i, j, k;
-    if (!box_point(a.b, i, j, k)) return;
+    int k = a.b.lo[2] + blockIdx.x * 32 + threadIdx.x;
+    int j = a.b.lo[1] + blockIdx.y * 8 + threadIdx.y;
+    int i0 = a.b.lo[0] + blockIdx.z * kRhsMarch;
+    if (k >= a.b.lo[2] + a.b.ext[2] || j >= a.b.lo[1] + a.b.ext[1]) return;
+    int iend = min(i0 + kRhsMarch, a.b.lo[0] + a.b.ext[0]);
     const View3<const double> &F = a.F;
-    double f0 = F(i, j, k);
-    fpair c = fp_of(f0), c2 = fpair{-2.0f * c.h, -2.0f * c.l};
-    fpair ex = fp_of(F(i + 1, j, k)), wx = fp_of(F(i - 1, j, k));
-    fpair ey = fp_of(F(i, j + 1, k)), wy = fp_of(F(i, j - 1, k));
-    fpair ez = fp_of(F(i, j, k + 1)), wz = fp_of(F(i, j, k - 1));
-    fpair Sx = fp_add(fp_add(ex, wx), c2), Sy = fp_add(fp_add(ey, wy), c2), Sz = fp_add(fp_add(ez, wz), c2);
-    fpair h = fp_add(fp_add(fp_mul(q.k2[0], Sx), fp_mul(q.k2[1], Sy)), fp_mul(q.k2[2], Sz));
-    h = fp_add(h, fp_neg(fp_mul(Slices<C, 0>::sump(a.V.v[0], i, j, k), fp_mul(fp_add(ex, fp_neg(wx)), q.k1n[0]))));
-    h = fp_add(h, fp_neg(fp_mul(Slices<C, 1>::sump(a.V.v[1], i, j, k), fp_mul(fp_add(ey, fp_neg(wy)), q.k1n[1]))));
-    h = fp_add(h, fp_neg(fp_mul(Slices<C, 2>::sump(a.V.v[2], i, j, k), fp_mul(fp_add(ez, fp_neg(wz)), q.k1n[2]))));
-    if (C == 2 && a.buoyancy) h = fp_add(h, fp_mul(q.fb2, fp_add(fp_of(a.T(i, j, k)), fp_of(a.T(i, j, k + 1)))));
-    double sp = C == 0 ? a.P(i + 1, j, k) : C == 1 ? a.P(i, j + 1, k) : a.P(i, j, k + 1);
-    h = fp_add(h, fp_neg(fp_mul(q.g[C], fp_add(fp_of(sp), fp_neg(fp_of(a.P(i, j, k)))))));
-    h = fp_mul(h, q.dt);
-    a.H(i, j, k) = (f0 + f2d(h.h)) + f2d(h.l);
-    // N0 = H - F + k1 sum_d c_d S_d(F) of the Jacobi solve that follows (k_cn_pack's
-    // quantity, from the same split values)
-    fpair n0 = fp_add(h, fp_add(fp_add(fp_mul(cf.kc[0], Sx), fp_mul(cf.kc[1], Sy)), fp_mul(cf.kc[2], Sz)));
-    long o = F.off(i, j, k);
-    n0h[o] = n0.h;
-    n0l[o] = n0.l;
+    const View3<const double> &V0 = a.V.v[0], &V1 = a.V.v[1], &V2 = a.V.v[2];
+    fpair wx = fp_of(F(i0 - 1, j, k)), c = fp_of(F(i0, j, k));
+    // carried slice halves: C = 0: Y(i) = V1(i,j) + V1(i,j-1), Z(i) = V2(i,k) + V2(i,k-1) (slice = half(i) + half(i+1));
+    // C = 1 / 2: W(i) = V0(i,j) + V0(i,j+1) / V0(i,k) + V0(i,k+1) (slice = W(i) + W(i-1))
+    fpair ya, za, wa, pa;
+    if (C == 0) {
+        ya = fp_add(fp_of(V1(i0, j, k)), fp_of(V1(i0, j - 1, k)));
+        za = fp_add(fp_of(V2(i0, j, k)), fp_of(V2(i0, j, k - 1)));
+        pa = fp_of(a.P(i0, j, k));
+    } else if (C == 1) {
+        wa = fp_add(fp_of(V0(i0 - 1, j, k)), fp_of(V0(i0 - 1, j + 1, k)));
+    } else {
+        wa = fp_add(fp_of(V0(i0 - 1, j, k)), fp_of(V0(i0 - 1, j, k + 1)));
+    }
+    for (int i = i0; i < iend; ++i) {
+        double f0 = F(i, j, k);
+        fpair c2 = fpair{-2.0f * c.h, -2.0f * c.l};
+        fpair ex = fp_of(F(i + 1, j, k));
+        fpair ey = fp_of(F(i, j + 1, k)), wy = fp_of(F(i, j - 1, k));
+        fpair ez = fp_of(F(i, j, k + 1)), wz = fp_of(F(i, j, k - 1));
+        fpair Sx = fp_add(fp_add(ex, wx), c2), Sy = fp_add(fp_add(ey, wy), c2), Sz = fp_add(fp_add(ez, wz), c2);
+        fpair h = fp_add(fp_add(fp_mul(q.k2[0], Sx), fp_mul(q.k2[1], Sy)), fp_mul(q.k2[2], Sz));
+        fpair s0, s1, s2, dp;
+        if (C == 0) {
+            s0 = c;   // Slices<0,0>: Vx itself
+            fpair yb = fp_add(fp_of(V1(i + 1, j, k)), fp_of(V1(i + 1, j - 1, k)));
+            fpair zb = fp_add(fp_of(V2(i + 1, j, k)), fp_of(V2(i + 1, j, k - 1)));
+            s1 = fp_add(ya, yb);
+            s2 = fp_add(za, zb);
+            ya = yb;
+            za = zb;
+            fpair pb = fp_of(a.P(i + 1, j, k));
+            dp = fp_add(pb, fp_neg(pa));
+            pa = pb;
+        } else if (C == 1) {
+            fpair wb = fp_add(fp_of(V0(i, j, k)), fp_of(V0(i, j + 1, k)));
+            s0 = fp_add(wb, wa);
+            wa = wb;
+            s1 = c;   // Slices<1,1>: Vy itself
+            s2 = Slices<1, 2>::sump(V2, i, j, k);
+            dp = fp_add(fp_of(a.P(i, j + 1, k)), fp_neg(fp_of(a.P(i, j, k))));
+        } else {
+            fpair wb = fp_add(fp_of(V0(i, j, k)), fp_of(V0(i, j, k + 1)));
+            s0 = fp_add(wb, wa);
+            wa = wb;
+            s1 = Slices<2, 1>::sump(V1, i, j, k);
+            s2 = c;   // Slices<2,2>: Vz itself
+            dp = fp_add(fp_of(a.P(i, j, k + 1)), fp_neg(fp_of(a.P(i, j, k))));
+        }
+        h = fp_add(h, fp_neg(fp_mul(s0, fp_mul(fp_add(ex, fp_neg(wx)), q.k1n[0]))));
+        h = fp_add(h, fp_neg(fp_mul(s1, fp_mul(fp_add(ey, fp_neg(wy)), q.k1n[1]))));
+        h = fp_add(h, fp_neg(fp_mul(s2, fp_mul(fp_add(ez, fp_neg(wz)), q.k1n[2]))));
+        if (C == 2 && a.buoyancy) h = fp_add(h, fp_mul(q.fb2, fp_add(fp_of(a.T(i, j, k)), fp_of(a.T(i, j, k + 1)))));
+        h = fp_add(h, fp_neg(fp_mul(q.g[C], dp)));
+        h = fp_mul(h, q.dt);
+        a.H(i, j, k) = (f0 + f2d(h.h)) + f2d(h.l);
+        // N0 = H - F + k1 sum_d c_d S_d(F) of the Jacobi solve that follows (k_cn_pack's
+        // quantity, from the same split values)
+        fpair n0 = fp_add(h, fp_add(fp_add(fp_mul(cf.kc[0], Sx), fp_mul(cf.kc[1], Sy)), fp_mul(cf.kc[2], Sz)));
+        long o = F.off(i, j, k);
+        n0h[o] = n0.h;
+        n0l[o] = n0.l;
+        wx = c;
+        c = ex;
+    }
 }
 
 static RhsFast make_rhs_fast(const Ctx &c, double visc) {
@@ -1170,9 +1224,10 @@ int compute_rhs(Ctx &c) {
             int e = cnp_ensure(c);
             if (e) return e;
             float *n0h = c.cnp + (size_t)2 * q * c.cnpCount, *n0l = n0h + c.cnpCount;
-            if (q == 0) k_rhs_df<0><<<g, bl, 0, c.stream>>>(a, qd, cf, n0h, n0l);
-            if (q == 1) k_rhs_df<1><<<g, bl, 0, c.stream>>>(a, qd, cf, n0h, n0l);
-            if (q == 2) k_rhs_df<2><<<g, bl, 0, c.stream>>>(a, qd, cf, n0h, n0l);
+            dim3 gr((a.b.ext[2] + 31) / 32, (a.b.ext[1] + 7) / 8, (a.b.ext[0] + kRhsMarch - 1) / kRhsMarch), br(32, 8, 1);
+            if (q == 0) k_rhs_df<0><<<gr, br, 0, c.stream>>>(a, qd, cf, n0h, n0l);
+            if (q == 1) k_rhs_df<1><<<gr, br, 0, c.stream>>>(a, qd, cf, n0h, n0l);
+            if (q == 2) k_rhs_df<2><<<gr, br, 0, c.stream>>>(a, qd, cf, n0h, n0l);
             c.n0Fresh[q] = 1;
         } else if (fast) {
             if (q == 0) k_rhs_fast<0><<<g, bl, 0, c.stream>>>(a, qf);

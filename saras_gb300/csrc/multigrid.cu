@@ -572,12 +572,18 @@ __device__ __noinline__ void scatter_slow(T *P, int sx, int sy, int i, int j, in
 // in-plane neighbours and the right-hand side.
 constexpr int kIch = 8;
 
+// Levels where the sweep's ghost images are worth a separate launch.
+static bool big_level(const Level &L) { return (long)(L.n[0] + 1) * (L.n[1] + 1) * (L.n[2] + 1) >= (1L << 20); }
+
 static void march_dims(const Level &L, dim3 &g, dim3 &b) {
     b = dim3(32, 8, 1);
     g = dim3((L.n[2] + 1 + 31) / 32, (L.n[1] + 1 + 7) / 8, (L.n[0] + 1 + kIch - 1) / kIch);
 }
 
-template <typename T, bool ZERO>
+// GHOSTS: write the face-ghost images in the kernel (small levels, where a
+// separate k_tgt_ghosts launch would cost more than the sweep); large levels
+// leave them to k_tgt_ghosts, which keeps device calls out of this kernel.
+template <typename T, bool ZERO, bool GHOSTS>
 __global__ void __launch_bounds__(256) k_tgt_sweep(T *__restrict__ out, const T *__restrict__ in, const T *__restrict__ r,
                                                    int sx, int sy, MgBC bc, TgK<T> c) {
     int k = blockIdx.x * 32 + threadIdx.x;
@@ -627,6 +633,15 @@ __global__ void __launch_bounds__(256) k_tgt_sweep(T *__restrict__ out, const T 
     } else {
         for (int q = 0; q < n; ++q) point(o0 + q * sx);
     }
+    if (GHOSTS) {
+        bool edge_jk = j <= 1 || k <= 1 || j >= bc.E[1] - 1 || k >= bc.E[2] - 1;
+        if (edge_jk || i0 <= 1 || i0 + n - 1 >= bc.E[0] - 1) {
+            for (int q = 0; q < n; ++q) {
+                int i = i0 + q;
+                if (edge_jk || i <= 1 || i >= bc.E[0] - 1) scatter_slow(out, sx, sy, i, j, k, out[o0 + q * sx], bc);
+            }
+        }
+    }
 }
 
 // Face-ghost images (put_scatter) of the boundary points of a level array,
@@ -646,6 +661,37 @@ __global__ void k_tgt_ghosts(T *__restrict__ p, int sx, int sy, MgBC bc) {
         q[a1] = (int)(t / (bc.E[a2] + 1));
         q[a2] = (int)(t % (bc.E[a2] + 1));
         put_scatter(V, q[0], q[1], q[2], V(q[0], q[1], q[2]), bc);
+    }
+}
+
+// Target-mode prolongation + add (vertex-centred trilinear) on the core; the
+// face-ghost images follow with k_tgt_ghosts.  A thread owns a fine (j, k)
+// column and marches fine planes in pairs: the coarse plane m interpolated to
+// (j, k) serves fine plane 2m and, averaged with plane m+1, fine plane 2m+1.
+template <typename T>
+__global__ void __launch_bounds__(256) k_tgt_prolong_add(T *__restrict__ pf, const T *__restrict__ pc, int sxf, int syf, int sxc, int syc,
+                                                         MgBC bc) {
+    int k = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y, i0 = blockIdx.z * kIch;   // kIch is even
+    if (j > bc.E[1] || k > bc.E[2]) return;
+    int iend = min(i0 + kIch - 1, bc.E[0]);
+    int k2 = k >> 1, j2 = j >> 1;
+    bool ko = k & 1, jo = j & 1;
+    auto A = [&](int m) -> T {   // coarse plane m at (j, k)
+        const T *q = pc + (long)(m + 1) * sxc + (long)(j2 + 1) * syc + (k2 + 1);
+        T v0 = ko ? (T)0.5 * (q[0] + q[1]) : q[0];
+        if (!jo) return v0;
+        T v1 = ko ? (T)0.5 * (q[syc] + q[syc + 1]) : q[syc];
+        return (T)0.5 * (v0 + v1);
+    };
+    long o = (long)(i0 + 1) * sxf + (long)(j + 1) * syf + (k + 1);
+    T am = A(i0 >> 1);
+    for (int i = i0; i <= iend; i += 2, o += 2 * (long)sxf) {
+        pf[o] += am;
+        if (i + 1 <= iend) {
+            T ap = A((i >> 1) + 1);
+            pf[o + sxf] += (T)0.5 * (am + ap);
+            am = ap;
+        }
     }
 }
 
@@ -1042,12 +1088,17 @@ static int smooth(Ctx &c, int l, int count, bool zero_first, bool tgt) {
     for (int n = 0; n < count; ++n) {
         prof_begin(c, pk, l);
         if (tgt) {
-            if (n == 0 && zero_first) k_tgt_sweep<T, true><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
-            else k_tgt_sweep<T, false><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
-            long face = (long)(L.n[0] + 1) * (L.n[1] + 1);
-            face = std::max(face, std::max((long)(L.n[0] + 1) * (L.n[2] + 1), (long)(L.n[1] + 1) * (L.n[2] + 1)));
-            k_tgt_ghosts<T><<<dim3((unsigned)std::min<long>((face + 255) / 256, 64), 6), 256, 0, c.stream>>>(B_<T>(L), sx, sy, bc);
-            count_launch(c);
+            bool z = n == 0 && zero_first;
+            if (big_level(L)) {
+                if (z) k_tgt_sweep<T, true, false><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
+                else k_tgt_sweep<T, false, false><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
+                k_tgt_ghosts<T><<<dim3(64, 6), 256, 0, c.stream>>>(B_<T>(L), sx, sy, bc);
+                count_launch(c);
+            } else if (z) {
+                k_tgt_sweep<T, true, true><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
+            } else {
+                k_tgt_sweep<T, false, true><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
+            }
         } else if (n == 0 && zero_first)
             k_mg_sweep<T, true><<<g, b, 0, c.stream>>>(lview<T>(L, B_<T>(L)), lcview<T>(L, A_<T>(L)), lcview<T>(L, R_<T>(L)), kk, bc, omega);
         else
@@ -1109,7 +1160,15 @@ static int prolong_level(Ctx &c, int l, bool tgt, bool add) {
     int pk = sizeof(T) == 8 ? PK_MG_PROLONG64 : PK_MG_PROLONG32;
     double pts = (double)(L.n[0] + 1) * (L.n[1] + 1) * (L.n[2] + 1);
     prof_begin(c, pk, l);
-    k_mg_prolong_add<T><<<g, b, 0, c.stream>>>(lview<T>(L, A_<T>(L)), lcview<T>(C, A_<T>(C)), bc, add ? 1 : 0);
+    if (tgt && add && big_level(L)) {
+        dim3 gm, bm; march_dims(L, gm, bm);
+        int sx = (L.n[1] + 3) * (L.n[2] + 3), sy = L.n[2] + 3;
+        k_tgt_prolong_add<T><<<gm, bm, 0, c.stream>>>(A_<T>(L), A_<T>(C), sx, sy, (C.n[1] + 3) * (C.n[2] + 3), C.n[2] + 3, bc);
+        k_tgt_ghosts<T><<<dim3(64, 6), 256, 0, c.stream>>>(A_<T>(L), sx, sy, bc);
+        count_launch(c);
+    } else {
+        k_mg_prolong_add<T><<<g, b, 0, c.stream>>>(lview<T>(L, A_<T>(L)), lcview<T>(C, A_<T>(C)), bc, add ? 1 : 0);
+    }
     count_launch(c);
     prof_end(c, pk, l, sizeof(T) * pts * (2.0 + 1.0 / 8.0));
     return chk(c, "mg prolong");
