@@ -110,6 +110,7 @@ struct Ctx {
     float *cnp = nullptr;      // split-FP64 Jacobi solve: N0 of each component and the D ping-pong (float pairs)
     long cnpCount = 0;
     int n0Fresh[4] = {0, 0, 0, 0};   // N0 of component q written by this step's right-hand side
+    int tailLt = -1;          // first level of the fused coarse V-cycle tail (target modes), or -1
     // target-mode V-cycles replayed as CUDA graphs: [FP32?][zero start?]
     cudaGraphExec_t vgraph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
     long long vgraphLaunches[2][2] = {{0, 0}, {0, 0}};

@@ -309,21 +309,16 @@ __device__ void smem_impose_bc(T *p, int X, int Y, int Z, const MgBC &bc, const 
     __syncthreads();
 }
 
+// The coarsest-level solve on shared-memory arrays: p (zeroed by the caller)
+// and r in the padded layout of a level with core 0..X, 0..Y, 0..Z.
 template <typename T>
-__global__ void k_mg_coarse(View3<T> pg, View3<const T> rg, MgK kk, MgBC bc, T tol, int maxCount, int tgtMode,
-                            long long *iters) {
-    extern __shared__ unsigned char smraw[];
-    int X = bc.E[0], Y = bc.E[1], Z = bc.E[2];
-    int n = (X + 3) * (Y + 3) * (Z + 3);
-    T *p = reinterpret_cast<T *>(smraw);
-    T *r = p + n;
+__device__ void coarse_gs(T *p, T *r, int X, int Y, int Z, const MgK &kk, const MgBC &bc, T tol, int maxCount, int tgtMode,
+                          long long *iters) {
     __shared__ T red[32];
     __shared__ int stop;
     int sy = Z + 3, sx = (Y + 3) * (Z + 3);
     auto at = [&](T *a, int i, int j, int k) -> T & { return a[(i + 1) * sx + (j + 1) * sy + (k + 1)]; };
     int tid = threadIdx.x, nt = blockDim.x;
-    for (int t = tid; t < n; t += nt) { p[t] = (T)0; r[t] = rg.p[t]; }   // pressureData(d) = 0 (poisson.cc:258)
-    __syncthreads();
     T thresh = tol;
     if (tgtMode) {
         // trapezoidal-weight mean of r over the core (weights 1/2 on end planes)
@@ -397,8 +392,22 @@ __global__ void k_mg_coarse(View3<T> pg, View3<const T> rg, MgK kk, MgBC bc, T t
         if (stop) break;
     }
     smem_impose_bc(p, X, Y, Z, bc, (const T *)nullptr, (const T *)nullptr, (const T *)nullptr);
-    for (int t = tid; t < n; t += nt) pg.p[t] = p[t];
+    __syncthreads();
     if (tid == 0 && iters) *iters += sweeps;
+}
+
+template <typename T>
+__global__ void k_mg_coarse(View3<T> pg, View3<const T> rg, MgK kk, MgBC bc, T tol, int maxCount, int tgtMode,
+                            long long *iters) {
+    extern __shared__ unsigned char smraw[];
+    int X = bc.E[0], Y = bc.E[1], Z = bc.E[2];
+    int n = (X + 3) * (Y + 3) * (Z + 3);
+    T *p = reinterpret_cast<T *>(smraw);
+    T *r = p + n;
+    for (int t = threadIdx.x; t < n; t += blockDim.x) { p[t] = (T)0; r[t] = rg.p[t]; }   // pressureData(d) = 0 (poisson.cc:258)
+    __syncthreads();
+    coarse_gs(p, r, X, Y, Z, kk, bc, tol, maxCount, tgtMode, iters);
+    for (int t = threadIdx.x; t < n; t += blockDim.x) pg.p[t] = p[t];
 }
 
 // ------------------------------------------------------------------ FP64 drivers
@@ -944,6 +953,158 @@ __global__ void k_tgt_rhs(View3<double> b, View3<const double> rhs, MgBC bc, con
     block_max_to(m, maxabs);
 }
 
+// ---- the coarse end of a target-mode V-cycle in one CTA
+// Levels Lt..depth (at most 16 intervals per axis at Lt) fit in shared memory
+// together; below ~50k points their sweeps, residuals and transfers are
+// launch-latency bound, and the coarsest Gauss-Seidel loop runs on one CTA
+// anyway.  k_mg_tail runs that whole sub-cycle: pre-smoothing from zero and
+// restriction down to the coarsest level, the coarsest solve (coarse_gs),
+// prolongation and post-smoothing back up to Lt, with the kernels' arithmetic
+// (k_tgt_sweep, k_tgt_residual, k_mg_restrict, k_mg_prolong_add), and writes
+// the level-Lt iterate with its face-ghost images to global memory.
+constexpr int kTailMaxLevels = 8;
+constexpr int kTailThreads = 1024;
+
+template <typename T>
+struct TailArgs {
+    int nl;                          // levels in the tail: Lt .. Lt + nl - 1 (the coarsest)
+    MgBC bc[kTailMaxLevels];
+    TgK<T> tk[kTailMaxLevels];       // sweep constants (damped Jacobi)
+    TgK<T> tr[kTailMaxLevels];       // residual constants (weight 1)
+    MgK kkc;                         // coarsest level (Gauss-Seidel)
+    T tol;
+    int maxc, pre, post;
+    const T *rin;                    // level-Lt right-hand side (padded)
+    T *pout;                         // level-Lt iterate (padded)
+    long long *iters;
+};
+
+template <typename T>
+__device__ __forceinline__ int tail_count(const MgBC &b) { return (b.E[0] + 3) * (b.E[1] + 3) * (b.E[2] + 3); }
+
+template <typename T, bool ZERO>
+__device__ void tail_sweep(T *out, const T *in, const T *r, const MgBC &bc, const TgK<T> &c) {
+    int E1 = bc.E[1], E2 = bc.E[2];
+    int sy = E2 + 3, sx = (E1 + 3) * sy;
+    int n = (bc.E[0] + 1) * (E1 + 1) * (E2 + 1);
+    View3<T> V; V.p = out; V.sx = sx; V.sy = sy;
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        int k = t % (E2 + 1), j = (t / (E2 + 1)) % (E1 + 1), i = t / ((E2 + 1) * (E1 + 1));
+        int o = (i + 1) * sx + (j + 1) * sy + (k + 1);
+        T v;
+        if (ZERO) v = c.ar * r[o];
+        else v = fma(c.ax, in[o - sx] + in[o + sx], fma(c.ay, in[o + sy] + in[o - sy], fma(c.az, in[o + 1] + in[o - 1], fma(c.ar, r[o], c.om1 * in[o]))));
+        put_scatter(V, i, j, k, v, bc);
+    }
+    __syncthreads();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kTailThreads) k_mg_tail(TailArgs<T> a) {
+    extern __shared__ unsigned char smraw[];
+    T *base = reinterpret_cast<T *>(smraw);
+    T *P[kTailMaxLevels], *Q[kTailMaxLevels], *R[kTailMaxLevels];
+    {
+        T *q = base;
+        for (int l = 0; l < a.nl; ++l) {
+            int n = tail_count<T>(a.bc[l]);
+            P[l] = q; Q[l] = q + n; R[l] = q + 2 * n;
+            q += 3 * n;
+        }
+    }
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int t = tid; t < tail_count<T>(a.bc[0]); t += nt) R[0][t] = a.rin[t];
+    __syncthreads();
+    for (int l = 0; l + 1 < a.nl; ++l) {
+        const MgBC &bc = a.bc[l];
+        int E1 = bc.E[1], E2 = bc.E[2], sy = E2 + 3, sx = (E1 + 3) * sy;
+        // pre-smoothing from zero (the first sweep ignores its input)
+        for (int n = 0; n < a.pre; ++n) {
+            if (n == 0) tail_sweep<T, true>(Q[l], P[l], R[l], bc, a.tk[l]);
+            else tail_sweep<T, false>(Q[l], P[l], R[l], bc, a.tk[l]);
+            T *x = P[l]; P[l] = Q[l]; Q[l] = x;
+        }
+        // residual into Q (core), then full-weighting restriction (pads resolved by index)
+        int n = (bc.E[0] + 1) * (E1 + 1) * (E2 + 1);
+        const TgK<T> &c = a.tr[l];
+        for (int t = tid; t < n; t += nt) {
+            int k = t % (E2 + 1), j = (t / (E2 + 1)) % (E1 + 1), i = t / ((E2 + 1) * (E1 + 1));
+            int o = (i + 1) * sx + (j + 1) * sy + (k + 1);
+            const T *p = P[l];
+            T lap = fma(c.lx, p[o - sx] + p[o + sx], fma(c.ly, p[o + sy] + p[o - sy], fma(c.lz, p[o + 1] + p[o - 1], c.lc * p[o])));
+            Q[l][o] = R[l][o] - lap;
+        }
+        __syncthreads();
+        const MgBC &bcc = a.bc[l + 1];
+        int C1 = bcc.E[1], C2 = bcc.E[2], csy = C2 + 3, csx = (C1 + 3) * csy;
+        int nc = (bcc.E[0] + 1) * (C1 + 1) * (C2 + 1);
+        View3<const T> tv; tv.p = Q[l]; tv.sx = sx; tv.sy = sy;
+        for (int t = tid; t < nc; t += nt) {
+            int k = t % (C2 + 1), j = (t / (C2 + 1)) % (C1 + 1), i = t / ((C2 + 1) * (C1 + 1));
+            int i2 = 2 * i, j2 = 2 * j, k2 = 2 * k;
+            bool interior = i2 > 0 && j2 > 0 && k2 > 0 && i2 < bc.E[0] && j2 < bc.E[1] && k2 < bc.E[2];
+            auto T_ = [&](int x, int y, int z) -> T { return interior ? tv(x, y, z) : pad_val(tv, x, y, z, bc); };
+            T facePoints = (T_(i2 + 1, j2, k2) + T_(i2 - 1, j2, k2) + T_(i2, j2 + 1, k2) + T_(i2, j2 - 1, k2) +
+                            T_(i2, j2, k2 + 1) + T_(i2, j2, k2 - 1)) * (T)0.0625;
+            T edgePoints = (T_(i2 + 1, j2 + 1, k2) + T_(i2 + 1, j2 - 1, k2) + T_(i2 - 1, j2 - 1, k2) + T_(i2 - 1, j2 + 1, k2) +
+                            T_(i2, j2 + 1, k2 + 1) + T_(i2, j2 - 1, k2 + 1) + T_(i2, j2 - 1, k2 - 1) + T_(i2, j2 + 1, k2 - 1) +
+                            T_(i2 + 1, j2, k2 + 1) + T_(i2 + 1, j2, k2 - 1) + T_(i2 - 1, j2, k2 - 1) + T_(i2 - 1, j2, k2 + 1)) * (T)0.03125;
+            T vertPoints = (T_(i2 + 1, j2 + 1, k2 + 1) + T_(i2 + 1, j2 + 1, k2 - 1) + T_(i2 + 1, j2 - 1, k2 + 1) +
+                            T_(i2 - 1, j2 + 1, k2 + 1) + T_(i2 + 1, j2 - 1, k2 - 1) + T_(i2 - 1, j2 + 1, k2 - 1) +
+                            T_(i2 - 1, j2 - 1, k2 + 1) + T_(i2 - 1, j2 - 1, k2 - 1)) * (T)0.015625;
+            R[l + 1][(i + 1) * csx + (j + 1) * csy + (k + 1)] = facePoints + edgePoints + vertPoints + tv(i2, j2, k2) * (T)0.125;
+        }
+        __syncthreads();
+    }
+    // coarsest level
+    {
+        int L = a.nl - 1;
+        const MgBC &bc = a.bc[L];
+        for (int t = tid; t < tail_count<T>(bc); t += nt) P[L][t] = (T)0;
+        __syncthreads();
+        coarse_gs(P[L], R[L], bc.E[0], bc.E[1], bc.E[2], a.kkc, bc, a.tol, a.maxc, 1, a.iters);
+    }
+    // back up: prolongation + add, post-smoothing
+    for (int l = a.nl - 2; l >= 0; --l) {
+        const MgBC &bc = a.bc[l], &bcc = a.bc[l + 1];
+        int E1 = bc.E[1], E2 = bc.E[2], sy = E2 + 3, sx = (E1 + 3) * sy;
+        int n = (bc.E[0] + 1) * (E1 + 1) * (E2 + 1);
+        View3<T> pf; pf.p = P[l]; pf.sx = sx; pf.sy = sy;
+        View3<const T> C; C.p = P[l + 1]; C.sy = bcc.E[2] + 3; C.sx = (bcc.E[1] + 3) * C.sy;
+        for (int t = tid; t < n; t += nt) {
+            int k = t % (E2 + 1), j = (t / (E2 + 1)) % (E1 + 1), i = t / ((E2 + 1) * (E1 + 1));
+            int i2 = i / 2, j2 = j / 2, k2 = k / 2;
+            bool io = i & 1, jo = j & 1, ko = k & 1;
+            T v;
+            if (io) {
+                if (jo) {
+                    if (ko) v = (C(i2, j2, k2) + C(i2 + 1, j2, k2) + C(i2, j2 + 1, k2) + C(i2, j2, k2 + 1) + C(i2 + 1, j2 + 1, k2) +
+                                 C(i2 + 1, j2, k2 + 1) + C(i2, j2 + 1, k2 + 1) + C(i2 + 1, j2 + 1, k2 + 1)) * (T)0.125;
+                    else v = (C(i2, j2, k2) + C(i2, j2 + 1, k2) + C(i2 + 1, j2, k2) + C(i2 + 1, j2 + 1, k2)) * (T)0.25;
+                } else {
+                    if (ko) v = (C(i2, j2, k2) + C(i2, j2, k2 + 1) + C(i2 + 1, j2, k2) + C(i2 + 1, j2, k2 + 1)) * (T)0.25;
+                    else v = (C(i2, j2, k2) + C(i2 + 1, j2, k2)) * (T)0.5;
+                }
+            } else {
+                if (jo) {
+                    if (ko) v = (C(i2, j2, k2) + C(i2, j2, k2 + 1) + C(i2, j2 + 1, k2) + C(i2, j2 + 1, k2 + 1)) * (T)0.25;
+                    else v = (C(i2, j2, k2) + C(i2, j2 + 1, k2)) * (T)0.5;
+                } else {
+                    if (ko) v = (C(i2, j2, k2) + C(i2, j2, k2 + 1)) * (T)0.5;
+                    else v = C(i2, j2, k2);
+                }
+            }
+            put_scatter(pf, i, j, k, v + pf(i, j, k), bc);
+        }
+        __syncthreads();
+        for (int m = 0; m < a.post; ++m) {
+            tail_sweep<T, false>(Q[l], P[l], R[l], bc, a.tk[l]);
+            T *x = P[l]; P[l] = Q[l]; Q[l] = x;
+        }
+    }
+    for (int t = tid; t < tail_count<T>(a.bc[0]); t += nt) a.pout[t] = P[0][t];
+}
+
 // ------------------------------------------------------------------ host
 static MgBC level_bc(const Ctx &c, int l, bool tgt) {
     MgBC b;
@@ -974,6 +1135,20 @@ static int chk(Ctx &c, const char *what) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) { c.err = std::string(what) + ": " + cudaGetErrorString(e); return SARAS_CUDA_ERROR; }
     return SARAS_OK;
+}
+
+// First level of the fused coarse tail (k_mg_tail), or -1: all axes at most 16
+// intervals, at least two levels, and every tail level in shared memory.
+static int tail_level(const Ctx &c) {
+    for (int l = 1; l < c.depth; ++l) {
+        const Level &L = c.lv[l];
+        if (std::max(L.n[0], std::max(L.n[1], L.n[2])) > 16) continue;
+        if (c.depth - l + 1 > kTailMaxLevels) return -1;
+        size_t bytes = 0;
+        for (int q = l; q <= c.depth; ++q) bytes += 3 * sizeof(double) * (size_t)c.lv[q].count;
+        return bytes <= 200 * 1024 ? l : -1;
+    }
+    return -1;
 }
 
 int mg_setup(Ctx &c) {
@@ -1015,6 +1190,11 @@ int mg_setup(Ctx &c) {
     if (smem > 220 * 1024) { c.err = "coarsest multigrid level too large for one CTA; increase V-Cycle Depth"; return SARAS_BAD_CONFIG; }
     SARAS_CUDA_TRY(cudaFuncSetAttribute(k_mg_coarse<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     SARAS_CUDA_TRY(cudaFuncSetAttribute(k_mg_coarse<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    c.tailLt = tail_level(c);
+    if (c.tailLt > 0) {
+        SARAS_CUDA_TRY(cudaFuncSetAttribute(k_mg_tail<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        SARAS_CUDA_TRY(cudaFuncSetAttribute(k_mg_tail<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    }
     if (p.testPoisson) {
         // multigrid_d3::initDirichlet (poisson_d3.cc:513-572), np = 1
         const Level &L0 = c.lv[0];
@@ -1174,15 +1354,42 @@ static int prolong_level(Ctx &c, int l, bool tgt, bool add) {
     return chk(c, "mg prolong");
 }
 
+template <typename T>
+static int tail_run(Ctx &c, int Lt) {
+    TailArgs<T> a;
+    a.nl = c.depth - Lt + 1;
+    size_t smem = 0;
+    for (int q = 0; q < a.nl; ++q) {
+        Level &L = c.lv[Lt + q];
+        a.bc[q] = level_bc(c, Lt + q, true);
+        a.tk[q] = make_tgk<T>(L, c.p.jacobiWeight);
+        a.tr[q] = make_tgk<T>(L, 1.0);
+        smem += 3 * sizeof(T) * (size_t)L.count;
+    }
+    a.kkc = make_k(c.lv[c.depth]);
+    a.tol = (T)1.0e-3;   // as coarse_solve in the target modes
+    a.maxc = 500;
+    a.pre = c.p.preSmooth;
+    a.post = c.p.postSmooth;
+    a.rin = R_<T>(c.lv[Lt]);
+    a.pout = A_<T>(c.lv[Lt]);
+    a.iters = (long long *)(c.dscal + 40);
+    k_mg_tail<T><<<1, kTailThreads, smem, c.stream>>>(a);
+    count_launch(c);
+    return chk(c, "mg tail");
+}
+
 // poisson::vCycle (poisson.cc:219-280) on level arrays of precision T.
 // zero0: the level-0 iterate starts at 0 (inner FP32 solve of the mixed mode).
 template <typename T>
 static int vcycle(Ctx &c, bool tgt, bool zero0) {
     int s;
     int d = c.depth;
+    int Lt = tgt ? c.tailLt : -1;   // target modes: levels Lt.. run as one fused kernel
     if ((s = smooth<T>(c, 0, c.p.preSmooth, zero0, tgt))) return s;
     for (int l = 0; l < d; ++l) {
         if ((s = restrict_level<T>(c, l, tgt))) return s;
+        if (l + 1 == Lt) { if ((s = tail_run<T>(c, Lt))) return s; d = Lt; break; }
         if (l + 1 == d) { if ((s = coarse_solve<T>(c, tgt))) return s; }
         else if ((s = smooth<T>(c, l + 1, c.p.preSmooth, true, tgt))) return s;
     }

@@ -195,14 +195,14 @@ struct L0View {
 };
 
 // Level-0 padded field -> level-1 core array: full weighting (coarse point i on
-// fine point 2i, taps outside the grid skipped).  The weights are powers of
-// two, so every weighted term of a split value is exact and the sum is kept in
-// float-pair arithmetic (no FP64 pipe work but the final addition).
+// fine point 2i, taps outside the grid skipped), in FP64: 27 fused
+// multiply-adds per coarse point are about 3.4 FP64 operations per fine point,
+// cheaper here than splitting every fine value into a float pair.
 __global__ void k_restrict0(L0View f, Grid3 g1, double *out) {
     long v = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (v >= g1.n()) return;
     int x = (int)(v % g1.W), y = (int)((v / g1.W) % g1.H), z = (int)(v / ((long)g1.W * g1.H));
-    fpair s = fpair{0.0f, 0.0f};
+    double s = 0.0;
     for (int dz = -1; dz <= 1; ++dz) {
         int zz = 2 * z + dz;
         if (zz < 0 || zz > f.n[0]) continue;
@@ -212,13 +212,11 @@ __global__ void k_restrict0(L0View f, Grid3 g1, double *out) {
             for (int dx = -1; dx <= 1; ++dx) {
                 int xx = 2 * x + dx;
                 if (xx < 0 || xx > f.n[2]) continue;
-                float w = fw1(dz) * fw1(dy) * fw1(dx);
-                fpair t = fp_of(f.at(zz, yy, xx));
-                s = fp_add(s, fpair{t.h * w, t.l * w});
+                s = fma((double)(fw1(dz) * fw1(dy) * fw1(dx)), f.at(zz, yy, xx), s);
             }
         }
     }
-    out[v] = f2d(s.h) + f2d(s.l);
+    out[v] = s;
 }
 
 // Level-l core array -> level-l+1 core array, the same weights (FP64; these
