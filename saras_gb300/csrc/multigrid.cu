@@ -396,6 +396,87 @@ __device__ void coarse_gs(T *p, T *r, int X, int Y, int Z, const MgK &kk, const 
     if (tid == 0 && iters) *iters += sweeps;
 }
 
+// The target modes' coarsest solve inside k_mg_tail, by one warp: the
+// compatible right-hand side (trapezoidal mean removed), then red-black
+// Gauss-Seidel sweeps (the two colours of i+j+k, ghosts refreshed before each)
+// until max|r - Lp| falls below tol times its initial value or maxCount
+// sweeps.  A warp needs no block barriers, which bound the block-wide
+// wavefront sweep on a level of about a hundred points.  Only the two
+// colours' order differs from the lexicographic sweep; the target modes only
+// need a small coarse residual, not the reference's iterates.
+template <typename T>
+__device__ void warp_ghosts(T *p, int X, int Y, int Z, const MgBC &bc) {
+    int lane = threadIdx.x & 31, sy = Z + 3, sx = (Y + 3) * sy;
+    auto at = [&](int i, int j, int k) -> T & { return p[(i + 1) * sx + (j + 1) * sy + (k + 1)]; };
+    for (int t = lane; t < (Y + 3) * (Z + 3); t += 32) {
+        int j = t / (Z + 3) - 1, k = t % (Z + 3) - 1;
+        if (bc.per[0]) { at(X + 1, j, k) = at(1, j, k); at(-1, j, k) = at(X - 1, j, k); }
+        else { at(-1, j, k) = at(1, j, k); at(X + 1, j, k) = at(X - 1, j, k); }
+    }
+    __syncwarp();
+    for (int t = lane; t < (X + 3) * (Z + 3); t += 32) {
+        int i = t / (Z + 3) - 1, k = t % (Z + 3) - 1;
+        if (bc.per[1]) { at(i, Y + 1, k) = at(i, 1, k); at(i, -1, k) = at(i, Y - 1, k); }
+        else { at(i, -1, k) = at(i, 1, k); at(i, Y + 1, k) = at(i, Y - 1, k); }
+    }
+    __syncwarp();
+    for (int t = lane; t < (X + 3) * (Y + 3); t += 32) {
+        int i = t / (Y + 3) - 1, j = t % (Y + 3) - 1;
+        if (bc.per[2]) { at(i, j, -1) = at(i, j, Z - 1); at(i, j, Z + 1) = at(i, j, 1); }
+        else { at(i, j, -1) = at(i, j, 1); at(i, j, Z + 1) = at(i, j, Z - 1); }
+    }
+    __syncwarp();
+}
+
+template <typename T>
+__device__ void coarse_rbgs_warp(T *p, T *r, int X, int Y, int Z, const MgK &kk, const MgBC &bc, T tol, int maxCount, long long *iters) {
+    int lane = threadIdx.x & 31, sy = Z + 3, sx = (Y + 3) * sy;
+    int n = (X + 1) * (Y + 1) * (Z + 1);
+    auto at = [&](T *a, int i, int j, int k) -> T & { return a[(i + 1) * sx + (j + 1) * sy + (k + 1)]; };
+    T sm = 0, sw = 0;
+    for (int t = lane; t < n; t += 32) {
+        int k = t % (Z + 1), j = (t / (Z + 1)) % (Y + 1), i = t / ((Z + 1) * (Y + 1));
+        T wt = (T)((i == 0 || i == X) ? 0.5 : 1.0) * (T)((j == 0 || j == Y) ? 0.5 : 1.0) * (T)((k == 0 || k == Z) ? 0.5 : 1.0);
+        sm += wt * at(r, i, j, k);
+        sw += wt;
+    }
+    T mean = warp_sum(sm) / warp_sum(sw);
+    T m0 = 0;
+    for (int t = lane; t < n; t += 32) {
+        int k = t % (Z + 1), j = (t / (Z + 1)) % (Y + 1), i = t / ((Z + 1) * (Y + 1));
+        at(r, i, j, k) -= mean;
+        m0 = fmax(m0, fabs(at(r, i, j, k)));
+    }
+    __syncwarp();
+    T thresh = tol * warp_max(m0);
+    long long sweeps = 0;
+    for (int it = 0; it <= maxCount; ++it) {
+        for (int colour = 0; colour < 2; ++colour) {
+            warp_ghosts(p, X, Y, Z, bc);
+            for (int t = lane; t < n; t += 32) {
+                int k = t % (Z + 1), j = (t / (Z + 1)) % (Y + 1), i = t / ((Z + 1) * (Y + 1));
+                if (((i + j + k) & 1) != colour) continue;
+                at(p, i, j, k) = mg_update<T>(at(p, i + 1, j, k), at(p, i - 1, j, k), at(p, i, j + 1, k), at(p, i, j - 1, k),
+                                              at(p, i, j, k + 1), at(p, i, j, k - 1), at(r, i, j, k), kk);
+            }
+            __syncwarp();
+        }
+        sweeps += 1;
+        warp_ghosts(p, X, Y, Z, bc);
+        T m = 0;
+        for (int t = lane; t < n; t += 32) {
+            int k = t % (Z + 1), j = (t / (Z + 1)) % (Y + 1), i = t / ((Z + 1) * (Y + 1));
+            T lap = mg_lap<T>(at(p, i + 1, j, k), at(p, i - 1, j, k), at(p, i, j + 1, k), at(p, i, j - 1, k), at(p, i, j, k + 1),
+                              at(p, i, j, k - 1), at(p, i, j, k), kk);
+            T v = fabs(at(r, i, j, k) - lap);
+            if (v != v) v = (T)INFINITY;
+            m = fmax(m, v);
+        }
+        if (warp_max(m) < thresh) break;
+    }
+    if (lane == 0 && iters) *iters += sweeps;
+}
+
 template <typename T>
 __global__ void k_mg_coarse(View3<T> pg, View3<const T> rg, MgK kk, MgBC bc, T tol, int maxCount, int tgtMode,
                             long long *iters) {
@@ -1062,7 +1143,8 @@ __global__ void __launch_bounds__(kTailThreads) k_mg_tail(TailArgs<T> a) {
         const MgBC &bc = a.bc[L];
         for (int t = tid; t < tail_count<T>(bc); t += nt) P[L][t] = (T)0;
         __syncthreads();
-        coarse_gs(P[L], R[L], bc.E[0], bc.E[1], bc.E[2], a.kkc, bc, a.tol, a.maxc, 1, a.iters);
+        if (tid < 32) coarse_rbgs_warp(P[L], R[L], bc.E[0], bc.E[1], bc.E[2], a.kkc, bc, a.tol, a.maxc, a.iters);
+        __syncthreads();
     }
     // back up: prolongation + add, post-smoothing
     for (int l = a.nl - 2; l >= 0; --l) {

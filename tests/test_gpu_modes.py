@@ -35,6 +35,30 @@ def test_target_modes_reach_residual(mode):
         assert 0 < st.vcycles < 100
 
 
+@pytest.mark.parametrize("guess", [F.GUESS_EXTRAPOLATE, F.GUESS_QUADRATIC, F.GUESS_PARITY])
+def test_history_guesses_reach_target_with_fewer_cycles(guess):
+    """The history-based initial guesses (extrapolations of the previous
+    pressure corrections) reach the same residual target as the previous
+    pressure, in no more V-cycles, and are reported as the guess source."""
+    _, prev = target_case(F.MG_MIXED)
+    _, g = target_case(F.MG_MIXED)
+    g.set_guess_mode(guess)
+    cyc = {"prev": [], "guess": []}
+    sources = []
+    for step in range(8):
+        s1, st1 = prev.time_advance()
+        s2, st2 = g.time_advance()
+        assert s1 == 0 and s2 == 0
+        assert st2.fine_residual <= 1e-8
+        if step >= 4:
+            cyc["prev"].append(st1.vcycles)
+            cyc["guess"].append(st2.vcycles)
+            sources.append(st2.guess_source)
+    assert sum(cyc["guess"]) <= sum(cyc["prev"])
+    assert all(src in (0, guess) for src in sources) and guess in sources
+    assert C.rel_err(g.get(F.FIELD_P), prev.get(F.FIELD_P)) < 1e-7
+
+
 def test_mixed_matches_plain_fp64():
     """Every result of the precision form states its error against the plain FP64 solve."""
     _, a = target_case(F.MG_PLAIN_TARGET)
