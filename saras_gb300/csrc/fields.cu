@@ -238,6 +238,38 @@ __global__ void k_divergence(View3<double> D, Vel V, Box full, UC u, double scal
     D(i, j, k) = out;
 }
 
+// Split-FP64 form (fastKernels = 2) of the scaled divergence: the three face
+// differences from split values, the folded factors as float pairs (about
+// 2^-44 of the largest term), one FP64 addition per point; one thread per
+// (j, k) column of the P full box marching along i with Vx(i-1) carried.
+// Points outside the P core are 0, as in k_divergence.
+struct DivDf {
+    fpair k[3];
+};
+constexpr int kProjMarch = 8;   // points per thread along i (divergence, projection)
+
+__global__ void __launch_bounds__(256) k_divergence_df(View3<double> D, Vel V, Box full, DivDf q) {
+    int k = full.lo[2] + blockIdx.x * 32 + threadIdx.x;
+    int j = full.lo[1] + blockIdx.y * 8 + threadIdx.y;
+    int i0 = full.lo[0] + blockIdx.z * kProjMarch;
+    if (k >= full.lo[2] + full.ext[2] || j >= full.lo[1] + full.ext[1]) return;
+    int iend = min(i0 + kProjMarch, full.lo[0] + full.ext[0]);
+    bool jk = j >= 0 && k >= 0 && j < D.n[1] && k < D.n[2];
+    fpair xm = fpair{0.0f, 0.0f};
+    bool have = false;   // xm holds Vx(i-1)
+    for (int i = i0; i < iend; ++i) {
+        if (!(jk && i >= 0 && i < D.n[0])) { D(i, j, k) = 0.0; continue; }
+        if (!have) { xm = fp_of(V.v[0](i - 1, j, k)); have = true; }
+        fpair xc = fp_of(V.v[0](i, j, k));
+        fpair dx = fp_add(xc, fp_neg(xm));
+        fpair dy = fp_add(fp_of(V.v[1](i, j, k)), fp_neg(fp_of(V.v[1](i, j - 1, k))));
+        fpair dz = fp_add(fp_of(V.v[2](i, j, k)), fp_neg(fp_of(V.v[2](i, j, k - 1))));
+        fpair sum = fp_add(fp_add(fp_mul(q.k[0], dx), fp_mul(q.k[1], dy)), fp_mul(q.k[2], dz));
+        D(i, j, k) = f2d(sum.h) + f2d(sum.l);
+        xm = xc;
+    }
+}
+
 // Whole-array dst = a*dst + b*src (field arithmetic of field.cc:631-715).
 __global__ void k_axpby(double *dst, double a, const double *src, double b, long n) {
     long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
@@ -759,6 +791,59 @@ __global__ void k_project(View3<double> out, View3<const double> in, View3<const
     out(i, j, k) = targeted ? bc_resolve(prog, i, j, k, base) : base(i, j, k);
 }
 
+// The fused-form projection with its boundary program split in two launches
+// (as the split Jacobi sweep): k_project_bulk marches the bulk box (the points
+// no boundary op targets: V - fastDt (Pp(+1) - Pp), no device calls, Pp along
+// the component's own axis carried in registers for Vx), k_project_shell
+// resolves the program on the remaining points of the full box.
+template <int C>
+__global__ void __launch_bounds__(256) k_project_bulk(View3<double> out, View3<const double> in, View3<const double> Pp, BcProgram prog,
+                                                      double fastDt) {
+    int k = prog.blo[2] + blockIdx.x * 32 + threadIdx.x;
+    int j = prog.blo[1] + blockIdx.y * 8 + threadIdx.y;
+    int i0 = prog.blo[0] + blockIdx.z * kProjMarch;
+    if (k > prog.bhi[2] || j > prog.bhi[1]) return;
+    int iend = min(i0 + kProjMarch - 1, prog.bhi[0]);
+    bool jk = j < in.n[1] && k < in.n[2];
+    double pc = Pp(i0, j, k);
+    for (int i = i0; i <= iend; ++i) {
+        double v = in(i, j, k);
+        double pn = C == 0 ? Pp(i + 1, j, k) : C == 1 ? Pp(i, j + 1, k) : Pp(i, j, k + 1);
+        if (jk && i < in.n[0]) v = fma(-fastDt, pn - pc, v);
+        out(i, j, k) = v;
+        pc = C == 0 ? pn : Pp(i + 1, j, k);
+    }
+}
+
+template <int C>
+__global__ void k_project_shell(View3<double> out, View3<const double> in, View3<const double> Pp, BcProgram prog, Box full,
+                                double fastDt) {
+    int s = blockIdx.y, d = s >> 1;
+    int lo[3], hi[3];
+    for (int e = 0; e < 3; ++e) {
+        if (e < d) { lo[e] = prog.blo[e]; hi[e] = prog.bhi[e]; }
+        else { lo[e] = full.lo[e]; hi[e] = full.lo[e] + full.ext[e] - 1; }
+    }
+    if (s & 1) lo[d] = prog.bhi[d] + 1;
+    else hi[d] = prog.blo[d] - 1;
+    if (lo[0] > hi[0] || lo[1] > hi[1] || lo[2] > hi[2]) return;
+    auto base = [&](int x, int y, int z) -> double {
+        double v = in(x, y, z);
+        if (x >= 0 && y >= 0 && z >= 0 && x < in.n[0] && y < in.n[1] && z < in.n[2]) {
+            double sp = C == 0 ? Pp(x + 1, y, z) : C == 1 ? Pp(x, y + 1, z) : Pp(x, y, z + 1);
+            v = fma(-fastDt, sp - Pp(x, y, z), v);
+        }
+        return v;
+    };
+    long n1 = hi[1] - lo[1] + 1, n2 = hi[2] - lo[2] + 1, n = (long)(hi[0] - lo[0] + 1) * n1 * n2;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+        int k = lo[2] + (int)(t % n2), j = lo[1] + (int)((t / n2) % n1), i = lo[0] + (int)(t / (n1 * n2));
+        bool targeted = false;
+        for (int o = 0; o < prog.nops; ++o) if (in_box(prog.op[o].lo, prog.op[o].hi, i, j, k)) { targeted = true; break; }
+        out(i, j, k) = targeted ? bc_resolve(prog, i, j, k, base) : base(i, j, k);
+    }
+}
+
 // ------------------------------------------------------------------ diagnostics
 // tseries::writeTSData (tseries.cc:137-246): per-block partial sums of the
 // face-averaged energy and of <w T>, and the block max of the divergence over
@@ -1110,8 +1195,15 @@ int vfield_divergence(Ctx &c, double *dst, bool scale_dt) {
     prof_begin(c, PK_DIVERGENCE, 0);
     Fold3 fk;
     for (int d = 0; d < 3; ++d) fk.k[d] = u.gm[d] * u.ih[d] * (scale_dt ? 1.0 / c.dt : 1.0);
-    k_divergence<<<g, bl, 0, c.stream>>>(D, make_vel(c), fb, u, 1.0 / c.dt, scale_dt ? 1 : 0,
-                                         (scale_dt && c.p.testPoisson) ? 1 : 0, c.p.fastKernels != 0, fk);
+    if (c.p.fastKernels == 2 && !(scale_dt && c.p.testPoisson)) {
+        DivDf q;
+        for (int d = 0; d < 3; ++d) { q.k[d].h = (float)fk.k[d]; q.k[d].l = (float)(fk.k[d] - (double)q.k[d].h); }
+        dim3 gd((fb.ext[2] + 31) / 32, (fb.ext[1] + 7) / 8, (fb.ext[0] + kProjMarch - 1) / kProjMarch);
+        k_divergence_df<<<gd, dim3(32, 8), 0, c.stream>>>(D, make_vel(c), fb, q);
+    } else {
+        k_divergence<<<g, bl, 0, c.stream>>>(D, make_vel(c), fb, u, 1.0 / c.dt, scale_dt ? 1 : 0,
+                                             (scale_dt && c.p.testPoisson) ? 1 : 0, c.p.fastKernels != 0, fk);
+    }
     count_launch(c);
     prof_end(c, PK_DIVERGENCE, 0, 5.0 * 8.0 * (double)D.size());
     return check_launch(c, "divergence");
@@ -1434,7 +1526,16 @@ int project(Ctx &c, bool with_bc) {
         View3<const double> in = cview(c, field), Pp = cview(c, SARAS_FIELD_PP);
         double fdt = u.gm[q] * u.ih[q] * c.dt;
         int wb = with_bc ? 1 : 0;
-        if (c.p.fastKernels) {
+        if (c.p.fastKernels && with_bc) {
+            const BcProgram &pg = f.full;
+            dim3 gb((pg.bhi[2] - pg.blo[2] + 1 + 31) / 32, (pg.bhi[1] - pg.blo[1] + 1 + 7) / 8,
+                    (pg.bhi[0] - pg.blo[0] + 1 + kProjMarch - 1) / kProjMarch);
+            dim3 gs(64, 6);
+            if (q == 0) { k_project_bulk<0><<<gb, dim3(32, 8), 0, c.stream>>>(out, in, Pp, pg, fdt); k_project_shell<0><<<gs, 256, 0, c.stream>>>(out, in, Pp, pg, fb, fdt); }
+            if (q == 1) { k_project_bulk<1><<<gb, dim3(32, 8), 0, c.stream>>>(out, in, Pp, pg, fdt); k_project_shell<1><<<gs, 256, 0, c.stream>>>(out, in, Pp, pg, fb, fdt); }
+            if (q == 2) { k_project_bulk<2><<<gb, dim3(32, 8), 0, c.stream>>>(out, in, Pp, pg, fdt); k_project_shell<2><<<gs, 256, 0, c.stream>>>(out, in, Pp, pg, fb, fdt); }
+            count_launch(c);
+        } else if (c.p.fastKernels) {
             if (q == 0) k_project<0, true><<<g, bl, 0, c.stream>>>(out, in, Pp, f.full, fb, u, c.dt, wb, fdt);
             if (q == 1) k_project<1, true><<<g, bl, 0, c.stream>>>(out, in, Pp, f.full, fb, u, c.dt, wb, fdt);
             if (q == 2) k_project<2, true><<<g, bl, 0, c.stream>>>(out, in, Pp, f.full, fb, u, c.dt, wb, fdt);

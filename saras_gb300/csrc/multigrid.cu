@@ -968,6 +968,44 @@ __global__ void __launch_bounds__(256) k_fx_update(long long *__restrict__ pout,
     if (bad) atomicExch(flag, 1);
 }
 
+// The fixed-point iterate straight from the previous Pp: core points with
+// their face-ghost images (k_mg_init_p's put_scatter), no FP64 level copy.
+__global__ void k_fx_init(long long *__restrict__ dst, View3<const double> src, MgBC bc, int s, int *flag) {
+    int i, j, k;
+    if (!core_pt(bc.E, i, j, k)) return;
+    bool bad = false;
+    View3<long long> V;
+    V.p = dst; V.sx = src.sx; V.sy = src.sy;
+    put_scatter(V, i, j, k, d2fx(src(i, j, k), s, bad), bc);
+    if (bad) atomicExch(flag, 1);
+}
+
+// The solve's output written straight into Pp: every padded point takes the
+// value of the core point the imposeBC composition maps it to (k_mg_output's
+// mapping, target modes: periodic or mirror per axis), converted once to FP64;
+// chk receives round(Pp 2^s), the FP64 result back in fixed point, whose exact
+// residual is the residual of what the solve returns.
+__global__ void k_fx_output(double *__restrict__ dst, long long *__restrict__ chk, const long long *__restrict__ src, MgBC bc,
+                            double inv2s, int s, int *flag) {
+    int E1 = bc.E[1], E2 = bc.E[2];
+    long sy = E2 + 3, sx = (long)(E1 + 3) * sy;
+    long n = (long)(bc.E[0] + 3) * sx;
+    bool bad = false;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+        int q[3] = {(int)(t / sx) - 1, (int)((t / sy) % (E1 + 3)) - 1, (int)(t % sy) - 1};
+        for (int d = 2; d >= 0; --d) {
+            int E = bc.E[d];
+            if (q[d] >= 0 && q[d] <= E) continue;
+            if (bc.per[d]) q[d] = q[d] < 0 ? E - 1 : 1;
+            else q[d] = q[d] < 0 ? 1 : E - 1;
+        }
+        double x = __ll2double_rn(src[(q[0] + 1) * sx + (q[1] + 1) * sy + (q[2] + 1)]) * inv2s;
+        dst[t] = x;
+        chk[t] = d2fx(x, s, bad);
+    }
+    if (bad) atomicExch(flag, 1);
+}
+
 // dst = round(src 2^s) over a whole padded array (face-ghost images included).
 __global__ void k_fx_from(long long *__restrict__ dst, const double *__restrict__ src, long n, int s, int *flag) {
     bool bad = false;
@@ -1000,38 +1038,48 @@ __global__ void k_fx_to(double *__restrict__ dst, long long *__restrict__ chk, c
 }
 
 // ---- target modes (FP64 / mixed)
-// Trapezoidal-weight partial sums of the core of rhs.
-__global__ void k_trap_sum(View3<const double> rhs, MgBC bc, double *part) {
-    __shared__ double sm[32];
-    int E0 = bc.E[0], E1 = bc.E[1], E2 = bc.E[2];
-    long n = (long)(E0 + 1) * (E1 + 1) * (E2 + 1);
+// Trapezoidal-weight partial sums of the core of rhs: one thread per (j, k)
+// column marching kIch points along i (32-bit index arithmetic), one partial
+// per block in block order.
+__global__ void __launch_bounds__(256) k_trap_sum(View3<const double> rhs, MgBC bc, double *part) {
+    __shared__ double sm[8];
+    int k = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y, i0 = blockIdx.z * kIch;
     // weight 2^-(number of axes on which the point is an end point), as one
     // table lookup: the product of three halves costs GB300's FP64 pipe
     const double wt[4] = {1.0, 0.5, 0.25, 0.125};
     double s = 0;
-    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
-        int k = (int)(t % (E2 + 1)), j = (int)((t / (E2 + 1)) % (E1 + 1)), i = (int)(t / ((long)(E2 + 1) * (E1 + 1)));
-        int ends = (i == 0 || i == E0) + (j == 0 || j == E1) + (k == 0 || k == E2);
-        s = fma(wt[ends], rhs(i, j, k), s);
+    if (j <= bc.E[1] && k <= bc.E[2]) {
+        int ejk = (j == 0 || j == bc.E[1]) + (k == 0 || k == bc.E[2]);
+        int iend = min(i0 + kIch - 1, bc.E[0]);
+        for (int i = i0; i <= iend; ++i) s = fma(wt[ejk + (i == 0 || i == bc.E[0])], rhs(i, j, k), s);
     }
     s = warp_sum(s);
-    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
+    if (threadIdx.x == 0) sm[threadIdx.y] = s;
     __syncthreads();
-    if (threadIdx.x == 0) { double S = 0; for (int w = 0; w < (int)(blockDim.x >> 5); ++w) S += sm[w]; part[blockIdx.x] = S; }
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        double S = 0;
+        for (int w = 0; w < 8; ++w) S += sm[w];
+        part[((long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = S;
+    }
 }
 
-// b = rhs - trapmean over the core; block max |b|.  The mean is one product
-// with 1/wsum (wsum = product of the interval counts).
-__global__ void k_tgt_rhs(View3<double> b, View3<const double> rhs, MgBC bc, const double *sum, double inv_wsum, double *maxabs) {
-    int i, j, k;
-    bool ok = core_pt(bc.E, i, j, k);
-    double m = 0;
-    if (ok) {
-        double v = rhs(i, j, k) - *sum * inv_wsum;
-        b(i, j, k) = v;
-        m = fabs(v);
+// b = rhs - trapmean over the core; max |b| (block maxima, atomic).  The mean
+// is one product with 1/wsum (wsum = product of the interval counts).
+__global__ void __launch_bounds__(256) k_tgt_rhs(View3<double> b, View3<const double> rhs, MgBC bc, const double *sum, double inv_wsum,
+                                                 double *maxabs) {
+    int k = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y, i0 = blockIdx.z * kIch;
+    unsigned long long m = 0;
+    if (j <= bc.E[1] && k <= bc.E[2]) {
+        double mean = *sum * inv_wsum;
+        int iend = min(i0 + kIch - 1, bc.E[0]);
+        for (int i = i0; i <= iend; ++i) {
+            double v = rhs(i, j, k) - mean;
+            b(i, j, k) = v;
+            unsigned long long a = abs_bits(v);
+            m = a > m ? a : m;
+        }
     }
-    block_max_to(m, maxabs);
+    block_max_bits_to(m, maxabs);
 }
 
 // ---- the coarse end of a target-mode V-cycle in one CTA
@@ -1668,8 +1716,8 @@ int mg_fine_residual(Ctx &c, const double *pp, double *maxres, double *maxb) {
 // values), and the counters are set.  done = false (a value left the
 // fixed-point range, which takes a diverging iterate) leaves L0.pa() holding
 // the previous Pp again for the FP64 refinement loop.
-static int mixed_fixed(Ctx &c, double bmax, double target, bool wantGuess, double &r, int &source, int &cyc, int &steps, bool &done,
-                       saras_step_stats *st) {
+static int mixed_fixed(Ctx &c, double bmax, double pmax, double target, bool wantGuess, double &r, int &source, int &cyc, int &steps,
+                       bool &done, saras_step_stats *st) {
     int s;
     Level &L0 = c.lv[0];
     MgBC bc0 = level_bc(c, 0, true);
@@ -1682,15 +1730,16 @@ static int mixed_fixed(Ctx &c, double bmax, double target, bool wantGuess, doubl
     long long *B = c.fx[2];
     unsigned long long *dmax = reinterpret_cast<unsigned long long *>(c.dscal + 34);
     int *dflag = reinterpret_cast<int *>(c.dscal + 35);
-    // scale: |P|, |B| <= 2^55 for the largest of max|p| (padded array) and max|b| / l
-    SARAS_CUDA_TRY(cudaMemsetAsync(c.dscal + 33, 0, sizeof(double) * 3, c.stream));
-    k_maxabs<<<grid_blocks(L0.count), 256, 0, c.stream>>>(L0.pa(), L0.count, c.dscal + 33);
-    count_launch(c);
-    if ((s = chk(c, "fixed-point scale"))) return s;
-    if ((s = read_scalars(c, 33, 1))) return s;
+    // scale: |P|, |B| <= 2^55 for the largest of max|p| (the padded Pp) and max|b| / l
+    SARAS_CUDA_TRY(cudaMemsetAsync(c.dscal + 34, 0, sizeof(double) * 2, c.stream));
     double l = L0.lx;
-    double M = std::max(c.hscal[33], bmax / l);
-    if (!(M > 0.0) || !std::isfinite(M)) return SARAS_OK;   // nothing to scale (or not finite): FP64 path
+    double M = std::max(pmax, bmax / l);
+    if (!(M > 0.0) || !std::isfinite(M)) {   // nothing to scale (or not finite): the FP64 path, from Pp
+        dim3 gi, bi; core_dims(L0, gi, bi);
+        k_mg_init_p<double><<<gi, bi, 0, c.stream>>>(lview<double>(L0, L0.pa()), lcview<double>(L0, c.f[SARAS_FIELD_PP]), bc0);
+        count_launch(c);
+        return chk(c, "fixed-point skip");
+    }
     int sc = 54 - std::ilogb(M);
     sc = std::max(-900, std::min(900, sc));
     double inv2s = std::ldexp(1.0, -sc);
@@ -1729,7 +1778,7 @@ static int mixed_fixed(Ctx &c, double bmax, double target, bool wantGuess, doubl
     };
     bool bad = false;
     int built = 0;
-    k_fx_from<<<nbF, 256, 0, c.stream>>>(c.fx[0], L0.pa(), L0.count, sc, dflag);
+    k_fx_init<<<gc, bcd, 0, c.stream>>>(c.fx[0], lcview<double>(L0, c.f[SARAS_FIELD_PP]), bc0, sc, dflag);
     count_launch(c);
     if ((s = refine(0, false, r, bad))) return s;
     if (bad) return SARAS_OK;
@@ -1769,7 +1818,7 @@ static int mixed_fixed(Ctx &c, double bmax, double target, bool wantGuess, doubl
         }
         if (bad) break;
         // the FP64 result, and the exact residual of those FP64 values
-        k_fx_to<<<nbF, 256, 0, c.stream>>>(L0.pa(), c.fx[cur ^ 1], c.fx[cur], L0.count, inv2s, sc, dflag);
+        k_fx_output<<<nbF, 256, 0, c.stream>>>(c.f[SARAS_FIELD_PP], c.fx[cur ^ 1], c.fx[cur], bc0, inv2s, sc, dflag);
         count_launch(c);
         double rf = 0;
         if ((s = refine(cur ^ 1, false, rf, bad))) return s;
@@ -1800,23 +1849,30 @@ static int mg_solve_target(Ctx &c, int *cycles, double *residual, saras_step_sta
     int nb = std::min(grid_blocks(ncore), c.redCap);
     // b = rhs - trapezoidal mean (stored in level-0 FP64 r)
     SARAS_CUDA_TRY(cudaMemsetAsync(c.dscal + 30, 0, sizeof(double) * 6, c.stream));
-    k_trap_sum<<<nb, 256, 0, c.stream>>>(lcview<double>(L0, c.f[SARAS_FIELD_MGRHS]), bc0, c.red);
-    k_final_reduce<<<1, 256, 0, c.stream>>>(c.red, nb, 0, c.dscal + 30);
+    dim3 gmr, bmr; march_dims(L0, gmr, bmr);
+    int nparts = (int)(gmr.x * gmr.y * gmr.z);
+    if (nparts > c.redCap) { c.err = "reduction buffer too small"; return SARAS_TOO_LARGE; }
+    k_trap_sum<<<gmr, bmr, 0, c.stream>>>(lcview<double>(L0, c.f[SARAS_FIELD_MGRHS]), bc0, c.red);
+    k_final_reduce<<<1, 256, 0, c.stream>>>(c.red, nparts, 0, c.dscal + 30);
     double wsum = 1.0;
     for (int d = 0; d < 3; ++d) wsum *= (double)L0.n[d];
-    k_tgt_rhs<<<g, b, 0, c.stream>>>(lview<double>(L0, L0.r), lcview<double>(L0, c.f[SARAS_FIELD_MGRHS]), bc0, c.dscal + 30, 1.0 / wsum, c.dscal + 31);
+    k_tgt_rhs<<<gmr, bmr, 0, c.stream>>>(lview<double>(L0, L0.r), lcview<double>(L0, c.f[SARAS_FIELD_MGRHS]), bc0, c.dscal + 30, 1.0 / wsum,
+                                        c.dscal + 31);
     // pressure history for the learned / extrapolated guess
     bool wantGuess = c.guessMode != SARAS_GUESS_PREVIOUS;
     if (wantGuess || c.collecting) {
         if ((s = unet_begin_solve(c))) return s;
     }
-    // p = Pp (initial guess) with face ghosts
+    // p = Pp (initial guess) with face ghosts; the fixed-point path reads Pp
+    // itself and only needs max|Pp| for its scale
+    bool fixedPath = c.mgMode == SARAS_MG_MIXED && L0.lx == L0.ly && L0.ly == L0.lz;
     L0.cur = 0;
-    k_mg_init_p<double><<<g, b, 0, c.stream>>>(lview<double>(L0, L0.pa()), lcview<double>(L0, c.f[SARAS_FIELD_PP]), bc0);
+    if (fixedPath) k_maxabs<<<grid_blocks(L0.count), 256, 0, c.stream>>>(c.f[SARAS_FIELD_PP], L0.count, c.dscal + 33);
+    else k_mg_init_p<double><<<g, b, 0, c.stream>>>(lview<double>(L0, L0.pa()), lcview<double>(L0, c.f[SARAS_FIELD_PP]), bc0);
     count_launch(c, 4);
     if ((s = chk(c, "target load"))) return s;
-    if ((s = read_scalars(c, 31, 1))) return s;
-    double bmax = c.hscal[31];
+    if ((s = read_scalars(c, 31, 3))) return s;
+    double bmax = c.hscal[31], pmax = c.hscal[33];
     double target = c.mgTarget * bmax;
     int sx0 = (L0.n[1] + 3) * (L0.n[2] + 3), sy0 = L0.n[2] + 3;
     TgK<double> t0 = make_tgk<double>(L0, 1.0);
@@ -1848,8 +1904,8 @@ static int mg_solve_target(Ctx &c, int *cycles, double *residual, saras_step_sta
     double r = 0;
     int source = 0, cyc = 0, steps = 0, built = 0;
     bool fixedDone = false;
-    if (c.mgMode == SARAS_MG_MIXED && L0.lx == L0.ly && L0.ly == L0.lz) {
-        if ((s = mixed_fixed(c, bmax, target, wantGuess, r, source, cyc, steps, fixedDone, st))) return s;
+    if (fixedPath) {
+        if ((s = mixed_fixed(c, bmax, pmax, target, wantGuess, r, source, cyc, steps, fixedDone, st))) return s;
     }
     if (!fixedDone) {
     if ((s = fine_res(false, &r))) return s;
@@ -1891,9 +1947,11 @@ static int mg_solve_target(Ctx &c, int *cycles, double *residual, saras_step_sta
     }
     if (!fixedDone && built) unet_record(c, built, cyc);
     if (st) { st->refine_steps = steps; st->fine_residual = bmax > 0 ? r / bmax : r; }
-    k_mg_output<<<grid_blocks(L0.count), 256, 0, c.stream>>>(lview<double>(L0, c.f[SARAS_FIELD_PP]), lcview<double>(L0, L0.pa()), bc0,
-                                                             nullptr, nullptr, nullptr);
-    count_launch(c);
+    if (!fixedDone) {   // the fixed-point path has written Pp already (k_fx_output)
+        k_mg_output<<<grid_blocks(L0.count), 256, 0, c.stream>>>(lview<double>(L0, c.f[SARAS_FIELD_PP]), lcview<double>(L0, L0.pa()), bc0,
+                                                                 nullptr, nullptr, nullptr);
+        count_launch(c);
+    }
     if ((s = chk(c, "target output"))) return s;
     if (c.collecting && r <= target) {
         if ((s = unet_collect_sample(c, L0.r))) return s;
