@@ -48,11 +48,14 @@ def tgv_params(mode, guess=0, ind=GRID_INDEX, depth=DEPTH):
     p.tStp = DT
     p.cnTolerance = 1.0e-8
     p.mgTolerance = 1.0e-8
-    p.preSmooth = p.postSmooth = 3
+    # each arm with the smoothing it is fastest with at 257^3: the plain FP64
+    # solve with V(3,3) (8 cycles; V(4,4) 7 and V(5,5) 6 cycles take longer),
+    # the mixed solve with V(4,4) (3 cycles, against 4 with V(3,3))
+    p.preSmooth = p.postSmooth = 4 if mode == _abi.MG_MIXED else 3
     p.mgMode = mode
     p.mgTarget = TARGET
     p.mgMaxCycles = 100
-    p.mixedCycles = 2
+    p.mixedCycles = 3
     p.jacobiWeight = 6.0 / 7.0 if mode != _abi.MG_REFERENCE else 1.0
     p.fastKernels = 2 if mode != _abi.MG_REFERENCE else 0
     p.guessMode = guess
@@ -220,7 +223,8 @@ def run_ours(args, dist):
     totals = []
     for k in range(len(names)):
         n, ms, b = g.profile_read(k)
-        totals.append((ms, k, n, b))
+        if b > 0:   # kernel slots with algorithmic bytes (not the initial-guess phase)
+            totals.append((ms, k, n, b))
         g.profile_enable(k, False)
     dom = max(totals)[1]
     g.profile_enable(dom, True)
@@ -328,7 +332,9 @@ def run_ours(args, dist):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic (Taylor-Green initial condition)",
         "config": {
             "workload": "Taylor-Green vortex 257^3 (2^8+1 vertex points per axis), [0,2pi]^3 PPP, Re 1600, dt 5e-4; "
-                        "pressure solve: FP32 V(3,3) cycles (two per refinement step) inside iterative refinement with an exact fixed-point residual, to max|b-Ap|/max|b| <= 1e-8",
+                        "pressure solve: FP32 V(4,4) cycles inside iterative refinement with an exact fixed-point residual (three cycles in the "
+                        "first refinement step, later steps sized by the measured contraction), to max|b-Ap|/max|b| <= 1e-8; "
+                        "plain arm: FP64 V(3,3) cycles to the same residual",
             "grid": [257, 257, 257], "vcycle_depth": DEPTH, "mg_mode": "mixed_fp32_in_fp64",
             "warm_start": "unet (3-level 16/32/64, tcgen05 BF16 convs) correcting 2 Pp(n-1) - Pp(n-2), "
                           "least-squares step length, fallback to the previous pressure"
@@ -388,20 +394,21 @@ def run_reference(args, dist):
     init_tgv(o, p)
     for k in range(args.warmup):
         o.time_advance()
+    steps = min(args.steps, 20)   # about a second a step on 16 cores: the run stays within a few minutes
     t0 = time.perf_counter()
-    for k in range(args.steps):
+    for k in range(steps):
         o.time_advance()
     el = time.perf_counter() - t0
-    v = args.steps / el
+    v = steps / el
     return {
         "impl": "reference", "metric": METRIC, "value": round(v, 6), "unit": "steps/s", "n_gpus": dist.world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * el / args.steps, 1), "higher_is_better": True,
+        "steps": steps, "warmup": args.warmup, "ms_per_step": round(1e3 * el / steps, 1), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (Taylor-Green initial condition)",
         "config": {"workload": "Taylor-Green vortex 257^3, Re 1600, dt 5e-4; reference multigrid (Jacobi V(3,3), "
                                "V-cycle loop capped at 2 cycles per step as the bounded sample)",
                    "grid": [257, 257, 257], "implementation": "CPU oracle (strict restatement of the reference), OpenMP"},
         "cpu_baseline": {"value": round(v, 6), "unit": "steps/s", "cores": threads, "kind": "port",
-                         "sample": "%d reference steps of TGV 257^3, V-cycle loop capped at 2 cycles" % args.steps},
+                         "sample": "%d reference steps of TGV 257^3, V-cycle loop capped at 2 cycles" % steps},
         "e2e": {"value": round(v, 6), "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -409,7 +416,7 @@ def run_reference(args, dist):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=100)   # about 1 s timed: several nvidia-smi clock samples
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--guess", default="learned", choices=["learned", "extrapolate", "quadratic", "previous"],

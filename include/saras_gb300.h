@@ -107,7 +107,10 @@ typedef struct saras_params {
     int mgMode;               /* enum saras_mg_mode */
     double mgTarget;          /* residual target of the PLAIN_TARGET / MIXED modes */
     int mgMaxCycles;          /* cap on V-cycles (target modes)                 */
-    int mixedCycles;          /* FP32 V-cycles per refinement step              */
+    int mixedCycles;          /* FP32 V-cycles of the first refinement step of a
+                                 solve; later steps (and every step with 0) run
+                                 the fewest, at most this many, that the measured
+                                 contraction per V-cycle predicts to meet mgTarget */
     int guessMode;            /* enum saras_guess                               */
     double jacobiWeight;      /* damping of the Jacobi smoother (1.0 = reference) */
     int seed;

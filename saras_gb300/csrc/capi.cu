@@ -18,8 +18,23 @@ static thread_local std::string g_err;
 void set_error(const std::string &msg) { g_err = msg; }
 
 // ------------------------------------------------------------------ profiler
+// While a V-cycle is being captured as a CUDA graph the events are recorded as
+// external event-record nodes of the graph (cudaEventRecordExternal), and
+// prof_graph_replay gives those nodes fresh events at every replay, so the
+// slots keep timing their kernels inside replayed graphs.
+static void prof_capture_event(Ctx &c, int k, bool end, double bytes) {
+    ProfNode n;
+    cudaEventCreate(&n.captured);
+    cudaEventRecordWithFlags(n.captured, c.stream, cudaEventRecordExternal);
+    n.slot = k;
+    n.end = end;
+    n.bytes = bytes;
+    c.profCaptured.push_back(n);
+}
+
 void prof_begin(Ctx &c, int k, int level) {
     if (level != 0 || k < 0 || k >= PK_COUNT || !c.prof[k].enabled) return;
+    if (c.profCapturing) { prof_capture_event(c, k, false, 0.0); return; }
     cudaEvent_t e;
     cudaEventCreate(&e);
     cudaEventRecord(e, c.stream);
@@ -43,6 +58,7 @@ static void prof_drain(Ctx &c, int k) {
 
 void prof_end(Ctx &c, int k, int level, double bytes) {
     if (level != 0 || k < 0 || k >= PK_COUNT || !c.prof[k].enabled) return;
+    if (c.profCapturing) { prof_capture_event(c, k, true, bytes); return; }
     cudaEvent_t e;
     cudaEventCreate(&e);
     cudaEventRecord(e, c.stream);
@@ -52,10 +68,27 @@ void prof_end(Ctx &c, int k, int level, double bytes) {
     if (c.prof[k].ev.size() >= 8192) prof_drain(c, k);
 }
 
+int prof_graph_replay(Ctx &c, cudaGraphExec_t ge, const std::vector<ProfNode> &nodes) {
+    for (const ProfNode &n : nodes) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return SARAS_CUDA_ERROR;
+        if (cudaGraphExecEventRecordNodeSetEvent(ge, n.node, e) != cudaSuccess) {
+            cudaEventDestroy(e);
+            return SARAS_CUDA_ERROR;
+        }
+        ProfSlot &s = c.prof[n.slot];
+        s.ev.push_back(e);
+        if (n.end) { s.launches += 1; s.bytes += n.bytes; }
+    }
+    for (int k = 0; k < PK_COUNT; ++k)
+        if (c.prof[k].ev.size() >= 8192) prof_drain(c, k);
+    return SARAS_OK;
+}
+
 static const char *kProfNames[PK_COUNT] = {
     "mg_smooth_fp64", "mg_smooth_fp32", "mg_residual_fp64", "mg_residual_fp32", "mg_restrict_fp64", "mg_restrict_fp32",
     "mg_prolong_fp64", "mg_prolong_fp32", "refine_residual_fp64", "refine_update_fp64", "nse_rhs", "cn_jacobi",
-    "projection", "divergence", "conv3d_fwd_tcgen05", "conv3d_bwd_tcgen05"};
+    "projection", "divergence", "conv3d_fwd_tcgen05", "conv3d_bwd_tcgen05", "initial_guess"};
 
 // ------------------------------------------------------------------ yaml
 static std::string trim(const std::string &s) {

@@ -25,6 +25,7 @@ enum ProfKernel : int {
     PK_DIVERGENCE,
     PK_CONV_FWD,          // U-Net implicit-GEMM convolution (tcgen05)
     PK_CONV_BWD,
+    PK_GUESS,             // initial guess of a target-mode solve: histories, restrictions, network, guess
     PK_COUNT
 };
 
@@ -34,6 +35,16 @@ struct ProfSlot {
     long long launches = 0;
     double bytes = 0.0;
     double ms = 0.0;
+};
+
+// A profiling event recorded while a V-cycle was captured as a CUDA graph: an
+// event-record node of the graph, which every replay points at a fresh event.
+struct ProfNode {
+    cudaEvent_t captured = nullptr;   // the event recorded at capture time
+    cudaGraphNode_t node = nullptr;
+    int slot = 0;
+    bool end = false;                 // stop event (closes one launch of the slot)
+    double bytes = 0.0;
 };
 
 // One multigrid level in both precisions.
@@ -89,9 +100,6 @@ struct Ctx {
     int mgMaxCycles = 200;
     int maxCount = 0;
     double *wallX = nullptr, *wallY = nullptr, *wallZ = nullptr;   // Dirichlet check walls
-    double *coarseInv = nullptr;   // dense coarse-level inverse (target modes)
-    float *coarseInv32 = nullptr;
-    int coarseN = 0;
     // reductions
     double *red = nullptr;          // partial sums (device)
     int redCap = 0;
@@ -111,8 +119,16 @@ struct Ctx {
     long cnpCount = 0;
     int n0Fresh[4] = {0, 0, 0, 0};   // N0 of component q written by this step's right-hand side
     int tailLt = -1;          // first level of the fused coarse V-cycle tail (target modes), or -1
+    double rhoMixed = 0.1;    // measured residual contraction per FP32 V-cycle (mixed mode, mixedCycles = 0)
+    int coarseN = 0;          // coarsest core points solved by coarseM (0: Gauss-Seidel instead)
+    double *coarseM64 = nullptr;   // coarsest-level solution operator (coarseN x coarseN, row-major)
+    float *coarseM32 = nullptr;
     // target-mode V-cycles replayed as CUDA graphs: [FP32?][zero start?]
     cudaGraphExec_t vgraph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    cudaGraph_t vgraphSrc[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};   // kept for the event-node handles
+    std::vector<ProfNode> vgraphProf[2][2];   // profiling event nodes of each graph, in capture order
+    bool profCapturing = false;               // prof_begin / prof_end record graph event nodes
+    std::vector<ProfNode> profCaptured;
     long long vgraphLaunches[2][2] = {{0, 0}, {0, 0}};
     std::vector<int> vgraphState[2][2];
     int histCount = 0;
@@ -171,6 +187,7 @@ int unet_infer(Ctx &c, double *out);
 int unet_begin_solve(Ctx &c);
 int unet_guess(Ctx &c, const double *b, double *dst, int mode);
 void vgraph_reset(Ctx &c);
+int prof_graph_replay(Ctx &c, cudaGraphExec_t ge, const std::vector<ProfNode> &nodes);
 int unet_pick(Ctx &c);
 void unet_record(Ctx &c, int built, int cycles);
 int unet_collect_sample(Ctx &c, const double *b);

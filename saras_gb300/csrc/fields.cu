@@ -362,85 +362,118 @@ struct RhsDf {
     fpair fb2, dt;
 };
 
-// One thread per (j, k) column of the component's core box marching kRhsMarch
-// points along i: the split values of F(i-1), F(i), F(i+1), of P along i (Vx)
-// and the in-plane pair sums of the velocity slices that step in i (the
-// Slices patterns with an i offset) are carried from point to point, so each
-// of those values is split once per column instead of at every stencil use.
-constexpr int kRhsMarch = 8;
+// All three components in one pass.  A stencil of one component reads about
+// a dozen values of the four fields, and splitting each read into a float pair
+// would cost about 35 splits a point over the three components.  Here a CTA
+// owns a 32 (k) x 8 (j) tile of columns and marches kRhs3March planes along i;
+// each plane of Vx, Vy, Vz and P on the tile plus a one-point halo is read
+// once, split once and kept in shared memory (four rolling planes, so one
+// barrier a plane), from where the three components' stencils read it.
+// Indices are logical (each field keeps its own core counts and strides); a
+// component is evaluated where (i, j, k) is in its core.  The terms and their
+// order per component follow k_rhs_fast.
+constexpr int kRhs3March = 16;
+constexpr int kR3K = 34, kR3N = 10 * kR3K;   // tile (8 x 32) + halo, per field and plane
+
+struct Rhs3Args {
+    const double *f[4];        // Vx, Vy, Vz, P
+    int n[4][3];               // their core counts
+    long sx[4], sy[4];         // and strides
+    const double *T;           // buoyancy: T, in P's layout
+    double *H[3];              // component layouts
+    float *n0h[3], *n0l[3];
+    int nu[3];                 // union of the cores
+    int buoyancy;
+    RhsDf q[3];
+    CnDf cf[3];
+};
 
 template <int C>
-__global__ void __launch_bounds__(256) k_rhs_df(RhsArgs a, RhsDf q, CnDf cf, float *n0h, float *n0l) {
-    int k = a.b.lo[2] + blockIdx.x * 32 + threadIdx.x;
-    int j = a.b.lo[1] + blockIdx.y * 8 + threadIdx.y;
-    int i0 = a.b.lo[0] + blockIdx.z * kRhsMarch;
-    if (k >= a.b.lo[2] + a.b.ext[2] || j >= a.b.lo[1] + a.b.ext[1]) return;
-    int iend = min(i0 + kRhsMarch, a.b.lo[0] + a.b.ext[0]);
-    const View3<const double> &F = a.F;
-    const View3<const double> &V0 = a.V.v[0], &V1 = a.V.v[1], &V2 = a.V.v[2];
-    fpair wx = fp_of(F(i0 - 1, j, k)), c = fp_of(F(i0, j, k));
-    // carried slice halves: C = 0: Y(i) = V1(i,j) + V1(i,j-1), Z(i) = V2(i,k) + V2(i,k-1) (slice = half(i) + half(i+1));
-    // C = 1 / 2: W(i) = V0(i,j) + V0(i,j+1) / V0(i,k) + V0(i,k+1) (slice = W(i) + W(i-1))
-    fpair ya, za, wa, pa;
+__device__ __forceinline__ void rhs3_point(const Rhs3Args &a, const float2 (*sm)[4][kR3N], int i, int j, int k, int c0) {
+    if (i >= a.n[C][0] || j >= a.n[C][1] || k >= a.n[C][2]) return;
+    auto G = [&](int f, int di, int dj, int dk) -> fpair {
+        float2 v = sm[(i + di) & 3][f][c0 + dj * kR3K + dk];
+        return fpair{v.x, v.y};
+    };
+    const long o = (long)(i + 1) * a.sx[C] + (long)(j + 1) * a.sy[C] + (k + 1);
+    const RhsDf &q = a.q[C];
+    fpair c = G(C, 0, 0, 0), ex = G(C, 1, 0, 0), wx = G(C, -1, 0, 0);
+    fpair ey = G(C, 0, 1, 0), wy = G(C, 0, -1, 0), ez = G(C, 0, 0, 1), wz = G(C, 0, 0, -1);
+    fpair c2 = fpair{-2.0f * c.h, -2.0f * c.l};
+    fpair Sx = fp_add(fp_add(ex, wx), c2), Sy = fp_add(fp_add(ey, wy), c2), Sz = fp_add(fp_add(ez, wz), c2);
+    fpair h = fp_add(fp_add(fp_mul(q.k2[0], Sx), fp_mul(q.k2[1], Sy)), fp_mul(q.k2[2], Sz));
+    fpair s0, s1, s2, dp;
     if (C == 0) {
-        ya = fp_add(fp_of(V1(i0, j, k)), fp_of(V1(i0, j - 1, k)));
-        za = fp_add(fp_of(V2(i0, j, k)), fp_of(V2(i0, j, k - 1)));
-        pa = fp_of(a.P(i0, j, k));
+        s0 = c;
+        s1 = fp_add(fp_add(G(1, 0, 0, 0), G(1, 0, -1, 0)), fp_add(G(1, 1, 0, 0), G(1, 1, -1, 0)));
+        s2 = fp_add(fp_add(G(2, 0, 0, 0), G(2, 0, 0, -1)), fp_add(G(2, 1, 0, 0), G(2, 1, 0, -1)));
+        dp = fp_add(G(3, 1, 0, 0), fp_neg(G(3, 0, 0, 0)));
     } else if (C == 1) {
-        wa = fp_add(fp_of(V0(i0 - 1, j, k)), fp_of(V0(i0 - 1, j + 1, k)));
+        s0 = fp_add(fp_add(G(0, 0, 0, 0), G(0, 0, 1, 0)), fp_add(G(0, -1, 0, 0), G(0, -1, 1, 0)));
+        s1 = c;
+        s2 = fp_add(fp_add(G(2, 0, 0, 0), G(2, 0, 0, -1)), fp_add(G(2, 0, 1, 0), G(2, 0, 1, -1)));
+        dp = fp_add(G(3, 0, 1, 0), fp_neg(G(3, 0, 0, 0)));
     } else {
-        wa = fp_add(fp_of(V0(i0 - 1, j, k)), fp_of(V0(i0 - 1, j, k + 1)));
+        s0 = fp_add(fp_add(G(0, 0, 0, 0), G(0, 0, 0, 1)), fp_add(G(0, -1, 0, 0), G(0, -1, 0, 1)));
+        s1 = fp_add(fp_add(G(1, 0, 0, 0), G(1, 0, -1, 0)), fp_add(G(1, 0, 0, 1), G(1, 0, -1, 1)));
+        s2 = c;
+        dp = fp_add(G(3, 0, 0, 1), fp_neg(G(3, 0, 0, 0)));
     }
-    for (int i = i0; i < iend; ++i) {
-        double f0 = F(i, j, k);
-        fpair c2 = fpair{-2.0f * c.h, -2.0f * c.l};
-        fpair ex = fp_of(F(i + 1, j, k));
-        fpair ey = fp_of(F(i, j + 1, k)), wy = fp_of(F(i, j - 1, k));
-        fpair ez = fp_of(F(i, j, k + 1)), wz = fp_of(F(i, j, k - 1));
-        fpair Sx = fp_add(fp_add(ex, wx), c2), Sy = fp_add(fp_add(ey, wy), c2), Sz = fp_add(fp_add(ez, wz), c2);
-        fpair h = fp_add(fp_add(fp_mul(q.k2[0], Sx), fp_mul(q.k2[1], Sy)), fp_mul(q.k2[2], Sz));
-        fpair s0, s1, s2, dp;
-        if (C == 0) {
-            s0 = c;   // Slices<0,0>: Vx itself
-            fpair yb = fp_add(fp_of(V1(i + 1, j, k)), fp_of(V1(i + 1, j - 1, k)));
-            fpair zb = fp_add(fp_of(V2(i + 1, j, k)), fp_of(V2(i + 1, j, k - 1)));
-            s1 = fp_add(ya, yb);
-            s2 = fp_add(za, zb);
-            ya = yb;
-            za = zb;
-            fpair pb = fp_of(a.P(i + 1, j, k));
-            dp = fp_add(pb, fp_neg(pa));
-            pa = pb;
-        } else if (C == 1) {
-            fpair wb = fp_add(fp_of(V0(i, j, k)), fp_of(V0(i, j + 1, k)));
-            s0 = fp_add(wb, wa);
-            wa = wb;
-            s1 = c;   // Slices<1,1>: Vy itself
-            s2 = Slices<1, 2>::sump(V2, i, j, k);
-            dp = fp_add(fp_of(a.P(i, j + 1, k)), fp_neg(fp_of(a.P(i, j, k))));
-        } else {
-            fpair wb = fp_add(fp_of(V0(i, j, k)), fp_of(V0(i, j, k + 1)));
-            s0 = fp_add(wb, wa);
-            wa = wb;
-            s1 = Slices<2, 1>::sump(V1, i, j, k);
-            s2 = c;   // Slices<2,2>: Vz itself
-            dp = fp_add(fp_of(a.P(i, j, k + 1)), fp_neg(fp_of(a.P(i, j, k))));
+    h = fp_add(h, fp_neg(fp_mul(s0, fp_mul(fp_add(ex, fp_neg(wx)), q.k1n[0]))));
+    h = fp_add(h, fp_neg(fp_mul(s1, fp_mul(fp_add(ey, fp_neg(wy)), q.k1n[1]))));
+    h = fp_add(h, fp_neg(fp_mul(s2, fp_mul(fp_add(ez, fp_neg(wz)), q.k1n[2]))));
+    if (C == 2 && a.buoyancy) {
+        long ot = (long)(i + 1) * a.sx[3] + (long)(j + 1) * a.sy[3] + (k + 1);
+        h = fp_add(h, fp_mul(q.fb2, fp_add(fp_of(a.T[ot]), fp_of(a.T[ot + 1]))));
+    }
+    h = fp_add(h, fp_neg(fp_mul(q.g[C], dp)));
+    h = fp_mul(h, q.dt);
+    a.H[C][o] = (a.f[C][o] + f2d(h.h)) + f2d(h.l);
+    const CnDf &cf = a.cf[C];
+    fpair n0 = fp_add(h, fp_add(fp_add(fp_mul(cf.kc[0], Sx), fp_mul(cf.kc[1], Sy)), fp_mul(cf.kc[2], Sz)));
+    a.n0h[C][o] = n0.h;
+    a.n0l[C][o] = n0.l;
+}
+
+__global__ void __launch_bounds__(256) k_rhs_df3(Rhs3Args a) {
+    __shared__ float2 sm[4][4][kR3N];
+    const int tid = threadIdx.y * 32 + threadIdx.x;
+    const int k0 = blockIdx.x * 32, j0 = blockIdx.y * 8, i0 = blockIdx.z * kRhs3March;
+    const int iend = min(i0 + kRhs3March, a.nu[0]);
+    int js[2], ks[2];
+    bool lt[2];
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        int t = tid + 256 * s;
+        int jj = t / kR3K;
+        js[s] = j0 - 1 + jj;
+        ks[s] = k0 - 1 + (t - jj * kR3K);
+        lt[s] = t < kR3N;
+    }
+    auto load_plane = [&](int ip) {
+        float2(*slot)[kR3N] = sm[ip & 3];
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+            if (!lt[s]) continue;
+            int t = tid + 256 * s, j = js[s], k = ks[s];
+#pragma unroll
+            for (int f = 0; f < 4; ++f) {
+                if (ip > a.n[f][0] || j > a.n[f][1] || k > a.n[f][2]) continue;   // outside the padded field
+                fpair x = fp_of(a.f[f][(long)(ip + 1) * a.sx[f] + (long)(j + 1) * a.sy[f] + (k + 1)]);
+                slot[f][t] = make_float2(x.h, x.l);
+            }
         }
-        h = fp_add(h, fp_neg(fp_mul(s0, fp_mul(fp_add(ex, fp_neg(wx)), q.k1n[0]))));
-        h = fp_add(h, fp_neg(fp_mul(s1, fp_mul(fp_add(ey, fp_neg(wy)), q.k1n[1]))));
-        h = fp_add(h, fp_neg(fp_mul(s2, fp_mul(fp_add(ez, fp_neg(wz)), q.k1n[2]))));
-        if (C == 2 && a.buoyancy) h = fp_add(h, fp_mul(q.fb2, fp_add(fp_of(a.T(i, j, k)), fp_of(a.T(i, j, k + 1)))));
-        h = fp_add(h, fp_neg(fp_mul(q.g[C], dp)));
-        h = fp_mul(h, q.dt);
-        a.H(i, j, k) = (f0 + f2d(h.h)) + f2d(h.l);
-        // N0 = H - F + k1 sum_d c_d S_d(F) of the Jacobi solve that follows (k_cn_pack's
-        // quantity, from the same split values)
-        fpair n0 = fp_add(h, fp_add(fp_add(fp_mul(cf.kc[0], Sx), fp_mul(cf.kc[1], Sy)), fp_mul(cf.kc[2], Sz)));
-        long o = F.off(i, j, k);
-        n0h[o] = n0.h;
-        n0l[o] = n0.l;
-        wx = c;
-        c = ex;
+    };
+    load_plane(i0 - 1);
+    load_plane(i0);
+    const int j = j0 + threadIdx.y, k = k0 + threadIdx.x;
+    const int c0 = (threadIdx.y + 1) * kR3K + (threadIdx.x + 1);
+    for (int i = i0; i < iend; ++i) {
+        load_plane(i + 1);
+        __syncthreads();
+        rhs3_point<0>(a, sm, i, j, k, c0);
+        rhs3_point<1>(a, sm, i, j, k, c0);
+        rhs3_point<2>(a, sm, i, j, k, c0);
     }
 }
 
@@ -749,9 +782,10 @@ __global__ void k_cn_delta_shell(CnDelta a) {
     if (s & 1) lo[d] = a.prog.bhi[d] + 1;
     else hi[d] = a.prog.blo[d] - 1;
     if (lo[0] > hi[0] || lo[1] > hi[1] || lo[2] > hi[2]) return;
-    long n1 = hi[1] - lo[1] + 1, n2 = hi[2] - lo[2] + 1, n = (long)(hi[0] - lo[0] + 1) * n1 * n2;
-    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
-        int k = lo[2] + (int)(t % n2), j = lo[1] + (int)((t / n2) % n1), i = lo[0] + (int)(t / (n1 * n2));
+    // 32-bit index arithmetic: a slab holds fewer than 2^31 points
+    const int n1 = hi[1] - lo[1] + 1, n2 = hi[2] - lo[2] + 1, n = (hi[0] - lo[0] + 1) * n1 * n2;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        int r = t / n2, k = lo[2] + (t - r * n2), q = r / n1, j = lo[1] + (r - q * n1), i = lo[0] + q;
         long o = a.off(i, j, k);
         fpair out = cn_delta_boundary(a, i, j, k, o);
         a.oh[o] = out.h;
@@ -835,9 +869,10 @@ __global__ void k_project_shell(View3<double> out, View3<const double> in, View3
         }
         return v;
     };
-    long n1 = hi[1] - lo[1] + 1, n2 = hi[2] - lo[2] + 1, n = (long)(hi[0] - lo[0] + 1) * n1 * n2;
-    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
-        int k = lo[2] + (int)(t % n2), j = lo[1] + (int)((t / n2) % n1), i = lo[0] + (int)(t / (n1 * n2));
+    // 32-bit index arithmetic: a slab holds fewer than 2^31 points
+    const int n1 = hi[1] - lo[1] + 1, n2 = hi[2] - lo[2] + 1, n = (hi[0] - lo[0] + 1) * n1 * n2;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        int r = t / n2, k = lo[2] + (t - r * n2), q = r / n1, j = lo[1] + (r - q * n1), i = lo[0] + q;
         bool targeted = false;
         for (int o = 0; o < prog.nops; ++o) if (in_box(prog.op[o].lo, prog.op[o].hi, i, j, k)) { targeted = true; break; }
         out(i, j, k) = targeted ? bc_resolve(prog, i, j, k, base) : base(i, j, k);
@@ -1294,6 +1329,7 @@ int compute_rhs(Ctx &c) {
     prof_begin(c, PK_RHS, 0);
     RhsFast qf = make_rhs_fast(c, a.visc);
     bool fast = c.p.fastKernels != 0;
+    Rhs3Args a3;   // fastKernels = 2: one k_rhs_df3 launch for the three components
     for (int q = 0; q < 3; ++q) {
         a.H = mview(c, SARAS_FIELD_NSE_X + q);
         a.F = cview(c, SARAS_FIELD_VX + q);
@@ -1316,11 +1352,31 @@ int compute_rhs(Ctx &c) {
             int e = cnp_ensure(c);
             if (e) return e;
             float *n0h = c.cnp + (size_t)2 * q * c.cnpCount, *n0l = n0h + c.cnpCount;
-            dim3 gr((a.b.ext[2] + 31) / 32, (a.b.ext[1] + 7) / 8, (a.b.ext[0] + kRhsMarch - 1) / kRhsMarch), br(32, 8, 1);
-            if (q == 0) k_rhs_df<0><<<gr, br, 0, c.stream>>>(a, qd, cf, n0h, n0l);
-            if (q == 1) k_rhs_df<1><<<gr, br, 0, c.stream>>>(a, qd, cf, n0h, n0l);
-            if (q == 2) k_rhs_df<2><<<gr, br, 0, c.stream>>>(a, qd, cf, n0h, n0l);
             c.n0Fresh[q] = 1;
+            {
+                a3.f[q] = a.F.p;
+                a3.H[q] = a.H.p;
+                a3.n0h[q] = n0h;
+                a3.n0l[q] = n0l;
+                a3.q[q] = qd;
+                a3.cf[q] = cf;
+                bytes += 8.0 * (double)a.H.size();
+                if (q < 2) continue;
+                a3.f[3] = a.P.p;
+                a3.T = a.T.p;
+                for (int f = 0; f < 4; ++f) {
+                    const View3<const double> &v = f < 3 ? a.V.v[f] : a.P;
+                    for (int d = 0; d < 3; ++d) a3.n[f][d] = v.n[d];
+                    a3.sx[f] = v.sx;
+                    a3.sy[f] = v.sy;
+                }
+                for (int d = 0; d < 3; ++d) a3.nu[d] = std::max(std::max(a3.n[0][d], a3.n[1][d]), std::max(a3.n[2][d], a3.n[3][d]));
+                a3.buoyancy = a.buoyancy;
+                dim3 gr((a3.nu[2] + 31) / 32, (a3.nu[1] + 7) / 8, (a3.nu[0] + kRhs3March - 1) / kRhs3March);
+                k_rhs_df3<<<gr, dim3(32, 8, 1), 0, c.stream>>>(a3);
+                count_launch(c);
+                break;
+            }
         } else if (fast) {
             if (q == 0) k_rhs_fast<0><<<g, bl, 0, c.stream>>>(a, qf);
             if (q == 1) k_rhs_fast<1><<<g, bl, 0, c.stream>>>(a, qf);
@@ -1333,7 +1389,9 @@ int compute_rhs(Ctx &c) {
         count_launch(c);
         bytes += 8.0 * (double)a.H.size();
     }
-    prof_end(c, PK_RHS, 0, bytes * (a.buoyancy ? 6.0 : 5.0));
+    // algorithmic bytes per point and component: F, two other velocity
+    // components, P (+ T) in, H out (+ N0 as a float pair with fastKernels = 2)
+    prof_end(c, PK_RHS, 0, bytes * ((a.buoyancy ? 6.0 : 5.0) + (c.p.fastKernels == 2 ? 1.0 : 0.0)));
     return check_launch(c, "rhs");
 }
 

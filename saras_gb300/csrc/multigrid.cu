@@ -650,6 +650,22 @@ static TgK<T> make_tgk(const Level &L, double omega) {
     return k;
 }
 
+// Face-ghost images of core point (i, j, k) in the target modes (put_scatter
+// without the Dirichlet cases: mirror 1 -> -1, E-1 -> E+1; periodic E-1 -> -1,
+// 1 -> E+1), inline: no device call in the caller.
+template <typename T>
+__device__ __forceinline__ void tgt_images(T *P, int sx, int sy, int i, int j, int k, T v, const MgBC &bc) {
+    const long o = (long)(i + 1) * sx + (long)(j + 1) * sy + (k + 1);
+    const int q[3] = {i, j, k};
+    const long st[3] = {sx, sy, 1};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        int E = bc.E[d];
+        if (q[d] == 1) P[o + (long)((bc.per[d] ? E + 1 : -1) - 1) * st[d]] = v;
+        if (q[d] == E - 1) P[o + (long)((bc.per[d] ? -1 : E + 1) - (E - 1)) * st[d]] = v;
+    }
+}
+
 template <typename T>
 __device__ __noinline__ void scatter_slow(T *P, int sx, int sy, int i, int j, int k, T v, const MgBC &bc) {
     View3<T> V; V.p = P; V.sx = sx; V.sy = sy;
@@ -728,30 +744,37 @@ __global__ void __launch_bounds__(256) k_tgt_sweep(T *__restrict__ out, const T 
         if (edge_jk || i0 <= 1 || i0 + n - 1 >= bc.E[0] - 1) {
             for (int q = 0; q < n; ++q) {
                 int i = i0 + q;
-                if (edge_jk || i <= 1 || i >= bc.E[0] - 1) scatter_slow(out, sx, sy, i, j, k, out[o0 + q * sx], bc);
+                if (edge_jk || i <= 1 || i >= bc.E[0] - 1) tgt_images(out, sx, sy, i, j, k, out[o0 + q * sx], bc);
             }
         }
     }
 }
 
-// Face-ghost images (put_scatter) of the boundary points of a level array,
-// after a sweep that wrote the core only.  The points that have images are
-// those with a coordinate 1 or E-1 on some axis (periodic: E-1 -> -1, 1 -> E+1;
-// mirror: 1 -> -1, E-1 -> E+1): blockIdx.y picks one of those six planes.
+// Face-ghost images of a level array after a kernel that wrote the core only
+// (target modes: mirror 1 -> -1, E-1 -> E+1; periodic E-1 -> -1, 1 -> E+1,
+// as put_scatter).  blockIdx.y picks one of the six ghost faces, which is a
+// copy of the core plane at 1 or E-1 along that axis; a (64 x 4) block walks
+// rows of that plane, k (or j) fastest, with no index divisions.
 template <typename T>
-__global__ void k_tgt_ghosts(T *__restrict__ p, int sx, int sy, MgBC bc) {
-    int plane = blockIdx.y, d = plane >> 1;
-    int v = (plane & 1) ? bc.E[d] - 1 : 1;
-    int a1 = d == 0 ? 1 : 0, a2 = d == 2 ? 1 : 2;   // the other two axes
-    long n = (long)(bc.E[a1] + 1) * (bc.E[a2] + 1);
-    View3<T> V; V.p = p; V.sx = sx; V.sy = sy;
-    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
-        int q[3];
-        q[d] = v;
-        q[a1] = (int)(t / (bc.E[a2] + 1));
-        q[a2] = (int)(t % (bc.E[a2] + 1));
-        put_scatter(V, q[0], q[1], q[2], V(q[0], q[1], q[2]), bc);
-    }
+__global__ void __launch_bounds__(256) k_tgt_ghosts(T *__restrict__ p, int sx, int sy, MgBC bc) {
+    const int d = blockIdx.y >> 1, side = blockIdx.y & 1, E = bc.E[d];
+    const int v = side ? E - 1 : 1;                                        // source plane
+    const int g = bc.per[d] ? (side ? -1 : E + 1) : (side ? E + 1 : -1);   // ghost plane it fills
+    const int a1 = d == 0 ? 1 : 0, a2 = d == 2 ? 1 : 2;                     // the other two axes
+    const long st[3] = {sx, sy, 1};
+    const long base = (long)(v + 1) * st[d], delta = (long)(g - v) * st[d];
+    const int n1 = bc.E[a1] + 1, n2 = bc.E[a2] + 1;
+    for (int r = blockIdx.x * blockDim.y + threadIdx.y; r < n1; r += gridDim.x * blockDim.y)
+        for (int c = threadIdx.x; c < n2; c += blockDim.x) {
+            long o = base + (long)(r + 1) * st[a1] + (long)(c + 1) * st[a2];
+            p[o + delta] = p[o];
+        }
+}
+
+static void tgt_ghosts_dims(const Level &L, dim3 &g, dim3 &b) {
+    b = dim3(64, 4, 1);
+    int rows = std::max(L.n[0], std::max(L.n[1], L.n[2])) + 1;
+    g = dim3((rows + 3) / 4, 6, 1);
 }
 
 // Target-mode prolongation + add (vertex-centred trilinear) on the core; the
@@ -774,6 +797,18 @@ __global__ void __launch_bounds__(256) k_tgt_prolong_add(T *__restrict__ pf, con
         return (T)0.5 * (v0 + v1);
     };
     long o = (long)(i0 + 1) * sxf + (long)(j + 1) * syf + (k + 1);
+    if (iend - i0 + 1 == kIch) {
+        // a full segment: every load issued before the first store (the coarse
+        // plane i0 / 2 + kIch / 2 is at most the coarse core's last plane)
+        T a[kIch / 2 + 1], v[kIch];
+#pragma unroll
+        for (int q = 0; q <= kIch / 2; ++q) a[q] = A((i0 >> 1) + q);
+#pragma unroll
+        for (int q = 0; q < kIch; ++q) v[q] = pf[o + q * (long)sxf];
+#pragma unroll
+        for (int q = 0; q < kIch; ++q) pf[o + q * (long)sxf] = v[q] + ((q & 1) ? (T)0.5 * (a[q >> 1] + a[(q >> 1) + 1]) : a[q >> 1]);
+        return;
+    }
     T am = A(i0 >> 1);
     for (int i = i0; i <= iend; i += 2, o += 2 * (long)sxf) {
         pf[o] += am;
@@ -813,6 +848,53 @@ __global__ void __launch_bounds__(256) k_tgt_residual(OT *__restrict__ out, cons
         }
     }
     if (MAXRED) block_max_bits_to(m, maxres);
+}
+
+// Full-weighting restriction of a target-mode residual (k_mg_restrict's
+// weights (1/64) [1 2 1]^3, summed separably): one thread per coarse (J, K)
+// column marching kRrCh coarse planes along I; each fine plane's in-plane
+// [1 2 1] x [1 2 1] sum is formed once and the odd fine plane between two
+// coarse planes serves both.  Fine positions outside the core are read at
+// their mirror / periodic images (the pads k_mg_restrict resolves).
+constexpr int kRrCh = 8;   // coarse planes per thread
+
+__device__ __forceinline__ int pad_img(int q, int E, int per) {
+    if (q < 0) return per ? E - 1 : 1;
+    if (q > E) return per ? 1 : E - 1;
+    return q;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_tgt_restrict(T *__restrict__ rc, const T *__restrict__ r, int sx, int sy, int csx, int csy,
+                                                       MgBC bcf) {
+    const int K = blockIdx.x * 32 + threadIdx.x, J = blockIdx.y * 8 + threadIdx.y, I0 = blockIdx.z * kRrCh;
+    const int E0 = bcf.E[0], E1 = bcf.E[1], E2 = bcf.E[2];
+    if (K > E2 / 2 || J > E1 / 2) return;
+    long oj[3];
+    int ok[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        oj[a] = (long)(pad_img(2 * J - 1 + a, E1, bcf.per[1]) + 1) * sy;
+        ok[a] = pad_img(2 * K - 1 + a, E2, bcf.per[2]) + 1;
+    }
+    auto plane = [&](int i) -> T {
+        const T *q = r + (long)(pad_img(i, E0, bcf.per[0]) + 1) * sx;
+        T row[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const T *qa = q + oj[a];
+            row[a] = qa[ok[0]] + (T)2 * qa[ok[1]] + qa[ok[2]];
+        }
+        return row[0] + (T)2 * row[1] + row[2];
+    };
+    const int Iend = min(I0 + kRrCh - 1, E0 / 2);
+    T lo = plane(2 * I0 - 1);
+#pragma unroll 2
+    for (int I = I0; I <= Iend; ++I) {
+        T mid = plane(2 * I), hi = plane(2 * I + 1);
+        rc[(long)(I + 1) * csx + (long)(J + 1) * csy + (K + 1)] = (lo + (T)2 * mid + hi) * (T)0.015625;
+        lo = hi;
+    }
 }
 
 // p64 += e32 over the core (FP64 correction accumulation) with face ghosts.
@@ -1101,6 +1183,8 @@ struct TailArgs {
     TgK<T> tk[kTailMaxLevels];       // sweep constants (damped Jacobi)
     TgK<T> tr[kTailMaxLevels];       // residual constants (weight 1)
     MgK kkc;                         // coarsest level (Gauss-Seidel)
+    const T *M;                      // coarsest solution operator (nM x nM), or null: Gauss-Seidel
+    int nM;
     T tol;
     int maxc, pre, post;
     const T *rin;                    // level-Lt right-hand side (padded)
@@ -1111,20 +1195,44 @@ struct TailArgs {
 template <typename T>
 __device__ __forceinline__ int tail_count(const MgBC &b) { return (b.E[0] + 3) * (b.E[1] + 3) * (b.E[2] + 3); }
 
+// The core points (i, j, k) of an (X1 x Y1 x Z1)-point level, k fastest, that
+// thread t visits at t, t + nt, ...: the first point by division, the others
+// by adding the stride nt in mixed radix (one carry per digit at most, since
+// each digit of the stride is below its radix), so the loop body is free of
+// integer divisions.
+template <typename F>
+__device__ __forceinline__ void tail_for(int X1, int Y1, int Z1, F f) {
+    const int nt = blockDim.x, n = X1 * Y1 * Z1, YZ = Y1 * Z1;
+    int t = threadIdx.x;
+    if (t >= n) return;
+    int i = t / YZ, r = t - i * YZ, j = r / Z1, k = r - j * Z1;
+    const int di = nt / YZ, rr = nt - di * YZ, dj = rr / Z1, dk = rr - dj * Z1;
+    for (; t < n; t += nt) {
+        f(i, j, k);
+        k += dk;
+        if (k >= Z1) { k -= Z1; ++j; }
+        j += dj;
+        if (j >= Y1) { j -= Y1; ++i; }
+        i += di;
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ bool near_face(int i, int j, int k, const MgBC &bc) {
+    return i <= 1 || j <= 1 || k <= 1 || i >= bc.E[0] - 1 || j >= bc.E[1] - 1 || k >= bc.E[2] - 1;
+}
+
 template <typename T, bool ZERO>
 __device__ void tail_sweep(T *out, const T *in, const T *r, const MgBC &bc, const TgK<T> &c) {
-    int E1 = bc.E[1], E2 = bc.E[2];
-    int sy = E2 + 3, sx = (E1 + 3) * sy;
-    int n = (bc.E[0] + 1) * (E1 + 1) * (E2 + 1);
-    View3<T> V; V.p = out; V.sx = sx; V.sy = sy;
-    for (int t = threadIdx.x; t < n; t += blockDim.x) {
-        int k = t % (E2 + 1), j = (t / (E2 + 1)) % (E1 + 1), i = t / ((E2 + 1) * (E1 + 1));
+    const int E1 = bc.E[1], E2 = bc.E[2], sy = E2 + 3, sx = (E1 + 3) * sy;
+    tail_for(bc.E[0] + 1, E1 + 1, E2 + 1, [&](int i, int j, int k) {
         int o = (i + 1) * sx + (j + 1) * sy + (k + 1);
         T v;
         if (ZERO) v = c.ar * r[o];
         else v = fma(c.ax, in[o - sx] + in[o + sx], fma(c.ay, in[o + sy] + in[o - sy], fma(c.az, in[o + 1] + in[o - 1], fma(c.ar, r[o], c.om1 * in[o]))));
-        put_scatter(V, i, j, k, v, bc);
-    }
+        out[o] = v;
+        if (near_face<T>(i, j, k, bc)) tgt_images(out, sx, sy, i, j, k, v, bc);
+    });
     __syncthreads();
 }
 
@@ -1153,56 +1261,89 @@ __global__ void __launch_bounds__(kTailThreads) k_mg_tail(TailArgs<T> a) {
             else tail_sweep<T, false>(Q[l], P[l], R[l], bc, a.tk[l]);
             T *x = P[l]; P[l] = Q[l]; Q[l] = x;
         }
-        // residual into Q (core), then full-weighting restriction (pads resolved by index)
-        int n = (bc.E[0] + 1) * (E1 + 1) * (E2 + 1);
+        // residual into Q (core), then full-weighting restriction (k_tgt_restrict's
+        // separable form; fine positions outside the core at their images)
         const TgK<T> &c = a.tr[l];
-        for (int t = tid; t < n; t += nt) {
-            int k = t % (E2 + 1), j = (t / (E2 + 1)) % (E1 + 1), i = t / ((E2 + 1) * (E1 + 1));
-            int o = (i + 1) * sx + (j + 1) * sy + (k + 1);
-            const T *p = P[l];
-            T lap = fma(c.lx, p[o - sx] + p[o + sx], fma(c.ly, p[o + sy] + p[o - sy], fma(c.lz, p[o + 1] + p[o - 1], c.lc * p[o])));
-            Q[l][o] = R[l][o] - lap;
+        {
+            const T *p = P[l], *rr = R[l];
+            T *qq = Q[l];
+            tail_for(bc.E[0] + 1, E1 + 1, E2 + 1, [&](int i, int j, int k) {
+                int o = (i + 1) * sx + (j + 1) * sy + (k + 1);
+                T lap = fma(c.lx, p[o - sx] + p[o + sx], fma(c.ly, p[o + sy] + p[o - sy], fma(c.lz, p[o + 1] + p[o - 1], c.lc * p[o])));
+                qq[o] = rr[o] - lap;
+            });
         }
         __syncthreads();
         const MgBC &bcc = a.bc[l + 1];
         int C1 = bcc.E[1], C2 = bcc.E[2], csy = C2 + 3, csx = (C1 + 3) * csy;
-        int nc = (bcc.E[0] + 1) * (C1 + 1) * (C2 + 1);
-        View3<const T> tv; tv.p = Q[l]; tv.sx = sx; tv.sy = sy;
-        for (int t = tid; t < nc; t += nt) {
-            int k = t % (C2 + 1), j = (t / (C2 + 1)) % (C1 + 1), i = t / ((C2 + 1) * (C1 + 1));
-            int i2 = 2 * i, j2 = 2 * j, k2 = 2 * k;
-            bool interior = i2 > 0 && j2 > 0 && k2 > 0 && i2 < bc.E[0] && j2 < bc.E[1] && k2 < bc.E[2];
-            auto T_ = [&](int x, int y, int z) -> T { return interior ? tv(x, y, z) : pad_val(tv, x, y, z, bc); };
-            T facePoints = (T_(i2 + 1, j2, k2) + T_(i2 - 1, j2, k2) + T_(i2, j2 + 1, k2) + T_(i2, j2 - 1, k2) +
-                            T_(i2, j2, k2 + 1) + T_(i2, j2, k2 - 1)) * (T)0.0625;
-            T edgePoints = (T_(i2 + 1, j2 + 1, k2) + T_(i2 + 1, j2 - 1, k2) + T_(i2 - 1, j2 - 1, k2) + T_(i2 - 1, j2 + 1, k2) +
-                            T_(i2, j2 + 1, k2 + 1) + T_(i2, j2 - 1, k2 + 1) + T_(i2, j2 - 1, k2 - 1) + T_(i2, j2 + 1, k2 - 1) +
-                            T_(i2 + 1, j2, k2 + 1) + T_(i2 + 1, j2, k2 - 1) + T_(i2 - 1, j2, k2 - 1) + T_(i2 - 1, j2, k2 + 1)) * (T)0.03125;
-            T vertPoints = (T_(i2 + 1, j2 + 1, k2 + 1) + T_(i2 + 1, j2 + 1, k2 - 1) + T_(i2 + 1, j2 - 1, k2 + 1) +
-                            T_(i2 - 1, j2 + 1, k2 + 1) + T_(i2 + 1, j2 - 1, k2 - 1) + T_(i2 - 1, j2 + 1, k2 - 1) +
-                            T_(i2 - 1, j2 - 1, k2 + 1) + T_(i2 - 1, j2 - 1, k2 - 1)) * (T)0.015625;
-            R[l + 1][(i + 1) * csx + (j + 1) * csy + (k + 1)] = facePoints + edgePoints + vertPoints + tv(i2, j2, k2) * (T)0.125;
+        {
+            const T *qf = Q[l];
+            T *rc = R[l + 1];
+            tail_for(bcc.E[0] + 1, C1 + 1, C2 + 1, [&](int I, int J, int K) {
+                int oj[3], ok[3];
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    oj[q] = (pad_img(2 * J - 1 + q, E1, bc.per[1]) + 1) * sy;
+                    ok[q] = pad_img(2 * K - 1 + q, E2, bc.per[2]) + 1;
+                }
+                T acc = (T)0;
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    const T *pl = qf + (pad_img(2 * I - 1 + q, bc.E[0], bc.per[0]) + 1) * sx;
+                    T row[3];
+#pragma unroll
+                    for (int w = 0; w < 3; ++w) {
+                        const T *pr = pl + oj[w];
+                        row[w] = pr[ok[0]] + (T)2 * pr[ok[1]] + pr[ok[2]];
+                    }
+                    T sp = row[0] + (T)2 * row[1] + row[2];
+                    acc += q == 1 ? (T)2 * sp : sp;
+                }
+                rc[(I + 1) * csx + (J + 1) * csy + (K + 1)] = acc * (T)0.015625;
+            });
         }
         __syncthreads();
     }
-    // coarsest level
+    // coarsest level: e = M r with the precomputed solution operator (one warp
+    // per row, the core right-hand side gathered into a compact vector first),
+    // else Gauss-Seidel to tol
     {
         int L = a.nl - 1;
         const MgBC &bc = a.bc[L];
         for (int t = tid; t < tail_count<T>(bc); t += nt) P[L][t] = (T)0;
-        __syncthreads();
-        if (tid < 32) coarse_rbgs_warp(P[L], R[L], bc.E[0], bc.E[1], bc.E[2], a.kkc, bc, a.tol, a.maxc, a.iters);
-        __syncthreads();
+        if (a.M) {
+            int Y = bc.E[1], Z = bc.E[2], sy = Z + 3, sx = (Y + 3) * sy;
+            T *rv = Q[L];
+            const T *rl = R[L];
+            tail_for(bc.E[0] + 1, Y + 1, Z + 1, [&](int i, int j, int k) {
+                rv[(i * (Y + 1) + j) * (Z + 1) + k] = rl[(i + 1) * sx + (j + 1) * sy + (k + 1)];
+            });
+            __syncthreads();
+            int lane = tid & 31;
+            for (int row = tid >> 5; row < a.nM; row += nt >> 5) {
+                const T *m = a.M + (long)row * a.nM;
+                T s = (T)0;
+                for (int q = lane; q < a.nM; q += 32) s = fma(m[q], rv[q], s);
+                s = warp_sum(s);
+                if (lane == 0) {
+                    int k = row % (Z + 1), j = (row / (Z + 1)) % (Y + 1), i = row / ((Z + 1) * (Y + 1));
+                    P[L][(i + 1) * sx + (j + 1) * sy + (k + 1)] = s;
+                }
+            }
+            __syncthreads();
+        } else {
+            __syncthreads();
+            if (tid < 32) coarse_rbgs_warp(P[L], R[L], bc.E[0], bc.E[1], bc.E[2], a.kkc, bc, a.tol, a.maxc, a.iters);
+            __syncthreads();
+        }
     }
     // back up: prolongation + add, post-smoothing
     for (int l = a.nl - 2; l >= 0; --l) {
         const MgBC &bc = a.bc[l], &bcc = a.bc[l + 1];
         int E1 = bc.E[1], E2 = bc.E[2], sy = E2 + 3, sx = (E1 + 3) * sy;
-        int n = (bc.E[0] + 1) * (E1 + 1) * (E2 + 1);
-        View3<T> pf; pf.p = P[l]; pf.sx = sx; pf.sy = sy;
+        T *pf = P[l];
         View3<const T> C; C.p = P[l + 1]; C.sy = bcc.E[2] + 3; C.sx = (bcc.E[1] + 3) * C.sy;
-        for (int t = tid; t < n; t += nt) {
-            int k = t % (E2 + 1), j = (t / (E2 + 1)) % (E1 + 1), i = t / ((E2 + 1) * (E1 + 1));
+        tail_for(bc.E[0] + 1, E1 + 1, E2 + 1, [&](int i, int j, int k) {
             int i2 = i / 2, j2 = j / 2, k2 = k / 2;
             bool io = i & 1, jo = j & 1, ko = k & 1;
             T v;
@@ -1224,8 +1365,11 @@ __global__ void __launch_bounds__(kTailThreads) k_mg_tail(TailArgs<T> a) {
                     else v = C(i2, j2, k2);
                 }
             }
-            put_scatter(pf, i, j, k, v + pf(i, j, k), bc);
-        }
+            int o = (i + 1) * sx + (j + 1) * sy + (k + 1);
+            v = v + pf[o];
+            pf[o] = v;
+            if (near_face<T>(i, j, k, bc)) tgt_images(pf, sx, sy, i, j, k, v, bc);
+        });
         __syncthreads();
         for (int m = 0; m < a.post; ++m) {
             tail_sweep<T, false>(Q[l], P[l], R[l], bc, a.tk[l]);
@@ -1281,6 +1425,63 @@ static int tail_level(const Ctx &c) {
     return -1;
 }
 
+// Solution operator of the coarsest level of the fused tail.  The target-mode
+// coarsest problem A e = r (the level Laplacian with mirror / periodic ghosts)
+// is singular: A 1 = 0 and w^T A = 0 for the trapezoidal weights w.  M is the
+// top-left n x n block of the inverse of the bordered matrix [[A, 1], [w^T, 0]],
+// so e = M r solves A e = r - (w.r / w.1) 1 with w.e = 0: the compatible
+// system that the Gauss-Seidel path solves after removing the weighted mean,
+// here exactly.  Points are numbered k fastest, then j, then i.  Gauss-Jordan
+// elimination with partial pivoting in FP64; false if a pivot vanishes.
+static bool coarse_solution_operator(int X, int Y, int Z, const double l[3], const int per[3], std::vector<double> &M) {
+    const int E[3] = {X, Y, Z};
+    const int n = (X + 1) * (Y + 1) * (Z + 1), N = n + 1;
+    auto id = [&](const int q[3]) { return (q[0] * (Y + 1) + q[1]) * (Z + 1) + q[2]; };
+    auto img = [&](int q, int d) { return q < 0 ? (per[d] ? E[d] - 1 : 1) : q > E[d] ? (per[d] ? 1 : E[d] - 1) : q; };
+    std::vector<double> B((size_t)N * N, 0.0), R((size_t)N * n, 0.0);
+    int q[3];
+    for (q[0] = 0; q[0] <= X; ++q[0])
+        for (q[1] = 0; q[1] <= Y; ++q[1])
+            for (q[2] = 0; q[2] <= Z; ++q[2]) {
+                int P = id(q);
+                double w = 1.0;
+                for (int d = 0; d < 3; ++d) {
+                    B[(size_t)P * N + P] -= 2.0 * l[d];
+                    for (int s = -1; s <= 1; s += 2) {
+                        int r[3] = {q[0], q[1], q[2]};
+                        r[d] = img(q[d] + s, d);
+                        B[(size_t)P * N + id(r)] += l[d];
+                    }
+                    if (q[d] == 0 || q[d] == E[d]) w *= 0.5;
+                }
+                B[(size_t)P * N + n] = 1.0;
+                B[(size_t)n * N + P] = w;
+                R[(size_t)P * n + P] = 1.0;
+            }
+    for (int col = 0; col < N; ++col) {
+        int piv = col;
+        for (int r = col + 1; r < N; ++r)
+            if (std::fabs(B[(size_t)r * N + col]) > std::fabs(B[(size_t)piv * N + col])) piv = r;
+        if (!(std::fabs(B[(size_t)piv * N + col]) > 1e-300)) return false;
+        if (piv != col) {
+            for (int t = 0; t < N; ++t) std::swap(B[(size_t)piv * N + t], B[(size_t)col * N + t]);
+            for (int t = 0; t < n; ++t) std::swap(R[(size_t)piv * n + t], R[(size_t)col * n + t]);
+        }
+        double inv = 1.0 / B[(size_t)col * N + col];
+        for (int t = 0; t < N; ++t) B[(size_t)col * N + t] *= inv;
+        for (int t = 0; t < n; ++t) R[(size_t)col * n + t] *= inv;
+        for (int r = 0; r < N; ++r) {
+            if (r == col) continue;
+            double f = B[(size_t)r * N + col];
+            if (f == 0.0) continue;
+            for (int t = 0; t < N; ++t) B[(size_t)r * N + t] -= f * B[(size_t)col * N + t];
+            for (int t = 0; t < n; ++t) R[(size_t)r * n + t] -= f * R[(size_t)col * n + t];
+        }
+    }
+    M.assign(R.begin(), R.begin() + (size_t)n * n);
+    return true;
+}
+
 int mg_setup(Ctx &c) {
     const saras_params &p = c.p;
     c.depth = p.vcDepth;
@@ -1324,6 +1525,20 @@ int mg_setup(Ctx &c) {
     if (c.tailLt > 0) {
         SARAS_CUDA_TRY(cudaFuncSetAttribute(k_mg_tail<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         SARAS_CUDA_TRY(cudaFuncSetAttribute(k_mg_tail<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        // the tail's coarsest solve as a matrix-vector product when the level is small
+        const Level &Lc = c.lv[c.depth];
+        long nc = (long)(Lc.n[0] + 1) * (Lc.n[1] + 1) * (Lc.n[2] + 1);
+        double l[3] = {Lc.lx, Lc.ly, Lc.lz};
+        int per[3] = {p.xPer, p.yPer, p.zPer};
+        std::vector<double> M;
+        if (nc <= 512 && coarse_solution_operator(Lc.n[0], Lc.n[1], Lc.n[2], l, per, M)) {
+            std::vector<float> M32(M.begin(), M.end());
+            SARAS_CUDA_TRY(cudaMalloc(&c.coarseM64, M.size() * sizeof(double)));
+            SARAS_CUDA_TRY(cudaMalloc(&c.coarseM32, M32.size() * sizeof(float)));
+            SARAS_CUDA_TRY(cudaMemcpy(c.coarseM64, M.data(), M.size() * sizeof(double), cudaMemcpyHostToDevice));
+            SARAS_CUDA_TRY(cudaMemcpy(c.coarseM32, M32.data(), M32.size() * sizeof(float), cudaMemcpyHostToDevice));
+            c.coarseN = (int)nc;
+        }
     }
     if (p.testPoisson) {
         // multigrid_d3::initDirichlet (poisson_d3.cc:513-572), np = 1
@@ -1353,6 +1568,8 @@ void mg_free(Ctx &c) {
     c.lv.clear();
     cudaFree(c.wallX); cudaFree(c.wallY); cudaFree(c.wallZ);
     c.wallX = c.wallY = c.wallZ = nullptr;
+    cudaFree(c.coarseM64); cudaFree(c.coarseM32);
+    c.coarseM64 = nullptr; c.coarseM32 = nullptr; c.coarseN = 0;
 }
 
 // Level-0 Dirichlet wall values into the face ghosts of a level-0 array
@@ -1402,7 +1619,8 @@ static int smooth(Ctx &c, int l, int count, bool zero_first, bool tgt) {
             if (big_level(L)) {
                 if (z) k_tgt_sweep<T, true, false><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
                 else k_tgt_sweep<T, false, false><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
-                k_tgt_ghosts<T><<<dim3(64, 6), 256, 0, c.stream>>>(B_<T>(L), sx, sy, bc);
+                dim3 gg, bg; tgt_ghosts_dims(L, gg, bg);
+                k_tgt_ghosts<T><<<gg, bg, 0, c.stream>>>(B_<T>(L), sx, sy, bc);
                 count_launch(c);
             } else if (z) {
                 k_tgt_sweep<T, true, true><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
@@ -1449,6 +1667,16 @@ static int restrict_level(Ctx &c, int l, bool tgt) {
         int sx = (L.n[1] + 3) * (L.n[2] + 3), sy = L.n[2] + 3;
         dim3 gm, bm; march_dims(L, gm, bm);
         k_tgt_residual<T, T, false><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bcf, make_tgk<T>(L, 1.0), nullptr);
+        count_launch(c);
+        prof_end(c, pk, l, 3.0 * sizeof(T) * pts);
+        pk = sizeof(T) == 8 ? PK_MG_RESTRICT64 : PK_MG_RESTRICT32;
+        prof_begin(c, pk, l);
+        int csx = (C.n[1] + 3) * (C.n[2] + 3), csy = C.n[2] + 3;
+        dim3 gr((C.n[2] + 1 + 31) / 32, (C.n[1] + 1 + 7) / 8, (C.n[0] + 1 + kRrCh - 1) / kRrCh);
+        k_tgt_restrict<T><<<gr, dim3(32, 8, 1), 0, c.stream>>>(R_<T>(C), B_<T>(L), sx, sy, csx, csy, bcf);
+        count_launch(c);
+        prof_end(c, pk, l, sizeof(T) * pts * (1.0 + 1.0 / 8.0));
+        return chk(c, "mg restrict");
     } else
         k_mg_residual<T><<<g, b, 0, c.stream>>>(lview<T>(L, B_<T>(L)), lcview<T>(L, A_<T>(L)), lcview<T>(L, R_<T>(L)), kk, bcf);
     count_launch(c);
@@ -1474,7 +1702,8 @@ static int prolong_level(Ctx &c, int l, bool tgt, bool add) {
         dim3 gm, bm; march_dims(L, gm, bm);
         int sx = (L.n[1] + 3) * (L.n[2] + 3), sy = L.n[2] + 3;
         k_tgt_prolong_add<T><<<gm, bm, 0, c.stream>>>(A_<T>(L), A_<T>(C), sx, sy, (C.n[1] + 3) * (C.n[2] + 3), C.n[2] + 3, bc);
-        k_tgt_ghosts<T><<<dim3(64, 6), 256, 0, c.stream>>>(A_<T>(L), sx, sy, bc);
+        dim3 gg, bg; tgt_ghosts_dims(L, gg, bg);
+        k_tgt_ghosts<T><<<gg, bg, 0, c.stream>>>(A_<T>(L), sx, sy, bc);
         count_launch(c);
     } else {
         k_mg_prolong_add<T><<<g, b, 0, c.stream>>>(lview<T>(L, A_<T>(L)), lcview<T>(C, A_<T>(C)), bc, add ? 1 : 0);
@@ -1497,6 +1726,9 @@ static int tail_run(Ctx &c, int Lt) {
         smem += 3 * sizeof(T) * (size_t)L.count;
     }
     a.kkc = make_k(c.lv[c.depth]);
+    a.M = nullptr;
+    a.nM = c.coarseN;
+    if (c.coarseN) a.M = sizeof(T) == 8 ? (const T *)c.coarseM64 : (const T *)c.coarseM32;
     a.tol = (T)1.0e-3;   // as coarse_solve in the target modes
     a.maxc = 500;
     a.pre = c.p.preSmooth;
@@ -1541,46 +1773,78 @@ static int vcycle(Ctx &c, bool tgt, bool zero0) {
 static std::vector<int> level_state(const Ctx &c) {
     std::vector<int> st;
     for (const Level &L : c.lv) { st.push_back(L.cur); st.push_back(L.cur32); }
+    for (const ProfSlot &ps : c.prof) st.push_back(ps.enabled ? 1 : 0);   // the profiling event nodes it holds
     return st;
 }
 
+static void vgraph_drop(Ctx &c, int a, int b) {
+    if (c.vgraph[a][b]) cudaGraphExecDestroy(c.vgraph[a][b]);
+    if (c.vgraphSrc[a][b]) cudaGraphDestroy(c.vgraphSrc[a][b]);
+    for (ProfNode &n : c.vgraphProf[a][b]) cudaEventDestroy(n.captured);
+    c.vgraph[a][b] = nullptr;
+    c.vgraphSrc[a][b] = nullptr;
+    c.vgraphProf[a][b].clear();
+}
+
 void vgraph_reset(Ctx &c) {
-    for (auto &row : c.vgraph)
-        for (cudaGraphExec_t &g : row) {
-            if (g) cudaGraphExecDestroy(g);
-            g = nullptr;
-        }
+    for (int a = 0; a < 2; ++a)
+        for (int b = 0; b < 2; ++b) vgraph_drop(c, a, b);
+}
+
+// The event-record nodes of graph g that carry the profiling events recorded
+// during its capture, in capture order.
+static int map_prof_nodes(Ctx &c, cudaGraph_t g, std::vector<ProfNode> &out) {
+    out = c.profCaptured;
+    c.profCaptured.clear();
+    if (out.empty()) return SARAS_OK;
+    size_t n = 0;
+    SARAS_CUDA_TRY(cudaGraphGetNodes(g, nullptr, &n));
+    std::vector<cudaGraphNode_t> nodes(n);
+    SARAS_CUDA_TRY(cudaGraphGetNodes(g, nodes.data(), &n));
+    for (cudaGraphNode_t nd : nodes) {
+        cudaGraphNodeType t;
+        SARAS_CUDA_TRY(cudaGraphNodeGetType(nd, &t));
+        if (t != cudaGraphNodeTypeEventRecord) continue;
+        cudaEvent_t ev;
+        SARAS_CUDA_TRY(cudaGraphEventRecordNodeGetEvent(nd, &ev));
+        for (ProfNode &p : out)
+            if (p.captured == ev) p.node = nd;
+    }
+    for (const ProfNode &p : out)
+        if (!p.node) { c.err = "V-cycle graph: profiling event node not found"; return SARAS_CUDA_ERROR; }
+    return SARAS_OK;
 }
 
 template <typename T>
 static int vcycle_tgt(Ctx &c, bool zero0) {
-    bool profiling = false;
-    for (const ProfSlot &ps : c.prof) profiling = profiling || ps.enabled;
-    if (profiling) return vcycle<T>(c, true, zero0);
     int a = sizeof(T) == 4 ? 1 : 0, b = zero0 ? 1 : 0;
-    cudaGraphExec_t &ge = c.vgraph[a][b];
     std::vector<int> st = level_state(c);
-    if (ge && c.vgraphState[a][b] != st) {
-        cudaGraphExecDestroy(ge);
-        ge = nullptr;
-    }
-    if (!ge) {
+    if (c.vgraph[a][b] && c.vgraphState[a][b] != st) vgraph_drop(c, a, b);
+    if (!c.vgraph[a][b]) {
         long long l0 = c.launches;
+        for (ProfNode &n : c.profCaptured) cudaEventDestroy(n.captured);
+        c.profCaptured.clear();
         SARAS_CUDA_TRY(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+        c.profCapturing = true;
         int s = vcycle<T>(c, true, zero0);
+        c.profCapturing = false;
         cudaGraph_t g = nullptr;
         cudaError_t e = cudaStreamEndCapture(c.stream, &g);
         if (s || e != cudaSuccess) {
             if (g) cudaGraphDestroy(g);
+            for (ProfNode &n : c.profCaptured) cudaEventDestroy(n.captured);
+            c.profCaptured.clear();
             cudaGetLastError();
             if (s) return s;
             c.err = std::string("V-cycle capture: ") + cudaGetErrorString(e);
             return SARAS_CUDA_ERROR;
         }
-        e = cudaGraphInstantiate(&ge, g, 0);
-        cudaGraphDestroy(g);
+        c.vgraphSrc[a][b] = g;
+        if ((s = map_prof_nodes(c, g, c.vgraphProf[a][b]))) { vgraph_drop(c, a, b); return s; }
+        e = cudaGraphInstantiate(&c.vgraph[a][b], g, 0);
         if (e != cudaSuccess) {
-            ge = nullptr;
+            c.vgraph[a][b] = nullptr;
+            vgraph_drop(c, a, b);
             c.err = std::string("V-cycle graph: ") + cudaGetErrorString(e);
             return SARAS_CUDA_ERROR;
         }
@@ -1588,12 +1852,13 @@ static int vcycle_tgt(Ctx &c, bool zero0) {
         c.launches = l0;
         c.vgraphState[a][b] = st;
         if (level_state(c) != st) {   // a cycle that does not restore the level states is never replayed
-            cudaGraphExecDestroy(ge);
-            ge = nullptr;
+            vgraph_drop(c, a, b);
             return vcycle<T>(c, true, zero0);
         }
     }
-    SARAS_CUDA_TRY(cudaGraphLaunch(ge, c.stream));
+    int s = prof_graph_replay(c, c.vgraph[a][b], c.vgraphProf[a][b]);
+    if (s) { c.err = "V-cycle graph: profiling events"; return s; }
+    SARAS_CUDA_TRY(cudaGraphLaunch(c.vgraph[a][b], c.stream));
     c.launches += c.vgraphLaunches[a][b];
     return SARAS_OK;
 }
@@ -1716,6 +1981,31 @@ int mg_fine_residual(Ctx &c, const double *pp, double *maxres, double *maxb) {
 // values), and the counters are set.  done = false (a value left the
 // fixed-point range, which takes a diverging iterate) leaves L0.pa() holding
 // the previous Pp again for the FP64 refinement loop.
+constexpr int kMaxAdaptiveCycles = 8;   // V-cycles in one refinement step at most (mixedCycles = 0)
+
+// V-cycles of the next refinement step from residual r.  The first step of a
+// solve runs mixedCycles cycles; a later step (the target was missed), or any
+// step with mixedCycles = 0, runs the fewest that the measured contraction per
+// cycle predicts to reach the target, at most mixedCycles (kMaxAdaptiveCycles
+// for 0); never beyond mgMaxCycles in total.
+static int refine_cycles(const Ctx &c, double r, double target, int cyc, bool first) {
+    int cap = c.p.mixedCycles > 0 ? c.p.mixedCycles : kMaxAdaptiveCycles;
+    int n = cap;
+    if (!(first && c.p.mixedCycles > 0)) {
+        double need = std::log(target / r) / std::log(c.rhoMixed);
+        n = std::isfinite(need) ? std::max(1, std::min(cap, (int)std::ceil(need - 1e-3))) : 1;
+    }
+    return std::min(n, std::max(1, c.mgMaxCycles - cyc));
+}
+
+// Running estimate of the contraction per FP32 V-cycle from one refinement
+// step (r0 -> r over n cycles), kept within [0.005, 0.5].
+static void note_contraction(Ctx &c, double r0, double r, int n) {
+    if (!(r0 > 0.0) || !(r > 0.0) || !std::isfinite(r) || !std::isfinite(r0)) return;
+    double rho = std::pow(r / r0, 1.0 / n);
+    c.rhoMixed = std::min(0.5, std::max(0.005, 0.5 * c.rhoMixed + 0.5 * rho));
+}
+
 static int mixed_fixed(Ctx &c, double bmax, double pmax, double target, bool wantGuess, double &r, int &source, int &cyc, int &steps,
                        bool &done, saras_step_stats *st) {
     int s;
@@ -1756,7 +2046,8 @@ static int mixed_fixed(Ctx &c, double bmax, double pmax, double target, bool wan
         if (withE) {
             prof_begin(c, PK_REFINE_UPDATE, 0);
             k_fx_update<<<gm0, bm0, 0, c.stream>>>(c.fx[q ^ 1], c.fx[q], L0.pa32(), B, L0.r32, sx0, sy0, bc0, sc, (float)rs, dmax, dflag);
-            k_tgt_ghosts<long long><<<dim3(64, 6), 256, 0, c.stream>>>(c.fx[q ^ 1], sx0, sy0, bc0);
+            dim3 gg, bg; tgt_ghosts_dims(L0, gg, bg);
+            k_tgt_ghosts<long long><<<gg, bg, 0, c.stream>>>(c.fx[q ^ 1], sx0, sy0, bc0);
             count_launch(c);
             prof_end(c, PK_REFINE_UPDATE, 0, (8.0 + 4.0 + 8.0 + 8.0 + 4.0) * (double)L0.count);
         } else {
@@ -1785,7 +2076,9 @@ static int mixed_fixed(Ctx &c, double bmax, double pmax, double target, bool wan
     int cur = 0;
     if (wantGuess && c.histCount >= 2) {
         built = unet_pick(c);
+        prof_begin(c, PK_GUESS, 0);
         int gs = unet_guess(c, L0.r, L0.pb(), built);
+        prof_end(c, PK_GUESS, 0, 0.0);
         if (gs == SARAS_OK) {
             double rg = 0;
             k_fx_from<<<nbF, 256, 0, c.stream>>>(c.fx[1], L0.pb(), L0.count, sc, dflag);
@@ -1807,7 +2100,9 @@ static int mixed_fixed(Ctx &c, double bmax, double pmax, double target, bool wan
     while (true) {
         while (r > target && cyc < c.mgMaxCycles) {
             if (!std::isfinite(r)) { c.err = "multigrid residual is not finite"; return SARAS_NOT_FINITE; }
-            for (int q = 0; q < std::max(1, c.p.mixedCycles); ++q) {
+            int n = refine_cycles(c, r, target, cyc, steps == 0);
+            double r0 = r;
+            for (int q = 0; q < n; ++q) {
                 if ((s = vcycle_tgt<float>(c, q == 0))) return s;
                 cyc += 1;
             }
@@ -1815,6 +2110,7 @@ static int mixed_fixed(Ctx &c, double bmax, double pmax, double target, bool wan
             if ((s = refine(cur, true, r, bad))) return s;
             if (bad) break;
             cur ^= 1;
+            note_contraction(c, r0, r, n);
         }
         if (bad) break;
         // the FP64 result, and the exact residual of those FP64 values
@@ -1861,7 +2157,10 @@ static int mg_solve_target(Ctx &c, int *cycles, double *residual, saras_step_sta
     // pressure history for the learned / extrapolated guess
     bool wantGuess = c.guessMode != SARAS_GUESS_PREVIOUS;
     if (wantGuess || c.collecting) {
-        if ((s = unet_begin_solve(c))) return s;
+        prof_begin(c, PK_GUESS, 0);
+        s = unet_begin_solve(c);
+        prof_end(c, PK_GUESS, 0, 0.0);
+        if (s) return s;
     }
     // p = Pp (initial guess) with face ghosts; the fixed-point path reads Pp
     // itself and only needs max|Pp| for its scale
@@ -1936,12 +2235,15 @@ static int mg_solve_target(Ctx &c, int *cycles, double *residual, saras_step_sta
             if ((s = fine_res(false, &r))) return s;
         } else {
             // inner FP32 solve of A e = r32 from e = 0
-            for (int q = 0; q < std::max(1, c.p.mixedCycles); ++q) {
+            int n = refine_cycles(c, r, target, cyc, steps == 0);
+            double r0 = r;
+            for (int q = 0; q < n; ++q) {
                 if ((s = vcycle_tgt<float>(c, q == 0))) return s;
                 cyc += 1;
             }
             steps += 1;
             if ((s = fine_res(true, &r))) return s;
+            note_contraction(c, r0, r, n);
         }
     }
     }

@@ -35,6 +35,52 @@ def test_target_modes_reach_residual(mode):
         assert 0 < st.vcycles < 100
 
 
+def test_profiling_inside_replayed_vcycles():
+    """A profile slot enabled after the V-cycle graphs exist is recorded by
+    event nodes inside the replayed graphs: one launch per level-0 sweep."""
+    p, g = target_case(F.MG_MIXED)
+    names = S.Solver.profile_names()
+    k = names.index("mg_smooth_fp32")
+    for _ in range(2):
+        assert g.time_advance()[0] == 0
+    g.profile_enable(k, True)
+    cycles = 0
+    for _ in range(3):
+        s, st = g.time_advance()
+        assert s == 0 and st.fine_residual <= 1e-8
+        cycles += st.vcycles
+    n, ms, b = g.profile_read(k)
+    assert n == cycles * (p.preSmooth + p.postSmooth)
+    assert ms > 0.0 and b > 0.0
+
+
+def test_adaptive_refinement_cycles():
+    """mixedCycles = 0: each refinement step runs the V-cycles that the measured
+    contraction predicts; the target is met with fewer refinement steps than
+    one cycle per step, the V-cycle count stays that of the fixed form within
+    one, and the pressure agrees with the plain FP64 solve."""
+    _, fixed = target_case(F.MG_MIXED)            # mixedCycles = 1
+    p, adapt = target_case(F.MG_MIXED)
+    adapt.close()
+    p.mixedCycles = 0
+    adapt = S.Solver(p)
+    C.initialise(adapt, p, "tgv")
+    _, plain = target_case(F.MG_PLAIN_TARGET)
+    steps = {"fixed": 0, "adapt": 0}
+    for step in range(6):
+        s1, st1 = fixed.time_advance()
+        s2, st2 = adapt.time_advance()
+        s3, _ = plain.time_advance()
+        assert s1 == 0 and s2 == 0 and s3 == 0
+        assert st2.fine_residual <= 1e-8
+        if step >= 2:
+            steps["fixed"] += st1.refine_steps
+            steps["adapt"] += st2.refine_steps
+            assert st2.vcycles <= st1.vcycles + 1
+    assert steps["adapt"] < steps["fixed"]
+    assert C.rel_err(adapt.get(F.FIELD_P), plain.get(F.FIELD_P)) < 1e-7
+
+
 @pytest.mark.parametrize("guess", [F.GUESS_EXTRAPOLATE, F.GUESS_QUADRATIC, F.GUESS_PARITY])
 def test_history_guesses_reach_target_with_fewer_cycles(guess):
     """The history-based initial guesses (extrapolations of the previous
