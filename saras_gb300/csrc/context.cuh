@@ -118,6 +118,7 @@ struct Ctx {
     float *cnp = nullptr;      // split-FP64 Jacobi solve: N0 of each component and the D ping-pong (float pairs)
     long cnpCount = 0;
     int n0Fresh[4] = {0, 0, 0, 0};   // N0 of component q written by this step's right-hand side
+    int cnSweeps[4] = {2, 2, 2, 2};  // split Jacobi sweeps the last solve of component q launched
     int tailLt = -1;          // first level of the fused coarse V-cycle tail (target modes), or -1
     double rhoMixed = 0.1;    // measured residual contraction per FP32 V-cycle (mixed mode, mixedCycles = 0)
     int coarseN = 0;          // coarsest core points solved by coarseM (0: Gauss-Seidel instead)

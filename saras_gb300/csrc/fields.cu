@@ -671,8 +671,21 @@ struct CnDelta {
     CnDf f;
     int withResidual;
     double *resMax;            // max |corr| (times Dn on the host)
+    double *vout;              // final sweep: C0 + D out into this FP64 array instead of D
     __device__ long off(int i, int j, int k) const { return (long)(i + 1) * sx + (long)(j + 1) * sy + (k + 1); }
 };
+
+// The new iterate of point o: D out, or (final sweep) C0 + D in FP64, the sum
+// k_cn_unpack forms.
+template <bool FINAL>
+__device__ __forceinline__ void cn_delta_store(const CnDelta &a, long o, fpair out) {
+    if (FINAL) {
+        a.vout[o] = (a.C0[o] + f2d(out.h)) + f2d(out.l);
+    } else {
+        a.oh[o] = out.h;
+        a.ol[o] = out.l;
+    }
+}
 
 // D + corr at bulk point o.
 __device__ __forceinline__ fpair cn_delta_image(const CnDelta &a, long o, fpair &corr) {
@@ -725,6 +738,7 @@ __device__ __forceinline__ fpair cn_delta_boundary(const CnDelta &a, int i, int 
 // along i (block 32 x 8): the index work is paid once per column segment.
 constexpr int kCnMarch = 8;
 
+template <bool FINAL>
 __global__ void __launch_bounds__(256) k_cn_delta(CnDelta a) {
     int k = a.full.lo[2] + blockIdx.x * 32 + threadIdx.x;
     int j = a.full.lo[1] + blockIdx.y * 8 + threadIdx.y;
@@ -749,8 +763,7 @@ __global__ void __launch_bounds__(256) k_cn_delta(CnDelta a) {
                 fpair corr = fp_mul(num, a.f.invDn);
                 fpair out = fp_add(D, corr);
                 m = max(m, __float_as_uint(corr.h) & 0x7fffffffu);
-                a.oh[o] = out.h;
-                a.ol[o] = out.l;
+                cn_delta_store<FINAL>(a, o, out);
                 hm = hc;
                 hc = hp;
             }
@@ -762,8 +775,7 @@ __global__ void __launch_bounds__(256) k_cn_delta(CnDelta a) {
             fpair corr;
             fpair out = cn_delta_image(a, o, corr);
             m = max(m, __float_as_uint(corr.h) & 0x7fffffffu);   // |corr| bits; NaN stays above Inf
-            a.oh[o] = out.h;
-            a.ol[o] = out.l;
+            cn_delta_store<FINAL>(a, o, out);
         }
     }
     if (a.withResidual) block_maxf_to(__uint_as_float(m), a.resMax);
@@ -772,6 +784,7 @@ __global__ void __launch_bounds__(256) k_cn_delta(CnDelta a) {
 // The non-bulk points of the full box (the boundary program's targets), as six
 // disjoint slabs: along axis d the points below / above the bulk range, with the
 // axes before d restricted to the bulk range and the axes after d full.
+template <bool FINAL>
 __global__ void k_cn_delta_shell(CnDelta a) {
     int s = blockIdx.y, d = s >> 1;
     int lo[3], hi[3];
@@ -787,9 +800,7 @@ __global__ void k_cn_delta_shell(CnDelta a) {
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         int r = t / n2, k = lo[2] + (t - r * n2), q = r / n1, j = lo[1] + (r - q * n1), i = lo[0] + q;
         long o = a.off(i, j, k);
-        fpair out = cn_delta_boundary(a, i, j, k, o);
-        a.oh[o] = out.h;
-        a.ol[o] = out.l;
+        cn_delta_store<FINAL>(a, o, cn_delta_boundary(a, i, j, k, o));
     }
 }
 
@@ -1441,53 +1452,110 @@ static int cn_solve_delta(Ctx &c, int comp, int field, const CnFast &fa, double 
     d.full = fa.full;
     d.f = fd;
     d.resMax = c.dscal;
+    d.vout = nullptr;
     float *cur[2] = {dA, dAl}, *nxt[2] = {dB, dBl};
     dim3 gm((fa.full.ext[2] + 31) / 32, (fa.full.ext[1] + 7) / 8, (fa.full.ext[0] + kCnMarch - 1) / kCnMarch), bm(32, 8, 1);
-    auto launch = [&](int withRes) {
+    // vout: a final sweep, which writes C0 + D into vout (the field's scratch partner)
+    // instead of D, the sum k_cn_unpack would form
+    auto launch = [&](int withRes, double *vout) {
         d.dh = cur[0]; d.dl = cur[1]; d.oh = nxt[0]; d.ol = nxt[1];
         d.withResidual = withRes;
+        d.vout = vout;
         prof_begin(c, PK_CN, 0);
-        k_cn_delta<<<gm, bm, 0, c.stream>>>(d);
-        k_cn_delta_shell<<<dim3(64, 6), 256, 0, c.stream>>>(d);
+        if (vout) {
+            k_cn_delta<true><<<gm, bm, 0, c.stream>>>(d);
+            k_cn_delta_shell<true><<<dim3(64, 6), 256, 0, c.stream>>>(d);
+        } else {
+            k_cn_delta<false><<<gm, bm, 0, c.stream>>>(d);
+            k_cn_delta_shell<false><<<dim3(64, 6), 256, 0, c.stream>>>(d);
+        }
         count_launch(c, 2);
-        prof_end(c, PK_CN, 0, bytes);
+        prof_end(c, PK_CN, 0, vout ? bytes * 4.0 / 3.0 : bytes);
     };
-    launch(0);
-    std::swap(cur, nxt);
-    int sweeps = 1, failed = 0, status = SARAS_OK;
-    double res = 0;
-    while (true) {
-        SARAS_CUDA_TRY(cudaMemsetAsync(c.dscal, 0, sizeof(double), c.stream));
-        launch(1);
+    auto read_res = [&](double &r) -> int {
         int s = check_launch(c, "cn");
         if (s) return s;
         SARAS_CUDA_TRY(cudaMemcpyAsync(c.hscal, c.dscal, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
         SARAS_CUDA_TRY(cudaStreamSynchronize(c.stream));
-        res = c.hscal[0] * Dn;
-        if (!std::isfinite(res)) { c.err = "Jacobi residual is not finite"; status = SARAS_NOT_FINITE; break; }
-        if (res < c.p.cnTolerance) break;     // cur is the answer
-        // The Jacobi map contracts the max norm of successive corrections by
-        // rho = 1 - 1/Dn (its off-diagonal weights over the diagonal; boundary
-        // copies and reflections keep the weights' magnitudes), so the residual of
-        // the iterate this sweep produced is at most rho * res: when that bound is
-        // below the tolerance, the sweep that would only confirm it is skipped.
-        double bound = res * (1.0 - 1.0 / Dn) * 1.01;
-        if (bound < c.p.cnTolerance) {
+        r = c.hscal[0] * Dn;
+        return SARAS_OK;
+    };
+    // The Jacobi map contracts the max norm of successive corrections by
+    // rho = 1 - 1/Dn (its off-diagonal weights over the diagonal; boundary
+    // copies and reflections keep the weights' magnitudes), so the residual of
+    // the iterate a sweep produced is at most rho * (that sweep's residual): when
+    // that bound is below the tolerance, the sweep that would only confirm it is
+    // skipped.
+    const double rho = 1.0 - 1.0 / Dn;
+    int sweeps = 0, failed = 0, status = SARAS_OK;
+    double res = 0;
+    bool inField = false;   // the answer is already in the field (a final sweep was accepted)
+    // Speculative final sweep: the sweeps the previous solve of this component
+    // launched run without host round trips, the last of them as a final sweep.
+    // If its residual bound meets the tolerance its output is the answer (no
+    // unpack pass); if its own residual does, the previous iterate is, as in the
+    // loop below; otherwise the loop resumes from that previous iterate.
+    int slot = scratch_slot(field);
+    int spec = slot >= 0 ? std::max(1, c.cnSweeps[comp]) : 0;
+    if (spec > 0) {
+        for (int q = 1; q < spec; ++q) {
+            launch(0, nullptr);
             std::swap(cur, nxt);
             sweeps += 1;
-            res = bound;
-            break;
         }
-        failed += 1;
-        if (failed > c.maxIterations) { status = SARAS_NOT_CONVERGED; break; }
-        std::swap(cur, nxt);
-        sweeps += 1;
+        SARAS_CUDA_TRY(cudaMemsetAsync(c.dscal, 0, sizeof(double), c.stream));
+        launch(1, c.scratch[slot]);
+        int s = read_res(res);
+        if (s) return s;
+        if (!std::isfinite(res)) {
+            c.err = "Jacobi residual is not finite";
+            status = SARAS_NOT_FINITE;
+        } else if (res < c.p.cnTolerance && sweeps > 0) {
+            c.cnSweeps[comp] = spec;   // cur (the previous iterate) is the answer
+            spec = -1;
+        } else if (res * rho * 1.01 < c.p.cnTolerance) {
+            std::swap(c.f[field], c.scratch[slot]);
+            c.cnSweeps[comp] = spec;
+            sweeps = spec;
+            res = res * rho * 1.01;
+            inField = true;
+            spec = -1;
+        }
+    }
+    if (status == SARAS_OK && spec >= 0) {
+        if (sweeps == 0) {
+            launch(0, nullptr);
+            std::swap(cur, nxt);
+            sweeps = 1;
+        }
+        while (true) {
+            SARAS_CUDA_TRY(cudaMemsetAsync(c.dscal, 0, sizeof(double), c.stream));
+            launch(1, nullptr);
+            int s = read_res(res);
+            if (s) return s;
+            if (!std::isfinite(res)) { c.err = "Jacobi residual is not finite"; status = SARAS_NOT_FINITE; break; }
+            if (res < c.p.cnTolerance) { c.cnSweeps[comp] = sweeps + 1; break; }   // cur is the answer
+            double bound = res * rho * 1.01;
+            if (bound < c.p.cnTolerance) {
+                std::swap(cur, nxt);
+                sweeps += 1;
+                res = bound;
+                c.cnSweeps[comp] = sweeps;
+                break;
+            }
+            failed += 1;
+            if (failed > c.maxIterations) { status = SARAS_NOT_CONVERGED; break; }
+            std::swap(cur, nxt);
+            sweeps += 1;
+        }
     }
     // the field becomes C0 + D (also on failure, as the FP64 form leaves its last iterate)
-    k_cn_unpack<<<std::min<long>((n + 255) / 256, 152L * 16), 256, 0, c.stream>>>(V.p, cur[0], cur[1], n);
-    count_launch(c);
-    int s = check_launch(c, "cn unpack");
-    if (s) return s;
+    if (!inField) {
+        k_cn_unpack<<<std::min<long>((n + 255) / 256, 152L * 16), 256, 0, c.stream>>>(V.p, cur[0], cur[1], n);
+        count_launch(c);
+        int s = check_launch(c, "cn unpack");
+        if (s) return s;
+    }
     if (iters) *iters = status == SARAS_NOT_CONVERGED ? failed : sweeps;
     if (maxerr) *maxerr = res;
     return status;

@@ -16,10 +16,13 @@
 // vertex-grid operator with mirror or periodic ghosts) and use a damped Jacobi
 // smoother; they exist for the throughput comparison and are not drop-ins.
 //
-// Ghost handling: the smoother and prolongation write every face-ghost image of
-// the points they produce (imposeBC, poisson_d3.cc:575-668, restricted to the
-// face ghosts a 7-point stencil reads); the restriction resolves the pads of
-// the residual array (updatePads, poisson_d3.cc:671-686) by index mapping.
+// Ghost handling: in the reference mode the smoother and prolongation write
+// every face-ghost image of the points they produce (imposeBC,
+// poisson_d3.cc:575-668, restricted to the face ghosts a 7-point stencil
+// reads), and the restriction resolves the pads of the residual array
+// (updatePads, poisson_d3.cc:671-686) by index mapping.  The target-mode level
+// kernels resolve every face neighbour by index mapping (pad_img, nbr_jk) and
+// write the core only.
 // Compiled with --fmad=false (see fields.cu).
 
 #include <cmath>
@@ -678,18 +681,43 @@ __device__ __noinline__ void scatter_slow(T *P, int sx, int sy, int i, int j, in
 // in-plane neighbours and the right-hand side.
 constexpr int kIch = 8;
 
-// Levels where the sweep's ghost images are worth a separate launch.
-static bool big_level(const Level &L) { return (long)(L.n[0] + 1) * (L.n[1] + 1) * (L.n[2] + 1) >= (1L << 20); }
 
 static void march_dims(const Level &L, dim3 &g, dim3 &b) {
     b = dim3(32, 8, 1);
     g = dim3((L.n[2] + 1 + 31) / 32, (L.n[1] + 1 + 7) / 8, (L.n[0] + 1 + kIch - 1) / kIch);
 }
 
-// GHOSTS: write the face-ghost images in the kernel (small levels, where a
-// separate k_tgt_ghosts launch would cost more than the sweep); large levels
-// leave them to k_tgt_ghosts, which keeps device calls out of this kernel.
-template <typename T, bool ZERO, bool GHOSTS>
+// Index of the value a target-mode pad position -1 or E+1 holds: its mirror /
+// periodic image in the core (mirror 1 -> -1, E-1 -> E+1; periodic E-1 -> -1,
+// 1 -> E+1, the face-ghost images put_scatter writes).
+__device__ __forceinline__ int pad_img(int q, int E, int per) {
+    if (q < 0) return per ? E - 1 : 1;
+    if (q > E) return per ? 1 : E - 1;
+    return q;
+}
+
+// Neighbour offsets of a (j, k) column of a target-mode level: +-sy and +-1,
+// or at a face the offsets of the core images.  The target-mode level kernels
+// read the images directly and never the ghost layer, so no kernel has to
+// keep face ghosts current between sweeps.
+struct NbrJK {
+    long yp, ym;   // j + 1, j - 1
+    int zp, zm;    // k + 1, k - 1
+};
+__device__ __forceinline__ NbrJK nbr_jk(int j, int k, int sy, const MgBC &bc) {
+    NbrJK n;
+    n.yp = (long)(pad_img(j + 1, bc.E[1], bc.per[1]) - j) * sy;
+    n.ym = (long)(pad_img(j - 1, bc.E[1], bc.per[1]) - j) * sy;
+    n.zp = pad_img(k + 1, bc.E[2], bc.per[2]) - k;
+    n.zm = pad_img(k - 1, bc.E[2], bc.per[2]) - k;
+    return n;
+}
+// Offset from plane i to plane i + d (d = +-1), through the image at a face.
+__device__ __forceinline__ long nbr_x(int i, int d, int sx, const MgBC &bc) {
+    return (long)(pad_img(i + d, bc.E[0], bc.per[0]) - i) * sx;
+}
+
+template <typename T, bool ZERO>
 __global__ void __launch_bounds__(256) k_tgt_sweep(T *__restrict__ out, const T *__restrict__ in, const T *__restrict__ r,
                                                    int sx, int sy, MgBC bc, TgK<T> c) {
     int k = blockIdx.x * 32 + threadIdx.x;
@@ -697,34 +725,22 @@ __global__ void __launch_bounds__(256) k_tgt_sweep(T *__restrict__ out, const T 
     int i0 = blockIdx.z * kIch;
     if (j > bc.E[1] || k > bc.E[2]) return;
     int n = min(kIch, bc.E[0] - i0 + 1);
-    const int o0 = (i0 + 1) * sx + (j + 1) * sy + (k + 1);
+    const NbrJK nb = nbr_jk(j, k, sy, bc);
+    const long o0 = (long)(i0 + 1) * sx + (long)(j + 1) * sy + (k + 1);
     T cm = (T)0, cc = (T)0;
-    if (!ZERO) { cm = in[o0 - sx]; cc = in[o0]; }
-    auto point = [&](int o) {
-        T v;
-        if (ZERO) {
-            v = c.ar * r[o];
-        } else {
-            T cp = in[o + sx];
-            T ns = in[o + sy] + in[o - sy], ud = in[o + 1] + in[o - 1];
-            v = fma(c.ax, cm + cp, fma(c.ay, ns, fma(c.az, ud, fma(c.ar, r[o], c.om1 * cc))));
-            cm = cc;
-            cc = cp;
-        }
-        out[o] = v;
-    };
-    // a full column segment: every load of the segment issued before the first
-    // store (the loads are independent of the stores, and issuing them together
-    // keeps enough bytes in flight for HBM), then the updates; afterwards the
-    // face-ghost images of the segment's boundary points
-    if (n == kIch) {
+    if (!ZERO) { cm = in[o0 + nbr_x(i0, -1, sx, bc)]; cc = in[o0]; }
+    // a full column segment (its planes i0 + 1 .. i0 + kIch are core planes):
+    // every load of the segment issued before the first store (the loads are
+    // independent of the stores, and issuing them together keeps enough bytes
+    // in flight for HBM), then the updates
+    if (n == kIch && i0 + kIch <= bc.E[0]) {
         T nc[kIch + 1], ns[kIch], ud[kIch], rr[kIch];
 #pragma unroll
         for (int q = 0; q < kIch; ++q) {
-            int o = o0 + q * sx;
+            long o = o0 + (long)q * sx;
             nc[q + 1] = ZERO ? (T)0 : in[o + sx];
-            ns[q] = ZERO ? (T)0 : in[o + sy] + in[o - sy];
-            ud[q] = ZERO ? (T)0 : in[o + 1] + in[o - 1];
+            ns[q] = ZERO ? (T)0 : in[o + nb.yp] + in[o + nb.ym];
+            ud[q] = ZERO ? (T)0 : in[o + nb.zp] + in[o + nb.zm];
             rr[q] = r[o];
         }
         nc[0] = cc;
@@ -734,51 +750,29 @@ __global__ void __launch_bounds__(256) k_tgt_sweep(T *__restrict__ out, const T 
             if (ZERO) v = c.ar * rr[q];
             else v = fma(c.ax, cm + nc[q + 1], fma(c.ay, ns[q], fma(c.az, ud[q], fma(c.ar, rr[q], c.om1 * nc[q]))));
             cm = nc[q];
-            out[o0 + q * sx] = v;
+            out[o0 + (long)q * sx] = v;
         }
-    } else {
-        for (int q = 0; q < n; ++q) point(o0 + q * sx);
+        return;
     }
-    if (GHOSTS) {
-        bool edge_jk = j <= 1 || k <= 1 || j >= bc.E[1] - 1 || k >= bc.E[2] - 1;
-        if (edge_jk || i0 <= 1 || i0 + n - 1 >= bc.E[0] - 1) {
-            for (int q = 0; q < n; ++q) {
-                int i = i0 + q;
-                if (edge_jk || i <= 1 || i >= bc.E[0] - 1) tgt_images(out, sx, sy, i, j, k, out[o0 + q * sx], bc);
-            }
+    for (int q = 0; q < n; ++q) {
+        long o = o0 + (long)q * sx;
+        T v;
+        if (ZERO) {
+            v = c.ar * r[o];
+        } else {
+            T cp = in[o + nbr_x(i0 + q, 1, sx, bc)];
+            T ns = in[o + nb.yp] + in[o + nb.ym], ud = in[o + nb.zp] + in[o + nb.zm];
+            v = fma(c.ax, cm + cp, fma(c.ay, ns, fma(c.az, ud, fma(c.ar, r[o], c.om1 * cc))));
+            cm = cc;
+            cc = cp;
         }
+        out[o] = v;
     }
 }
 
-// Face-ghost images of a level array after a kernel that wrote the core only
-// (target modes: mirror 1 -> -1, E-1 -> E+1; periodic E-1 -> -1, 1 -> E+1,
-// as put_scatter).  blockIdx.y picks one of the six ghost faces, which is a
-// copy of the core plane at 1 or E-1 along that axis; a (64 x 4) block walks
-// rows of that plane, k (or j) fastest, with no index divisions.
-template <typename T>
-__global__ void __launch_bounds__(256) k_tgt_ghosts(T *__restrict__ p, int sx, int sy, MgBC bc) {
-    const int d = blockIdx.y >> 1, side = blockIdx.y & 1, E = bc.E[d];
-    const int v = side ? E - 1 : 1;                                        // source plane
-    const int g = bc.per[d] ? (side ? -1 : E + 1) : (side ? E + 1 : -1);   // ghost plane it fills
-    const int a1 = d == 0 ? 1 : 0, a2 = d == 2 ? 1 : 2;                     // the other two axes
-    const long st[3] = {sx, sy, 1};
-    const long base = (long)(v + 1) * st[d], delta = (long)(g - v) * st[d];
-    const int n1 = bc.E[a1] + 1, n2 = bc.E[a2] + 1;
-    for (int r = blockIdx.x * blockDim.y + threadIdx.y; r < n1; r += gridDim.x * blockDim.y)
-        for (int c = threadIdx.x; c < n2; c += blockDim.x) {
-            long o = base + (long)(r + 1) * st[a1] + (long)(c + 1) * st[a2];
-            p[o + delta] = p[o];
-        }
-}
-
-static void tgt_ghosts_dims(const Level &L, dim3 &g, dim3 &b) {
-    b = dim3(64, 4, 1);
-    int rows = std::max(L.n[0], std::max(L.n[1], L.n[2])) + 1;
-    g = dim3((rows + 3) / 4, 6, 1);
-}
-
-// Target-mode prolongation + add (vertex-centred trilinear) on the core; the
-// face-ghost images follow with k_tgt_ghosts.  A thread owns a fine (j, k)
+// Target-mode prolongation + add (vertex-centred trilinear) on the core (the
+// target-mode kernels read face neighbours at their images, so no ghost layer
+// is written).  A thread owns a fine (j, k)
 // column and marches fine planes in pairs: the coarse plane m interpolated to
 // (j, k) serves fine plane 2m and, averaged with plane m+1, fine plane 2m+1.
 template <typename T>
@@ -830,12 +824,13 @@ __global__ void __launch_bounds__(256) k_tgt_residual(OT *__restrict__ out, cons
     unsigned long long m = 0ull;
     if (j <= bc.E[1] && k <= bc.E[2]) {
         int iend = min(i0 + kIch - 1, bc.E[0]);
-        int o = (i0 + 1) * sx + (j + 1) * sy + (k + 1);
-        T cm = p[o - sx], cc = p[o];
+        const NbrJK nb = nbr_jk(j, k, sy, bc);
+        long o = (long)(i0 + 1) * sx + (long)(j + 1) * sy + (k + 1);
+        T cm = p[o + nbr_x(i0, -1, sx, bc)], cc = p[o];
 #pragma unroll 4
         for (int i = i0; i <= iend; ++i, o += sx) {
-            T cp = p[o + sx];
-            T ns = p[o + sy] + p[o - sy], ud = p[o + 1] + p[o - 1];
+            T cp = p[o + (i < bc.E[0] ? (long)sx : nbr_x(i, 1, sx, bc))];
+            T ns = p[o + nb.yp] + p[o + nb.ym], ud = p[o + nb.zp] + p[o + nb.zm];
             T lap = fma(c.lx, cm + cp, fma(c.ly, ns, fma(c.lz, ud, c.lc * cc)));
             T res = b[o] - lap;
             if (out) out[o] = (OT)res;
@@ -858,11 +853,6 @@ __global__ void __launch_bounds__(256) k_tgt_residual(OT *__restrict__ out, cons
 // their mirror / periodic images (the pads k_mg_restrict resolves).
 constexpr int kRrCh = 8;   // coarse planes per thread
 
-__device__ __forceinline__ int pad_img(int q, int E, int per) {
-    if (q < 0) return per ? E - 1 : 1;
-    if (q > E) return per ? 1 : E - 1;
-    return q;
-}
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_tgt_restrict(T *__restrict__ rc, const T *__restrict__ r, int sx, int sy, int csx, int csy,
@@ -926,44 +916,28 @@ __global__ void __launch_bounds__(256) k_tgt_update(double *__restrict__ p, cons
 // integer operations at the FP32 rate, 64 times its FP64 rate, so the
 // residual is bound by HBM.
 //
-// WITH_E: the iterate is first advanced by the FP32 correction e of the inner
-// V-cycle, P_out = P_in + round(e 2^s) (face-ghost images included), and the
-// residual is that of P_out.  r32 receives r in FP32 (the next V-cycle's
-// right-hand side), maxr the block maxima of |B - ...| in integer units, flag
-// any value outside the fixed-point range.
-template <bool WITH_E>
-__global__ void __launch_bounds__(256) k_fx_refine(long long *__restrict__ pout, const long long *__restrict__ pin,
-                                                   const float *__restrict__ e, const long long *__restrict__ bfx,
-                                                   float *__restrict__ r32, int sx, int sy, MgBC bc, int s, float rscale,
-                                                   unsigned long long *maxr, int *flag) {
+// k_fx_refine: the residual of P; r32 receives r in FP32 (the next V-cycle's
+// right-hand side), maxr the block maxima of |B - ...| in integer units.
+// Neighbours at the faces are read at their core images (nbr_jk, nbr_x).
+__global__ void __launch_bounds__(256) k_fx_refine(const long long *__restrict__ pin, const long long *__restrict__ bfx,
+                                                   float *__restrict__ r32, int sx, int sy, MgBC bc, float rscale,
+                                                   unsigned long long *maxr) {
     int k = blockIdx.x * 32 + threadIdx.x;
     int j = blockIdx.y * 8 + threadIdx.y;
     int i0 = blockIdx.z * kIch;
     unsigned long long m = 0;
-    bool bad = false;
     if (j <= bc.E[1] && k <= bc.E[2]) {
         int iend = min(i0 + kIch - 1, bc.E[0]);
-        int o = (i0 + 1) * sx + (j + 1) * sy + (k + 1);
-        bool edge_jk = j <= 1 || k <= 1 || j >= bc.E[1] - 1 || k >= bc.E[2] - 1;
-        auto val = [&](int q) -> long long {
-            long long v = pin[q];
-            if (WITH_E) v += f2fx(e[q], s, bad);
-            return v;
-        };
-        long long cm = val(o - sx), cc = val(o);
+        const NbrJK nb = nbr_jk(j, k, sy, bc);
+        long o = (long)(i0 + 1) * sx + (long)(j + 1) * sy + (k + 1);
+        long long cm = pin[o + nbr_x(i0, -1, sx, bc)], cc = pin[o];
         for (int i = i0; i <= iend; ++i, o += sx) {
-            long long cp = val(o + sx);
-            long long nb = (cm + cp) + (val(o + sy) + val(o - sy)) + (val(o + 1) + val(o - 1));
-            long long r = bfx[o] - (nb - 6 * cc);
+            long long cp = pin[o + (i < bc.E[0] ? (long)sx : nbr_x(i, 1, sx, bc))];
+            long long nsum = (cm + cp) + (pin[o + nb.yp] + pin[o + nb.ym]) + (pin[o + nb.zp] + pin[o + nb.zm]);
+            long long r = bfx[o] - (nsum - 6 * cc);
             r32[o] = fx2f(r) * rscale;
             unsigned long long a = (unsigned long long)(r < 0 ? -r : r);
             m = a > m ? a : m;
-            if (WITH_E) {
-                pout[o] = cc;
-                unsigned long long ac = (unsigned long long)(cc < 0 ? -cc : cc);
-                if (ac > (1ull << 59)) bad = true;
-                if (edge_jk || i <= 1 || i >= bc.E[0] - 1) scatter_slow(pout, sx, sy, i, j, k, cc, bc);
-            }
             cm = cc;
             cc = cp;
         }
@@ -981,49 +955,60 @@ __global__ void __launch_bounds__(256) k_fx_refine(long long *__restrict__ pout,
         for (int q = 0; q < 8; ++q) b = sm[q] > b ? sm[q] : b;
         atomicMax(maxr, b);
     }
-    if (bad) atomicExch(flag, 1);
 }
 
-// (k_fx_update writes the core; the face-ghost images follow with k_tgt_ghosts.)
-// The WITH_E step of k_fx_refine with the in-plane neighbours shared through
-// shared memory: each advanced value P + round(e 2^s) is formed once per
-// block (the tile's halo adds a third), instead of once per stencil use.
-// Block 32 (k) x 8 (j) marching kIch planes along i; the plane tile is double
-// buffered, and the column's own i-1 / i+1 values stay in registers.
+// The iterate advanced by the FP32 correction e of the inner V-cycles,
+// P_out = P_in + round(e 2^s), and the residual of P_out (as k_fx_refine), with
+// the in-plane neighbours shared through shared memory: each advanced value is
+// formed once per block (the tile's halo adds a third), instead of once per
+// stencil use.  Block 32 (k) x 8 (j) marching kIch planes along i; the plane
+// tiles rotate through three buffers (one barrier a plane), tile positions and
+// planes outside the core are read at their images, and the column's own
+// i - 1 / i + 1 values stay in registers.  flag: a value outside the
+// fixed-point range.
 __global__ void __launch_bounds__(256) k_fx_update(long long *__restrict__ pout, const long long *__restrict__ pin,
                                                    const float *__restrict__ e, const long long *__restrict__ bfx,
                                                    float *__restrict__ r32, int sx, int sy, MgBC bc, int s, float rscale,
                                                    unsigned long long *maxr, int *flag) {
-    __shared__ long long tile[2][10][34];
-    int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
-    int k0 = blockIdx.x * 32, j0 = blockIdx.y * 8, i0 = blockIdx.z * kIch;
-    int k = k0 + tx, j = j0 + ty;
-    int iend = min(i0 + kIch - 1, bc.E[0]);
+    __shared__ long long tile[3][10][34];
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
+    const int k0 = blockIdx.x * 32, j0 = blockIdx.y * 8, i0 = blockIdx.z * kIch;
+    const int k = k0 + tx, j = j0 + ty;
+    const int iend = min(i0 + kIch - 1, bc.E[0]);
     bool bad = false;
     auto val = [&](long q) -> long long { return pin[q] + f2fx(e[q], s, bad); };
-    // plane i of the tile: points (j0 - 1 .. j0 + 8, k0 - 1 .. k0 + 32), inside the padded box
+    // the two tile positions this thread loads: (j0 - 1 .. j0 + 8, k0 - 1 .. k0 + 32)
+    long lo[2];
+    bool lv[2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        int t = tid + 256 * q;
+        int jj = t / 34, kk = t - jj * 34;
+        int jg = j0 + jj - 1, kg = k0 + kk - 1;
+        lv[q] = t < 340 && jg <= bc.E[1] + 1 && kg <= bc.E[2] + 1;
+        lo[q] = (long)(pad_img(jg, bc.E[1], bc.per[1]) + 1) * sy + (pad_img(kg, bc.E[2], bc.per[2]) + 1);
+    }
     auto load_plane = [&](int i, int buf) {
-        for (int t = tid; t < 340; t += 256) {
-            int jj = t / 34, kk = t - jj * 34;
-            int jg = j0 + jj - 1, kg = k0 + kk - 1;
-            long long v = 0;
-            if (jg <= bc.E[1] + 1 && kg <= bc.E[2] + 1) v = val((long)(i + 1) * sx + (long)(jg + 1) * sy + (kg + 1));
-            tile[buf][jj][kk] = v;
+        long base = (long)(pad_img(i, bc.E[0], bc.per[0]) + 1) * sx;
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            int t = tid + 256 * q;
+            if (t < 340) (&tile[buf][0][0])[t] = lv[q] ? val(base + lo[q]) : 0;
         }
     };
-    bool active = j <= bc.E[1] && k <= bc.E[2];
+    const bool active = j <= bc.E[1] && k <= bc.E[2];
     long o = (long)(i0 + 1) * sx + (long)(j + 1) * sy + (k + 1);
-    long long cm = active ? val(o - sx) : 0;
+    long long cm = active ? val(o + nbr_x(i0, -1, sx, bc)) : 0;
     unsigned long long m = 0;
     load_plane(i0, 0);
     for (int i = i0; i <= iend; ++i, o += sx) {
-        int b = (i - i0) & 1;
-        load_plane(i + 1, b ^ 1);
+        const int b = (i - i0) % 3, bn = (i - i0 + 1) % 3;
+        load_plane(i + 1, bn);
         __syncthreads();
         if (active) {
-            long long cc = tile[b][ty + 1][tx + 1], cp = tile[b ^ 1][ty + 1][tx + 1];
-            long long nb = (cm + cp) + (tile[b][ty][tx + 1] + tile[b][ty + 2][tx + 1]) + (tile[b][ty + 1][tx] + tile[b][ty + 1][tx + 2]);
-            long long r = bfx[o] - (nb - 6 * cc);
+            long long cc = tile[b][ty + 1][tx + 1], cp = tile[bn][ty + 1][tx + 1];
+            long long nsum = (cm + cp) + (tile[b][ty][tx + 1] + tile[b][ty + 2][tx + 1]) + (tile[b][ty + 1][tx] + tile[b][ty + 1][tx + 2]);
+            long long r = bfx[o] - (nsum - 6 * cc);
             r32[o] = fx2f(r) * rscale;
             unsigned long long a = (unsigned long long)(r < 0 ? -r : r);
             m = a > m ? a : m;
@@ -1032,7 +1017,6 @@ __global__ void __launch_bounds__(256) k_fx_update(long long *__restrict__ pout,
             if (ac > (1ull << 59)) bad = true;
             cm = cc;
         }
-        __syncthreads();
     }
 #pragma unroll
     for (int off = 16; off; off >>= 1) {
@@ -1615,18 +1599,8 @@ static int smooth(Ctx &c, int l, int count, bool zero_first, bool tgt) {
     for (int n = 0; n < count; ++n) {
         prof_begin(c, pk, l);
         if (tgt) {
-            bool z = n == 0 && zero_first;
-            if (big_level(L)) {
-                if (z) k_tgt_sweep<T, true, false><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
-                else k_tgt_sweep<T, false, false><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
-                dim3 gg, bg; tgt_ghosts_dims(L, gg, bg);
-                k_tgt_ghosts<T><<<gg, bg, 0, c.stream>>>(B_<T>(L), sx, sy, bc);
-                count_launch(c);
-            } else if (z) {
-                k_tgt_sweep<T, true, true><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
-            } else {
-                k_tgt_sweep<T, false, true><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
-            }
+            if (n == 0 && zero_first) k_tgt_sweep<T, true><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
+            else k_tgt_sweep<T, false><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
         } else if (n == 0 && zero_first)
             k_mg_sweep<T, true><<<g, b, 0, c.stream>>>(lview<T>(L, B_<T>(L)), lcview<T>(L, A_<T>(L)), lcview<T>(L, R_<T>(L)), kk, bc, omega);
         else
@@ -1698,13 +1672,10 @@ static int prolong_level(Ctx &c, int l, bool tgt, bool add) {
     int pk = sizeof(T) == 8 ? PK_MG_PROLONG64 : PK_MG_PROLONG32;
     double pts = (double)(L.n[0] + 1) * (L.n[1] + 1) * (L.n[2] + 1);
     prof_begin(c, pk, l);
-    if (tgt && add && big_level(L)) {
+    if (tgt && add) {   // the core only: target-mode kernels read face neighbours at their images
         dim3 gm, bm; march_dims(L, gm, bm);
         int sx = (L.n[1] + 3) * (L.n[2] + 3), sy = L.n[2] + 3;
         k_tgt_prolong_add<T><<<gm, bm, 0, c.stream>>>(A_<T>(L), A_<T>(C), sx, sy, (C.n[1] + 3) * (C.n[2] + 3), C.n[2] + 3, bc);
-        dim3 gg, bg; tgt_ghosts_dims(L, gg, bg);
-        k_tgt_ghosts<T><<<gg, bg, 0, c.stream>>>(A_<T>(L), sx, sy, bc);
-        count_launch(c);
     } else {
         k_mg_prolong_add<T><<<g, b, 0, c.stream>>>(lview<T>(L, A_<T>(L)), lcview<T>(C, A_<T>(C)), bc, add ? 1 : 0);
     }
@@ -2046,13 +2017,10 @@ static int mixed_fixed(Ctx &c, double bmax, double pmax, double target, bool wan
         if (withE) {
             prof_begin(c, PK_REFINE_UPDATE, 0);
             k_fx_update<<<gm0, bm0, 0, c.stream>>>(c.fx[q ^ 1], c.fx[q], L0.pa32(), B, L0.r32, sx0, sy0, bc0, sc, (float)rs, dmax, dflag);
-            dim3 gg, bg; tgt_ghosts_dims(L0, gg, bg);
-            k_tgt_ghosts<long long><<<gg, bg, 0, c.stream>>>(c.fx[q ^ 1], sx0, sy0, bc0);
-            count_launch(c);
             prof_end(c, PK_REFINE_UPDATE, 0, (8.0 + 4.0 + 8.0 + 8.0 + 4.0) * (double)L0.count);
         } else {
             prof_begin(c, PK_REFINE_RESID, 0);
-            k_fx_refine<false><<<gm0, bm0, 0, c.stream>>>(nullptr, c.fx[q], nullptr, B, L0.r32, sx0, sy0, bc0, sc, (float)rs, dmax, dflag);
+            k_fx_refine<<<gm0, bm0, 0, c.stream>>>(c.fx[q], B, L0.r32, sx0, sy0, bc0, (float)rs, dmax);
             prof_end(c, PK_REFINE_RESID, 0, (8.0 + 8.0 + 4.0) * (double)L0.count);
         }
         count_launch(c);

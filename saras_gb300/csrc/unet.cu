@@ -195,28 +195,45 @@ struct L0View {
 };
 
 // Level-0 padded field -> level-1 core array: full weighting (coarse point i on
-// fine point 2i, taps outside the grid skipped), in FP64: 27 fused
-// multiply-adds per coarse point are about 3.4 FP64 operations per fine point,
-// cheaper here than splitting every fine value into a float pair.
-__global__ void k_restrict0(L0View f, Grid3 g1, double *out) {
-    long v = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (v >= g1.n()) return;
-    int x = (int)(v % g1.W), y = (int)((v / g1.W) % g1.H), z = (int)(v / ((long)g1.W * g1.H));
-    double s = 0.0;
-    for (int dz = -1; dz <= 1; ++dz) {
-        int zz = 2 * z + dz;
-        if (zz < 0 || zz > f.n[0]) continue;
+// fine point 2i, weights (1/64) [1 2 1]^3, taps outside the grid skipped).  In
+// FP64 the 27 fused multiply-adds a coarse point are bound by GB300's FP64
+// pipe; here every fine value is split into a float pair (integer work) and
+// the separable sums run in float-pair arithmetic (about 2^-44 of the largest
+// tap), one FP64 addition a coarse point.  One thread per coarse (y, x)
+// column marches kR0Ch coarse planes, the odd fine plane between two coarse
+// planes serving both.
+constexpr int kR0Ch = 8;
+
+__global__ void __launch_bounds__(256) k_restrict0(L0View f, Grid3 g1, double *out) {
+    const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y, z0 = blockIdx.z * kR0Ch;
+    if (x >= g1.W || y >= g1.H) return;
+    const int zend = min(z0 + kR0Ch, g1.D);
+    auto plane = [&](int zz) -> fpair {   // in-plane [1 2 1] x [1 2 1] sum of fine plane zz (0 outside)
+        fpair s = fpair{0.0f, 0.0f};
+        if (zz < 0 || zz > f.n[0]) return s;
+#pragma unroll
         for (int dy = -1; dy <= 1; ++dy) {
             int yy = 2 * y + dy;
             if (yy < 0 || yy > f.n[1]) continue;
+            fpair r = fpair{0.0f, 0.0f};
+#pragma unroll
             for (int dx = -1; dx <= 1; ++dx) {
                 int xx = 2 * x + dx;
                 if (xx < 0 || xx > f.n[2]) continue;
-                s = fma((double)(fw1(dz) * fw1(dy) * fw1(dx)), f.at(zz, yy, xx), s);
+                fpair v = fp_of(f.at(zz, yy, xx));
+                r = fp_add(r, dx == 0 ? fpair{2.0f * v.h, 2.0f * v.l} : v);
             }
+            s = fp_add(s, dy == 0 ? fpair{2.0f * r.h, 2.0f * r.l} : r);
         }
+        return s;
+    };
+    fpair lo = plane(2 * z0 - 1);
+    for (int z = z0; z < zend; ++z) {
+        fpair mid = plane(2 * z), hi = plane(2 * z + 1);
+        fpair t = fp_add(fp_add(lo, fpair{2.0f * mid.h, 2.0f * mid.l}), hi);
+        out[((long)z * g1.H + y) * g1.W + x] = (f2d(t.h) + f2d(t.l)) * 0.015625;
+        lo = hi;
     }
-    out[v] = s;
 }
 
 // Level-l core array -> level-l+1 core array, the same weights (FP64; these
@@ -467,6 +484,8 @@ struct UNet {
     // (moving averages), the basis of the choice between them
     double cycNet = 0.0, cycExt = 0.0;
     int usesNet = 0, usesExt = 0, solves = 0;
+    int probeEvery = 8, nextProbe = 0;       // probe schedule of the guess that is not preferred
+    bool preferNet = false;
     // training samples: 3 feature channels + target per voxel
     std::vector<float *> samples;
     int nsamples = 0, cap = 0, next = 0;
@@ -781,7 +800,8 @@ static int restrict_to_base(Ctx &c, const double *src, double *dst) {
     const Level &L1 = c.lv[1];
     Grid3 g1{L1.n[0] + 1, L1.n[1] + 1, L1.n[2] + 1};
     double *first = u->lb == 1 ? dst : u->tmp[0];
-    k_restrict0<<<(int)((g1.n() + 255) / 256), 256, 0, c.stream>>>(l0view(c, src), g1, first);
+    k_restrict0<<<dim3((g1.W + 31) / 32, (g1.H + 7) / 8, (g1.D + kR0Ch - 1) / kR0Ch), dim3(32, 8, 1), 0, c.stream>>>(l0view(c, src), g1,
+                                                                                                                 first);
     count_launch(c);
     Grid3 gf = g1;
     for (int l = 2; l <= u->lb; ++l) {
@@ -852,11 +872,16 @@ int unet_begin_solve(Ctx &c) {
 
 // SARAS_GUESS_LEARNED picks, per solve, between the network's guess and plain
 // extrapolation by the V-cycles each has needed (moving averages over its
-// recent solves): the cheaper one is used, and the other is tried every
-// kProbe-th solve so that its average stays current.  A network that does not
-// beat extrapolation on the running problem is thus only evaluated on probe
-// solves, and one that does is used throughout.
-constexpr int kProbe = 8;
+// recent solves).  Building the network's guess costs about half a level-0
+// V-cycle more than extrapolating (restrictions, features, forward pass), so
+// the network is preferred when its average is lower by more than that.  The
+// other guess is probed so that its average stays current: first after
+// kProbe solves, then at doubling intervals up to kProbeMax while the
+// preference holds (back to kProbe when it changes).  A network that does not
+// beat extrapolation on the running problem is thus evaluated on a few solves
+// in a hundred, and one that does is used throughout.
+constexpr int kProbe = 8, kProbeMax = 64;
+constexpr double kNetCostCycles = 0.5;
 
 int unet_pick(Ctx &c) {
     if (c.guessMode != SARAS_GUESS_LEARNED) return c.guessMode;
@@ -865,8 +890,17 @@ int unet_pick(Ctx &c) {
     u->solves += 1;
     if (u->usesNet < 2) return SARAS_GUESS_LEARNED;
     if (u->usesExt < 2) return SARAS_GUESS_EXTRAPOLATE;
-    bool netBetter = u->cycNet <= u->cycExt;
-    if (u->solves % kProbe == 0) netBetter = !netBetter;
+    bool netBetter = u->cycNet + kNetCostCycles < u->cycExt;
+    if (netBetter != u->preferNet) {
+        u->preferNet = netBetter;
+        u->probeEvery = kProbe;
+        u->nextProbe = u->solves + kProbe;
+    }
+    if (u->solves >= u->nextProbe) {
+        netBetter = !netBetter;
+        u->nextProbe = u->solves + u->probeEvery;
+        u->probeEvery = std::min(kProbeMax, 2 * u->probeEvery);
+    }
     return netBetter ? SARAS_GUESS_LEARNED : SARAS_GUESS_EXTRAPOLATE;
 }
 
