@@ -1598,6 +1598,7 @@ static int smooth(Ctx &c, int l, int count, bool zero_first, bool tgt) {
     dim3 gm, bm; march_dims(L, gm, bm);
     for (int n = 0; n < count; ++n) {
         prof_begin(c, pk, l);
+        const double lb = (n == 0 && zero_first) ? bytes * 2.0 / 3.0 : bytes;   // a zero start reads no iterate
         if (tgt) {
             if (n == 0 && zero_first) k_tgt_sweep<T, true><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
             else k_tgt_sweep<T, false><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
@@ -1606,7 +1607,7 @@ static int smooth(Ctx &c, int l, int count, bool zero_first, bool tgt) {
         else
             k_mg_sweep<T, false><<<g, b, 0, c.stream>>>(lview<T>(L, B_<T>(L)), lcview<T>(L, A_<T>(L)), lcview<T>(L, R_<T>(L)), kk, bc, omega);
         count_launch(c);
-        prof_end(c, pk, l, (n == 0 && zero_first) ? bytes * 2.0 / 3.0 : bytes);
+        prof_end(c, pk, l, lb);
         flip<T>(L);
     }
     return chk(c, "mg smooth");
@@ -1822,8 +1823,9 @@ static int vcycle_tgt(Ctx &c, bool zero0) {
         c.vgraphLaunches[a][b] = c.launches - l0;
         c.launches = l0;
         c.vgraphState[a][b] = st;
-        if (level_state(c) != st) {   // a cycle that does not restore the level states is never replayed
-            vgraph_drop(c, a, b);
+        if (level_state(c) != st) {   // a cycle that does not restore the level states is never replayed:
+            vgraph_drop(c, a, b);     // back to the states before the capture, then run it directly
+            for (size_t q = 0; q < c.lv.size(); ++q) { c.lv[q].cur = st[2 * q]; c.lv[q].cur32 = st[2 * q + 1]; }
             return vcycle<T>(c, true, zero0);
         }
     }

@@ -35,6 +35,30 @@ def test_target_modes_reach_residual(mode):
         assert 0 < st.vcycles < 100
 
 
+def test_mixed_solve_v44_three_cycles():
+    """A 65^3 mixed solve with the benchmark's cycle shape (V(4,4), three FP32
+    cycles in the first refinement step) reaches the target and agrees with
+    the plain FP64 solve."""
+    def case(mode):
+        p = C.tgv(ind=6, depth=4, dt=5e-4)
+        p.mgMode = mode
+        p.mgTarget = 1e-8
+        p.mgMaxCycles = 100
+        p.jacobiWeight = 6.0 / 7.0
+        p.fastKernels = 2
+        p.preSmooth = p.postSmooth = 4
+        p.mixedCycles = 3
+        g = S.Solver(p)
+        C.initialise(g, p, "tgv")
+        return g
+    m, f = case(F.MG_MIXED), case(F.MG_PLAIN_TARGET)
+    for _ in range(3):
+        s1, st1 = m.time_advance()
+        s2, _ = f.time_advance()
+        assert s1 == 0 and s2 == 0 and st1.fine_residual <= 1e-8
+    assert C.rel_err(m.get(F.FIELD_P), f.get(F.FIELD_P)) < 1e-7
+
+
 def test_profiling_inside_replayed_vcycles():
     """A profile slot enabled after the V-cycle graphs exist is recorded by
     event nodes inside the replayed graphs: one launch per level-0 sweep."""
