@@ -48,14 +48,17 @@ def tgv_params(mode, guess=0, ind=GRID_INDEX, depth=DEPTH):
     p.tStp = DT
     p.cnTolerance = 1.0e-8
     p.mgTolerance = 1.0e-8
-    # each arm with the smoothing it is fastest with at 257^3: the plain FP64
-    # solve with V(3,3) (8 cycles; V(4,4) 7 and V(5,5) 6 cycles take longer),
-    # the mixed solve with V(4,4) (3 cycles, against 4 with V(3,3))
-    p.preSmooth = p.postSmooth = 4 if mode == _abi.MG_MIXED else 3
+    # both target-mode arms with the smoothing each is fastest with at 257^3:
+    # Chebyshev V(3,3) (plain FP64: 7 cycles, 27.7 ms a step, against 8 cycles
+    # and 31.1 ms with damped-Jacobi V(3,3) and 6-7 cycles with V(4,4) / V(5,5);
+    # mixed: 3 cycles in one refinement step), refinement steps sized by the
+    # measured contraction per cycle
+    p.preSmooth = p.postSmooth = 3
+    p.smoother = _abi.SMOOTHER_CHEBYSHEV if mode != _abi.MG_REFERENCE else _abi.SMOOTHER_JACOBI
     p.mgMode = mode
     p.mgTarget = TARGET
     p.mgMaxCycles = 100
-    p.mixedCycles = 3
+    p.mixedCycles = 0
     p.jacobiWeight = 6.0 / 7.0 if mode != _abi.MG_REFERENCE else 1.0
     p.fastKernels = 2 if mode != _abi.MG_REFERENCE else 0
     p.guessMode = guess
@@ -332,9 +335,9 @@ def run_ours(args, dist):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic (Taylor-Green initial condition)",
         "config": {
             "workload": "Taylor-Green vortex 257^3 (2^8+1 vertex points per axis), [0,2pi]^3 PPP, Re 1600, dt 5e-4; "
-                        "pressure solve: FP32 V(4,4) cycles inside iterative refinement with an exact fixed-point residual (three cycles in the "
-                        "first refinement step, later steps sized by the measured contraction), to max|b-Ap|/max|b| <= 1e-8; "
-                        "plain arm: FP64 V(3,3) cycles to the same residual",
+                        "pressure solve: FP32 V(3,3) cycles (Chebyshev-weighted Jacobi smoothing) inside iterative refinement with an "
+                        "exact fixed-point residual, refinement steps sized by the measured contraction per cycle, to "
+                        "max|b-Ap|/max|b| <= 1e-8; plain arm: FP64 V(3,3) cycles, same smoothing, same residual",
             "grid": [257, 257, 257], "vcycle_depth": DEPTH, "mg_mode": "mixed_fp32_in_fp64",
             "warm_start": "unet (3-level 16/32/64, tcgen05 BF16 convs) correcting 2 Pp(n-1) - Pp(n-2), "
                           "least-squares step length, fallback to the previous pressure"

@@ -120,6 +120,11 @@ typedef struct saras_params {
                                  CN Jacobi update in split-FP64 form (FP64 values
                                  carried in float pairs, about 1e-14 relative);
                                  0: reference arithmetic (the drop-in)          */
+    int smoother;             /* target modes: 0 damped Jacobi (jacobiWeight);
+                                 1 Chebyshev: each smoothing phase of n sweeps
+                                 is the degree-n Chebyshev polynomial of D^-1 A
+                                 on [1/3, 2], applied as n Jacobi sweeps with
+                                 the weights 1 / (its roots) (n <= 16)          */
 } saras_params;
 
 typedef struct saras_step_stats {

@@ -25,6 +25,7 @@ FIELD_NAMES = ["Vx", "Vy", "Vz", "P", "T", "Pp", "mgRHS", "nseRHS.Vx", "nseRHS.V
 
 MG_REFERENCE, MG_PLAIN_TARGET, MG_MIXED = 0, 1, 2
 GUESS_PREVIOUS, GUESS_LEARNED, GUESS_EXTRAPOLATE, GUESS_QUADRATIC, GUESS_PARITY = 0, 1, 2, 3, 4
+SMOOTHER_JACOBI, SMOOTHER_CHEBYSHEV = 0, 1
 
 _I, _D = ctypes.c_int, ctypes.c_double
 
@@ -58,6 +59,7 @@ class saras_params(ctypes.Structure):
         ("jacobiWeight", _D),
         ("seed", _I),
         ("fastKernels", _I),
+        ("smoother", _I),
     ]
 
     def to_dict(self):
@@ -98,6 +100,7 @@ def default_params():
     p.mgTarget, p.mgMaxCycles, p.mixedCycles, p.guessMode = 1.0e-8, 200, 1, GUESS_PREVIOUS
     p.jacobiWeight, p.seed = 1.0, 42
     p.fastKernels = 0
+    p.smoother = SMOOTHER_JACOBI
     return p
 
 

@@ -25,7 +25,7 @@ namespace saras {
 // Constants of the split-FP64 Jacobi solve (see k_cn_delta).
 struct CnDf {
     fpair kc[3];     // k1 c1, k1 c2, k1 c3 as float pairs (N0)
-    float kf[3];     // the same as floats (sweeps: S_d(D) is small)
+    float kf[3];     // the same as floats (the coupling sum of the sweeps)
     fpair invDn;     // 1 / Dn
 };
 
@@ -239,10 +239,13 @@ __global__ void k_divergence(View3<double> D, Vel V, Box full, UC u, double scal
 }
 
 // Split-FP64 form (fastKernels = 2) of the scaled divergence: the three face
-// differences from split values, the folded factors as float pairs (about
-// 2^-44 of the largest term), one FP64 addition per point; one thread per
-// (j, k) column of the P full box marching along i with Vx(i-1) carried.
-// Points outside the P core are 0, as in k_divergence.
+// differences in FP64 (the velocity is nearly solenoidal, so the divergence is
+// about 1e-10 of the velocity's scale and the differences need all 53 bits:
+// split values of 47 bits leave 1e-5 of noise in the pressure right-hand
+// side), each difference split into a float pair, the folded factors as float
+// pairs, one FP64 addition per point; one thread per (j, k) column of the P
+// full box marching along i with Vx(i-1) carried.  Points outside the P core
+// are 0, as in k_divergence.
 struct DivDf {
     fpair k[3];
 };
@@ -255,15 +258,15 @@ __global__ void __launch_bounds__(256) k_divergence_df(View3<double> D, Vel V, B
     if (k >= full.lo[2] + full.ext[2] || j >= full.lo[1] + full.ext[1]) return;
     int iend = min(i0 + kProjMarch, full.lo[0] + full.ext[0]);
     bool jk = j >= 0 && k >= 0 && j < D.n[1] && k < D.n[2];
-    fpair xm = fpair{0.0f, 0.0f};
+    double xm = 0.0;
     bool have = false;   // xm holds Vx(i-1)
     for (int i = i0; i < iend; ++i) {
         if (!(jk && i >= 0 && i < D.n[0])) { D(i, j, k) = 0.0; continue; }
-        if (!have) { xm = fp_of(V.v[0](i - 1, j, k)); have = true; }
-        fpair xc = fp_of(V.v[0](i, j, k));
-        fpair dx = fp_add(xc, fp_neg(xm));
-        fpair dy = fp_add(fp_of(V.v[1](i, j, k)), fp_neg(fp_of(V.v[1](i, j - 1, k))));
-        fpair dz = fp_add(fp_of(V.v[2](i, j, k)), fp_neg(fp_of(V.v[2](i, j, k - 1))));
+        if (!have) { xm = V.v[0](i - 1, j, k); have = true; }
+        double xc = V.v[0](i, j, k);
+        fpair dx = fp_of(xc - xm);
+        fpair dy = fp_of(V.v[1](i, j, k) - V.v[1](i, j - 1, k));
+        fpair dz = fp_of(V.v[2](i, j, k) - V.v[2](i, j, k - 1));
         fpair sum = fp_add(fp_add(fp_mul(q.k[0], dx), fp_mul(q.k[1], dy)), fp_mul(q.k[2], dz));
         D(i, j, k) = f2d(sum.h) + f2d(sum.l);
         xm = xc;
@@ -654,7 +657,7 @@ __global__ void __launch_bounds__(256) k_cn_pack(View3<const double> V, View3<co
     fpair sy = fp_add(fp_add(fp_of(V(i, j + 1, k)), fp_of(V(i, j - 1, k))), c2);
     fpair sz = fp_add(fp_add(fp_of(V(i, j, k + 1)), fp_of(V(i, j, k - 1))), c2);
     fpair q = fp_add(fp_add(fp_mul(f.kc[0], sx), fp_mul(f.kc[1], sy)), fp_mul(f.kc[2], sz));
-    fpair n = fp_add(fp_add(fp_of(rhs(i, j, k)), fp_neg(c)), q);
+    fpair n = fp_add(fp_of(rhs(i, j, k) - V(i, j, k)), q);   // rhs - C0 in FP64: both O(1), the difference small
     long o = V.off(i, j, k);
     n0h[o] = n.h;
     n0l[o] = n.l;
@@ -687,15 +690,35 @@ __device__ __forceinline__ void cn_delta_store(const CnDelta &a, long o, fpair o
     }
 }
 
-// D + corr at bulk point o.
-__device__ __forceinline__ fpair cn_delta_image(const CnDelta &a, long o, fpair &corr) {
-    fpair D = fpair{a.dh[o], a.dl[o]};
-    float d2 = 2.0f * D.h;
-    float q = fmaf(a.f.kf[0], (a.dh[o + a.sx] + a.dh[o - a.sx]) - d2,
-                   fmaf(a.f.kf[1], (a.dh[o + a.sy] + a.dh[o - a.sy]) - d2, a.f.kf[2] * ((a.dh[o + 1] + a.dh[o - 1]) - d2)));
+// p + m - 2 c for float pairs p, m, c (one axis of the discrete Laplacian of
+// D) as a float: the high parts' sum by TwoSum, its difference with 2 c.h
+// (exact for smooth D, where the two are within a factor of two), then the
+// rounding error and the low parts.  The pressure right-hand side is the
+// divergence of the Jacobi result, about 1e-10 of the velocity's scale, and the
+// plain float sum of the high parts (24 bits of D) left 1e-5 of noise in it;
+// this form keeps the sum to 24 bits of itself.
+__device__ __forceinline__ float cn_lap1(fpair p, fpair m, fpair c) {
+    float s, e;
+    two_sum(p.h, m.h, s, e);
+    return (s - 2.0f * c.h) + (e + ((p.l + m.l) - 2.0f * c.l));
+}
+
+// The Jacobi update of D at bulk point o from its neighbours along each axis:
+// corr = (N0 - D + sum_d k1 c_d (p_d + m_d - 2 D)) / Dn.
+__device__ __forceinline__ fpair cn_delta_update(const CnDelta &a, long o, fpair D, fpair xp, fpair xm, fpair yp, fpair ym, fpair zp,
+                                                 fpair zm, fpair &corr) {
+    float q = fmaf(a.f.kf[0], cn_lap1(xp, xm, D), fmaf(a.f.kf[1], cn_lap1(yp, ym, D), a.f.kf[2] * cn_lap1(zp, zm, D)));
     fpair num = fp_add(fp_add(fpair{a.n0h[o], a.n0l[o]}, fp_neg(D)), fpair{q, 0.0f});
     corr = fp_mul(num, a.f.invDn);
     return fp_add(D, corr);
+}
+
+__device__ __forceinline__ fpair cn_d(const CnDelta &a, long o) { return fpair{a.dh[o], a.dl[o]}; }
+
+// D + corr at bulk point o.
+__device__ __forceinline__ fpair cn_delta_image(const CnDelta &a, long o, fpair &corr) {
+    return cn_delta_update(a, o, cn_d(a, o), cn_d(a, o + a.sx), cn_d(a, o - a.sx), cn_d(a, o + a.sy), cn_d(a, o - a.sy), cn_d(a, o + 1),
+                           cn_d(a, o - 1), corr);
 }
 
 __device__ __forceinline__ fpair fp_of_c(double x) {
@@ -707,25 +730,34 @@ __device__ __forceinline__ fpair fp_of_c(double x) {
 
 // Boundary point (i, j, k): the program resolved on C0 + D in float pairs (the
 // FP64 form's bc_resolve with base = Jacobi image at bulk points, 0 elsewhere),
-// minus C0 there.
+// minus C0 there.  A chain of copies (periodic images, no reflection or
+// constant) gives D(source) + (C0(source) - C0(here)): exactly D(source) when
+// C0 holds exact copies there, so the field's copied ghosts stay exact copies
+// of their sources, as the FP64 form's are.
 __device__ __forceinline__ fpair cn_delta_boundary(const CnDelta &a, int i, int j, int k, long o) {
     const BcProgram &prog = a.prog;
     int chain[kMaxBcOps];
     int nchain = 0;
     fpair value = fpair{0.0f, 0.0f};
-    bool haveConst = false;
+    bool haveConst = false, reflects = false;
     int q[3] = {i, j, k};
     for (int op = prog.nops - 1; op >= 0; --op) {
         const BcOp &b = prog.op[op];
         if (q[0] < b.lo[0] || q[0] > b.hi[0] || q[1] < b.lo[1] || q[1] > b.hi[1] || q[2] < b.lo[2] || q[2] > b.hi[2]) continue;
         if (b.kind == OP_CONST) { value = fp_of_c(b.c); haveConst = true; break; }
         chain[nchain++] = op;
+        reflects = reflects || b.kind == OP_REFLECT;
         q[0] += b.shift[0]; q[1] += b.shift[1]; q[2] += b.shift[2];
     }
     if (!haveConst && in_box(prog.blo, prog.bhi, q[0], q[1], q[2])) {
         long os = a.off(q[0], q[1], q[2]);
         fpair corr;
-        value = fp_add(fp_of(a.C0[os]), cn_delta_image(a, os, corr));
+        fpair d = cn_delta_image(a, os, corr);
+        if (!reflects) {
+            fpair z = fp_add(fp_of(a.C0[os]), fp_neg(fp_of(a.C0[o])));
+            return (z.h == 0.0f && z.l == 0.0f) ? d : fp_add(d, z);
+        }
+        value = fp_add(fp_of(a.C0[os]), d);
     }
     for (int cix = nchain - 1; cix >= 0; --cix) {
         const BcOp &b = prog.op[chain[cix]];
@@ -751,21 +783,16 @@ __global__ void __launch_bounds__(256) k_cn_delta(CnDelta a) {
             // a whole segment of bulk points: branch-free, the column's own i-1 / i / i+1
             // high parts carried in registers, every load of the segment in flight together
             long o = a.off(i0, j, k);
-            float hm = a.dh[o - a.sx], hc = a.dh[o];
+            fpair dm = cn_d(a, o - a.sx), dc = cn_d(a, o);
 #pragma unroll
             for (int q = 0; q < kCnMarch; ++q, o += a.sx) {
-                float hp = a.dh[o + a.sx];
-                fpair D = fpair{hc, a.dl[o]};
-                float d2 = 2.0f * hc;
-                float qq = fmaf(a.f.kf[0], (hp + hm) - d2,
-                                fmaf(a.f.kf[1], (a.dh[o + a.sy] + a.dh[o - a.sy]) - d2, a.f.kf[2] * ((a.dh[o + 1] + a.dh[o - 1]) - d2)));
-                fpair num = fp_add(fp_add(fpair{a.n0h[o], a.n0l[o]}, fp_neg(D)), fpair{qq, 0.0f});
-                fpair corr = fp_mul(num, a.f.invDn);
-                fpair out = fp_add(D, corr);
+                fpair dp = cn_d(a, o + a.sx);
+                fpair corr;
+                fpair out = cn_delta_update(a, o, dc, dp, dm, cn_d(a, o + a.sy), cn_d(a, o - a.sy), cn_d(a, o + 1), cn_d(a, o - 1), corr);
                 m = max(m, __float_as_uint(corr.h) & 0x7fffffffu);
                 cn_delta_store<FINAL>(a, o, out);
-                hm = hc;
-                hc = hp;
+                dm = dc;
+                dc = dp;
             }
             iend = i0;   // segment done (the generic loop below runs no iteration)
         }

@@ -1158,13 +1158,15 @@ __global__ void __launch_bounds__(256) k_tgt_rhs(View3<double> b, View3<const do
 // (k_tgt_sweep, k_tgt_residual, k_mg_restrict, k_mg_prolong_add), and writes
 // the level-Lt iterate with its face-ghost images to global memory.
 constexpr int kTailMaxLevels = 8;
+constexpr int kTailMaxSweeps = 16;
 constexpr int kTailThreads = 1024;
 
 template <typename T>
 struct TailArgs {
     int nl;                          // levels in the tail: Lt .. Lt + nl - 1 (the coarsest)
     MgBC bc[kTailMaxLevels];
-    TgK<T> tk[kTailMaxLevels];       // sweep constants (damped Jacobi)
+    TgK<T> tk[kTailMaxLevels];       // sweep constants at weight 1 (scaled per sweep by wpre / wpost)
+    T wpre[kTailMaxSweeps], wpost[kTailMaxSweeps];   // sweep weights (smooth_weight)
     TgK<T> tr[kTailMaxLevels];       // residual constants (weight 1)
     MgK kkc;                         // coarsest level (Gauss-Seidel)
     const T *M;                      // coarsest solution operator (nM x nM), or null: Gauss-Seidel
@@ -1206,6 +1208,15 @@ __device__ __forceinline__ bool near_face(int i, int j, int k, const MgBC &bc) {
     return i <= 1 || j <= 1 || k <= 1 || i >= bc.E[0] - 1 || j >= bc.E[1] - 1 || k >= bc.E[2] - 1;
 }
 
+// The sweep constants at weight w from those at weight 1.
+template <typename T>
+__device__ __forceinline__ TgK<T> tgk_weight(const TgK<T> &c1, T w) {
+    TgK<T> c = c1;
+    c.ax = w * c1.ax; c.ay = w * c1.ay; c.az = w * c1.az; c.ar = w * c1.ar;
+    c.om1 = (T)1 - w;
+    return c;
+}
+
 template <typename T, bool ZERO>
 __device__ void tail_sweep(T *out, const T *in, const T *r, const MgBC &bc, const TgK<T> &c) {
     const int E1 = bc.E[1], E2 = bc.E[2], sy = E2 + 3, sx = (E1 + 3) * sy;
@@ -1241,8 +1252,9 @@ __global__ void __launch_bounds__(kTailThreads) k_mg_tail(TailArgs<T> a) {
         int E1 = bc.E[1], E2 = bc.E[2], sy = E2 + 3, sx = (E1 + 3) * sy;
         // pre-smoothing from zero (the first sweep ignores its input)
         for (int n = 0; n < a.pre; ++n) {
-            if (n == 0) tail_sweep<T, true>(Q[l], P[l], R[l], bc, a.tk[l]);
-            else tail_sweep<T, false>(Q[l], P[l], R[l], bc, a.tk[l]);
+            const TgK<T> cw = tgk_weight(a.tk[l], a.wpre[n]);
+            if (n == 0) tail_sweep<T, true>(Q[l], P[l], R[l], bc, cw);
+            else tail_sweep<T, false>(Q[l], P[l], R[l], bc, cw);
             T *x = P[l]; P[l] = Q[l]; Q[l] = x;
         }
         // residual into Q (core), then full-weighting restriction (k_tgt_restrict's
@@ -1356,7 +1368,7 @@ __global__ void __launch_bounds__(kTailThreads) k_mg_tail(TailArgs<T> a) {
         });
         __syncthreads();
         for (int m = 0; m < a.post; ++m) {
-            tail_sweep<T, false>(Q[l], P[l], R[l], bc, a.tk[l]);
+            tail_sweep<T, false>(Q[l], P[l], R[l], bc, tgk_weight(a.tk[l], a.wpost[m]));
             T *x = P[l]; P[l] = Q[l]; Q[l] = x;
         }
     }
@@ -1398,6 +1410,7 @@ static int chk(Ctx &c, const char *what) {
 // First level of the fused coarse tail (k_mg_tail), or -1: all axes at most 16
 // intervals, at least two levels, and every tail level in shared memory.
 static int tail_level(const Ctx &c) {
+    if (c.p.preSmooth > kTailMaxSweeps || c.p.postSmooth > kTailMaxSweeps) return -1;
     for (int l = 1; l < c.depth; ++l) {
         const Level &L = c.lv[l];
         if (std::max(L.n[0], std::max(L.n[1], L.n[2])) > 16) continue;
@@ -1584,6 +1597,23 @@ template <typename T> static void flip(Level &L);
 template <> void flip<double>(Level &L) { L.cur ^= 1; }
 template <> void flip<float>(Level &L) { L.cur32 ^= 1; }
 
+// Weight of sweep n of a target-mode smoothing phase of `count` sweeps.
+// Damped Jacobi: jacobiWeight throughout.  Chebyshev (smoother = 1): the phase
+// is the degree-count Chebyshev polynomial of D^-1 A (its spectrum is in
+// [0, 2] for the mirror / periodic 7-point Laplacian) that is smallest on the
+// modes the coarse grid cannot represent, lambda in [1/3, 2]: sweep n has the
+// weight 1 / lambda_n for a root lambda_n of that polynomial.  The roots are
+// taken alternately from the two ends of the interval, which keeps the
+// intermediate iterates' growth small.  For 4 sweeps the polynomial is below
+// 0.062 on [1/3, 2]; damped Jacobi with weight 6/7 gives (5/7)^4 = 0.26.
+static double smooth_weight(const Ctx &c, int n, int count) {
+    if (c.p.smoother != 1 || count < 1) return c.p.jacobiWeight;
+    const double a = 1.0 / 3.0, b = 2.0;
+    int r = (n % 2 == 0) ? n / 2 : count - 1 - n / 2;   // 0, m-1, 1, m-2, ...
+    double lam = 0.5 * (b + a) + 0.5 * (b - a) * std::cos(M_PI * (2.0 * r + 1.0) / (2.0 * count));
+    return 1.0 / lam;
+}
+
 template <typename T>
 static int smooth(Ctx &c, int l, int count, bool zero_first, bool tgt) {
     Level &L = c.lv[l];
@@ -1593,10 +1623,10 @@ static int smooth(Ctx &c, int l, int count, bool zero_first, bool tgt) {
     T omega = tgt ? (T)c.p.jacobiWeight : (T)1.0;
     int pk = sizeof(T) == 8 ? PK_MG_SMOOTH64 : PK_MG_SMOOTH32;
     double bytes = 3.0 * sizeof(T) * (double)(L.n[0] + 1) * (L.n[1] + 1) * (L.n[2] + 1);
-    TgK<T> tk = make_tgk<T>(L, c.p.jacobiWeight);
     int sx = (L.n[1] + 3) * (L.n[2] + 3), sy = L.n[2] + 3;
     dim3 gm, bm; march_dims(L, gm, bm);
     for (int n = 0; n < count; ++n) {
+        TgK<T> tk = make_tgk<T>(L, tgt ? smooth_weight(c, n, count) : c.p.jacobiWeight);
         prof_begin(c, pk, l);
         const double lb = (n == 0 && zero_first) ? bytes * 2.0 / 3.0 : bytes;   // a zero start reads no iterate
         if (tgt) {
@@ -1693,7 +1723,7 @@ static int tail_run(Ctx &c, int Lt) {
     for (int q = 0; q < a.nl; ++q) {
         Level &L = c.lv[Lt + q];
         a.bc[q] = level_bc(c, Lt + q, true);
-        a.tk[q] = make_tgk<T>(L, c.p.jacobiWeight);
+        a.tk[q] = make_tgk<T>(L, 1.0);
         a.tr[q] = make_tgk<T>(L, 1.0);
         smem += 3 * sizeof(T) * (size_t)L.count;
     }
@@ -1703,8 +1733,12 @@ static int tail_run(Ctx &c, int Lt) {
     if (c.coarseN) a.M = sizeof(T) == 8 ? (const T *)c.coarseM64 : (const T *)c.coarseM32;
     a.tol = (T)1.0e-3;   // as coarse_solve in the target modes
     a.maxc = 500;
-    a.pre = c.p.preSmooth;
-    a.post = c.p.postSmooth;
+    a.pre = std::min(c.p.preSmooth, kTailMaxSweeps);
+    a.post = std::min(c.p.postSmooth, kTailMaxSweeps);
+    for (int n = 0; n < kTailMaxSweeps; ++n) {
+        a.wpre[n] = (T)smooth_weight(c, n, c.p.preSmooth);
+        a.wpost[n] = (T)smooth_weight(c, n, c.p.postSmooth);
+    }
     a.rin = R_<T>(c.lv[Lt]);
     a.pout = A_<T>(c.lv[Lt]);
     a.iters = (long long *)(c.dscal + 40);
