@@ -434,6 +434,7 @@ __device__ __forceinline__ void rhs3_point(const Rhs3Args &a, const float2 (*sm)
     a.H[C][o] = (a.f[C][o] + f2d(h.h)) + f2d(h.l);
     const CnDf &cf = a.cf[C];
     fpair n0 = fp_add(h, fp_add(fp_add(fp_mul(cf.kc[0], Sx), fp_mul(cf.kc[1], Sy)), fp_mul(cf.kc[2], Sz)));
+    n0 = fp_mul(n0, cf.invDn);   // A = N0 / Dn: the Jacobi solve's first iterate from D = 0
     a.n0h[C][o] = n0.h;
     a.n0l[C][o] = n0.l;
 }
@@ -647,7 +648,7 @@ static CnDf cn_df_consts(const CnFast &fa) {
     return d;
 }
 
-// N0 at the bulk points of the field's full box.
+// A = N0 / Dn at the bulk points of the field's full box.
 __global__ void __launch_bounds__(256) k_cn_pack(View3<const double> V, View3<const double> rhs, BcProgram prog, Box full, CnDf f,
                                                  float *n0h, float *n0l) {
     int i, j, k;
@@ -658,6 +659,7 @@ __global__ void __launch_bounds__(256) k_cn_pack(View3<const double> V, View3<co
     fpair sz = fp_add(fp_add(fp_of(V(i, j, k + 1)), fp_of(V(i, j, k - 1))), c2);
     fpair q = fp_add(fp_add(fp_mul(f.kc[0], sx), fp_mul(f.kc[1], sy)), fp_mul(f.kc[2], sz));
     fpair n = fp_add(fp_of(rhs(i, j, k) - V(i, j, k)), q);   // rhs - C0 in FP64: both O(1), the difference small
+    n = fp_mul(n, f.invDn);                                  // stored as A = N0 / Dn (the first sweep from D = 0)
     long o = V.off(i, j, k);
     n0h[o] = n.h;
     n0l[o] = n.l;
@@ -704,12 +706,12 @@ __device__ __forceinline__ float cn_lap1(fpair p, fpair m, fpair c) {
 }
 
 // The Jacobi update of D at bulk point o from its neighbours along each axis:
-// corr = (N0 - D + sum_d k1 c_d (p_d + m_d - 2 D)) / Dn.
+// corr = (N0 - D + sum_d k1 c_d (p_d + m_d - 2 D)) / Dn, with A = N0 / Dn stored
+// (the first iterate from D = 0, which the right-hand-side kernel writes).
 __device__ __forceinline__ fpair cn_delta_update(const CnDelta &a, long o, fpair D, fpair xp, fpair xm, fpair yp, fpair ym, fpair zp,
                                                  fpair zm, fpair &corr) {
     float q = fmaf(a.f.kf[0], cn_lap1(xp, xm, D), fmaf(a.f.kf[1], cn_lap1(yp, ym, D), a.f.kf[2] * cn_lap1(zp, zm, D)));
-    fpair num = fp_add(fp_add(fpair{a.n0h[o], a.n0l[o]}, fp_neg(D)), fpair{q, 0.0f});
-    corr = fp_mul(num, a.f.invDn);
+    corr = fp_add(fpair{a.n0h[o], a.n0l[o]}, fp_mul(fp_add(fpair{q, 0.0f}, fp_neg(D)), a.f.invDn));
     return fp_add(D, corr);
 }
 
@@ -734,6 +736,7 @@ __device__ __forceinline__ fpair fp_of_c(double x) {
 // constant) gives D(source) + (C0(source) - C0(here)): exactly D(source) when
 // C0 holds exact copies there, so the field's copied ghosts stay exact copies
 // of their sources, as the FP64 form's are.
+template <bool COPY>
 __device__ __forceinline__ fpair cn_delta_boundary(const CnDelta &a, int i, int j, int k, long o) {
     const BcProgram &prog = a.prog;
     int chain[kMaxBcOps];
@@ -752,7 +755,7 @@ __device__ __forceinline__ fpair cn_delta_boundary(const CnDelta &a, int i, int 
     if (!haveConst && in_box(prog.blo, prog.bhi, q[0], q[1], q[2])) {
         long os = a.off(q[0], q[1], q[2]);
         fpair corr;
-        fpair d = cn_delta_image(a, os, corr);
+        fpair d = COPY ? cn_d(a, os) : cn_delta_image(a, os, corr);
         if (!reflects) {
             fpair z = fp_add(fp_of(a.C0[os]), fp_neg(fp_of(a.C0[o])));
             return (z.h == 0.0f && z.l == 0.0f) ? d : fp_add(d, z);
@@ -811,7 +814,10 @@ __global__ void __launch_bounds__(256) k_cn_delta(CnDelta a) {
 // The non-bulk points of the full box (the boundary program's targets), as six
 // disjoint slabs: along axis d the points below / above the bulk range, with the
 // axes before d restricted to the bulk range and the axes after d full.
-template <bool FINAL>
+// COPY: no Jacobi update -- the non-bulk points of D (in place in dh / dl)
+// from the current D at their sources: the boundary values of the first
+// iterate A, which the right-hand-side kernel writes on the bulk only.
+template <bool FINAL, bool COPY>
 __global__ void k_cn_delta_shell(CnDelta a) {
     int s = blockIdx.y, d = s >> 1;
     int lo[3], hi[3];
@@ -827,7 +833,7 @@ __global__ void k_cn_delta_shell(CnDelta a) {
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         int r = t / n2, k = lo[2] + (t - r * n2), q = r / n1, j = lo[1] + (r - q * n1), i = lo[0] + q;
         long o = a.off(i, j, k);
-        cn_delta_store<FINAL>(a, o, cn_delta_boundary(a, i, j, k, o));
+        cn_delta_store<FINAL>(a, o, cn_delta_boundary<COPY>(a, i, j, k, o));
     }
 }
 
@@ -1470,7 +1476,6 @@ static int cn_solve_delta(Ctx &c, int comp, int field, const CnFast &fa, double 
         count_launch(c);
     }
     c.n0Fresh[comp] = 0;
-    SARAS_CUDA_TRY(cudaMemsetAsync(dA, 0, sizeof(float) * 2 * (size_t)N, c.stream));
     CnDelta d;
     d.C0 = V.p;
     d.n0h = n0h; d.n0l = n0l;
@@ -1480,21 +1485,31 @@ static int cn_solve_delta(Ctx &c, int comp, int field, const CnFast &fa, double 
     d.f = fd;
     d.resMax = c.dscal;
     d.vout = nullptr;
-    float *cur[2] = {dA, dAl}, *nxt[2] = {dB, dBl};
+    d.withResidual = 0;
+    // The first iterate from D = 0 is A = N0 / Dn itself (on the bulk, written with
+    // N0): its non-bulk points from their boundary-program sources, in place.
+    d.dh = d.oh = n0h;
+    d.dl = d.ol = n0l;
+    k_cn_delta_shell<false, true><<<dim3(64, 6), 256, 0, c.stream>>>(d);
+    count_launch(c);
+    // The iterates: A (read only), then alternately P and Q.
+    float *const bufs[3][2] = {{n0h, n0l}, {dA, dAl}, {dB, dBl}};
+    int cur = 0, nxt = 1;
+    auto advance = [&]() { int w = nxt; nxt = (w == 1) ? 2 : 1; cur = w; };
     dim3 gm((fa.full.ext[2] + 31) / 32, (fa.full.ext[1] + 7) / 8, (fa.full.ext[0] + kCnMarch - 1) / kCnMarch), bm(32, 8, 1);
     // vout: a final sweep, which writes C0 + D into vout (the field's scratch partner)
     // instead of D, the sum k_cn_unpack would form
     auto launch = [&](int withRes, double *vout) {
-        d.dh = cur[0]; d.dl = cur[1]; d.oh = nxt[0]; d.ol = nxt[1];
+        d.dh = bufs[cur][0]; d.dl = bufs[cur][1]; d.oh = bufs[nxt][0]; d.ol = bufs[nxt][1];
         d.withResidual = withRes;
         d.vout = vout;
         prof_begin(c, PK_CN, 0);
         if (vout) {
             k_cn_delta<true><<<gm, bm, 0, c.stream>>>(d);
-            k_cn_delta_shell<true><<<dim3(64, 6), 256, 0, c.stream>>>(d);
+            k_cn_delta_shell<true, false><<<dim3(64, 6), 256, 0, c.stream>>>(d);
         } else {
             k_cn_delta<false><<<gm, bm, 0, c.stream>>>(d);
-            k_cn_delta_shell<false><<<dim3(64, 6), 256, 0, c.stream>>>(d);
+            k_cn_delta_shell<false, false><<<dim3(64, 6), 256, 0, c.stream>>>(d);
         }
         count_launch(c, 2);
         prof_end(c, PK_CN, 0, vout ? bytes * 4.0 / 3.0 : bytes);
@@ -1514,7 +1529,7 @@ static int cn_solve_delta(Ctx &c, int comp, int field, const CnFast &fa, double 
     // that bound is below the tolerance, the sweep that would only confirm it is
     // skipped.
     const double rho = 1.0 - 1.0 / Dn;
-    int sweeps = 0, failed = 0, status = SARAS_OK;
+    int sweeps = 1, failed = 0, status = SARAS_OK;   // sweep 1 (from D = 0) is A
     double res = 0;
     bool inField = false;   // the answer is already in the field (a final sweep was accepted)
     // Speculative final sweep: the sweeps the previous solve of this component
@@ -1523,11 +1538,11 @@ static int cn_solve_delta(Ctx &c, int comp, int field, const CnFast &fa, double 
     // unpack pass); if its own residual does, the previous iterate is, as in the
     // loop below; otherwise the loop resumes from that previous iterate.
     int slot = scratch_slot(field);
-    int spec = slot >= 0 ? std::max(1, c.cnSweeps[comp]) : 0;
+    int spec = slot >= 0 ? std::max(2, c.cnSweeps[comp]) : 0;
     if (spec > 0) {
-        for (int q = 1; q < spec; ++q) {
+        for (int q = 2; q < spec; ++q) {
             launch(0, nullptr);
-            std::swap(cur, nxt);
+            advance();
             sweeps += 1;
         }
         SARAS_CUDA_TRY(cudaMemsetAsync(c.dscal, 0, sizeof(double), c.stream));
@@ -1550,11 +1565,6 @@ static int cn_solve_delta(Ctx &c, int comp, int field, const CnFast &fa, double 
         }
     }
     if (status == SARAS_OK && spec >= 0) {
-        if (sweeps == 0) {
-            launch(0, nullptr);
-            std::swap(cur, nxt);
-            sweeps = 1;
-        }
         while (true) {
             SARAS_CUDA_TRY(cudaMemsetAsync(c.dscal, 0, sizeof(double), c.stream));
             launch(1, nullptr);
@@ -1564,7 +1574,7 @@ static int cn_solve_delta(Ctx &c, int comp, int field, const CnFast &fa, double 
             if (res < c.p.cnTolerance) { c.cnSweeps[comp] = sweeps + 1; break; }   // cur is the answer
             double bound = res * rho * 1.01;
             if (bound < c.p.cnTolerance) {
-                std::swap(cur, nxt);
+                advance();
                 sweeps += 1;
                 res = bound;
                 c.cnSweeps[comp] = sweeps;
@@ -1572,13 +1582,13 @@ static int cn_solve_delta(Ctx &c, int comp, int field, const CnFast &fa, double 
             }
             failed += 1;
             if (failed > c.maxIterations) { status = SARAS_NOT_CONVERGED; break; }
-            std::swap(cur, nxt);
+            advance();
             sweeps += 1;
         }
     }
     // the field becomes C0 + D (also on failure, as the FP64 form leaves its last iterate)
     if (!inField) {
-        k_cn_unpack<<<std::min<long>((n + 255) / 256, 152L * 16), 256, 0, c.stream>>>(V.p, cur[0], cur[1], n);
+        k_cn_unpack<<<std::min<long>((n + 255) / 256, 152L * 16), 256, 0, c.stream>>>(V.p, bufs[cur][0], bufs[cur][1], n);
         count_launch(c);
         int s = check_launch(c, "cn unpack");
         if (s) return s;
