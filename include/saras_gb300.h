@@ -125,6 +125,9 @@ typedef struct saras_params {
                                  is the degree-n Chebyshev polynomial of D^-1 A
                                  on [1/3, 2], applied as n Jacobi sweeps with
                                  the weights 1 / (its roots) (n <= 16)          */
+    int coarseSmooth;         /* target modes: sweeps per smoothing phase on the
+                                 levels below the finest (0: preSmooth /
+                                 postSmooth, as on the finest level)           */
 } saras_params;
 
 typedef struct saras_step_stats {

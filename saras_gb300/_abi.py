@@ -60,6 +60,7 @@ class saras_params(ctypes.Structure):
         ("seed", _I),
         ("fastKernels", _I),
         ("smoother", _I),
+        ("coarseSmooth", _I),
     ]
 
     def to_dict(self):
@@ -101,6 +102,7 @@ def default_params():
     p.jacobiWeight, p.seed = 1.0, 42
     p.fastKernels = 0
     p.smoother = SMOOTHER_JACOBI
+    p.coarseSmooth = 0
     return p
 
 

@@ -219,7 +219,8 @@ int saras_parse_yaml(const char *path, saras_params *p, char *err, int errlen) {
                  {"Multigrid/Post-Smoothing Count", &p->postSmooth}, {"Multigrid/Residual Type", &p->resType},
                  {"GB300/Multigrid Mode", &p->mgMode}, {"GB300/Max V-Cycles", &p->mgMaxCycles},
                  {"GB300/Mixed Inner Cycles", &p->mixedCycles}, {"GB300/Guess Mode", &p->guessMode}, {"GB300/Seed", &p->seed},
-                 {"GB300/Fast Kernels", &p->fastKernels}, {"GB300/Smoother", &p->smoother}};
+                 {"GB300/Fast Kernels", &p->fastKernels}, {"GB300/Smoother", &p->smoother},
+                 {"GB300/Coarse Smoothing Count", &p->coarseSmooth}};
     DK dbls[] = {{"Program/Reynolds Number", &p->Re}, {"Program/Rossby Number", &p->Ro}, {"Program/Rayleigh Number", &p->Ra},
                  {"Program/Prandtl Number", &p->Pr}, {"Program/Taylor Number", &p->Ta}, {"Program/X Length", &p->Lx},
                  {"Program/Y Length", &p->Ly}, {"Program/Z Length", &p->Lz}, {"Program/Plate Radius", &p->patchRadius},
@@ -275,7 +276,11 @@ static int validate(const saras_params *p, std::string &why) {
     if (p->guessMode < SARAS_GUESS_PREVIOUS || p->guessMode > SARAS_GUESS_PARITY) { why = "bad guess mode"; return SARAS_BAD_CONFIG; }
     if (p->fastKernels < 0 || p->fastKernels > 2) { why = "Fast Kernels must be 0, 1 or 2"; return SARAS_BAD_CONFIG; }
     if (p->smoother < 0 || p->smoother > 1) { why = "Smoother must be 0 (Jacobi) or 1 (Chebyshev)"; return SARAS_BAD_CONFIG; }
-    if (p->smoother == 1 && (p->preSmooth > 16 || p->postSmooth > 16)) { why = "Chebyshev smoothing takes at most 16 sweeps a phase"; return SARAS_BAD_CONFIG; }
+    if (p->smoother == 1 && (p->preSmooth > 16 || p->postSmooth > 16 || p->coarseSmooth > 16)) {
+        why = "Chebyshev smoothing takes at most 16 sweeps a phase";
+        return SARAS_BAD_CONFIG;
+    }
+    if (p->coarseSmooth < 0) { why = "negative Coarse Smoothing Count"; return SARAS_BAD_CONFIG; }
     if (p->resType < 0 || p->resType > 2) { why = "bad residual type"; return SARAS_BAD_CONFIG; }
     return SARAS_OK;
 }

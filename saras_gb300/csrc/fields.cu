@@ -439,7 +439,7 @@ __device__ __forceinline__ void rhs3_point(const Rhs3Args &a, const float2 (*sm)
     a.n0l[C][o] = n0.l;
 }
 
-__global__ void __launch_bounds__(256) k_rhs_df3(Rhs3Args a) {
+__global__ void __launch_bounds__(256, 5) k_rhs_df3(Rhs3Args a) {
     __shared__ float2 sm[4][4][kR3N];
     const int tid = threadIdx.y * 32 + threadIdx.x;
     const int k0 = blockIdx.x * 32, j0 = blockIdx.y * 8, i0 = blockIdx.z * kRhs3March;
@@ -774,7 +774,7 @@ __device__ __forceinline__ fpair cn_delta_boundary(const CnDelta &a, int i, int 
 constexpr int kCnMarch = 8;
 
 template <bool FINAL>
-__global__ void __launch_bounds__(256) k_cn_delta(CnDelta a) {
+__global__ void __launch_bounds__(256, 5) k_cn_delta(CnDelta a) {
     int k = a.full.lo[2] + blockIdx.x * 32 + threadIdx.x;
     int j = a.full.lo[1] + blockIdx.y * 8 + threadIdx.y;
     int i0 = a.full.lo[0] + blockIdx.z * kCnMarch;

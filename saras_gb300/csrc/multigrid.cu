@@ -919,6 +919,19 @@ __global__ void __launch_bounds__(256) k_tgt_update(double *__restrict__ p, cons
 // k_fx_refine: the residual of P; r32 receives r in FP32 (the next V-cycle's
 // right-hand side), maxr the block maxima of |B - ...| in integer units.
 // Neighbours at the faces are read at their core images (nbr_jk, nbr_x).
+// P rounded to the 53 significant bits of an FP64 value (to nearest, ties to
+// even): the fixed-point value of the FP64 number P 2^-s that k_fx_output
+// writes (the scaling by 2^-s is exact), from integer operations only.
+__device__ __forceinline__ long long round53(long long p) {
+    unsigned long long a = p < 0 ? 0ull - (unsigned long long)p : (unsigned long long)p;
+    if (a < (1ull << 53)) return p;
+    int sh = 11 - __clzll((long long)a);   // bits below the 53 kept: 64 - clz - 53
+    unsigned long long low = a & ((1ull << sh) - 1), half = 1ull << (sh - 1), q = a >> sh;
+    if (low > half || (low == half && (q & 1ull))) q += 1;
+    a = q << sh;
+    return p < 0 ? -(long long)a : (long long)a;
+}
+
 __global__ void __launch_bounds__(256) k_fx_refine(const long long *__restrict__ pin, const long long *__restrict__ bfx,
                                                    float *__restrict__ r32, int sx, int sy, MgBC bc, float rscale,
                                                    unsigned long long *maxr) {
@@ -935,7 +948,7 @@ __global__ void __launch_bounds__(256) k_fx_refine(const long long *__restrict__
             long long cp = pin[o + (i < bc.E[0] ? (long)sx : nbr_x(i, 1, sx, bc))];
             long long nsum = (cm + cp) + (pin[o + nb.yp] + pin[o + nb.ym]) + (pin[o + nb.zp] + pin[o + nb.zm]);
             long long r = bfx[o] - (nsum - 6 * cc);
-            r32[o] = fx2f(r) * rscale;
+            if (r32) r32[o] = fx2f(r) * rscale;
             unsigned long long a = (unsigned long long)(r < 0 ? -r : r);
             m = a > m ? a : m;
             cm = cc;
@@ -1051,25 +1064,25 @@ __global__ void k_fx_init(long long *__restrict__ dst, View3<const double> src, 
 // mapping, target modes: periodic or mirror per axis), converted once to FP64;
 // chk receives round(Pp 2^s), the FP64 result back in fixed point, whose exact
 // residual is the residual of what the solve returns.
-__global__ void k_fx_output(double *__restrict__ dst, long long *__restrict__ chk, const long long *__restrict__ src, MgBC bc,
-                            double inv2s, int s, int *flag) {
-    int E1 = bc.E[1], E2 = bc.E[2];
-    long sy = E2 + 3, sx = (long)(E1 + 3) * sy;
-    long n = (long)(bc.E[0] + 3) * sx;
-    bool bad = false;
-    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
-        int q[3] = {(int)(t / sx) - 1, (int)((t / sy) % (E1 + 3)) - 1, (int)(t % sy) - 1};
-        for (int d = 2; d >= 0; --d) {
-            int E = bc.E[d];
-            if (q[d] >= 0 && q[d] <= E) continue;
-            if (bc.per[d]) q[d] = q[d] < 0 ? E - 1 : 1;
-            else q[d] = q[d] < 0 ? 1 : E - 1;
-        }
-        double x = __ll2double_rn(src[(q[0] + 1) * sx + (q[1] + 1) * sy + (q[2] + 1)]) * inv2s;
-        dst[t] = x;
-        chk[t] = d2fx(x, s, bad);
+// Pp = P 2^-s over the whole padded array (face ghosts: their images), and
+// chk = the fixed-point value of that FP64 number (round53 of P) for the check
+// of the output; one thread per point of a (k, j) row, blockIdx.z the plane.
+__global__ void k_fx_output(double *__restrict__ dst, long long *__restrict__ chk, const long long *__restrict__ src, MgBC bc, double inv2s) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x - 1, j = blockIdx.y * blockDim.y + threadIdx.y - 1, i = blockIdx.z - 1;
+    const int E1 = bc.E[1], E2 = bc.E[2];
+    if (j > E1 + 1 || k > E2 + 1) return;
+    const long sy = E2 + 3, sx = (long)(E1 + 3) * sy;
+    int q[3] = {i, j, k};
+    for (int d = 2; d >= 0; --d) {
+        int E = bc.E[d];
+        if (q[d] >= 0 && q[d] <= E) continue;
+        if (bc.per[d]) q[d] = q[d] < 0 ? E - 1 : 1;
+        else q[d] = q[d] < 0 ? 1 : E - 1;
     }
-    if (bad) atomicExch(flag, 1);
+    const long o = (i + 1) * sx + (j + 1) * sy + (k + 1);
+    const long long p = src[(q[0] + 1) * sx + (q[1] + 1) * sy + (q[2] + 1)];
+    dst[o] = __ll2double_rn(p) * inv2s;
+    chk[o] = round53(p);
 }
 
 // dst = round(src 2^s) over a whole padded array (face-ghost images included).
@@ -1410,7 +1423,7 @@ static int chk(Ctx &c, const char *what) {
 // First level of the fused coarse tail (k_mg_tail), or -1: all axes at most 16
 // intervals, at least two levels, and every tail level in shared memory.
 static int tail_level(const Ctx &c) {
-    if (c.p.preSmooth > kTailMaxSweeps || c.p.postSmooth > kTailMaxSweeps) return -1;
+    if (c.p.preSmooth > kTailMaxSweeps || c.p.postSmooth > kTailMaxSweeps || c.p.coarseSmooth > kTailMaxSweeps) return -1;
     for (int l = 1; l < c.depth; ++l) {
         const Level &L = c.lv[l];
         if (std::max(L.n[0], std::max(L.n[1], L.n[2])) > 16) continue;
@@ -1715,6 +1728,13 @@ static int prolong_level(Ctx &c, int l, bool tgt, bool add) {
     return chk(c, "mg prolong");
 }
 
+// Sweeps of a smoothing phase below the finest level: coarseSmooth in the
+// target modes when set, else the phase's count on the finest level.
+static int coarse_sweeps(const Ctx &c, bool tgt, bool pre) {
+    if (tgt && c.p.coarseSmooth > 0) return c.p.coarseSmooth;
+    return pre ? c.p.preSmooth : c.p.postSmooth;
+}
+
 template <typename T>
 static int tail_run(Ctx &c, int Lt) {
     TailArgs<T> a;
@@ -1733,11 +1753,12 @@ static int tail_run(Ctx &c, int Lt) {
     if (c.coarseN) a.M = sizeof(T) == 8 ? (const T *)c.coarseM64 : (const T *)c.coarseM32;
     a.tol = (T)1.0e-3;   // as coarse_solve in the target modes
     a.maxc = 500;
-    a.pre = std::min(c.p.preSmooth, kTailMaxSweeps);
-    a.post = std::min(c.p.postSmooth, kTailMaxSweeps);
+    int cpre = coarse_sweeps(c, true, true), cpost = coarse_sweeps(c, true, false);
+    a.pre = std::min(cpre, kTailMaxSweeps);
+    a.post = std::min(cpost, kTailMaxSweeps);
     for (int n = 0; n < kTailMaxSweeps; ++n) {
-        a.wpre[n] = (T)smooth_weight(c, n, c.p.preSmooth);
-        a.wpost[n] = (T)smooth_weight(c, n, c.p.postSmooth);
+        a.wpre[n] = (T)smooth_weight(c, n, cpre);
+        a.wpost[n] = (T)smooth_weight(c, n, cpost);
     }
     a.rin = R_<T>(c.lv[Lt]);
     a.pout = A_<T>(c.lv[Lt]);
@@ -1759,11 +1780,11 @@ static int vcycle(Ctx &c, bool tgt, bool zero0) {
         if ((s = restrict_level<T>(c, l, tgt))) return s;
         if (l + 1 == Lt) { if ((s = tail_run<T>(c, Lt))) return s; d = Lt; break; }
         if (l + 1 == d) { if ((s = coarse_solve<T>(c, tgt))) return s; }
-        else if ((s = smooth<T>(c, l + 1, c.p.preSmooth, true, tgt))) return s;
+        else if ((s = smooth<T>(c, l + 1, coarse_sweeps(c, tgt, true), true, tgt))) return s;
     }
     for (int l = d - 1; l >= 0; --l) {
         if ((s = prolong_level<T>(c, l, tgt, true))) return s;
-        if ((s = smooth<T>(c, l, c.p.postSmooth, false, tgt))) return s;
+        if ((s = smooth<T>(c, l, l > 0 ? coarse_sweeps(c, tgt, false) : c.p.postSmooth, false, tgt))) return s;
     }
     return SARAS_OK;
 }
@@ -2071,6 +2092,21 @@ static int mixed_fixed(Ctx &c, double bmax, double pmax, double target, bool wan
         bad = fl != 0;
         return SARAS_OK;
     };
+    // the exact residual of the FP64 output (chk = P rounded to FP64), max only
+    auto refine_out = [&](int q, double &out) -> int {
+        SARAS_CUDA_TRY(cudaMemsetAsync(c.dscal + 34, 0, sizeof(double), c.stream));
+        prof_begin(c, PK_REFINE_RESID, 0);
+        k_fx_refine<<<gm0, bm0, 0, c.stream>>>(c.fx[q], B, nullptr, sx0, sy0, bc0, (float)rs, dmax);
+        prof_end(c, PK_REFINE_RESID, 0, (8.0 + 8.0) * (double)L0.count);
+        count_launch(c);
+        int e = chk(c, "fixed-point output check");
+        if (e) return e;
+        unsigned long long mx = 0;
+        SARAS_CUDA_TRY(cudaMemcpyAsync(&mx, dmax, sizeof(mx), cudaMemcpyDeviceToHost, c.stream));
+        SARAS_CUDA_TRY(cudaStreamSynchronize(c.stream));
+        out = (double)mx * rs;
+        return SARAS_OK;
+    };
     bool bad = false;
     int built = 0;
     k_fx_init<<<gc, bcd, 0, c.stream>>>(c.fx[0], lcview<double>(L0, c.f[SARAS_FIELD_PP]), bc0, sc, dflag);
@@ -2118,11 +2154,13 @@ static int mixed_fixed(Ctx &c, double bmax, double pmax, double target, bool wan
         }
         if (bad) break;
         // the FP64 result, and the exact residual of those FP64 values
-        k_fx_output<<<nbF, 256, 0, c.stream>>>(c.f[SARAS_FIELD_PP], c.fx[cur ^ 1], c.fx[cur], bc0, inv2s, sc, dflag);
-        count_launch(c);
+        {
+            dim3 bo(64, 4, 1), go((L0.n[2] + 3 + 63) / 64, (L0.n[1] + 3 + 3) / 4, L0.n[0] + 3);
+            k_fx_output<<<go, bo, 0, c.stream>>>(c.f[SARAS_FIELD_PP], c.fx[cur ^ 1], c.fx[cur], bc0, inv2s);
+            count_launch(c);
+        }
         double rf = 0;
-        if ((s = refine(cur ^ 1, false, rf, bad))) return s;
-        if (bad) break;
+        if ((s = refine_out(cur ^ 1, rf))) return s;
         r = rf;
         cur ^= 1;
         if (r <= target || cyc >= c.mgMaxCycles) {
