@@ -48,15 +48,16 @@ def tgv_params(mode, guess=0, ind=GRID_INDEX, depth=DEPTH):
     p.tStp = DT
     p.cnTolerance = 1.0e-8
     p.mgTolerance = 1.0e-8
-    # both target-mode arms with the smoothing each is fastest with at 257^3:
-    # Chebyshev V(3,3); the plain FP64 arm with 8 sweeps a phase on the coarser
-    # levels (5 cycles, 24.1 ms a step, against 7 cycles and 27.0 ms with 3, and
-    # 8 cycles and 31.1 ms with damped-Jacobi V(3,3)); the mixed arm with 3
-    # there (3 cycles in one refinement step; more coarse sweeps leave it at 3
-    # cycles), refinement steps sized by the measured contraction per cycle
+    # both target-mode arms with the cycle each is fastest with at 257^3
+    # (ms a step): plain FP64 -- Chebyshev-smoothed cycles with 3 sweeps a phase
+    # and a W-cycle at the second level 23.6 (V-cycle 27.0, V-cycle with 8
+    # coarse sweeps 24.0, damped-Jacobi V(3,3) 31.1); mixed -- Chebyshev V(3,3)
+    # 5.40 (3 cycles in one refinement step; the W-cycle at the second level
+    # with 6 coarse sweeps needs 2 cycles but takes 5.62), refinement steps
+    # sized by the measured contraction per cycle
     p.preSmooth = p.postSmooth = 3
     p.smoother = _abi.SMOOTHER_CHEBYSHEV if mode != _abi.MG_REFERENCE else _abi.SMOOTHER_JACOBI
-    p.coarseSmooth = 8 if mode == _abi.MG_PLAIN_TARGET else 0
+    p.coarseCycles = 2 if mode == _abi.MG_PLAIN_TARGET else 1
     p.mgMode = mode
     p.mgTarget = TARGET
     p.mgMaxCycles = 100
@@ -339,7 +340,7 @@ def run_ours(args, dist):
             "workload": "Taylor-Green vortex 257^3 (2^8+1 vertex points per axis), [0,2pi]^3 PPP, Re 1600, dt 5e-4; "
                         "pressure solve: FP32 V(3,3) cycles (Chebyshev-weighted Jacobi smoothing) inside iterative refinement with an "
                         "exact fixed-point residual, refinement steps sized by the measured contraction per cycle, to "
-                        "max|b-Ap|/max|b| <= 1e-8; plain arm: FP64 V(3,3) cycles, same smoothing (8 sweeps a phase below the finest level), same residual",
+                        "max|b-Ap|/max|b| <= 1e-8; plain arm: FP64 cycles with the same smoothing and a W-cycle at the second level, same residual",
             "grid": [257, 257, 257], "vcycle_depth": DEPTH, "mg_mode": "mixed_fp32_in_fp64",
             "warm_start": "unet (3-level 16/32/64, tcgen05 BF16 convs) correcting 2 Pp(n-1) - Pp(n-2), "
                           "least-squares step length, fallback to the previous pressure"

@@ -128,6 +128,9 @@ typedef struct saras_params {
     int coarseSmooth;         /* target modes: sweeps per smoothing phase on the
                                  levels below the finest (0: preSmooth /
                                  postSmooth, as on the finest level)           */
+    int coarseCycles;         /* target modes: cycles on the second level per
+                                 visit of the finest (0 or 1: V-cycle; 2: a
+                                 W-cycle at the second level; at most 4)       */
 } saras_params;
 
 typedef struct saras_step_stats {

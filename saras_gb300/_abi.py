@@ -61,6 +61,7 @@ class saras_params(ctypes.Structure):
         ("fastKernels", _I),
         ("smoother", _I),
         ("coarseSmooth", _I),
+        ("coarseCycles", _I),
     ]
 
     def to_dict(self):
@@ -103,6 +104,7 @@ def default_params():
     p.fastKernels = 0
     p.smoother = SMOOTHER_JACOBI
     p.coarseSmooth = 0
+    p.coarseCycles = 0
     return p
 
 

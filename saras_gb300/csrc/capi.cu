@@ -220,7 +220,7 @@ int saras_parse_yaml(const char *path, saras_params *p, char *err, int errlen) {
                  {"GB300/Multigrid Mode", &p->mgMode}, {"GB300/Max V-Cycles", &p->mgMaxCycles},
                  {"GB300/Mixed Inner Cycles", &p->mixedCycles}, {"GB300/Guess Mode", &p->guessMode}, {"GB300/Seed", &p->seed},
                  {"GB300/Fast Kernels", &p->fastKernels}, {"GB300/Smoother", &p->smoother},
-                 {"GB300/Coarse Smoothing Count", &p->coarseSmooth}};
+                 {"GB300/Coarse Smoothing Count", &p->coarseSmooth}, {"GB300/Coarse Cycles", &p->coarseCycles}};
     DK dbls[] = {{"Program/Reynolds Number", &p->Re}, {"Program/Rossby Number", &p->Ro}, {"Program/Rayleigh Number", &p->Ra},
                  {"Program/Prandtl Number", &p->Pr}, {"Program/Taylor Number", &p->Ta}, {"Program/X Length", &p->Lx},
                  {"Program/Y Length", &p->Ly}, {"Program/Z Length", &p->Lz}, {"Program/Plate Radius", &p->patchRadius},
@@ -281,6 +281,7 @@ static int validate(const saras_params *p, std::string &why) {
         return SARAS_BAD_CONFIG;
     }
     if (p->coarseSmooth < 0) { why = "negative Coarse Smoothing Count"; return SARAS_BAD_CONFIG; }
+    if (p->coarseCycles < 0 || p->coarseCycles > 4) { why = "Coarse Cycles must be 0 to 4"; return SARAS_BAD_CONFIG; }
     if (p->resType < 0 || p->resType > 2) { why = "bad residual type"; return SARAS_BAD_CONFIG; }
     return SARAS_OK;
 }

@@ -1770,23 +1770,30 @@ static int tail_run(Ctx &c, int Lt) {
 
 // poisson::vCycle (poisson.cc:219-280) on level arrays of precision T.
 // zero0: the level-0 iterate starts at 0 (inner FP32 solve of the mixed mode).
+// A cycle from level l down (pre-smoothing, from zero when zero, restriction)
+// and back up (prolongation + add, post-smoothing); the levels from the fused
+// tail's first one run as that kernel.  gamma cycles on level l + 1 for each
+// visit of level l when l == 0 (gamma = 2: a W-cycle at level 1).
+template <typename T>
+static int cycle_from(Ctx &c, int l, bool tgt, bool zero, int gamma) {
+    int s;
+    int Lt = tgt ? c.tailLt : -1;   // target modes: levels Lt.. run as one fused kernel
+    if (l == Lt) return tail_run<T>(c, Lt);
+    if (l == c.depth) return coarse_solve<T>(c, tgt);
+    const int pre = l > 0 ? coarse_sweeps(c, tgt, true) : c.p.preSmooth;
+    const int post = l > 0 ? coarse_sweeps(c, tgt, false) : c.p.postSmooth;
+    if ((s = smooth<T>(c, l, pre, zero, tgt))) return s;
+    if ((s = restrict_level<T>(c, l, tgt))) return s;
+    const int g = l == 0 ? gamma : 1;
+    for (int q = 0; q < g; ++q)
+        if ((s = cycle_from<T>(c, l + 1, tgt, q == 0, 1))) return s;
+    if ((s = prolong_level<T>(c, l, tgt, true))) return s;
+    return smooth<T>(c, l, post, false, tgt);
+}
+
 template <typename T>
 static int vcycle(Ctx &c, bool tgt, bool zero0) {
-    int s;
-    int d = c.depth;
-    int Lt = tgt ? c.tailLt : -1;   // target modes: levels Lt.. run as one fused kernel
-    if ((s = smooth<T>(c, 0, c.p.preSmooth, zero0, tgt))) return s;
-    for (int l = 0; l < d; ++l) {
-        if ((s = restrict_level<T>(c, l, tgt))) return s;
-        if (l + 1 == Lt) { if ((s = tail_run<T>(c, Lt))) return s; d = Lt; break; }
-        if (l + 1 == d) { if ((s = coarse_solve<T>(c, tgt))) return s; }
-        else if ((s = smooth<T>(c, l + 1, coarse_sweeps(c, tgt, true), true, tgt))) return s;
-    }
-    for (int l = d - 1; l >= 0; --l) {
-        if ((s = prolong_level<T>(c, l, tgt, true))) return s;
-        if ((s = smooth<T>(c, l, l > 0 ? coarse_sweeps(c, tgt, false) : c.p.postSmooth, false, tgt))) return s;
-    }
-    return SARAS_OK;
+    return cycle_from<T>(c, 0, tgt, zero0, tgt ? std::max(1, c.p.coarseCycles) : 1);
 }
 
 // The target-mode V-cycle issues about ten kernels per level, most of them

@@ -59,6 +59,39 @@ def test_mixed_solve_v44_three_cycles():
     assert C.rel_err(m.get(F.FIELD_P), f.get(F.FIELD_P)) < 1e-7
 
 
+@pytest.mark.parametrize("smoother,coarse_smooth,coarse_cycles", [(0, 0, 1), (1, 0, 1), (1, 6, 1), (1, 0, 2), (1, 4, 2)])
+def test_cycle_shapes_reach_target(smoother, coarse_smooth, coarse_cycles):
+    """Every smoother / coarse-smoothing / coarse-cycle combination reaches the
+    residual target in both target modes, and the two modes' pressures agree;
+    the Chebyshev smoother needs no more cycles than damped Jacobi."""
+    out = {}
+    for mode in (F.MG_PLAIN_TARGET, F.MG_MIXED):
+        p = C.tgv(ind=5, depth=3, dt=5e-4)
+        p.mgMode = mode
+        p.mgTarget = 1e-8
+        p.mgMaxCycles = 100
+        p.jacobiWeight = 6.0 / 7.0
+        p.fastKernels = 2
+        p.smoother = smoother
+        p.coarseSmooth = coarse_smooth
+        p.coarseCycles = coarse_cycles
+        p.mixedCycles = 0
+        g = S.Solver(p)
+        C.initialise(g, p, "tgv")
+        cyc = 0
+        for _ in range(3):
+            s, st = g.time_advance()
+            assert s == 0 and st.fine_residual <= 1e-8
+            cyc += st.vcycles
+        out[mode] = (g.get(F.FIELD_P), cyc)
+        g.close()
+    assert C.rel_err(out[F.MG_MIXED][0], out[F.MG_PLAIN_TARGET][0]) < 1e-7
+    if smoother == 1 and coarse_smooth == 0 and coarse_cycles == 1:
+        _, jac = target_case(F.MG_PLAIN_TARGET, fast=2)
+        cj = sum(jac.time_advance()[1].vcycles for _ in range(3))
+        assert out[F.MG_PLAIN_TARGET][1] <= cj
+
+
 def test_profiling_inside_replayed_vcycles():
     """A profile slot enabled after the V-cycle graphs exist is recorded by
     event nodes inside the replayed graphs: one launch per level-0 sweep."""
