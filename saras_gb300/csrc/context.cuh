@@ -133,6 +133,7 @@ struct Ctx {
     long long vgraphLaunches[2][2] = {{0, 0}, {0, 0}};
     std::vector<int> vgraphState[2][2];
     int histCount = 0;
+    bool ppInHist = false;    // Pp's buffer moved to pHist[0] by unet_begin_solve; the solve has not written Pp yet
     bool collecting = false;
     // profiling
     ProfSlot prof[PK_COUNT];
@@ -186,7 +187,7 @@ int unet_collect(Ctx &c);
 int unet_train(Ctx &c, int iters, double lr, double *loss);
 int unet_infer(Ctx &c, double *out);
 int unet_begin_solve(Ctx &c);
-int unet_guess(Ctx &c, const double *b, double *dst, int mode);
+int unet_guess(Ctx &c, const double *b, double *dst, int mode, long long *fxdst = nullptr, int sc = 0, int *flag = nullptr);
 void vgraph_reset(Ctx &c);
 int prof_graph_replay(Ctx &c, cudaGraphExec_t ge, const std::vector<ProfNode> &nodes);
 int unet_pick(Ctx &c);

@@ -16,6 +16,7 @@
 #include <cstring>
 #include <vector>
 #include <algorithm>
+#include <type_traits>
 
 #include "context.cuh"
 #include "tc_conv.cuh"
@@ -326,9 +327,11 @@ __global__ void k_loss(const float *d, const float *dstar, bf16 *gout, long nv, 
 // Guess on level 0: 2 P1 - P2 (kind 1: 3 P1 - 3 P2 + P3, kind 2: P1 + P2 - P3) plus, with d, the
 // network correction alpha s_t P(d), P the trilinear interpolation from level
 // lb (repeated linear prolongation of vertex grids), at core points with the
-// face-ghost images.
-__global__ void k_apply_guess(double *out, L0View p1, L0View p2, L0View p3, int kind, const float *d, Grid3 g, int lb,
-                              const double *scales, const double *alpha, int per0, int per1, int per2) {
+// face-ghost images.  OT = long long: the guess goes straight into the
+// fixed-point iterate, round(v 2^s) (flag set when out of range).
+template <typename OT>
+__global__ void k_apply_guess(OT *out, L0View p1, L0View p2, L0View p3, int kind, const float *d, Grid3 g, int lb,
+                              const double *scales, const double *alpha, int per0, int per1, int per2, int s, int *flag) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y * blockDim.y + threadIdx.y;
     int i = blockIdx.z;
@@ -351,7 +354,15 @@ __global__ void k_apply_guess(double *out, L0View p1, L0View p2, L0View p3, int 
         v += (*alpha * scales[5]) * (double)(c0 + fz * (c1 - c0));
     }
     long sy = p1.n[2] + 3, sx = (long)(p1.n[1] + 3) * sy;
-    auto put = [&](int a, int b, int c) { out[(long)(a + 1) * sx + (long)(b + 1) * sy + (c + 1)] = v; };
+    OT w;
+    if constexpr (std::is_same<OT, long long>::value) {
+        bool bad = false;
+        w = d2fx(v, s, bad);
+        if (bad) atomicExch(flag, 1);
+    } else {
+        w = v;
+    }
+    auto put = [&](int a, int b, int c) { out[(long)(a + 1) * sx + (long)(b + 1) * sy + (c + 1)] = w; };
     put(i, j, k);
     int q[3] = {i, j, k};
     int per[3] = {per0, per1, per2};
@@ -480,6 +491,8 @@ struct UNet {
     double *tmp[2] = {nullptr, nullptr};     // intermediate levels 1 .. lb-1 of a restriction
     int nb = 0, np = 0;                      // consecutive solves with rb / rp pushed
     bool bPushed = false;                    // rb[0] holds this solve's b
+    bool track = false;                      // this solve pushes rb / rp
+    bool wantNet = false;                    // the network was picked before its rings were complete
     // V-cycles per solve with the network's guess and with plain extrapolation
     // (moving averages), the basis of the choice between them
     double cycNet = 0.0, cycExt = 0.0;
@@ -816,10 +829,10 @@ static int restrict_to_base(Ctx &c, const double *src, double *dst) {
     return ucheck(c, "restrict");
 }
 
-// rb ring: this solve's R b (once per solve).
+// rb ring: this solve's R b (once per solve, in the solves that keep the rings).
 static int push_b(Ctx &c, const double *b) {
     UNet *u = U(c);
-    if (u->bPushed) return SARAS_OK;
+    if (!u->track || u->bPushed) return SARAS_OK;
     std::swap(u->rb[2], u->rb[1]);
     std::swap(u->rb[1], u->rb[0]);
     u->nb += 1;
@@ -846,28 +859,56 @@ static int features(Ctx &c, float *feat, float *target) {
 // ------------------------------------------------------------------ solver hooks
 namespace saras {
 
+// Whether this solve keeps the restricted histories.  The network's inputs
+// are R b of this and the two previous solves and R Pp of the two previous
+// ones, so the rings run while pairs are collected and in the solves leading
+// up to any solve that may use the network: its first uses, while it is
+// preferred, after a pick that found the rings incomplete, and from two solves
+// before a scheduled probe of it.  Elsewhere the learned mode costs what
+// extrapolation costs.
+static bool rings_due(const Ctx &c, const UNet *u) {
+    if (c.collecting) return true;
+    if (c.guessMode != SARAS_GUESS_LEARNED || !u->trained) return false;
+    if (u->wantNet || u->usesNet < 2 || u->preferNet) return true;
+    return u->usesExt >= 2 && u->solves + 3 >= u->nextProbe;
+}
+
 // Called at the start of a target-mode solve: rotate the pressure history
-// (and, with the network in use, its restriction to level lb).
+// (and, in the solves that keep them, its restriction to level lb).  When Pp
+// and a history buffer have one size, the rotation moves buffers instead of
+// copying: Pp's buffer (P of the last solve) becomes pHist[0] and the oldest
+// history buffer becomes Pp, which the solve then writes in full; until it
+// does, the previous Pp is pHist[0] (c.ppInHist).
 int unet_begin_solve(Ctx &c) {
     int s = ensure_hist(c);
     if (s) return s;
     double *oldest = c.pHist[2];
     c.pHist[2] = c.pHist[1];
     c.pHist[1] = c.pHist[0];
-    c.pHist[0] = oldest;
-    SARAS_CUDA_TRY(cudaMemcpyAsync(c.pHist[0], c.f[SARAS_FIELD_PP], sizeof(double) * c.lv[0].count, cudaMemcpyDeviceToDevice, c.stream));
+    const FieldInfo &fp = c.info[SARAS_FIELD_PP];
+    long ppCount = (long)(fp.n[0] + 2) * (fp.n[1] + 2) * (fp.n[2] + 2);
+    if (ppCount == c.lv[0].count) {
+        c.pHist[0] = c.f[SARAS_FIELD_PP];
+        c.f[SARAS_FIELD_PP] = oldest;
+        c.ppInHist = true;
+    } else {
+        c.pHist[0] = oldest;
+        SARAS_CUDA_TRY(cudaMemcpyAsync(c.pHist[0], c.f[SARAS_FIELD_PP], sizeof(double) * c.lv[0].count, cudaMemcpyDeviceToDevice,
+                                       c.stream));
+    }
     c.histCount += 1;
     UNet *u = U(c);
-    if (u && (c.collecting || c.guessMode == SARAS_GUESS_LEARNED)) {
-        std::swap(u->rp[2], u->rp[1]);
-        std::swap(u->rp[1], u->rp[0]);
-        u->np += 1;
-        u->bPushed = false;
-        if ((s = restrict_to_base(c, c.pHist[0], u->rp[0]))) return s;
-    } else if (u) {
+    if (!u) return SARAS_OK;
+    u->bPushed = false;
+    u->track = rings_due(c, u);
+    if (!u->track) {
         u->np = u->nb = 0;   // the restricted histories are no longer consecutive
+        return SARAS_OK;
     }
-    return SARAS_OK;
+    std::swap(u->rp[2], u->rp[1]);
+    std::swap(u->rp[1], u->rp[0]);
+    u->np += 1;
+    return restrict_to_base(c, c.pHist[0], u->rp[0]);
 }
 
 // SARAS_GUESS_LEARNED picks, per solve, between the network's guess and plain
@@ -886,22 +927,34 @@ constexpr double kNetCostCycles = 0.5;
 int unet_pick(Ctx &c) {
     if (c.guessMode != SARAS_GUESS_LEARNED) return c.guessMode;
     UNet *u = U(c);
-    if (!u || !u->trained || u->nb < 2 || u->np < 2) return SARAS_GUESS_EXTRAPOLATE;   // R b ring completed by this solve's push
+    if (!u || !u->trained) return SARAS_GUESS_EXTRAPOLATE;
     u->solves += 1;
-    if (u->usesNet < 2) return SARAS_GUESS_LEARNED;
-    if (u->usesExt < 2) return SARAS_GUESS_EXTRAPOLATE;
-    bool netBetter = u->cycNet + kNetCostCycles < u->cycExt;
-    if (netBetter != u->preferNet) {
-        u->preferNet = netBetter;
-        u->probeEvery = kProbe;
-        u->nextProbe = u->solves + kProbe;
+    bool net, probe = false;
+    if (u->usesNet < 2) {
+        net = true;
+    } else if (u->usesExt < 2) {
+        net = false;
+    } else {
+        bool netBetter = u->cycNet + kNetCostCycles < u->cycExt;
+        if (netBetter != u->preferNet) {
+            u->preferNet = netBetter;
+            u->probeEvery = kProbe;
+            u->nextProbe = u->solves + kProbe;
+        }
+        probe = u->solves >= u->nextProbe;
+        net = probe ? !netBetter : netBetter;
     }
-    if (u->solves >= u->nextProbe) {
-        netBetter = !netBetter;
+    // the rings are complete once this solve pushes its R b
+    if (net && !(u->track && u->nb >= 2 && u->np >= 2)) {
+        u->wantNet = true;   // they run from the next solve on; the pick (a probe too) waits for them
+        return SARAS_GUESS_EXTRAPOLATE;
+    }
+    u->wantNet = false;
+    if (probe) {
         u->nextProbe = u->solves + u->probeEvery;
         u->probeEvery = std::min(kProbeMax, 2 * u->probeEvery);
     }
-    return netBetter ? SARAS_GUESS_LEARNED : SARAS_GUESS_EXTRAPOLATE;
+    return net ? SARAS_GUESS_LEARNED : SARAS_GUESS_EXTRAPOLATE;
 }
 
 void unet_record(Ctx &c, int built, int cycles) {
@@ -917,9 +970,11 @@ void unet_record(Ctx &c, int built, int cycles) {
     }
 }
 
-// Build the learned (or extrapolated) guess for the level-0 iterate into `dst`;
-// b is the compatible right-hand side.  Returns BAD_CONFIG if unavailable.
-int unet_guess(Ctx &c, const double *b, double *dst, int mode) {
+// Build the learned (or extrapolated) guess for the level-0 iterate into `dst`,
+// or with fxdst into the fixed-point iterate fxdst (round(v 2^sc), flag set
+// when out of range); b is the compatible right-hand side.  Returns
+// BAD_CONFIG if unavailable.
+int unet_guess(Ctx &c, const double *b, double *dst, int mode, long long *fxdst, int sc, int *flag) {
     bool use_net = mode == SARAS_GUESS_LEARNED;
     int quad = mode == SARAS_GUESS_QUADRATIC ? 1 : mode == SARAS_GUESS_PARITY ? 2 : 0;
     if (c.histCount < 2 + (quad ? 1 : 0)) return SARAS_BAD_CONFIG;
@@ -947,10 +1002,16 @@ int unet_guess(Ctx &c, const double *b, double *dst, int mode) {
     }
     const Level &L0 = c.lv[0];
     dim3 b2(64, 4), g2((L0.n[2] + 1 + 63) / 64, (L0.n[1] + 1 + 3) / 4, L0.n[0] + 1);
-    k_apply_guess<<<g2, b2, 0, c.stream>>>(dst, l0view(c, c.pHist[0]), l0view(c, c.pHist[1]), l0view(c, c.pHist[2]), quad,
-                                           use_net ? u->out : nullptr, use_net ? u->g[0] : Grid3{1, 1, 1}, use_net ? u->lb : 0,
-                                           use_net ? u->scales : nullptr, use_net ? u->scales + 4 : nullptr, c.p.xPer, c.p.yPer,
-                                           c.p.zPer);
+    const float *d = use_net ? u->out : nullptr;
+    Grid3 gd = use_net ? u->g[0] : Grid3{1, 1, 1};
+    int lb = use_net ? u->lb : 0;
+    const double *sca = use_net ? u->scales : nullptr, *alpha = use_net ? u->scales + 4 : nullptr;
+    if (fxdst)
+        k_apply_guess<long long><<<g2, b2, 0, c.stream>>>(fxdst, l0view(c, c.pHist[0]), l0view(c, c.pHist[1]), l0view(c, c.pHist[2]), quad,
+                                                          d, gd, lb, sca, alpha, c.p.xPer, c.p.yPer, c.p.zPer, sc, flag);
+    else
+        k_apply_guess<double><<<g2, b2, 0, c.stream>>>(dst, l0view(c, c.pHist[0]), l0view(c, c.pHist[1]), l0view(c, c.pHist[2]), quad,
+                                                       d, gd, lb, sca, alpha, c.p.xPer, c.p.yPer, c.p.zPer, 0, nullptr);
     count_launch(c);
     return ucheck(c, "guess");
 }
