@@ -687,6 +687,45 @@ static void march_dims(const Level &L, dim3 &g, dim3 &b) {
     g = dim3((L.n[2] + 1 + 31) / 32, (L.n[1] + 1 + 7) / 8, (L.n[0] + 1 + kIch - 1) / kIch);
 }
 
+// Column launches of the marching sweep, residual, prolongation and
+// fixed-point residual: one thread per (j, k) column of the core, numbered k
+// fastest over the whole (j, k) plane, kColBlock threads a block, blockIdx.y
+// the segment of kIch planes.  A level's rows are 2^m + 1 points long, so the
+// 32 x 8 tiles of march_dims leave one block in 2^(m-5) + 1 with a single
+// active lane per warp.  That costs the FP64 kernels pipe time (a warp
+// instruction occupies the FP64 pipe whatever its active lanes; they run at
+// its rate on this part), so FP64 launches take columns; the FP32 kernels
+// wait on memory instead and keep the tiles, whose in-plane j neighbours
+// come from L1 (columns measured 9% slower for the FP32 sweep at 257^3).
+constexpr int kColBlock = 256;
+static void col_dims(const Level &L, dim3 &g, dim3 &b) {
+    long cols = (long)(L.n[1] + 1) * (L.n[2] + 1);
+    b = dim3(kColBlock, 1, 1);
+    g = dim3((unsigned)((cols + kColBlock - 1) / kColBlock), (L.n[0] + 1 + kIch - 1) / kIch, 1);
+}
+template <typename T>
+static void level_dims(const Level &L, dim3 &g, dim3 &b) {
+    if (sizeof(T) == 8) col_dims(L, g, b);
+    else march_dims(L, g, b);
+}
+// The (j, k) column and plane segment of this thread under the launch shape
+// of level_dims (COL: columns); false outside the core.
+template <bool COL>
+__device__ __forceinline__ bool col_of(const MgBC &bc, int &j, int &k, int &seg) {
+    if (COL) {
+        const int W = bc.E[2] + 1;
+        const int t = blockIdx.x * kColBlock + threadIdx.x;
+        j = t / W;
+        k = t - j * W;
+        seg = blockIdx.y;
+        return j <= bc.E[1];
+    }
+    k = blockIdx.x * 32 + threadIdx.x;
+    j = blockIdx.y * 8 + threadIdx.y;
+    seg = blockIdx.z;
+    return j <= bc.E[1] && k <= bc.E[2];
+}
+
 // Index of the value a target-mode pad position -1 or E+1 holds: its mirror /
 // periodic image in the core (mirror 1 -> -1, E-1 -> E+1; periodic E-1 -> -1,
 // 1 -> E+1, the face-ghost images put_scatter writes).
@@ -720,10 +759,9 @@ __device__ __forceinline__ long nbr_x(int i, int d, int sx, const MgBC &bc) {
 template <typename T, bool ZERO>
 __global__ void __launch_bounds__(256) k_tgt_sweep(T *__restrict__ out, const T *__restrict__ in, const T *__restrict__ r,
                                                    int sx, int sy, MgBC bc, TgK<T> c) {
-    int k = blockIdx.x * 32 + threadIdx.x;
-    int j = blockIdx.y * 8 + threadIdx.y;
-    int i0 = blockIdx.z * kIch;
-    if (j > bc.E[1] || k > bc.E[2]) return;
+    int j, k, seg;
+    if (!col_of<sizeof(T) == 8>(bc, j, k, seg)) return;
+    const int i0 = seg * kIch;
     int n = min(kIch, bc.E[0] - i0 + 1);
     const NbrJK nb = nbr_jk(j, k, sy, bc);
     const long o0 = (long)(i0 + 1) * sx + (long)(j + 1) * sy + (k + 1);
@@ -778,8 +816,9 @@ __global__ void __launch_bounds__(256) k_tgt_sweep(T *__restrict__ out, const T 
 template <typename T>
 __global__ void __launch_bounds__(256) k_tgt_prolong_add(T *__restrict__ pf, const T *__restrict__ pc, int sxf, int syf, int sxc, int syc,
                                                          MgBC bc) {
-    int k = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y, i0 = blockIdx.z * kIch;   // kIch is even
-    if (j > bc.E[1] || k > bc.E[2]) return;
+    int j, k, seg;
+    if (!col_of<sizeof(T) == 8>(bc, j, k, seg)) return;
+    const int i0 = seg * kIch;   // kIch is even
     int iend = min(i0 + kIch - 1, bc.E[0]);
     int k2 = k >> 1, j2 = j >> 1;
     bool ko = k & 1, jo = j & 1;
@@ -818,11 +857,11 @@ __global__ void __launch_bounds__(256) k_tgt_prolong_add(T *__restrict__ pf, con
 template <typename T, typename OT, bool MAXRED>
 __global__ void __launch_bounds__(256) k_tgt_residual(OT *__restrict__ out, const T *__restrict__ p, const T *__restrict__ b,
                                                       int sx, int sy, MgBC bc, TgK<T> c, double *maxres) {
-    int k = blockIdx.x * 32 + threadIdx.x;
-    int j = blockIdx.y * 8 + threadIdx.y;
-    int i0 = blockIdx.z * kIch;
+    int j, k, seg;
+    const bool on = col_of<sizeof(T) == 8>(bc, j, k, seg);
+    const int i0 = seg * kIch;
     unsigned long long m = 0ull;
-    if (j <= bc.E[1] && k <= bc.E[2]) {
+    if (on) {
         int iend = min(i0 + kIch - 1, bc.E[0]);
         const NbrJK nb = nbr_jk(j, k, sy, bc);
         long o = (long)(i0 + 1) * sx + (long)(j + 1) * sy + (k + 1);
@@ -935,11 +974,11 @@ __device__ __forceinline__ long long round53(long long p) {
 __global__ void __launch_bounds__(256) k_fx_refine(const long long *__restrict__ pin, const long long *__restrict__ bfx,
                                                    float *__restrict__ r32, int sx, int sy, MgBC bc, float rscale,
                                                    unsigned long long *maxr) {
-    int k = blockIdx.x * 32 + threadIdx.x;
-    int j = blockIdx.y * 8 + threadIdx.y;
-    int i0 = blockIdx.z * kIch;
+    int j, k, seg;
+    const bool on = col_of<true>(bc, j, k, seg);
+    const int i0 = seg * kIch;
     unsigned long long m = 0;
-    if (j <= bc.E[1] && k <= bc.E[2]) {
+    if (on) {
         int iend = min(i0 + kIch - 1, bc.E[0]);
         const NbrJK nb = nbr_jk(j, k, sy, bc);
         long o = (long)(i0 + 1) * sx + (long)(j + 1) * sy + (k + 1);
@@ -955,19 +994,7 @@ __global__ void __launch_bounds__(256) k_fx_refine(const long long *__restrict__
             cc = cp;
         }
     }
-#pragma unroll
-    for (int off = 16; off; off >>= 1) {
-        unsigned long long o2 = __shfl_xor_sync(0xffffffffu, m, off);
-        m = o2 > m ? o2 : m;
-    }
-    __shared__ unsigned long long sm[8];
-    if (threadIdx.x == 0) sm[threadIdx.y] = m;
-    __syncthreads();
-    if (threadIdx.x == 0 && threadIdx.y == 0) {
-        unsigned long long b = 0;
-        for (int q = 0; q < 8; ++q) b = sm[q] > b ? sm[q] : b;
-        atomicMax(maxr, b);
-    }
+    block_max_bits_to(m, reinterpret_cast<double *>(maxr));
 }
 
 // The iterate advanced by the FP32 correction e of the inner V-cycles,
@@ -1637,7 +1664,7 @@ static int smooth(Ctx &c, int l, int count, bool zero_first, bool tgt) {
     int pk = sizeof(T) == 8 ? PK_MG_SMOOTH64 : PK_MG_SMOOTH32;
     double bytes = 3.0 * sizeof(T) * (double)(L.n[0] + 1) * (L.n[1] + 1) * (L.n[2] + 1);
     int sx = (L.n[1] + 3) * (L.n[2] + 3), sy = L.n[2] + 3;
-    dim3 gm, bm; march_dims(L, gm, bm);
+    dim3 gm, bm; level_dims<T>(L, gm, bm);
     for (int n = 0; n < count; ++n) {
         TgK<T> tk = make_tgk<T>(L, tgt ? smooth_weight(c, n, count) : c.p.jacobiWeight);
         prof_begin(c, pk, l);
@@ -1683,7 +1710,7 @@ static int restrict_level(Ctx &c, int l, bool tgt) {
     prof_begin(c, pk, l);
     if (tgt) {
         int sx = (L.n[1] + 3) * (L.n[2] + 3), sy = L.n[2] + 3;
-        dim3 gm, bm; march_dims(L, gm, bm);
+        dim3 gm, bm; level_dims<T>(L, gm, bm);
         k_tgt_residual<T, T, false><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bcf, make_tgk<T>(L, 1.0), nullptr);
         count_launch(c);
         prof_end(c, pk, l, 3.0 * sizeof(T) * pts);
@@ -1717,7 +1744,7 @@ static int prolong_level(Ctx &c, int l, bool tgt, bool add) {
     double pts = (double)(L.n[0] + 1) * (L.n[1] + 1) * (L.n[2] + 1);
     prof_begin(c, pk, l);
     if (tgt && add) {   // the core only: target-mode kernels read face neighbours at their images
-        dim3 gm, bm; march_dims(L, gm, bm);
+        dim3 gm, bm; level_dims<T>(L, gm, bm);
         int sx = (L.n[1] + 3) * (L.n[2] + 3), sy = L.n[2] + 3;
         k_tgt_prolong_add<T><<<gm, bm, 0, c.stream>>>(A_<T>(L), A_<T>(C), sx, sy, (C.n[1] + 3) * (C.n[2] + 3), C.n[2] + 3, bc);
     } else {
@@ -2078,6 +2105,7 @@ static int mixed_fixed(Ctx &c, const double *pp0, double bmax, double pmax, doub
     double rs = l * inv2s;   // residual units -> value
     int sx0 = (L0.n[1] + 3) * (L0.n[2] + 3), sy0 = L0.n[2] + 3;
     dim3 gm0, bm0; march_dims(L0, gm0, bm0);
+    dim3 gk0, bk0; col_dims(L0, gk0, bk0);
     dim3 gc, bcd; core_dims(L0, gc, bcd);
     int nbF = grid_blocks(L0.count);
     k_fx_rhs<<<gc, bcd, 0, c.stream>>>(B, L0.r, sx0, sy0, bc0, std::ldexp(1.0, sc) / l, dflag);
@@ -2091,7 +2119,7 @@ static int mixed_fixed(Ctx &c, const double *pp0, double bmax, double pmax, doub
             prof_end(c, PK_REFINE_UPDATE, 0, (8.0 + 4.0 + 8.0 + 8.0 + 4.0) * (double)L0.count);
         } else {
             prof_begin(c, PK_REFINE_RESID, 0);
-            k_fx_refine<<<gm0, bm0, 0, c.stream>>>(c.fx[q], B, L0.r32, sx0, sy0, bc0, (float)rs, dmax);
+            k_fx_refine<<<gk0, bk0, 0, c.stream>>>(c.fx[q], B, L0.r32, sx0, sy0, bc0, (float)rs, dmax);
             prof_end(c, PK_REFINE_RESID, 0, (8.0 + 8.0 + 4.0) * (double)L0.count);
         }
         count_launch(c);
@@ -2110,7 +2138,7 @@ static int mixed_fixed(Ctx &c, const double *pp0, double bmax, double pmax, doub
     auto refine_out = [&](int q, double &out) -> int {
         SARAS_CUDA_TRY(cudaMemsetAsync(c.dscal + 34, 0, sizeof(double), c.stream));
         prof_begin(c, PK_REFINE_RESID, 0);
-        k_fx_refine<<<gm0, bm0, 0, c.stream>>>(c.fx[q], B, nullptr, sx0, sy0, bc0, (float)rs, dmax);
+        k_fx_refine<<<gk0, bk0, 0, c.stream>>>(c.fx[q], B, nullptr, sx0, sy0, bc0, (float)rs, dmax);
         prof_end(c, PK_REFINE_RESID, 0, (8.0 + 8.0) * (double)L0.count);
         count_launch(c);
         int e = chk(c, "fixed-point output check");
@@ -2245,6 +2273,7 @@ static int mg_solve_target_run(Ctx &c, int *cycles, double *residual, saras_step
     int sx0 = (L0.n[1] + 3) * (L0.n[2] + 3), sy0 = L0.n[2] + 3;
     TgK<double> t0 = make_tgk<double>(L0, 1.0);
     dim3 gm0, bm0; march_dims(L0, gm0, bm0);
+    dim3 gk0, bk0; col_dims(L0, gk0, bk0);
     auto fine_res = [&](bool withE, double *out) -> int {
         SARAS_CUDA_TRY(cudaMemsetAsync(c.dscal + 32, 0, sizeof(double), c.stream));
         if (withE) {
@@ -2255,10 +2284,10 @@ static int mg_solve_target_run(Ctx &c, int *cycles, double *residual, saras_step
         }
         prof_begin(c, PK_REFINE_RESID, 0);
         if (c.mgMode == SARAS_MG_MIXED) {
-            k_tgt_residual<double, float, true><<<gm0, bm0, 0, c.stream>>>(L0.r32, L0.pa(), L0.r, sx0, sy0, bc0, t0, c.dscal + 32);
+            k_tgt_residual<double, float, true><<<gk0, bk0, 0, c.stream>>>(L0.r32, L0.pa(), L0.r, sx0, sy0, bc0, t0, c.dscal + 32);
             prof_end(c, PK_REFINE_RESID, 0, (8.0 + 8.0 + 4.0) * (double)ncore);
         } else {
-            k_tgt_residual<double, double, true><<<gm0, bm0, 0, c.stream>>>(nullptr, L0.pa(), L0.r, sx0, sy0, bc0, t0, c.dscal + 32);
+            k_tgt_residual<double, double, true><<<gk0, bk0, 0, c.stream>>>(nullptr, L0.pa(), L0.r, sx0, sy0, bc0, t0, c.dscal + 32);
             prof_end(c, PK_REFINE_RESID, 0, (8.0 + 8.0) * (double)ncore);
         }
         count_launch(c);
