@@ -998,7 +998,10 @@ __global__ void __launch_bounds__(256) k_fx_refine(const long long *__restrict__
 }
 
 // The iterate advanced by the FP32 correction e of the inner V-cycles,
-// P_out = P_in + round(e 2^s), and the residual of P_out (as k_fx_refine), with
+// P_out = round53(P_in + round(e 2^s)) (so that every iterate is a value FP64
+// holds exactly: P_out 2^-s is the solve's FP64 output, written to dst at the
+// core points when dst is given), and the residual of P_out (as k_fx_refine),
+// which is then the exact residual of that output; with
 // the in-plane neighbours shared through shared memory: each advanced value is
 // formed once per block (the tile's halo adds a third), instead of once per
 // stencil use.  Block 32 (k) x 8 (j) marching kIch planes along i; the plane
@@ -1009,14 +1012,14 @@ __global__ void __launch_bounds__(256) k_fx_refine(const long long *__restrict__
 __global__ void __launch_bounds__(256) k_fx_update(long long *__restrict__ pout, const long long *__restrict__ pin,
                                                    const float *__restrict__ e, const long long *__restrict__ bfx,
                                                    float *__restrict__ r32, int sx, int sy, MgBC bc, int s, float rscale,
-                                                   unsigned long long *maxr, int *flag) {
+                                                   unsigned long long *maxr, int *flag, double *__restrict__ dst, double inv2s) {
     __shared__ long long tile[3][10][34];
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
     const int k0 = blockIdx.x * 32, j0 = blockIdx.y * 8, i0 = blockIdx.z * kIch;
     const int k = k0 + tx, j = j0 + ty;
     const int iend = min(i0 + kIch - 1, bc.E[0]);
     bool bad = false;
-    auto val = [&](long q) -> long long { return pin[q] + f2fx(e[q], s, bad); };
+    auto val = [&](long q) -> long long { return round53(pin[q] + f2fx(e[q], s, bad)); };
     // the two tile positions this thread loads: (j0 - 1 .. j0 + 8, k0 - 1 .. k0 + 32)
     long lo[2];
     bool lv[2];
@@ -1053,6 +1056,7 @@ __global__ void __launch_bounds__(256) k_fx_update(long long *__restrict__ pout,
             unsigned long long a = (unsigned long long)(r < 0 ? -r : r);
             m = a > m ? a : m;
             pout[o] = cc;
+            if (dst) dst[o] = __ll2double_rn(cc) * inv2s;
             unsigned long long ac = (unsigned long long)(cc < 0 ? -cc : cc);
             if (ac > (1ull << 59)) bad = true;
             cm = cc;
@@ -1088,13 +1092,12 @@ __global__ void k_fx_init(long long *__restrict__ dst, View3<const double> src, 
 
 // The solve's output written straight into Pp: every padded point takes the
 // value of the core point the imposeBC composition maps it to (k_mg_output's
-// mapping, target modes: periodic or mirror per axis), converted once to FP64;
-// chk receives round(Pp 2^s), the FP64 result back in fixed point, whose exact
-// residual is the residual of what the solve returns.
-// Pp = P 2^-s over the whole padded array (face ghosts: their images), and
-// chk = the fixed-point value of that FP64 number (round53 of P) for the check
-// of the output; one thread per point of a (k, j) row, blockIdx.z the plane.
-__global__ void k_fx_output(double *__restrict__ dst, long long *__restrict__ chk, const long long *__restrict__ src, MgBC bc, double inv2s) {
+// mapping, target modes: periodic or mirror per axis), P 2^-s.  Every
+// fixed-point iterate is a value FP64 holds exactly (an FP64 value scaled by
+// 2^s, or round53 in k_fx_update), so the conversion is exact and the
+// iterate's residual is the exact residual of what the solve returns.  One
+// thread per point of a (k, j) row, blockIdx.z the plane.
+__global__ void k_fx_output(double *__restrict__ dst, const long long *__restrict__ src, MgBC bc, double inv2s) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x - 1, j = blockIdx.y * blockDim.y + threadIdx.y - 1, i = blockIdx.z - 1;
     const int E1 = bc.E[1], E2 = bc.E[2];
     if (j > E1 + 1 || k > E2 + 1) return;
@@ -1107,16 +1110,32 @@ __global__ void k_fx_output(double *__restrict__ dst, long long *__restrict__ ch
         else q[d] = q[d] < 0 ? 1 : E - 1;
     }
     const long o = (i + 1) * sx + (j + 1) * sy + (k + 1);
-    const long long p = src[(q[0] + 1) * sx + (q[1] + 1) * sy + (q[2] + 1)];
-    dst[o] = __ll2double_rn(p) * inv2s;
-    chk[o] = round53(p);
+    dst[o] = __ll2double_rn(src[(q[0] + 1) * sx + (q[1] + 1) * sy + (q[2] + 1)]) * inv2s;
 }
 
-// dst = round(src 2^s) over a whole padded array (face-ghost images included).
-__global__ void k_fx_from(long long *__restrict__ dst, const double *__restrict__ src, long n, int s, int *flag) {
-    bool bad = false;
-    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) dst[t] = d2fx(src[t], s, bad);
-    if (bad) atomicExch(flag, 1);
+// The ghost positions of the output Pp (k_fx_output's mapping) once the
+// core holds P 2^-s: blockIdx.z the face (axis z / 2, low or high side),
+// threads over that face's padded positions.  Points on edges and corners
+// are written by every face they lie on, with one value.
+__global__ void k_fx_output_shell(double *__restrict__ dst, const long long *__restrict__ src, MgBC bc, double inv2s) {
+    const int d = blockIdx.z >> 1, side = blockIdx.z & 1;
+    const int a = (d + 1) % 3, b = (d + 2) % 3;
+    const int na = bc.E[a] + 3, nb = bc.E[b] + 3;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= na * nb) return;
+    int q[3];
+    q[d] = side ? bc.E[d] + 1 : -1;
+    q[a] = t / nb - 1;
+    q[b] = t - (q[a] + 1) * nb - 1;
+    const long sy = bc.E[2] + 3, sx = (long)(bc.E[1] + 3) * sy;
+    const long o = (q[0] + 1) * sx + (q[1] + 1) * sy + (q[2] + 1);
+    for (int e = 0; e < 3; ++e) {
+        int E = bc.E[e];
+        if (q[e] >= 0 && q[e] <= E) continue;
+        if (bc.per[e]) q[e] = q[e] < 0 ? E - 1 : 1;
+        else q[e] = q[e] < 0 ? 1 : E - 1;
+    }
+    dst[o] = __ll2double_rn(src[(q[0] + 1) * sx + (q[1] + 1) * sy + (q[2] + 1)]) * inv2s;
 }
 
 // B = round(b mul) over the core (mul = 2^s / l; the residual reads b only there).
@@ -1129,19 +1148,6 @@ __global__ void k_fx_rhs(long long *__restrict__ dst, const double *__restrict__
     if (bad) atomicExch(flag, 1);
 }
 
-// p = P 2^-s (FP64, rounded once) over the whole padded array; with chk, also
-// chk = round(p 2^s): the FP64 result back in fixed point, whose exact residual
-// is the residual of what the solve returns.
-__global__ void k_fx_to(double *__restrict__ dst, long long *__restrict__ chk, const long long *__restrict__ src, long n, double inv2s,
-                        int s, int *flag) {
-    bool bad = false;
-    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
-        double x = __ll2double_rn(src[t]) * inv2s;
-        dst[t] = x;
-        if (chk) chk[t] = d2fx(x, s, bad);
-    }
-    if (bad) atomicExch(flag, 1);
-}
 
 // ---- target modes (FP64 / mixed)
 // Trapezoidal-weight partial sums of the core of rhs: one thread per (j, k)
@@ -2107,16 +2113,19 @@ static int mixed_fixed(Ctx &c, const double *pp0, double bmax, double pmax, doub
     dim3 gm0, bm0; march_dims(L0, gm0, bm0);
     dim3 gk0, bk0; col_dims(L0, gk0, bk0);
     dim3 gc, bcd; core_dims(L0, gc, bcd);
-    int nbF = grid_blocks(L0.count);
     k_fx_rhs<<<gc, bcd, 0, c.stream>>>(B, L0.r, sx0, sy0, bc0, std::ldexp(1.0, sc) / l, dflag);
     count_launch(c);
+    // With Pp's buffer free for the output (the previous Pp is pHist[0]), every
+    // refinement update writes its FP64 iterate into Pp's core as it goes.
+    double *outp = c.ppInHist ? c.f[SARAS_FIELD_PP] : nullptr;
     // residual of fixed iterate q (with e: advanced into q ^ 1 first); returns the max in value units
     auto refine = [&](int q, bool withE, double &out, bool &bad) -> int {
         SARAS_CUDA_TRY(cudaMemsetAsync(c.dscal + 34, 0, sizeof(double), c.stream));
         if (withE) {
             prof_begin(c, PK_REFINE_UPDATE, 0);
-            k_fx_update<<<gm0, bm0, 0, c.stream>>>(c.fx[q ^ 1], c.fx[q], L0.pa32(), B, L0.r32, sx0, sy0, bc0, sc, (float)rs, dmax, dflag);
-            prof_end(c, PK_REFINE_UPDATE, 0, (8.0 + 4.0 + 8.0 + 8.0 + 4.0) * (double)L0.count);
+            k_fx_update<<<gm0, bm0, 0, c.stream>>>(c.fx[q ^ 1], c.fx[q], L0.pa32(), B, L0.r32, sx0, sy0, bc0, sc, (float)rs, dmax, dflag,
+                                                   outp, inv2s);
+            prof_end(c, PK_REFINE_UPDATE, 0, (8.0 + 4.0 + 8.0 + 8.0 + 4.0 + (outp ? 8.0 : 0.0)) * (double)L0.count);
         } else {
             prof_begin(c, PK_REFINE_RESID, 0);
             k_fx_refine<<<gk0, bk0, 0, c.stream>>>(c.fx[q], B, L0.r32, sx0, sy0, bc0, (float)rs, dmax);
@@ -2132,21 +2141,6 @@ static int mixed_fixed(Ctx &c, const double *pp0, double bmax, double pmax, doub
         SARAS_CUDA_TRY(cudaStreamSynchronize(c.stream));
         out = (double)mx * rs;
         bad = fl != 0;
-        return SARAS_OK;
-    };
-    // the exact residual of the FP64 output (chk = P rounded to FP64), max only
-    auto refine_out = [&](int q, double &out) -> int {
-        SARAS_CUDA_TRY(cudaMemsetAsync(c.dscal + 34, 0, sizeof(double), c.stream));
-        prof_begin(c, PK_REFINE_RESID, 0);
-        k_fx_refine<<<gk0, bk0, 0, c.stream>>>(c.fx[q], B, nullptr, sx0, sy0, bc0, (float)rs, dmax);
-        prof_end(c, PK_REFINE_RESID, 0, (8.0 + 8.0) * (double)L0.count);
-        count_launch(c);
-        int e = chk(c, "fixed-point output check");
-        if (e) return e;
-        unsigned long long mx = 0;
-        SARAS_CUDA_TRY(cudaMemcpyAsync(&mx, dmax, sizeof(mx), cudaMemcpyDeviceToHost, c.stream));
-        SARAS_CUDA_TRY(cudaStreamSynchronize(c.stream));
-        out = (double)mx * rs;
         return SARAS_OK;
     };
     bool bad = false;
@@ -2190,38 +2184,37 @@ static int mixed_fixed(Ctx &c, const double *pp0, double bmax, double pmax, doub
         }
     }
     if (st) { st->guess_residual = bmax > 0 ? r / bmax : r; st->guess_source = source; }
-    while (true) {
-        while (r > target && cyc < c.mgMaxCycles) {
-            if (!std::isfinite(r)) { c.err = "multigrid residual is not finite"; return SARAS_NOT_FINITE; }
-            int n = refine_cycles(c, r, target, cyc, steps == 0);
-            double r0 = r;
-            for (int q = 0; q < n; ++q) {
-                if ((s = vcycle_tgt<float>(c, q == 0))) return s;
-                cyc += 1;
-            }
-            steps += 1;
-            if ((s = refine(cur, true, r, bad))) return s;
-            if (bad) break;
-            cur ^= 1;
-            note_contraction(c, r0, r, n);
+    bool updated = false;
+    while (r > target && cyc < c.mgMaxCycles) {
+        if (!std::isfinite(r)) { c.err = "multigrid residual is not finite"; return SARAS_NOT_FINITE; }
+        int n = refine_cycles(c, r, target, cyc, steps == 0);
+        double r0 = r;
+        for (int q = 0; q < n; ++q) {
+            if ((s = vcycle_tgt<float>(c, q == 0))) return s;
+            cyc += 1;
         }
+        steps += 1;
+        if ((s = refine(cur, true, r, bad))) return s;
         if (bad) break;
-        // the FP64 result, and the exact residual of those FP64 values
-        {
-            dim3 bo(64, 4, 1), go((L0.n[2] + 3 + 63) / 64, (L0.n[1] + 3 + 3) / 4, L0.n[0] + 3);
-            k_fx_output<<<go, bo, 0, c.stream>>>(c.f[SARAS_FIELD_PP], c.fx[cur ^ 1], c.fx[cur], bc0, inv2s);
-            count_launch(c);
-            c.ppInHist = false;
-        }
-        double rf = 0;
-        if ((s = refine_out(cur ^ 1, rf))) return s;
-        r = rf;
         cur ^= 1;
-        if (r <= target || cyc >= c.mgMaxCycles) {
-            if (built) unet_record(c, built, cyc);
-            done = true;
-            return SARAS_OK;
+        updated = true;
+        note_contraction(c, r0, r, n);
+    }
+    if (!bad) {
+        // the FP64 result P 2^-s (exact), whose exact residual is r
+        if (updated && outp) {   // the core is written: the ghost positions
+            int most = 0;   // padded points of the largest face
+            for (int d = 0; d < 3; ++d) most = std::max(most, (L0.n[(d + 1) % 3] + 3) * (L0.n[(d + 2) % 3] + 3));
+            k_fx_output_shell<<<dim3((most + 255) / 256, 1, 6), 256, 0, c.stream>>>(outp, c.fx[cur], bc0, inv2s);
+        } else {
+            dim3 bo(64, 4, 1), go((L0.n[2] + 3 + 63) / 64, (L0.n[1] + 3 + 3) / 4, L0.n[0] + 3);
+            k_fx_output<<<go, bo, 0, c.stream>>>(c.f[SARAS_FIELD_PP], c.fx[cur], bc0, inv2s);
         }
+        count_launch(c);
+        c.ppInHist = false;
+        if (built) unet_record(c, built, cyc);
+        done = true;
+        return chk(c, "fixed-point output");
     }
     // out of range: restart from the previous Pp in FP64
     L0.cur = 0;

@@ -886,8 +886,8 @@ int unet_begin_solve(Ctx &c) {
     c.pHist[2] = c.pHist[1];
     c.pHist[1] = c.pHist[0];
     const FieldInfo &fp = c.info[SARAS_FIELD_PP];
-    long ppCount = (long)(fp.n[0] + 2) * (fp.n[1] + 2) * (fp.n[2] + 2);
-    if (ppCount == c.lv[0].count) {
+    const Level &L0 = c.lv[0];
+    if (fp.n[0] + 2 == L0.n[0] + 3 && fp.n[1] + 2 == L0.n[1] + 3 && fp.n[2] + 2 == L0.n[2] + 3) {   // one padded shape
         c.pHist[0] = c.f[SARAS_FIELD_PP];
         c.f[SARAS_FIELD_PP] = oldest;
         c.ppInHist = true;
