@@ -886,19 +886,25 @@ __global__ void __launch_bounds__(256) k_tgt_residual(OT *__restrict__ out, cons
 
 // Full-weighting restriction of a target-mode residual (k_mg_restrict's
 // weights (1/64) [1 2 1]^3, summed separably): one thread per coarse (J, K)
-// column marching kRrCh coarse planes along I; each fine plane's in-plane
+// column (column launch, k fastest over the coarse plane) marching rr_ch
+// coarse planes along I; each fine plane's in-plane
 // [1 2 1] x [1 2 1] sum is formed once and the odd fine plane between two
 // coarse planes serves both.  Fine positions outside the core are read at
 // their mirror / periodic images (the pads k_mg_restrict resolves).
-constexpr int kRrCh = 8;   // coarse planes per thread
+// Coarse planes per thread: FP32 restrictions wait on memory and keep
+// longer chains (each odd fine plane serves two coarse planes); FP64 ones
+// are bound by the FP64 pipe and want more threads (measured at 257^3).
+template <typename T>
+constexpr int rr_ch() { return sizeof(T) == 8 ? 4 : 8; }
 
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_tgt_restrict(T *__restrict__ rc, const T *__restrict__ r, int sx, int sy, int csx, int csy,
                                                        MgBC bcf) {
-    const int K = blockIdx.x * 32 + threadIdx.x, J = blockIdx.y * 8 + threadIdx.y, I0 = blockIdx.z * kRrCh;
     const int E0 = bcf.E[0], E1 = bcf.E[1], E2 = bcf.E[2];
-    if (K > E2 / 2 || J > E1 / 2) return;
+    const int W = E2 / 2 + 1, t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int J = t / W, K = t - J * W, I0 = blockIdx.y * rr_ch<T>();
+    if (J > E1 / 2) return;
     long oj[3];
     int ok[3];
 #pragma unroll
@@ -916,7 +922,7 @@ __global__ void __launch_bounds__(256) k_tgt_restrict(T *__restrict__ rc, const 
         }
         return row[0] + (T)2 * row[1] + row[2];
     };
-    const int Iend = min(I0 + kRrCh - 1, E0 / 2);
+    const int Iend = min(I0 + rr_ch<T>() - 1, E0 / 2);
     T lo = plane(2 * I0 - 1);
 #pragma unroll 2
     for (int I = I0; I <= Iend; ++I) {
@@ -1195,15 +1201,20 @@ __global__ void __launch_bounds__(256) k_tgt_rhs(View3<double> b, View3<const do
 }
 
 // ---- the coarse end of a target-mode V-cycle in one CTA
-// Levels Lt..depth (at most 16 intervals per axis at Lt) fit in shared memory
-// together; below ~50k points their sweeps, residuals and transfers are
-// launch-latency bound, and the coarsest Gauss-Seidel loop runs on one CTA
-// anyway.  k_mg_tail runs that whole sub-cycle: pre-smoothing from zero and
+// Levels Lt..depth (at most kTailIntervals intervals per axis at Lt) fit in
+// shared memory together; at these sizes their sweeps, residuals and
+// transfers are launch-latency bound, and the coarsest Gauss-Seidel loop runs
+// on one CTA anyway.  k_mg_tail runs that whole sub-cycle: pre-smoothing from zero and
 // restriction down to the coarsest level, the coarsest solve (coarse_gs),
 // prolongation and post-smoothing back up to Lt, with the kernels' arithmetic
 // (k_tgt_sweep, k_tgt_residual, k_mg_restrict, k_mg_prolong_add), and writes
 // the level-Lt iterate with its face-ghost images to global memory.
 constexpr int kTailMaxLevels = 8;
+// The tail's first level: 9^3 at most.  One CTA runs a 17^3 level's Chebyshev
+// sweeps instruction-bound on one SM; graph-replayed kernels on all SMs ran
+// the 257^3 steps 0.7% (mixed) and 3% (plain FP64) faster with 17^3 outside
+// the tail.
+constexpr int kTailIntervals = 8;
 constexpr int kTailMaxSweeps = 16;
 constexpr int kTailThreads = 1024;
 
@@ -1459,7 +1470,7 @@ static int tail_level(const Ctx &c) {
     if (c.p.preSmooth > kTailMaxSweeps || c.p.postSmooth > kTailMaxSweeps || c.p.coarseSmooth > kTailMaxSweeps) return -1;
     for (int l = 1; l < c.depth; ++l) {
         const Level &L = c.lv[l];
-        if (std::max(L.n[0], std::max(L.n[1], L.n[2])) > 16) continue;
+        if (std::max(L.n[0], std::max(L.n[1], L.n[2])) > kTailIntervals) continue;
         if (c.depth - l + 1 > kTailMaxLevels) return -1;
         size_t bytes = 0;
         for (int q = l; q <= c.depth; ++q) bytes += 3 * sizeof(double) * (size_t)c.lv[q].count;
@@ -1723,8 +1734,9 @@ static int restrict_level(Ctx &c, int l, bool tgt) {
         pk = sizeof(T) == 8 ? PK_MG_RESTRICT64 : PK_MG_RESTRICT32;
         prof_begin(c, pk, l);
         int csx = (C.n[1] + 3) * (C.n[2] + 3), csy = C.n[2] + 3;
-        dim3 gr((C.n[2] + 1 + 31) / 32, (C.n[1] + 1 + 7) / 8, (C.n[0] + 1 + kRrCh - 1) / kRrCh);
-        k_tgt_restrict<T><<<gr, dim3(32, 8, 1), 0, c.stream>>>(R_<T>(C), B_<T>(L), sx, sy, csx, csy, bcf);
+        long ccols = (long)(C.n[1] + 1) * (C.n[2] + 1);
+        dim3 gr((unsigned)((ccols + 255) / 256), (C.n[0] + 1 + rr_ch<T>() - 1) / rr_ch<T>(), 1);
+        k_tgt_restrict<T><<<gr, dim3(256, 1, 1), 0, c.stream>>>(R_<T>(C), B_<T>(L), sx, sy, csx, csy, bcf);
         count_launch(c);
         prof_end(c, pk, l, sizeof(T) * pts * (1.0 + 1.0 / 8.0));
         return chk(c, "mg restrict");
