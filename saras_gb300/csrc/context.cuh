@@ -191,6 +191,7 @@ int unet_guess(Ctx &c, const double *b, double *dst, int mode, long long *fxdst 
 void vgraph_reset(Ctx &c);
 int prof_graph_replay(Ctx &c, cudaGraphExec_t ge, const std::vector<ProfNode> &nodes);
 int unet_pick(Ctx &c);
+bool unet_tracking(const Ctx &c);
 void unet_record(Ctx &c, int built, int cycles);
 int unet_collect_sample(Ctx &c, const double *b);
 int conv3d_check(int mode, int D, int H, int W, int cin, int cout, const unsigned short *x, const unsigned short *dy,

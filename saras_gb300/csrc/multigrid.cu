@@ -1144,60 +1144,92 @@ __global__ void k_fx_output_shell(double *__restrict__ dst, const long long *__r
     dst[o] = __ll2double_rn(src[(q[0] + 1) * sx + (q[1] + 1) * sy + (q[2] + 1)]) * inv2s;
 }
 
-// B = round(b mul) over the core (mul = 2^s / l; the residual reads b only there).
-__global__ void k_fx_rhs(long long *__restrict__ dst, const double *__restrict__ b, int sx, int sy, MgBC bc, double mul, int *flag) {
-    int i, j, k;
-    if (!core_pt(bc.E, i, j, k)) return;
-    long o = (long)(i + 1) * sx + (long)(j + 1) * sy + (k + 1);
+// B = round((rhs - mean) mul) over the core (mul = 2^s / l; the residual reads
+// B only there), and, with bout, b = rhs - mean itself (the FP64 right-hand
+// side that the restricted histories and the FP64 fallback read).  Column
+// launch.
+__global__ void __launch_bounds__(256) k_fx_rhs(long long *__restrict__ dst, double *__restrict__ bout, const double *__restrict__ rhs,
+                                                int sx, int sy, MgBC bc, double mean, double mul, int *flag) {
+    int j, k, seg;
+    if (!col_of<true>(bc, j, k, seg)) return;
+    const int i0 = seg * kIch, iend = min(i0 + kIch - 1, bc.E[0]);
+    long o = (long)(i0 + 1) * sx + (long)(j + 1) * sy + (k + 1);
     bool bad = false;
-    dst[o] = d2fx(b[o] * mul, 0, bad);
+    for (int i = i0; i <= iend; ++i, o += sx) {
+        const double b = rhs[o] - mean;
+        if (bout) bout[o] = b;
+        dst[o] = d2fx(b * mul, 0, bad);
+    }
     if (bad) atomicExch(flag, 1);
 }
 
 
 // ---- target modes (FP64 / mixed)
-// Trapezoidal-weight partial sums of the core of rhs: one thread per (j, k)
-// column marching kIch points along i (32-bit index arithmetic), one partial
-// per block in block order.
-__global__ void __launch_bounds__(256) k_trap_sum(View3<const double> rhs, MgBC bc, double *part) {
+// Order-preserving key of a double (unsigned comparison of keys = numeric
+// comparison of values, NaN above +Inf), and its inverse on the host.
+__device__ __forceinline__ unsigned long long order_key(double v) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+static double order_key_value(unsigned long long key) {
+    unsigned long long b = (key >> 63) ? (key & 0x7fffffffffffffffull) : ~key;
+    double v;
+    std::memcpy(&v, &b, sizeof v);
+    return v;
+}
+
+// The inputs of a target-mode solve in one pass over the core: trapezoidal-
+// weight partial sums of rhs (one per block, in block order), max and min of
+// rhs (keys: max |rhs - mean| = max(max - mean, mean - min), exactly, as
+// rounding is monotone), and with pp, max |pp| (the fixed-point scale).
+// Column launch.
+__global__ void __launch_bounds__(256) k_tgt_stats(View3<const double> rhs, const double *__restrict__ pp, MgBC bc, double *part,
+                                                   double *kmax, double *kmin, double *pmax) {
     __shared__ double sm[8];
-    int k = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y, i0 = blockIdx.z * kIch;
+    int j, k, seg;
+    const bool on = col_of<true>(bc, j, k, seg);
     // weight 2^-(number of axes on which the point is an end point), as one
     // table lookup: the product of three halves costs GB300's FP64 pipe
     const double wt[4] = {1.0, 0.5, 0.25, 0.125};
     double s = 0;
-    if (j <= bc.E[1] && k <= bc.E[2]) {
-        int ejk = (j == 0 || j == bc.E[1]) + (k == 0 || k == bc.E[2]);
-        int iend = min(i0 + kIch - 1, bc.E[0]);
-        for (int i = i0; i <= iend; ++i) s = fma(wt[ejk + (i == 0 || i == bc.E[0])], rhs(i, j, k), s);
-    }
-    s = warp_sum(s);
-    if (threadIdx.x == 0) sm[threadIdx.y] = s;
-    __syncthreads();
-    if (threadIdx.x == 0 && threadIdx.y == 0) {
-        double S = 0;
-        for (int w = 0; w < 8; ++w) S += sm[w];
-        part[((long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = S;
-    }
-}
-
-// b = rhs - trapmean over the core; max |b| (block maxima, atomic).  The mean
-// is one product with 1/wsum (wsum = product of the interval counts).
-__global__ void __launch_bounds__(256) k_tgt_rhs(View3<double> b, View3<const double> rhs, MgBC bc, const double *sum, double inv_wsum,
-                                                 double *maxabs) {
-    int k = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y, i0 = blockIdx.z * kIch;
-    unsigned long long m = 0;
-    if (j <= bc.E[1] && k <= bc.E[2]) {
-        double mean = *sum * inv_wsum;
-        int iend = min(i0 + kIch - 1, bc.E[0]);
-        for (int i = i0; i <= iend; ++i) {
-            double v = rhs(i, j, k) - mean;
-            b(i, j, k) = v;
-            unsigned long long a = abs_bits(v);
-            m = a > m ? a : m;
+    unsigned long long hi = 0, lo = 0, pm = 0;
+    if (on) {
+        const int ejk = (j == 0 || j == bc.E[1]) + (k == 0 || k == bc.E[2]);
+        const int i0 = seg * kIch, iend = min(i0 + kIch - 1, bc.E[0]);
+        long o = (long)(i0 + 1) * rhs.sx + (long)(j + 1) * rhs.sy + (k + 1);
+        for (int i = i0; i <= iend; ++i, o += rhs.sx) {
+            const double v = rhs.p[o];
+            s = fma(wt[ejk + (i == 0 || i == bc.E[0])], v, s);
+            const unsigned long long key = order_key(v);
+            hi = key > hi ? key : hi;
+            lo = ~key > lo ? ~key : lo;
+            if (pp) {
+                const unsigned long long a = abs_bits(pp[o]);
+                pm = a > pm ? a : pm;
+            }
         }
     }
-    block_max_bits_to(m, maxabs);
+    s = warp_sum(s);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double S = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) S += sm[w];
+        part[(long)blockIdx.y * gridDim.x + blockIdx.x] = S;
+    }
+    block_max_bits_to(hi, kmax);
+    block_max_bits_to(lo, kmin);
+    if (pp) block_max_bits_to(pm, pmax);
+}
+
+// b = rhs - mean over the core (the FP64 right-hand side).  Column launch.
+__global__ void __launch_bounds__(256) k_tgt_rhs(double *__restrict__ b, const double *__restrict__ rhs, int sx, int sy, MgBC bc,
+                                                 double mean) {
+    int j, k, seg;
+    if (!col_of<true>(bc, j, k, seg)) return;
+    const int i0 = seg * kIch, iend = min(i0 + kIch - 1, bc.E[0]);
+    long o = (long)(i0 + 1) * sx + (long)(j + 1) * sy + (k + 1);
+    for (int i = i0; i <= iend; ++i, o += sx) b[o] = rhs[o] - mean;
 }
 
 // ---- the coarse end of a target-mode V-cycle in one CTA
@@ -2093,8 +2125,8 @@ static void note_contraction(Ctx &c, double r0, double r, int n) {
 // by a cycle at most.
 constexpr double kGuessTrusted = 1e-4;
 
-static int mixed_fixed(Ctx &c, const double *pp0, double bmax, double pmax, double target, bool wantGuess, double &r, int &source, int &cyc,
-                       int &steps, bool &done, saras_step_stats *st) {
+static int mixed_fixed(Ctx &c, const double *pp0, double mean, double bmax, double pmax, double target, bool wantGuess, double &r, int &source,
+                       int &cyc, int &steps, bool &done, saras_step_stats *st) {
     int s;
     Level &L0 = c.lv[0];
     MgBC bc0 = level_bc(c, 0, true);
@@ -2111,21 +2143,28 @@ static int mixed_fixed(Ctx &c, const double *pp0, double bmax, double pmax, doub
     SARAS_CUDA_TRY(cudaMemsetAsync(c.dscal + 34, 0, sizeof(double) * 2, c.stream));
     double l = L0.lx;
     double M = std::max(pmax, bmax / l);
-    if (!(M > 0.0) || !std::isfinite(M)) {   // nothing to scale (or not finite): the FP64 path, from Pp
+    int sx0 = (L0.n[1] + 3) * (L0.n[2] + 3), sy0 = L0.n[2] + 3;
+    dim3 gk0, bk0; col_dims(L0, gk0, bk0);
+    const double *rhs = c.f[SARAS_FIELD_MGRHS];
+    // the FP64 path's start (b in level-0 r, p = Pp) when the fixed-point path gives up
+    bool bDone = false;
+    auto fp64_start = [&]() -> int {
         dim3 gi, bi; core_dims(L0, gi, bi);
+        if (!bDone) k_tgt_rhs<<<gk0, bk0, 0, c.stream>>>(L0.r, rhs, sx0, sy0, bc0, mean);
         k_mg_init_p<double><<<gi, bi, 0, c.stream>>>(lview<double>(L0, L0.pa()), lcview<double>(L0, pp0), bc0);
-        count_launch(c);
-        return chk(c, "fixed-point skip");
-    }
+        count_launch(c, bDone ? 1 : 2);
+        return chk(c, "fixed-point fallback");
+    };
+    if (!(M > 0.0) || !std::isfinite(M)) return fp64_start();   // nothing to scale (or not finite)
     int sc = 54 - std::ilogb(M);
     sc = std::max(-900, std::min(900, sc));
     double inv2s = std::ldexp(1.0, -sc);
     double rs = l * inv2s;   // residual units -> value
-    int sx0 = (L0.n[1] + 3) * (L0.n[2] + 3), sy0 = L0.n[2] + 3;
     dim3 gm0, bm0; march_dims(L0, gm0, bm0);
-    dim3 gk0, bk0; col_dims(L0, gk0, bk0);
     dim3 gc, bcd; core_dims(L0, gc, bcd);
-    k_fx_rhs<<<gc, bcd, 0, c.stream>>>(B, L0.r, sx0, sy0, bc0, std::ldexp(1.0, sc) / l, dflag);
+    // b itself only where it is read: the learned guess's restricted history, and pairs collected for training
+    bDone = c.collecting || unet_tracking(c);
+    k_fx_rhs<<<gk0, bk0, 0, c.stream>>>(B, bDone ? L0.r : nullptr, rhs, sx0, sy0, bc0, mean, std::ldexp(1.0, sc) / l, dflag);
     count_launch(c);
     // With Pp's buffer free for the output (the previous Pp is pHist[0]), every
     // refinement update writes its FP64 iterate into Pp's core as it goes.
@@ -2171,7 +2210,7 @@ static int mixed_fixed(Ctx &c, const double *pp0, double bmax, double pmax, doub
         prof_end(c, PK_GUESS, 0, 0.0);
         if (gs == SARAS_OK) {
             if ((s = refine(1, false, rg, bad))) return s;
-            if (bad) return SARAS_OK;
+            if (bad) return fp64_start();
             if (rg <= kGuessTrusted * bmax) {
                 r = rg;
                 source = built;
@@ -2186,10 +2225,10 @@ static int mixed_fixed(Ctx &c, const double *pp0, double bmax, double pmax, doub
         k_fx_init<<<gc, bcd, 0, c.stream>>>(c.fx[0], lcview<double>(L0, pp0), bc0, sc, dflag);
         count_launch(c);
         if ((s = refine(0, false, r, bad))) return s;
-        if (bad) return SARAS_OK;
+        if (bad) return fp64_start();
         if (gs == SARAS_OK && rg < r) {   // the guess after all: its FP32 residual back into r32
             if ((s = refine(1, false, rg, bad))) return s;
-            if (bad) return SARAS_OK;
+            if (bad) return fp64_start();
             r = rg;
             source = built;
             cur = 1;
@@ -2230,10 +2269,8 @@ static int mixed_fixed(Ctx &c, const double *pp0, double bmax, double pmax, doub
     }
     // out of range: restart from the previous Pp in FP64
     L0.cur = 0;
-    k_mg_init_p<double><<<gc, bcd, 0, c.stream>>>(lview<double>(L0, L0.pa()), lcview<double>(L0, pp0), bc0);
-    count_launch(c);
     r = 0; source = 0; cyc = 0; steps = 0;
-    return chk(c, "fixed-point fallback");
+    return fp64_start();
 }
 
 // Target modes: plain FP64 V-cycles or FP32 V-cycles inside FP64 refinement.
@@ -2244,17 +2281,7 @@ static int mg_solve_target_run(Ctx &c, int *cycles, double *residual, saras_step
     dim3 g, b; core_dims(L0, g, b);
     long ncore = (long)(L0.n[0] + 1) * (L0.n[1] + 1) * (L0.n[2] + 1);
     int nb = std::min(grid_blocks(ncore), c.redCap);
-    // b = rhs - trapezoidal mean (stored in level-0 FP64 r)
     SARAS_CUDA_TRY(cudaMemsetAsync(c.dscal + 30, 0, sizeof(double) * 6, c.stream));
-    dim3 gmr, bmr; march_dims(L0, gmr, bmr);
-    int nparts = (int)(gmr.x * gmr.y * gmr.z);
-    if (nparts > c.redCap) { c.err = "reduction buffer too small"; return SARAS_TOO_LARGE; }
-    k_trap_sum<<<gmr, bmr, 0, c.stream>>>(lcview<double>(L0, c.f[SARAS_FIELD_MGRHS]), bc0, c.red);
-    k_final_reduce<<<1, 256, 0, c.stream>>>(c.red, nparts, 0, c.dscal + 30);
-    double wsum = 1.0;
-    for (int d = 0; d < 3; ++d) wsum *= (double)L0.n[d];
-    k_tgt_rhs<<<gmr, bmr, 0, c.stream>>>(lview<double>(L0, L0.r), lcview<double>(L0, c.f[SARAS_FIELD_MGRHS]), bc0, c.dscal + 30, 1.0 / wsum,
-                                        c.dscal + 31);
     // pressure history for the learned / extrapolated guess
     bool wantGuess = c.guessMode != SARAS_GUESS_PREVIOUS;
     if (wantGuess || c.collecting) {
@@ -2264,21 +2291,42 @@ static int mg_solve_target_run(Ctx &c, int *cycles, double *residual, saras_step
         if (s) return s;
     }
     const double *pp0 = c.ppInHist ? c.pHist[0] : c.f[SARAS_FIELD_PP];   // the previous Pp
-    // p = Pp (initial guess) with face ghosts; the fixed-point path reads Pp
-    // itself and only needs max|Pp| for its scale
+    const double *rhs = c.f[SARAS_FIELD_MGRHS];
+    // the fixed-point path forms b = rhs - trapezoidal mean itself and needs
+    // max|Pp| for its scale; the FP64 path stores b in level-0 r and starts
+    // from p = Pp with face ghosts
     bool fixedPath = c.mgMode == SARAS_MG_MIXED && L0.lx == L0.ly && L0.ly == L0.lz;
-    L0.cur = 0;
-    if (fixedPath) k_maxabs<<<grid_blocks(L0.count), 256, 0, c.stream>>>(pp0, L0.count, c.dscal + 33);
-    else k_mg_init_p<double><<<g, b, 0, c.stream>>>(lview<double>(L0, L0.pa()), lcview<double>(L0, pp0), bc0);
-    count_launch(c, 4);
-    if ((s = chk(c, "target load"))) return s;
-    if ((s = read_scalars(c, 31, 3))) return s;
-    double bmax = c.hscal[31], pmax = c.hscal[33];
-    double target = c.mgTarget * bmax;
     int sx0 = (L0.n[1] + 3) * (L0.n[2] + 3), sy0 = L0.n[2] + 3;
+    dim3 gk0, bk0; col_dims(L0, gk0, bk0);
+    int nparts = (int)(gk0.x * gk0.y);
+    if (nparts > c.redCap) { c.err = "reduction buffer too small"; return SARAS_TOO_LARGE; }
+    k_tgt_stats<<<gk0, bk0, 0, c.stream>>>(lcview<double>(L0, rhs), fixedPath ? pp0 : nullptr, bc0, c.red, c.dscal + 31, c.dscal + 32,
+                                           c.dscal + 33);
+    k_final_reduce<<<1, 256, 0, c.stream>>>(c.red, nparts, 0, c.dscal + 30);
+    count_launch(c, 2);
+    if ((s = chk(c, "target load"))) return s;
+    if ((s = read_scalars(c, 30, 4))) return s;
+    double wsum = 1.0;
+    for (int d = 0; d < 3; ++d) wsum *= (double)L0.n[d];
+    const double mean = c.hscal[30] * (1.0 / wsum);
+    double bmax, pmax = c.hscal[33];
+    {
+        unsigned long long kh, kl;
+        std::memcpy(&kh, &c.hscal[31], sizeof kh);
+        std::memcpy(&kl, &c.hscal[32], sizeof kl);
+        const double up = order_key_value(kh) - mean, dn = mean - order_key_value(~kl);
+        bmax = (std::isnan(up) || std::isnan(dn)) ? up + dn : std::max(up, dn);
+    }
+    L0.cur = 0;
+    if (!fixedPath) {
+        dim3 g, b; core_dims(L0, g, b);
+        k_tgt_rhs<<<gk0, bk0, 0, c.stream>>>(L0.r, rhs, sx0, sy0, bc0, mean);
+        k_mg_init_p<double><<<g, b, 0, c.stream>>>(lview<double>(L0, L0.pa()), lcview<double>(L0, pp0), bc0);
+        count_launch(c, 2);
+    }
+    double target = c.mgTarget * bmax;
     TgK<double> t0 = make_tgk<double>(L0, 1.0);
     dim3 gm0, bm0; march_dims(L0, gm0, bm0);
-    dim3 gk0, bk0; col_dims(L0, gk0, bk0);
     auto fine_res = [&](bool withE, double *out) -> int {
         SARAS_CUDA_TRY(cudaMemsetAsync(c.dscal + 32, 0, sizeof(double), c.stream));
         if (withE) {
@@ -2307,7 +2355,7 @@ static int mg_solve_target_run(Ctx &c, int *cycles, double *residual, saras_step
     int source = 0, cyc = 0, steps = 0, built = 0;
     bool fixedDone = false;
     if (fixedPath) {
-        if ((s = mixed_fixed(c, pp0, bmax, pmax, target, wantGuess, r, source, cyc, steps, fixedDone, st))) return s;
+        if ((s = mixed_fixed(c, pp0, mean, bmax, pmax, target, wantGuess, r, source, cyc, steps, fixedDone, st))) return s;
     }
     if (!fixedDone) {
     if ((s = fine_res(false, &r))) return s;

@@ -873,6 +873,12 @@ static bool rings_due(const Ctx &c, const UNet *u) {
     return u->usesExt >= 2 && u->solves + 3 >= u->nextProbe;
 }
 
+// Whether this solve pushes R b (the FP64 b must then be stored).
+bool unet_tracking(const Ctx &c) {
+    const UNet *u = reinterpret_cast<const UNet *>(c.unet);
+    return u && u->track;
+}
+
 // Called at the start of a target-mode solve: rotate the pressure history
 // (and, in the solves that keep them, its restriction to level lb).  When Pp
 // and a history buffer have one size, the rotation moves buffers instead of
