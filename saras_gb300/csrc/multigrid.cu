@@ -756,8 +756,13 @@ __device__ __forceinline__ long nbr_x(int i, int d, int sx, const MgBC &bc) {
     return (long)(pad_img(i + d, bc.E[0], bc.per[0]) - i) * sx;
 }
 
+// FP32: __launch_bounds__(256, 6) caps the registers at 40 (six blocks a SM):
+// with them the sweep keeps more of a segment's loads in flight than with the
+// 32 the compiler picks unbounded (46.5 us against 49.0 a level-0 sweep at
+// 257^3; 4 and 5 blocks measured 48.7 and 47.4).  FP64 sweeps wait on the
+// FP64 pipe instead; five blocks leave them the registers they took unbounded.
 template <typename T, bool ZERO>
-__global__ void __launch_bounds__(256) k_tgt_sweep(T *__restrict__ out, const T *__restrict__ in, const T *__restrict__ r,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 6 : 5) k_tgt_sweep(T *__restrict__ out, const T *__restrict__ in, const T *__restrict__ r,
                                                    int sx, int sy, MgBC bc, TgK<T> c) {
     int j, k, seg;
     if (!col_of<sizeof(T) == 8>(bc, j, k, seg)) return;
@@ -855,12 +860,35 @@ __global__ void __launch_bounds__(256) k_tgt_prolong_add(T *__restrict__ pf, con
 
 // r_out = b - Lap(p) over the core; optional max |r| (FP64 accumulation).
 template <typename T, typename OT, bool MAXRED>
-__global__ void __launch_bounds__(256) k_tgt_residual(OT *__restrict__ out, const T *__restrict__ p, const T *__restrict__ b,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 6 : 5) k_tgt_residual(OT *__restrict__ out, const T *__restrict__ p, const T *__restrict__ b,
                                                       int sx, int sy, MgBC bc, TgK<T> c, double *maxres) {
     int j, k, seg;
     const bool on = col_of<sizeof(T) == 8>(bc, j, k, seg);
     const int i0 = seg * kIch;
     unsigned long long m = 0ull;
+    if (!MAXRED && on && i0 + kIch <= bc.E[0]) {
+        // a full column segment (as in k_tgt_sweep): every load before the first store
+        const NbrJK nb = nbr_jk(j, k, sy, bc);
+        const long o0 = (long)(i0 + 1) * sx + (long)(j + 1) * sy + (k + 1);
+        T nc[kIch + 1], ns[kIch], ud[kIch], rr[kIch];
+        T cm = p[o0 + nbr_x(i0, -1, sx, bc)];
+        nc[0] = p[o0];
+#pragma unroll
+        for (int q = 0; q < kIch; ++q) {
+            long o = o0 + (long)q * sx;
+            nc[q + 1] = p[o + sx];
+            ns[q] = p[o + nb.yp] + p[o + nb.ym];
+            ud[q] = p[o + nb.zp] + p[o + nb.zm];
+            rr[q] = b[o];
+        }
+#pragma unroll
+        for (int q = 0; q < kIch; ++q) {
+            T lap = fma(c.lx, cm + nc[q + 1], fma(c.ly, ns[q], fma(c.lz, ud[q], c.lc * nc[q])));
+            out[o0 + (long)q * sx] = (OT)(rr[q] - lap);
+            cm = nc[q];
+        }
+        return;
+    }
     if (on) {
         int iend = min(i0 + kIch - 1, bc.E[0]);
         const NbrJK nb = nbr_jk(j, k, sy, bc);

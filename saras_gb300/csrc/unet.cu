@@ -870,7 +870,7 @@ static bool rings_due(const Ctx &c, const UNet *u) {
     if (c.collecting) return true;
     if (c.guessMode != SARAS_GUESS_LEARNED || !u->trained) return false;
     if (u->wantNet || u->usesNet < 2 || u->preferNet) return true;
-    return u->usesExt >= 2 && u->solves + 3 >= u->nextProbe;
+    return u->usesExt >= 2 && u->nextProbe > 0 && u->solves + 3 >= u->nextProbe;
 }
 
 // Whether this solve pushes R b (the FP64 b must then be stored).
@@ -942,6 +942,7 @@ int unet_pick(Ctx &c) {
         net = false;
     } else {
         bool netBetter = u->cycNet + kNetCostCycles < u->cycExt;
+        if (u->nextProbe == 0) u->nextProbe = u->solves + kProbe;   // the first comparison starts the schedule
         if (netBetter != u->preferNet) {
             u->preferNet = netBetter;
             u->probeEvery = kProbe;
