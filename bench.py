@@ -49,15 +49,17 @@ def tgv_params(mode, guess=0, ind=GRID_INDEX, depth=DEPTH):
     p.cnTolerance = 1.0e-8
     p.mgTolerance = 1.0e-8
     # both target-mode arms with the cycle each is fastest with at 257^3
-    # (ms a step): plain FP64 -- Chebyshev-smoothed cycles with 3 sweeps a phase
-    # and a W-cycle at the second level 23.6 (V-cycle 27.0, V-cycle with 8
-    # coarse sweeps 24.0, damped-Jacobi V(3,3) 31.1); mixed -- Chebyshev V(3,3)
-    # 5.40 (3 cycles in one refinement step; the W-cycle at the second level
-    # with 6 coarse sweeps needs 2 cycles but takes 5.62), refinement steps
-    # sized by the measured contraction per cycle
-    p.preSmooth = p.postSmooth = 3
+    # (ms a step): plain FP64 -- Chebyshev (2,2) cycles with three cycles at
+    # the second level a visit, 15.5 (4 cycles; with two 16.6, four 17.1,
+    # Chebyshev (3,3) with three 19.0, damped-Jacobi (2,2) with three 21.7,
+    # Chebyshev V(3,3) 23.9); mixed -- Chebyshev V(3,3) 4.61 (3 cycles in one
+    # refinement step; V(2,2) 4.68 with 4, (2,2) with two cycles at the second
+    # level 4.70, (3,3) with three 4.86), refinement steps sized by the
+    # measured contraction per cycle
+    plain = mode == _abi.MG_PLAIN_TARGET
+    p.preSmooth = p.postSmooth = 2 if plain else 3
     p.smoother = _abi.SMOOTHER_CHEBYSHEV if mode != _abi.MG_REFERENCE else _abi.SMOOTHER_JACOBI
-    p.coarseCycles = 2 if mode == _abi.MG_PLAIN_TARGET else 1
+    p.coarseCycles = 3 if plain else 1
     p.mgMode = mode
     p.mgTarget = TARGET
     p.mgMaxCycles = 100
@@ -340,7 +342,7 @@ def run_ours(args, dist):
             "workload": "Taylor-Green vortex 257^3 (2^8+1 vertex points per axis), [0,2pi]^3 PPP, Re 1600, dt 5e-4; "
                         "pressure solve: FP32 V(3,3) cycles (Chebyshev-weighted Jacobi smoothing) inside iterative refinement with an "
                         "exact fixed-point residual, refinement steps sized by the measured contraction per cycle, to "
-                        "max|b-Ap|/max|b| <= 1e-8; plain arm: FP64 cycles with the same smoothing and a W-cycle at the second level, same residual",
+                        "max|b-Ap|/max|b| <= 1e-8; plain arm: FP64 Chebyshev (2,2) cycles with three cycles at the second level a visit, same residual",
             "grid": [257, 257, 257], "vcycle_depth": DEPTH, "mg_mode": "mixed_fp32_in_fp64",
             "warm_start": "unet (3-level 16/32/64, tcgen05 BF16 convs) correcting 2 Pp(n-1) - Pp(n-2), "
                           "least-squares step length, fallback to the previous pressure"

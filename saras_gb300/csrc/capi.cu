@@ -281,6 +281,15 @@ static int validate(const saras_params *p, std::string &why) {
         return SARAS_BAD_CONFIG;
     }
     if (p->coarseSmooth < 0) { why = "negative Coarse Smoothing Count"; return SARAS_BAD_CONFIG; }
+    // Target-mode cycles on a periodic axis need three sweeps a level at least:
+    // V(1,1) cycles (weight 6/7, either smoother) stalled near 1e-5 of max|b|
+    // on the 65^3 Taylor-Green vortex and then diverged; V(2,1), V(1,2) and
+    // V(2,2) converged.
+    if (p->mgMode != SARAS_MG_REFERENCE && (p->xPer || p->yPer || p->zPer) &&
+        (p->preSmooth + p->postSmooth < 3 || (p->coarseSmooth > 0 && 2 * p->coarseSmooth < 3))) {
+        why = "target multigrid modes on periodic axes need at least 3 smoothing sweeps a level (pre + post, or 2 x Coarse Smoothing Count)";
+        return SARAS_BAD_CONFIG;
+    }
     if (p->coarseCycles < 0 || p->coarseCycles > 4) { why = "Coarse Cycles must be 0 to 4"; return SARAS_BAD_CONFIG; }
     if (p->resType < 0 || p->resType > 2) { why = "bad residual type"; return SARAS_BAD_CONFIG; }
     return SARAS_OK;

@@ -70,3 +70,14 @@ def test_bad_config_rejected_before_device():
     with pytest.raises(saras_gb300.SarasError) as e:
         saras_gb300.Solver(p)
     assert e.value.status == _abi.BAD_CONFIG
+
+
+def test_periodic_target_mode_needs_three_sweeps():
+    """V(1,1) target-mode cycles diverge on periodic axes: rejected before any device work."""
+    for pre, post, cs in ((1, 1, 0), (2, 2, 1)):
+        p = _abi.default_params()
+        p.mgMode = _abi.MG_MIXED
+        p.preSmooth, p.postSmooth, p.coarseSmooth = pre, post, cs
+        with pytest.raises(saras_gb300.SarasError) as e:
+            saras_gb300.Solver(p)
+        assert e.value.status == _abi.BAD_CONFIG
