@@ -262,6 +262,12 @@ int saras_profile_read(saras_ctx *ctx, int kernel_id, long long *launches,
                        double *total_ms, double *bytes);
 const char *saras_profile_name(int kernel_id);
 int saras_profile_count(void);
+/* Time the kernels of one replayed target-mode V-cycle in `every` (1: all, the
+ * default).  The timing events inside a replayed cycle separate its kernels
+ * on the GPU (about 0.14 ms a 257^3 step for the six level-0 sweeps of three
+ * cycles); sampled replays keep that cost to 1/every while the timed launches
+ * still spread over the whole run.  Launches outside V-cycles are all timed. */
+int saras_profile_sample(saras_ctx *ctx, int every);
 /* CUDA events on the context stream for whole-step timing: record event
  * `slot` (0..15) now; elapsed milliseconds between two recorded slots. */
 int saras_event_record(saras_ctx *ctx, int slot);

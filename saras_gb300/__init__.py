@@ -235,6 +235,10 @@ class Solver:
     def profile_enable(self, kernel_id, enable=True):
         self._chk(self.lib.saras_profile_enable(self.h, kernel_id, 1 if enable else 0))
 
+    def profile_sample(self, every):
+        """Time the kernels of one replayed V-cycle in `every` (saras_profile_sample)."""
+        self._chk(self.lib.saras_profile_sample(self.h, int(every)))
+
     def profile_read(self, kernel_id):
         n, ms, b = ctypes.c_longlong(), ctypes.c_double(), ctypes.c_double()
         self._chk(self.lib.saras_profile_read(self.h, kernel_id, ctypes.byref(n), ctypes.byref(ms), ctypes.byref(b)))

@@ -170,6 +170,7 @@ def load():
         "saras_profile_read": (_I, [vp, _I, ctypes.POINTER(ctypes.c_longlong), dp, dp]),
         "saras_profile_name": (cp, [_I]),
         "saras_profile_count": (_I, []),
+        "saras_profile_sample": (_I, [vp, _I]),
         "saras_event_record": (_I, [vp, _I]),
         "saras_event_elapsed": (_I, [vp, _I, _I, dp]),
     }

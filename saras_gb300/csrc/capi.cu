@@ -32,11 +32,24 @@ static void prof_capture_event(Ctx &c, int k, bool end, double bytes) {
     c.profCaptured.push_back(n);
 }
 
+// Timing events come from a pool (created once, returned by prof_drain), so
+// profiling a replayed V-cycle costs its event-node updates and no event
+// creation on the host path between the GPU's launches.
+static cudaEvent_t prof_event(Ctx &c) {
+    if (!c.evPool.empty()) {
+        cudaEvent_t e = c.evPool.back();
+        c.evPool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    return e;
+}
+
 void prof_begin(Ctx &c, int k, int level) {
-    if (level != 0 || k < 0 || k >= PK_COUNT || !c.prof[k].enabled) return;
+    if (level != 0 || k < 0 || k >= PK_COUNT || !c.prof[k].enabled || c.profSuppress) return;
     if (c.profCapturing) { prof_capture_event(c, k, false, 0.0); return; }
-    cudaEvent_t e;
-    cudaEventCreate(&e);
+    cudaEvent_t e = prof_event(c);
     cudaEventRecord(e, c.stream);
     c.prof[k].ev.push_back(e);
 }
@@ -50,17 +63,16 @@ static void prof_drain(Ctx &c, int k) {
         float ms = 0;
         cudaEventElapsedTime(&ms, s.ev[2 * q], s.ev[2 * q + 1]);
         s.ms += ms;
-        cudaEventDestroy(s.ev[2 * q]);
-        cudaEventDestroy(s.ev[2 * q + 1]);
+        c.evPool.push_back(s.ev[2 * q]);
+        c.evPool.push_back(s.ev[2 * q + 1]);
     }
     s.ev.erase(s.ev.begin(), s.ev.begin() + 2 * pairs);
 }
 
 void prof_end(Ctx &c, int k, int level, double bytes) {
-    if (level != 0 || k < 0 || k >= PK_COUNT || !c.prof[k].enabled) return;
+    if (level != 0 || k < 0 || k >= PK_COUNT || !c.prof[k].enabled || c.profSuppress) return;
     if (c.profCapturing) { prof_capture_event(c, k, true, bytes); return; }
-    cudaEvent_t e;
-    cudaEventCreate(&e);
+    cudaEvent_t e = prof_event(c);
     cudaEventRecord(e, c.stream);
     c.prof[k].ev.push_back(e);
     c.prof[k].launches += 1;
@@ -70,10 +82,10 @@ void prof_end(Ctx &c, int k, int level, double bytes) {
 
 int prof_graph_replay(Ctx &c, cudaGraphExec_t ge, const std::vector<ProfNode> &nodes) {
     for (const ProfNode &n : nodes) {
-        cudaEvent_t e;
-        if (cudaEventCreate(&e) != cudaSuccess) return SARAS_CUDA_ERROR;
+        cudaEvent_t e = prof_event(c);
+        if (!e) return SARAS_CUDA_ERROR;
         if (cudaGraphExecEventRecordNodeSetEvent(ge, n.node, e) != cudaSuccess) {
-            cudaEventDestroy(e);
+            c.evPool.push_back(e);
             return SARAS_CUDA_ERROR;
         }
         ProfSlot &s = c.prof[n.slot];
@@ -345,6 +357,7 @@ int saras_destroy(saras_ctx *h) {
     for (int q = 0; q < 3; ++q) cudaFree(c.pHist[q]);
     cudaFree(c.cnp);
     for (int k = 0; k < PK_COUNT; ++k) for (cudaEvent_t e : c.prof[k].ev) cudaEventDestroy(e);
+    for (cudaEvent_t e : c.evPool) cudaEventDestroy(e);
     for (int k = 0; k < 16; ++k) if (c.userEv[k]) cudaEventDestroy(c.userEv[k]);
     if (c.stream) cudaStreamDestroy(c.stream);
     delete h;
@@ -473,6 +486,11 @@ int saras_profile_enable(saras_ctx *h, int kernel_id, int enable) {
     prof_drain(h->c, kernel_id);
     if (enable) { s.launches = 0; s.bytes = 0; s.ms = 0; }
     s.enabled = enable != 0;
+    while (enable && h->c.evPool.size() < 1024) {   // events for a few hundred timed launches up front
+        cudaEvent_t e = nullptr;
+        SARAS_CUDA_TRY(cudaEventCreate(&e));
+        h->c.evPool.push_back(e);
+    }
     return SARAS_OK;
 }
 
@@ -484,6 +502,13 @@ int saras_profile_read(saras_ctx *h, int kernel_id, long long *launches, double 
     if (launches) *launches = s.launches;
     if (total_ms) *total_ms = s.ms;
     if (bytes) *bytes = s.bytes;
+    return SARAS_OK;
+}
+
+int saras_profile_sample(saras_ctx *h, int every) {
+    if (!h || every < 1) return SARAS_BAD_ARG;
+    h->c.profEvery = every;
+    h->c.profReplays = 0;
     return SARAS_OK;
 }
 

@@ -125,18 +125,24 @@ struct Ctx {
     double *coarseM64 = nullptr;   // coarsest-level solution operator (coarseN x coarseN, row-major)
     float *coarseM32 = nullptr;
     // target-mode V-cycles replayed as CUDA graphs: [FP32?][zero start?]
-    cudaGraphExec_t vgraph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
-    cudaGraph_t vgraphSrc[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};   // kept for the event-node handles
-    std::vector<ProfNode> vgraphProf[2][2];   // profiling event nodes of each graph, in capture order
+    // [FP32?][zero start?][timed?]: with profiling on, the timed instance holds
+    // the profiling event nodes and replays one cycle in profEvery
+    cudaGraphExec_t vgraph[2][2][2] = {};
+    cudaGraph_t vgraphSrc[2][2][2] = {};      // kept for the event-node handles
+    std::vector<ProfNode> vgraphProf[2][2][2];   // profiling event nodes of each graph, in capture order
     bool profCapturing = false;               // prof_begin / prof_end record graph event nodes
+    bool profSuppress = false;                // prof_begin / prof_end record nothing (untimed capture)
+    int profEvery = 1;
+    long long profReplays = 0;
     std::vector<ProfNode> profCaptured;
-    long long vgraphLaunches[2][2] = {{0, 0}, {0, 0}};
-    std::vector<int> vgraphState[2][2];
+    long long vgraphLaunches[2][2][2] = {};
+    std::vector<int> vgraphState[2][2][2];
     int histCount = 0;
     bool ppInHist = false;    // Pp's buffer moved to pHist[0] by unet_begin_solve; the solve has not written Pp yet
     bool collecting = false;
     // profiling
     ProfSlot prof[PK_COUNT];
+    std::vector<cudaEvent_t> evPool;          // timing events not in use
     cudaEvent_t userEv[16] = {nullptr};
     std::string err;
 };

@@ -1909,25 +1909,32 @@ static int vcycle(Ctx &c, bool tgt, bool zero0) {
 // of times per cycle (pre + post smoothing) and so returns to its starting
 // state.  The graph is rebuilt when the level states differ from the ones it
 // was captured with; with kernel profiling on, the cycle runs uncaptured.
-static std::vector<int> level_state(const Ctx &c) {
+static std::vector<int> level_state(const Ctx &c, bool timed) {
     std::vector<int> st;
     for (const Level &L : c.lv) { st.push_back(L.cur); st.push_back(L.cur32); }
-    for (const ProfSlot &ps : c.prof) st.push_back(ps.enabled ? 1 : 0);   // the profiling event nodes it holds
+    for (const ProfSlot &ps : c.prof) st.push_back(timed && ps.enabled ? 1 : 0);   // the profiling event nodes it holds
     return st;
 }
 
-static void vgraph_drop(Ctx &c, int a, int b) {
-    if (c.vgraph[a][b]) cudaGraphExecDestroy(c.vgraph[a][b]);
-    if (c.vgraphSrc[a][b]) cudaGraphDestroy(c.vgraphSrc[a][b]);
-    for (ProfNode &n : c.vgraphProf[a][b]) cudaEventDestroy(n.captured);
-    c.vgraph[a][b] = nullptr;
-    c.vgraphSrc[a][b] = nullptr;
-    c.vgraphProf[a][b].clear();
+static bool any_profiling(const Ctx &c) {
+    for (const ProfSlot &ps : c.prof)
+        if (ps.enabled) return true;
+    return false;
+}
+
+static void vgraph_drop(Ctx &c, int a, int b, int t) {
+    if (c.vgraph[a][b][t]) cudaGraphExecDestroy(c.vgraph[a][b][t]);
+    if (c.vgraphSrc[a][b][t]) cudaGraphDestroy(c.vgraphSrc[a][b][t]);
+    for (ProfNode &n : c.vgraphProf[a][b][t]) cudaEventDestroy(n.captured);
+    c.vgraph[a][b][t] = nullptr;
+    c.vgraphSrc[a][b][t] = nullptr;
+    c.vgraphProf[a][b][t].clear();
 }
 
 void vgraph_reset(Ctx &c) {
     for (int a = 0; a < 2; ++a)
-        for (int b = 0; b < 2; ++b) vgraph_drop(c, a, b);
+        for (int b = 0; b < 2; ++b)
+            for (int t = 0; t < 2; ++t) vgraph_drop(c, a, b, t);
 }
 
 // The event-record nodes of graph g that carry the profiling events recorded
@@ -1956,17 +1963,22 @@ static int map_prof_nodes(Ctx &c, cudaGraph_t g, std::vector<ProfNode> &out) {
 
 template <typename T>
 static int vcycle_tgt(Ctx &c, bool zero0) {
-    int a = sizeof(T) == 4 ? 1 : 0, b = zero0 ? 1 : 0;
-    std::vector<int> st = level_state(c);
-    if (c.vgraph[a][b] && c.vgraphState[a][b] != st) vgraph_drop(c, a, b);
-    if (!c.vgraph[a][b]) {
+    // with profiling on, one replay in profEvery runs the instance holding the
+    // timing event nodes; the others run an instance captured without them
+    const int a = sizeof(T) == 4 ? 1 : 0, b = zero0 ? 1 : 0;
+    const int t = any_profiling(c) && (c.profEvery <= 1 || c.profReplays++ % c.profEvery == 0) ? 1 : 0;
+    std::vector<int> st = level_state(c, t == 1);
+    if (c.vgraph[a][b][t] && c.vgraphState[a][b][t] != st) vgraph_drop(c, a, b, t);
+    if (!c.vgraph[a][b][t]) {
         long long l0 = c.launches;
         for (ProfNode &n : c.profCaptured) cudaEventDestroy(n.captured);
         c.profCaptured.clear();
         SARAS_CUDA_TRY(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
         c.profCapturing = true;
+        c.profSuppress = t == 0;
         int s = vcycle<T>(c, true, zero0);
         c.profCapturing = false;
+        c.profSuppress = false;
         cudaGraph_t g = nullptr;
         cudaError_t e = cudaStreamEndCapture(c.stream, &g);
         if (s || e != cudaSuccess) {
@@ -1978,28 +1990,28 @@ static int vcycle_tgt(Ctx &c, bool zero0) {
             c.err = std::string("V-cycle capture: ") + cudaGetErrorString(e);
             return SARAS_CUDA_ERROR;
         }
-        c.vgraphSrc[a][b] = g;
-        if ((s = map_prof_nodes(c, g, c.vgraphProf[a][b]))) { vgraph_drop(c, a, b); return s; }
-        e = cudaGraphInstantiate(&c.vgraph[a][b], g, 0);
+        c.vgraphSrc[a][b][t] = g;
+        if ((s = map_prof_nodes(c, g, c.vgraphProf[a][b][t]))) { vgraph_drop(c, a, b, t); return s; }
+        e = cudaGraphInstantiate(&c.vgraph[a][b][t], g, 0);
         if (e != cudaSuccess) {
-            c.vgraph[a][b] = nullptr;
-            vgraph_drop(c, a, b);
+            c.vgraph[a][b][t] = nullptr;
+            vgraph_drop(c, a, b, t);
             c.err = std::string("V-cycle graph: ") + cudaGetErrorString(e);
             return SARAS_CUDA_ERROR;
         }
-        c.vgraphLaunches[a][b] = c.launches - l0;
+        c.vgraphLaunches[a][b][t] = c.launches - l0;
         c.launches = l0;
-        c.vgraphState[a][b] = st;
-        if (level_state(c) != st) {   // a cycle that does not restore the level states is never replayed:
-            vgraph_drop(c, a, b);     // back to the states before the capture, then run it directly
+        c.vgraphState[a][b][t] = st;
+        if (level_state(c, t == 1) != st) {   // a cycle that does not restore the level states is never replayed:
+            vgraph_drop(c, a, b, t);          // back to the states before the capture, then run it directly
             for (size_t q = 0; q < c.lv.size(); ++q) { c.lv[q].cur = st[2 * q]; c.lv[q].cur32 = st[2 * q + 1]; }
             return vcycle<T>(c, true, zero0);
         }
     }
-    int s = prof_graph_replay(c, c.vgraph[a][b], c.vgraphProf[a][b]);
+    int s = prof_graph_replay(c, c.vgraph[a][b][t], c.vgraphProf[a][b][t]);
     if (s) { c.err = "V-cycle graph: profiling events"; return s; }
-    SARAS_CUDA_TRY(cudaGraphLaunch(c.vgraph[a][b], c.stream));
-    c.launches += c.vgraphLaunches[a][b];
+    SARAS_CUDA_TRY(cudaGraphLaunch(c.vgraph[a][b][t], c.stream));
+    c.launches += c.vgraphLaunches[a][b][t];
     return SARAS_OK;
 }
 

@@ -111,6 +111,31 @@ def test_profiling_inside_replayed_vcycles():
     assert ms > 0.0 and b > 0.0
 
 
+def test_profiling_sampled_vcycles():
+    """saras_profile_sample(every): one replayed V-cycle in `every` carries the
+    timing events (the first of the run, then every `every`-th); the others
+    run the untimed graph, and the solves are unchanged."""
+    p, g = target_case(F.MG_MIXED)
+    _, ref = target_case(F.MG_MIXED)
+    names = S.Solver.profile_names()
+    k = names.index("mg_smooth_fp32")
+    for _ in range(2):
+        assert g.time_advance()[0] == 0
+        assert ref.time_advance()[0] == 0
+    g.profile_enable(k, True)
+    g.profile_sample(3)
+    cycles = 0
+    for _ in range(4):
+        s, st = g.time_advance()
+        s2, st2 = ref.time_advance()
+        assert s == 0 and s2 == 0 and st.vcycles == st2.vcycles
+        cycles += st.vcycles
+    n, ms, b = g.profile_read(k)
+    assert n == ((cycles + 2) // 3) * (p.preSmooth + p.postSmooth)
+    assert ms > 0.0 and b > 0.0
+    assert np.array_equal(g.get(F.FIELD_P), ref.get(F.FIELD_P))
+
+
 def test_adaptive_refinement_cycles():
     """mixedCycles = 0: each refinement step runs the V-cycles that the measured
     contraction predicts; the target is met with fewer refinement steps than
