@@ -2474,6 +2474,12 @@ int mg_solve(Ctx &c, int *cycles, double *residual, saras_step_stats *st) {
     SARAS_CUDA_TRY(cudaMemsetAsync(c.dscal + 40, 0, sizeof(double), c.stream));
     int s = c.mgMode == SARAS_MG_REFERENCE ? mg_solve_reference(c, cycles, residual) : mg_solve_target(c, cycles, residual, st);
     if (s) return s;
+    if (c.mgMode != SARAS_MG_REFERENCE && c.tailLt >= 0 && c.coarseN > 0) {
+        // the coarsest level is solved by its operator: no Gauss-Seidel
+        // iterations to count, and no synchronisation to read them
+        if (st) st->coarse_iters = 0;
+        return SARAS_OK;
+    }
     SARAS_CUDA_TRY(cudaMemcpyAsync(&before, c.dscal + 40, sizeof(long long), cudaMemcpyDeviceToHost, c.stream));
     SARAS_CUDA_TRY(cudaStreamSynchronize(c.stream));
     c.coarseIters += before;
