@@ -160,6 +160,13 @@ const char *saras_last_error(const saras_ctx *ctx);
 int saras_field_dims(const saras_ctx *ctx, int field, int dims[3]);
 int saras_upload(saras_ctx *ctx, int field, const double *host);
 int saras_download(saras_ctx *ctx, int field, double *host);
+/* Several fields at once (n <= SARAS_NUM_FIELDS): the copies run concurrently
+ * on their own streams, ordered after the context's work (download) or before
+ * it (upload), and the call returns when all of them are done, like n calls of
+ * saras_upload / saras_download.  Host buffers in page-locked memory let the
+ * copy engines work in parallel. */
+int saras_upload_fields(saras_ctx *ctx, int n, const int *fields, const double *const *hosts);
+int saras_download_fields(saras_ctx *ctx, int n, const int *fields, double *const *hosts);
 int saras_synchronize(saras_ctx *ctx);
 /* Number of device kernels this context has launched so far. */
 long long saras_launch_count(const saras_ctx *ctx);

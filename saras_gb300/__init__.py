@@ -259,6 +259,21 @@ class Solver:
     def download_ptr(self, field, ptr):
         self._chk(self.lib.saras_download(self.h, field, ctypes.cast(ptr, ctypes.POINTER(ctypes.c_double))))
 
+    def _fields_ptrs(self, fields, ptrs):
+        n = len(fields)
+        f = (ctypes.c_int * n)(*fields)
+        P = ctypes.POINTER(ctypes.c_double)
+        p = (P * n)(*[ctypes.cast(x, P) for x in ptrs])
+        return n, f, p
+
+    def upload_fields_ptr(self, fields, ptrs):
+        """Upload several fields at once from raw host pointers (concurrent copies)."""
+        self._chk(self.lib.saras_upload_fields(self.h, *self._fields_ptrs(fields, ptrs)))
+
+    def download_fields_ptr(self, fields, ptrs):
+        """Download several fields at once into raw host pointers (concurrent copies)."""
+        self._chk(self.lib.saras_download_fields(self.h, *self._fields_ptrs(fields, ptrs)))
+
     @staticmethod
     def profile_names():
         lib = _abi.load()

@@ -132,6 +132,8 @@ def load():
         "saras_field_dims": (_I, [vp, _I, ip]),
         "saras_upload": (_I, [vp, _I, dp]),
         "saras_download": (_I, [vp, _I, dp]),
+        "saras_upload_fields": (_I, [vp, _I, ip, ctypes.POINTER(dp)]),
+        "saras_download_fields": (_I, [vp, _I, ip, ctypes.POINTER(dp)]),
         "saras_synchronize": (_I, [vp]),
         "saras_launch_count": (ctypes.c_longlong, [vp]),
         "saras_apply_bc": (_I, [vp, _I]),

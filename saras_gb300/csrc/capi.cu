@@ -359,6 +359,8 @@ int saras_destroy(saras_ctx *h) {
     for (int k = 0; k < PK_COUNT; ++k) for (cudaEvent_t e : c.prof[k].ev) cudaEventDestroy(e);
     for (cudaEvent_t e : c.evPool) cudaEventDestroy(e);
     for (int k = 0; k < 16; ++k) if (c.userEv[k]) cudaEventDestroy(c.userEv[k]);
+    for (int q = 0; q < SARAS_NUM_FIELDS; ++q) if (c.copyStream[q]) cudaStreamDestroy(c.copyStream[q]);
+    for (int q = 0; q <= SARAS_NUM_FIELDS; ++q) if (c.copyEvent[q]) cudaEventDestroy(c.copyEvent[q]);
     if (c.stream) cudaStreamDestroy(c.stream);
     delete h;
     return SARAS_OK;
@@ -394,6 +396,41 @@ int saras_download(saras_ctx *h, int field, double *host) {
     SARAS_CUDA_TRY(cudaMemcpyAsync(host, c.f[field], sizeof(double) * field_count(c, field), cudaMemcpyDeviceToHost, c.stream));
     SARAS_CUDA_TRY(cudaStreamSynchronize(c.stream));
     return SARAS_OK;
+}
+
+// Field copies on one stream each: every copy stream waits for the context
+// stream's work so far, and (upload) the context stream waits for every copy.
+static int copy_fields(Ctx &c, int n, const int *fields, const void *const *hosts, bool up) {
+    if (n < 0 || n > SARAS_NUM_FIELDS || (n > 0 && (!fields || !hosts))) return SARAS_BAD_ARG;
+    for (int q = 0; q < n; ++q)
+        if (fields[q] < 0 || fields[q] >= SARAS_NUM_FIELDS || !hosts[q]) return SARAS_BAD_ARG;
+    for (int q = 0; q <= n; ++q)
+        if (!c.copyEvent[q]) SARAS_CUDA_TRY(cudaEventCreateWithFlags(&c.copyEvent[q], cudaEventDisableTiming));
+    SARAS_CUDA_TRY(cudaEventRecord(c.copyEvent[n], c.stream));
+    for (int q = 0; q < n; ++q) {
+        if (!c.copyStream[q]) SARAS_CUDA_TRY(cudaStreamCreateWithFlags(&c.copyStream[q], cudaStreamNonBlocking));
+        cudaStream_t st = c.copyStream[q];
+        SARAS_CUDA_TRY(cudaStreamWaitEvent(st, c.copyEvent[n], 0));
+        size_t bytes = sizeof(double) * field_count(c, fields[q]);
+        if (up) SARAS_CUDA_TRY(cudaMemcpyAsync(c.f[fields[q]], hosts[q], bytes, cudaMemcpyHostToDevice, st));
+        else SARAS_CUDA_TRY(cudaMemcpyAsync(const_cast<void *>(hosts[q]), c.f[fields[q]], bytes, cudaMemcpyDeviceToHost, st));
+        SARAS_CUDA_TRY(cudaEventRecord(c.copyEvent[q], st));
+    }
+    for (int q = 0; q < n; ++q) {
+        SARAS_CUDA_TRY(cudaStreamWaitEvent(c.stream, c.copyEvent[q], 0));
+        SARAS_CUDA_TRY(cudaEventSynchronize(c.copyEvent[q]));
+    }
+    return SARAS_OK;
+}
+
+int saras_upload_fields(saras_ctx *h, int n, const int *fields, const double *const *hosts) {
+    if (!h) return SARAS_BAD_ARG;
+    return copy_fields(h->c, n, fields, reinterpret_cast<const void *const *>(hosts), true);
+}
+
+int saras_download_fields(saras_ctx *h, int n, const int *fields, double *const *hosts) {
+    if (!h) return SARAS_BAD_ARG;
+    return copy_fields(h->c, n, fields, reinterpret_cast<const void *const *>(hosts), false);
 }
 
 int saras_synchronize(saras_ctx *h) {

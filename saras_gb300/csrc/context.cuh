@@ -79,6 +79,8 @@ struct Ctx {
     saras_params p;
     int dev = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t copyStream[SARAS_NUM_FIELDS] = {};   // saras_upload_fields / saras_download_fields
+    cudaEvent_t copyEvent[SARAS_NUM_FIELDS + 1] = {};
     bool scalar = false;
     // grid (grid.cc:59-136, uniform)
     int Ns[3], Nc[3];

@@ -317,3 +317,23 @@ def test_solvepde_ldc_runs_and_stays_bounded():
     assert len(series) == 4
     assert all(0.0 < e < 1.0 for _, e, _, _ in series)
     assert all(abs(d) < 1.0 for _, _, d, _ in series)
+
+
+def test_batched_field_transfers_match_single():
+    """saras_upload_fields / saras_download_fields move the same bytes as
+    per-field saras_upload / saras_download, from and into page-locked memory."""
+    torch = pytest.importorskip("torch")
+    p, g = target_case(F.MG_MIXED)
+    fields = [F.FIELD_VX, F.FIELD_VY, F.FIELD_VZ, F.FIELD_P]
+    assert g.time_advance()[0] == 0
+    host = [torch.empty(g.dims(f), dtype=torch.float64, pin_memory=True) for f in fields]
+    g.download_fields_ptr(fields, [t.data_ptr() for t in host])
+    for f, t in zip(fields, host):
+        assert np.array_equal(t.numpy(), g.get(f))
+    rng = np.random.default_rng(7)
+    new = [rng.standard_normal(g.dims(f)) for f in fields]
+    for t, a in zip(host, new):
+        t.numpy()[...] = a
+    g.upload_fields_ptr(fields, [t.data_ptr() for t in host])
+    for f, a in zip(fields, new):
+        assert np.array_equal(g.get(f), a)
