@@ -104,6 +104,17 @@ __device__ __forceinline__ fpair fp_mul(fpair a, fpair b) {
     return fp_norm(p, e);
 }
 
+// a b + c in one normalisation: the high product's exact FMA residual and the
+// TwoSum of the high parts, the cross terms and c's low part in float.
+__device__ __forceinline__ fpair fp_fma(fpair a, fpair b, fpair c) {
+    float p = a.h * b.h;
+    float e = fmaf(a.h, b.h, -p);
+    float s, t;
+    two_sum(p, c.h, s, t);
+    t += e + fmaf(a.h, b.l, fmaf(a.l, b.h, c.l));
+    return fp_norm(s, t);
+}
+
 __device__ __forceinline__ fpair fp_of(double x) {
     fpair r;
     dsplit(x, r.h, r.l);

@@ -404,7 +404,7 @@ __device__ __forceinline__ void rhs3_point(const Rhs3Args &a, const float2 (*sm)
     fpair ey = G(C, 0, 1, 0), wy = G(C, 0, -1, 0), ez = G(C, 0, 0, 1), wz = G(C, 0, 0, -1);
     fpair c2 = fpair{-2.0f * c.h, -2.0f * c.l};
     fpair Sx = fp_add(fp_add(ex, wx), c2), Sy = fp_add(fp_add(ey, wy), c2), Sz = fp_add(fp_add(ez, wz), c2);
-    fpair h = fp_add(fp_add(fp_mul(q.k2[0], Sx), fp_mul(q.k2[1], Sy)), fp_mul(q.k2[2], Sz));
+    fpair h = fp_fma(q.k2[0], Sx, fp_fma(q.k2[1], Sy, fp_mul(q.k2[2], Sz)));
     fpair s0, s1, s2, dp;
     if (C == 0) {
         s0 = c;
@@ -422,18 +422,18 @@ __device__ __forceinline__ void rhs3_point(const Rhs3Args &a, const float2 (*sm)
         s2 = c;
         dp = fp_add(G(3, 0, 0, 1), fp_neg(G(3, 0, 0, 0)));
     }
-    h = fp_add(h, fp_neg(fp_mul(s0, fp_mul(fp_add(ex, fp_neg(wx)), q.k1n[0]))));
-    h = fp_add(h, fp_neg(fp_mul(s1, fp_mul(fp_add(ey, fp_neg(wy)), q.k1n[1]))));
-    h = fp_add(h, fp_neg(fp_mul(s2, fp_mul(fp_add(ez, fp_neg(wz)), q.k1n[2]))));
+    h = fp_fma(fp_neg(s0), fp_mul(fp_add(ex, fp_neg(wx)), q.k1n[0]), h);
+    h = fp_fma(fp_neg(s1), fp_mul(fp_add(ey, fp_neg(wy)), q.k1n[1]), h);
+    h = fp_fma(fp_neg(s2), fp_mul(fp_add(ez, fp_neg(wz)), q.k1n[2]), h);
     if (C == 2 && a.buoyancy) {
         long ot = (long)(i + 1) * a.sx[3] + (long)(j + 1) * a.sy[3] + (k + 1);
         h = fp_add(h, fp_mul(q.fb2, fp_add(fp_of(a.T[ot]), fp_of(a.T[ot + 1]))));
     }
-    h = fp_add(h, fp_neg(fp_mul(q.g[C], dp)));
+    h = fp_fma(fp_neg(q.g[C]), dp, h);
     h = fp_mul(h, q.dt);
     a.H[C][o] = (a.f[C][o] + f2d(h.h)) + f2d(h.l);
     const CnDf &cf = a.cf[C];
-    fpair n0 = fp_add(h, fp_add(fp_add(fp_mul(cf.kc[0], Sx), fp_mul(cf.kc[1], Sy)), fp_mul(cf.kc[2], Sz)));
+    fpair n0 = fp_fma(cf.kc[0], Sx, fp_fma(cf.kc[1], Sy, fp_fma(cf.kc[2], Sz, h)));
     n0 = fp_mul(n0, cf.invDn);   // A = N0 / Dn: the Jacobi solve's first iterate from D = 0
     a.n0h[C][o] = n0.h;
     a.n0l[C][o] = n0.l;
