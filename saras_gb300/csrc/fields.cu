@@ -267,7 +267,7 @@ __global__ void __launch_bounds__(256) k_divergence_df(View3<double> D, Vel V, B
         fpair dx = fp_of(xc - xm);
         fpair dy = fp_of(V.v[1](i, j, k) - V.v[1](i, j - 1, k));
         fpair dz = fp_of(V.v[2](i, j, k) - V.v[2](i, j, k - 1));
-        fpair sum = fp_add(fp_add(fp_mul(q.k[0], dx), fp_mul(q.k[1], dy)), fp_mul(q.k[2], dz));
+        fpair sum = fp_fma(q.k[0], dx, fp_fma(q.k[1], dy, fp_mul(q.k[2], dz)));
         D(i, j, k) = f2d(sum.h) + f2d(sum.l);
         xm = xc;
     }
@@ -711,7 +711,7 @@ __device__ __forceinline__ float cn_lap1(fpair p, fpair m, fpair c) {
 __device__ __forceinline__ fpair cn_delta_update(const CnDelta &a, long o, fpair D, fpair xp, fpair xm, fpair yp, fpair ym, fpair zp,
                                                  fpair zm, fpair &corr) {
     float q = fmaf(a.f.kf[0], cn_lap1(xp, xm, D), fmaf(a.f.kf[1], cn_lap1(yp, ym, D), a.f.kf[2] * cn_lap1(zp, zm, D)));
-    corr = fp_add(fpair{a.n0h[o], a.n0l[o]}, fp_mul(fp_add(fpair{q, 0.0f}, fp_neg(D)), a.f.invDn));
+    corr = fp_fma(fp_add(fpair{q, 0.0f}, fp_neg(D)), a.f.invDn, fpair{a.n0h[o], a.n0l[o]});
     return fp_add(D, corr);
 }
 
