@@ -200,7 +200,8 @@ void vgraph_reset(Ctx &c);
 int prof_graph_replay(Ctx &c, cudaGraphExec_t ge, const std::vector<ProfNode> &nodes);
 int unet_pick(Ctx &c);
 bool unet_tracking(const Ctx &c);
-void unet_record(Ctx &c, int built, int cycles);
+int unet_shadow(Ctx &c, int built);
+void unet_note_start(Ctx &c, int built, double rel);
 int unet_collect_sample(Ctx &c, const double *b);
 int conv3d_check(int mode, int D, int H, int W, int cin, int cout, const unsigned short *x, const unsigned short *dy,
                  const float *w, const float *bias, int relu, float *out);

@@ -2245,7 +2245,7 @@ static int mixed_fixed(Ctx &c, const double *pp0, double mean, double bmax, doub
     // is computed too and the smaller one starts the solve
     bool started = false;
     double rg = 0;
-    int gs = SARAS_BAD_CONFIG;
+    int gs = SARAS_BAD_CONFIG, gq = 1;   // gq: the fixed-point iterate holding the guess
     if (wantGuess && c.histCount >= 2) {
         built = unet_pick(c);
         prof_begin(c, PK_GUESS, 0);
@@ -2254,10 +2254,33 @@ static int mixed_fixed(Ctx &c, const double *pp0, double mean, double bmax, doub
         if (gs == SARAS_OK) {
             if ((s = refine(1, false, rg, bad))) return s;
             if (bad) return fp64_start();
+            unet_note_start(c, built, rg / bmax);
+            // the learned mode's probes build the other guess too; the better starts
+            if (const int other = unet_shadow(c, built)) {
+                prof_begin(c, PK_GUESS, 0);
+                const int go = unet_guess(c, L0.r, nullptr, other, c.fx[0], sc, dflag);
+                prof_end(c, PK_GUESS, 0, 0.0);
+                if (go == SARAS_OK) {
+                    double ro = 0;
+                    if ((s = refine(0, false, ro, bad))) return s;
+                    if (bad) return fp64_start();
+                    unet_note_start(c, other, ro / bmax);
+                    if (ro < rg) {
+                        rg = ro;
+                        built = other;
+                        gq = 0;
+                    } else if ((s = refine(1, false, rg, bad))) {   // the first guess's FP32 residual back into r32
+                        return s;
+                    }
+                    if (bad) return fp64_start();
+                } else if (go != SARAS_BAD_CONFIG) {
+                    return go;
+                }
+            }
             if (rg <= kGuessTrusted * bmax) {
                 r = rg;
                 source = built;
-                cur = 1;
+                cur = gq;
                 started = true;
             }
         } else if (gs != SARAS_BAD_CONFIG) {
@@ -2265,16 +2288,18 @@ static int mixed_fixed(Ctx &c, const double *pp0, double mean, double bmax, doub
         }
     }
     if (!started) {
-        k_fx_init<<<gc, bcd, 0, c.stream>>>(c.fx[0], lcview<double>(L0, pp0), bc0, sc, dflag);
+        const int pq = gq ^ 1;   // the previous Pp into the other iterate
+        k_fx_init<<<gc, bcd, 0, c.stream>>>(c.fx[pq], lcview<double>(L0, pp0), bc0, sc, dflag);
         count_launch(c);
-        if ((s = refine(0, false, r, bad))) return s;
+        if ((s = refine(pq, false, r, bad))) return s;
         if (bad) return fp64_start();
+        cur = pq;
         if (gs == SARAS_OK && rg < r) {   // the guess after all: its FP32 residual back into r32
-            if ((s = refine(1, false, rg, bad))) return s;
+            if ((s = refine(gq, false, rg, bad))) return s;
             if (bad) return fp64_start();
             r = rg;
             source = built;
-            cur = 1;
+            cur = gq;
         }
     }
     if (st) { st->guess_residual = bmax > 0 ? r / bmax : r; st->guess_source = source; }
@@ -2306,7 +2331,6 @@ static int mixed_fixed(Ctx &c, const double *pp0, double mean, double bmax, doub
         }
         count_launch(c);
         c.ppInHist = false;
-        if (built) unet_record(c, built, cyc);
         done = true;
         return chk(c, "fixed-point output");
     }
@@ -2404,11 +2428,13 @@ static int mg_solve_target_run(Ctx &c, int *cycles, double *residual, saras_step
     if ((s = fine_res(false, &r))) return s;
     if (wantGuess && c.histCount >= 2) {
         built = unet_pick(c);
+        unet_shadow(c, built);   // one guess at a time on this path
         int gs = unet_guess(c, L0.r, L0.pb(), built);
         if (gs == SARAS_OK) {
             L0.cur ^= 1;
             double rg = 0;
             if ((s = fine_res(false, &rg))) return s;
+            unet_note_start(c, built, rg / bmax);
             if (rg < r) {
                 r = rg;
                 source = built;
@@ -2441,7 +2467,6 @@ static int mg_solve_target_run(Ctx &c, int *cycles, double *residual, saras_step
         }
     }
     }
-    if (!fixedDone && built) unet_record(c, built, cyc);
     if (st) { st->refine_steps = steps; st->fine_residual = bmax > 0 ? r / bmax : r; }
     if (!fixedDone) {   // the fixed-point path has written Pp already (k_fx_output)
         k_mg_output<<<grid_blocks(L0.count), 256, 0, c.stream>>>(lview<double>(L0, c.f[SARAS_FIELD_PP]), lcview<double>(L0, L0.pa()), bc0,

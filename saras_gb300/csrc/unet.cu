@@ -493,9 +493,10 @@ struct UNet {
     bool bPushed = false;                    // rb[0] holds this solve's b
     bool track = false;                      // this solve pushes rb / rp
     bool wantNet = false;                    // the network was picked before its rings were complete
+    bool shadow = false;                     // this solve builds both guesses
     // V-cycles per solve with the network's guess and with plain extrapolation
     // (moving averages), the basis of the choice between them
-    double cycNet = 0.0, cycExt = 0.0;
+    double lrNet = 0.0, lrExt = 0.0;         // log10 of the start's residual / max|b|
     int usesNet = 0, usesExt = 0, solves = 0;
     int probeEvery = 8, nextProbe = 0;       // probe schedule of the guess that is not preferred
     bool preferNet = false;
@@ -869,8 +870,8 @@ namespace saras {
 static bool rings_due(const Ctx &c, const UNet *u) {
     if (c.collecting) return true;
     if (c.guessMode != SARAS_GUESS_LEARNED || !u->trained) return false;
-    if (u->wantNet || u->usesNet < 2 || u->preferNet) return true;
-    return u->usesExt >= 2 && u->nextProbe > 0 && u->solves + 3 >= u->nextProbe;
+    if (u->wantNet || u->usesNet < 2 || u->usesExt < 2 || u->preferNet) return true;
+    return u->nextProbe > 0 && u->solves + 3 >= u->nextProbe;
 }
 
 // Whether this solve pushes R b (the FP64 b must then be stored).
@@ -918,30 +919,32 @@ int unet_begin_solve(Ctx &c) {
 }
 
 // SARAS_GUESS_LEARNED picks, per solve, between the network's guess and plain
-// extrapolation by the V-cycles each has needed (moving averages over its
-// recent solves).  Building the network's guess costs about half a level-0
-// V-cycle more than extrapolating (restrictions, features, forward pass), so
-// the network is preferred when its average is lower by more than that.  The
-// other guess is probed so that its average stays current: first after
+// extrapolation by the residual each leaves (moving averages of its log10
+// over recent solves: the V-cycles a solve needs follow it, about one a
+// decade).  Building the network's guess costs about half a level-0 V-cycle
+// more than extrapolating (restrictions, features, forward pass), so the
+// network is preferred when its average is lower by more than half a decade.
+// The other guess is probed so that its average stays current: first after
 // kProbe solves, then at doubling intervals up to kProbeMax while the
-// preference holds (back to kProbe when it changes).  A network that does not
-// beat extrapolation on the running problem is thus evaluated on a few solves
-// in a hundred, and one that does is used throughout.
+// preference holds (back to kProbe when it changes).  A probe, and each of the
+// first two uses of either guess, builds both guesses (unet_shadow) and the
+// better one starts the solve, so probing a worse guess costs its building
+// and one residual pass, not V-cycles.
 constexpr int kProbe = 8, kProbeMax = 64;
-constexpr double kNetCostCycles = 0.5;
+constexpr double kNetCostDecades = 0.5;
 
 int unet_pick(Ctx &c) {
     if (c.guessMode != SARAS_GUESS_LEARNED) return c.guessMode;
     UNet *u = U(c);
     if (!u || !u->trained) return SARAS_GUESS_EXTRAPOLATE;
     u->solves += 1;
+    u->shadow = false;
     bool net, probe = false;
-    if (u->usesNet < 2) {
-        net = true;
-    } else if (u->usesExt < 2) {
-        net = false;
+    if (u->usesNet < 2 || u->usesExt < 2) {
+        net = u->usesNet < 2;
+        u->shadow = true;
     } else {
-        bool netBetter = u->cycNet + kNetCostCycles < u->cycExt;
+        bool netBetter = u->lrNet + kNetCostDecades < u->lrExt;
         if (u->nextProbe == 0) u->nextProbe = u->solves + kProbe;   // the first comparison starts the schedule
         if (netBetter != u->preferNet) {
             u->preferNet = netBetter;
@@ -949,11 +952,14 @@ int unet_pick(Ctx &c) {
             u->nextProbe = u->solves + kProbe;
         }
         probe = u->solves >= u->nextProbe;
-        net = probe ? !netBetter : netBetter;
+        net = netBetter;
+        u->shadow = probe;
     }
     // the rings are complete once this solve pushes its R b
-    if (net && !(u->track && u->nb >= 2 && u->np >= 2)) {
+    const bool ready = u->track && u->nb >= 2 && u->np >= 2;
+    if ((net || u->shadow) && !ready) {
         u->wantNet = true;   // they run from the next solve on; the pick (a probe too) waits for them
+        u->shadow = false;
         return SARAS_GUESS_EXTRAPOLATE;
     }
     u->wantNet = false;
@@ -964,15 +970,24 @@ int unet_pick(Ctx &c) {
     return net ? SARAS_GUESS_LEARNED : SARAS_GUESS_EXTRAPOLATE;
 }
 
-void unet_record(Ctx &c, int built, int cycles) {
+// The guess this solve also builds beside `built` (0: none).
+int unet_shadow(Ctx &c, int built) {
     UNet *u = U(c);
-    if (!u || c.guessMode != SARAS_GUESS_LEARNED) return;
-    const double w = 0.3;
+    if (!u || c.guessMode != SARAS_GUESS_LEARNED || !u->shadow) return 0;
+    u->shadow = false;
+    return built == SARAS_GUESS_LEARNED ? SARAS_GUESS_EXTRAPOLATE : SARAS_GUESS_LEARNED;
+}
+
+// The residual (relative to max|b|) that guess `built` left at the start of a solve.
+void unet_note_start(Ctx &c, int built, double rel) {
+    UNet *u = U(c);
+    if (!u || c.guessMode != SARAS_GUESS_LEARNED || !(rel > 0.0) || !std::isfinite(rel)) return;
+    const double w = 0.3, lr = std::log10(rel);
     if (built == SARAS_GUESS_LEARNED) {
-        u->cycNet = u->usesNet ? (1.0 - w) * u->cycNet + w * cycles : cycles;
+        u->lrNet = u->usesNet ? (1.0 - w) * u->lrNet + w * lr : lr;
         u->usesNet += 1;
     } else if (built == SARAS_GUESS_EXTRAPOLATE) {
-        u->cycExt = u->usesExt ? (1.0 - w) * u->cycExt + w * cycles : cycles;
+        u->lrExt = u->usesExt ? (1.0 - w) * u->lrExt + w * lr : lr;
         u->usesExt += 1;
     }
 }
