@@ -2213,7 +2213,7 @@ static int mixed_fixed(Ctx &c, const double *pp0, double mean, double bmax, doub
     // refinement update writes its FP64 iterate into Pp's core as it goes.
     double *outp = c.ppInHist ? c.f[SARAS_FIELD_PP] : nullptr;
     // residual of fixed iterate q (with e: advanced into q ^ 1 first); returns the max in value units
-    auto refine = [&](int q, bool withE, double &out, bool &bad) -> int {
+    auto refine = [&](int q, bool withE, double &out, bool &bad, bool fill32 = true) -> int {
         SARAS_CUDA_TRY(cudaMemsetAsync(c.dscal + 34, 0, sizeof(double), c.stream));
         if (withE) {
             prof_begin(c, PK_REFINE_UPDATE, 0);
@@ -2222,8 +2222,8 @@ static int mixed_fixed(Ctx &c, const double *pp0, double mean, double bmax, doub
             prof_end(c, PK_REFINE_UPDATE, 0, (8.0 + 4.0 + 8.0 + 8.0 + 4.0 + (outp ? 8.0 : 0.0)) * (double)L0.count);
         } else {
             prof_begin(c, PK_REFINE_RESID, 0);
-            k_fx_refine<<<gk0, bk0, 0, c.stream>>>(c.fx[q], B, L0.r32, sx0, sy0, bc0, (float)rs, dmax);
-            prof_end(c, PK_REFINE_RESID, 0, (8.0 + 8.0 + 4.0) * (double)L0.count);
+            k_fx_refine<<<gk0, bk0, 0, c.stream>>>(c.fx[q], B, fill32 ? L0.r32 : nullptr, sx0, sy0, bc0, (float)rs, dmax);
+            prof_end(c, PK_REFINE_RESID, 0, (8.0 + 8.0 + (fill32 ? 4.0 : 0.0)) * (double)L0.count);
         }
         count_launch(c);
         int e = chk(c, "fixed-point refinement");
@@ -2262,17 +2262,16 @@ static int mixed_fixed(Ctx &c, const double *pp0, double mean, double bmax, doub
                 prof_end(c, PK_GUESS, 0, 0.0);
                 if (go == SARAS_OK) {
                     double ro = 0;
-                    if ((s = refine(0, false, ro, bad))) return s;
+                    if ((s = refine(0, false, ro, bad, false))) return s;   // its max only; r32 keeps the first guess's
                     if (bad) return fp64_start();
                     unet_note_start(c, other, ro / bmax);
                     if (ro < rg) {
+                        if ((s = refine(0, false, ro, bad))) return s;      // its FP32 residual into r32
+                        if (bad) return fp64_start();
                         rg = ro;
                         built = other;
                         gq = 0;
-                    } else if ((s = refine(1, false, rg, bad))) {   // the first guess's FP32 residual back into r32
-                        return s;
                     }
-                    if (bad) return fp64_start();
                 } else if (go != SARAS_BAD_CONFIG) {
                     return go;
                 }
