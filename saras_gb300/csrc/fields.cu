@@ -523,6 +523,31 @@ __global__ void k_bc_apply(View3<double> out, View3<const double> in, BcProgram 
     out(i, j, k) = bc_resolve(prog, i, j, k, [&](int a, int b, int c) -> double { return in(a, b, c); });
 }
 
+// k_bc_apply in place (copy_bulk = 0) over the non-bulk points only, as six
+// disjoint slabs (blockIdx.y: along axis d = slab / 2 the points below / above
+// the bulk range, the axes before d restricted to the bulk range, the axes
+// after d full): the bulk points, which the in-place form leaves alone, cost no
+// threads.
+__global__ void k_bc_apply_shell(View3<double> out, View3<const double> in, BcProgram prog, Box full) {
+    const int s = blockIdx.y, d = s >> 1;
+    int lo[3], hi[3];
+    for (int e = 0; e < 3; ++e) {
+        if (e < d) { lo[e] = prog.blo[e]; hi[e] = prog.bhi[e]; }
+        else { lo[e] = full.lo[e]; hi[e] = full.lo[e] + full.ext[e] - 1; }
+    }
+    if (s & 1) lo[d] = prog.bhi[d] + 1;
+    else hi[d] = prog.blo[d] - 1;
+    if (lo[0] > hi[0] || lo[1] > hi[1] || lo[2] > hi[2]) return;
+    const int n1 = hi[1] - lo[1] + 1, n2 = hi[2] - lo[2] + 1, n = (hi[0] - lo[0] + 1) * n1 * n2;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int r = t / n2, k = lo[2] + (t - r * n2), q = r / n1, j = lo[1] + (r - q * n1), i = lo[0] + q;
+        bool targeted = false;
+        for (int o = 0; o < prog.nops; ++o) if (in_box(prog.op[o].lo, prog.op[o].hi, i, j, k)) { targeted = true; break; }
+        if (!targeted) continue;
+        out(i, j, k) = bc_resolve(prog, i, j, k, [&](int a, int b, int c) -> double { return in(a, b, c); });
+    }
+}
+
 // ------------------------------------------------------------------ Crank-Nicolson Jacobi
 // hydro_d3::solveVx (hydro_d3.cc:374-422) fused: one launch computes the
 // residual of the incoming iterate V_in over the bulk (lines 393-407) and the
@@ -1196,8 +1221,9 @@ static int apply_program(Ctx &c, int field, const BcProgram &prog) {
         std::swap(c.f[field], c.scratch[slot]);
     } else {
         // Programs of fields without a scratch partner only copy from core
-        // points that no op targets (syncData), so they run in place.
-        k_bc_apply<<<g, b, 0, c.stream>>>(mview(c, field), cview(c, field), prog, fb, 0);
+        // points that no op targets (syncData), so they run in place, on the
+        // non-bulk points alone.
+        k_bc_apply_shell<<<dim3(64, 6), 256, 0, c.stream>>>(mview(c, field), cview(c, field), prog, fb);
         count_launch(c);
     }
     return check_launch(c, "k_bc_apply");
