@@ -332,13 +332,13 @@ __global__ void k_loss(const float *d, const float *dstar, bf16 *gout, long nv, 
 template <typename OT>
 __global__ void k_apply_guess(OT *out, L0View p1, L0View p2, L0View p3, int kind, const float *d, Grid3 g, int lb,
                               const double *scales, const double *alpha, int per0, int per1, int per2, int s, int *flag) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    int j = blockIdx.y * blockDim.y + threadIdx.y;
-    int i = blockIdx.z;
-    if (i > p1.n[0] || j > p1.n[1] || k > p1.n[2]) return;
+    // one thread per point of plane blockIdx.z, numbered k fastest over the
+    // whole (j, k) plane (rows of 2^m + 1 points leave no idle warps)
+    const int W = p1.n[2] + 1, t = blockIdx.x * blockDim.x + threadIdx.x, j = t / W, k = t - j * W, i = blockIdx.z;
+    if (j > p1.n[1]) return;
     double v = kind == 1 ? 3.0 * (p1.at(i, j, k) - p2.at(i, j, k)) + p3.at(i, j, k)
              : kind == 2 ? (p1.at(i, j, k) + p2.at(i, j, k)) - p3.at(i, j, k)
-                         : 2.0 * p1.at(i, j, k) - p2.at(i, j, k);
+                         : fma(2.0, p1.at(i, j, k), -p2.at(i, j, k));   // 2 P1 is exact: one rounding, as before
     if (d) {
         int m = (1 << lb) - 1;
         float inv = 1.0f / (float)(1 << lb);
@@ -1023,7 +1023,7 @@ int unet_guess(Ctx &c, const double *b, double *dst, int mode, long long *fxdst,
         count_launch(c, 4);
     }
     const Level &L0 = c.lv[0];
-    dim3 b2(64, 4), g2((L0.n[2] + 1 + 63) / 64, (L0.n[1] + 1 + 3) / 4, L0.n[0] + 1);
+    dim3 b2(256), g2((unsigned)(((long)(L0.n[1] + 1) * (L0.n[2] + 1) + 255) / 256), 1, L0.n[0] + 1);
     const float *d = use_net ? u->out : nullptr;
     Grid3 gd = use_net ? u->g[0] : Grid3{1, 1, 1};
     int lb = use_net ? u->lb : 0;
