@@ -1,8 +1,9 @@
 """Solver configurations and initial states shared by the parity tests.
 
-Each case mirrors a BASELINE workload at a size the CPU oracle finishes in
-seconds (the same code paths as the full-size runs: same boundary types,
-multigrid depth pattern and tolerances).
+Each case mirrors one of the reference's benchmark workloads (Taylor-Green
+vortex, lid-driven cavity, Rayleigh-Benard convection) at a size the CPU
+oracle finishes in seconds (the same code paths as the full-size runs: same
+boundary types, multigrid depth pattern and tolerances).
 """
 import math
 
