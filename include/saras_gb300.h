@@ -206,9 +206,13 @@ int saras_cn_solve(saras_ctx *ctx, int component, int *iters, double *max_error)
  * component; the second Jacobi iterate and the residual slot live in a fixed
  * 32 MiB device array reserved by the library on every GPU that loads it, so
  * padded fields above 4 Mi points (e.g. beyond 161^3) return SARAS_TOO_LARGE.
- * The first call on a device resolves that array's address: make it before
- * any stream capture.  Calls that overlap on the GPU share the array and race.
- * stream may be NULL (legacy default stream). */
+ * fastKernels 0 and 1 run the same iteration as saras_cn_solve; fastKernels 2
+ * runs the fastKernels 1 iteration (saras_cn_solve's split-FP64 form needs
+ * more scratch than the fixed array holds): the same system and stopping
+ * rule with different rounding, so results agree to about the tolerance and
+ * counts may differ by one.  The first call on a device resolves that array's
+ * address: make it before any stream capture.  Calls that overlap on the GPU
+ * share the array and race.  stream may be NULL (legacy default stream). */
 int saras_cn_solve_noalloc(const saras_params *p, int component, double *v, const double *rhs, void *stream,
                            int *iters, double *max_error);
 /* poisson::mgSolve(Pp, mgRHS) (poisson.cc:100-205). */

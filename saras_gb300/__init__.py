@@ -333,23 +333,85 @@ def grid_coords(params):
     return out
 
 
+_TRIG_CACHE = {}
+
+
+def _sin_pi(q, m):
+    """sin(pi q / m) for integer arrays q, correctly rounded to FP64.
+
+    Evaluated in 50-digit decimal arithmetic (Machin's formula for pi, the
+    Taylor series of sin on the reduced argument), so the initial fields are
+    the same bits on every host: a library sin/cos may differ by an ulp
+    between machines, and a one-ulp difference in an initial field can move a
+    tolerance-stopped iteration count by one step in a long parity run."""
+    import decimal
+    key = int(m)
+    if key not in _TRIG_CACHE:
+        ctx = decimal.Context(prec=50)
+        D = ctx.create_decimal
+
+        def arctan_inv(x):     # arctan(1/x) for an integer x
+            x = D(x)
+            x2 = ctx.multiply(x, x)
+            term = ctx.divide(D(1), x)
+            total, n, sign = term, 1, 1
+            while True:
+                term = ctx.divide(term, x2)
+                n += 2
+                sign = -sign
+                t = ctx.divide(term, D(n))
+                if t.adjusted() < -60:
+                    break
+                total = ctx.add(total, t) if sign > 0 else ctx.subtract(total, t)
+            return total
+        pi = ctx.multiply(D(4), ctx.subtract(ctx.multiply(D(4), arctan_inv(5)), arctan_inv(239)))
+        table = np.empty(2 * key, dtype=np.float64)
+        for r in range(2 * key):
+            rr = r if r <= key else r - 2 * key          # argument in [-pi, pi]
+            if rr % key == 0:                            # sin(0) = sin(pi) = 0 exactly
+                table[r] = 0.0
+                continue
+            x = ctx.divide(ctx.multiply(pi, D(rr)), D(key))
+            x2 = ctx.multiply(x, x)
+            term, total, n = x, x, 1
+            while True:
+                term = ctx.divide(ctx.multiply(term, x2), D((n + 1) * (n + 2)))
+                n += 2
+                if term.is_zero() or term.adjusted() < -60:
+                    break
+                total = ctx.subtract(total, term) if (n // 2) % 2 == 1 else ctx.add(total, term)
+            table[r] = float(total)
+        _TRIG_CACHE[key] = table
+    t = _TRIG_CACHE[key]
+    return t[np.mod(np.asarray(q, dtype=np.int64), 2 * key)]
+
+
+def _cos_pi(q, m):
+    """cos(pi q / m) = sin(pi (q + m/2) / m), correctly rounded (q, m integers)."""
+    return _sin_pi(2 * np.asarray(q, dtype=np.int64) + m, 2 * m)
+
+
 def taylor_green_velocity(params):
-    """taylorGreen::initializeField (lib/initial/taylorGreen.cc:54-100) over the padded arrays."""
-    (xs, xc), (ys, yc), (zs, zc) = grid_coords(params)
-    tp = 2.0 * math.pi
-    Vx = (np.sin(tp * xc / params.Lx)[:, None, None] * np.cos(tp * ys / params.Ly)[None, :, None] *
-          np.cos(tp * zs / params.Lz)[None, None, :])
-    Vy = (-np.cos(tp * xs / params.Lx)[:, None, None] * np.sin(tp * yc / params.Ly)[None, :, None] *
-          np.cos(tp * zs / params.Lz)[None, None, :])
+    """taylorGreen::initializeField (lib/initial/taylorGreen.cc:54-100) over the padded arrays:
+    u = sin(2 pi x / L) cos(2 pi y / L) cos(2 pi z / L), v = -cos sin cos.  Vertex
+    coordinates are x_i = L i / n and face coordinates L (i + 1/2) / n (i from -1),
+    so every factor is sin or cos of pi q / n for an integer q (correctly rounded)."""
+    n = [2 ** params.xInd, 2 ** params.yInd, 2 ** params.zInd]
+    vs = [2 * np.arange(-1, m + 2, dtype=np.int64) for m in n]        # 2 pi x_i / L = pi (2 i) / n
+    fc = [2 * np.arange(-1, m + 1, dtype=np.int64) + 1 for m in n]    # 2 pi x_(i+1/2) / L = pi (2 i + 1) / n
+    Vx = (_sin_pi(fc[0], n[0])[:, None, None] * _cos_pi(vs[1], n[1])[None, :, None] *
+          _cos_pi(vs[2], n[2])[None, None, :])
+    Vy = (-_cos_pi(vs[0], n[0])[:, None, None] * _sin_pi(fc[1], n[1])[None, :, None] *
+          _cos_pi(vs[2], n[2])[None, None, :])
     return Vx, Vy
 
 
 def taylor_green_pressure(params):
-    """p = (cos 2x + cos 2y)(cos 2z + 2)/16 on the vertex grid (x scaled by 2 pi / L)."""
-    (xs, _), (ys, _), (zs, _) = grid_coords(params)
-    tp = 2.0 * math.pi
-    return ((np.cos(2 * tp * xs / params.Lx)[:, None, None] + np.cos(2 * tp * ys / params.Ly)[None, :, None]) *
-            (np.cos(2 * tp * zs / params.Lz)[None, None, :] + 2.0) / 16.0)
+    """p = (cos 2x + cos 2y)(cos 2z + 2)/16 on the vertex grid (x scaled by 2 pi / L),
+    with correctly rounded cosines of pi (4 i) / n."""
+    n = [2 ** params.xInd, 2 ** params.yInd, 2 ** params.zInd]
+    c = [_cos_pi(4 * np.arange(-1, m + 2, dtype=np.int64), m) for m in n]
+    return ((c[0][:, None, None] + c[1][None, :, None]) * (c[2][None, None, :] + 2.0) / 16.0)
 
 
 def splitmix64(x):

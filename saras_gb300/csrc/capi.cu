@@ -280,7 +280,7 @@ static int validate(const saras_params *p, std::string &why) {
     if ((1 << p->xInd) < coarsest || (1 << p->yInd) < coarsest || (1 << p->zInd) < coarsest) { why = "grid too coarse for the V-Cycle depth"; return SARAS_BAD_CONFIG; }
     if (p->xGrid || p->yGrid || p->zGrid) { why = "only uniform meshes (Mesh Type UUU) are supported"; return SARAS_BAD_CONFIG; }
     if (p->dScheme != 1) { why = "Undefined finite differencing scheme"; return SARAS_BAD_CONFIG; }
-    if (p->gsSmooth != 0) { why = "Gauss-Seidel smoothing on fine levels is not available on the GPU; use Smoothing Method 0"; return SARAS_BAD_CONFIG; }
+    if (p->gsSmooth < 0 || p->gsSmooth > 1) { why = "Smoothing Method must be 0 (Jacobi) or 1 (Gauss-Seidel)"; return SARAS_BAD_CONFIG; }
     if (p->nonHgBC) { why = "heating-plate boundary condition is not supported"; return SARAS_BAD_CONFIG; }
     if (p->probType >= 5 && (p->rbcType < 1 || p->rbcType > 4)) { why = "undefined RBC Type"; return SARAS_BAD_CONFIG; }
     if (p->tStp <= 0 || p->Re <= 0 || p->Lx <= 0 || p->Ly <= 0 || p->Lz <= 0) { why = "non-positive time step, Re or length"; return SARAS_BAD_CONFIG; }
@@ -400,21 +400,40 @@ int saras_download(saras_ctx *h, int field, double *host) {
 
 // Field copies on one stream each: every copy stream waits for the context
 // stream's work so far, and (upload) the context stream waits for every copy.
+// A field may appear once per call (two concurrent copies into one device
+// buffer would race).  If issuing fails part way, the copies already issued
+// are waited for before returning, so no copy still reads or writes the
+// caller's host buffers when the error comes back.
 static int copy_fields(Ctx &c, int n, const int *fields, const void *const *hosts, bool up) {
     if (n < 0 || n > SARAS_NUM_FIELDS || (n > 0 && (!fields || !hosts))) return SARAS_BAD_ARG;
-    for (int q = 0; q < n; ++q)
+    bool seen[SARAS_NUM_FIELDS] = {};
+    for (int q = 0; q < n; ++q) {
         if (fields[q] < 0 || fields[q] >= SARAS_NUM_FIELDS || !hosts[q]) return SARAS_BAD_ARG;
+        if (seen[fields[q]]) { c.err = "a field appears twice in one copy call"; set_error(c.err); return SARAS_BAD_ARG; }
+        seen[fields[q]] = true;
+    }
     for (int q = 0; q <= n; ++q)
         if (!c.copyEvent[q]) SARAS_CUDA_TRY(cudaEventCreateWithFlags(&c.copyEvent[q], cudaEventDisableTiming));
-    SARAS_CUDA_TRY(cudaEventRecord(c.copyEvent[n], c.stream));
-    for (int q = 0; q < n; ++q) {
+    for (int q = 0; q < n; ++q)
         if (!c.copyStream[q]) SARAS_CUDA_TRY(cudaStreamCreateWithFlags(&c.copyStream[q], cudaStreamNonBlocking));
+    SARAS_CUDA_TRY(cudaEventRecord(c.copyEvent[n], c.stream));
+    int issued = 0;
+    cudaError_t e = cudaSuccess;
+    for (int q = 0; q < n && e == cudaSuccess; ++q) {
         cudaStream_t st = c.copyStream[q];
-        SARAS_CUDA_TRY(cudaStreamWaitEvent(st, c.copyEvent[n], 0));
         size_t bytes = sizeof(double) * field_count(c, fields[q]);
-        if (up) SARAS_CUDA_TRY(cudaMemcpyAsync(c.f[fields[q]], hosts[q], bytes, cudaMemcpyHostToDevice, st));
-        else SARAS_CUDA_TRY(cudaMemcpyAsync(const_cast<void *>(hosts[q]), c.f[fields[q]], bytes, cudaMemcpyDeviceToHost, st));
-        SARAS_CUDA_TRY(cudaEventRecord(c.copyEvent[q], st));
+        e = cudaStreamWaitEvent(st, c.copyEvent[n], 0);
+        if (e == cudaSuccess) {
+            issued = q + 1;
+            e = up ? cudaMemcpyAsync(c.f[fields[q]], hosts[q], bytes, cudaMemcpyHostToDevice, st)
+                   : cudaMemcpyAsync(const_cast<void *>(hosts[q]), c.f[fields[q]], bytes, cudaMemcpyDeviceToHost, st);
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(c.copyEvent[q], st);
+    }
+    if (e != cudaSuccess) {
+        for (int q = 0; q < issued; ++q) cudaStreamSynchronize(c.copyStream[q]);
+        set_error(std::string("field copy: ") + cudaGetErrorString(e));
+        return SARAS_CUDA_ERROR;
     }
     for (int q = 0; q < n; ++q) {
         SARAS_CUDA_TRY(cudaStreamWaitEvent(c.stream, c.copyEvent[q], 0));

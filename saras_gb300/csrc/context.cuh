@@ -101,6 +101,7 @@ struct Ctx {
     double mgTarget = 1e-8;
     int mgMaxCycles = 200;
     int maxCount = 0;
+    int numSMs = 1;           // multiprocessors of the context's device
     double *wallX = nullptr, *wallY = nullptr, *wallZ = nullptr;   // Dirichlet check walls
     // reductions
     double *red = nullptr;          // partial sums (device)

@@ -12,6 +12,7 @@
 // spacings dXi = 2^-n and by hx*hx are exact power-of-two scalings and are
 // applied as multiplications by the exact reciprocals.
 
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <algorithm>
@@ -1907,7 +1908,10 @@ namespace saras {
 
 constexpr long kNoAllocMaxPoints = 4L << 20;   // 4 Mi doubles (32 MiB): padded field arrays up to this size
 static __device__ __align__(256) double g_cn_scratch[kNoAllocMaxPoints + 32];
-static double *g_cn_scratch_dev[64] = {nullptr};   // device address of g_cn_scratch, per device ordinal
+// Device address of g_cn_scratch, per device ordinal.  Atomic: two host
+// threads making their first call on a device at the same time both look the
+// address up and store the same value, without a data race on the slot.
+static std::atomic<double *> g_cn_scratch_dev[64];
 
 // The wall objects of walls_for(), written into a fixed array (no host heap use).
 static int walls_fixed(const saras_params &p, int field, Wall *w) {
@@ -1945,9 +1949,11 @@ static int walls_fixed(const saras_params &p, int field, Wall *w) {
 }  // namespace saras
 
 // The same Jacobi iteration as saras_cn_solve (same kernels, same stopping
-// rule and iteration cap), on caller-owned device arrays v (in: current
-// iterate with its boundary values, out: solution) and rhs.  Nothing is
-// allocated.  The first call on a device looks up the device address of the
+// rule and iteration cap) for fastKernels 0 and 1, on caller-owned device
+// arrays v (in: current iterate with its boundary values, out: solution) and
+// rhs; with fastKernels = 2 it runs the fastKernels = 1 iteration (the same
+// system and stopping rule in FP64 fused multiply-adds, where saras_cn_solve
+// runs the split-FP64 delta form).  Nothing is allocated.  The first call on a device looks up the device address of the
 // scratch array; make that first call before any stream capture.  Every call
 // shares the one array, so calls that overlap on the GPU (other streams,
 // other host threads) race: order them on one stream or serialise them.
@@ -1962,16 +1968,15 @@ extern "C" int saras_cn_solve_noalloc(const saras_params *p, int component, doub
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); set_error("no CUDA device"); return SARAS_NO_DEVICE; }
     if (dev < 0 || dev >= 64) { set_error("device ordinal beyond 63"); return SARAS_BAD_ARG; }
-    if (!g_cn_scratch_dev[dev]) {
-        double *ptr = nullptr;
-        cudaError_t e = cudaGetSymbolAddress((void **)&ptr, g_cn_scratch);
-        if (e != cudaSuccess || !ptr) {
+    double *scratch = g_cn_scratch_dev[dev].load(std::memory_order_acquire);
+    if (!scratch) {
+        cudaError_t e = cudaGetSymbolAddress((void **)&scratch, g_cn_scratch);
+        if (e != cudaSuccess || !scratch) {
             set_error(std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
             return SARAS_CUDA_ERROR;
         }
-        g_cn_scratch_dev[dev] = ptr;
+        g_cn_scratch_dev[dev].store(scratch, std::memory_order_release);
     }
-    double *scratch = g_cn_scratch_dev[dev];
     double *resSlot = scratch + kNoAllocMaxPoints;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
 
@@ -2071,7 +2076,10 @@ extern "C" int saras_cn_solve_noalloc(const saras_params *p, int component, doub
         cin.p = in.p; cin.n[0] = in.n[0]; cin.n[1] = in.n[1]; cin.n[2] = in.n[2]; cin.sx = in.sx; cin.sy = in.sy;
         if (fast) {
             fa.in = cin; fa.out = out; fa.withResidual = withRes;
-            k_cn_fast<<<g, bl, 0, st>>>(fa);   // both fast forms: the split-FP64 one needs more scratch
+            // fastKernels 1 and 2 both run this fused multiply-add form: the
+            // split-FP64 form of fastKernels = 2 keeps N0 and the correction
+            // as float pairs, 12 more floats a point than the fixed array holds
+            k_cn_fast<<<g, bl, 0, st>>>(fa);
         } else {
             a.in = cin; a.out = out; a.withResidual = withRes;
             k_cn<<<g, bl, 0, st>>>(a);

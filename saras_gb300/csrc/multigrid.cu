@@ -494,6 +494,143 @@ __global__ void k_mg_coarse(View3<T> pg, View3<const T> rg, MgK kk, MgBC bc, T t
     for (int t = threadIdx.x; t < n; t += blockDim.x) pg.p[t] = p[t];
 }
 
+// ------------------------------------------------------------------ Gauss-Seidel smoothing
+// gsSmooth = 1 (poisson_d3.cc:137-150): every level is smoothed in place in
+// lexicographic order, so each point sees the updated values of its (i-1),
+// (j-1), (k-1) neighbours and the old values of its (i+1), (j+1), (k+1)
+// neighbours.  The points of one hyperplane i + j + k = s depend only on
+// plane s - 1 (updated) and plane s + 1 (old): updating the planes in
+// increasing s, each plane in parallel, performs the same arithmetic on the
+// same operands as the lexicographic loop, bit for bit, in X + Y + Z + 1
+// dependent stages.  imposeBC runs before every sweep and once after
+// (poisson_d3.cc:124, 181); the ghosts a sweep reads are those of the state
+// before it, which the stages never write.
+
+// Levels whose iterate and right-hand side fit in shared memory (at most
+// kGsBlockSmem bytes together): one CTA, the stages separated by
+// __syncthreads.  zero: pressureData = 0 on entry.
+constexpr size_t kGsBlockSmem = 200 * 1024;
+__global__ void k_mg_gs_block(View3<double> pg, View3<const double> rg, MgK kk, MgBC bc, int count, int zero,
+                              const double *wx, const double *wy, const double *wz) {
+    extern __shared__ unsigned char smraw[];
+    const int X = bc.E[0], Y = bc.E[1], Z = bc.E[2];
+    const int n = (X + 3) * (Y + 3) * (Z + 3), sy = Z + 3, sx = (Y + 3) * (Z + 3);
+    double *p = reinterpret_cast<double *>(smraw);
+    double *r = p + n;
+    auto at = [&](double *a, int i, int j, int k) -> double & { return a[(i + 1) * sx + (j + 1) * sy + (k + 1)]; };
+    for (int t = threadIdx.x; t < n; t += blockDim.x) { p[t] = zero ? 0.0 : pg.p[t]; r[t] = rg.p[t]; }
+    __syncthreads();
+    for (int it = 0; it < count; ++it) {
+        smem_impose_bc(p, X, Y, Z, bc, wx, wy, wz);
+        for (int s = 0; s <= X + Y + Z; ++s) {
+            for (int t = threadIdx.x; t < (X + 1) * (Y + 1); t += blockDim.x) {
+                int i = t / (Y + 1), j = t % (Y + 1), k = s - i - j;
+                if (k < 0 || k > Z) continue;
+                at(p, i, j, k) = mg_update<double>(at(p, i + 1, j, k), at(p, i - 1, j, k), at(p, i, j + 1, k), at(p, i, j - 1, k),
+                                                   at(p, i, j, k + 1), at(p, i, j, k - 1), at(r, i, j, k), kk);
+            }
+            __syncthreads();
+        }
+    }
+    smem_impose_bc(p, X, Y, Z, bc, wx, wy, wz);
+    for (int t = threadIdx.x; t < n; t += blockDim.x) pg.p[t] = p[t];
+}
+
+// Value that imposeBC (x planes, y planes, then z planes over full extents,
+// poisson_d3.cc:575-668 with updatePads first) leaves at the ghost point
+// (i, j, k), resolved from the core: the last writer first (z, then y, then
+// x); periodic and mirror copies map one coordinate to its image, Dirichlet
+// walls of the check case end the chain with their fixed value, and
+// homogeneous Dirichlet images change sign.
+__device__ __forceinline__ double mg_ghost_value(const View3<const double> &p, int i, int j, int k, const MgBC &bc,
+                                                 const double *wx, const double *wy, const double *wz) {
+    int q[3] = {i, j, k};
+    const int E1 = bc.E[1], E2 = bc.E[2];
+    double sign = 1.0;
+    for (int d = 2; d >= 0; --d) {
+        int E = bc.E[d];
+        if (q[d] >= 0 && q[d] <= E) continue;
+        if (bc.per[d]) { q[d] = q[d] < 0 ? E - 1 : 1; continue; }
+        if (bc.dirichlet && !bc.zeroBC) {
+            const double *w = d == 0 ? wx : d == 1 ? wy : wz;
+            int a = d == 0 ? q[1] : q[0], b = d == 2 ? q[1] : q[2];
+            int nb = d == 2 ? (E1 + 3) : (E2 + 3);
+            return sign * w[(a + 1) * nb + (b + 1)];
+        }
+        if (bc.dirichlet) sign = -sign;
+        q[d] = q[d] < 0 ? 1 : E - 1;
+    }
+    return sign * __ldcg(&p(q[0], q[1], q[2]));
+}
+
+// Grid-wide barrier for the cooperative Gauss-Seidel kernel: block arrivals
+// are counted on *count (zeroed before the launch); the b-th barrier waits
+// for b * gridDim.x arrivals.  The wait is bounded: after kGsSpinLimit polls
+// (about a second) the block records the failure in *err and every block
+// leaves the kernel at its next barrier.
+constexpr long long kGsSpinLimit = 1ll << 24;
+__device__ __forceinline__ bool gs_grid_sync(unsigned *count, unsigned target, int *err) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(count, 1u);
+        long long spins = 0;
+        int good = 1;
+        while (*(volatile unsigned *)count < target) {
+            if (*(volatile int *)err) { good = 0; break; }
+            if (++spins > kGsSpinLimit) { atomicExch(err, 1); good = 0; break; }
+            __nanosleep(64);
+        }
+        __threadfence();
+        ok = good;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// Levels too large for one CTA's shared memory: a cooperative launch over
+// gridDim.x co-resident blocks, the stages separated by grid barriers.  The
+// iterate is read past L1 (ld.global.cg), so a block never sees a line that
+// another block has updated since.  `count` sweeps, each preceded by the
+// ghost fill, and a final ghost fill.
+__global__ void __launch_bounds__(256) k_mg_gs_grid(View3<double> p, View3<const double> r, MgK kk, MgBC bc, int count,
+                                                    unsigned *sync, int *err, const double *wx, const double *wy,
+                                                    const double *wz) {
+    const int X = bc.E[0], Y = bc.E[1], Z = bc.E[2];
+    const long tid = blockIdx.x * (long)blockDim.x + threadIdx.x, nt = (long)gridDim.x * blockDim.x;
+    const View3<const double> pc{p.p, {p.n[0], p.n[1], p.n[2]}, p.sx, p.sy};
+    // ghost points: two full x planes, two y planes (x core), two z planes (x, y core)
+    const long fx = (long)(Y + 3) * (Z + 3), fy = (long)(X + 1) * (Z + 3), fz = (long)(X + 1) * (Y + 1);
+    const long ng = 2 * (fx + fy + fz);
+    unsigned target = 0;
+    for (int it = 0;; ++it) {
+        for (long t = tid; t < ng; t += nt) {
+            int i, j, k;
+            long u = t;
+            if (u < 2 * fx) { i = u < fx ? -1 : X + 1; u %= fx; j = (int)(u / (Z + 3)) - 1; k = (int)(u % (Z + 3)) - 1; }
+            else if ((u -= 2 * fx) < 2 * fy) { j = u < fy ? -1 : Y + 1; u %= fy; i = (int)(u / (Z + 3)); k = (int)(u % (Z + 3)) - 1; }
+            else { u -= 2 * fy; k = u < fz ? -1 : Z + 1; u %= fz; i = (int)(u / (Y + 1)); j = (int)(u % (Y + 1)); }
+            p(i, j, k) = mg_ghost_value(pc, i, j, k, bc, wx, wy, wz);   // reads the core past L1
+        }
+        if (it == count) break;
+        target += gridDim.x;
+        if (!gs_grid_sync(sync, target, err)) return;
+        for (int s = 0; s <= X + Y + Z; ++s) {
+            const int ilo = max(0, s - Y - Z), ihi = min(X, s), jlo = max(0, s - X - Z), jhi = min(Y, s);
+            const long nj = jhi - jlo + 1, m = (long)(ihi - ilo + 1) * nj;
+            for (long t = tid; t < m; t += nt) {
+                const int i = ilo + (int)(t / nj), j = jlo + (int)(t % nj), k = s - i - j;
+                if (k < 0 || k > Z) continue;
+                p(i, j, k) = mg_update<double>(__ldcg(&p(i + 1, j, k)), __ldcg(&p(i - 1, j, k)), __ldcg(&p(i, j + 1, k)),
+                                               __ldcg(&p(i, j - 1, k)), __ldcg(&p(i, j, k + 1)), __ldcg(&p(i, j, k - 1)), r(i, j, k), kk);
+            }
+            target += gridDim.x;
+            if (!gs_grid_sync(sync, target, err)) return;
+        }
+    }
+}
+
 // ------------------------------------------------------------------ FP64 drivers
 // Load the level-0 right-hand side: residualData(0)(core) = rhs(core), then
 // updatePads (poisson.cc:114-118); per-block partial sums for the padded mean.
@@ -1638,6 +1775,9 @@ int mg_setup(Ctx &c) {
     if (smem > 220 * 1024) { c.err = "coarsest multigrid level too large for one CTA; increase V-Cycle Depth"; return SARAS_BAD_CONFIG; }
     SARAS_CUDA_TRY(cudaFuncSetAttribute(k_mg_coarse<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     SARAS_CUDA_TRY(cudaFuncSetAttribute(k_mg_coarse<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    SARAS_CUDA_TRY(cudaDeviceGetAttribute(&c.numSMs, cudaDevAttrMultiProcessorCount, c.dev));
+    SARAS_CUDA_TRY(cudaFuncSetAttribute(k_mg_gs_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGsBlockSmem));
+    SARAS_CUDA_TRY(cudaMemsetAsync(c.dflag, 0, 2 * sizeof(int), c.stream));
     c.tailLt = tail_level(c);
     if (c.tailLt > 0) {
         SARAS_CUDA_TRY(cudaFuncSetAttribute(k_mg_tail<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
@@ -1734,8 +1874,48 @@ static double smooth_weight(const Ctx &c, int n, int count) {
     return 1.0 / lam;
 }
 
+// Gauss-Seidel smoothing of level l (reference mode with gsSmooth = 1): one
+// CTA from shared memory for levels up to kGsBlockSmem of iterate plus
+// right-hand side, else the cooperative grid kernel with one block an SM at
+// most (a stage has at most (X+1)(Y+1) points).
+static int gs_smooth(Ctx &c, int l, int count, bool zero_first) {
+    Level &L = c.lv[l];
+    MgBC bc = level_bc(c, l, false);
+    MgK kk = make_k(L);
+    const bool walls = bc.dirichlet && !bc.zeroBC;
+    const double *wx = walls ? c.wallX : nullptr, *wy = walls ? c.wallY : nullptr, *wz = walls ? c.wallZ : nullptr;
+    View3<double> pv = lview<double>(L, L.pa());
+    View3<const double> rv = lcview<double>(L, L.r);
+    const size_t smem = 2 * sizeof(double) * (size_t)L.count;
+    if (smem <= kGsBlockSmem) {
+        k_mg_gs_block<<<1, 512, smem, c.stream>>>(pv, rv, kk, bc, count, zero_first ? 1 : 0, wx, wy, wz);
+        count_launch(c);
+        return chk(c, "mg Gauss-Seidel");
+    }
+    if (zero_first) SARAS_CUDA_TRY(cudaMemsetAsync(L.pa(), 0, sizeof(double) * (size_t)L.count, c.stream));
+    SARAS_CUDA_TRY(cudaMemsetAsync(c.dflag, 0, sizeof(int), c.stream));   // barrier arrivals
+    const long pairs = (long)(L.n[0] + 1) * (L.n[1] + 1);
+    int blocks = (int)std::max<long>(1, std::min<long>((pairs + 255) / 256, c.numSMs));
+    unsigned *sync = reinterpret_cast<unsigned *>(c.dflag);
+    int *err = c.dflag + 1;
+    void *args[] = {&pv, &rv, &kk, &bc, &count, &sync, &err, &wx, &wy, &wz};
+    SARAS_CUDA_TRY(cudaLaunchCooperativeKernel((const void *)k_mg_gs_grid, dim3(blocks), dim3(256), args, 0, c.stream));
+    count_launch(c);
+    return chk(c, "mg Gauss-Seidel");
+}
+
+// Status of the Gauss-Seidel grid barriers since the last reset (synchronises).
+static int gs_status(Ctx &c) {
+    int e = 0;
+    SARAS_CUDA_TRY(cudaMemcpyAsync(&e, c.dflag + 1, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    SARAS_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    if (e) { c.err = "Gauss-Seidel smoothing: a grid barrier wait timed out"; return SARAS_CUDA_ERROR; }
+    return SARAS_OK;
+}
+
 template <typename T>
 static int smooth(Ctx &c, int l, int count, bool zero_first, bool tgt) {
+    if (!tgt && c.p.gsSmooth && sizeof(T) == 8) return gs_smooth(c, l, count, zero_first);
     Level &L = c.lv[l];
     MgBC bc = level_bc(c, l, tgt);
     MgK kk = make_k(L);
@@ -2113,6 +2293,7 @@ static int mg_solve_reference(Ctx &c, int *cycles, double *residual) {
             prev = res;
         }
     }
+    if (c.p.gsSmooth && (s = gs_status(c))) return s;
     // inFn.F = pressureData(0) over the padded array (poisson.cc:151)
     k_mg_output<<<grid_blocks(L0.count), 256, 0, c.stream>>>(lview<double>(L0, c.f[SARAS_FIELD_PP]), lcview<double>(L0, L0.pa()), bc0,
                                                              c.wallX, c.wallY, c.wallZ);
@@ -2540,7 +2721,9 @@ int mg_get_level(Ctx &c, int level, int which, double *host) {
 int mg_smooth_level(Ctx &c, int level, int count) {
     if (level < 0 || level > c.depth) return SARAS_BAD_ARG;
     if (level == c.depth && count < 0) return coarse_solve<double>(c, false);
-    return smooth<double>(c, level, count, false, false);
+    int s = smooth<double>(c, level, count, false, false);
+    if (!s && c.p.gsSmooth) s = gs_status(c);
+    return s;
 }
 
 int mg_restrict_level(Ctx &c, int level) {

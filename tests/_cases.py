@@ -65,8 +65,16 @@ def rbc(ind=(4, 4, 3), depth=2, dt=5.0e-4):
     return p
 
 
+def base_kind(kind):
+    """The case family of an initial-state kind ("tgv_p1" is a Taylor-Green case)."""
+    return "tgv" if kind.startswith("tgv") else kind
+
+
 def initialise(solver, p, kind):
-    """Apply the constructor sequence of hydro_d3 / scalar_d3 to a Solver or Oracle."""
+    """Apply the constructor sequence of hydro_d3 / scalar_d3 to a Solver or Oracle.
+
+    kind "tgv" adds the harness-set Taylor-Green pressure; "tgv_p1" keeps the
+    reference's own P = 1 (hydro_d3.cc:90) under the Taylor-Green velocity."""
     F = _abi
     if kind == "rbc":
         solver.set(F.FIELD_P, np.ones(solver.dims(F.FIELD_P)))
@@ -74,11 +82,11 @@ def initialise(solver, p, kind):
         for f in (F.FIELD_VX, F.FIELD_VY, F.FIELD_VZ, F.FIELD_T):
             solver.apply_bc(f)
         return
-    if kind == "tgv":
+    if kind in ("tgv", "tgv_p1"):
         Vx, Vy = taylor_green_velocity(p)
         solver.set(F.FIELD_VX, Vx)
         solver.set(F.FIELD_VY, Vy)
-        solver.set(F.FIELD_P, taylor_green_pressure(p))
+        solver.set(F.FIELD_P, taylor_green_pressure(p) if kind == "tgv" else np.ones(solver.dims(F.FIELD_P)))
     else:
         solver.set(F.FIELD_P, np.ones(solver.dims(F.FIELD_P)))
     for f in (F.FIELD_VX, F.FIELD_VY, F.FIELD_VZ):

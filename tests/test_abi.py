@@ -30,10 +30,27 @@ def test_params_struct_matches_library_defaults():
         assert getattr(p, name) == getattr(q, name), name
 
 
-@pytest.mark.parametrize("cfg", ["ldc_33.yaml", "tgv_129.yaml", "tgv_257.yaml", "rbc_257.yaml", "tgv_513.yaml"])
+@pytest.mark.parametrize("cfg", ["ldc_33.yaml", "tgv_129.yaml", "tgv_257.yaml", "rbc_257.yaml", "tgv_513.yaml", "tgv_65_gs.yaml"])
 def test_parse_shipped_configs(cfg):
     p = saras_gb300.parser(os.path.join(HERE, "golden", "configs", cfg))
     assert p.xInd >= 5 and p.vcDepth >= 3
+
+
+REFERENCE_INPUT = "/root/reference/input/parameters.yaml"
+
+
+@pytest.mark.skipif(not os.path.exists(REFERENCE_INPUT), reason="the reference checkout is not on this machine")
+def test_shipped_input_file_values():
+    """tests/golden/configs/tgv_65_gs.yaml holds the values of the reference's own
+    input/parameters.yaml (Gauss-Seidel V(4,4), 65^3 Taylor-Green): every reference
+    key parses to the same value from both files."""
+    a = saras_gb300.parser(REFERENCE_INPUT).to_dict()
+    b = saras_gb300.parser(os.path.join(HERE, "golden", "configs", "tgv_65_gs.yaml")).to_dict()
+    ext = {"testPoisson", "mgMode", "mgTarget", "mgMaxCycles", "mixedCycles", "guessMode", "jacobiWeight", "seed",
+           "fastKernels", "smoother", "coarseSmooth", "coarseCycles"}
+    diff = {k: (a[k], b[k]) for k in a if k not in ext and a[k] != b[k]}
+    assert not diff, diff
+    assert a["gsSmooth"] == 1
 
 
 def test_parse_rejects_bad_config(tmp_path):
@@ -65,11 +82,12 @@ def test_no_device_fails_loudly():
 
 
 def test_bad_config_rejected_before_device():
-    p = _abi.default_params()
-    p.gsSmooth = 1
-    with pytest.raises(saras_gb300.SarasError) as e:
-        saras_gb300.Solver(p)
-    assert e.value.status == _abi.BAD_CONFIG
+    for field, value in (("gsSmooth", 2), ("dScheme", 2), ("resType", 3)):
+        p = _abi.default_params()
+        setattr(p, field, value)
+        with pytest.raises(saras_gb300.SarasError) as e:
+            saras_gb300.Solver(p)
+        assert e.value.status == _abi.BAD_CONFIG, field
 
 
 def test_periodic_target_mode_needs_three_sweeps():

@@ -109,14 +109,25 @@ def test_cn_solve(kind):
         assert_close(g.get(f), o.get(f), "CN " + F.FIELD_NAMES[f])
 
 
-@pytest.mark.parametrize("kind", ["ldc", "tgv", "rbc"])
-def test_multigrid_level_operators(kind):
+LEVEL_CASES = [(k, 4, 0) for k in ("ldc", "tgv", "rbc")] + [(k, ind, 1) for k in ("ldc", "tgv", "rbc") for ind in (4, 5)]
+
+
+@pytest.mark.parametrize("kind,ind,gs", LEVEL_CASES)
+def test_multigrid_level_operators(kind, ind, gs):
     """smooth / residual+restriction / coarsest GS / prolongation+add / computeError,
     fed level by level the way vCycle feeds them (poisson.cc:219-280).  Level
     data is set right before use: the reference's Jacobi swap exchanges the
     arrays of every level at once (poisson_d3.cc:168), so data parked on other
-    levels does not survive a smoothing call."""
-    p, g, o = pair(kind, depth=2)
+    levels does not survive a smoothing call.  gs = 1: lexicographic
+    Gauss-Seidel smoothing (poisson_d3.cc:137-150), bit for bit; at ind 5 the
+    finest level (35^3 padded) runs the multi-CTA wavefront kernel, the others
+    the shared-memory one."""
+    kw = dict(ind=(ind, ind, ind - 1) if kind == "rbc" else ind, depth=2)
+    p = C.CASES[kind](**kw)
+    p.gsSmooth = gs
+    g, o = Solver(p), Oracle(p)
+    C.initialise(g, p, kind)
+    C.initialise(o, p, kind)
     rng = np.random.default_rng(3)
 
     def put(lvl, which, a):
@@ -149,10 +160,15 @@ def test_multigrid_level_operators(kind):
         assert eg == eo, (norm, eg, eo)
 
 
-@pytest.mark.parametrize("kind", ["ldc", "tgv", "rbc"])
-def test_mg_solve(kind):
-    """poisson::mgSolve on the divergence of a random velocity field."""
-    p, g, o = pair(kind)
+@pytest.mark.parametrize("kind,ind,gs", [(k, 4, 0) for k in ("ldc", "tgv", "rbc")] + [(k, 5, 1) for k in ("ldc", "tgv", "rbc")])
+def test_mg_solve(kind, ind, gs):
+    """poisson::mgSolve on the divergence of a random velocity field (gs = 1:
+    Gauss-Seidel smoothing on every level, as the reference's shipped input)."""
+    p = C.CASES[kind](ind=(ind, ind, ind - 1) if kind == "rbc" else ind, depth=2 if ind == 4 else 3)
+    p.gsSmooth = gs
+    g, o = Solver(p), Oracle(p)
+    C.initialise(g, p, kind)
+    C.initialise(o, p, kind)
     rng = np.random.default_rng(17)
     for f in (F.FIELD_VX, F.FIELD_VY, F.FIELD_VZ):
         a = g.get(f) + 0.1 * rng.standard_normal(g.dims(f))
@@ -166,11 +182,16 @@ def test_mg_solve(kind):
     assert_close(g.get(F.FIELD_PP), o.get(F.FIELD_PP), "Pp")
 
 
-@pytest.mark.parametrize("kind,steps", [("ldc", 10), ("tgv", 10), ("rbc", 10)])
-def test_time_advance(kind, steps):
+@pytest.mark.parametrize("kind,steps,gs", [("ldc", 10, 0), ("tgv", 10, 0), ("rbc", 10, 0), ("ldc", 5, 1), ("tgv", 5, 1),
+                                           ("rbc", 5, 1)])
+def test_time_advance(kind, steps, gs):
     """hydro_d3 / scalar_d3 timeAdvance: equal iteration counts every step and
-    V, P (and T) within 1e-10 after the run."""
-    p, g, o = pair(kind)
+    V, P (and T) within 1e-10 after the run (gs = 1: Gauss-Seidel smoothing)."""
+    p = C.CASES[kind]()
+    p.gsSmooth = gs
+    g, o = Solver(p), Oracle(p)
+    C.initialise(g, p, kind)
+    C.initialise(o, p, kind)
     fields = [F.FIELD_VX, F.FIELD_VY, F.FIELD_VZ, F.FIELD_P, F.FIELD_PP] + ([F.FIELD_T] if kind == "rbc" else [])
     for step in range(steps):
         sg, stg = g.time_advance()
@@ -198,10 +219,13 @@ def test_reference_kats(kind):
     assert g.hydro_test_periodic() <= 1e-10
 
 
-def test_dirichlet_poisson_check():
+@pytest.mark.parametrize("ind,gs", [(4, 0), (4, 1), (5, 1)])
+def test_dirichlet_poisson_check(ind, gs):
     """TEST_POISSON: rhs = 1, Dirichlet walls r^2/6 (poisson_d3.cc:513-572); the
-    discrete Laplacian is exact for quadratics, so the solve recovers r^2/6."""
-    p = C.ldc(ind=4, depth=2)
+    discrete Laplacian is exact for quadratics, so the solve recovers r^2/6
+    (gs = 1: Gauss-Seidel smoothing with the fixed wall values in the ghosts)."""
+    p = C.ldc(ind=ind, depth=2)
+    p.gsSmooth = gs
     p.probType = 2
     p.testPoisson = 1
     p.vcCount = 25

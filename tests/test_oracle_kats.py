@@ -78,18 +78,81 @@ def test_tgv_nonlinear_term(ind, depth):
     assert err <= 2 * math.pi * h
 
 
-def test_derivatives_second_order():
-    """Central differences of the restatement converge at second order."""
-    errs = []
+def test_tgv_staggered_divergence_vanishes():
+    """The staggered divergence of the Taylor-Green field is zero up to rounding."""
     for ind in (4, 5):
         p = tgv_params((ind, ind, ind), 2)
         o = Oracle(p)
         Vx, Vy = taylor_green_velocity(p)
         o.set(F.FIELD_VX, Vx); o.set(F.FIELD_VY, Vy)
         o.vfield_divergence()
-        errs.append(np.max(np.abs(o.get(F.FIELD_MGRHS)[1:-1, 1:-1, 1:-1])))
-    # the staggered divergence of TGV is exactly 0 up to rounding
-    assert max(errs) < 1e-12
+        assert np.max(np.abs(o.get(F.FIELD_MGRHS)[1:-1, 1:-1, 1:-1])) < 1e-12
+
+
+def _orders(errs):
+    return [math.log2(errs[q] / errs[q + 1]) for q in range(len(errs) - 1)]
+
+
+def test_second_derivative_converges_at_second_order():
+    """computeDiff (vfield.cc:104-146) of u = sin x cos y cos z on [0, 2 pi]^3:
+    with the Crank-Nicolson factor 1/2 of calcDerivative2xx (derivative.cc:185-189)
+    the result approximates Laplacian(u) / 2 = -3 u / 2, and its error falls by
+    4 per halving of h (measured order >= 1.9)."""
+    errs = []
+    for ind in (4, 5, 6):
+        p = C.tgv(ind=ind, depth=2)
+        o = Oracle(p)
+        Vx, Vy = taylor_green_velocity(p)
+        o.set(F.FIELD_VX, Vx); o.set(F.FIELD_VY, Vy)
+        for f in (F.FIELD_NSE_X, F.FIELD_NSE_Y, F.FIELD_NSE_Z):
+            o.set(f, np.zeros(o.dims(f)))
+        o.vfield_compute_diff()
+        H = o.get(F.FIELD_NSE_X)
+        errs.append(np.max(np.abs(H[1:-1, 1:-1, 1:-1] + 1.5 * Vx[1:-1, 1:-1, 1:-1])))
+    assert min(_orders(errs)) >= 1.9, (errs, _orders(errs))
+
+
+def test_gradient_converges_at_second_order():
+    """sfield::gradient (sfield.cc:155-171) of P = (cos 2x + cos 2y)(cos 2z + 2)/16:
+    the face-centred difference approximates dP/dx = -sin(2x)(cos 2z + 2)/8 with
+    an error that falls by 4 per halving of h (measured order >= 1.9)."""
+    from saras_gb300 import taylor_green_pressure
+    errs = []
+    for ind in (4, 5, 6):
+        p = C.tgv(ind=ind, depth=2)
+        o = Oracle(p)
+        o.set(F.FIELD_P, taylor_green_pressure(p))
+        o.sfield_gradient(F.FIELD_P)
+        G = o.get(F.FIELD_GRAD_X)
+        n = 2 ** ind
+        xc = 2 * math.pi * (np.arange(-1, n + 1) + 0.5) / n
+        zs = 2 * math.pi * np.arange(-1, n + 2) / n
+        ana = -np.sin(2 * xc)[:, None, None] * (np.cos(2 * zs) + 2.0)[None, None, :] / 8.0
+        errs.append(np.max(np.abs(G - ana * np.ones_like(G))[1:-1, 1:-1, 1:-1]))
+    assert min(_orders(errs)) >= 1.9, (errs, _orders(errs))
+
+
+def test_crank_nicolson_half_factor():
+    """calcDerivative2xx applies 0.5 * central22n / h^2 when iScheme = 1
+    (derivative.cc:185-189): computeDiff of u = x^2 (and v = y^2, w = z^2, with
+    x the face coordinate of each component) is 1 everywhere on the core, half
+    of the true second derivative 2.  Unit cube, so the metric is 1."""
+    p = C.ldc(ind=4, depth=2)
+    o = Oracle(p)
+    n = 2 ** p.xInd
+    face = (np.arange(-1, n + 1) + 0.5) / n
+    vert = np.arange(-1, n + 2) / n
+    shapes = [o.dims(f) for f in (F.FIELD_VX, F.FIELD_VY, F.FIELD_VZ)]
+    o.set(F.FIELD_VX, np.broadcast_to((face ** 2)[:, None, None], shapes[0]))
+    o.set(F.FIELD_VY, np.broadcast_to((face ** 2)[None, :, None], shapes[1]))
+    o.set(F.FIELD_VZ, np.broadcast_to((face ** 2)[None, None, :], shapes[2]))
+    assert len(vert) == shapes[1][0]
+    for f in (F.FIELD_NSE_X, F.FIELD_NSE_Y, F.FIELD_NSE_Z):
+        o.set(f, np.zeros(o.dims(f)))
+    o.vfield_compute_diff()
+    for f in (F.FIELD_NSE_X, F.FIELD_NSE_Y, F.FIELD_NSE_Z):
+        H = o.get(f)[1:-1, 1:-1, 1:-1]
+        assert np.max(np.abs(H - 1.0)) < 1e-12, (F.FIELD_NAMES[f], H.min(), H.max())
 
 
 def test_dirichlet_r2_over_6():
