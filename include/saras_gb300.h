@@ -118,7 +118,10 @@ typedef struct saras_params {
                                  RHS, divergence and projection kernels (not
                                  bit-identical to the reference); 2: as 1, with the
                                  CN Jacobi update in split-FP64 form (FP64 values
-                                 carried in float pairs, about 1e-14 relative);
+                                 carried in float pairs, about 1e-14 relative) and
+                                 the right-hand side formed straight as that
+                                 solve's first iterate, so saras_time_advance
+                                 leaves nseRHS unwritten;
                                  0: reference arithmetic (the drop-in)          */
     int smoother;             /* target modes: 0 damped Jacobi (jacobiWeight);
                                  1 Chebyshev: each smoothing phase of n sweeps
@@ -226,6 +229,33 @@ int saras_time_advance(saras_ctx *ctx, saras_step_stats *stats);
 /* tseries::writeTSData (tseries.cc:137-178, 195-246): energy, signed max
  * divergence and (scalar runs) Nusselt number. */
 int saras_diagnostics(saras_ctx *ctx, double *energy, double *max_div, double *nusselt);
+
+/* ------------------------------------------------------ time step, probes, restart */
+/* vfield::computeTStp (vfield.cc:267-284): dt = courantNumber (dXi / max|Vx| +
+ * dEt / max|Vy| + dZt / max|Vz|), the maxima over each padded array
+ * (field::fieldMax, field.cc:602-617). */
+int saras_compute_tstp(saras_ctx *ctx, double *dt);
+/* The time step of the following steps; hydro_d3::solvePDE sets it from
+ * computeTStp capped at "Time-Step" when "Use CFL Condition" is true
+ * (hydro_d3.cc:196-203). */
+int saras_set_dt(saras_ctx *ctx, double dt);
+/* parser::parseProbes / testProbes (parser.cc:424-575): the "Probes" sets of a
+ * parameters file expanded into (i, j, k) triplets.  *count receives the total;
+ * at most `capacity` triplets are written to ijk. */
+int saras_parse_probes(const char *path, int *ijk, int capacity, int *count, char *err, int errlen);
+/* probes::getData (probes.cc:174-189): out[p * nfields + f] = fields[f] at
+ * logical index (i, j, k) of probe p (each index within -1 .. n of its axis). */
+int saras_probe(saras_ctx *ctx, int n, const int *ijk, int nfields, const int *fields, double *out);
+/* writer::writeRestart (writer.cc:455-540) / reader::readData (reader.cc:213-296):
+ * "Time" and the cores of Vx, Vy, Vz, P (and T for the scalar solver), the
+ * reference restart file's datasets and core shapes, in a raw little-endian
+ * container: "SARASRST", int32 version 1, int32 field count n, float64 time,
+ * n x {char name[16], int32 core points along x, y, z}, then the cores as
+ * float64 in C order.  Reading fills the cores (ghosts 0) and checks the
+ * shapes (reader.cc:338-399); the caller then applies the boundary conditions,
+ * as the hydro_d3 / scalar_d3 constructors do. */
+int saras_write_restart(saras_ctx *ctx, const char *path, double time);
+int saras_read_restart(saras_ctx *ctx, const char *path, double *time);
 
 /* ------------------------------------------------------ multigrid test hooks */
 /* multigrid_d3::testProlong / testTransfer / testPeriodic (poisson_d3.cc:689-857)

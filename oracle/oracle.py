@@ -64,6 +64,8 @@ def _load():
             "orc_coarse_iters": (ctypes.c_longlong, [vp]),
             "orc_time_advance": (I, [vp, ctypes.POINTER(saras_step_stats)]),
             "orc_diagnostics": (I, [vp, dp, dp, dp]),
+            "orc_compute_tstp": (I, [vp, dp]),
+            "orc_set_dt": (I, [vp, D]),
             "orc_mg_test_prolong": (I, [vp, dp]),
             "orc_mg_test_transfer": (I, [vp, dp]),
             "orc_mg_test_periodic": (I, [vp, dp]),
@@ -176,6 +178,14 @@ class Oracle:
         e, d, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
         s = self.lib.orc_diagnostics(self.h, ctypes.byref(e), ctypes.byref(d), ctypes.byref(n))
         return s, e.value, d.value, n.value
+
+    def compute_tstp(self):
+        dt = ctypes.c_double()
+        self._chk(self.lib.orc_compute_tstp(self.h, ctypes.byref(dt)), "computeTStp")
+        return dt.value
+
+    def set_dt(self, dt):
+        self._chk(self.lib.orc_set_dt(self.h, float(dt)), "set_dt")
 
     def _kat(self, fn):
         e = ctypes.c_double()

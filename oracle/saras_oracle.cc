@@ -1144,6 +1144,20 @@ struct Solver {
     }
 
     // tseries::writeTSData (tseries.cc:137-178, 195-246) at np = 1.
+    // field::fieldMax (field.cc:602-617): max |F| over the padded array.
+    static double fieldMax(const A3 &F) {
+        double m = 0.0;
+        for (double x : F.v) m = std::max(m, std::fabs(x));
+        return m;
+    }
+
+    // vfield::computeTStp (vfield.cc:267-284).
+    void computeTStp(double &dtOut) const {
+        double delx = g.dXi, dely = g.dEt, delz = g.dZt;
+        double Umax = fieldMax(fx.F), Vmax = fieldMax(fy.F), Wmax = fieldMax(fz.F);
+        dtOut = p.courantNumber * (delx / Umax + dely / Vmax + delz / Wmax);
+    }
+
     int diagnostics(double *energy, double *maxDiv, double *nusselt) {
         A3 divV; divV.resize(-1, -1, -1, fp.cnt[0], fp.cnt[1], fp.cnt[2]);
         divergence(divV);
@@ -1351,6 +1365,8 @@ int orc_mg_solve(void *h, int *cycles, double *res) {
 long long orc_coarse_iters(void *h) { return ((Handle *)h)->s.mg.coarseIters; }
 int orc_time_advance(void *h, saras_step_stats *st) { return ((Handle *)h)->s.timeAdvance(st); }
 int orc_diagnostics(void *h, double *e, double *d, double *nu) { return ((Handle *)h)->s.diagnostics(e, d, nu); }
+int orc_compute_tstp(void *h, double *dt) { ((Handle *)h)->s.computeTStp(*dt); return SARAS_OK; }
+int orc_set_dt(void *h, double dt) { ((Handle *)h)->s.dt = dt; return SARAS_OK; }
 int orc_mg_test_prolong(void *h, double *err) { *err = ((Handle *)h)->s.mg.testProlong(); return SARAS_OK; }
 int orc_mg_test_transfer(void *h, double *err) { *err = ((Handle *)h)->s.mg.testTransfer(); return SARAS_OK; }
 int orc_mg_test_periodic(void *h, double *err) { *err = ((Handle *)h)->s.mg.testPeriodic(); return SARAS_OK; }

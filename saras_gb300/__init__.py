@@ -43,6 +43,24 @@ def _dp(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
 
 
+def parse_probes(path):
+    """parser::parseProbes / testProbes (parser.cc:424-575): the probe points of a
+    parameters file as an (n, 3) array of (i, j, k)."""
+    lib = _abi.load()
+    err = ctypes.create_string_buffer(512)
+    n = ctypes.c_int()
+    IP = ctypes.POINTER(ctypes.c_int)
+    s = lib.saras_parse_probes(str(path).encode(), None, 0, ctypes.byref(n), err, 512)
+    if s != 0:
+        raise SarasError(s, err.value.decode())
+    out = np.zeros((n.value, 3), dtype=np.int32)
+    if n.value:
+        s = lib.saras_parse_probes(str(path).encode(), out.ctypes.data_as(IP), n.value, ctypes.byref(n), err, 512)
+        if s != 0:
+            raise SarasError(s, err.value.decode())
+    return out
+
+
 def parser(path):
     """parser::parser (lib/io/parser.cc:47-59): read and check parameters.yaml."""
     lib = _abi.load()
@@ -169,6 +187,33 @@ class Solver:
         if s not in (0, _abi.DIVERGENCE_LIMIT):
             self._chk(s)
         return s, e.value, d.value, n.value
+
+    # -- time step, probes, restart
+    def compute_tstp(self):
+        """vfield::computeTStp (vfield.cc:267-284)."""
+        dt = ctypes.c_double()
+        self._chk(self.lib.saras_compute_tstp(self.h, ctypes.byref(dt)))
+        return dt.value
+
+    def set_dt(self, dt):
+        self._chk(self.lib.saras_set_dt(self.h, float(dt)))
+
+    def probe(self, ijk, fields=(FIELD_VX, FIELD_VY, FIELD_VZ, FIELD_P)):
+        """probes::getData (probes.cc:174-189): values of `fields` at the (i, j, k) triplets."""
+        a = np.ascontiguousarray(np.asarray(ijk, dtype=np.int32).reshape(-1, 3))
+        f = np.ascontiguousarray(np.asarray(fields, dtype=np.int32))
+        out = np.empty((a.shape[0], f.size), dtype=np.float64)
+        IP = ctypes.POINTER(ctypes.c_int)
+        self._chk(self.lib.saras_probe(self.h, a.shape[0], a.ctypes.data_as(IP), f.size, f.ctypes.data_as(IP), _dp(out)))
+        return out
+
+    def write_restart(self, path, time):
+        self._chk(self.lib.saras_write_restart(self.h, str(path).encode(), float(time)))
+
+    def read_restart(self, path):
+        t = ctypes.c_double()
+        self._chk(self.lib.saras_read_restart(self.h, str(path).encode(), ctypes.byref(t)))
+        return t.value
 
     # -- multigrid test hooks
     def _kat(self, fn):
@@ -440,27 +485,40 @@ def rbc_temperature(params, seed=42, amplitude=1.0e-3):
 
 
 class hydro_d3:
-    """hydro_d3 (src/solvers/hydro/hydro_d3.cc:63-119): P = 1 (or a given
-    pressure), the initial condition of icType, then the velocity BCs."""
+    """hydro_d3 (src/solvers/hydro/hydro_d3.cc:63-119): with "Restart Run"
+    (params.restartFlag) the fields and the time from the restart file;
+    otherwise P = 1 (or a given pressure) and the initial condition of icType;
+    then the velocity BCs."""
 
-    def __init__(self, params, pressure=None, velocity=None):
+    restart_path = "output/restartFile.saras"
+
+    def __init__(self, params, pressure=None, velocity=None, restart=None):
         self.params = params
         self.solver = Solver(params)
         s = self.solver
-        P = np.ones(s.dims(FIELD_P)) if pressure is None else pressure
-        s.set(FIELD_P, P)
-        if velocity is not None:
-            for f, a in zip((FIELD_VX, FIELD_VY, FIELD_VZ), velocity):
-                if a is not None:
-                    s.set(f, a)
-        elif params.icType == 1:
-            Vx, Vy = taylor_green_velocity(params)
-            s.set(FIELD_VX, Vx)
-            s.set(FIELD_VY, Vy)
-        for f in (FIELD_VX, FIELD_VY, FIELD_VZ):
-            s.apply_bc(f)
         self.time = 0.0
+        if params.restartFlag:
+            self.time = s.read_restart(restart or self.restart_path)
+        else:
+            P = np.ones(s.dims(FIELD_P)) if pressure is None else pressure
+            s.set(FIELD_P, P)
+            if velocity is not None:
+                for f, a in zip((FIELD_VX, FIELD_VY, FIELD_VZ), velocity):
+                    if a is not None:
+                        s.set(f, a)
+            elif params.icType == 1:
+                Vx, Vy = taylor_green_velocity(params)
+                s.set(FIELD_VX, Vx)
+                s.set(FIELD_VY, Vy)
+        for f in self._bc_fields():
+            s.apply_bc(f)
         self.timeStepCount = 0
+
+    def _bc_fields(self):
+        return (FIELD_VX, FIELD_VY, FIELD_VZ)
+
+    def _probe_fields(self):
+        return (FIELD_VX, FIELD_VY, FIELD_VZ, FIELD_P)
 
     def timeAdvance(self):
         st, stats = self.solver.time_advance()
@@ -468,37 +526,91 @@ class hydro_d3:
             raise SarasError(st, "Jacobi iterations not converging")
         return stats
 
-    def solvePDE(self, on_step=None):
-        """hydro_d3::solvePDE (hydro_d3.cc:122-251) without file output."""
-        dt = self.params.tStp
+    def _write_probes(self, f, probes, time):
+        """probes::probeData (probes.cc:120-166): one line a probe."""
+        vals = self.solver.probe(probes, self._probe_fields())
+        for (i, j, k), row in zip(probes, vals):
+            f.write("%6.4f\t%4d\t%4d\t%4d\t" % (time, i, j, k) + "\t".join("%16.8f" % v for v in row) + "\n")
+
+    def solvePDE(self, on_step=None, probes=None, output=None):
+        """hydro_d3::solvePDE (hydro_d3.cc:122-251): the time loop with the CFL
+        time step ("Use CFL Condition": computeTStp after each step, capped at
+        "Time-Step"), the time series every "I/O Count" steps, probes every
+        "Probe Time Interval" (ProbesData.dat) and restart files every
+        "Restart Write Interval" (restartFile.saras) in the directory `output`
+        when it is given.  Solution files are not written.  Returns the time
+        series [(time, energy, max divergence, Nusselt)]."""
+        import os
+        p = self.params
+        dt = p.tStp
+        self.solver.set_dt(dt)
         series = []
-        while True:
-            stats = self.timeAdvance()
-            self.timeStepCount += 1
-            self.time += dt
-            if self.timeStepCount % max(1, self.params.ioCnt) == 0:
-                s, e, d, n = self.solver.diagnostics()
-                series.append((self.time, e, d, n))
-                if s != 0:
-                    raise SarasError(s, "Maximum divergence exceeds limit")
-            if on_step:
-                on_step(self, stats)
-            if abs(self.params.tMax - self.time) < 0.5 * dt:
-                break
+        pfile = None
+        if output is not None:
+            os.makedirs(output, exist_ok=True)
+        if probes is not None and len(probes) and p.readProbes and output is not None:
+            pfile = open(os.path.join(output, "ProbesData.dat"), "a")
+            if not p.restartFlag:
+                names = ["Vx", "Vy", "Vz", "P", "T"][:len(self._probe_fields())]
+                pfile.write("#VARIABLES = Time, X, Y, Z, " + ", ".join(names) + "\n")
+                self._write_probes(pfile, probes, self.time)
+        s0, e0, d0, n0 = self.solver.diagnostics()
+        series.append((self.time, e0, d0, n0))
+        prTime = self.time + p.prInt - math.fmod(self.time, p.prInt)
+        rsTime = self.time + p.rsInt - math.fmod(self.time, p.rsInt)
+        try:
+            while True:
+                stats = self.timeAdvance()
+                if p.useCFL:
+                    dt = self.solver.compute_tstp()
+                    if dt > p.tStp:
+                        dt = p.tStp
+                    self.solver.set_dt(dt)
+                self.timeStepCount += 1
+                self.time += dt
+                if self.timeStepCount % max(1, p.ioCnt) == 0:
+                    s, e, d, n = self.solver.diagnostics()
+                    series.append((self.time, e, d, n))
+                    if s != 0:
+                        raise SarasError(s, "Maximum divergence exceeds limit")
+                if pfile is not None and abs(prTime - self.time) < 0.5 * dt:
+                    self._write_probes(pfile, probes, self.time)
+                    prTime += p.prInt
+                if output is not None and abs(rsTime - self.time) < 0.5 * dt:
+                    self.solver.write_restart(os.path.join(output, "restartFile.saras"), self.time)
+                    rsTime += p.rsInt
+                if on_step:
+                    on_step(self, stats)
+                if abs(p.tMax - self.time) < 0.5 * dt:
+                    break
+        finally:
+            if pfile is not None:
+                pfile.close()
         return series
 
 
 class scalar_d3(hydro_d3):
-    """scalar_d3 (src/solvers/scalar/scalar_d3.cc:62-107): P = 1, T = 0 (or a
-    given temperature), V = 0, then the velocity and temperature BCs."""
+    """scalar_d3 (src/solvers/scalar/scalar_d3.cc:62-107): with "Restart Run"
+    the fields (T included) and the time from the restart file, otherwise
+    P = 1, T = 0 (or a given temperature), V = 0; then the velocity and
+    temperature BCs."""
 
-    def __init__(self, params, temperature=None, pressure=None):
+    def __init__(self, params, temperature=None, pressure=None, restart=None):
         self.params = params
         self.solver = Solver(params)
         s = self.solver
-        s.set(FIELD_P, np.ones(s.dims(FIELD_P)) if pressure is None else pressure)
-        s.set(FIELD_T, np.zeros(s.dims(FIELD_T)) if temperature is None else temperature)
-        for f in (FIELD_VX, FIELD_VY, FIELD_VZ, FIELD_T):
-            s.apply_bc(f)
         self.time = 0.0
+        if params.restartFlag:
+            self.time = s.read_restart(restart or self.restart_path)
+        else:
+            s.set(FIELD_P, np.ones(s.dims(FIELD_P)) if pressure is None else pressure)
+            s.set(FIELD_T, np.zeros(s.dims(FIELD_T)) if temperature is None else temperature)
+        for f in self._bc_fields():
+            s.apply_bc(f)
         self.timeStepCount = 0
+
+    def _bc_fields(self):
+        return (FIELD_VX, FIELD_VY, FIELD_VZ, FIELD_T)
+
+    def _probe_fields(self):
+        return (FIELD_VX, FIELD_VY, FIELD_VZ, FIELD_P, FIELD_T)

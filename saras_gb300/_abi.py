@@ -151,6 +151,12 @@ def load():
         "saras_mg_set_mode": (_I, [vp, _I, _D, _I]),
         "saras_time_advance": (_I, [vp, ctypes.POINTER(saras_step_stats)]),
         "saras_diagnostics": (_I, [vp, dp, dp, dp]),
+        "saras_compute_tstp": (_I, [vp, dp]),
+        "saras_set_dt": (_I, [vp, _D]),
+        "saras_parse_probes": (_I, [cp, ip, _I, ip, ctypes.c_char_p, _I]),
+        "saras_probe": (_I, [vp, _I, ip, _I, ip, dp]),
+        "saras_write_restart": (_I, [vp, cp, _D]),
+        "saras_read_restart": (_I, [vp, cp, dp]),
         "saras_mg_test_prolong": (_I, [vp, dp]),
         "saras_mg_test_transfer": (_I, [vp, dp]),
         "saras_mg_test_periodic": (_I, [vp, dp]),

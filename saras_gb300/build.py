@@ -66,7 +66,7 @@ def build(verbose=False, ptxas_info=False):
     with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
         objs = list(ex.map(lambda u: _compile(u, extra, verbose or ptxas_info), UNITS))
     if _stale(LIB, objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + ["-lcuda"]
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))

@@ -9,6 +9,9 @@
 #include <string>
 #include <map>
 #include <algorithm>
+#include <array>
+#include <cstdio>
+#include <vector>
 
 #include "context.cuh"
 
@@ -356,6 +359,7 @@ int saras_destroy(saras_ctx *h) {
     if (c.hscal) cudaFreeHost(c.hscal);
     for (int q = 0; q < 3; ++q) cudaFree(c.pHist[q]);
     cudaFree(c.cnp);
+    cudaFree(c.probeBuf);
     for (int k = 0; k < PK_COUNT; ++k) for (cudaEvent_t e : c.prof[k].ev) cudaEventDestroy(e);
     for (cudaEvent_t e : c.evPool) cudaEventDestroy(e);
     for (int k = 0; k < 16; ++k) if (c.userEv[k]) cudaEventDestroy(c.userEv[k]);
@@ -494,6 +498,208 @@ int saras_mg_set_mode(saras_ctx *h, int mode, double target, int max_cycles) {
 int saras_time_advance(saras_ctx *h, saras_step_stats *stats) {
     CTX_OR_FAIL(h);
     return time_advance(h->c, stats);
+}
+
+// parser::parseProbes / testProbes (parser.cc:424-575): each "[x, y, z]" set
+// of the "Probes" value gives one index list per axis, an integer or a range
+// "start:end:count" expanded to start + round(i (end - start) / (count - 1));
+// the probes are the sets' Cartesian products (x outermost), in set order.
+// Every index must lie in 0 .. 2^index + 1 of its axis.
+static bool expand_probes(const std::string &spec, const int ind[3], std::vector<int> &out, std::string &err) {
+    size_t pos = 0;
+    while (true) {
+        size_t lb = spec.find('[', pos);
+        if (lb == std::string::npos) break;
+        size_t rb = spec.find(']', lb);
+        if (rb == std::string::npos) { err = "unbalanced [ in Probes"; return false; }
+        const std::string set = spec.substr(lb + 1, rb - lb - 1);
+        pos = rb + 1;
+        std::vector<std::vector<int>> lists;
+        std::stringstream ss(set);
+        std::string item;
+        while (std::getline(ss, item, ',')) {
+            item = trim(item);
+            std::vector<int> v;
+            if (item.find(':') == std::string::npos) {
+                int x;
+                if (!to_int(item, x)) { err = "bad probe index '" + item + "'"; return false; }
+                v.push_back(x);
+            } else {
+                int a, b, n;
+                std::string t = item;
+                size_t c1 = t.find(':'), c2 = t.find(':', c1 + 1);
+                if (c2 == std::string::npos || !to_int(trim(t.substr(0, c1)), a) || !to_int(trim(t.substr(c1 + 1, c2 - c1 - 1)), b) ||
+                    !to_int(trim(t.substr(c2 + 1)), n) || a < 0 || b < 0 || n < 0) {
+                    err = "bad probe range '" + item + "'";
+                    return false;
+                }
+                if (a == b || n == 1) v.push_back(a);
+                else
+                    for (int i = 0; i < n; ++i) {
+                        double inc = ((double)b - (double)a) / ((double)n - 1.0);
+                        v.push_back(a + (int)std::round((double)i * inc));
+                    }
+            }
+            lists.push_back(v);
+        }
+        if (lists.size() != 3) {
+            err = "Number of indices for the probe(s) [" + set + "] does not match dimensionality of problem";
+            return false;
+        }
+        for (int x : lists[0])
+            for (int y : lists[1])
+                for (int z : lists[2]) { out.push_back(x); out.push_back(y); out.push_back(z); }
+    }
+    const char *axis = "XYZ";
+    for (size_t q = 0; q < out.size(); ++q) {
+        int d = (int)(q % 3), lim = (1 << ind[d]) + 1;
+        if (out[q] < 0 || out[q] > lim) {
+            err = std::string("The ") + axis[d] + " index of a probe lies outside the bounds of the domain";
+            return false;
+        }
+    }
+    return true;
+}
+
+int saras_parse_probes(const char *path, int *ijk, int capacity, int *count, char *err, int errlen) {
+    if (!path || !count || capacity < 0 || (capacity > 0 && !ijk)) return SARAS_BAD_ARG;
+    saras_params p;
+    int s = saras_parse_yaml(path, &p, err, errlen);
+    if (s) return s;
+    std::map<std::string, std::string> kv;
+    std::string e;
+    if (!read_yaml(path, kv, e)) return fail(err, errlen, e, SARAS_BAD_CONFIG);
+    std::vector<int> out;
+    const int ind[3] = {p.xInd, p.yInd, p.zInd};
+    if (kv.count("Solver/Probes") && !expand_probes(kv["Solver/Probes"], ind, out, e)) return fail(err, errlen, e, SARAS_BAD_CONFIG);
+    *count = (int)(out.size() / 3);
+    for (int q = 0; q < std::min(*count, capacity); ++q)
+        for (int d = 0; d < 3; ++d) ijk[3 * q + d] = out[3 * q + d];
+    return SARAS_OK;
+}
+
+// Restart files (writer::writeRestart, writer.cc:455-540, written every
+// "Restart Write Interval", hydro_d3.cc:229-231; reader::readData,
+// reader.cc:213-296): "Time" and the cores of Vx, Vy, Vz, P (and T with the
+// scalar solver) with the reference restart file's dataset names and core
+// shapes, in a raw little-endian container (no HDF5 library is linked):
+//   "SARASRST", int32 version 1, int32 field count n, float64 time,
+//   n x {char name[16] (NUL-padded), int32 core points along x, y, z},
+//   then the n cores as float64 in C order (z fastest), in header order.
+static const char kRestartMagic[8] = {'S', 'A', 'R', 'A', 'S', 'R', 'S', 'T'};
+
+static std::vector<int> restart_fields(const Ctx &c) {
+    std::vector<int> f = {SARAS_FIELD_VX, SARAS_FIELD_VY, SARAS_FIELD_VZ, SARAS_FIELD_P};
+    if (c.scalar) f.push_back(SARAS_FIELD_T);
+    return f;
+}
+static const char *restart_name(int f) {
+    switch (f) {
+        case SARAS_FIELD_VX: return "Vx";
+        case SARAS_FIELD_VY: return "Vy";
+        case SARAS_FIELD_VZ: return "Vz";
+        case SARAS_FIELD_P: return "P";
+        default: return "T";
+    }
+}
+
+int saras_write_restart(saras_ctx *h, const char *path, double time) {
+    if (!h || !path) return SARAS_BAD_ARG;
+    Ctx &c = h->c;
+    const std::vector<int> fields = restart_fields(c);
+    FILE *fp = std::fopen(path, "wb");
+    if (!fp) { c.err = std::string("cannot create ") + path; return SARAS_BAD_ARG; }
+    int32_t hdr[2] = {1, (int32_t)fields.size()};
+    bool ok = std::fwrite(kRestartMagic, 1, 8, fp) == 8 && std::fwrite(hdr, sizeof(int32_t), 2, fp) == 2 &&
+              std::fwrite(&time, sizeof(double), 1, fp) == 1;
+    for (int f : fields) {
+        char name[16] = {0};
+        std::strncpy(name, restart_name(f), 15);
+        int32_t dims[3] = {c.info[f].n[0], c.info[f].n[1], c.info[f].n[2]};
+        ok = ok && std::fwrite(name, 1, 16, fp) == 16 && std::fwrite(dims, sizeof(int32_t), 3, fp) == 3;
+    }
+    std::vector<double> pad, core;
+    for (int f : fields) {
+        if (!ok) break;
+        const int n0 = c.info[f].n[0], n1 = c.info[f].n[1], n2 = c.info[f].n[2];
+        pad.resize(field_count(c, f));
+        int s = saras_download(h, f, pad.data());
+        if (s) { std::fclose(fp); return s; }
+        core.resize((size_t)n0 * n1 * n2);
+        for (int i = 0; i < n0; ++i)
+            for (int j = 0; j < n1; ++j)
+                std::memcpy(&core[((size_t)i * n1 + j) * n2], &pad[((size_t)(i + 1) * (n1 + 2) + (j + 1)) * (n2 + 2) + 1],
+                            sizeof(double) * n2);
+        ok = std::fwrite(core.data(), sizeof(double), core.size(), fp) == core.size();
+    }
+    if (std::fclose(fp) != 0) ok = false;
+    if (!ok) { c.err = std::string("writing ") + path + " failed"; return SARAS_BAD_ARG; }
+    return SARAS_OK;
+}
+
+int saras_read_restart(saras_ctx *h, const char *path, double *time) {
+    if (!h || !path) return SARAS_BAD_ARG;
+    Ctx &c = h->c;
+    FILE *fp = std::fopen(path, "rb");
+    if (!fp) { c.err = std::string("Restart flag is true, but could not open restart file ") + path; return SARAS_BAD_CONFIG; }
+    char magic[8];
+    int32_t hdr[2];
+    double t = 0.0;
+    bool ok = std::fread(magic, 1, 8, fp) == 8 && std::memcmp(magic, kRestartMagic, 8) == 0 && std::fread(hdr, sizeof(int32_t), 2, fp) == 2 &&
+              hdr[0] == 1 && hdr[1] > 0 && hdr[1] <= SARAS_NUM_FIELDS && std::fread(&t, sizeof(double), 1, fp) == 1;
+    std::vector<std::string> names;
+    std::vector<std::array<int32_t, 3>> dims;
+    for (int q = 0; ok && q < hdr[1]; ++q) {
+        char name[17] = {0};
+        std::array<int32_t, 3> d;
+        ok = std::fread(name, 1, 16, fp) == 16 && std::fread(d.data(), sizeof(int32_t), 3, fp) == 3 && d[0] > 0 && d[1] > 0 && d[2] > 0;
+        names.push_back(name);
+        dims.push_back(d);
+    }
+    if (!ok) { std::fclose(fp); c.err = std::string(path) + " is not a restart file of this format"; return SARAS_BAD_CONFIG; }
+    const long dataStart = std::ftell(fp);
+    // reader::restartCheck (reader.cc:338-399): every field present with the context's core shape
+    std::vector<double> pad;
+    for (int f : restart_fields(c)) {
+        long off = dataStart;
+        int q = 0;
+        for (; q < (int)names.size() && names[q] != restart_name(f); ++q) off += (long)sizeof(double) * dims[q][0] * dims[q][1] * dims[q][2];
+        const int n0 = c.info[f].n[0], n1 = c.info[f].n[1], n2 = c.info[f].n[2];
+        if (q == (int)names.size() || dims[q][0] != n0 || dims[q][1] != n1 || dims[q][2] != n2) {
+            std::fclose(fp);
+            c.err = std::string("restart file does not match the grid: field ") + restart_name(f);
+            return SARAS_BAD_CONFIG;
+        }
+        pad.assign(field_count(c, f), 0.0);
+        if (std::fseek(fp, off, SEEK_SET) != 0) ok = false;
+        for (int i = 0; ok && i < n0; ++i)
+            for (int j = 0; ok && j < n1; ++j)
+                ok = std::fread(&pad[((size_t)(i + 1) * (n1 + 2) + (j + 1)) * (n2 + 2) + 1], sizeof(double), n2, fp) == (size_t)n2;
+        if (!ok) { std::fclose(fp); c.err = std::string("reading ") + path + " failed"; return SARAS_BAD_CONFIG; }
+        int s = saras_upload(h, f, pad.data());
+        if (s) { std::fclose(fp); return s; }
+    }
+    std::fclose(fp);
+    if (time) *time = t;
+    return SARAS_OK;
+}
+
+int saras_compute_tstp(saras_ctx *h, double *dt) {
+    CTX_OR_FAIL(h);
+    if (!dt) return SARAS_BAD_ARG;
+    return compute_tstp(h->c, dt);
+}
+
+int saras_set_dt(saras_ctx *h, double dt) {
+    CTX_OR_FAIL(h);
+    if (!(dt > 0.0) || !std::isfinite(dt)) return SARAS_BAD_ARG;
+    h->c.dt = dt;
+    return SARAS_OK;
+}
+
+int saras_probe(saras_ctx *h, int n, const int *ijk, int nfields, const int *fields, double *out) {
+    CTX_OR_FAIL(h);
+    return probe(h->c, n, ijk, nfields, fields, out);
 }
 
 int saras_diagnostics(saras_ctx *h, double *energy, double *max_div, double *nusselt) {

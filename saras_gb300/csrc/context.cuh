@@ -1,6 +1,8 @@
 // context.cuh -- the solver context behind the C ABI.
 #pragma once
 
+#include <cuda.h>
+
 #include "common.cuh"
 
 struct saras_ctx;
@@ -102,11 +104,20 @@ struct Ctx {
     int mgMaxCycles = 200;
     int maxCount = 0;
     int numSMs = 1;           // multiprocessors of the context's device
+    // finest-level FP32 plane-streaming stencils (TMA, target modes): tensor
+    // maps of the two iterate buffers (a32, b32) with the main and the side
+    // box, and the launch shape; planeOk false when the level does not fit
+    bool planeOk = false;
+    CUtensorMap planeMap[2], planeSide[2];
+    int planeOps = 0, planeSideFloats = 0, planeSlotFloats = 0, planeSegPlanes = 0, planeSegs = 0, planeMaxQ = 0;
+    size_t planeSmem = 0;
     double *wallX = nullptr, *wallY = nullptr, *wallZ = nullptr;   // Dirichlet check walls
     // reductions
     double *red = nullptr;          // partial sums (device)
     int redCap = 0;
     double *dscal = nullptr;        // device scalars
+    void *probeBuf = nullptr;       // probe indices and values (grown on demand)
+    size_t probeBytes = 0;
     double *hscal = nullptr;        // pinned host mirror
     int *dflag = nullptr;
     // stats
@@ -171,6 +182,8 @@ int compute_trhs(Ctx &c);
 int cn_solve(Ctx &c, int comp, int *iters, double *maxerr);
 int project(Ctx &c, bool with_bc);
 int diagnostics(Ctx &c, double *energy, double *maxdiv, double *nusselt);
+int compute_tstp(Ctx &c, double *dt);
+int probe(Ctx &c, int n, const int *ijk, int nf, const int *fields, double *out);
 int hydro_test_periodic(Ctx &c, double *err);
 int time_advance(Ctx &c, saras_step_stats *st);
 

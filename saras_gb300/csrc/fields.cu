@@ -353,44 +353,75 @@ __global__ void __launch_bounds__(256) k_rhs_fast(RhsArgs a, RhsFast q) {
     a.H(i, j, k) = fma(h, q.dt, f0);
 }
 
-// Split-FP64 form (fastKernels = 2) of the same right-hand side,
-//   H = F + dt (visc Lap F - (V.grad) F [+ Fb avg T] - grad P),
-// evaluated in float-pair arithmetic (df64.cuh) from split values: every
-// intermediate keeps about 44 bits, so H is good to about 2^-44 of the
-// largest term (about 1e-13 for O(1) fields).  FP64 work per point: the two
-// additions that form F + dt h.
-struct RhsDf {
-    fpair k2[3];     // visc m2h ih2
-    fpair k1n[3];    // 0.5 ih m1 / (number of velocity values averaged along that axis)
-    fpair g[3];      // gm ih (pressure gradient)
-    fpair fb2, dt;
-};
+// Split-FP64 form (fastKernels = 2): k_rhs_df3 below, float-pair arithmetic
+// (df64.cuh) from split values, every intermediate good to about 2^-44.
 
-// All three components in one pass.  A stencil of one component reads about
-// a dozen values of the four fields, and splitting each read into a float pair
-// would cost about 35 splits a point over the three components.  Here a CTA
-// owns a 32 (k) x 8 (j) tile of columns and marches kRhs3March planes along i;
-// each plane of Vx, Vy, Vz and P on the tile plus a one-point halo is read
-// once, split once and kept in shared memory (four rolling planes, so one
-// barrier a plane), from where the three components' stencils read it.
-// Indices are logical (each field keeps its own core counts and strides); a
-// component is evaluated where (i, j, k) is in its core.  The terms and their
-// order per component follow k_rhs_fast.
+// All three components in one pass, written straight as the first iterate of
+// the split-FP64 Jacobi solve.  With C0 = V at the start of the step the delta
+// form's N0 = H - C0 + k1 sum_d c_d S_d(C0) (k_cn_pack) does not contain C0:
+//   A = N0 / Dn = sum_d KL_d S_d - sum_d KN_d s_d delta_d - KG dP [+ KB (T + T')]
+// with S_d = F(+d) + F(-d) - 2F, delta_d = F(+d) - F(-d), s_d the velocity
+// values averaged along d (summed; the 1/count is in KN_d), and the constants
+// KL_d = (dt visc m2h ih2 + k1 c_d) / Dn, KN_d = dt 0.5 ih m1 / count / Dn,
+// KG = dt gm ih / Dn, KB = dt Fb / 2 / Dn folded on the host.  nseRHS itself
+// (H = F + dt h) is not formed: the solve needs only A, so the FP64 additions
+// that would carry F's 53 bits into H are not spent.  A is about dt |h| in
+// size and good to about 2^-44 of its largest term.
+//
+// A stencil of one component reads about a dozen values of the four fields,
+// and splitting each read into a float pair would cost about 35 splits a point
+// over the three components.  Here a CTA owns a 32 (k) x 8 (j) tile of columns
+// and marches kRhs3March planes along i; each plane of Vx, Vy, Vz and P on the
+// tile plus a one-point halo is read once, split once and kept in shared
+// memory (four rolling planes, so one barrier a plane), from where the three
+// components' stencils read it.  Indices are logical (each field keeps its own
+// core counts and strides); a component is evaluated where (i, j, k) is in its
+// core.
 constexpr int kRhs3March = 16;
 constexpr int kR3K = 34, kR3N = 10 * kR3K;   // tile (8 x 32) + halo, per field and plane
+
+struct Rhs3K {
+    fpair kl[3];   // Laplacian: viscous term and the Jacobi coupling of N0
+    fpair kn[3];   // advection
+    fpair kg;      // pressure gradient
+    fpair kb;      // buoyancy (Vz)
+};
 
 struct Rhs3Args {
     const double *f[4];        // Vx, Vy, Vz, P
     int n[4][3];               // their core counts
     long sx[4], sy[4];         // and strides
     const double *T;           // buoyancy: T, in P's layout
-    double *H[3];              // component layouts
-    float *n0h[3], *n0l[3];
+    float *n0h[3], *n0l[3];    // A of each component, component layouts
     int nu[3];                 // union of the cores
     int buoyancy;
-    RhsDf q[3];
-    CnDf cf[3];
+    Rhs3K q[3];
 };
+
+// p + m - 2 c as an unnormalised pair: two TwoSums of the high parts (exact),
+// the low parts and rounding errors in the second float.
+__device__ __forceinline__ fpair lap_pair(fpair p, fpair m, fpair c) {
+    float s, e, h, e2;
+    two_sum(p.h, m.h, s, e);
+    two_sum(s, -2.0f * c.h, h, e2);
+    return fpair{h, e2 + (e + ((p.l + m.l) - 2.0f * c.l))};
+}
+
+// p - m as an unnormalised pair.
+__device__ __forceinline__ fpair sub_pair(fpair p, fpair m) {
+    float s, e;
+    two_sum(p.h, -m.h, s, e);
+    return fpair{s, e + (p.l - m.l)};
+}
+
+// a + b + c + d as an unnormalised pair.
+__device__ __forceinline__ fpair sum4_pair(fpair a, fpair b, fpair c, fpair d) {
+    float s1, e1, s2, e2, s, e3;
+    two_sum(a.h, b.h, s1, e1);
+    two_sum(c.h, d.h, s2, e2);
+    two_sum(s1, s2, s, e3);
+    return fpair{s, (e1 + e2 + e3) + ((a.l + b.l) + (c.l + d.l))};
+}
 
 template <int C>
 __device__ __forceinline__ void rhs3_point(const Rhs3Args &a, const float2 (*sm)[4][kR3N], int i, int j, int k, int c0) {
@@ -400,44 +431,37 @@ __device__ __forceinline__ void rhs3_point(const Rhs3Args &a, const float2 (*sm)
         return fpair{v.x, v.y};
     };
     const long o = (long)(i + 1) * a.sx[C] + (long)(j + 1) * a.sy[C] + (k + 1);
-    const RhsDf &q = a.q[C];
+    const Rhs3K &q = a.q[C];
     fpair c = G(C, 0, 0, 0), ex = G(C, 1, 0, 0), wx = G(C, -1, 0, 0);
     fpair ey = G(C, 0, 1, 0), wy = G(C, 0, -1, 0), ez = G(C, 0, 0, 1), wz = G(C, 0, 0, -1);
-    fpair c2 = fpair{-2.0f * c.h, -2.0f * c.l};
-    fpair Sx = fp_add(fp_add(ex, wx), c2), Sy = fp_add(fp_add(ey, wy), c2), Sz = fp_add(fp_add(ez, wz), c2);
-    fpair h = fp_fma(q.k2[0], Sx, fp_fma(q.k2[1], Sy, fp_mul(q.k2[2], Sz)));
+    fpair acc = fp_fma(q.kl[0], lap_pair(ex, wx, c), fp_fma(q.kl[1], lap_pair(ey, wy, c), fp_mul(q.kl[2], lap_pair(ez, wz, c))));
     fpair s0, s1, s2, dp;
     if (C == 0) {
         s0 = c;
-        s1 = fp_add(fp_add(G(1, 0, 0, 0), G(1, 0, -1, 0)), fp_add(G(1, 1, 0, 0), G(1, 1, -1, 0)));
-        s2 = fp_add(fp_add(G(2, 0, 0, 0), G(2, 0, 0, -1)), fp_add(G(2, 1, 0, 0), G(2, 1, 0, -1)));
-        dp = fp_add(G(3, 1, 0, 0), fp_neg(G(3, 0, 0, 0)));
+        s1 = sum4_pair(G(1, 0, 0, 0), G(1, 0, -1, 0), G(1, 1, 0, 0), G(1, 1, -1, 0));
+        s2 = sum4_pair(G(2, 0, 0, 0), G(2, 0, 0, -1), G(2, 1, 0, 0), G(2, 1, 0, -1));
+        dp = sub_pair(G(3, 1, 0, 0), G(3, 0, 0, 0));
     } else if (C == 1) {
-        s0 = fp_add(fp_add(G(0, 0, 0, 0), G(0, 0, 1, 0)), fp_add(G(0, -1, 0, 0), G(0, -1, 1, 0)));
+        s0 = sum4_pair(G(0, 0, 0, 0), G(0, 0, 1, 0), G(0, -1, 0, 0), G(0, -1, 1, 0));
         s1 = c;
-        s2 = fp_add(fp_add(G(2, 0, 0, 0), G(2, 0, 0, -1)), fp_add(G(2, 0, 1, 0), G(2, 0, 1, -1)));
-        dp = fp_add(G(3, 0, 1, 0), fp_neg(G(3, 0, 0, 0)));
+        s2 = sum4_pair(G(2, 0, 0, 0), G(2, 0, 0, -1), G(2, 0, 1, 0), G(2, 0, 1, -1));
+        dp = sub_pair(G(3, 0, 1, 0), G(3, 0, 0, 0));
     } else {
-        s0 = fp_add(fp_add(G(0, 0, 0, 0), G(0, 0, 0, 1)), fp_add(G(0, -1, 0, 0), G(0, -1, 0, 1)));
-        s1 = fp_add(fp_add(G(1, 0, 0, 0), G(1, 0, -1, 0)), fp_add(G(1, 0, 0, 1), G(1, 0, -1, 1)));
+        s0 = sum4_pair(G(0, 0, 0, 0), G(0, 0, 0, 1), G(0, -1, 0, 0), G(0, -1, 0, 1));
+        s1 = sum4_pair(G(1, 0, 0, 0), G(1, 0, -1, 0), G(1, 0, 0, 1), G(1, 0, -1, 1));
         s2 = c;
-        dp = fp_add(G(3, 0, 0, 1), fp_neg(G(3, 0, 0, 0)));
+        dp = sub_pair(G(3, 0, 0, 1), G(3, 0, 0, 0));
     }
-    h = fp_fma(fp_neg(s0), fp_mul(fp_add(ex, fp_neg(wx)), q.k1n[0]), h);
-    h = fp_fma(fp_neg(s1), fp_mul(fp_add(ey, fp_neg(wy)), q.k1n[1]), h);
-    h = fp_fma(fp_neg(s2), fp_mul(fp_add(ez, fp_neg(wz)), q.k1n[2]), h);
+    acc = fp_fma(fp_neg(q.kn[0]), fp_mul(s0, sub_pair(ex, wx)), acc);
+    acc = fp_fma(fp_neg(q.kn[1]), fp_mul(s1, sub_pair(ey, wy)), acc);
+    acc = fp_fma(fp_neg(q.kn[2]), fp_mul(s2, sub_pair(ez, wz)), acc);
     if (C == 2 && a.buoyancy) {
         long ot = (long)(i + 1) * a.sx[3] + (long)(j + 1) * a.sy[3] + (k + 1);
-        h = fp_add(h, fp_mul(q.fb2, fp_add(fp_of(a.T[ot]), fp_of(a.T[ot + 1]))));
+        acc = fp_fma(q.kb, fp_add(fp_of(a.T[ot]), fp_of(a.T[ot + 1])), acc);
     }
-    h = fp_fma(fp_neg(q.g[C]), dp, h);
-    h = fp_mul(h, q.dt);
-    a.H[C][o] = (a.f[C][o] + f2d(h.h)) + f2d(h.l);
-    const CnDf &cf = a.cf[C];
-    fpair n0 = fp_fma(cf.kc[0], Sx, fp_fma(cf.kc[1], Sy, fp_fma(cf.kc[2], Sz, h)));
-    n0 = fp_mul(n0, cf.invDn);   // A = N0 / Dn: the Jacobi solve's first iterate from D = 0
-    a.n0h[C][o] = n0.h;
-    a.n0l[C][o] = n0.l;
+    acc = fp_fma(fp_neg(q.kg), dp, acc);
+    a.n0h[C][o] = acc.h;
+    a.n0l[C][o] = acc.l;
 }
 
 __global__ void __launch_bounds__(256, 5) k_rhs_df3(Rhs3Args a) {
@@ -1435,32 +1459,29 @@ int compute_rhs(Ctx &c) {
         a.b = core_box(c.info[SARAS_FIELD_VX + q]);
         dim3 g, bl; box_launch_dims(a.b, g, bl);
         if (c.p.fastKernels == 2) {
-            RhsDf qd;
             auto pr = [](double x) { fpair r; r.h = (float)x; r.l = (float)(x - (double)r.h); return r; };
-            for (int d = 0; d < 3; ++d) {
-                qd.k2[d] = pr(qf.K2[d]);
-                qd.k1n[d] = pr(qf.K1[d] / (q == d ? 1.0 : 4.0));   // Slices<q, d>::n
-                qd.g[d] = pr(qf.G[d]);
-            }
-            qd.fb2 = pr(qf.Fb2);
-            qd.dt = pr(qf.dt);
             CnArgs ca;
             CnFast cfa;
             cn_setup(c, q, ca, cfa);
-            CnDf cf = cn_df_consts(cfa);
+            const double kc[3] = {cfa.k1 * cfa.c1, cfa.k1 * cfa.c2, cfa.k1 * cfa.c3};
+            Rhs3K qk;
+            for (int d = 0; d < 3; ++d) {
+                qk.kl[d] = pr((c.dt * qf.K2[d] + kc[d]) * cfa.invDn);
+                qk.kn[d] = pr(c.dt * (qf.K1[d] / (q == d ? 1.0 : 4.0)) * cfa.invDn);   // Slices<q, d>::n
+            }
+            qk.kg = pr(c.dt * qf.G[q] * cfa.invDn);
+            qk.kb = pr(c.dt * qf.Fb2 * cfa.invDn);
             int e = cnp_ensure(c);
             if (e) return e;
             float *n0h = c.cnp + (size_t)2 * q * c.cnpCount, *n0l = n0h + c.cnpCount;
             c.n0Fresh[q] = 1;
             {
-                a3.f[q] = a.F.p;
-                a3.H[q] = a.H.p;
                 a3.n0h[q] = n0h;
                 a3.n0l[q] = n0l;
-                a3.q[q] = qd;
-                a3.cf[q] = cf;
+                a3.q[q] = qk;
                 bytes += 8.0 * (double)a.H.size();
                 if (q < 2) continue;
+                a3.f[0] = a.V.v[0].p; a3.f[1] = a.V.v[1].p; a3.f[2] = a.V.v[2].p;
                 a3.f[3] = a.P.p;
                 a3.T = a.T.p;
                 for (int f = 0; f < 4; ++f) {
@@ -1489,8 +1510,11 @@ int compute_rhs(Ctx &c) {
         bytes += 8.0 * (double)a.H.size();
     }
     // algorithmic bytes per point and component: F, two other velocity
-    // components, P (+ T) in, H out (+ N0 as a float pair with fastKernels = 2)
-    prof_end(c, PK_RHS, 0, bytes * ((a.buoyancy ? 6.0 : 5.0) + (c.p.fastKernels == 2 ? 1.0 : 0.0)));
+    // components, P (+ T) in and H out; with fastKernels = 2 the four fields
+    // (+ T) are read once for the three components and A (a float pair) is
+    // written instead of H
+    if (c.p.fastKernels == 2) prof_end(c, PK_RHS, 0, bytes * (a.buoyancy ? 8.0 : 7.0) / 3.0);
+    else prof_end(c, PK_RHS, 0, bytes * (a.buoyancy ? 6.0 : 5.0));
     return check_launch(c, "rhs");
 }
 
@@ -1803,6 +1827,85 @@ int diagnostics(Ctx &c, double *energy, double *maxdiv, double *nusselt) {
     if (maxdiv) *maxdiv = c.hscal[12];
     if (nusselt) *nusselt = c.scalar ? 1.0 + (c.hscal[11] / c.totalVol) / c.kappa : 0.0;
     return c.hscal[12] > 1.0e5 ? SARAS_DIVERGENCE_LIMIT : SARAS_OK;
+}
+
+// max |F| over a whole padded array (field::fieldMax, field.cc:602-617): exact in any order.
+__global__ void k_field_maxabs(const double *a, long n, double *out) {
+    double m = 0;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+        double v = fabs(a[t]);
+        if (v != v) v = INFINITY;
+        m = fmax(m, v);
+    }
+    block_max_to(m, out);
+}
+
+// vfield::computeTStp (vfield.cc:267-284): dt = courantNumber (dXi / Umax +
+// dEt / Vmax + dZt / Wmax) with U/V/Wmax = fieldMax of Vx/Vy/Vz, in the
+// reference's operation order (a zero maximum gives an infinite term, which
+// solvePDE's cap at "Time-Step" then replaces, hydro_d3.cc:196-203).
+int compute_tstp(Ctx &c, double *dt) {
+    SARAS_CUDA_TRY(cudaMemsetAsync(c.dscal + 48, 0, 3 * sizeof(double), c.stream));
+    for (int q = 0; q < 3; ++q) {
+        long n = mview(c, SARAS_FIELD_VX + q).size();
+        int nb = (int)std::max<long>(1, std::min<long>((n + 255) / 256, 152L * 4));
+        k_field_maxabs<<<nb, 256, 0, c.stream>>>(c.f[SARAS_FIELD_VX + q], n, c.dscal + 48 + q);
+    }
+    count_launch(c, 3);
+    SARAS_CUDA_TRY(cudaMemcpyAsync(c.hscal + 48, c.dscal + 48, 3 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    SARAS_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    int s = check_launch(c, "computeTStp");
+    if (s) return s;
+    const double Umax = c.hscal[48], Vmax = c.hscal[49], Wmax = c.hscal[50];
+    *dt = c.p.courantNumber * (c.dXi[0] / Umax + c.dXi[1] / Vmax + c.dXi[2] / Wmax);
+    return SARAS_OK;
+}
+
+// probes::getData (probes.cc:174-189): the value of each field at each probe
+// point (logical indices of the field's padded array); out[p * nf + f].
+struct ProbeFields {
+    const double *f[SARAS_NUM_FIELDS];
+    long sx[SARAS_NUM_FIELDS], sy[SARAS_NUM_FIELDS];
+};
+__global__ void k_probe(const int *ijk, int n, ProbeFields pf, int nf, double *out) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n * nf) return;
+    int p = t / nf, f = t - p * nf;
+    const int i = ijk[3 * p], j = ijk[3 * p + 1], k = ijk[3 * p + 2];
+    out[t] = pf.f[f][(long)(i + 1) * pf.sx[f] + (long)(j + 1) * pf.sy[f] + (k + 1)];
+}
+
+int probe(Ctx &c, int n, const int *ijk, int nf, const int *fields, double *out) {
+    if (n < 0 || nf < 0 || nf > SARAS_NUM_FIELDS || (n > 0 && (!ijk || !out)) || (nf > 0 && !fields)) return SARAS_BAD_ARG;
+    if (n == 0 || nf == 0) return SARAS_OK;
+    ProbeFields pf;
+    for (int q = 0; q < nf; ++q) {
+        if (fields[q] < 0 || fields[q] >= SARAS_NUM_FIELDS) return SARAS_BAD_ARG;
+        View3<double> v = mview(c, fields[q]);
+        pf.f[q] = v.p; pf.sx[q] = v.sx; pf.sy[q] = v.sy;
+        for (int p = 0; p < n; ++p)
+            for (int d = 0; d < 3; ++d)
+                if (ijk[3 * p + d] < -1 || ijk[3 * p + d] > v.n[d]) {
+                    c.err = "probe index outside the padded field";
+                    return SARAS_BAD_ARG;
+                }
+    }
+    const size_t need = sizeof(int) * 3 * (size_t)n + sizeof(double) * (size_t)n * nf + 256;
+    if (need > c.probeBytes) {
+        cudaFree(c.probeBuf);
+        c.probeBuf = nullptr;
+        c.probeBytes = 0;
+        SARAS_CUDA_TRY(cudaMalloc(&c.probeBuf, need));
+        c.probeBytes = need;
+    }
+    int *dijk = reinterpret_cast<int *>(c.probeBuf);
+    double *dout = reinterpret_cast<double *>(static_cast<char *>(c.probeBuf) + ((sizeof(int) * 3 * (size_t)n + 255) / 256) * 256);
+    SARAS_CUDA_TRY(cudaMemcpyAsync(dijk, ijk, sizeof(int) * 3 * (size_t)n, cudaMemcpyHostToDevice, c.stream));
+    k_probe<<<(n * nf + 255) / 256, 256, 0, c.stream>>>(dijk, n, pf, nf, dout);
+    count_launch(c);
+    SARAS_CUDA_TRY(cudaMemcpyAsync(out, dout, sizeof(double) * (size_t)n * nf, cudaMemcpyDeviceToHost, c.stream));
+    SARAS_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return check_launch(c, "probes");
 }
 
 // hydro_d3::testPeriodic (hydro_d3.cc:536-679): fill Vx, Vy (and the expected

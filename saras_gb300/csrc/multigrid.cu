@@ -26,11 +26,15 @@
 // Compiled with --fmad=false (see fields.cu).
 
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <algorithm>
 
 #include "context.cuh"
 #include "df64.cuh"
+#include "tma.cuh"
+
+#include <cudaTypedefs.h>
 
 namespace saras {
 
@@ -1049,6 +1053,160 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 6 : 5) k_tgt_residual(OT
     if (MAXRED) block_max_bits_to(m, maxres);
 }
 
+// ---- finest-level FP32 stencils staged through shared memory by the TMA
+// The target-mode FP32 Jacobi sweep and residual of the finest level (the
+// inner V-cycles of the mixed mode spend most of their HBM traffic there)
+// stream x planes through a ring of shared-memory slots that the Tensor Memory
+// Accelerator fills.  A CTA owns kPlaneRows consecutive j rows over the whole
+// k extent (the level's last CTA also its one extra row: rows are 2^m + 1
+// points) and a segment of consecutive i planes.  Rows j0-1 .. j0+R of one
+// plane are one contiguous span of the padded level array, copied as 2D boxes
+// of a tensor map that views the array as rows of four floats: the padded row
+// pitch, 2^m + 3 floats, is no multiple of 16 bytes, which the strides of a
+// 3D tensor map must be.  With the whole k extent in the slot, the periodic
+// and mirror images along k are in the slot as well; along j the mirror
+// images are in the tile's halo rows and a periodic image row is one more box
+// (a second tensor map with a one-row box); along i the slot of plane -1 or
+// E+1 holds its image plane.  One thread fills the ring (kPlaneRing slots,
+// each with its mbarrier: planes i-1, i, i+1 and two ahead); every thread
+// computes its points of plane i from three slots, reads r with plain
+// coalesced loads issued a plane ahead and writes its results with plain
+// coalesced stores.  The arithmetic is k_tgt_sweep's / k_tgt_residual's,
+// operand for operand, so the results are the same bits.
+constexpr int kPlaneRows = 8;
+constexpr int kPlaneRing = 5;
+constexpr int kPlaneBox = 240;      // main box: 240 rows of four floats
+constexpr int kPlaneThreads = 256;
+
+struct PlaneArgs {
+    float *out;
+    const float *r;
+    int sx, sy;          // strides of the padded level array, floats
+    MgBC bc;
+    TgK<float> c;
+    int nops;            // main boxes a plane
+    int sideFloats;      // floats of the side box (its tensor map's box)
+    int slotFloats;      // floats a slot: nops main boxes + the side box, a multiple of 32
+    int planesPerSeg;
+    int *err;            // set when an mbarrier wait gives up
+};
+
+template <int MODE, int MAXQ>
+__global__ void __launch_bounds__(kPlaneThreads, 3)
+    k_tgt_plane_tma(const __grid_constant__ CUtensorMap map, const __grid_constant__ CUtensorMap sideMap, const PlaneArgs a) {
+    extern __shared__ __align__(128) float sm[];
+    __shared__ uint64_t bar[kPlaneRing];
+    const int tid = threadIdx.x;
+    const int E0 = a.bc.E[0], E1 = a.bc.E[1], E2 = a.bc.E[2];
+    const int W = E2 + 1, sx = a.sx, sy = a.sy;
+    const int nTiles = (E1 + 1) / kPlaneRows;
+    const int j0 = blockIdx.x * kPlaneRows;
+    const int R = (int)blockIdx.x == nTiles - 1 ? E1 + 1 - j0 : kPlaneRows;
+    const int i0 = blockIdx.y * a.planesPerSeg;
+    const int i1 = min(i0 + a.planesPerSeg, E0 + 1);
+    if (i0 >= i1) return;
+    const int nplanes = i1 - i0 + 2;   // planes i0-1 .. i1
+    const bool per1 = a.bc.per[1] != 0, per2 = a.bc.per[2] != 0;
+    const bool side = per1 && (j0 == 0 || j0 + R - 1 == E1);
+    const int sideRow = j0 == 0 ? E1 - 1 : 1;   // periodic image of row -1 / E1 + 1
+    const uint32_t tx = (uint32_t)(a.nops * kPlaneBox * 16 + (side ? a.sideFloats * 4 : 0));
+    if (tid == 0) {
+        for (int q = 0; q < kPlaneRing; ++q) mbar_init(&bar[q], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    auto plane_img = [&](int q) { return pad_img(i0 - 1 + q, E0, a.bc.per[0]); };
+    auto issue = [&](int q) {   // plane i0 - 1 + q into slot q % kPlaneRing
+        const int ii = plane_img(q);
+        const long start = (long)(ii + 1) * sx + (long)j0 * sy;   // array row j0: row j0 - 1
+        const int slot = q % kPlaneRing;
+        uint64_t *m = &bar[slot];
+        mbar_arrive_expect_tx(m, tx);
+        const uint32_t dst = su32(sm + (size_t)slot * a.slotFloats);
+        const int c0 = (int)(start >> 2);
+        for (int op = 0; op < a.nops; ++op) tma_load_2d(dst + op * kPlaneBox * 16, &map, 0, c0 + op * kPlaneBox, m);
+        if (side) tma_load_2d(dst + a.nops * kPlaneBox * 16, &sideMap, 0, (int)(((long)(ii + 1) * sx + (long)(sideRow + 1) * sy) >> 2), m);
+    };
+    int issued = 0;
+    if (tid == 0)
+        for (; issued < min(kPlaneRing, nplanes); ++issued) issue(issued);
+    // this thread's points of a plane: p = tid + 256 q over the tile's R x W points
+    const int npts = R * W;
+    // P[q]: the point's index in a slot after the plane's base offset; its
+    // offset in a plane of the level array is P[q] + j0 sy
+    int P[MAXQ];
+    unsigned edge = 0u;
+#pragma unroll
+    for (int q = 0; q < MAXQ; ++q) {
+        const int p = tid + q * kPlaneThreads;
+        const int row = p / W, col = p - row * W;
+        P[q] = (row + 1) * sy + col + 1;
+        if (p < npts && (col == 0 || col == E2 || j0 + row == 0 || j0 + row == E1)) edge |= 1u << q;
+    }
+    const int gj = j0 * sy;
+    auto base = [&](int q) { return (int)((((long)(plane_img(q) + 1) * sx + (long)j0 * sy)) & 3); };
+    auto side_base = [&](int q) { return (int)((((long)(plane_img(q) + 1) * sx + (long)(sideRow + 1) * sy)) & 3); };
+    const TgK<float> &c = a.c;
+    bool ok = true;
+    int waited = 0;   // planes whose slot this thread has waited for
+    for (int i = i0; i < i1 && ok; ++i) {
+        const int qc = i - i0 + 1;   // plane i is plane qc of the segment
+        // r of plane i first: its loads are in flight while the slots are awaited
+        float rr[MAXQ];
+#pragma unroll
+        for (int q = 0; q < MAXQ; ++q)
+            rr[q] = tid + q * kPlaneThreads < npts ? __ldcs(a.r + (long)(i + 1) * sx + gj + P[q]) : 0.0f;
+        while (ok && waited <= qc + 1) {
+            if (mbar_wait(&bar[waited % kPlaneRing], (waited / kPlaneRing) & 1, a.err)) ++waited;
+            else ok = false;
+        }
+        if (ok) {
+            const float *sp = sm + (size_t)((qc - 1) % kPlaneRing) * a.slotFloats + base(qc - 1);
+            const float *sc = sm + (size_t)(qc % kPlaneRing) * a.slotFloats + base(qc);
+            const float *sn = sm + (size_t)((qc + 1) % kPlaneRing) * a.slotFloats + base(qc + 1);
+            const float *ss = sm + (size_t)(qc % kPlaneRing) * a.slotFloats + a.nops * kPlaneBox * 4 + side_base(qc);
+            float *out = a.out + (long)(i + 1) * sx + gj;
+#pragma unroll
+            for (int q = 0; q < MAXQ; ++q) {
+                const int p = tid + q * kPlaneThreads;
+                if (p >= npts) continue;
+                const int x = P[q];
+                const float C = sc[x], Wv = sp[x], Ev = sn[x];
+                float N, S, U, D;
+                if (!((edge >> q) & 1u)) {
+                    N = sc[x + sy]; S = sc[x - sy]; U = sc[x + 1]; D = sc[x - 1];
+                } else {
+                    const int row = p / W, col = p - row * W, j = j0 + row;
+                    N = j == E1 ? (per1 ? ss[col + 1] : sc[x - sy]) : sc[x + sy];
+                    S = j == 0 ? (per1 ? ss[col + 1] : sc[x + sy]) : sc[x - sy];
+                    U = col == E2 ? (per2 ? sc[x + 1 - E2] : sc[x - 1]) : sc[x + 1];
+                    D = col == 0 ? (per2 ? sc[x + E2 - 1] : sc[x + 1]) : sc[x - 1];
+                }
+                float v;
+                if (MODE == 0) {
+                    v = fmaf(c.ax, Wv + Ev, fmaf(c.ay, N + S, fmaf(c.az, U + D, fmaf(c.ar, rr[q], c.om1 * C))));
+                } else {
+                    const float lap = fmaf(c.lx, Wv + Ev, fmaf(c.ly, N + S, fmaf(c.lz, U + D, c.lc * C)));
+                    v = rr[q] - lap;
+                }
+                out[x] = v;
+            }
+        }
+        // every thread is done with plane qc - 1's slot: refill it with plane qc - 1 + ring
+        ok = !__syncthreads_or(!ok);
+        if (ok && tid == 0 && issued < nplanes) {
+            fence_async_smem();
+            issue(issued);
+            ++issued;
+        }
+    }
+    if (!ok && tid == 0) {
+        // leave no copy in flight: wait (bounded) for every issued plane not yet seen complete
+        int seen = waited;
+        for (; seen < issued; ++seen) mbar_wait(&bar[seen % kPlaneRing], (seen / kPlaneRing) & 1, nullptr);
+    }
+}
+
 // Full-weighting restriction of a target-mode residual (k_mg_restrict's
 // weights (1/64) [1 2 1]^3, summed separably): one thread per coarse (J, K)
 // column (column launch, k fastest over the coarse plane) marching rr_ch
@@ -1736,6 +1894,110 @@ static bool coarse_solution_operator(int X, int Y, int Z, const double l[3], con
     return true;
 }
 
+// Tensor maps and launch shape of the finest-level plane-streaming kernels
+// (k_tgt_plane_tma).  The level array is viewed as rows of four floats; a
+// main box is kPlaneBox such rows, the side box one padded row (plus the
+// 4-float alignment).  Off (the other kernels run) when a tile would not fit,
+// when the level has fewer than two tiles of rows, or when SARAS_PLANE_TMA=0
+// is set in the environment (a diagnostic switch: both paths compute the same
+// bits).
+// The driver's cuTensorMapEncodeTiled, looked up through the runtime (the
+// library does not link the driver library, so it loads on machines without
+// one and reports SARAS_NO_DEVICE there).
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+static int plane_setup(Ctx &c) {
+    c.planeOk = false;
+    PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+    if (!encode) return SARAS_OK;
+    const char *env = std::getenv("SARAS_PLANE_TMA");
+    if (env && env[0] == '0') return SARAS_OK;
+    Level &L = c.lv[0];
+    const int E0 = L.n[0], E1 = L.n[1], E2 = L.n[2];
+    const int sy = E2 + 3, W = E2 + 1;
+    const int nTiles = (E1 + 1) / kPlaneRows;
+    if (nTiles < 2 || E0 < 2) return SARAS_OK;
+    const int maxRows = (E1 + 1) - kPlaneRows * (nTiles - 1);
+    const int maxq = (maxRows * W + kPlaneThreads - 1) / kPlaneThreads;
+    if (maxq > 19) return SARAS_OK;
+    const long mainChunks = ((long)(maxRows + 2) * sy + 6) / 4;
+    const int nops = (int)((mainChunks + kPlaneBox - 1) / kPlaneBox);
+    const int sideChunks = (sy + 6) / 4;
+    if (sideChunks > 256) return SARAS_OK;
+    int slot = nops * kPlaneBox * 4 + sideChunks * 4;
+    slot = (slot + 31) / 32 * 32;
+    const size_t smem = (size_t)kPlaneRing * slot * sizeof(float);
+    if (smem > 200 * 1024) return SARAS_OK;
+    cuuint64_t dims[2] = {4, (cuuint64_t)(L.count / 4)};
+    cuuint64_t strides[1] = {16};
+    cuuint32_t box[2] = {4, (cuuint32_t)kPlaneBox}, sbox[2] = {4, (cuuint32_t)sideChunks}, es[2] = {1, 1};
+    for (int b = 0; b < 2; ++b) {
+        float *base = b ? L.b32 : L.a32;
+        if (encode(&c.planeMap[b], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, es,
+                                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS ||
+            encode(&c.planeSide[b], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, sbox, es,
+                                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return SARAS_OK;   // the other kernels run
+    }
+    c.planeMaxQ = maxq <= 10 ? 10 : 19;
+    const void *fns[2] = {c.planeMaxQ == 10 ? (const void *)k_tgt_plane_tma<0, 10> : (const void *)k_tgt_plane_tma<0, 19>,
+                          c.planeMaxQ == 10 ? (const void *)k_tgt_plane_tma<1, 10> : (const void *)k_tgt_plane_tma<1, 19>};
+    for (const void *f : fns) SARAS_CUDA_TRY(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // one wave: as many CTAs as fit (shared memory bounds them), tiles x segments of planes
+    int perSM = 0;
+    SARAS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, fns[0], kPlaneThreads, smem));
+    perSM = std::max(1, perSM);
+    const int segs0 = std::max(1, (c.numSMs * perSM) / nTiles);
+    c.planeSegPlanes = (E0 + 1 + segs0 - 1) / segs0;
+    c.planeSegs = (E0 + 1 + c.planeSegPlanes - 1) / c.planeSegPlanes;
+    c.planeOps = nops;
+    c.planeSideFloats = sideChunks * 4;
+    c.planeSlotFloats = slot;
+    c.planeSmem = smem;
+    c.planeOk = true;
+    return SARAS_OK;
+}
+
+// Finest-level FP32 sweep (mode 0) or residual (mode 1) through the plane-streaming kernel.
+static void plane_launch(Ctx &c, int mode, float *out, const float *in, const float *r, const MgBC &bc, const TgK<float> &tk) {
+    Level &L = c.lv[0];
+    PlaneArgs a;
+    a.out = out;
+    a.r = r;
+    a.sy = L.n[2] + 3;
+    a.sx = (L.n[1] + 3) * a.sy;
+    a.bc = bc;
+    a.c = tk;
+    a.nops = c.planeOps;
+    a.sideFloats = c.planeSideFloats;
+    a.slotFloats = c.planeSlotFloats;
+    a.planesPerSeg = c.planeSegPlanes;
+    a.err = c.dflag + 2;
+    const int b = in == L.a32 ? 0 : 1;
+    dim3 g((L.n[1] + 1) / kPlaneRows, c.planeSegs, 1);
+    if (c.planeMaxQ == 10) {
+        if (mode == 0) k_tgt_plane_tma<0, 10><<<g, kPlaneThreads, c.planeSmem, c.stream>>>(c.planeMap[b], c.planeSide[b], a);
+        else k_tgt_plane_tma<1, 10><<<g, kPlaneThreads, c.planeSmem, c.stream>>>(c.planeMap[b], c.planeSide[b], a);
+    } else {
+        if (mode == 0) k_tgt_plane_tma<0, 19><<<g, kPlaneThreads, c.planeSmem, c.stream>>>(c.planeMap[b], c.planeSide[b], a);
+        else k_tgt_plane_tma<1, 19><<<g, kPlaneThreads, c.planeSmem, c.stream>>>(c.planeMap[b], c.planeSide[b], a);
+    }
+}
+
 int mg_setup(Ctx &c) {
     const saras_params &p = c.p;
     c.depth = p.vcDepth;
@@ -1777,7 +2039,8 @@ int mg_setup(Ctx &c) {
     SARAS_CUDA_TRY(cudaFuncSetAttribute(k_mg_coarse<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     SARAS_CUDA_TRY(cudaDeviceGetAttribute(&c.numSMs, cudaDevAttrMultiProcessorCount, c.dev));
     SARAS_CUDA_TRY(cudaFuncSetAttribute(k_mg_gs_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGsBlockSmem));
-    SARAS_CUDA_TRY(cudaMemsetAsync(c.dflag, 0, 2 * sizeof(int), c.stream));
+    SARAS_CUDA_TRY(cudaMemsetAsync(c.dflag, 0, 3 * sizeof(int), c.stream));
+    if (int e = plane_setup(c)) return e;
     c.tailLt = tail_level(c);
     if (c.tailLt > 0) {
         SARAS_CUDA_TRY(cudaFuncSetAttribute(k_mg_tail<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
@@ -1931,7 +2194,10 @@ static int smooth(Ctx &c, int l, int count, bool zero_first, bool tgt) {
         const double lb = (n == 0 && zero_first) ? bytes * 2.0 / 3.0 : bytes;   // a zero start reads no iterate
         if (tgt) {
             if (n == 0 && zero_first) k_tgt_sweep<T, true><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
-            else k_tgt_sweep<T, false><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
+            else if constexpr (sizeof(T) == 4) {
+                if (l == 0 && c.planeOk) plane_launch(c, 0, B_<T>(L), A_<T>(L), R_<T>(L), bc, tk);
+                else k_tgt_sweep<T, false><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
+            } else k_tgt_sweep<T, false><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
         } else if (n == 0 && zero_first)
             k_mg_sweep<T, true><<<g, b, 0, c.stream>>>(lview<T>(L, B_<T>(L)), lcview<T>(L, A_<T>(L)), lcview<T>(L, R_<T>(L)), kk, bc, omega);
         else
@@ -1971,7 +2237,15 @@ static int restrict_level(Ctx &c, int l, bool tgt) {
     if (tgt) {
         int sx = (L.n[1] + 3) * (L.n[2] + 3), sy = L.n[2] + 3;
         dim3 gm, bm; level_dims<T>(L, gm, bm);
-        k_tgt_residual<T, T, false><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bcf, make_tgk<T>(L, 1.0), nullptr);
+        bool planed = false;
+        if constexpr (sizeof(T) == 4) {
+            if (l == 0 && c.planeOk) {
+                plane_launch(c, 1, B_<T>(L), A_<T>(L), R_<T>(L), bcf, make_tgk<T>(L, 1.0));
+                planed = true;
+            }
+        }
+        if (!planed)
+            k_tgt_residual<T, T, false><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bcf, make_tgk<T>(L, 1.0), nullptr);
         count_launch(c);
         prof_end(c, pk, l, 3.0 * sizeof(T) * pts);
         pk = sizeof(T) == 8 ? PK_MG_RESTRICT64 : PK_MG_RESTRICT32;
@@ -2410,10 +2684,12 @@ static int mixed_fixed(Ctx &c, const double *pp0, double mean, double bmax, doub
         int e = chk(c, "fixed-point refinement");
         if (e) return e;
         unsigned long long mx = 0;
-        int fl = 0;
+        int fl = 0, tmaErr = 0;
         SARAS_CUDA_TRY(cudaMemcpyAsync(&mx, dmax, sizeof(mx), cudaMemcpyDeviceToHost, c.stream));
         SARAS_CUDA_TRY(cudaMemcpyAsync(&fl, dflag, sizeof(fl), cudaMemcpyDeviceToHost, c.stream));
+        if (c.planeOk) SARAS_CUDA_TRY(cudaMemcpyAsync(&tmaErr, c.dflag + 2, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
         SARAS_CUDA_TRY(cudaStreamSynchronize(c.stream));
+        if (tmaErr) { c.err = "plane-streaming stencil: an mbarrier wait timed out"; return SARAS_CUDA_ERROR; }
         out = (double)mx * rs;
         bad = fl != 0;
         return SARAS_OK;

@@ -337,3 +337,44 @@ def test_batched_field_transfers_match_single():
     g.upload_fields_ptr(fields, [t.data_ptr() for t in host])
     for f, a in zip(fields, new):
         assert np.array_equal(g.get(f), a)
+
+
+@pytest.mark.parametrize("kind", ["tgv", "ldc", "rbc"])
+def test_plane_streaming_stencils_match_column_kernels(kind):
+    """The finest-level FP32 sweep and residual staged through shared memory by
+    the TMA (k_tgt_plane_tma) compute the same bits as the column kernels
+    (k_tgt_sweep, k_tgt_residual): three mixed-mode steps with each, fields
+    bitwise equal, equal V-cycle counts.  Periodic (TGV), mirror (LDC) and
+    mixed (RBC: PPN) faces; SARAS_PLANE_TMA=0 selects the column kernels."""
+    import os
+    mk = {"tgv": C.tgv, "ldc": C.ldc, "rbc": C.rbc}[kind]
+    out = {}
+    for tma in (True, False):
+        p = mk(ind=(6, 6, 5) if kind == "rbc" else 6, depth=4)
+        p.mgMode = F.MG_MIXED
+        p.mgTarget = 1e-8
+        p.mgMaxCycles = 100
+        p.jacobiWeight = 6.0 / 7.0
+        p.fastKernels = 2
+        p.smoother = F.SMOOTHER_CHEBYSHEV
+        old = os.environ.get("SARAS_PLANE_TMA")
+        if not tma:
+            os.environ["SARAS_PLANE_TMA"] = "0"
+        try:
+            g = S.Solver(p)
+        finally:
+            if old is None:
+                os.environ.pop("SARAS_PLANE_TMA", None)
+            else:
+                os.environ["SARAS_PLANE_TMA"] = old
+        C.initialise(g, p, kind)
+        cyc = []
+        for _ in range(3):
+            s, st = g.time_advance()
+            assert s == 0
+            cyc.append(st.vcycles)
+        out[tma] = (cyc, [g.get(f) for f in (F.FIELD_VX, F.FIELD_VY, F.FIELD_VZ, F.FIELD_P)])
+        g.close()
+    assert out[True][0] == out[False][0]
+    for a, b in zip(out[True][1], out[False][1]):
+        assert np.array_equal(a, b)
