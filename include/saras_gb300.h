@@ -285,6 +285,17 @@ int saras_unet_collect(saras_ctx *ctx);
 int saras_unet_train(saras_ctx *ctx, int iters, double lr, double *loss);
 int saras_unet_infer(saras_ctx *ctx, int field_out);
 int saras_set_guess_mode(saras_ctx *ctx, int mode);
+/* The U-Net's parameter count and finest grid (D, H, W: the voxels of one
+ * sample of features). */
+int saras_unet_shape(saras_ctx *ctx, long long *nparam, int dims[3]);
+/* One forward and backward pass of the U-Net with the training kernels and no
+ * update: features (D*H*W x 3 FP32, channels last), target (D*H*W) and
+ * parameters (nparam FP32 in the layout the training updates; NULL keeps the
+ * current ones) in; the network output d (D*H*W), the loss
+ * 0.5 mean (d - target)^2 and its gradient with respect to every parameter
+ * out (each output may be NULL). */
+int saras_unet_grad_check(saras_ctx *ctx, const float *feat, const float *target, const float *params, float *out,
+                          double *loss, float *grad);
 /* Stand-alone check of the tensor-core 3x3x3 convolution (no context needed).
  * Channels-last BF16 activations (x: D*H*W*cin, dy: D*H*W*cout as raw bf16
  * bits), FP32 weights w[cout][27][cin], bias[cout].  mode 0: forward,

@@ -273,6 +273,28 @@ class Solver:
     def unet_infer(self):
         self._chk(self.lib.saras_unet_infer(self.h, FIELD_PP))
 
+    def unet_shape(self):
+        """(parameter count, (D, H, W) of the network's finest grid)."""
+        n = ctypes.c_longlong()
+        d = (ctypes.c_int * 3)()
+        self._chk(self.lib.saras_unet_shape(self.h, ctypes.byref(n), d))
+        return n.value, tuple(d)
+
+    def unet_grad_check(self, feat, target, params=None):
+        """One forward/backward pass of the U-Net (saras_unet_grad_check): returns
+        (output d, loss, gradient with respect to the parameters)."""
+        nparam, dims = self.unet_shape()
+        nv = dims[0] * dims[1] * dims[2]
+        f = np.ascontiguousarray(feat, dtype=np.float32).reshape(nv, 3)
+        t = np.ascontiguousarray(target, dtype=np.float32).reshape(nv)
+        pp = None if params is None else np.ascontiguousarray(params, dtype=np.float32).reshape(nparam)
+        out = np.empty(nv, dtype=np.float32)
+        grad = np.empty(nparam, dtype=np.float32)
+        loss = ctypes.c_double()
+        self._chk(self.lib.saras_unet_grad_check(self.h, f.ctypes.data, t.ctypes.data, None if pp is None else pp.ctypes.data,
+                                                 out.ctypes.data, ctypes.byref(loss), grad.ctypes.data))
+        return out.reshape(dims), loss.value, grad
+
     def set_guess_mode(self, mode):
         self._chk(self.lib.saras_set_guess_mode(self.h, mode))
 

@@ -172,6 +172,8 @@ def load():
         "saras_unet_train": (_I, [vp, _I, _D, dp]),
         "saras_unet_infer": (_I, [vp, _I]),
         "saras_set_guess_mode": (_I, [vp, _I]),
+        "saras_unet_shape": (_I, [vp, ctypes.POINTER(ctypes.c_longlong), ip]),
+        "saras_unet_grad_check": (_I, [vp, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, dp, ctypes.c_void_p]),
         "saras_conv3d_check": (_I, [_I, _I, _I, _I, _I, _I, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _I,
                                     ctypes.POINTER(ctypes.c_float)]),
         "saras_profile_enable": (_I, [vp, _I, _I]),

@@ -684,6 +684,18 @@ int saras_read_restart(saras_ctx *h, const char *path, double *time) {
     return SARAS_OK;
 }
 
+int saras_unet_shape(saras_ctx *h, long long *nparam, int dims[3]) {
+    CTX_OR_FAIL(h);
+    return unet_shape(h->c, nparam, dims);
+}
+
+int saras_unet_grad_check(saras_ctx *h, const float *feat, const float *target, const float *params, float *out, double *loss,
+                          float *grad) {
+    CTX_OR_FAIL(h);
+    if (!feat || !target) return SARAS_BAD_ARG;
+    return unet_grad_check(h->c, feat, target, params, out, loss, grad);
+}
+
 int saras_compute_tstp(saras_ctx *h, double *dt) {
     CTX_OR_FAIL(h);
     if (!dt) return SARAS_BAD_ARG;

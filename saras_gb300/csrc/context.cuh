@@ -108,8 +108,9 @@ struct Ctx {
     // maps of the two iterate buffers (a32, b32) with the main and the side
     // box, and the launch shape; planeOk false when the level does not fit
     bool planeOk = false;
-    CUtensorMap planeMap[2], planeSide[2];
-    int planeOps = 0, planeSideFloats = 0, planeSlotFloats = 0, planeSegPlanes = 0, planeSegs = 0, planeMaxQ = 0;
+    CUtensorMap planeMap[2], planeSide[2], planeR;
+    int planeMainRows = 0, planeSideRows = 0, planeRRows = 0, planeSideOff = 0, planeROff = 0, planeSlotFloats = 0, planeSegPlanes = 0,
+        planeSegs = 0, planeMaxQ = 0;
     size_t planeSmem = 0;
     double *wallX = nullptr, *wallY = nullptr, *wallZ = nullptr;   // Dirichlet check walls
     // reductions
@@ -208,6 +209,8 @@ void unet_free(Ctx &c);
 int unet_collect(Ctx &c);
 int unet_train(Ctx &c, int iters, double lr, double *loss);
 int unet_infer(Ctx &c, double *out);
+int unet_shape(Ctx &c, long long *nparam, int dims[3]);
+int unet_grad_check(Ctx &c, const float *feat, const float *target, const float *params, float *out, double *loss, float *grad);
 int unet_begin_solve(Ctx &c);
 int unet_guess(Ctx &c, const double *b, double *dst, int mode, long long *fxdst = nullptr, int sc = 0, int *flag = nullptr);
 void vgraph_reset(Ctx &c);

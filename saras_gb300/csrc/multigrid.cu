@@ -1061,42 +1061,51 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 6 : 5) k_tgt_residual(OT
 // k extent (the level's last CTA also its one extra row: rows are 2^m + 1
 // points) and a segment of consecutive i planes.  Rows j0-1 .. j0+R of one
 // plane are one contiguous span of the padded level array, copied as 2D boxes
-// of a tensor map that views the array as rows of four floats: the padded row
-// pitch, 2^m + 3 floats, is no multiple of 16 bytes, which the strides of a
-// 3D tensor map must be.  With the whole k extent in the slot, the periodic
+// of a tensor map that views the array as rows of kPlaneVec floats: the
+// padded row pitch, 2^m + 3 floats, is no multiple of 16 bytes, which the
+// strides of a 3D tensor map must be, and 256-byte box rows keep the copy
+// engine's requests full (boxes of 16-byte rows measured half the bandwidth).  With the whole k extent in the slot, the periodic
 // and mirror images along k are in the slot as well; along j the mirror
 // images are in the tile's halo rows and a periodic image row is one more box
 // (a second tensor map with a one-row box); along i the slot of plane -1 or
-// E+1 holds its image plane.  One thread fills the ring (kPlaneRing slots,
-// each with its mbarrier: planes i-1, i, i+1 and two ahead); every thread
-// computes its points of plane i from three slots, reads r with plain
-// coalesced loads issued a plane ahead and writes its results with plain
-// coalesced stores.  The arithmetic is k_tgt_sweep's / k_tgt_residual's,
+// E+1 holds its image plane.  The right-hand side's rows j0 .. j0+R-1 come in
+// the same slot (a third map).
+//
+// Warp-specialised: one producer warp (its lane 0) issues the copies of plane
+// q into slot q % kPlaneRing once the consumers have released the plane that
+// held the slot (an "empty" mbarrier per slot, one arrival per consumer warp);
+// kPlaneConsumers consumer warps wait on a slot's "full" mbarrier (the
+// copies' transaction count), compute their points of plane i from the slots
+// of planes i-1, i, i+1 and store them with plain coalesced stores.  No
+// CTA-wide barrier inside the loop: each consumer warp runs ahead as far as
+// the data allows.  The arithmetic is k_tgt_sweep's / k_tgt_residual's,
 // operand for operand, so the results are the same bits.
 constexpr int kPlaneRows = 8;
-constexpr int kPlaneRing = 5;
-constexpr int kPlaneBox = 240;      // main box: 240 rows of four floats
-constexpr int kPlaneThreads = 256;
+constexpr int kPlaneRing = 4;
+constexpr int kPlaneVec = 64;       // floats a tensor-map row (256 bytes)
+constexpr int kPlaneConsumers = 8;  // consumer warps
+constexpr int kPlaneThreads = 32 * kPlaneConsumers;
+constexpr int kPlaneBlock = kPlaneThreads + 32;
 
 struct PlaneArgs {
     float *out;
-    const float *r;
     int sx, sy;          // strides of the padded level array, floats
     MgBC bc;
     TgK<float> c;
-    int nops;            // main boxes a plane
-    int sideFloats;      // floats of the side box (its tensor map's box)
-    int slotFloats;      // floats a slot: nops main boxes + the side box, a multiple of 32
+    int mainRows, sideRows, rRows;   // box heights (rows of kPlaneVec floats) of the three maps
+    int sideOff, rOff;   // floats from a slot's start to the side box and the right-hand side's box
+    int slotFloats;      // floats a slot
     int planesPerSeg;
     int *err;            // set when an mbarrier wait gives up
 };
 
 template <int MODE, int MAXQ>
-__global__ void __launch_bounds__(kPlaneThreads, 3)
-    k_tgt_plane_tma(const __grid_constant__ CUtensorMap map, const __grid_constant__ CUtensorMap sideMap, const PlaneArgs a) {
+__global__ void __launch_bounds__(kPlaneBlock, 2)
+    k_tgt_plane_tma(const __grid_constant__ CUtensorMap map, const __grid_constant__ CUtensorMap sideMap,
+                    const __grid_constant__ CUtensorMap rMap, const PlaneArgs a) {
     extern __shared__ __align__(128) float sm[];
-    __shared__ uint64_t bar[kPlaneRing];
-    const int tid = threadIdx.x;
+    __shared__ uint64_t full[kPlaneRing], empty[kPlaneRing];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int E0 = a.bc.E[0], E1 = a.bc.E[1], E2 = a.bc.E[2];
     const int W = E2 + 1, sx = a.sx, sy = a.sy;
     const int nTiles = (E1 + 1) / kPlaneRows;
@@ -1109,32 +1118,53 @@ __global__ void __launch_bounds__(kPlaneThreads, 3)
     const bool per1 = a.bc.per[1] != 0, per2 = a.bc.per[2] != 0;
     const bool side = per1 && (j0 == 0 || j0 + R - 1 == E1);
     const int sideRow = j0 == 0 ? E1 - 1 : 1;   // periodic image of row -1 / E1 + 1
-    const uint32_t tx = (uint32_t)(a.nops * kPlaneBox * 16 + (side ? a.sideFloats * 4 : 0));
+    const int sideOff = a.sideOff, rOff = a.rOff;
+    auto plane_img = [&](int q) { return pad_img(i0 - 1 + q, E0, a.bc.per[0]); };
+    // each span is copied from the kPlaneVec-float boundary at or below its
+    // start: its data sits at this offset in its box
+    auto base = [&](int q) { return (int)((unsigned long)((long)(plane_img(q) + 1) * sx + (long)j0 * sy) & (kPlaneVec - 1)); };
+    auto side_base = [&](int q) { return (int)((unsigned long)((long)(plane_img(q) + 1) * sx + (long)(sideRow + 1) * sy) & (kPlaneVec - 1)); };
+    auto r_base = [&](int q) { return (int)((unsigned long)((long)(plane_img(q) + 1) * sx + (long)(j0 + 1) * sy) & (kPlaneVec - 1)); };
     if (tid == 0) {
-        for (int q = 0; q < kPlaneRing; ++q) mbar_init(&bar[q], 1);
+        for (int q = 0; q < kPlaneRing; ++q) {
+            mbar_init(&full[q], 1);
+            mbar_init(&empty[q], kPlaneConsumers);
+        }
         fence_mbar_init();
     }
     __syncthreads();
-    auto plane_img = [&](int q) { return pad_img(i0 - 1 + q, E0, a.bc.per[0]); };
-    auto issue = [&](int q) {   // plane i0 - 1 + q into slot q % kPlaneRing
-        const int ii = plane_img(q);
-        const long start = (long)(ii + 1) * sx + (long)j0 * sy;   // array row j0: row j0 - 1
-        const int slot = q % kPlaneRing;
-        uint64_t *m = &bar[slot];
-        mbar_arrive_expect_tx(m, tx);
-        const uint32_t dst = su32(sm + (size_t)slot * a.slotFloats);
-        const int c0 = (int)(start >> 2);
-        for (int op = 0; op < a.nops; ++op) tma_load_2d(dst + op * kPlaneBox * 16, &map, 0, c0 + op * kPlaneBox, m);
-        if (side) tma_load_2d(dst + a.nops * kPlaneBox * 16, &sideMap, 0, (int)(((long)(ii + 1) * sx + (long)(sideRow + 1) * sy) >> 2), m);
-    };
-    int issued = 0;
-    if (tid == 0)
-        for (; issued < min(kPlaneRing, nplanes); ++issued) issue(issued);
-    // this thread's points of a plane: p = tid + 256 q over the tile's R x W points
+    if (warp == kPlaneConsumers) {
+        // ---- producer
+        if (lane != 0) return;
+        const uint32_t tx = (uint32_t)((a.mainRows + a.rRows + (side ? a.sideRows : 0)) * kPlaneVec * 4);
+        int q = 0;
+        bool ok = true;
+        for (; q < nplanes && ok; ++q) {
+            const int slot = q % kPlaneRing;
+            if (q >= kPlaneRing && !mbar_wait_sleep(&empty[slot], ((q / kPlaneRing) - 1) & 1, a.err)) { ok = false; break; }
+            const int ii = plane_img(q);
+            uint64_t *m = &full[slot];
+            const uint32_t dst = su32(sm + (size_t)slot * a.slotFloats);
+            // every box lands at a 128-byte aligned address (the layout's
+            // invariant, checked here so that a bad layout reports instead of
+            // issuing a misaligned copy)
+            if (((dst | (uint32_t)(sideOff * 4) | (uint32_t)(rOff * 4)) & 127u) != 0u) {
+                atomicExch(a.err, 2);
+                ok = false;
+                break;
+            }
+            mbar_arrive_expect_tx(m, tx);
+            tma_load_2d(dst, &map, 0, (int)((((long)(ii + 1) * sx + (long)j0 * sy)) / kPlaneVec), m);   // array row j0: row j0 - 1
+            if (side) tma_load_2d(dst + sideOff * 4, &sideMap, 0, (int)(((long)(ii + 1) * sx + (long)(sideRow + 1) * sy) / kPlaneVec), m);
+            tma_load_2d(dst + rOff * 4, &rMap, 0, (int)((((long)(ii + 1) * sx + (long)(j0 + 1) * sy)) / kPlaneVec), m);
+        }
+        // leave no copy in flight: every issued plane's slot complete (bounded) before the CTA may end
+        for (int w = max(0, q - kPlaneRing); w < q; ++w) mbar_wait_sleep(&full[w % kPlaneRing], (w / kPlaneRing) & 1, nullptr);
+        return;
+    }
+    // ---- consumers: this thread's points of a plane, p = tid + 256 q over the tile's R x W points
     const int npts = R * W;
-    // P[q]: the point's index in a slot after the plane's base offset; its
-    // offset in a plane of the level array is P[q] + j0 sy
-    int P[MAXQ];
+    int P[MAXQ];   // the point's index in a slot after the plane's base offset (row 0 of a slot is row j0 - 1)
     unsigned edge = 0u;
 #pragma unroll
     for (int q = 0; q < MAXQ; ++q) {
@@ -1144,66 +1174,51 @@ __global__ void __launch_bounds__(kPlaneThreads, 3)
         if (p < npts && (col == 0 || col == E2 || j0 + row == 0 || j0 + row == E1)) edge |= 1u << q;
     }
     const int gj = j0 * sy;
-    auto base = [&](int q) { return (int)((((long)(plane_img(q) + 1) * sx + (long)j0 * sy)) & 3); };
-    auto side_base = [&](int q) { return (int)((((long)(plane_img(q) + 1) * sx + (long)(sideRow + 1) * sy)) & 3); };
     const TgK<float> &c = a.c;
     bool ok = true;
-    int waited = 0;   // planes whose slot this thread has waited for
+    int waited = 0;   // planes whose full barrier this thread has seen complete
     for (int i = i0; i < i1 && ok; ++i) {
         const int qc = i - i0 + 1;   // plane i is plane qc of the segment
-        // r of plane i first: its loads are in flight while the slots are awaited
-        float rr[MAXQ];
-#pragma unroll
-        for (int q = 0; q < MAXQ; ++q)
-            rr[q] = tid + q * kPlaneThreads < npts ? __ldcs(a.r + (long)(i + 1) * sx + gj + P[q]) : 0.0f;
-        while (ok && waited <= qc + 1) {
-            if (mbar_wait(&bar[waited % kPlaneRing], (waited / kPlaneRing) & 1, a.err)) ++waited;
-            else ok = false;
+        while (waited <= qc + 1) {
+            if (!mbar_wait_sleep(&full[waited % kPlaneRing], (waited / kPlaneRing) & 1, a.err)) { ok = false; break; }
+            ++waited;
         }
-        if (ok) {
-            const float *sp = sm + (size_t)((qc - 1) % kPlaneRing) * a.slotFloats + base(qc - 1);
-            const float *sc = sm + (size_t)(qc % kPlaneRing) * a.slotFloats + base(qc);
-            const float *sn = sm + (size_t)((qc + 1) % kPlaneRing) * a.slotFloats + base(qc + 1);
-            const float *ss = sm + (size_t)(qc % kPlaneRing) * a.slotFloats + a.nops * kPlaneBox * 4 + side_base(qc);
-            float *out = a.out + (long)(i + 1) * sx + gj;
+        if (!ok) break;
+        const float *sp = sm + (size_t)((qc - 1) % kPlaneRing) * a.slotFloats + base(qc - 1);
+        const float *scs = sm + (size_t)(qc % kPlaneRing) * a.slotFloats;
+        const float *sc = scs + base(qc);
+        const float *sn = sm + (size_t)((qc + 1) % kPlaneRing) * a.slotFloats + base(qc + 1);
+        const float *ss = scs + sideOff + side_base(qc);
+        const float *sr = scs + rOff + r_base(qc) - sy;   // P[q] counts rows from j0 - 1
+        float *out = a.out + (long)(i + 1) * sx + gj;
 #pragma unroll
-            for (int q = 0; q < MAXQ; ++q) {
-                const int p = tid + q * kPlaneThreads;
-                if (p >= npts) continue;
-                const int x = P[q];
-                const float C = sc[x], Wv = sp[x], Ev = sn[x];
-                float N, S, U, D;
-                if (!((edge >> q) & 1u)) {
-                    N = sc[x + sy]; S = sc[x - sy]; U = sc[x + 1]; D = sc[x - 1];
-                } else {
-                    const int row = p / W, col = p - row * W, j = j0 + row;
-                    N = j == E1 ? (per1 ? ss[col + 1] : sc[x - sy]) : sc[x + sy];
-                    S = j == 0 ? (per1 ? ss[col + 1] : sc[x + sy]) : sc[x - sy];
-                    U = col == E2 ? (per2 ? sc[x + 1 - E2] : sc[x - 1]) : sc[x + 1];
-                    D = col == 0 ? (per2 ? sc[x + E2 - 1] : sc[x + 1]) : sc[x - 1];
-                }
-                float v;
-                if (MODE == 0) {
-                    v = fmaf(c.ax, Wv + Ev, fmaf(c.ay, N + S, fmaf(c.az, U + D, fmaf(c.ar, rr[q], c.om1 * C))));
-                } else {
-                    const float lap = fmaf(c.lx, Wv + Ev, fmaf(c.ly, N + S, fmaf(c.lz, U + D, c.lc * C)));
-                    v = rr[q] - lap;
-                }
-                out[x] = v;
+        for (int q = 0; q < MAXQ; ++q) {
+            const int p = tid + q * kPlaneThreads;
+            if (p >= npts) continue;
+            const int x = P[q];
+            const float C = sc[x], Wv = sp[x], Ev = sn[x], rv = sr[x];
+            float N, S, U, D;
+            if (!((edge >> q) & 1u)) {
+                N = sc[x + sy]; S = sc[x - sy]; U = sc[x + 1]; D = sc[x - 1];
+            } else {
+                const int row = p / W, col = p - row * W, j = j0 + row;
+                N = j == E1 ? (per1 ? ss[col + 1] : sc[x - sy]) : sc[x + sy];
+                S = j == 0 ? (per1 ? ss[col + 1] : sc[x + sy]) : sc[x - sy];
+                U = col == E2 ? (per2 ? sc[x + 1 - E2] : sc[x - 1]) : sc[x + 1];
+                D = col == 0 ? (per2 ? sc[x + E2 - 1] : sc[x + 1]) : sc[x - 1];
             }
+            float v;
+            if (MODE == 0) {
+                v = fmaf(c.ax, Wv + Ev, fmaf(c.ay, N + S, fmaf(c.az, U + D, fmaf(c.ar, rv, c.om1 * C))));
+            } else {
+                const float lap = fmaf(c.lx, Wv + Ev, fmaf(c.ly, N + S, fmaf(c.lz, U + D, c.lc * C)));
+                v = rv - lap;
+            }
+            out[x] = v;
         }
-        // every thread is done with plane qc - 1's slot: refill it with plane qc - 1 + ring
-        ok = !__syncthreads_or(!ok);
-        if (ok && tid == 0 && issued < nplanes) {
-            fence_async_smem();
-            issue(issued);
-            ++issued;
-        }
-    }
-    if (!ok && tid == 0) {
-        // leave no copy in flight: wait (bounded) for every issued plane not yet seen complete
-        int seen = waited;
-        for (; seen < issued; ++seen) mbar_wait(&bar[seen % kPlaneRing], (seen / kPlaneRing) & 1, nullptr);
+        // plane qc - 1 is read no more by this warp: one arrival of the warp on its slot's empty barrier
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[(qc - 1) % kPlaneRing]);
     }
 }
 
@@ -1895,9 +1910,9 @@ static bool coarse_solution_operator(int X, int Y, int Z, const double l[3], con
 }
 
 // Tensor maps and launch shape of the finest-level plane-streaming kernels
-// (k_tgt_plane_tma).  The level array is viewed as rows of four floats; a
-// main box is kPlaneBox such rows, the side box one padded row (plus the
-// 4-float alignment).  Off (the other kernels run) when a tile would not fit,
+// (k_tgt_plane_tma).  The level array is viewed as rows of kPlaneVec floats;
+// the main box covers a tile's rows j0-1 .. j0+R of a plane, the side box one
+// padded row, the right-hand side's box rows j0 .. j0+R-1.  Off (the other kernels run) when a tile would not fit,
 // when the level has fewer than two tiles of rows, or when SARAS_PLANE_TMA=0
 // is set in the environment (a diagnostic switch: both paths compute the same
 // bits).
@@ -1932,40 +1947,48 @@ static int plane_setup(Ctx &c) {
     const int maxRows = (E1 + 1) - kPlaneRows * (nTiles - 1);
     const int maxq = (maxRows * W + kPlaneThreads - 1) / kPlaneThreads;
     if (maxq > 19) return SARAS_OK;
-    const long mainChunks = ((long)(maxRows + 2) * sy + 6) / 4;
-    const int nops = (int)((mainChunks + kPlaneBox - 1) / kPlaneBox);
-    const int sideChunks = (sy + 6) / 4;
-    if (sideChunks > 256) return SARAS_OK;
-    int slot = nops * kPlaneBox * 4 + sideChunks * 4;
-    slot = (slot + 31) / 32 * 32;
+    // box heights in rows of kPlaneVec floats: a span plus up to kPlaneVec - 1
+    // floats before its start (the copy starts at the boundary below it).
+    // TMA writes shared memory at 128-byte aligned addresses: every box starts
+    // at a multiple of kPlaneVec floats in its slot
+    const long mainRows = ((long)(maxRows + 2) * sy + 2 * kPlaneVec - 2) / kPlaneVec;
+    const long sideRows = ((long)sy + 2 * kPlaneVec - 2) / kPlaneVec;
+    const long rRows = ((long)maxRows * sy + 2 * kPlaneVec - 2) / kPlaneVec;
+    if (mainRows > 256 || sideRows > 256 || rRows > 256) return SARAS_OK;
+    const int sideOff = (int)mainRows * kPlaneVec, rOff = sideOff + (int)sideRows * kPlaneVec;
+    const int slot = rOff + (int)rRows * kPlaneVec;
     const size_t smem = (size_t)kPlaneRing * slot * sizeof(float);
     if (smem > 200 * 1024) return SARAS_OK;
-    cuuint64_t dims[2] = {4, (cuuint64_t)(L.count / 4)};
-    cuuint64_t strides[1] = {16};
-    cuuint32_t box[2] = {4, (cuuint32_t)kPlaneBox}, sbox[2] = {4, (cuuint32_t)sideChunks}, es[2] = {1, 1};
+    cuuint64_t dims[2] = {(cuuint64_t)kPlaneVec, (cuuint64_t)(L.count / kPlaneVec)};
+    cuuint64_t strides[1] = {(cuuint64_t)kPlaneVec * sizeof(float)};
+    cuuint32_t box[2] = {(cuuint32_t)kPlaneVec, (cuuint32_t)mainRows}, sbox[2] = {(cuuint32_t)kPlaneVec, (cuuint32_t)sideRows},
+               rbox[2] = {(cuuint32_t)kPlaneVec, (cuuint32_t)rRows};
+    cuuint32_t es[2] = {1, 1};
+    auto enc = [&](CUtensorMap *m, float *base, const cuuint32_t *bx) {
+        return encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, bx, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                      CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+    };
     for (int b = 0; b < 2; ++b) {
         float *base = b ? L.b32 : L.a32;
-        if (encode(&c.planeMap[b], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, es,
-                                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS ||
-            encode(&c.planeSide[b], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, sbox, es,
-                                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-            return SARAS_OK;   // the other kernels run
+        if (!enc(&c.planeMap[b], base, box) || !enc(&c.planeSide[b], base, sbox)) return SARAS_OK;   // the other kernels run
     }
+    if (!enc(&c.planeR, L.r32, rbox)) return SARAS_OK;
     c.planeMaxQ = maxq <= 10 ? 10 : 19;
     const void *fns[2] = {c.planeMaxQ == 10 ? (const void *)k_tgt_plane_tma<0, 10> : (const void *)k_tgt_plane_tma<0, 19>,
                           c.planeMaxQ == 10 ? (const void *)k_tgt_plane_tma<1, 10> : (const void *)k_tgt_plane_tma<1, 19>};
     for (const void *f : fns) SARAS_CUDA_TRY(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     // one wave: as many CTAs as fit (shared memory bounds them), tiles x segments of planes
     int perSM = 0;
-    SARAS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, fns[0], kPlaneThreads, smem));
+    SARAS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, fns[0], kPlaneBlock, smem));
     perSM = std::max(1, perSM);
     const int segs0 = std::max(1, (c.numSMs * perSM) / nTiles);
     c.planeSegPlanes = (E0 + 1 + segs0 - 1) / segs0;
     c.planeSegs = (E0 + 1 + c.planeSegPlanes - 1) / c.planeSegPlanes;
-    c.planeOps = nops;
-    c.planeSideFloats = sideChunks * 4;
+    c.planeMainRows = (int)mainRows;
+    c.planeSideRows = (int)sideRows;
+    c.planeRRows = (int)rRows;
+    c.planeSideOff = sideOff;
+    c.planeROff = rOff;
     c.planeSlotFloats = slot;
     c.planeSmem = smem;
     c.planeOk = true;
@@ -1975,26 +1998,29 @@ static int plane_setup(Ctx &c) {
 // Finest-level FP32 sweep (mode 0) or residual (mode 1) through the plane-streaming kernel.
 static void plane_launch(Ctx &c, int mode, float *out, const float *in, const float *r, const MgBC &bc, const TgK<float> &tk) {
     Level &L = c.lv[0];
+    (void)r;   // the right-hand side comes through its tensor map (the level's r32)
     PlaneArgs a;
     a.out = out;
-    a.r = r;
     a.sy = L.n[2] + 3;
     a.sx = (L.n[1] + 3) * a.sy;
     a.bc = bc;
     a.c = tk;
-    a.nops = c.planeOps;
-    a.sideFloats = c.planeSideFloats;
+    a.mainRows = c.planeMainRows;
+    a.sideRows = c.planeSideRows;
+    a.rRows = c.planeRRows;
+    a.sideOff = c.planeSideOff;
+    a.rOff = c.planeROff;
     a.slotFloats = c.planeSlotFloats;
     a.planesPerSeg = c.planeSegPlanes;
     a.err = c.dflag + 2;
     const int b = in == L.a32 ? 0 : 1;
     dim3 g((L.n[1] + 1) / kPlaneRows, c.planeSegs, 1);
     if (c.planeMaxQ == 10) {
-        if (mode == 0) k_tgt_plane_tma<0, 10><<<g, kPlaneThreads, c.planeSmem, c.stream>>>(c.planeMap[b], c.planeSide[b], a);
-        else k_tgt_plane_tma<1, 10><<<g, kPlaneThreads, c.planeSmem, c.stream>>>(c.planeMap[b], c.planeSide[b], a);
+        if (mode == 0) k_tgt_plane_tma<0, 10><<<g, kPlaneBlock, c.planeSmem, c.stream>>>(c.planeMap[b], c.planeSide[b], c.planeR, a);
+        else k_tgt_plane_tma<1, 10><<<g, kPlaneBlock, c.planeSmem, c.stream>>>(c.planeMap[b], c.planeSide[b], c.planeR, a);
     } else {
-        if (mode == 0) k_tgt_plane_tma<0, 19><<<g, kPlaneThreads, c.planeSmem, c.stream>>>(c.planeMap[b], c.planeSide[b], a);
-        else k_tgt_plane_tma<1, 19><<<g, kPlaneThreads, c.planeSmem, c.stream>>>(c.planeMap[b], c.planeSide[b], a);
+        if (mode == 0) k_tgt_plane_tma<0, 19><<<g, kPlaneBlock, c.planeSmem, c.stream>>>(c.planeMap[b], c.planeSide[b], c.planeR, a);
+        else k_tgt_plane_tma<1, 19><<<g, kPlaneBlock, c.planeSmem, c.stream>>>(c.planeMap[b], c.planeSide[b], c.planeR, a);
     }
 }
 

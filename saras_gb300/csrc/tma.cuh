@@ -34,6 +34,31 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *m, uint32_t parity, int *err
     if (err) atomicExch(err, 1);
     return false;
 }
+// Bounded wait that lets the thread sleep between polls: each try_wait may
+// suspend the thread for up to kWaitHintNs until the phase completes (the
+// hardware wakes it), so waiting threads do not take issue slots from the
+// ones computing; at most kWaitPolls polls (about a second in all).
+constexpr uint32_t kWaitHintNs = 20000;
+constexpr int kWaitPolls = 50000;
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t *m, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(su32(m)), "r"(parity), "r"(kWaitHintNs)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_sleep(uint64_t *m, uint32_t parity, int *err) {
+    for (int it = 0; it < kWaitPolls; ++it)
+        if (mbar_try_wait_sleep(m, parity)) return true;
+    if (err) atomicExch(err, 1);
+    return false;
+}
+// One plain arrival.
+__device__ __forceinline__ void mbar_arrive(uint64_t *m) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(su32(m)) : "memory");
+}
 // One arrival that also announces `bytes` of asynchronous transactions.
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *m, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(su32(m)), "r"(bytes) : "memory");

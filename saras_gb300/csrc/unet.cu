@@ -1111,6 +1111,51 @@ int unet_train(Ctx &c, int iters, double lr, double *loss) {
     return SARAS_OK;
 }
 
+// The network's parameter count and finest grid (the voxels of one sample).
+int unet_shape(Ctx &c, long long *nparam, int dims[3]) {
+    int s = unet_alloc(c);
+    if (s) return s;
+    UNet *u = U(c);
+    if (nparam) *nparam = u->nparam;
+    if (dims) { dims[0] = u->g[0].D; dims[1] = u->g[0].H; dims[2] = u->g[0].W; }
+    return SARAS_OK;
+}
+
+// One training step's forward and backward pass without the update: the
+// features (nvox x 3, channels last) and target (nvox) of a sample, the
+// parameters (nparam, or null for the current ones) in; the output d (nvox),
+// loss 0.5 mean (d - target)^2 and its gradient with respect to every
+// parameter out.  The kernels are those of unet_train.
+int unet_grad_check(Ctx &c, const float *feat, const float *target, const float *params, float *out, double *loss, float *grad) {
+    int s = unet_alloc(c);
+    if (s) return s;
+    UNet *u = U(c);
+    const long n1 = u->g[0].n();
+    const int nb = (int)((n1 + 255) / 256);
+    if (params) SARAS_CUDA_TRY(cudaMemcpyAsync(u->param, params, sizeof(float) * u->nparam, cudaMemcpyHostToDevice, c.stream));
+    SARAS_CUDA_TRY(cudaMemcpyAsync(u->feat, feat, sizeof(float) * 3 * n1, cudaMemcpyHostToDevice, c.stream));
+    SARAS_CUDA_TRY(cudaMemcpyAsync(u->feat + 3 * n1, target, sizeof(float) * n1, cudaMemcpyHostToDevice, c.stream));
+    SARAS_CUDA_TRY(cudaMemsetAsync(u->err, 0, sizeof(int), c.stream));
+    if ((s = pack_all(c))) return s;
+    k_expand<<<(int)((n1 * 16 + 255) / 256), 256, 0, c.stream>>>(u->feat, u->x0, n1);
+    count_launch(c);
+    if ((s = unet_forward(c))) return s;
+    k_loss<<<nb, 256, 0, c.stream>>>(u->out, u->feat + 3 * n1, u->grd[A_X0], n1, u->part);
+    k_final_reduce<<<1, 256, 0, c.stream>>>(u->part, nb, 0, u->scales + 3);
+    count_launch(c, 2);
+    if ((s = unet_backward(c, u->grd[A_X0]))) return s;
+    double sum = 0.0;
+    int herr = 0;
+    if (out) SARAS_CUDA_TRY(cudaMemcpyAsync(out, u->out, sizeof(float) * n1, cudaMemcpyDeviceToHost, c.stream));
+    if (grad) SARAS_CUDA_TRY(cudaMemcpyAsync(grad, u->grad, sizeof(float) * u->nparam, cudaMemcpyDeviceToHost, c.stream));
+    SARAS_CUDA_TRY(cudaMemcpyAsync(&sum, u->scales + 3, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    SARAS_CUDA_TRY(cudaMemcpyAsync(&herr, u->err, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    SARAS_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    if (herr) { c.err = "tensor-core convolution timed out waiting on an mbarrier"; return SARAS_CUDA_ERROR; }
+    if (loss) *loss = sum / (double)n1;
+    return ucheck(c, "unet grad check");
+}
+
 // The learned guess for the current right-hand side into `out` (history and
 // the level-lb rings as the next solve would see them; no rotation).
 int unet_infer(Ctx &c, double *out) {

@@ -307,14 +307,16 @@ def test_cycle_cap_reports_not_converged():
 
 
 def test_solvepde_ldc_runs_and_stays_bounded():
-    """hydro_d3::solvePDE on the LDC case: energy grows from the lid, divergence stays small."""
+    """hydro_d3::solvePDE on the LDC case: energy grows from the lid, divergence
+    stays small; the series holds the initial state (tseries::writeTSData before
+    the loop, hydro_d3.cc:167) and every fifth step."""
     p = C.ldc(ind=4, depth=2)
     p.tMax = 0.02
     p.ioCnt = 5
     solver = S.hydro_d3(p)
     series = solver.solvePDE()
     assert solver.timeStepCount == 20
-    assert len(series) == 4
+    assert len(series) == 5 and series[0][0] == 0.0
     assert all(0.0 < e < 1.0 for _, e, _, _ in series)
     assert all(abs(d) < 1.0 for _, _, d, _ in series)
 
