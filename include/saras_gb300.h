@@ -66,8 +66,11 @@ enum saras_guess {
     SARAS_GUESS_LEARNED = 1,  /* U-Net guess with fallback to the previous Pp      */
     SARAS_GUESS_EXTRAPOLATE = 2, /* 2 Pp(n-1) - Pp(n-2) with the same fallback (ablation) */
     SARAS_GUESS_QUADRATIC = 3,   /* 3 Pp(n-1) - 3 Pp(n-2) + Pp(n-3), same fallback (ablation) */
-    SARAS_GUESS_PARITY = 4       /* Pp(n-1) + Pp(n-2) - Pp(n-3): exact for a linear trend plus a
+    SARAS_GUESS_PARITY = 4,      /* Pp(n-1) + Pp(n-2) - Pp(n-3): exact for a linear trend plus a
                                     period-2 oscillation, same fallback (ablation) */
+    SARAS_GUESS_NETWORK = 5      /* the U-Net guess in every solve once its histories are
+                                    complete, never the per-solve choice of SARAS_GUESS_LEARNED
+                                    (ablation: what the network alone buys) */
 };
 
 /*

@@ -60,6 +60,7 @@ def _load():
             "orc_tfield_compute_nlin": (I, [vp]),
             "orc_axpby": (I, [vp, I, D, I, D]),
             "orc_cn_solve": (I, [vp, I, ip, dp]),
+            "orc_cn_residual": (I, [vp, I, dp]),
             "orc_mg_solve": (I, [vp, ip, dp]),
             "orc_coarse_iters": (ctypes.c_longlong, [vp]),
             "orc_time_advance": (I, [vp, ctypes.POINTER(saras_step_stats)]),
@@ -160,6 +161,12 @@ class Oracle:
         it, err = ctypes.c_int(), ctypes.c_double()
         s = self.lib.orc_cn_solve(self.h, comp, ctypes.byref(it), ctypes.byref(err))
         return s, it.value, err.value
+
+    def cn_residual(self, comp):
+        """The Crank-Nicolson residual test of the current field (no sweep)."""
+        r = ctypes.c_double()
+        self._chk(self.lib.orc_cn_residual(self.h, comp, ctypes.byref(r)), "cn_residual")
+        return r.value
 
     def mg_solve(self):
         cyc, res = ctypes.c_int(), ctypes.c_double()

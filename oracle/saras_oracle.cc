@@ -1074,6 +1074,26 @@ struct Solver {
         return SARAS_OK;
     }
 
+    // The residual test of the loop above, for the field as it stands: max over
+    // the core of |V - (nu dt / 2) L(V) - rhs| (hydro_d3.cc:392-400).
+    double cnResidual(int c) {
+        Field &f = fieldOf(c);
+        A3 &V = f.F;
+        const A3 &rhs = c == VX ? nseX : c == VY ? nseY : c == VZ ? nseZ : tmpRHS;
+        const A1 *mx, *my, *mz;
+        cnMetrics(c, mx, my, mz);
+        const double coef = (c == TF) ? kappa : nu;
+        double maxError = 0.0;
+        for (int iX = f.blb[0]; iX <= f.bub[0]; iX++) for (int iY = f.blb[1]; iY <= f.bub[1]; iY++) for (int iZ = f.blb[2]; iZ <= f.bub[2]; iZ++) {
+            double L = (*mx)(iX) * (V(iX + 1, iY, iZ) - 2.0 * V(iX, iY, iZ) + V(iX - 1, iY, iZ)) / (hx * hx) +
+                       (*my)(iY) * (V(iX, iY + 1, iZ) - 2.0 * V(iX, iY, iZ) + V(iX, iY - 1, iZ)) / (hy * hy) +
+                       (*mz)(iZ) * (V(iX, iY, iZ + 1) - 2.0 * V(iX, iY, iZ) + V(iX, iY, iZ - 1)) / (hz * hz);
+            double val = isScalar ? V(iX, iY, iZ) - L * 0.5 * dt * coef : V(iX, iY, iZ) - L * 0.5 * dt * inverseRe;
+            maxError = std::max(maxError, std::fabs(val - rhs(iX, iY, iZ)));
+        }
+        return maxError;
+    }
+
     static void axpby(A3 &dst, double a, const A3 *src, double b) {
         if (src) for (size_t n = 0; n < dst.v.size(); ++n) dst.v[n] = a * dst.v[n] + b * src->v[n];
         else for (size_t n = 0; n < dst.v.size(); ++n) dst.v[n] = a * dst.v[n];
@@ -1364,6 +1384,11 @@ int orc_mg_solve(void *h, int *cycles, double *res) {
 }
 long long orc_coarse_iters(void *h) { return ((Handle *)h)->s.mg.coarseIters; }
 int orc_time_advance(void *h, saras_step_stats *st) { return ((Handle *)h)->s.timeAdvance(st); }
+int orc_cn_residual(void *h, int comp, double *res) {
+    if (comp < 0 || comp > 3) return SARAS_BAD_ARG;
+    *res = ((Handle *)h)->s.cnResidual(comp == 3 ? TF : comp);
+    return SARAS_OK;
+}
 int orc_diagnostics(void *h, double *e, double *d, double *nu) { return ((Handle *)h)->s.diagnostics(e, d, nu); }
 int orc_compute_tstp(void *h, double *dt) { ((Handle *)h)->s.computeTStp(*dt); return SARAS_OK; }
 int orc_set_dt(void *h, double dt) { ((Handle *)h)->s.dt = dt; return SARAS_OK; }

@@ -24,7 +24,7 @@ FIELD_NAMES = ["Vx", "Vy", "Vz", "P", "T", "Pp", "mgRHS", "nseRHS.Vx", "nseRHS.V
                "tmpRHS", "pressureGradient.Vx", "pressureGradient.Vy", "pressureGradient.Vz"]
 
 MG_REFERENCE, MG_PLAIN_TARGET, MG_MIXED = 0, 1, 2
-GUESS_PREVIOUS, GUESS_LEARNED, GUESS_EXTRAPOLATE, GUESS_QUADRATIC, GUESS_PARITY = 0, 1, 2, 3, 4
+GUESS_PREVIOUS, GUESS_LEARNED, GUESS_EXTRAPOLATE, GUESS_QUADRATIC, GUESS_PARITY, GUESS_NETWORK = 0, 1, 2, 3, 4, 5
 SMOOTHER_JACOBI, SMOOTHER_CHEBYSHEV = 0, 1
 
 _I, _D = ctypes.c_int, ctypes.c_double

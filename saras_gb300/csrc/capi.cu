@@ -288,7 +288,7 @@ static int validate(const saras_params *p, std::string &why) {
     if (p->probType >= 5 && (p->rbcType < 1 || p->rbcType > 4)) { why = "undefined RBC Type"; return SARAS_BAD_CONFIG; }
     if (p->tStp <= 0 || p->Re <= 0 || p->Lx <= 0 || p->Ly <= 0 || p->Lz <= 0) { why = "non-positive time step, Re or length"; return SARAS_BAD_CONFIG; }
     if (p->mgMode < 0 || p->mgMode > 2) { why = "bad multigrid mode"; return SARAS_BAD_CONFIG; }
-    if (p->guessMode < SARAS_GUESS_PREVIOUS || p->guessMode > SARAS_GUESS_PARITY) { why = "bad guess mode"; return SARAS_BAD_CONFIG; }
+    if (p->guessMode < SARAS_GUESS_PREVIOUS || p->guessMode > SARAS_GUESS_NETWORK) { why = "bad guess mode"; return SARAS_BAD_CONFIG; }
     if (p->fastKernels < 0 || p->fastKernels > 2) { why = "Fast Kernels must be 0, 1 or 2"; return SARAS_BAD_CONFIG; }
     if (p->smoother < 0 || p->smoother > 1) { why = "Smoother must be 0 (Jacobi) or 1 (Chebyshev)"; return SARAS_BAD_CONFIG; }
     if (p->smoother == 1 && (p->preSmooth > 16 || p->postSmooth > 16 || p->coarseSmooth > 16)) {
@@ -749,7 +749,7 @@ int saras_unet_infer(saras_ctx *h, int field_out) {
 }
 int saras_set_guess_mode(saras_ctx *h, int mode) {
     CTX_OR_FAIL(h);
-    if (mode < SARAS_GUESS_PREVIOUS || mode > SARAS_GUESS_PARITY) return SARAS_BAD_ARG;
+    if (mode < SARAS_GUESS_PREVIOUS || mode > SARAS_GUESS_NETWORK) return SARAS_BAD_ARG;
     h->c.guessMode = mode;
     return SARAS_OK;
 }

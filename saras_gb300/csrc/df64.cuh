@@ -121,53 +121,6 @@ __device__ __forceinline__ fpair fp_of(double x) {
     return r;
 }
 
-// ---- two float pairs at once (lane x and lane y), on the packed FP32x2
-// instructions of this GPU (__fadd2_rn, __fmul2_rn, __ffma2_rn: one
-// instruction for both lanes, each lane rounded as the scalar operation).
-// Every function below performs, lane by lane, the scalar function of the
-// same name above in the same order, so it gives the same bits.
-struct fpair2 {
-    float2 h, l;
-};
-__device__ __forceinline__ float2 f2neg(float2 a) { return make_float2(-a.x, -a.y); }
-__device__ __forceinline__ float2 f2add(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 f2sub(float2 a, float2 b) { return __fadd2_rn(a, f2neg(b)); }
-__device__ __forceinline__ float2 f2mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ float2 f2fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ float2 f2splat(float a) { return make_float2(a, a); }
-
-__device__ __forceinline__ void two_sum2(float2 a, float2 b, float2 &s, float2 &t) {
-    s = f2add(a, b);
-    float2 bb = f2sub(s, a);
-    t = f2add(f2sub(a, f2sub(s, bb)), f2sub(b, bb));
-}
-__device__ __forceinline__ fpair2 fp2_norm(float2 s, float2 t) {
-    float2 h = f2add(s, t);
-    return fpair2{h, f2sub(t, f2sub(h, s))};
-}
-__device__ __forceinline__ fpair2 fp2_add(fpair2 a, fpair2 b) {
-    float2 s, t;
-    two_sum2(a.h, b.h, s, t);
-    return fp2_norm(s, f2add(t, f2add(a.l, b.l)));
-}
-__device__ __forceinline__ fpair2 fp2_neg(fpair2 a) { return fpair2{f2neg(a.h), f2neg(a.l)}; }
-__device__ __forceinline__ fpair2 fp2_mul(fpair2 a, fpair2 b) {
-    float2 p = f2mul(a.h, b.h);
-    float2 e = f2fma(a.h, b.h, f2neg(p));
-    e = f2fma(a.h, b.l, f2fma(a.l, b.h, e));
-    return fp2_norm(p, e);
-}
-__device__ __forceinline__ fpair2 fp2_fma(fpair2 a, fpair2 b, fpair2 c) {
-    float2 p = f2mul(a.h, b.h);
-    float2 e = f2fma(a.h, b.h, f2neg(p));
-    float2 s, t;
-    two_sum2(p, c.h, s, t);
-    t = f2add(t, f2add(e, f2fma(a.h, b.l, f2fma(a.l, b.h, c.l))));
-    return fp2_norm(s, t);
-}
-__device__ __forceinline__ fpair2 fp2_splat(fpair a) { return fpair2{f2splat(a.h), f2splat(a.l)}; }
-__device__ __forceinline__ fpair2 fp2_of(fpair x, fpair y) { return fpair2{make_float2(x.h, y.h), make_float2(x.l, y.l)}; }
-
 // |f| < 2^128 and not NaN, from the bits (keeps the check off the FP64 pipe).
 __device__ __forceinline__ bool f_finite(float f) { return (__float_as_uint(f) & 0x7fffffffu) < 0x7f800000u; }
 

@@ -373,17 +373,12 @@ __global__ void __launch_bounds__(256) k_rhs_fast(RhsArgs a, RhsFast q) {
 // over the three components.  Here a CTA owns a 32 (k) x 8 (j) tile of columns
 // and marches kRhs3March planes along i; each plane of Vx, Vy, Vz and P on the
 // tile plus a one-point halo is read once, split once and kept in shared
-// memory, from where the three components' stencils read it.  A thread
-// computes two planes at a time, i in lane x and i + 1 in lane y of the packed
-// FP32x2 instructions (fpair2), which halves the arithmetic instructions of
-// the float pairs; a six-plane ring (i - 1 .. i + 2 in use, the next two
-// loading) keeps one barrier per two planes.  Indices are logical (each field
-// keeps its own core counts and strides); a component is evaluated where
-// (i, j, k) is in its core.
+// memory (four rolling planes, so one barrier a plane), from where the three
+// components' stencils read it.  Indices are logical (each field keeps its own
+// core counts and strides); a component is evaluated where (i, j, k) is in its
+// core.
 constexpr int kRhs3March = 16;
 constexpr int kR3K = 34, kR3N = 10 * kR3K;   // tile (8 x 32) + halo, per field and plane
-constexpr int kR3Ring = 6;
-constexpr size_t kRhs3Smem = sizeof(float2) * kR3Ring * 4 * kR3N;
 
 struct Rhs3K {
     fpair kl[3];   // Laplacian: viscous term and the Jacobi coupling of N0
@@ -404,86 +399,73 @@ struct Rhs3Args {
 };
 
 // p + m - 2 c as an unnormalised pair: two TwoSums of the high parts (exact),
-// the low parts and rounding errors in the second float (both lanes).
-__device__ __forceinline__ fpair2 lap_pair2(fpair2 p, fpair2 m, fpair2 c) {
-    float2 s, e, h, e2;
-    two_sum2(p.h, m.h, s, e);
-    two_sum2(s, f2mul(f2splat(-2.0f), c.h), h, e2);
-    return fpair2{h, f2add(e2, f2add(e, f2sub(f2add(p.l, m.l), f2mul(f2splat(2.0f), c.l))))};
+// the low parts and rounding errors in the second float.
+__device__ __forceinline__ fpair lap_pair(fpair p, fpair m, fpair c) {
+    float s, e, h, e2;
+    two_sum(p.h, m.h, s, e);
+    two_sum(s, -2.0f * c.h, h, e2);
+    return fpair{h, e2 + (e + ((p.l + m.l) - 2.0f * c.l))};
 }
 
 // p - m as an unnormalised pair.
-__device__ __forceinline__ fpair2 sub_pair2(fpair2 p, fpair2 m) {
-    float2 s, e;
-    two_sum2(p.h, f2neg(m.h), s, e);
-    return fpair2{s, f2add(e, f2sub(p.l, m.l))};
+__device__ __forceinline__ fpair sub_pair(fpair p, fpair m) {
+    float s, e;
+    two_sum(p.h, -m.h, s, e);
+    return fpair{s, e + (p.l - m.l)};
 }
 
 // a + b + c + d as an unnormalised pair.
-__device__ __forceinline__ fpair2 sum4_pair2(fpair2 a, fpair2 b, fpair2 c, fpair2 d) {
-    float2 s1, e1, s2, e2, s, e3;
-    two_sum2(a.h, b.h, s1, e1);
-    two_sum2(c.h, d.h, s2, e2);
-    two_sum2(s1, s2, s, e3);
-    return fpair2{s, f2add(f2add(f2add(e1, e2), e3), f2add(f2add(a.l, b.l), f2add(c.l, d.l)))};
+__device__ __forceinline__ fpair sum4_pair(fpair a, fpair b, fpair c, fpair d) {
+    float s1, e1, s2, e2, s, e3;
+    two_sum(a.h, b.h, s1, e1);
+    two_sum(c.h, d.h, s2, e2);
+    two_sum(s1, s2, s, e3);
+    return fpair{s, (e1 + e2 + e3) + ((a.l + b.l) + (c.l + d.l))};
 }
 
-__device__ __forceinline__ int r3slot(int plane) { return (plane + kR3Ring) % kR3Ring; }
-
-// Component C at (i, j, k) in lane x and (i + 1, j, k) in lane y; lane y is
-// stored only when `two` (the segment's last plane can be alone).
 template <int C>
-__device__ __forceinline__ void rhs3_point2(const Rhs3Args &a, const float2 *sm, int i, bool two, int j, int k, int c0) {
-    if (j >= a.n[C][1] || k >= a.n[C][2] || i >= a.n[C][0]) return;
-    auto G = [&](int f, int di, int dj, int dk) -> fpair2 {
-        const float2 u = sm[((size_t)r3slot(i + di) * 4 + f) * kR3N + c0 + dj * kR3K + dk];
-        const float2 v = sm[((size_t)r3slot(i + 1 + di) * 4 + f) * kR3N + c0 + dj * kR3K + dk];
-        return fpair2{make_float2(u.x, v.x), make_float2(u.y, v.y)};
+__device__ __forceinline__ void rhs3_point(const Rhs3Args &a, const float2 (*sm)[4][kR3N], int i, int j, int k, int c0) {
+    if (i >= a.n[C][0] || j >= a.n[C][1] || k >= a.n[C][2]) return;
+    auto G = [&](int f, int di, int dj, int dk) -> fpair {
+        float2 v = sm[(i + di) & 3][f][c0 + dj * kR3K + dk];
+        return fpair{v.x, v.y};
     };
+    const long o = (long)(i + 1) * a.sx[C] + (long)(j + 1) * a.sy[C] + (k + 1);
     const Rhs3K &q = a.q[C];
-    const fpair2 kl0 = fp2_splat(q.kl[0]), kl1 = fp2_splat(q.kl[1]), kl2 = fp2_splat(q.kl[2]);
-    fpair2 c = G(C, 0, 0, 0), ex = G(C, 1, 0, 0), wx = G(C, -1, 0, 0);
-    fpair2 ey = G(C, 0, 1, 0), wy = G(C, 0, -1, 0), ez = G(C, 0, 0, 1), wz = G(C, 0, 0, -1);
-    fpair2 acc = fp2_fma(kl0, lap_pair2(ex, wx, c), fp2_fma(kl1, lap_pair2(ey, wy, c), fp2_mul(kl2, lap_pair2(ez, wz, c))));
-    fpair2 s0, s1, s2, dp;
+    fpair c = G(C, 0, 0, 0), ex = G(C, 1, 0, 0), wx = G(C, -1, 0, 0);
+    fpair ey = G(C, 0, 1, 0), wy = G(C, 0, -1, 0), ez = G(C, 0, 0, 1), wz = G(C, 0, 0, -1);
+    fpair acc = fp_fma(q.kl[0], lap_pair(ex, wx, c), fp_fma(q.kl[1], lap_pair(ey, wy, c), fp_mul(q.kl[2], lap_pair(ez, wz, c))));
+    fpair s0, s1, s2, dp;
     if (C == 0) {
         s0 = c;
-        s1 = sum4_pair2(G(1, 0, 0, 0), G(1, 0, -1, 0), G(1, 1, 0, 0), G(1, 1, -1, 0));
-        s2 = sum4_pair2(G(2, 0, 0, 0), G(2, 0, 0, -1), G(2, 1, 0, 0), G(2, 1, 0, -1));
-        dp = sub_pair2(G(3, 1, 0, 0), G(3, 0, 0, 0));
+        s1 = sum4_pair(G(1, 0, 0, 0), G(1, 0, -1, 0), G(1, 1, 0, 0), G(1, 1, -1, 0));
+        s2 = sum4_pair(G(2, 0, 0, 0), G(2, 0, 0, -1), G(2, 1, 0, 0), G(2, 1, 0, -1));
+        dp = sub_pair(G(3, 1, 0, 0), G(3, 0, 0, 0));
     } else if (C == 1) {
-        s0 = sum4_pair2(G(0, 0, 0, 0), G(0, 0, 1, 0), G(0, -1, 0, 0), G(0, -1, 1, 0));
+        s0 = sum4_pair(G(0, 0, 0, 0), G(0, 0, 1, 0), G(0, -1, 0, 0), G(0, -1, 1, 0));
         s1 = c;
-        s2 = sum4_pair2(G(2, 0, 0, 0), G(2, 0, 0, -1), G(2, 0, 1, 0), G(2, 0, 1, -1));
-        dp = sub_pair2(G(3, 0, 1, 0), G(3, 0, 0, 0));
+        s2 = sum4_pair(G(2, 0, 0, 0), G(2, 0, 0, -1), G(2, 0, 1, 0), G(2, 0, 1, -1));
+        dp = sub_pair(G(3, 0, 1, 0), G(3, 0, 0, 0));
     } else {
-        s0 = sum4_pair2(G(0, 0, 0, 0), G(0, 0, 0, 1), G(0, -1, 0, 0), G(0, -1, 0, 1));
-        s1 = sum4_pair2(G(1, 0, 0, 0), G(1, 0, -1, 0), G(1, 0, 0, 1), G(1, 0, -1, 1));
+        s0 = sum4_pair(G(0, 0, 0, 0), G(0, 0, 0, 1), G(0, -1, 0, 0), G(0, -1, 0, 1));
+        s1 = sum4_pair(G(1, 0, 0, 0), G(1, 0, -1, 0), G(1, 0, 0, 1), G(1, 0, -1, 1));
         s2 = c;
-        dp = sub_pair2(G(3, 0, 0, 1), G(3, 0, 0, 0));
+        dp = sub_pair(G(3, 0, 0, 1), G(3, 0, 0, 0));
     }
-    acc = fp2_fma(fp2_neg(fp2_splat(q.kn[0])), fp2_mul(s0, sub_pair2(ex, wx)), acc);
-    acc = fp2_fma(fp2_neg(fp2_splat(q.kn[1])), fp2_mul(s1, sub_pair2(ey, wy)), acc);
-    acc = fp2_fma(fp2_neg(fp2_splat(q.kn[2])), fp2_mul(s2, sub_pair2(ez, wz)), acc);
-    const bool st2 = two && i + 1 < a.n[C][0];
+    acc = fp_fma(fp_neg(q.kn[0]), fp_mul(s0, sub_pair(ex, wx)), acc);
+    acc = fp_fma(fp_neg(q.kn[1]), fp_mul(s1, sub_pair(ey, wy)), acc);
+    acc = fp_fma(fp_neg(q.kn[2]), fp_mul(s2, sub_pair(ez, wz)), acc);
     if (C == 2 && a.buoyancy) {
-        const long ot = (long)(i + 1) * a.sx[3] + (long)(j + 1) * a.sy[3] + (k + 1);
-        const long ot2 = st2 ? ot + a.sx[3] : ot;
-        acc = fp2_fma(fp2_splat(q.kb), fp2_add(fp2_of(fp_of(a.T[ot]), fp_of(a.T[ot2])), fp2_of(fp_of(a.T[ot + 1]), fp_of(a.T[ot2 + 1]))),
-                      acc);
+        long ot = (long)(i + 1) * a.sx[3] + (long)(j + 1) * a.sy[3] + (k + 1);
+        acc = fp_fma(q.kb, fp_add(fp_of(a.T[ot]), fp_of(a.T[ot + 1])), acc);
     }
-    acc = fp2_fma(fp2_neg(fp2_splat(q.kg)), dp, acc);
-    const long o = (long)(i + 1) * a.sx[C] + (long)(j + 1) * a.sy[C] + (k + 1);
-    a.n0h[C][o] = acc.h.x;
-    a.n0l[C][o] = acc.l.x;
-    if (st2) {
-        a.n0h[C][o + a.sx[C]] = acc.h.y;
-        a.n0l[C][o + a.sx[C]] = acc.l.y;
-    }
+    acc = fp_fma(fp_neg(q.kg), dp, acc);
+    a.n0h[C][o] = acc.h;
+    a.n0l[C][o] = acc.l;
 }
 
-__global__ void __launch_bounds__(256, 2) k_rhs_df3(Rhs3Args a) {
-    extern __shared__ float2 sm[];   // [kR3Ring][4][kR3N]
+__global__ void __launch_bounds__(256, 5) k_rhs_df3(Rhs3Args a) {
+    __shared__ float2 sm[4][4][kR3N];
     const int tid = threadIdx.y * 32 + threadIdx.x;
     const int k0 = blockIdx.x * 32, j0 = blockIdx.y * 8, i0 = blockIdx.z * kRhs3March;
     const int iend = min(i0 + kRhs3March, a.nu[0]);
@@ -498,7 +480,7 @@ __global__ void __launch_bounds__(256, 2) k_rhs_df3(Rhs3Args a) {
         lt[s] = t < kR3N;
     }
     auto load_plane = [&](int ip) {
-        float2 *slot = sm + (size_t)r3slot(ip) * 4 * kR3N;
+        float2(*slot)[kR3N] = sm[ip & 3];
 #pragma unroll
         for (int s = 0; s < 2; ++s) {
             if (!lt[s]) continue;
@@ -507,7 +489,7 @@ __global__ void __launch_bounds__(256, 2) k_rhs_df3(Rhs3Args a) {
             for (int f = 0; f < 4; ++f) {
                 if (ip > a.n[f][0] || j > a.n[f][1] || k > a.n[f][2]) continue;   // outside the padded field
                 fpair x = fp_of(a.f[f][(long)(ip + 1) * a.sx[f] + (long)(j + 1) * a.sy[f] + (k + 1)]);
-                slot[f * kR3N + t] = make_float2(x.h, x.l);
+                slot[f][t] = make_float2(x.h, x.l);
             }
         }
     };
@@ -515,14 +497,12 @@ __global__ void __launch_bounds__(256, 2) k_rhs_df3(Rhs3Args a) {
     load_plane(i0);
     const int j = j0 + threadIdx.y, k = k0 + threadIdx.x;
     const int c0 = (threadIdx.y + 1) * kR3K + (threadIdx.x + 1);
-    for (int i = i0; i < iend; i += 2) {
+    for (int i = i0; i < iend; ++i) {
         load_plane(i + 1);
-        load_plane(i + 2);
         __syncthreads();
-        const bool two = i + 1 < iend;
-        rhs3_point2<0>(a, sm, i, two, j, k, c0);
-        rhs3_point2<1>(a, sm, i, two, j, k, c0);
-        rhs3_point2<2>(a, sm, i, two, j, k, c0);
+        rhs3_point<0>(a, sm, i, j, k, c0);
+        rhs3_point<1>(a, sm, i, j, k, c0);
+        rhs3_point<2>(a, sm, i, j, k, c0);
     }
 }
 
@@ -1247,7 +1227,6 @@ int fields_setup(Ctx &c) {
     }
     c.redCap = 1 << 16;
     SARAS_CUDA_TRY(cudaMalloc(&c.red, sizeof(double) * c.redCap * 3));
-    SARAS_CUDA_TRY(cudaFuncSetAttribute(k_rhs_df3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRhs3Smem));
     SARAS_CUDA_TRY(cudaMalloc(&c.dscal, sizeof(double) * 64));
     SARAS_CUDA_TRY(cudaMalloc(&c.dflag, sizeof(int) * 16));
     SARAS_CUDA_TRY(cudaMallocHost(&c.hscal, sizeof(double) * 64));
@@ -1514,7 +1493,7 @@ int compute_rhs(Ctx &c) {
                 for (int d = 0; d < 3; ++d) a3.nu[d] = std::max(std::max(a3.n[0][d], a3.n[1][d]), std::max(a3.n[2][d], a3.n[3][d]));
                 a3.buoyancy = a.buoyancy;
                 dim3 gr((a3.nu[2] + 31) / 32, (a3.nu[1] + 7) / 8, (a3.nu[0] + kRhs3March - 1) / kRhs3March);
-                k_rhs_df3<<<gr, dim3(32, 8, 1), kRhs3Smem, c.stream>>>(a3);
+                k_rhs_df3<<<gr, dim3(32, 8, 1), 0, c.stream>>>(a3);
                 count_launch(c);
                 break;
             }

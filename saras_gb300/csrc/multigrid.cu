@@ -1056,56 +1056,54 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 6 : 5) k_tgt_residual(OT
 // ---- finest-level FP32 stencils staged through shared memory by the TMA
 // The target-mode FP32 Jacobi sweep and residual of the finest level (the
 // inner V-cycles of the mixed mode spend most of their HBM traffic there)
-// stream x planes through a ring of shared-memory slots that the Tensor Memory
-// Accelerator fills.  A CTA owns kPlaneRows consecutive j rows over the whole
-// k extent (the level's last CTA also its one extra row: rows are 2^m + 1
-// points) and a segment of consecutive i planes.  Rows j0-1 .. j0+R of one
-// plane are one contiguous span of the padded level array, copied as 2D boxes
-// of a tensor map that views the array as rows of kPlaneVec floats: the
-// padded row pitch, 2^m + 3 floats, is no multiple of 16 bytes, which the
-// strides of a 3D tensor map must be, and 256-byte box rows keep the copy
-// engine's requests full (boxes of 16-byte rows measured half the bandwidth).  With the whole k extent in the slot, the periodic
-// and mirror images along k are in the slot as well; along j the mirror
-// images are in the tile's halo rows and a periodic image row is one more box
-// (a second tensor map with a one-row box); along i the slot of plane -1 or
-// E+1 holds its image plane.  The right-hand side's rows j0 .. j0+R-1 come in
-// the same slot (a third map).
+// stream x planes of the iterate through a ring of shared-memory slots that
+// the Tensor Memory Accelerator fills.  A CTA owns kPlaneRows consecutive j
+// rows over the whole k extent (the level's last CTA also its one extra row:
+// rows are 2^m + 1 points) and a segment of consecutive i planes.  Rows
+// j0-1 .. j0+R of one plane are one contiguous span of the padded level
+// array, copied as a 2D box of a tensor map that views the array as rows of
+// kPlaneVec floats: the padded row pitch, 2^m + 3 floats, is no multiple of
+// 16 bytes, which the strides of a 3D tensor map must be, and 256-byte box
+// rows keep the copy engine's requests full.  With the whole k extent in the
+// slot, the periodic and mirror images along k are in the slot as well; along
+// j the mirror images are in the tile's halo rows and a periodic image row is
+// one more box (a second tensor map with a one-row box); along i the slot of
+// plane -1 or E+1 holds its image plane.
 //
-// Warp-specialised: one producer warp (its lane 0) issues the copies of plane
-// q into slot q % kPlaneRing once the consumers have released the plane that
-// held the slot (an "empty" mbarrier per slot, one arrival per consumer warp);
-// kPlaneConsumers consumer warps wait on a slot's "full" mbarrier (the
-// copies' transaction count), compute their points of plane i from the slots
-// of planes i-1, i, i+1 and store them with plain coalesced stores.  No
-// CTA-wide barrier inside the loop: each consumer warp runs ahead as far as
-// the data allows.  The arithmetic is k_tgt_sweep's / k_tgt_residual's,
-// operand for operand, so the results are the same bits.
+// The iterate is the operand with reuse (seven reads a point); the right-hand
+// side is read once a point, so it bypasses shared memory: each thread loads
+// its points of the next plane's right-hand side into registers while it
+// computes the current plane.  Every thread computes; thread 0 also issues
+// the copies.  Plane q goes to slot q % kPlaneRing; after plane i is done
+// (one CTA barrier a plane), the slot of plane i - 1 is free and thread 0
+// refills it with plane i - 1 + kPlaneRing, so each copy has three planes'
+// compute time to land, and the two CTAs an SM keep several planes of copies
+// in flight.  The arithmetic is k_tgt_sweep's / k_tgt_residual's, operand for
+// operand, so the results are the same bits.
 constexpr int kPlaneRows = 8;
-constexpr int kPlaneRing = 4;
-constexpr int kPlaneVec = 64;       // floats a tensor-map row (256 bytes)
-constexpr int kPlaneConsumers = 8;  // consumer warps
-constexpr int kPlaneThreads = 32 * kPlaneConsumers;
-constexpr int kPlaneBlock = kPlaneThreads + 32;
+constexpr int kPlaneRing = 5;
+constexpr int kPlaneVec = 64;        // floats a tensor-map row (256 bytes)
+constexpr int kPlaneThreads = 512;
 
 struct PlaneArgs {
     float *out;
+    const float *r;      // right-hand side (residual mode: the level's b; sweep: its r)
     int sx, sy;          // strides of the padded level array, floats
     MgBC bc;
     TgK<float> c;
-    int mainRows, sideRows, rRows;   // box heights (rows of kPlaneVec floats) of the three maps
-    int sideOff, rOff;   // floats from a slot's start to the side box and the right-hand side's box
+    int mainRows, sideRows;   // box heights (rows of kPlaneVec floats) of the two maps
+    int sideOff;         // floats from a slot's start to the side box
     int slotFloats;      // floats a slot
     int planesPerSeg;
-    int *err;            // set when an mbarrier wait gives up
+    int *err;            // set when an mbarrier wait gives up (1) or the layout is misaligned (2)
 };
 
 template <int MODE, int MAXQ>
-__global__ void __launch_bounds__(kPlaneBlock, 2)
-    k_tgt_plane_tma(const __grid_constant__ CUtensorMap map, const __grid_constant__ CUtensorMap sideMap,
-                    const __grid_constant__ CUtensorMap rMap, const PlaneArgs a) {
-    extern __shared__ __align__(128) float sm[];
-    __shared__ uint64_t full[kPlaneRing], empty[kPlaneRing];
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+__global__ void __launch_bounds__(kPlaneThreads, MAXQ <= 5 ? 2 : 1)
+    k_tgt_plane_tma(const __grid_constant__ CUtensorMap map, const __grid_constant__ CUtensorMap sideMap, const PlaneArgs a) {
+    extern __shared__ __align__(128) float plane_sm[];
+    __shared__ uint64_t full[kPlaneRing];
+    const int tid = threadIdx.x;
     const int E0 = a.bc.E[0], E1 = a.bc.E[1], E2 = a.bc.E[2];
     const int W = E2 + 1, sx = a.sx, sy = a.sy;
     const int nTiles = (E1 + 1) / kPlaneRows;
@@ -1118,89 +1116,91 @@ __global__ void __launch_bounds__(kPlaneBlock, 2)
     const bool per1 = a.bc.per[1] != 0, per2 = a.bc.per[2] != 0;
     const bool side = per1 && (j0 == 0 || j0 + R - 1 == E1);
     const int sideRow = j0 == 0 ? E1 - 1 : 1;   // periodic image of row -1 / E1 + 1
-    const int sideOff = a.sideOff, rOff = a.rOff;
+    const int sideOff = a.sideOff;
+    // slots start at the first 128-byte boundary of the dynamic shared memory
+    // (the launch reserves 128 bytes more than the ring)
+    float *sm = plane_sm + (((128u - (su32(plane_sm) & 127u)) & 127u) >> 2);
     auto plane_img = [&](int q) { return pad_img(i0 - 1 + q, E0, a.bc.per[0]); };
     // each span is copied from the kPlaneVec-float boundary at or below its
     // start: its data sits at this offset in its box
     auto base = [&](int q) { return (int)((unsigned long)((long)(plane_img(q) + 1) * sx + (long)j0 * sy) & (kPlaneVec - 1)); };
     auto side_base = [&](int q) { return (int)((unsigned long)((long)(plane_img(q) + 1) * sx + (long)(sideRow + 1) * sy) & (kPlaneVec - 1)); };
-    auto r_base = [&](int q) { return (int)((unsigned long)((long)(plane_img(q) + 1) * sx + (long)(j0 + 1) * sy) & (kPlaneVec - 1)); };
+    const uint32_t tx = (uint32_t)((a.mainRows + (side ? a.sideRows : 0)) * kPlaneVec * 4);
+    int issued = 0;   // thread 0: planes whose copies are issued
+    auto issue = [&](int q) {
+        const int slot = q % kPlaneRing, ii = plane_img(q);
+        uint64_t *m = &full[slot];
+        const uint32_t dst = su32(sm + (size_t)slot * a.slotFloats);
+        mbar_arrive_expect_tx(m, tx);
+        tma_load_2d(dst, &map, 0, (int)(((long)(ii + 1) * sx + (long)j0 * sy) / kPlaneVec), m);   // array row j0: row j0 - 1
+        if (side) tma_load_2d(dst + sideOff * 4, &sideMap, 0, (int)(((long)(ii + 1) * sx + (long)(sideRow + 1) * sy) / kPlaneVec), m);
+        issued = q + 1;
+    };
+    bool ok = true;
     if (tid == 0) {
-        for (int q = 0; q < kPlaneRing; ++q) {
-            mbar_init(&full[q], 1);
-            mbar_init(&empty[q], kPlaneConsumers);
+        // every box lands at a 128-byte aligned address (the layout's
+        // invariant, checked so that a bad layout reports instead of issuing
+        // a misaligned copy)
+        if (((su32(sm) | (uint32_t)(a.slotFloats * 4) | (uint32_t)(sideOff * 4)) & 127u) != 0u) {
+            atomicExch(a.err, 2);
+            ok = false;
         }
+        for (int q = 0; q < kPlaneRing; ++q) mbar_init(&full[q], 1);
         fence_mbar_init();
-    }
-    __syncthreads();
-    if (warp == kPlaneConsumers) {
-        // ---- producer
-        if (lane != 0) return;
-        const uint32_t tx = (uint32_t)((a.mainRows + a.rRows + (side ? a.sideRows : 0)) * kPlaneVec * 4);
-        int q = 0;
-        bool ok = true;
-        for (; q < nplanes && ok; ++q) {
-            const int slot = q % kPlaneRing;
-            if (q >= kPlaneRing && !mbar_wait_sleep(&empty[slot], ((q / kPlaneRing) - 1) & 1, a.err)) { ok = false; break; }
-            const int ii = plane_img(q);
-            uint64_t *m = &full[slot];
-            const uint32_t dst = su32(sm + (size_t)slot * a.slotFloats);
-            // every box lands at a 128-byte aligned address (the layout's
-            // invariant, checked here so that a bad layout reports instead of
-            // issuing a misaligned copy)
-            if (((dst | (uint32_t)(sideOff * 4) | (uint32_t)(rOff * 4)) & 127u) != 0u) {
-                atomicExch(a.err, 2);
-                ok = false;
-                break;
-            }
-            mbar_arrive_expect_tx(m, tx);
-            tma_load_2d(dst, &map, 0, (int)((((long)(ii + 1) * sx + (long)j0 * sy)) / kPlaneVec), m);   // array row j0: row j0 - 1
-            if (side) tma_load_2d(dst + sideOff * 4, &sideMap, 0, (int)(((long)(ii + 1) * sx + (long)(sideRow + 1) * sy) / kPlaneVec), m);
-            tma_load_2d(dst + rOff * 4, &rMap, 0, (int)((((long)(ii + 1) * sx + (long)(j0 + 1) * sy)) / kPlaneVec), m);
+        if (ok) {
+            for (int q = 0; q < kPlaneRing && q < nplanes; ++q) issue(q);
+            for (int q = 0; q < 3 && ok; ++q) ok = mbar_wait(&full[q], 0, a.err);   // planes i0-1, i0, i0+1
         }
-        // leave no copy in flight: every issued plane's slot complete (bounded) before the CTA may end
-        for (int w = max(0, q - kPlaneRing); w < q; ++w) mbar_wait_sleep(&full[w % kPlaneRing], (w / kPlaneRing) & 1, nullptr);
+    }
+    if (__syncthreads_or(!ok)) {
+        if (tid == 0)   // leave no copy in flight (bounded)
+            for (int w = 0; w < issued; ++w) mbar_wait(&full[w % kPlaneRing], (w / kPlaneRing) & 1, nullptr);
         return;
     }
-    // ---- consumers: this thread's points of a plane, p = tid + 256 q over the tile's R x W points
+    // this thread's points of a plane, p = tid + 512 q over the tile's R x W points
     const int npts = R * W;
     int P[MAXQ];   // the point's index in a slot after the plane's base offset (row 0 of a slot is row j0 - 1)
-    unsigned edge = 0u;
+    unsigned edge = 0u, live = 0u;
 #pragma unroll
     for (int q = 0; q < MAXQ; ++q) {
         const int p = tid + q * kPlaneThreads;
         const int row = p / W, col = p - row * W;
         P[q] = (row + 1) * sy + col + 1;
+        if (p < npts) live |= 1u << q;
         if (p < npts && (col == 0 || col == E2 || j0 + row == 0 || j0 + row == E1)) edge |= 1u << q;
     }
     const int gj = j0 * sy;
     const TgK<float> &c = a.c;
-    bool ok = true;
-    int waited = 0;   // planes whose full barrier this thread has seen complete
-    for (int i = i0; i < i1 && ok; ++i) {
+    // right-hand side of plane i at this thread's points (P[q] counts rows from j0 - 1)
+    float rv[MAXQ], rn[MAXQ];
+    {
+        const float *rp = a.r + (long)(i0 + 1) * sx + gj;
+#pragma unroll
+        for (int q = 0; q < MAXQ; ++q) rv[q] = (live >> q) & 1u ? __ldg(rp + P[q]) : 0.0f;
+    }
+    // slot pointers (after each plane's base offset) of planes qc - 1, qc, qc + 1, rolled along
+    const float *sp = sm + base(0), *sc = sm + (size_t)a.slotFloats + base(1), *sn = sm + (size_t)2 * a.slotFloats + base(2);
+    int slotC = 1;
+    for (int i = i0; i < i1; ++i) {
         const int qc = i - i0 + 1;   // plane i is plane qc of the segment
-        while (waited <= qc + 1) {
-            if (!mbar_wait_sleep(&full[waited % kPlaneRing], (waited / kPlaneRing) & 1, a.err)) { ok = false; break; }
-            ++waited;
+        {
+            const float *rp = a.r + (long)(i + 2) * sx + gj;
+            const bool more = i + 1 < i1;
+#pragma unroll
+            for (int q = 0; q < MAXQ; ++q) rn[q] = more && ((live >> q) & 1u) ? __ldg(rp + P[q]) : 0.0f;
         }
-        if (!ok) break;
-        const float *sp = sm + (size_t)((qc - 1) % kPlaneRing) * a.slotFloats + base(qc - 1);
-        const float *scs = sm + (size_t)(qc % kPlaneRing) * a.slotFloats;
-        const float *sc = scs + base(qc);
-        const float *sn = sm + (size_t)((qc + 1) % kPlaneRing) * a.slotFloats + base(qc + 1);
-        const float *ss = scs + sideOff + side_base(qc);
-        const float *sr = scs + rOff + r_base(qc) - sy;   // P[q] counts rows from j0 - 1
+        const float *ss = side ? sm + (size_t)slotC * a.slotFloats + sideOff + side_base(qc) : sm;
         float *out = a.out + (long)(i + 1) * sx + gj;
 #pragma unroll
         for (int q = 0; q < MAXQ; ++q) {
-            const int p = tid + q * kPlaneThreads;
-            if (p >= npts) continue;
+            if (!((live >> q) & 1u)) continue;
             const int x = P[q];
-            const float C = sc[x], Wv = sp[x], Ev = sn[x], rv = sr[x];
+            const float C = sc[x], Wv = sp[x], Ev = sn[x];
             float N, S, U, D;
             if (!((edge >> q) & 1u)) {
                 N = sc[x + sy]; S = sc[x - sy]; U = sc[x + 1]; D = sc[x - 1];
             } else {
+                const int p = tid + q * kPlaneThreads;
                 const int row = p / W, col = p - row * W, j = j0 + row;
                 N = j == E1 ? (per1 ? ss[col + 1] : sc[x - sy]) : sc[x + sy];
                 S = j == 0 ? (per1 ? ss[col + 1] : sc[x + sy]) : sc[x - sy];
@@ -1209,17 +1209,33 @@ __global__ void __launch_bounds__(kPlaneBlock, 2)
             }
             float v;
             if (MODE == 0) {
-                v = fmaf(c.ax, Wv + Ev, fmaf(c.ay, N + S, fmaf(c.az, U + D, fmaf(c.ar, rv, c.om1 * C))));
+                v = fmaf(c.ax, Wv + Ev, fmaf(c.ay, N + S, fmaf(c.az, U + D, fmaf(c.ar, rv[q], c.om1 * C))));
             } else {
                 const float lap = fmaf(c.lx, Wv + Ev, fmaf(c.ly, N + S, fmaf(c.lz, U + D, c.lc * C)));
-                v = rv - lap;
+                v = rv[q] - lap;
             }
             out[x] = v;
         }
-        // plane qc - 1 is read no more by this warp: one arrival of the warp on its slot's empty barrier
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&empty[(qc - 1) % kPlaneRing]);
+        // one barrier a plane: every thread is done with plane qc - 1 (its slot
+        // takes plane qc - 1 + kPlaneRing), and thread 0 has seen plane qc + 2,
+        // which the next plane reads, land
+        if (tid == 0 && qc + 2 < nplanes) ok = mbar_wait(&full[(qc + 2) % kPlaneRing], ((qc + 2) / kPlaneRing) & 1, a.err);
+        if (__syncthreads_or(!ok)) break;
+        if (tid == 0 && qc - 1 + kPlaneRing < nplanes) {
+            fence_async_smem();
+            issue(qc - 1 + kPlaneRing);
+        }
+        slotC = slotC + 1 == kPlaneRing ? 0 : slotC + 1;
+        const int slotN = slotC + 1 == kPlaneRing ? 0 : slotC + 1;
+        sp = sc;
+        sc = sn;
+        sn = sm + (size_t)slotN * a.slotFloats + (qc + 2 < nplanes ? base(qc + 2) : 0);
+#pragma unroll
+        for (int q = 0; q < MAXQ; ++q) rv[q] = rn[q];
     }
+    // leave no copy in flight: every issued plane's slot complete (bounded) before the CTA ends
+    if (tid == 0)
+        for (int w = max(0, issued - kPlaneRing); w < issued; ++w) mbar_wait(&full[w % kPlaneRing], (w / kPlaneRing) & 1, nullptr);
 }
 
 // Full-weighting restriction of a target-mode residual (k_mg_restrict's
@@ -1912,7 +1928,7 @@ static bool coarse_solution_operator(int X, int Y, int Z, const double l[3], con
 // Tensor maps and launch shape of the finest-level plane-streaming kernels
 // (k_tgt_plane_tma).  The level array is viewed as rows of kPlaneVec floats;
 // the main box covers a tile's rows j0-1 .. j0+R of a plane, the side box one
-// padded row, the right-hand side's box rows j0 .. j0+R-1.  Off (the other kernels run) when a tile would not fit,
+// padded row.  Off (the other kernels run) when a tile would not fit,
 // when the level has fewer than two tiles of rows, or when SARAS_PLANE_TMA=0
 // is set in the environment (a diagnostic switch: both paths compute the same
 // bits).
@@ -1946,23 +1962,21 @@ static int plane_setup(Ctx &c) {
     if (nTiles < 2 || E0 < 2) return SARAS_OK;
     const int maxRows = (E1 + 1) - kPlaneRows * (nTiles - 1);
     const int maxq = (maxRows * W + kPlaneThreads - 1) / kPlaneThreads;
-    if (maxq > 19) return SARAS_OK;
+    if (maxq > 11) return SARAS_OK;
     // box heights in rows of kPlaneVec floats: a span plus up to kPlaneVec - 1
     // floats before its start (the copy starts at the boundary below it).
     // TMA writes shared memory at 128-byte aligned addresses: every box starts
     // at a multiple of kPlaneVec floats in its slot
     const long mainRows = ((long)(maxRows + 2) * sy + 2 * kPlaneVec - 2) / kPlaneVec;
     const long sideRows = ((long)sy + 2 * kPlaneVec - 2) / kPlaneVec;
-    const long rRows = ((long)maxRows * sy + 2 * kPlaneVec - 2) / kPlaneVec;
-    if (mainRows > 256 || sideRows > 256 || rRows > 256) return SARAS_OK;
-    const int sideOff = (int)mainRows * kPlaneVec, rOff = sideOff + (int)sideRows * kPlaneVec;
-    const int slot = rOff + (int)rRows * kPlaneVec;
-    const size_t smem = (size_t)kPlaneRing * slot * sizeof(float);
+    if (mainRows > 256 || sideRows > 256) return SARAS_OK;
+    const int sideOff = (int)mainRows * kPlaneVec;
+    const int slot = sideOff + (int)sideRows * kPlaneVec;
+    const size_t smem = (size_t)kPlaneRing * slot * sizeof(float) + 128;   // + alignment of the first slot
     if (smem > 200 * 1024) return SARAS_OK;
     cuuint64_t dims[2] = {(cuuint64_t)kPlaneVec, (cuuint64_t)(L.count / kPlaneVec)};
     cuuint64_t strides[1] = {(cuuint64_t)kPlaneVec * sizeof(float)};
-    cuuint32_t box[2] = {(cuuint32_t)kPlaneVec, (cuuint32_t)mainRows}, sbox[2] = {(cuuint32_t)kPlaneVec, (cuuint32_t)sideRows},
-               rbox[2] = {(cuuint32_t)kPlaneVec, (cuuint32_t)rRows};
+    cuuint32_t box[2] = {(cuuint32_t)kPlaneVec, (cuuint32_t)mainRows}, sbox[2] = {(cuuint32_t)kPlaneVec, (cuuint32_t)sideRows};
     cuuint32_t es[2] = {1, 1};
     auto enc = [&](CUtensorMap *m, float *base, const cuuint32_t *bx) {
         return encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, bx, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -1972,23 +1986,20 @@ static int plane_setup(Ctx &c) {
         float *base = b ? L.b32 : L.a32;
         if (!enc(&c.planeMap[b], base, box) || !enc(&c.planeSide[b], base, sbox)) return SARAS_OK;   // the other kernels run
     }
-    if (!enc(&c.planeR, L.r32, rbox)) return SARAS_OK;
-    c.planeMaxQ = maxq <= 10 ? 10 : 19;
-    const void *fns[2] = {c.planeMaxQ == 10 ? (const void *)k_tgt_plane_tma<0, 10> : (const void *)k_tgt_plane_tma<0, 19>,
-                          c.planeMaxQ == 10 ? (const void *)k_tgt_plane_tma<1, 10> : (const void *)k_tgt_plane_tma<1, 19>};
+    c.planeMaxQ = maxq <= 5 ? 5 : 11;
+    const void *fns[2] = {c.planeMaxQ == 5 ? (const void *)k_tgt_plane_tma<0, 5> : (const void *)k_tgt_plane_tma<0, 11>,
+                          c.planeMaxQ == 5 ? (const void *)k_tgt_plane_tma<1, 5> : (const void *)k_tgt_plane_tma<1, 11>};
     for (const void *f : fns) SARAS_CUDA_TRY(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     // one wave: as many CTAs as fit (shared memory bounds them), tiles x segments of planes
     int perSM = 0;
-    SARAS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, fns[0], kPlaneBlock, smem));
+    SARAS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, fns[0], kPlaneThreads, smem));
     perSM = std::max(1, perSM);
     const int segs0 = std::max(1, (c.numSMs * perSM) / nTiles);
     c.planeSegPlanes = (E0 + 1 + segs0 - 1) / segs0;
     c.planeSegs = (E0 + 1 + c.planeSegPlanes - 1) / c.planeSegPlanes;
     c.planeMainRows = (int)mainRows;
     c.planeSideRows = (int)sideRows;
-    c.planeRRows = (int)rRows;
     c.planeSideOff = sideOff;
-    c.planeROff = rOff;
     c.planeSlotFloats = slot;
     c.planeSmem = smem;
     c.planeOk = true;
@@ -1998,29 +2009,27 @@ static int plane_setup(Ctx &c) {
 // Finest-level FP32 sweep (mode 0) or residual (mode 1) through the plane-streaming kernel.
 static void plane_launch(Ctx &c, int mode, float *out, const float *in, const float *r, const MgBC &bc, const TgK<float> &tk) {
     Level &L = c.lv[0];
-    (void)r;   // the right-hand side comes through its tensor map (the level's r32)
     PlaneArgs a;
     a.out = out;
+    a.r = r;
     a.sy = L.n[2] + 3;
     a.sx = (L.n[1] + 3) * a.sy;
     a.bc = bc;
     a.c = tk;
     a.mainRows = c.planeMainRows;
     a.sideRows = c.planeSideRows;
-    a.rRows = c.planeRRows;
     a.sideOff = c.planeSideOff;
-    a.rOff = c.planeROff;
     a.slotFloats = c.planeSlotFloats;
     a.planesPerSeg = c.planeSegPlanes;
     a.err = c.dflag + 2;
     const int b = in == L.a32 ? 0 : 1;
     dim3 g((L.n[1] + 1) / kPlaneRows, c.planeSegs, 1);
-    if (c.planeMaxQ == 10) {
-        if (mode == 0) k_tgt_plane_tma<0, 10><<<g, kPlaneBlock, c.planeSmem, c.stream>>>(c.planeMap[b], c.planeSide[b], c.planeR, a);
-        else k_tgt_plane_tma<1, 10><<<g, kPlaneBlock, c.planeSmem, c.stream>>>(c.planeMap[b], c.planeSide[b], c.planeR, a);
+    if (c.planeMaxQ == 5) {
+        if (mode == 0) k_tgt_plane_tma<0, 5><<<g, kPlaneThreads, c.planeSmem, c.stream>>>(c.planeMap[b], c.planeSide[b], a);
+        else k_tgt_plane_tma<1, 5><<<g, kPlaneThreads, c.planeSmem, c.stream>>>(c.planeMap[b], c.planeSide[b], a);
     } else {
-        if (mode == 0) k_tgt_plane_tma<0, 19><<<g, kPlaneBlock, c.planeSmem, c.stream>>>(c.planeMap[b], c.planeSide[b], c.planeR, a);
-        else k_tgt_plane_tma<1, 19><<<g, kPlaneBlock, c.planeSmem, c.stream>>>(c.planeMap[b], c.planeSide[b], c.planeR, a);
+        if (mode == 0) k_tgt_plane_tma<0, 11><<<g, kPlaneThreads, c.planeSmem, c.stream>>>(c.planeMap[b], c.planeSide[b], a);
+        else k_tgt_plane_tma<1, 11><<<g, kPlaneThreads, c.planeSmem, c.stream>>>(c.planeMap[b], c.planeSide[b], a);
     }
 }
 

@@ -869,6 +869,7 @@ namespace saras {
 // extrapolation costs.
 static bool rings_due(const Ctx &c, const UNet *u) {
     if (c.collecting) return true;
+    if (c.guessMode == SARAS_GUESS_NETWORK) return u->trained;
     if (c.guessMode != SARAS_GUESS_LEARNED || !u->trained) return false;
     if (u->wantNet || u->usesNet < 2 || u->usesExt < 2 || u->preferNet) return true;
     return u->nextProbe > 0 && u->solves + 3 >= u->nextProbe;
@@ -934,8 +935,12 @@ constexpr int kProbe = 8, kProbeMax = 64;
 constexpr double kNetCostDecades = 0.5;
 
 int unet_pick(Ctx &c) {
-    if (c.guessMode != SARAS_GUESS_LEARNED) return c.guessMode;
     UNet *u = U(c);
+    if (c.guessMode == SARAS_GUESS_NETWORK) {   // the network whenever its histories are complete
+        if (!u || !u->trained) return SARAS_GUESS_EXTRAPOLATE;
+        return u->track && u->nb >= 2 && u->np >= 2 ? SARAS_GUESS_LEARNED : SARAS_GUESS_EXTRAPOLATE;
+    }
+    if (c.guessMode != SARAS_GUESS_LEARNED) return c.guessMode;
     if (!u || !u->trained) return SARAS_GUESS_EXTRAPOLATE;
     u->solves += 1;
     u->shadow = false;
@@ -1002,7 +1007,7 @@ int unet_guess(Ctx &c, const double *b, double *dst, int mode, long long *fxdst,
     if (c.histCount < 2 + (quad ? 1 : 0)) return SARAS_BAD_CONFIG;
     int s;
     UNet *u = U(c);
-    if (c.guessMode == SARAS_GUESS_LEARNED && u && u->trained && (s = push_b(c, b))) return s;
+    if ((c.guessMode == SARAS_GUESS_LEARNED || c.guessMode == SARAS_GUESS_NETWORK) && u && u->trained && (s = push_b(c, b))) return s;
     if (use_net) {
         if (!u || !u->trained) return SARAS_BAD_CONFIG;
         if (u->nb < 3 || u->np < 2) use_net = false;   // histories not yet consecutive: plain extrapolation

@@ -29,12 +29,21 @@ def test_cfl_time_step_matches_oracle(courant):
     """Each step: computeTStp on both sides (bit-equal: exact maxima, the
     reference's expression), capped at "Time-Step", then the next step runs
     with it; iteration counts equal every step, fields to 1e-10 at the end.
-    Courant 1e-3 gives steps below the cap, 0.1 steps at it."""
-    p, g, o = pair("tgv")
+    A random start (every velocity component of order one) makes Courant
+    1e-3 give steps below the cap and 0.1 steps at it."""
+    p = C.ldc()
     p.useCFL = 1
     p.courantNumber = courant
-    g.close(); g = S.Solver(p); C.initialise(g, p, "tgv")
-    o = Oracle(p); C.initialise(o, p, "tgv")
+    g, o = S.Solver(p), Oracle(p)
+    C.initialise(g, p, "ldc")
+    C.initialise(o, p, "ldc")
+    rng = np.random.default_rng(13)
+    for f in (F.FIELD_VX, F.FIELD_VY, F.FIELD_VZ):
+        a = rng.uniform(-1.0, 1.0, g.dims(f))
+        g.set(f, a)
+        o.set(f, a)
+        g.apply_bc(f)
+        o.apply_bc(f)
     capped = []
     for step in range(6):
         sg, stg = g.time_advance()
@@ -47,7 +56,7 @@ def test_cfl_time_step_matches_oracle(courant):
         capped.append(dt == p.tStp)
         g.set_dt(dt)
         o.set_dt(dt)
-    assert all(capped) == (courant == 0.1)
+    assert capped == [courant == 0.1] * 6, capped
     for f in (F.FIELD_VX, F.FIELD_VY, F.FIELD_VZ, F.FIELD_P):
         assert C.rel_err(g.get(f), o.get(f)) <= TOL, F.FIELD_NAMES[f]
 
@@ -136,3 +145,29 @@ def test_solvepde_writes_probes_and_restart(tmp_path):
     q.restartFlag = 1
     r = S.hydro_d3(q, restart=str(tmp_path / "restartFile.saras"))
     assert abs(r.time - 0.01) < 1e-12
+
+
+@pytest.mark.parametrize("kind,scale", [("rbc", 1.0), ("rbc", 1e7), ("ldc", 1e7)])
+def test_tseries_values_and_divergence_abort(kind, scale):
+    """tseries::writeTSData (tseries.cc:137-178, 195-246) on a random state:
+    energy to 1e-12 relative, the Nusselt number to 1e-10 (1 + a signed sum over
+    kappa: summation order), the signed maximum divergence to 1e-12, and the
+    abort status of tseries.cc:141-145 (divergence above 1e5) returned on both
+    sides when the velocities are scaled up."""
+    p, g, o = pair(kind)
+    rng = np.random.default_rng(29)
+    fields = [F.FIELD_VX, F.FIELD_VY, F.FIELD_VZ] + ([F.FIELD_T] if kind == "rbc" else [])
+    for f in fields:
+        a = scale * rng.uniform(-1.0, 1.0, g.dims(f)) if f != F.FIELD_T else rng.uniform(0.0, 1.0, g.dims(f))
+        g.set(f, a)
+        o.set(f, a)
+        g.apply_bc(f)
+        o.apply_bc(f)
+    sg, eg, dg, ng = g.diagnostics()
+    so, eo, do, no = o.diagnostics()
+    limit = F.DIVERGENCE_LIMIT if scale > 1.0 else 0
+    assert sg == so == limit
+    assert abs(eg - eo) <= 1e-12 * abs(eo)
+    assert abs(dg - do) <= 1e-12 * abs(do)
+    if kind == "rbc":
+        assert abs(ng - no) <= 1e-10 * abs(no), (ng, no)

@@ -8,6 +8,7 @@ import pytest
 
 import saras_gb300 as S
 from saras_gb300 import _abi as F
+from oracle.oracle import Oracle
 from tests import _cases as C
 
 pytestmark = pytest.mark.gpu
@@ -380,3 +381,31 @@ def test_plane_streaming_stencils_match_column_kernels(kind):
     assert out[True][0] == out[False][0]
     for a, b in zip(out[True][1], out[False][1]):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("kind", ["ldc", "rbc"])
+def test_split_cn_accepted_iterate_meets_tolerance(kind):
+    """fastKernels = 2 accepts a Crank-Nicolson iterate on a bound (the last
+    correction's size times the measured contraction) instead of evaluating its
+    residual: the accepted field's residual, evaluated by the oracle with the
+    reference's expression (hydro_d3.cc:392-400), is below cnTolerance for every
+    component, on walls (LDC) and with the scalar (RBC)."""
+    p = C.CASES[kind]()
+    p.fastKernels = 2
+    g, o = S.Solver(p), Oracle(p)
+    C.initialise(g, p, kind)
+    C.initialise(o, p, kind)
+    rng = np.random.default_rng(31)
+    comps = [0, 1, 2] + ([3] if kind == "rbc" else [])
+    for c in comps:
+        f = F.FIELD_T if c == 3 else F.FIELD_VX + c
+        r = F.FIELD_TRHS if c == 3 else F.FIELD_NSE_X + c
+        V = g.get(f)
+        rhs = V + 1e-2 * rng.standard_normal(V.shape)
+        g.set(r, rhs)
+        o.set(r, rhs)
+        s, iters, _ = g.cn_solve(c)
+        assert s == 0 and iters >= 2, (c, iters)
+        o.set(f, g.get(f))
+        res = o.cn_residual(c)
+        assert res < p.cnTolerance, (c, iters, res, p.cnTolerance)

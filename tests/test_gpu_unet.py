@@ -94,34 +94,51 @@ def _tgv_solver(guess):
 
 
 def test_learned_guess_reduces_vcycles():
-    """Three identical runs; after a warm-up that collects pairs, one continues
-    with the trained network, one with plain extrapolation, one with the
-    previous pressure (the method without the network)."""
-    runs = {name: _tgv_solver(F.GUESS_PREVIOUS) for name in ("net", "extrap", "prev")}
-    runs["net"].unet_collect()
+    """Four identical runs; after a warm-up that collects pairs, the trained
+    network is used by the per-solve selector (learned), in every solve
+    (network alone), and compared with plain extrapolation and with the
+    previous pressure (the method without any history).  What is asserted is
+    what holds: the network's guess starts closer than the previous pressure
+    and needs fewer V-cycles than it; the selector is never worse than
+    extrapolation by more than half a cycle a solve.  The network is not
+    asserted to beat extrapolation: on this flow its guess leaves about the
+    residual extrapolation leaves (both printed)."""
+    names = ("learned", "network", "extrap", "prev")
+    runs = {name: _tgv_solver(F.GUESS_PREVIOUS) for name in names}
+    runs["learned"].unet_collect()
+    runs["network"].unet_collect()
     for _ in range(12):
         for g in runs.values():
             s, st = g.time_advance()
             assert s == 0
-    loss = runs["net"].unet_train(150, 2e-3)
-    assert np.isfinite(loss)
-    runs["net"].set_guess_mode(F.GUESS_LEARNED)
+    for k in ("learned", "network"):
+        loss = runs[k].unet_train(150, 2e-3)
+        assert np.isfinite(loss)
+    runs["learned"].set_guess_mode(F.GUESS_LEARNED)
+    runs["network"].set_guess_mode(F.GUESS_NETWORK)
     runs["extrap"].set_guess_mode(F.GUESS_EXTRAPOLATE)
     cycles = {k: [] for k in runs}
-    sources = []
-    for _ in range(6):
+    start = {k: [] for k in runs}
+    sources = {k: [] for k in runs}
+    for _ in range(8):
         for k, g in runs.items():
             s, st = g.time_advance()
             assert s == 0 and st.fine_residual <= 1e-8
             cycles[k].append(st.vcycles)
-            if k == "net":
-                sources.append(st.guess_source)
+            start[k].append(st.guess_residual)
+            sources[k].append(st.guess_source)
     mean = {k: float(np.mean(v)) for k, v in cycles.items()}
-    print("V-cycles per step:", mean, "guess sources:", sources, "loss:", loss)
-    assert mean["net"] <= mean["prev"]
-    # all three runs solve to the same residual target: the fields agree
-    for f in (F.FIELD_VX, F.FIELD_P):
-        assert C.rel_err(runs["net"].get(f), runs["prev"].get(f)) < 1e-7
+    med = {k: float(np.median(v)) for k, v in start.items()}
+    print("V-cycles per step:", mean, "median start residual / max|b|:", med, "sources:", sources)
+    # the network-only run used the network once its histories were complete
+    assert sources["network"][-4:] == [F.GUESS_LEARNED] * 4, sources["network"]
+    assert med["network"] < med["prev"]
+    assert mean["network"] < mean["prev"]
+    assert mean["learned"] <= mean["extrap"] + 0.5
+    # all runs solve to the same residual target: the fields agree
+    for k in ("learned", "network", "extrap"):
+        for f in (F.FIELD_VX, F.FIELD_P):
+            assert C.rel_err(runs[k].get(f), runs["prev"].get(f)) < 1e-7, (k, f)
 
 
 # layer table of the U-Net (unet.cu): input channels (main, skip), output channels, level, ReLU
