@@ -254,6 +254,43 @@ def plain_arm(args, fast, before):
             "fastKernels": fast}
 
 
+def tma_arm(args, before):
+    """The headline arm with the finest level's FP32 sweeps and residuals run
+    through the TMA plane-streaming kernels (SARAS_PLANE_TMA=1; the same bits as
+    the default column kernels): steps/s over the headline's step window and the
+    level-0 sweep's HBM rate, beside the default's."""
+    import saras_gb300 as S
+    from saras_gb300 import _abi as F
+    old = os.environ.get("SARAS_PLANE_TMA")
+    os.environ["SARAS_PLANE_TMA"] = "1"
+    try:
+        p = tgv_params(F.MG_MIXED, F.GUESS_PREVIOUS)
+        g = S.Solver(p)
+    finally:
+        if old is None:
+            os.environ.pop("SARAS_PLANE_TMA", None)
+        else:
+            os.environ["SARAS_PLANE_TMA"] = old
+    active = g.plane_tma_active()
+    init_tgv(g, p)
+    g.set_guess_mode(F.GUESS_EXTRAPOLATE)
+    for k in range(before):
+        g.time_advance()
+    names = S.Solver.profile_names()
+    k_s = names.index("mg_smooth_fp32")
+    g.profile_enable(k_s, True)
+    g.profile_sample(PROF_EVERY)
+    ms, sts = time_steps(g, args.steps)
+    n_k, ms_k, b_k = g.profile_read(k_s)
+    g.close()
+    peak, _ = measured_peak_hbm()
+    avg = ms_k / n_k if n_k else None
+    gbs = (b_k / n_k) / (avg * 1e-3) / 1e9 if avg else None
+    return {"active": active, "steps_per_s": round(args.steps / (ms / 1e3), 3), "guess": "extrapolate",
+            "mg_smooth_fp32_avg_ms": round(avg, 4) if avg else None, "mg_smooth_fp32_GBs": round(gbs, 1) if gbs else None,
+            "mg_smooth_fp32_frac": round(gbs / peak, 4) if gbs else None, "kernel": "k_tgt_plane_tma"}
+
+
 def accuracy_run(args):
     """Config 3's accuracy figures: the headline arm (its guess mode, mixed
     refinement, fastKernels = 2) and the plain FP64 arm with the reference's
@@ -360,6 +397,7 @@ def run_ours(args, dist):
     if not args.no_plain and dist.rank == 0:
         plain = plain_arm(args, 2, done)
         plain_strict = plain_arm(args, 0, done)
+    tma = tma_arm(args, done) if (not args.no_plain and dist.rank == 0) else None
     acc = accuracy_run(args) if (not args.no_accuracy and dist.rank == 0) else None
     # --- end to end through the C ABI with pinned host buffers
     e2e = None
@@ -437,6 +475,7 @@ def run_ours(args, dist):
             "speedup_vs_plain_fp64": round(value / dist.world / plain["steps_per_s"], 3) if plain else None,
             "speedup_vs_plain_fp64_strict": round(value / dist.world / plain_strict["steps_per_s"], 3) if plain_strict else None,
             "accuracy_vs_plain_fp64": acc,
+            "plane_tma_variant": tma,
             "l2": "inputs larger than L2: every FP64 field is 259^3*8 B = 139 MB > 129 MB L2",
             "parallelism": "replicas" if dist.world > 1 else "single GPU",
         },
@@ -518,6 +557,151 @@ def run_reference(args, dist):
     }
 
 
+# ------------------------------------------------------------------ studies
+# Two further workloads, run on request (--workload); each prints one JSON
+# line of its own.  They are the learned-warm-start and at-scale studies of
+# the same time step, not the headline metric.
+def rbc_params(guess, ind=(8, 8, 7), depth=6, dt=5.0e-4):
+    """Rayleigh-Benard convection: 257 x 257 x 129 on a 2:2:1 box, periodic
+    sides, no-slip top and bottom (T = 1 bottom, 0 top), Ra 1e7, Pr 1; the
+    mixed-precision solve with the headline's cycle to the same 1e-8 residual."""
+    from saras_gb300 import _abi
+    p = _abi.default_params()
+    p.probType, p.icType = 5, 0
+    p.xPer = p.yPer = 1
+    p.zPer = 0
+    p.Lx, p.Ly, p.Lz = 2.0, 2.0, 1.0
+    p.xInd, p.yInd, p.zInd = ind
+    p.vcDepth = depth
+    p.Ra, p.Pr, p.rbcType, p.forceType = 1.0e7, 1.0, 2, 3
+    p.Re = 1.0
+    p.tStp = dt
+    p.cnTolerance = 1.0e-8
+    p.mgTolerance = 1.0e-8
+    p.preSmooth = p.postSmooth = 3
+    p.smoother = _abi.SMOOTHER_CHEBYSHEV
+    p.coarseCycles = 1
+    p.mgMode = _abi.MG_MIXED
+    p.mgTarget = TARGET
+    p.mgMaxCycles = 100
+    p.mixedCycles = 0
+    p.jacobiWeight = 6.0 / 7.0
+    p.fastKernels = 2
+    p.guessMode = guess
+    return p
+
+
+def study_rbc_learned(args):
+    """Rayleigh-Benard 257 x 257 x 129, 2000 steps: the first 300 with the
+    previous pressure as the guess (the U-Net arms collect training pairs there,
+    the last 32 of which are kept), then the U-Net is trained on the GPU and the
+    remaining steps run with it (the per-solve selector, and the network in
+    every solve), against the same steps with extrapolation and with the
+    previous pressure (the solver without the network)."""
+    import numpy as np
+    import saras_gb300 as S
+    from saras_gb300 import _abi as F
+    total, warm = args.study_steps or 2000, 300
+    arms = {"learned": F.GUESS_LEARNED, "network_every_solve": F.GUESS_NETWORK,
+            "extrapolation": F.GUESS_EXTRAPOLATE, "previous_pressure": F.GUESS_PREVIOUS}
+    res = {}
+    for name, mode in arms.items():
+        p = rbc_params(F.GUESS_PREVIOUS)
+        g = S.Solver(p)
+        g.set(F.FIELD_P, np.ones(g.dims(F.FIELD_P)))
+        g.set(F.FIELD_T, S.rbc_temperature(p, seed=42))
+        for f in (F.FIELD_VX, F.FIELD_VY, F.FIELD_VZ, F.FIELD_T):
+            g.apply_bc(f)
+        learned = mode in (F.GUESS_LEARNED, F.GUESS_NETWORK)
+        if learned:
+            g.unet_collect()
+        for k in range(warm):
+            s, st = g.time_advance()
+            if s != 0:
+                raise RuntimeError("%s: warm-up step %d failed: %d" % (name, k, s))
+        info = {}
+        if learned:
+            t0 = time.perf_counter()
+            info["final_loss"] = g.unet_train(args.train_iters, args.lr)
+            g.synchronize()
+            info["train_seconds"] = round(time.perf_counter() - t0, 2)
+            info["train_iters"] = args.train_iters
+        g.set_guess_mode(mode)
+        ms, sts = time_steps(g, total - warm)
+        vc = np.array([x[0] for x in sts], dtype=float)
+        src = [x[3] for x in sts]
+        res[name] = dict(info, vcycles_per_step=round(float(vc.mean()), 4),
+                         vcycles_per_step_last_1000=round(float(vc[-1000:].mean()), 4),
+                         steps_per_s=round(len(sts) / (ms / 1e3), 2), max_fine_residual=max(x[2] for x in sts),
+                         guess_sources={"previous": src.count(0), "network": src.count(1), "extrapolation": src.count(2)})
+        _, e, d, nu = g.diagnostics()
+        res[name]["end_state"] = {"energy": e, "max_div": d, "nusselt": nu}
+        g.close()
+    base = res["previous_pressure"]["vcycles_per_step"]
+    return {"study": "learned warm start, Rayleigh-Benard", "metric": "V-cycles per step (mixed solve to 1e-8)",
+            "workload": "Rayleigh-Benard 257x257x129, 2:2:1 box, PPN, Ra 1e7, Pr 1, dt 5e-4, %d steps; guess from step %d on "
+                        "(before: previous pressure; U-Net trained on pairs of those steps)" % (total, warm),
+            "arms": res,
+            "vcycle_reduction_vs_previous_pressure": {k: round(1.0 - v["vcycles_per_step"] / base, 4) for k, v in res.items()},
+            "data": "synthetic (linear conduction profile plus seeded uniform perturbation of amplitude 1e-3)"}
+
+
+def study_tgv513(args):
+    """Taylor-Green 513^3, dt 2.5e-4, 200 steps: the learned + mixed solve
+    against the plain FP64 solve to the same 1e-8 residual, with the HBM rate of
+    the kernels with the largest shares of the mixed arm."""
+    import saras_gb300 as S
+    from saras_gb300 import _abi as F
+    steps = args.study_steps or 200
+    out = {}
+    for arm in ("learned_mixed", "plain_fp64"):
+        mode = F.MG_MIXED if arm == "learned_mixed" else F.MG_PLAIN_TARGET
+        p = tgv_params(mode, F.GUESS_PREVIOUS, ind=9, depth=7)
+        p.tStp = 2.5e-4
+        g = S.Solver(p)
+        init_tgv(g, p)
+        done = 0
+        info = None
+        if arm == "learned_mixed":
+            g.unet_collect()
+            for k in range(args.collect):
+                g.time_advance()
+            t0 = time.perf_counter()
+            loss = g.unet_train(args.train_iters, args.lr)
+            g.synchronize()
+            info = {"final_loss": loss, "train_seconds": round(time.perf_counter() - t0, 2)}
+            g.set_guess_mode(F.GUESS_LEARNED)
+            done = args.collect
+        else:
+            for k in range(args.collect):
+                g.time_advance()
+            done = args.collect
+        names = S.Solver.profile_names()
+        for k in range(len(names)):
+            g.profile_enable(k, True)
+        g.profile_sample(PROF_EVERY)
+        ms, sts = time_steps(g, steps - done)
+        peak, _ = measured_peak_hbm()
+        kern = []
+        for k in range(len(names)):
+            n_k, ms_k, b_k = g.profile_read(k)
+            if n_k and b_k > 0 and ms_k > 0:
+                gbs = (b_k / n_k) / ((ms_k / n_k) * 1e-3) / 1e9
+                kern.append({"kernel": names[k], "avg_ms": round(ms_k / n_k, 4), "GB/s": round(gbs, 1),
+                             "frac_of_measured_hbm": round(gbs / peak, 3), "launches_timed": n_k})
+        kern.sort(key=lambda r: -r["avg_ms"] * r["launches_timed"])
+        vc = [x[0] for x in sts]
+        out[arm] = {"steps_timed": len(sts), "steps_before": done, "ms_per_step": round(ms / len(sts), 3),
+                    "steps_per_s": round(len(sts) / (ms / 1e3), 3), "vcycles_per_step": round(sum(vc) / len(vc), 3),
+                    "max_fine_residual": max(x[2] for x in sts), "learned": info, "kernels": kern[:8],
+                    "timing": "profiling events on (one V-cycle in %d timed)" % PROF_EVERY}
+        g.close()
+    return {"study": "combined at scale", "metric": "steps/s at 513^3, learned+mixed vs plain FP64 at equal 1e-8 residual",
+            "workload": "Taylor-Green 513^3, [0,2pi]^3 PPP, Re 1600, dt 2.5e-4, %d steps" % steps,
+            "arms": out, "speedup": round(out["learned_mixed"]["steps_per_s"] / out["plain_fp64"]["steps_per_s"], 3),
+            "data": "synthetic (Taylor-Green initial condition)"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -535,10 +719,17 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=30.0)
+    ap.add_argument("--workload", default="tgv257", choices=["tgv257", "rbc_learned", "tgv513"],
+                    help="tgv257: the headline line; rbc_learned, tgv513: the learned and at-scale studies")
+    ap.add_argument("--study-steps", type=int, default=0, help="total steps of a study (0: its configured count)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     args.learned = args.guess == "learned"
+    if args.workload != "tgv257":
+        study = study_rbc_learned if args.workload == "rbc_learned" else study_tgv513
+        print(json.dumps(study(args)), flush=True)
+        return
     dist = Dist()
     try:
         out = run_reference(args, dist) if args.impl == "reference" else run_ours(args, dist)

@@ -176,6 +176,10 @@ int saras_download_fields(saras_ctx *ctx, int n, const int *fields, double *cons
 int saras_synchronize(saras_ctx *ctx);
 /* Number of device kernels this context has launched so far. */
 long long saras_launch_count(const saras_ctx *ctx);
+/* 1 when the finest level's FP32 sweeps and residuals of the target modes run
+ * through the TMA plane-streaming kernels (environment SARAS_PLANE_TMA=1 at
+ * saras_create and a level that fits), 0 when the column kernels run. */
+int saras_plane_tma_active(const saras_ctx *ctx);
 
 /* ------------------------------------------------------ boundary fills */
 /* hydro::imposeUBCs/VBCs/WBCs (hydro.cc:386-461), scalar::imposeTBCs (scalar.cc:240-255):

@@ -130,6 +130,10 @@ class Solver:
     def launch_count(self):
         return self.lib.saras_launch_count(self.h)
 
+    def plane_tma_active(self):
+        """Whether the finest-level FP32 stencils run through the TMA kernels."""
+        return bool(self.lib.saras_plane_tma_active(self.h))
+
     # -- boundary and field operators
     def apply_bc(self, field):
         self._chk(self.lib.saras_apply_bc(self.h, field))

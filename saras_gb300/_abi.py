@@ -136,6 +136,7 @@ def load():
         "saras_download_fields": (_I, [vp, _I, ip, ctypes.POINTER(dp)]),
         "saras_synchronize": (_I, [vp]),
         "saras_launch_count": (ctypes.c_longlong, [vp]),
+        "saras_plane_tma_active": (_I, [vp]),
         "saras_apply_bc": (_I, [vp, _I]),
         "saras_sync_field": (_I, [vp, _I]),
         "saras_vfield_compute_diff": (_I, [vp]),

@@ -463,6 +463,7 @@ int saras_synchronize(saras_ctx *h) {
 }
 
 long long saras_launch_count(const saras_ctx *h) { return h ? h->c.launches : 0; }
+int saras_plane_tma_active(const saras_ctx *h) { return h && h->c.planeOk ? 1 : 0; }
 
 #define CTX_OR_FAIL(h) do { if (!h) return SARAS_BAD_ARG; } while (0)
 

@@ -106,10 +106,11 @@ struct Ctx {
     int numSMs = 1;           // multiprocessors of the context's device
     // finest-level FP32 plane-streaming stencils (TMA, target modes): tensor
     // maps of the two iterate buffers (a32, b32) with the main and the side
-    // box, and the launch shape; planeOk false when the level does not fit
+    // box and of the right-hand side (r32), and the launch shape; planeOk
+    // false when the level does not fit
     bool planeOk = false;
-    CUtensorMap planeMap[2], planeSide[2];
-    int planeMainRows = 0, planeSideRows = 0, planeSideOff = 0, planeSlotFloats = 0, planeSegPlanes = 0,
+    CUtensorMap planeMap[2], planeSide[2], planeR;
+    int planeMainRows = 0, planeSideRows = 0, planeRRows = 0, planeSideOff = 0, planeROff = 0, planeSlotFloats = 0, planeSegPlanes = 0,
         planeSegs = 0, planeMaxQ = 0;
     size_t planeSmem = 0;
     double *wallX = nullptr, *wallY = nullptr, *wallZ = nullptr;   // Dirichlet check walls

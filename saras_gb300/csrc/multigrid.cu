@@ -1068,31 +1068,28 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 6 : 5) k_tgt_residual(OT
 // slot, the periodic and mirror images along k are in the slot as well; along
 // j the mirror images are in the tile's halo rows and a periodic image row is
 // one more box (a second tensor map with a one-row box); along i the slot of
-// plane -1 or E+1 holds its image plane.
-//
-// The iterate is the operand with reuse (seven reads a point); the right-hand
-// side is read once a point, so it bypasses shared memory: each thread loads
-// its points of the next plane's right-hand side into registers while it
-// computes the current plane.  Every thread computes; thread 0 also issues
-// the copies.  Plane q goes to slot q % kPlaneRing; after plane i is done
+// plane -1 or E+1 holds its image plane.  The right-hand side's rows j0 ..
+// j0+R-1 come in the same slot (a third map): a plane of it read from global
+// memory into registers one plane ahead waited a full memory latency every
+// plane (measured 0.079 ms a 257^3 sweep, against 0.046 for the column kernel).
+// Every thread computes; thread 0 also issues the copies and waits on the
+// slot's mbarrier.  Plane q goes to slot q % kPlaneRing; after plane i is done
 // (one CTA barrier a plane), the slot of plane i - 1 is free and thread 0
-// refills it with plane i - 1 + kPlaneRing, so each copy has three planes'
-// compute time to land, and the two CTAs an SM keep several planes of copies
-// in flight.  The arithmetic is k_tgt_sweep's / k_tgt_residual's, operand for
+// refills it with plane i - 1 + kPlaneRing, so each copy has two planes'
+// compute time to land.  The arithmetic is k_tgt_sweep's / k_tgt_residual's, operand for
 // operand, so the results are the same bits.
 constexpr int kPlaneRows = 8;
-constexpr int kPlaneRing = 5;
+constexpr int kPlaneRing = 4;
 constexpr int kPlaneVec = 64;        // floats a tensor-map row (256 bytes)
 constexpr int kPlaneThreads = 512;
 
 struct PlaneArgs {
     float *out;
-    const float *r;      // right-hand side (residual mode: the level's b; sweep: its r)
     int sx, sy;          // strides of the padded level array, floats
     MgBC bc;
     TgK<float> c;
-    int mainRows, sideRows;   // box heights (rows of kPlaneVec floats) of the two maps
-    int sideOff;         // floats from a slot's start to the side box
+    int mainRows, sideRows, rRows;   // box heights (rows of kPlaneVec floats) of the three maps
+    int sideOff, rOff;   // floats from a slot's start to the side box and the right-hand side's box
     int slotFloats;      // floats a slot
     int planesPerSeg;
     int *err;            // set when an mbarrier wait gives up (1) or the layout is misaligned (2)
@@ -1100,7 +1097,8 @@ struct PlaneArgs {
 
 template <int MODE, int MAXQ>
 __global__ void __launch_bounds__(kPlaneThreads, MAXQ <= 5 ? 2 : 1)
-    k_tgt_plane_tma(const __grid_constant__ CUtensorMap map, const __grid_constant__ CUtensorMap sideMap, const PlaneArgs a) {
+    k_tgt_plane_tma(const __grid_constant__ CUtensorMap map, const __grid_constant__ CUtensorMap sideMap,
+                    const __grid_constant__ CUtensorMap rMap, const PlaneArgs a) {
     extern __shared__ __align__(128) float plane_sm[];
     __shared__ uint64_t full[kPlaneRing];
     const int tid = threadIdx.x;
@@ -1116,7 +1114,7 @@ __global__ void __launch_bounds__(kPlaneThreads, MAXQ <= 5 ? 2 : 1)
     const bool per1 = a.bc.per[1] != 0, per2 = a.bc.per[2] != 0;
     const bool side = per1 && (j0 == 0 || j0 + R - 1 == E1);
     const int sideRow = j0 == 0 ? E1 - 1 : 1;   // periodic image of row -1 / E1 + 1
-    const int sideOff = a.sideOff;
+    const int sideOff = a.sideOff, rOff = a.rOff;
     // slots start at the first 128-byte boundary of the dynamic shared memory
     // (the launch reserves 128 bytes more than the ring)
     float *sm = plane_sm + (((128u - (su32(plane_sm) & 127u)) & 127u) >> 2);
@@ -1125,7 +1123,8 @@ __global__ void __launch_bounds__(kPlaneThreads, MAXQ <= 5 ? 2 : 1)
     // start: its data sits at this offset in its box
     auto base = [&](int q) { return (int)((unsigned long)((long)(plane_img(q) + 1) * sx + (long)j0 * sy) & (kPlaneVec - 1)); };
     auto side_base = [&](int q) { return (int)((unsigned long)((long)(plane_img(q) + 1) * sx + (long)(sideRow + 1) * sy) & (kPlaneVec - 1)); };
-    const uint32_t tx = (uint32_t)((a.mainRows + (side ? a.sideRows : 0)) * kPlaneVec * 4);
+    auto r_base = [&](int q) { return (int)((unsigned long)((long)(plane_img(q) + 1) * sx + (long)(j0 + 1) * sy) & (kPlaneVec - 1)); };
+    const uint32_t tx = (uint32_t)((a.mainRows + a.rRows + (side ? a.sideRows : 0)) * kPlaneVec * 4);
     int issued = 0;   // thread 0: planes whose copies are issued
     auto issue = [&](int q) {
         const int slot = q % kPlaneRing, ii = plane_img(q);
@@ -1134,6 +1133,7 @@ __global__ void __launch_bounds__(kPlaneThreads, MAXQ <= 5 ? 2 : 1)
         mbar_arrive_expect_tx(m, tx);
         tma_load_2d(dst, &map, 0, (int)(((long)(ii + 1) * sx + (long)j0 * sy) / kPlaneVec), m);   // array row j0: row j0 - 1
         if (side) tma_load_2d(dst + sideOff * 4, &sideMap, 0, (int)(((long)(ii + 1) * sx + (long)(sideRow + 1) * sy) / kPlaneVec), m);
+        tma_load_2d(dst + rOff * 4, &rMap, 0, (int)(((long)(ii + 1) * sx + (long)(j0 + 1) * sy) / kPlaneVec), m);
         issued = q + 1;
     };
     bool ok = true;
@@ -1141,7 +1141,7 @@ __global__ void __launch_bounds__(kPlaneThreads, MAXQ <= 5 ? 2 : 1)
         // every box lands at a 128-byte aligned address (the layout's
         // invariant, checked so that a bad layout reports instead of issuing
         // a misaligned copy)
-        if (((su32(sm) | (uint32_t)(a.slotFloats * 4) | (uint32_t)(sideOff * 4)) & 127u) != 0u) {
+        if (((su32(sm) | (uint32_t)(a.slotFloats * 4) | (uint32_t)(sideOff * 4) | (uint32_t)(rOff * 4)) & 127u) != 0u) {
             atomicExch(a.err, 2);
             ok = false;
         }
@@ -1171,31 +1171,20 @@ __global__ void __launch_bounds__(kPlaneThreads, MAXQ <= 5 ? 2 : 1)
     }
     const int gj = j0 * sy;
     const TgK<float> &c = a.c;
-    // right-hand side of plane i at this thread's points (P[q] counts rows from j0 - 1)
-    float rv[MAXQ], rn[MAXQ];
-    {
-        const float *rp = a.r + (long)(i0 + 1) * sx + gj;
-#pragma unroll
-        for (int q = 0; q < MAXQ; ++q) rv[q] = (live >> q) & 1u ? __ldg(rp + P[q]) : 0.0f;
-    }
     // slot pointers (after each plane's base offset) of planes qc - 1, qc, qc + 1, rolled along
     const float *sp = sm + base(0), *sc = sm + (size_t)a.slotFloats + base(1), *sn = sm + (size_t)2 * a.slotFloats + base(2);
     int slotC = 1;
     for (int i = i0; i < i1; ++i) {
         const int qc = i - i0 + 1;   // plane i is plane qc of the segment
-        {
-            const float *rp = a.r + (long)(i + 2) * sx + gj;
-            const bool more = i + 1 < i1;
-#pragma unroll
-            for (int q = 0; q < MAXQ; ++q) rn[q] = more && ((live >> q) & 1u) ? __ldg(rp + P[q]) : 0.0f;
-        }
-        const float *ss = side ? sm + (size_t)slotC * a.slotFloats + sideOff + side_base(qc) : sm;
+        const float *scs = sm + (size_t)slotC * a.slotFloats;
+        const float *ss = side ? scs + sideOff + side_base(qc) : scs;
+        const float *sr = scs + rOff + r_base(qc) - sy;   // P[q] counts rows from j0 - 1
         float *out = a.out + (long)(i + 1) * sx + gj;
 #pragma unroll
         for (int q = 0; q < MAXQ; ++q) {
             if (!((live >> q) & 1u)) continue;
             const int x = P[q];
-            const float C = sc[x], Wv = sp[x], Ev = sn[x];
+            const float C = sc[x], Wv = sp[x], Ev = sn[x], rv = sr[x];
             float N, S, U, D;
             if (!((edge >> q) & 1u)) {
                 N = sc[x + sy]; S = sc[x - sy]; U = sc[x + 1]; D = sc[x - 1];
@@ -1209,10 +1198,10 @@ __global__ void __launch_bounds__(kPlaneThreads, MAXQ <= 5 ? 2 : 1)
             }
             float v;
             if (MODE == 0) {
-                v = fmaf(c.ax, Wv + Ev, fmaf(c.ay, N + S, fmaf(c.az, U + D, fmaf(c.ar, rv[q], c.om1 * C))));
+                v = fmaf(c.ax, Wv + Ev, fmaf(c.ay, N + S, fmaf(c.az, U + D, fmaf(c.ar, rv, c.om1 * C))));
             } else {
                 const float lap = fmaf(c.lx, Wv + Ev, fmaf(c.ly, N + S, fmaf(c.lz, U + D, c.lc * C)));
-                v = rv[q] - lap;
+                v = rv - lap;
             }
             out[x] = v;
         }
@@ -1230,8 +1219,6 @@ __global__ void __launch_bounds__(kPlaneThreads, MAXQ <= 5 ? 2 : 1)
         sp = sc;
         sc = sn;
         sn = sm + (size_t)slotN * a.slotFloats + (qc + 2 < nplanes ? base(qc + 2) : 0);
-#pragma unroll
-        for (int q = 0; q < MAXQ; ++q) rv[q] = rn[q];
     }
     // leave no copy in flight: every issued plane's slot complete (bounded) before the CTA ends
     if (tid == 0)
@@ -1928,10 +1915,11 @@ static bool coarse_solution_operator(int X, int Y, int Z, const double l[3], con
 // Tensor maps and launch shape of the finest-level plane-streaming kernels
 // (k_tgt_plane_tma).  The level array is viewed as rows of kPlaneVec floats;
 // the main box covers a tile's rows j0-1 .. j0+R of a plane, the side box one
-// padded row.  Off (the other kernels run) when a tile would not fit,
-// when the level has fewer than two tiles of rows, or when SARAS_PLANE_TMA=0
-// is set in the environment (a diagnostic switch: both paths compute the same
-// bits).
+// padded row, the right-hand side's box rows j0 .. j0+R-1.  Used when
+// SARAS_PLANE_TMA=1 is set in the environment and the level fits (at least
+// two tiles of rows, the ring within 200 KB); otherwise the column kernels run.
+// Both compute the same bits; the column kernels are the default because they
+// are faster on GB300 (257^3 level-0 sweep: 0.046 ms against 0.071 ms).
 // The driver's cuTensorMapEncodeTiled, looked up through the runtime (the
 // library does not link the driver library, so it loads on machines without
 // one and reports SARAS_NO_DEVICE there).
@@ -1954,7 +1942,7 @@ static int plane_setup(Ctx &c) {
     PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
     if (!encode) return SARAS_OK;
     const char *env = std::getenv("SARAS_PLANE_TMA");
-    if (env && env[0] == '0') return SARAS_OK;
+    if (!env || env[0] != '1') return SARAS_OK;
     Level &L = c.lv[0];
     const int E0 = L.n[0], E1 = L.n[1], E2 = L.n[2];
     const int sy = E2 + 3, W = E2 + 1;
@@ -1969,14 +1957,16 @@ static int plane_setup(Ctx &c) {
     // at a multiple of kPlaneVec floats in its slot
     const long mainRows = ((long)(maxRows + 2) * sy + 2 * kPlaneVec - 2) / kPlaneVec;
     const long sideRows = ((long)sy + 2 * kPlaneVec - 2) / kPlaneVec;
-    if (mainRows > 256 || sideRows > 256) return SARAS_OK;
-    const int sideOff = (int)mainRows * kPlaneVec;
-    const int slot = sideOff + (int)sideRows * kPlaneVec;
+    const long rRows = ((long)maxRows * sy + 2 * kPlaneVec - 2) / kPlaneVec;
+    if (mainRows > 256 || sideRows > 256 || rRows > 256) return SARAS_OK;
+    const int sideOff = (int)mainRows * kPlaneVec, rOff = sideOff + (int)sideRows * kPlaneVec;
+    const int slot = rOff + (int)rRows * kPlaneVec;
     const size_t smem = (size_t)kPlaneRing * slot * sizeof(float) + 128;   // + alignment of the first slot
     if (smem > 200 * 1024) return SARAS_OK;
     cuuint64_t dims[2] = {(cuuint64_t)kPlaneVec, (cuuint64_t)(L.count / kPlaneVec)};
     cuuint64_t strides[1] = {(cuuint64_t)kPlaneVec * sizeof(float)};
-    cuuint32_t box[2] = {(cuuint32_t)kPlaneVec, (cuuint32_t)mainRows}, sbox[2] = {(cuuint32_t)kPlaneVec, (cuuint32_t)sideRows};
+    cuuint32_t box[2] = {(cuuint32_t)kPlaneVec, (cuuint32_t)mainRows}, sbox[2] = {(cuuint32_t)kPlaneVec, (cuuint32_t)sideRows},
+               rbox[2] = {(cuuint32_t)kPlaneVec, (cuuint32_t)rRows};
     cuuint32_t es[2] = {1, 1};
     auto enc = [&](CUtensorMap *m, float *base, const cuuint32_t *bx) {
         return encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, bx, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -1986,6 +1976,7 @@ static int plane_setup(Ctx &c) {
         float *base = b ? L.b32 : L.a32;
         if (!enc(&c.planeMap[b], base, box) || !enc(&c.planeSide[b], base, sbox)) return SARAS_OK;   // the other kernels run
     }
+    if (!enc(&c.planeR, L.r32, rbox)) return SARAS_OK;
     c.planeMaxQ = maxq <= 5 ? 5 : 11;
     const void *fns[2] = {c.planeMaxQ == 5 ? (const void *)k_tgt_plane_tma<0, 5> : (const void *)k_tgt_plane_tma<0, 11>,
                           c.planeMaxQ == 5 ? (const void *)k_tgt_plane_tma<1, 5> : (const void *)k_tgt_plane_tma<1, 11>};
@@ -1999,7 +1990,9 @@ static int plane_setup(Ctx &c) {
     c.planeSegs = (E0 + 1 + c.planeSegPlanes - 1) / c.planeSegPlanes;
     c.planeMainRows = (int)mainRows;
     c.planeSideRows = (int)sideRows;
+    c.planeRRows = (int)rRows;
     c.planeSideOff = sideOff;
+    c.planeROff = rOff;
     c.planeSlotFloats = slot;
     c.planeSmem = smem;
     c.planeOk = true;
@@ -2009,27 +2002,29 @@ static int plane_setup(Ctx &c) {
 // Finest-level FP32 sweep (mode 0) or residual (mode 1) through the plane-streaming kernel.
 static void plane_launch(Ctx &c, int mode, float *out, const float *in, const float *r, const MgBC &bc, const TgK<float> &tk) {
     Level &L = c.lv[0];
+    (void)r;   // the right-hand side comes through its tensor map (the level's r32)
     PlaneArgs a;
     a.out = out;
-    a.r = r;
     a.sy = L.n[2] + 3;
     a.sx = (L.n[1] + 3) * a.sy;
     a.bc = bc;
     a.c = tk;
     a.mainRows = c.planeMainRows;
     a.sideRows = c.planeSideRows;
+    a.rRows = c.planeRRows;
     a.sideOff = c.planeSideOff;
+    a.rOff = c.planeROff;
     a.slotFloats = c.planeSlotFloats;
     a.planesPerSeg = c.planeSegPlanes;
     a.err = c.dflag + 2;
     const int b = in == L.a32 ? 0 : 1;
     dim3 g((L.n[1] + 1) / kPlaneRows, c.planeSegs, 1);
     if (c.planeMaxQ == 5) {
-        if (mode == 0) k_tgt_plane_tma<0, 5><<<g, kPlaneThreads, c.planeSmem, c.stream>>>(c.planeMap[b], c.planeSide[b], a);
-        else k_tgt_plane_tma<1, 5><<<g, kPlaneThreads, c.planeSmem, c.stream>>>(c.planeMap[b], c.planeSide[b], a);
+        if (mode == 0) k_tgt_plane_tma<0, 5><<<g, kPlaneThreads, c.planeSmem, c.stream>>>(c.planeMap[b], c.planeSide[b], c.planeR, a);
+        else k_tgt_plane_tma<1, 5><<<g, kPlaneThreads, c.planeSmem, c.stream>>>(c.planeMap[b], c.planeSide[b], c.planeR, a);
     } else {
-        if (mode == 0) k_tgt_plane_tma<0, 11><<<g, kPlaneThreads, c.planeSmem, c.stream>>>(c.planeMap[b], c.planeSide[b], a);
-        else k_tgt_plane_tma<1, 11><<<g, kPlaneThreads, c.planeSmem, c.stream>>>(c.planeMap[b], c.planeSide[b], a);
+        if (mode == 0) k_tgt_plane_tma<0, 11><<<g, kPlaneThreads, c.planeSmem, c.stream>>>(c.planeMap[b], c.planeSide[b], c.planeR, a);
+        else k_tgt_plane_tma<1, 11><<<g, kPlaneThreads, c.planeSmem, c.stream>>>(c.planeMap[b], c.planeSide[b], c.planeR, a);
     }
 }
 

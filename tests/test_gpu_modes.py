@@ -348,7 +348,8 @@ def test_plane_streaming_stencils_match_column_kernels(kind):
     the TMA (k_tgt_plane_tma) compute the same bits as the column kernels
     (k_tgt_sweep, k_tgt_residual): three mixed-mode steps with each, fields
     bitwise equal, equal V-cycle counts.  Periodic (TGV), mirror (LDC) and
-    mixed (RBC: PPN) faces; SARAS_PLANE_TMA=0 selects the column kernels."""
+    mixed (RBC: PPN) faces; SARAS_PLANE_TMA=1 selects the TMA kernels (the
+    column kernels are the default)."""
     import os
     mk = {"tgv": C.tgv, "ldc": C.ldc, "rbc": C.rbc}[kind]
     out = {}
@@ -361,10 +362,10 @@ def test_plane_streaming_stencils_match_column_kernels(kind):
         p.fastKernels = 2
         p.smoother = F.SMOOTHER_CHEBYSHEV
         old = os.environ.get("SARAS_PLANE_TMA")
-        if not tma:
-            os.environ["SARAS_PLANE_TMA"] = "0"
+        os.environ["SARAS_PLANE_TMA"] = "1" if tma else "0"
         try:
             g = S.Solver(p)
+            assert g.plane_tma_active() == tma
         finally:
             if old is None:
                 os.environ.pop("SARAS_PLANE_TMA", None)
