@@ -164,6 +164,11 @@ int saras_destroy(saras_ctx *ctx);
 const char *saras_last_error(const saras_ctx *ctx);
 /* Padded extents (n+2 per axis) of a field. */
 int saras_field_dims(const saras_ctx *ctx, int field, int dims[3]);
+/* Coordinates along axis (0 x, 1 y, 2 z) of the staggered (staggered = 1,
+ * xStaggr: n+1 core points) or collocated (0, xColloc: n core points) grid,
+ * ghosts included: out[0] is index -1 (grid.cc:370-403, 442-519).  count
+ * receives the number written (core points + 2); out may be NULL to query it. */
+int saras_grid_coords(const saras_ctx *ctx, int axis, int staggered, double *out, int capacity, int *count);
 int saras_upload(saras_ctx *ctx, int field, const double *host);
 int saras_download(saras_ctx *ctx, int field, double *host);
 /* Several fields at once (n <= SARAS_NUM_FIELDS): the copies run concurrently

@@ -140,6 +140,33 @@ struct Grid {
         for (int i = -1; i < cy + 1; i++) yColloc(i) = yLen * (et(i) + et(i + 1)) / 2.0;
         for (int i = -1; i < sz + 1; i++) zStaggr(i) = zLen * zt(i);
         for (int i = -1; i < cz + 1; i++) zColloc(i) = zLen * (zt(i) + zt(i + 1)) / 2.0;
+        // grid.cc:117-131 with createTanHypGrid (grid.cc:442-519): on the axes
+        // whose mesh type is 'D' (xGrid = 2) the core coordinates and metrics
+        // are replaced by the double-sided tangent-hyperbolic map; the ghost
+        // entries keep their uniform values.
+        const int gtype[3] = {p.xGrid, p.yGrid, p.zGrid};
+        const double beta[3] = {p.betaX, p.betaY, p.betaZ};
+        const A1 *tc[3] = {&xi, &et, &zt};
+        A1 *sco[3] = {&xStaggr, &yStaggr, &zStaggr}, *cco[3] = {&xColloc, &yColloc, &zColloc};
+        for (int d = 0; d < 3; ++d) {
+            if (gtype[d] != 2) continue;
+            const double b = beta[d], Ld = L[d];
+            const A1 &t = *tc[d];
+            auto metrics = [&](A1 *const m[3], int i, double x) {
+                (*m[0])(i) = std::tanh(b) / (b * Ld * (1.0 - std::pow((1.0 - 2.0 * x / Ld) * std::tanh(b), 2)));
+                (*m[1])(i) = -4.0 * std::pow(std::tanh(b), 3) * (1.0 - 2.0 * x / Ld) /
+                             (b * Ld * Ld * std::pow(1.0 - std::pow(std::tanh(b) * (1.0 - 2.0 * x / Ld), 2), 2));
+                (*m[2])(i) = std::pow((*m[0])(i), 2.0);
+            };
+            for (int i = 0; i < sc[d]; i++) {
+                (*sco[d])(i) = Ld * (1.0 - std::tanh(b * (1.0 - 2.0 * t(i))) / std::tanh(b)) / 2.0;
+                metrics(stg[d], i, (*sco[d])(i));
+            }
+            for (int i = 0; i < cc[d]; i++) {
+                (*cco[d])(i) = Ld * (1.0 - std::tanh(b * (1.0 - (t(i) + t(i + 1)))) / std::tanh(b)) / 2.0;
+                metrics(col[d], i, (*cco[d])(i));
+            }
+        }
     }
 };
 

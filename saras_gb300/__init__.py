@@ -113,6 +113,14 @@ class Solver:
         self._chk(self.lib.saras_field_dims(self.h, field, d))
         return tuple(d)
 
+    def grid_coords(self, axis, staggered):
+        """The library's coordinates along `axis` (ghosts included, index -1 first)."""
+        n = ctypes.c_int()
+        self._chk(self.lib.saras_grid_coords(self.h, axis, 1 if staggered else 0, None, 0, ctypes.byref(n)))
+        a = np.empty(n.value)
+        self._chk(self.lib.saras_grid_coords(self.h, axis, 1 if staggered else 0, _dp(a), n.value, ctypes.byref(n)))
+        return a
+
     def get(self, field):
         a = np.empty(self.dims(field), dtype=np.float64)
         self._chk(self.lib.saras_download(self.h, field, _dp(a)))
@@ -392,14 +400,22 @@ def conv3d_check(mode, x_bits, dy_bits, w, bias, relu, dims, cin, cout):
 # ---------------------------------------------------------------- initial conditions
 def grid_coords(params):
     """Vertex ("staggered") and cell ("collocated") coordinates including the
-    pads, grid.cc:370-403: xStaggr(i) = L*i*dXi, xColloc(i) = L*(xi(i)+xi(i+1))/2."""
+    pads, grid.cc:370-403: xStaggr(i) = L*i*dXi, xColloc(i) = L*(xi(i)+xi(i+1))/2;
+    on an axis with mesh type 'D' the core points follow the double-sided
+    tangent-hyperbolic map of grid.cc:442-519 (numpy's tanh: these arrays build
+    initial conditions; the solver's own coordinates are Solver.grid_coords)."""
     out = []
-    for ind, L in ((params.xInd, params.Lx), (params.yInd, params.Ly), (params.zInd, params.Lz)):
+    for ind, L, gt, beta in ((params.xInd, params.Lx, params.xGrid, params.betaX), (params.yInd, params.Ly, params.yGrid, params.betaY),
+                             (params.zInd, params.Lz, params.zGrid, params.betaZ)):
         n = 2 ** ind
         d = 1.0 / n
         xi = np.arange(-1, n + 2, dtype=np.float64) * d
         xs = L * xi
         xc = L * (xi[:-1] + xi[1:]) / 2.0
+        if gt == 2:
+            t = np.tanh(beta)
+            xs[1:n + 2] = L * (1.0 - np.tanh(beta * (1.0 - 2.0 * xi[1:n + 2])) / t) / 2.0
+            xc[1:n + 1] = L * (1.0 - np.tanh(beta * (1.0 - (xi[1:n + 1] + xi[2:n + 2]))) / t) / 2.0
         out.append((xs, xc))
     return out
 
@@ -466,7 +482,15 @@ def taylor_green_velocity(params):
     """taylorGreen::initializeField (lib/initial/taylorGreen.cc:54-100) over the padded arrays:
     u = sin(2 pi x / L) cos(2 pi y / L) cos(2 pi z / L), v = -cos sin cos.  Vertex
     coordinates are x_i = L i / n and face coordinates L (i + 1/2) / n (i from -1),
-    so every factor is sin or cos of pi q / n for an integer q (correctly rounded)."""
+    so every factor is sin or cos of pi q / n for an integer q (correctly rounded).
+    On a stretched mesh the factors are numpy's sin and cos of the coordinates
+    of grid_coords."""
+    if params.xGrid == 2 or params.yGrid == 2 or params.zGrid == 2:
+        (xs, xc), (ys, yc), (zs, zc) = grid_coords(params)
+        w = [2.0 * np.pi / params.Lx, 2.0 * np.pi / params.Ly, 2.0 * np.pi / params.Lz]
+        Vx = np.sin(w[0] * xc)[:, None, None] * np.cos(w[1] * ys)[None, :, None] * np.cos(w[2] * zs)[None, None, :]
+        Vy = -np.cos(w[0] * xs)[:, None, None] * np.sin(w[1] * yc)[None, :, None] * np.cos(w[2] * zs)[None, None, :]
+        return Vx, Vy
     n = [2 ** params.xInd, 2 ** params.yInd, 2 ** params.zInd]
     vs = [2 * np.arange(-1, m + 2, dtype=np.int64) for m in n]        # 2 pi x_i / L = pi (2 i) / n
     fc = [2 * np.arange(-1, m + 1, dtype=np.int64) + 1 for m in n]    # 2 pi x_(i+1/2) / L = pi (2 i + 1) / n

@@ -130,6 +130,7 @@ def load():
         "saras_destroy": (_I, [vp]),
         "saras_last_error": (cp, [vp]),
         "saras_field_dims": (_I, [vp, _I, ip]),
+        "saras_grid_coords": (_I, [vp, _I, _I, dp, _I, ip]),
         "saras_upload": (_I, [vp, _I, dp]),
         "saras_download": (_I, [vp, _I, dp]),
         "saras_upload_fields": (_I, [vp, _I, ip, ctypes.POINTER(dp)]),

@@ -17,8 +17,10 @@ DRIVER = os.path.join(OUT, "saras_gb300_run")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # --fmad=false: the FP64 kernels must round every product and sum exactly as
 # the reference expressions do (kernels that want fused multiply-adds call
-# fma() explicitly).
+# fma() explicitly); -ffp-contract=off does the same for the host code (grid
+# metrics), which Arm compilers would otherwise contract.
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
+          "-Xcompiler", "-ffp-contract=off",
           "--expt-relaxed-constexpr"]
 UNITS = ["capi.cu", "fields.cu", "multigrid.cu", "unet.cu"]
 

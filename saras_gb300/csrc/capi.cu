@@ -281,7 +281,21 @@ static int validate(const saras_params *p, std::string &why) {
     if (p->vcDepth < 1) { why = "V-Cycle Depth must be >= 1"; return SARAS_BAD_CONFIG; }
     int coarsest = (int)std::pow(2, p->vcDepth + 1);
     if ((1 << p->xInd) < coarsest || (1 << p->yInd) < coarsest || (1 << p->zInd) < coarsest) { why = "grid too coarse for the V-Cycle depth"; return SARAS_BAD_CONFIG; }
-    if (p->xGrid || p->yGrid || p->zGrid) { why = "only uniform meshes (Mesh Type UUU) are supported"; return SARAS_BAD_CONFIG; }
+    if (p->xGrid < 0 || p->xGrid > 2 || p->yGrid < 0 || p->yGrid > 2 || p->zGrid < 0 || p->zGrid > 2) { why = "bad grid type"; return SARAS_BAD_CONFIG; }
+    // Mesh Type 'D' (double-sided tangent-hyperbolic stretching, grid.cc:442-519)
+    // runs in the drop-in mode: the reference's multigrid and FP64 kernels read
+    // the metric arrays at every point; the GB300 extensions assume uniform
+    // metrics.  ('S', single-sided, builds a uniform grid in the reference,
+    // grid.cc:117-131, and does here.)
+    const bool stretched = p->xGrid == 2 || p->yGrid == 2 || p->zGrid == 2;
+    if (stretched && (p->mgMode != SARAS_MG_REFERENCE || p->fastKernels != 0 || p->guessMode != SARAS_GUESS_PREVIOUS || p->testPoisson)) {
+        why = "stretched meshes (Mesh Type 'D') run in the drop-in mode only: Multigrid Mode 0, Fast Kernels 0, Guess Mode 0, no Test Poisson";
+        return SARAS_BAD_CONFIG;
+    }
+    if ((p->xGrid == 2 && !(p->betaX > 0)) || (p->yGrid == 2 && !(p->betaY > 0)) || (p->zGrid == 2 && !(p->betaZ > 0))) {
+        why = "the Beta of a stretched axis must be positive";
+        return SARAS_BAD_CONFIG;
+    }
     if (p->dScheme != 1) { why = "Undefined finite differencing scheme"; return SARAS_BAD_CONFIG; }
     if (p->gsSmooth < 0 || p->gsSmooth > 1) { why = "Smoothing Method must be 0 (Jacobi) or 1 (Gauss-Seidel)"; return SARAS_BAD_CONFIG; }
     if (p->nonHgBC) { why = "heating-plate boundary condition is not supported"; return SARAS_BAD_CONFIG; }
@@ -355,7 +369,7 @@ int saras_destroy(saras_ctx *h) {
     mg_free(c);
     for (int f = 0; f < SARAS_NUM_FIELDS; ++f) cudaFree(c.f[f]);
     for (int q = 0; q < 4; ++q) cudaFree(c.scratch[q]);
-    cudaFree(c.red); cudaFree(c.dscal); cudaFree(c.dflag);
+    cudaFree(c.red); cudaFree(c.dscal); cudaFree(c.dflag); cudaFree(c.dmet);
     if (c.hscal) cudaFreeHost(c.hscal);
     for (int q = 0; q < 3; ++q) cudaFree(c.pHist[q]);
     cudaFree(c.cnp);
@@ -383,6 +397,16 @@ static long field_count(const Ctx &c, int f) {
 int saras_field_dims(const saras_ctx *h, int field, int dims[3]) {
     if (!h || !dims || field < 0 || field >= SARAS_NUM_FIELDS) return SARAS_BAD_ARG;
     for (int d = 0; d < 3; ++d) dims[d] = h->c.info[field].n[d] + 2;
+    return SARAS_OK;
+}
+
+int saras_grid_coords(const saras_ctx *h, int axis, int staggered, double *out, int capacity, int *count) {
+    if (!h || axis < 0 || axis > 2 || !count) return SARAS_BAD_ARG;
+    const std::vector<double> &x = h->c.hcoord[axis][staggered ? 1 : 0];
+    *count = (int)x.size();
+    if (!out) return SARAS_OK;
+    if (capacity < (int)x.size()) return SARAS_BAD_ARG;
+    std::memcpy(out, x.data(), sizeof(double) * x.size());
     return SARAS_OK;
 }
 
@@ -491,6 +515,7 @@ int saras_mg_solve(saras_ctx *h, int *vcycles, double *residual) {
 int saras_mg_set_mode(saras_ctx *h, int mode, double target, int max_cycles) {
     CTX_OR_FAIL(h);
     if (mode < 0 || mode > 2 || !(target > 0) || max_cycles < 1) return SARAS_BAD_ARG;
+    if (h->c.stretched && mode != SARAS_MG_REFERENCE) { set_error("stretched meshes run the reference multigrid only"); return SARAS_BAD_CONFIG; }
     h->c.mgMode = mode; h->c.mgTarget = target; h->c.mgMaxCycles = max_cycles;
     h->c.p.mgMode = mode; h->c.p.mgTarget = target; h->c.p.mgMaxCycles = max_cycles;
     return SARAS_OK;
@@ -751,6 +776,7 @@ int saras_unet_infer(saras_ctx *h, int field_out) {
 int saras_set_guess_mode(saras_ctx *h, int mode) {
     CTX_OR_FAIL(h);
     if (mode < SARAS_GUESS_PREVIOUS || mode > SARAS_GUESS_NETWORK) return SARAS_BAD_ARG;
+    if (h->c.stretched && mode != SARAS_GUESS_PREVIOUS) { set_error("stretched meshes take the previous pressure as the guess"); return SARAS_BAD_CONFIG; }
     h->c.guessMode = mode;
     return SARAS_OK;
 }

@@ -62,6 +62,10 @@ struct Level {
     double cx, cy, cz, c7, den;      // smoother: hyhz*xix2, hzhx*ety2, hxhy*ztz2, 2*hxhyhz, 4*(...)
     double lx, ly, lz;               // residual: xix2/(hx*hx) folded as products with 1/(hx*hx)
     double ihx2, ihy2, ihz2;         // 1/(hx*hx) (exact powers of two)
+    // stretched meshes: the level's staggered metrics xix2, xixx, ety2, etyy,
+    // ztz2, ztzz (poisson.cc:463-495), device pointers at index 0
+    double *metBlock = nullptr;
+    const double *xix2 = nullptr, *xixx = nullptr, *ety2 = nullptr, *etyy = nullptr, *ztz2 = nullptr, *ztzz = nullptr;
     double *pa() const { return cur == 0 ? a : b; }
     double *pb() const { return cur == 0 ? b : a; }
     float *pa32() const { return cur32 == 0 ? a32 : b32; }
@@ -84,10 +88,19 @@ struct Ctx {
     cudaStream_t copyStream[SARAS_NUM_FIELDS] = {};   // saras_upload_fields / saras_download_fields
     cudaEvent_t copyEvent[SARAS_NUM_FIELDS + 1] = {};
     bool scalar = false;
-    // grid (grid.cc:59-136, uniform)
+    // grid (grid.cc:59-136)
     int Ns[3], Nc[3];
     double dXi[3], ih[3], ih2[3], L[3];
-    double m1[3], m2[3];           // xi_x (=1/L) and xix2 (=pow(1/L,2))
+    double m1[3], m2[3];           // uniform metrics xi_x (=1/L) and xix2 (=pow(1/L,2))
+    // Coordinates and metrics of every axis d at the collocated (s = 0) and the
+    // staggered (s = 1) points, kind 0 xi_x, 1 xixx, 2 xix2 (grid.cc:290-320,
+    // 370-422, 442-519): uniform values everywhere, the tangent-hyperbolic map
+    // on the core of a stretched axis.  Host arrays start at index -1; device
+    // pointers point at index 0.
+    bool stretched = false;        // some axis has Mesh Type 'D'
+    std::vector<double> hmet[3][2][3], hcoord[3][2];
+    double *dmet = nullptr;
+    const double *met[3][2][3] = {};
     double inverseRe, nu, kappa, Fb, dt;
     double hx2hy2, hy2hz2, hz2hx2, hx2hy2hz2;
     int maxIterations;

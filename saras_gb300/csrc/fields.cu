@@ -5,12 +5,14 @@
 // reference writes it (no fused multiply-add contraction), which is what keeps
 // the plain path within 1e-10 of the reference's CPU arithmetic.
 //
-// Uniform grids (Mesh Type "UUU", the only meshes in scope) make every metric
-// array a constant: xi_x = 1/L, xix2 = pow(1/L, 2), xixx = 0 (grid.cc:405-421).
-// Terms multiplied by xixx (= 0) are therefore omitted; the remaining
-// operations keep the reference's evaluation order.  Divisions by the grid
-// spacings dXi = 2^-n and by hx*hx are exact power-of-two scalings and are
-// applied as multiplications by the exact reciprocals.
+// Uniform grids make every metric array a constant: xi_x = 1/L, xix2 =
+// pow(1/L, 2), xixx = 0 (grid.cc:405-421).  Terms multiplied by xixx (= 0) are
+// therefore omitted there; the remaining operations keep the reference's
+// evaluation order.  On a stretched mesh (Mesh Type 'D' on some axis, the
+// drop-in mode only) the reference-form kernels read the metric arrays at each
+// point and evaluate the full expressions, xixx terms included.  Divisions by
+// the grid spacings dXi = 2^-n and by hx*hx are exact power-of-two scalings and
+// are applied as multiplications by the exact reciprocals.
 
 #include <atomic>
 #include <cmath>
@@ -30,24 +32,44 @@ struct CnDf {
     fpair invDn;     // 1 / Dn
 };
 
-struct UC {                 // uniform-grid stencil constants
+struct UC {                 // stencil constants of one field
     double ih[3], ih2[3];   // 1/dXi and pow(1/dXi, 2)                 (derivative.cc:67-69)
+    double h[3];            // dXi, dEt, dZt
     double m1[3];           // first-derivative metric xi_x = 1/L        (derivative.cc:77-105)
     double m2h[3];          // 0.5*xix2 (iScheme 1) or xix2              (derivative.cc:185-189)
     double gm[3];           // gradient / divergence metric 1/L          (sfield.cc:166-170)
+    // stretched meshes (var != 0): the field's metric arrays along each axis
+    // (x_Metric, xxMetric, x2Metric of derivative.cc:77-105), the collocated
+    // xi_x of the gradient (sfield.cc:155-171) and the staggered xi_x of the
+    // divergence (vfield.cc:299-320)
+    const double *m1p[3], *mxp[3], *m2p[3], *gcp[3], *gsp[3];
+    int var, half;          // half: iScheme 1 (the 0.5 of calcDerivative2xx)
 };
 
-static UC make_uc(const Ctx &c) {
+static UC make_uc(const Ctx &c, int field) {
     UC u;
+    const FieldInfo &f = c.info[field];
     for (int d = 0; d < 3; ++d) {
         u.ih[d] = c.ih[d];
         u.ih2[d] = c.ih2[d];
+        u.h[d] = c.dXi[d];
         u.m1[d] = c.m1[d];
         u.m2h[d] = (c.p.iScheme == 1) ? 0.5 * c.m2[d] : c.m2[d];
         u.gm[d] = c.m1[d];
+        const int st = f.stag[d] ? 1 : 0;
+        u.m1p[d] = c.met[d][st][0];
+        u.mxp[d] = c.met[d][st][1];
+        u.m2p[d] = c.met[d][st][2];
+        u.gcp[d] = c.met[d][0][0];
+        u.gsp[d] = c.met[d][1][0];
     }
+    u.var = c.stretched ? 1 : 0;
+    u.half = c.p.iScheme == 1 ? 1 : 0;
     return u;
 }
+
+// metric of axis d at the point (i, j, k)
+__device__ __forceinline__ double at_axis(const double *m, int d, int i, int j, int k) { return m[d == 0 ? i : d == 1 ? j : k]; }
 
 template <typename T>
 __device__ __forceinline__ void nbr(const View3<T> &F, int d, int i, int j, int k, double &fm, double &fp) {
@@ -56,21 +78,28 @@ __device__ __forceinline__ void nbr(const View3<T> &F, int d, int i, int j, int 
     else { fm = F(i, j, k - 1); fp = F(i, j, k + 1); }
 }
 
-// derivative::calcDerivative2xx (derivative.cc:178-191), uniform grid:
-//   out = central22n(F)*ihx2;  result = 0.5*x2Metric*out
+// derivative::calcDerivative2xx (derivative.cc:178-191):
+//   tmp = central12n(F)*ihx;  out = central22n(F)*ihx2;
+//   result = xxMetric*tmp + 0.5*x2Metric*out   (uniform grid: 0.5*x2Metric*out)
 __device__ __forceinline__ double d2_at(const View3<const double> &F, int d, int i, int j, int k, const UC &u) {
     double fm, fp, f0 = F(i, j, k);
     nbr(F, d, i, j, k, fm, fp);
     double out = (fm - 2.0 * f0 + fp) * u.ih2[d];
-    return u.m2h[d] * out;
+    if (!u.var) return u.m2h[d] * out;
+    const double tmp = ((fp - fm) * 0.5) * u.ih[d];
+    const double x2 = at_axis(u.m2p[d], d, i, j, k);
+    return at_axis(u.mxp[d], d, i, j, k) * tmp + (u.half ? 0.5 * x2 * out : x2 * out);
 }
 // derivative::calcDerivative1_x (derivative.cc:121-126): x_Metric*(central12n(F)*ihx)
 __device__ __forceinline__ double d1_at(const View3<const double> &F, int d, int i, int j, int k, const UC &u) {
     double fm, fp;
     nbr(F, d, i, j, k, fm, fp);
     double t = ((fp - fm) * 0.5) * u.ih[d];
-    return u.m1[d] * t;
+    return (u.var ? at_axis(u.m1p[d], d, i, j, k) : u.m1[d]) * t;
 }
+// gradient metric (collocated xi_x along axis C) and divergence metric (staggered xi_x along d)
+__device__ __forceinline__ double grad_m(const UC &u, int C, int i, int j, int k) { return u.var ? at_axis(u.gcp[C], C, i, j, k) : u.gm[C]; }
+__device__ __forceinline__ double div_m(const UC &u, int d, int i, int j, int k) { return u.var ? at_axis(u.gsp[d], d, i, j, k) : u.gm[d]; }
 
 // Interpolation slices (field.cc:309-575): interTemp(core) accumulated in
 // slice order.  T = 0,1,2: target Vx, Vy, Vz;  T = 3: vertex field (P, T).
@@ -203,7 +232,7 @@ __global__ void k_gradient(View3<double> G, View3<const double> S, Box b, UC u) 
     int i, j, k;
     if (!box_point(b, i, j, k)) return;
     double sp = C == 0 ? S(i + 1, j, k) : C == 1 ? S(i, j + 1, k) : S(i, j, k + 1);
-    G(i, j, k) = (u.gm[C] * (sp - S(i, j, k))) * u.ih[C];
+    G(i, j, k) = (grad_m(u, C, i, j, k) * (sp - S(i, j, k))) * u.ih[C];
 }
 
 // vfield::divergence (vfield.cc:299-320), then optionally mgRHS *= 1/dt
@@ -230,9 +259,9 @@ __global__ void k_divergence(View3<double> D, Vel V, Box full, UC u, double scal
             D(i, j, k) = fma(fk.k[0], dx, fma(fk.k[1], dy, fk.k[2] * dz));
             return;
         }
-        double tx = (u.gm[0] * dx) * u.ih[0];
-        double ty = (u.gm[1] * dy) * u.ih[1];
-        double tz = (u.gm[2] * dz) * u.ih[2];
+        double tx = (div_m(u, 0, i, j, k) * dx) * u.ih[0];
+        double ty = (div_m(u, 1, i, j, k) * dy) * u.ih[1];
+        double tz = (div_m(u, 2, i, j, k) * dz) * u.ih[2];
         out = tx + ty + tz;
     }
     if (do_scale) out = out * scale;
@@ -315,7 +344,7 @@ __global__ void k_rhs(RhsArgs a) {
         h = h + a.Fb * t;
     }
     double sp = C == 0 ? a.P(i + 1, j, k) : C == 1 ? a.P(i, j + 1, k) : a.P(i, j, k + 1);
-    double g = (u.gm[C] * (sp - a.P(i, j, k))) * u.ih[C];
+    double g = (grad_m(u, C, i, j, k) * (sp - a.P(i, j, k))) * u.ih[C];
     h = h - g;
     h = h * a.dt;
     h = h + a.F(i, j, k);
@@ -598,14 +627,27 @@ struct CnArgs {
     double resCoef;          // inverseRe (hydro) or nu / kappa (scalar)
     int withResidual;
     double *resMax;
+    // stretched meshes: the metrics of the component at each index (mx(i),
+    // my(j), mz(k) of hydro_d3.cc:378-400), so c1..c3, B, Dn and lx..lz are
+    // formed per point from hy2hz2, hz2hx2, hx2hy2, h3 = hx2hy2hz2, Re, ihx2..ihz2
+    const double *mx, *my, *mz;
+    double hy2hz2, hz2hx2, hx2hy2, h3, Re, ihx2, ihy2, ihz2;
+    int var;
 };
 
 __device__ __forceinline__ double cn_guess(const CnArgs &a, int i, int j, int k) {
     const View3<const double> &V = a.in;
-    double A = a.c1 * (V(i + 1, j, k) + V(i - 1, j, k)) + a.c2 * (V(i, j + 1, k) + V(i, j - 1, k)) +
-               a.c3 * (V(i, j, k + 1) + V(i, j, k - 1));
+    double c1 = a.c1, c2 = a.c2, c3 = a.c3, Dn = a.Dn;
+    if (a.var) {
+        c1 = a.hy2hz2 * a.mx[i];
+        c2 = a.hz2hx2 * a.my[j];
+        c3 = a.hx2hy2 * a.mz[k];
+        const double B = c1 + c2 + c3;
+        Dn = a.scalarForm ? 1.0 + a.dt * a.coef * B / a.h3 : 1.0 + a.dt * B / (a.Re * a.h3);
+    }
+    double A = c1 * (V(i + 1, j, k) + V(i - 1, j, k)) + c2 * (V(i, j + 1, k) + V(i, j - 1, k)) + c3 * (V(i, j, k + 1) + V(i, j, k - 1));
     double num = a.scalarForm ? (A * a.dt) * a.coef / a.X : (A * a.dt) / a.X;
-    return (num + a.rhs(i, j, k)) / a.Dn;
+    return (num + a.rhs(i, j, k)) / Dn;
 }
 
 __global__ void k_cn(CnArgs a) {
@@ -618,9 +660,15 @@ __global__ void k_cn(CnArgs a) {
             if (a.withResidual) {
                 const View3<const double> &V = a.in;
                 double v0 = V(i, j, k);
-                double L = (a.lx * (V(i + 1, j, k) - 2.0 * v0 + V(i - 1, j, k))) +
-                           (a.ly * (V(i, j + 1, k) - 2.0 * v0 + V(i, j - 1, k))) +
-                           (a.lz * (V(i, j, k + 1) - 2.0 * v0 + V(i, j, k - 1)));
+                double L;
+                if (a.var)
+                    L = (a.mx[i] * (V(i + 1, j, k) - 2.0 * v0 + V(i - 1, j, k))) * a.ihx2 +
+                        (a.my[j] * (V(i, j + 1, k) - 2.0 * v0 + V(i, j - 1, k))) * a.ihy2 +
+                        (a.mz[k] * (V(i, j, k + 1) - 2.0 * v0 + V(i, j, k - 1))) * a.ihz2;
+                else
+                    L = (a.lx * (V(i + 1, j, k) - 2.0 * v0 + V(i - 1, j, k))) +
+                        (a.ly * (V(i, j + 1, k) - 2.0 * v0 + V(i, j - 1, k))) +
+                        (a.lz * (V(i, j, k + 1) - 2.0 * v0 + V(i, j, k - 1)));
                 double val = v0 - L * 0.5 * a.dt * a.resCoef;
                 res = fabs(val - a.rhs(i, j, k));
                 if (res != res) res = INFINITY;   // a NaN residual never converges
@@ -931,7 +979,7 @@ __global__ void k_project(View3<double> out, View3<const double> in, View3<const
         if (x >= 0 && y >= 0 && z >= 0 && x < in.n[0] && y < in.n[1] && z < in.n[2]) {
             double sp = C == 0 ? Pp(x + 1, y, z) : C == 1 ? Pp(x, y + 1, z) : Pp(x, y, z + 1);
             if (FAST) return fma(-fastDt, sp - Pp(x, y, z), v);
-            double g = (u.gm[C] * (sp - Pp(x, y, z))) * u.ih[C];
+            double g = (grad_m(u, C, x, y, z) * (sp - Pp(x, y, z))) * u.ih[C];
             v = v - g * dt;
         }
         return v;
@@ -1017,12 +1065,14 @@ __global__ void k_diag(Vel V, View3<const double> T, int has_t, int nP0, int nP1
         double a = (V.v[0](i - 1, j, k) + V.v[0](i, j, k)) / 2.0;
         double b = (V.v[1](i, j - 1, k) + V.v[1](i, j, k)) / 2.0;
         double c = (V.v[2](i, j, k - 1) + V.v[2](i, j, k)) / 2.0;
-        e += (a * a + b * b + c * c) * dv;
-        if (has_t) w += ((V.v[2](i, j, k) + V.v[2](i, j, k - 1)) / 2.0) * T(i, j, k) * dv;
+        // tseries.cc:150-165: the cell volume from the collocated metrics
+        const double dvp = u.var ? (u.h[0] / u.gcp[0][i]) * (u.h[1] / u.gcp[1][j]) * (u.h[2] / u.gcp[2][k]) : dv;
+        e += (a * a + b * b + c * c) * dvp;
+        if (has_t) w += ((V.v[2](i, j, k) + V.v[2](i, j, k - 1)) / 2.0) * T(i, j, k) * dvp;
         if (i < nc0 && j < nc1 && k < nc2) {
-            double tx = (u.gm[0] * (V.v[0](i, j, k) - V.v[0](i - 1, j, k))) * u.ih[0];
-            double ty = (u.gm[1] * (V.v[1](i, j, k) - V.v[1](i, j - 1, k))) * u.ih[1];
-            double tz = (u.gm[2] * (V.v[2](i, j, k) - V.v[2](i, j, k - 1))) * u.ih[2];
+            double tx = (div_m(u, 0, i, j, k) * (V.v[0](i, j, k) - V.v[0](i - 1, j, k))) * u.ih[0];
+            double ty = (div_m(u, 1, i, j, k) * (V.v[1](i, j, k) - V.v[1](i, j - 1, k))) * u.ih[1];
+            double tz = (div_m(u, 2, i, j, k) * (V.v[2](i, j, k) - V.v[2](i, j, k - 1))) * u.ih[2];
             dmax = fmax(dmax, tx + ty + tz);
         }
     }
@@ -1165,6 +1215,60 @@ static void set_field_info(Ctx &c, int field, bool xs, bool ys, bool zs) {
     for (int d = 0; d < 3; ++d) { f.sync.blo[d] = 0; f.sync.bhi[d] = f.n[d] - 1; }
 }
 
+// Coordinates and metrics (grid.cc:290-320 defaults, createUniformGrid
+// grid.cc:370-422, createTanHypGrid grid.cc:442-519): every axis is first
+// uniform over its whole padded range; an axis with Mesh Type 'D' (xGrid = 2)
+// then gets the double-sided tangent-hyperbolic map, with stretching factor
+// "X/Y/Z Beta", on its core points (ghost entries keep the uniform values).
+// The expressions are the reference's, so host code computing them must not
+// contract multiplies and adds (the library is built with -ffp-contract=off).
+static int grid_metrics(Ctx &c) {
+    const saras_params &p = c.p;
+    const int gtype[3] = {p.xGrid, p.yGrid, p.zGrid};
+    const double beta[3] = {p.betaX, p.betaY, p.betaZ};
+    c.stretched = false;
+    size_t total = 0;
+    for (int d = 0; d < 3; ++d) {
+        const double Ld = c.L[d];
+        const int n[2] = {c.Nc[d], c.Ns[d]};   // core counts: collocated, staggered
+        auto xi = [&](int i) { return double(i) * c.dXi[d]; };   // grid.cc:333-352
+        for (int st = 0; st < 2; ++st) {
+            const int len = n[st] + 2;   // indices -1 .. n
+            for (int m = 0; m < 3; ++m) c.hmet[d][st][m].assign(len, m == 0 ? c.m1[d] : m == 1 ? 0.0 : c.m2[d]);
+            c.hcoord[d][st].assign(len, 0.0);
+            for (int i = -1; i < n[st] + 1; ++i)
+                c.hcoord[d][st][i + 1] = st ? Ld * xi(i) : Ld * (xi(i) + xi(i + 1)) / 2.0;
+            total += 3 * (size_t)len;
+        }
+        if (gtype[d] != 2) continue;
+        c.stretched = true;
+        const double b = beta[d];
+        for (int st = 0; st < 2; ++st) {
+            for (int i = 0; i < n[st]; ++i) {
+                const double x = st ? Ld * (1.0 - std::tanh(b * (1.0 - 2.0 * xi(i))) / std::tanh(b)) / 2.0
+                                    : Ld * (1.0 - std::tanh(b * (1.0 - (xi(i) + xi(i + 1)))) / std::tanh(b)) / 2.0;
+                c.hcoord[d][st][i + 1] = x;
+                const double m1 = std::tanh(b) / (b * Ld * (1.0 - std::pow((1.0 - 2.0 * x / Ld) * std::tanh(b), 2)));
+                c.hmet[d][st][0][i + 1] = m1;
+                c.hmet[d][st][1][i + 1] = -4.0 * std::pow(std::tanh(b), 3) * (1.0 - 2.0 * x / Ld) /
+                                          (b * Ld * Ld * std::pow(1.0 - std::pow(std::tanh(b) * (1.0 - 2.0 * x / Ld), 2), 2));
+                c.hmet[d][st][2][i + 1] = std::pow(m1, 2.0);
+            }
+        }
+    }
+    SARAS_CUDA_TRY(cudaMalloc(&c.dmet, sizeof(double) * total));
+    size_t off = 0;
+    for (int d = 0; d < 3; ++d)
+        for (int st = 0; st < 2; ++st)
+            for (int m = 0; m < 3; ++m) {
+                const std::vector<double> &h = c.hmet[d][st][m];
+                SARAS_CUDA_TRY(cudaMemcpy(c.dmet + off, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice));
+                c.met[d][st][m] = c.dmet + off + 1;
+                off += h.size();
+            }
+    return SARAS_OK;
+}
+
 int fields_setup(Ctx &c) {
     const saras_params &p = c.p;
     int ind[3] = {p.xInd, p.yInd, p.zInd};
@@ -1194,9 +1298,11 @@ int fields_setup(Ctx &c) {
     c.hy2hz2 = std::pow(c.dXi[1], 2.0) * std::pow(c.dXi[2], 2.0);
     c.hx2hy2hz2 = std::pow(c.dXi[0], 2.0) * std::pow(c.dXi[1], 2.0) * std::pow(c.dXi[2], 2.0);
     c.maxIterations = c.Nc[0] * c.Nc[1] * c.Nc[2];                  // hydro.cc:74
+    if (int e = grid_metrics(c)) return e;
     c.totalVol = 0.0;                                                 // tseries.cc:90-108
+    const double *wx = c.hmet[0][0][0].data() + 1, *wy = c.hmet[1][0][0].data() + 1, *wz = c.hmet[2][0][0].data() + 1;
     for (int iX = 0; iX < c.Ns[0]; iX++) for (int iY = 0; iY < c.Ns[1]; iY++) for (int iZ = 0; iZ < c.Ns[2]; iZ++)
-        c.totalVol += (c.dXi[0] / c.m1[0]) * (c.dXi[1] / c.m1[1]) * (c.dXi[2] / c.m1[2]);
+        c.totalVol += (c.dXi[0] / wx[iX]) * (c.dXi[1] / wy[iY]) * (c.dXi[2] / wz[iZ]);
 
     set_field_info(c, SARAS_FIELD_VX, false, true, true);
     set_field_info(c, SARAS_FIELD_VY, true, false, true);
@@ -1286,8 +1392,8 @@ static Vel make_vel(const Ctx &c) {
 }
 
 int vfield_compute_diff(Ctx &c) {
-    UC u = make_uc(c);
     for (int q = 0; q < 3; ++q) {
+        UC u = make_uc(c, SARAS_FIELD_VX + q);
         Box b = core_box(c.info[SARAS_FIELD_VX + q]);
         dim3 g, bl; box_launch_dims(b, g, bl);
         k_op_diff<<<g, bl, 0, c.stream>>>(mview(c, SARAS_FIELD_NSE_X + q), cview(c, SARAS_FIELD_VX + q), b, u);
@@ -1297,9 +1403,9 @@ int vfield_compute_diff(Ctx &c) {
 }
 
 int vfield_compute_nlin(Ctx &c) {
-    UC u = make_uc(c);
     Vel V = make_vel(c);
     for (int q = 0; q < 3; ++q) {
+        UC u = make_uc(c, SARAS_FIELD_VX + q);
         Box b = core_box(c.info[SARAS_FIELD_VX + q]);
         dim3 g, bl; box_launch_dims(b, g, bl);
         if (q == 0) k_op_nlin<0><<<g, bl, 0, c.stream>>>(mview(c, SARAS_FIELD_NSE_X), cview(c, SARAS_FIELD_VX), V, b, u);
@@ -1312,7 +1418,7 @@ int vfield_compute_nlin(Ctx &c) {
 
 int tfield_compute_diff(Ctx &c) {
     if (!c.scalar) return SARAS_BAD_ARG;
-    UC u = make_uc(c);
+    UC u = make_uc(c, SARAS_FIELD_T);
     Box b = core_box(c.info[SARAS_FIELD_T]);
     dim3 g, bl; box_launch_dims(b, g, bl);
     k_op_diff<<<g, bl, 0, c.stream>>>(mview(c, SARAS_FIELD_TRHS), cview(c, SARAS_FIELD_T), b, u);
@@ -1322,7 +1428,7 @@ int tfield_compute_diff(Ctx &c) {
 
 int tfield_compute_nlin(Ctx &c) {
     if (!c.scalar) return SARAS_BAD_ARG;
-    UC u = make_uc(c);
+    UC u = make_uc(c, SARAS_FIELD_T);
     Box b = core_box(c.info[SARAS_FIELD_T]);
     dim3 g, bl; box_launch_dims(b, g, bl);
     k_op_nlin<3><<<g, bl, 0, c.stream>>>(mview(c, SARAS_FIELD_TRHS), cview(c, SARAS_FIELD_T), make_vel(c), b, u);
@@ -1332,7 +1438,7 @@ int tfield_compute_nlin(Ctx &c) {
 
 int sfield_gradient(Ctx &c, int sf) {
     if (sf != SARAS_FIELD_P && sf != SARAS_FIELD_PP) return SARAS_BAD_ARG;
-    UC u = make_uc(c);
+    UC u = make_uc(c, SARAS_FIELD_P);
     for (int q = 0; q < 3; ++q) {
         Box b = core_box(c.info[SARAS_FIELD_VX + q]);
         dim3 g, bl; box_launch_dims(b, g, bl);
@@ -1346,7 +1452,7 @@ int sfield_gradient(Ctx &c, int sf) {
 }
 
 int vfield_divergence(Ctx &c, double *dst, bool scale_dt) {
-    UC u = make_uc(c);
+    UC u = make_uc(c, SARAS_FIELD_P);
     Box fb = full_box(c.info[SARAS_FIELD_P]);
     dim3 g, bl; box_launch_dims(fb, g, bl);
     View3<double> D = mview_ptr(c, SARAS_FIELD_MGRHS, dst ? dst : c.f[SARAS_FIELD_MGRHS]);
@@ -1416,6 +1522,16 @@ static void cn_setup(Ctx &c, int comp, CnArgs &a, CnFast &fa) {
     a.ly = ety2 * (1.0 / (c.dXi[1] * c.dXi[1]));
     a.lz = ztz2 * (1.0 / (c.dXi[2] * c.dXi[2]));
     a.resMax = c.dscal;
+    // the metrics of the component (hydro_d3.cc:378-400, 433-455, 488-510;
+    // the T solve's ztz2Colloc, scalar_d3.cc:549-571)
+    static const int kSt[4][3] = {{0, 1, 1}, {1, 0, 1}, {1, 1, 0}, {1, 1, 0}};
+    a.mx = c.met[0][kSt[comp][0]][2];
+    a.my = c.met[1][kSt[comp][1]][2];
+    a.mz = c.met[2][kSt[comp][2]][2];
+    a.hy2hz2 = c.hy2hz2; a.hz2hx2 = c.hz2hx2; a.hx2hy2 = c.hx2hy2; a.h3 = c.hx2hy2hz2;
+    a.Re = c.p.Re;
+    a.ihx2 = 1.0 / (c.dXi[0] * c.dXi[0]); a.ihy2 = 1.0 / (c.dXi[1] * c.dXi[1]); a.ihz2 = 1.0 / (c.dXi[2] * c.dXi[2]);
+    a.var = c.stretched ? 1 : 0;
     fa.rhs = a.rhs; fa.prog = a.prog; fa.full = a.full;
     fa.c1 = a.c1; fa.c2 = a.c2; fa.c3 = a.c3;
     fa.k1 = a.scalarForm ? (a.dt * a.coef) / a.X : a.dt / a.X;
@@ -1438,7 +1554,7 @@ static int cnp_ensure(Ctx &c) {
 }
 
 int compute_rhs(Ctx &c) {
-    UC u = make_uc(c);
+    UC u = make_uc(c, SARAS_FIELD_VX);
     RhsArgs a;
     a.V = make_vel(c);
     a.P = cview(c, SARAS_FIELD_P);
@@ -1456,6 +1572,7 @@ int compute_rhs(Ctx &c) {
     for (int q = 0; q < 3; ++q) {
         a.H = mview(c, SARAS_FIELD_NSE_X + q);
         a.F = cview(c, SARAS_FIELD_VX + q);
+        a.u = make_uc(c, SARAS_FIELD_VX + q);
         a.b = core_box(c.info[SARAS_FIELD_VX + q]);
         dim3 g, bl; box_launch_dims(a.b, g, bl);
         if (c.p.fastKernels == 2) {
@@ -1519,7 +1636,7 @@ int compute_rhs(Ctx &c) {
 }
 
 int compute_trhs(Ctx &c) {
-    UC u = make_uc(c);
+    UC u = make_uc(c, SARAS_FIELD_T);
     RhsArgs a;
     a.V = make_vel(c);
     a.u = u;
@@ -1756,7 +1873,7 @@ __global__ void k_add(double *dst, const double *src, long n, int zero_first) {
 }
 
 int project(Ctx &c, bool with_bc) {
-    UC u = make_uc(c);
+    UC u = make_uc(c, SARAS_FIELD_P);
     long nP = make_view<double>(nullptr, c.info[SARAS_FIELD_P].n[0], c.info[SARAS_FIELD_P].n[1], c.info[SARAS_FIELD_P].n[2]).size();
     int blocks = (int)std::min<long>((nP + 255) / 256, 152L * 16);
     k_add<<<blocks, 256, 0, c.stream>>>(c.f[SARAS_FIELD_P], c.f[SARAS_FIELD_PP], nP, c.p.testPoisson ? 1 : 0);
@@ -1808,7 +1925,7 @@ int reduce_sum_partials(Ctx &c, int nparts, double *host_out) {
 }
 
 int diagnostics(Ctx &c, double *energy, double *maxdiv, double *nusselt) {
-    UC u = make_uc(c);
+    UC u = make_uc(c, SARAS_FIELD_P);
     int nb = 152 * 4;
     if (nb > c.redCap) nb = c.redCap;
     double dv = (c.dXi[0] / c.m1[0]) * (c.dXi[1] / c.m1[1]) * (c.dXi[2] / c.m1[2]);
@@ -2132,6 +2249,8 @@ extern "C" int saras_cn_solve_noalloc(const saras_params *p, int component, doub
         else { nu = std::sqrt(p->Pr / p->Ra); kappa = 1.0 / std::sqrt(p->Pr * p->Ra); }
     }
     CnArgs a;
+    a.var = 0;   // uniform meshes only (checked above)
+    a.mx = a.my = a.mz = nullptr;
     {
         View3<double> w = make_view<double>(const_cast<double *>(rhs), f.n[0], f.n[1], f.n[2]);
         a.rhs.p = w.p; a.rhs.n[0] = w.n[0]; a.rhs.n[1] = w.n[1]; a.rhs.n[2] = w.n[2]; a.rhs.sx = w.sx; a.rhs.sy = w.sy;

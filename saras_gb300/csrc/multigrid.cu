@@ -81,6 +81,11 @@ struct MgK {            // level stencil constants
     double cx, cy, cz, c7, den;
     double lx, ly, lz;
     float fcx, fcy, fcz, fc7, fden, flx, fly, flz;
+    // stretched meshes (var != 0, reference mode): the level's metric arrays
+    // (poisson.cc:463-495) and spacings, read at each point
+    const double *xix2, *xixx, *ety2, *etyy, *ztz2, *ztzz;
+    double hx, hy, hz, hxhy, hyhz, hzhx, hxhyhz, ihx2, ihy2, ihz2, i2hx, i2hy, i2hz;
+    int var;
 };
 
 static MgK make_k(const Level &L) {
@@ -89,6 +94,11 @@ static MgK make_k(const Level &L) {
     k.lx = L.lx; k.ly = L.ly; k.lz = L.lz;
     k.fcx = (float)L.cx; k.fcy = (float)L.cy; k.fcz = (float)L.cz; k.fc7 = (float)L.c7; k.fden = (float)L.den;
     k.flx = (float)L.lx; k.fly = (float)L.ly; k.flz = (float)L.lz;
+    k.xix2 = L.xix2; k.xixx = L.xixx; k.ety2 = L.ety2; k.etyy = L.etyy; k.ztz2 = L.ztz2; k.ztzz = L.ztzz;
+    k.hx = L.hx; k.hy = L.hy; k.hz = L.hz; k.hxhy = L.hxhy; k.hyhz = L.hyhz; k.hzhx = L.hzhx; k.hxhyhz = L.hxhyhz;
+    k.ihx2 = L.ihx2; k.ihy2 = L.ihy2; k.ihz2 = L.ihz2;
+    k.i2hx = 1.0 / (2.0 * L.hx); k.i2hy = 1.0 / (2.0 * L.hy); k.i2hz = 1.0 / (2.0 * L.hz);   // exact: powers of two
+    k.var = L.xix2 != nullptr;
     return k;
 }
 
@@ -114,17 +124,32 @@ template <> struct KSel<float> {
     static __device__ __forceinline__ float lz(const MgK &k) { return k.flz; }
 };
 
-// Smoother update, the expression of poisson_d3.cc:156-163 on a uniform grid
-// (the xixx, etyy, ztzz terms are exactly zero and omitted).
+// Smoother update, the expression of poisson_d3.cc:156-163 at point (x, y, z).
+// Uniform grid: the xixx, etyy, ztzz terms are exactly zero and omitted, the
+// metric products are level constants.  Stretched mesh (FP64 only): every
+// term, the metrics read at the point.
 template <typename T>
-__device__ __forceinline__ T mg_update(T E, T W, T N, T S, T U, T D, T r, const MgK &k) {
+__device__ __forceinline__ T mg_update(T E, T W, T N, T S, T U, T D, T r, const MgK &k, int x, int y, int z) {
     using K = KSel<T>;
+    if constexpr (sizeof(T) == 8) {
+        if (k.var)
+            return (k.hyhz * k.xix2[x] * (E + W) * 2.0 + k.hyhz * k.xixx[x] * (E - W) * k.hx + k.hzhx * k.ety2[y] * (N + S) * 2.0 +
+                    k.hzhx * k.etyy[y] * (N - S) * k.hy + k.hxhy * k.ztz2[z] * (U + D) * 2.0 + k.hxhy * k.ztzz[z] * (U - D) * k.hz -
+                    2.0 * k.hxhyhz * r) /
+                   (4.0 * (k.hyhz * k.xix2[x] + k.hzhx * k.ety2[y] + k.hxhy * k.ztz2[z]));
+    }
     return ((K::cx(k) * (E + W)) * (T)2.0 + (K::cy(k) * (N + S)) * (T)2.0 + (K::cz(k) * (U + D)) * (T)2.0 - K::c7(k) * r) / K::den(k);
 }
-// Laplacian, the expression of poisson_d3.cc:99-105 (uniform grid).
+// Laplacian, the expression of poisson_d3.cc:99-105 at point (x, y, z); the
+// divisions by (hx*hx) and (2*hx) are multiplications by exact reciprocals.
 template <typename T>
-__device__ __forceinline__ T mg_lap(T E, T W, T N, T S, T U, T D, T C, const MgK &k) {
+__device__ __forceinline__ T mg_lap(T E, T W, T N, T S, T U, T D, T C, const MgK &k, int x, int y, int z) {
     using K = KSel<T>;
+    if constexpr (sizeof(T) == 8) {
+        if (k.var)
+            return k.xix2[x] * (E - 2.0 * C + W) * k.ihx2 + k.xixx[x] * (E - W) * k.i2hx + k.ety2[y] * (N - 2.0 * C + S) * k.ihy2 +
+                   k.etyy[y] * (N - S) * k.i2hy + k.ztz2[z] * (U - 2.0 * C + D) * k.ihz2 + k.ztzz[z] * (U - D) * k.i2hz;
+    }
     return K::lx(k) * (E - (T)2.0 * C + W) + K::ly(k) * (N - (T)2.0 * C + S) + K::lz(k) * (U - (T)2.0 * C + D);
 }
 
@@ -169,12 +194,12 @@ __global__ void k_mg_sweep(View3<T> out, View3<const T> in, View3<const T> r, Mg
     if (!core_pt(bc.E, i, j, k)) return;
     T v;
     if (ZERO) {
-        v = mg_update<T>((T)0, (T)0, (T)0, (T)0, (T)0, (T)0, r(i, j, k), kk);
+        v = mg_update<T>((T)0, (T)0, (T)0, (T)0, (T)0, (T)0, r(i, j, k), kk, i, j, k);
         if (omega != (T)1.0) v = omega * v;
     } else {
         T C = in(i, j, k);
         v = mg_update<T>(in(i + 1, j, k), in(i - 1, j, k), in(i, j + 1, k), in(i, j - 1, k), in(i, j, k + 1), in(i, j, k - 1),
-                         r(i, j, k), kk);
+                         r(i, j, k), kk, i, j, k);
         if (omega != (T)1.0) v = C + omega * (v - C);
     }
     put_scatter(out, i, j, k, v, bc);
@@ -185,7 +210,7 @@ template <typename T>
 __global__ void k_mg_residual(View3<T> tmp, View3<const T> p, View3<const T> r, MgK kk, MgBC bc) {
     int i, j, k;
     if (!core_pt(bc.E, i, j, k)) return;
-    T lap = mg_lap<T>(p(i + 1, j, k), p(i - 1, j, k), p(i, j + 1, k), p(i, j - 1, k), p(i, j, k + 1), p(i, j, k - 1), p(i, j, k), kk);
+    T lap = mg_lap<T>(p(i + 1, j, k), p(i - 1, j, k), p(i, j + 1, k), p(i, j - 1, k), p(i, j, k + 1), p(i, j, k - 1), p(i, j, k), kk, i, j, k);
     tmp(i, j, k) = r(i, j, k) - lap;
 }
 
@@ -367,7 +392,7 @@ __device__ void coarse_gs(T *p, T *r, int X, int Y, int Z, const MgK &kk, const 
                 int k = s - i - j;
                 if (k < 0 || k > Z) continue;
                 at(p, i, j, k) = mg_update<T>(at(p, i + 1, j, k), at(p, i - 1, j, k), at(p, i, j + 1, k), at(p, i, j - 1, k),
-                                              at(p, i, j, k + 1), at(p, i, j, k - 1), at(r, i, j, k), kk);
+                                              at(p, i, j, k + 1), at(p, i, j, k - 1), at(r, i, j, k), kk, i, j, k);
             }
             __syncthreads();
         }
@@ -376,7 +401,7 @@ __device__ void coarse_gs(T *p, T *r, int X, int Y, int Z, const MgK &kk, const 
         for (int t = tid; t < (X + 1) * (Y + 1) * (Z + 1); t += nt) {
             int k = t % (Z + 1), j = (t / (Z + 1)) % (Y + 1), i = t / ((Z + 1) * (Y + 1));
             T lap = mg_lap<T>(at(p, i + 1, j, k), at(p, i - 1, j, k), at(p, i, j + 1, k), at(p, i, j - 1, k), at(p, i, j, k + 1),
-                              at(p, i, j, k - 1), at(p, i, j, k), kk);
+                              at(p, i, j, k - 1), at(p, i, j, k), kk, i, j, k);
             T v = fabs(at(r, i, j, k) - lap);
             if (v != v) v = (T)INFINITY;
             if (v > localMax) localMax = v;
@@ -464,7 +489,7 @@ __device__ void coarse_rbgs_warp(T *p, T *r, int X, int Y, int Z, const MgK &kk,
                 int k = t % (Z + 1), j = (t / (Z + 1)) % (Y + 1), i = t / ((Z + 1) * (Y + 1));
                 if (((i + j + k) & 1) != colour) continue;
                 at(p, i, j, k) = mg_update<T>(at(p, i + 1, j, k), at(p, i - 1, j, k), at(p, i, j + 1, k), at(p, i, j - 1, k),
-                                              at(p, i, j, k + 1), at(p, i, j, k - 1), at(r, i, j, k), kk);
+                                              at(p, i, j, k + 1), at(p, i, j, k - 1), at(r, i, j, k), kk, i, j, k);
             }
             __syncwarp();
         }
@@ -474,7 +499,7 @@ __device__ void coarse_rbgs_warp(T *p, T *r, int X, int Y, int Z, const MgK &kk,
         for (int t = lane; t < n; t += 32) {
             int k = t % (Z + 1), j = (t / (Z + 1)) % (Y + 1), i = t / ((Z + 1) * (Y + 1));
             T lap = mg_lap<T>(at(p, i + 1, j, k), at(p, i - 1, j, k), at(p, i, j + 1, k), at(p, i, j - 1, k), at(p, i, j, k + 1),
-                              at(p, i, j, k - 1), at(p, i, j, k), kk);
+                              at(p, i, j, k - 1), at(p, i, j, k), kk, i, j, k);
             T v = fabs(at(r, i, j, k) - lap);
             if (v != v) v = (T)INFINITY;
             m = fmax(m, v);
@@ -531,7 +556,7 @@ __global__ void k_mg_gs_block(View3<double> pg, View3<const double> rg, MgK kk, 
                 int i = t / (Y + 1), j = t % (Y + 1), k = s - i - j;
                 if (k < 0 || k > Z) continue;
                 at(p, i, j, k) = mg_update<double>(at(p, i + 1, j, k), at(p, i - 1, j, k), at(p, i, j + 1, k), at(p, i, j - 1, k),
-                                                   at(p, i, j, k + 1), at(p, i, j, k - 1), at(r, i, j, k), kk);
+                                                   at(p, i, j, k + 1), at(p, i, j, k - 1), at(r, i, j, k), kk, i, j, k);
             }
             __syncthreads();
         }
@@ -627,7 +652,7 @@ __global__ void __launch_bounds__(256) k_mg_gs_grid(View3<double> p, View3<const
                 const int i = ilo + (int)(t / nj), j = jlo + (int)(t % nj), k = s - i - j;
                 if (k < 0 || k > Z) continue;
                 p(i, j, k) = mg_update<double>(__ldcg(&p(i + 1, j, k)), __ldcg(&p(i - 1, j, k)), __ldcg(&p(i, j + 1, k)),
-                                               __ldcg(&p(i, j - 1, k)), __ldcg(&p(i, j, k + 1)), __ldcg(&p(i, j, k - 1)), r(i, j, k), kk);
+                                               __ldcg(&p(i, j - 1, k)), __ldcg(&p(i, j, k + 1)), __ldcg(&p(i, j, k - 1)), r(i, j, k), kk, i, j, k);
             }
             target += gridDim.x;
             if (!gs_grid_sync(sync, target, err)) return;
@@ -733,7 +758,7 @@ __global__ void k_mg_error_sq(View3<const double> p, View3<const double> r, MgK 
     for (long t = c0; t < c1; ++t) {
         int k = (int)(t % (E2 + 1)), j = (int)((t / (E2 + 1)) % (E1 + 1)), i = (int)(t / ((long)(E2 + 1) * (E1 + 1)));
         double lap = mg_lap<double>(p(i + 1, j, k), p(i - 1, j, k), p(i, j + 1, k), p(i, j - 1, k), p(i, j, k + 1), p(i, j, k - 1),
-                                    p(i, j, k), kk);
+                                    p(i, j, k), kk, i, j, k);
         double v = fabs(lap - r(i, j, k));
         sn += v * v;
         sd += r(i, j, k) * r(i, j, k);
@@ -751,7 +776,7 @@ __global__ void k_mg_error(View3<const double> p, View3<const double> r, MgK kk,
     for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
         int k = (int)(t % (E2 + 1)), j = (int)((t / (E2 + 1)) % (E1 + 1)), i = (int)(t / ((long)(E2 + 1) * (E1 + 1)));
         double lap = mg_lap<double>(p(i + 1, j, k), p(i - 1, j, k), p(i, j + 1, k), p(i, j - 1, k), p(i, j, k + 1), p(i, j, k - 1),
-                                    p(i, j, k), kk);
+                                    p(i, j, k), kk, i, j, k);
         double v = fabs(lap - r(i, j, k));
         if (v != v) v = INFINITY;
         m = fmax(m, v);
@@ -2053,6 +2078,27 @@ int mg_setup(Ctx &c) {
         L.den = 4.0 * (L.hyhz * xix2 + L.hzhx * ety2 + L.hxhy * ztz2);
         L.ihx2 = 1.0 / (L.hx * L.hx); L.ihy2 = 1.0 / (L.hy * L.hy); L.ihz2 = 1.0 / (L.hz * L.hz);
         L.lx = xix2 * L.ihx2; L.ly = ety2 * L.ihy2; L.lz = ztz2 * L.ihz2;
+        if (c.stretched) {
+            // poisson.cc:463-495: the staggered metrics of the finest grid at every
+            // 2^l-th point on the level's core, 0 at its two ghost indices
+            const int s2 = 1 << l;
+            const size_t len[3] = {(size_t)L.n[0] + 3, (size_t)L.n[1] + 3, (size_t)L.n[2] + 3};
+            std::vector<double> h(2 * (len[0] + len[1] + len[2]), 0.0);
+            size_t off[6];
+            size_t o = 0;
+            for (int d = 0; d < 3; ++d)
+                for (int m = 0; m < 2; ++m) {   // m 0: xix2, 1: xixx
+                    off[2 * d + m] = o;
+                    const std::vector<double> &src = c.hmet[d][1][m == 0 ? 2 : 1];
+                    for (int i = 0; i <= L.n[d]; ++i) h[o + 1 + i] = src[(size_t)i * s2 + 1];
+                    o += len[d];
+                }
+            SARAS_CUDA_TRY(cudaMalloc(&L.metBlock, sizeof(double) * h.size()));
+            SARAS_CUDA_TRY(cudaMemcpy(L.metBlock, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice));
+            L.xix2 = L.metBlock + off[0] + 1; L.xixx = L.metBlock + off[1] + 1;
+            L.ety2 = L.metBlock + off[2] + 1; L.etyy = L.metBlock + off[3] + 1;
+            L.ztz2 = L.metBlock + off[4] + 1; L.ztzz = L.metBlock + off[5] + 1;
+        }
         size_t b64 = sizeof(double) * L.count, b32 = sizeof(float) * L.count;
         SARAS_CUDA_TRY(cudaMalloc(&L.a, b64)); SARAS_CUDA_TRY(cudaMalloc(&L.b, b64)); SARAS_CUDA_TRY(cudaMalloc(&L.r, b64));
         SARAS_CUDA_TRY(cudaMemsetAsync(L.a, 0, b64, c.stream)); SARAS_CUDA_TRY(cudaMemsetAsync(L.b, 0, b64, c.stream));
@@ -2113,7 +2159,9 @@ int mg_setup(Ctx &c) {
 
 void mg_free(Ctx &c) {
     vgraph_reset(c);
-    for (Level &L : c.lv) { cudaFree(L.a); cudaFree(L.b); cudaFree(L.r); cudaFree(L.a32); cudaFree(L.b32); cudaFree(L.r32); }
+    for (Level &L : c.lv) {
+        cudaFree(L.a); cudaFree(L.b); cudaFree(L.r); cudaFree(L.a32); cudaFree(L.b32); cudaFree(L.r32); cudaFree(L.metBlock);
+    }
     for (long long *&q : c.fx) { cudaFree(q); q = nullptr; }
     c.lv.clear();
     cudaFree(c.wallX); cudaFree(c.wallY); cudaFree(c.wallZ);

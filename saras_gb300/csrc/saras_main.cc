@@ -55,24 +55,30 @@ Field host_field(saras_ctx *ctx, int f) {
 }
 
 // taylorGreen::initializeField (taylorGreen.cc:54-100) over the padded arrays,
-// with the coordinates of grid.cc:370-403 (uniform mesh).
+// with the library's coordinates (grid.cc:370-403 uniform, 442-519 stretched).
+std::vector<double> coords(saras_ctx *ctx, int axis, int staggered) {
+    int n = 0;
+    check(saras_grid_coords(ctx, axis, staggered, nullptr, 0, &n), ctx, "grid coordinates");
+    std::vector<double> x((size_t)n);
+    check(saras_grid_coords(ctx, axis, staggered, x.data(), n, &n), ctx, "grid coordinates");
+    return x;
+}
+
 void taylor_green(saras_ctx *ctx, const saras_params &p) {
     const double L[3] = {p.Lx, p.Ly, p.Lz};
-    const int ind[3] = {p.xInd, p.yInd, p.zInd};
-    auto xi = [&](int d, int i) { return double(i) * (1.0 / double(1 << ind[d])); };
-    auto staggr = [&](int d, int i) { return L[d] * xi(d, i); };
-    auto colloc = [&](int d, int i) { return L[d] * (xi(d, i) + xi(d, i + 1)) / 2.0; };
+    std::vector<double> xs = coords(ctx, 0, 1), xc = coords(ctx, 0, 0), ys = coords(ctx, 1, 1), yc = coords(ctx, 1, 0),
+                        zs = coords(ctx, 2, 1);
     Field vx = host_field(ctx, SARAS_FIELD_VX), vy = host_field(ctx, SARAS_FIELD_VY);
     for (int i = -1; i < vx.dims[0] - 1; ++i)
         for (int j = -1; j < vx.dims[1] - 1; ++j)
             for (int k = -1; k < vx.dims[2] - 1; ++k)
-                vx.at(i, j, k) = std::sin(2.0 * M_PI * colloc(0, i) / L[0]) * std::cos(2.0 * M_PI * staggr(1, j) / L[1]) *
-                                 std::cos(2.0 * M_PI * staggr(2, k) / L[2]);
+                vx.at(i, j, k) = std::sin(2.0 * M_PI * xc[i + 1] / L[0]) * std::cos(2.0 * M_PI * ys[j + 1] / L[1]) *
+                                 std::cos(2.0 * M_PI * zs[k + 1] / L[2]);
     for (int i = -1; i < vy.dims[0] - 1; ++i)
         for (int j = -1; j < vy.dims[1] - 1; ++j)
             for (int k = -1; k < vy.dims[2] - 1; ++k)
-                vy.at(i, j, k) = -std::cos(2.0 * M_PI * staggr(0, i) / L[0]) * std::sin(2.0 * M_PI * colloc(1, j) / L[1]) *
-                                 std::cos(2.0 * M_PI * staggr(2, k) / L[2]);
+                vy.at(i, j, k) = -std::cos(2.0 * M_PI * xs[i + 1] / L[0]) * std::sin(2.0 * M_PI * yc[j + 1] / L[1]) *
+                                 std::cos(2.0 * M_PI * zs[k + 1] / L[2]);
     check(saras_upload(ctx, SARAS_FIELD_VX, vx.v.data()), ctx, "upload Vx");
     check(saras_upload(ctx, SARAS_FIELD_VY, vy.v.data()), ctx, "upload Vy");
 }

@@ -65,9 +65,22 @@ def rbc(ind=(4, 4, 3), depth=2, dt=5.0e-4):
     return p
 
 
+def stretched(make, axes, beta):
+    """A case on a mesh with double-sided tangent-hyperbolic stretching (Mesh
+    Type 'D', grid.cc:442-519) along `axes`, stretching factor `beta`."""
+    def build(**kw):
+        p = make(**kw)
+        for a in axes:
+            setattr(p, "xyz"[a] + "Grid", 2)
+            setattr(p, "beta" + "XYZ"[a], beta)
+        return p
+    return build
+
+
 def base_kind(kind):
-    """The case family of an initial-state kind ("tgv_p1" is a Taylor-Green case)."""
-    return "tgv" if kind.startswith("tgv") else kind
+    """The case family of an initial-state kind ("tgv_p1" is a Taylor-Green
+    case, "ldc_d" the lid-driven cavity on a stretched mesh)."""
+    return "tgv" if kind.startswith("tgv") else kind.split("_")[0]
 
 
 def initialise(solver, p, kind):
@@ -76,13 +89,13 @@ def initialise(solver, p, kind):
     kind "tgv" adds the harness-set Taylor-Green pressure; "tgv_p1" keeps the
     reference's own P = 1 (hydro_d3.cc:90) under the Taylor-Green velocity."""
     F = _abi
-    if kind == "rbc":
+    if base_kind(kind) == "rbc":
         solver.set(F.FIELD_P, np.ones(solver.dims(F.FIELD_P)))
         solver.set(F.FIELD_T, rbc_temperature(p, seed=42))
         for f in (F.FIELD_VX, F.FIELD_VY, F.FIELD_VZ, F.FIELD_T):
             solver.apply_bc(f)
         return
-    if kind in ("tgv", "tgv_p1"):
+    if base_kind(kind) == "tgv":
         Vx, Vy = taylor_green_velocity(p)
         solver.set(F.FIELD_VX, Vx)
         solver.set(F.FIELD_VY, Vy)
@@ -93,7 +106,11 @@ def initialise(solver, p, kind):
         solver.apply_bc(f)
 
 
-CASES = {"ldc": ldc, "tgv": tgv, "rbc": rbc}
+CASES = {"ldc": ldc, "tgv": tgv, "rbc": rbc,
+         # stretched meshes: the cavity along every axis, the convection cell
+         # along z (its walls), the periodic vortex along x
+         "ldc_d": stretched(ldc, (0, 1, 2), 1.3), "rbc_d": stretched(rbc, (2,), 1.2), "tgv_d": stretched(tgv, (0,), 1.1)}
+STRETCHED = ["ldc_d", "tgv_d", "rbc_d"]
 
 
 def rel_err(a, b):

@@ -99,3 +99,29 @@ def test_periodic_target_mode_needs_three_sweeps():
         with pytest.raises(saras_gb300.SarasError) as e:
             saras_gb300.Solver(p)
         assert e.value.status == _abi.BAD_CONFIG
+
+
+def test_stretched_mesh_runs_the_drop_in_only(tmp_path):
+    """Mesh Type 'D' (tangent-hyperbolic stretching) parses and is accepted in
+    the drop-in mode (it then fails only for want of a device); with a GB300
+    extension (target multigrid, fast kernels, a history guess) or a
+    non-positive Beta it is rejected before any device work."""
+    p = _abi.default_params()
+    p.xGrid, p.betaX = 2, 1.3
+    with pytest.raises(saras_gb300.SarasError) as e:
+        saras_gb300.Solver(p)
+    assert e.value.status == _abi.NO_DEVICE
+    for field, value in (("mgMode", _abi.MG_MIXED), ("fastKernels", 2), ("guessMode", _abi.GUESS_EXTRAPOLATE), ("betaX", 0.0)):
+        q = _abi.default_params()
+        q.xGrid, q.betaX = 2, 1.3
+        if field == "mgMode":
+            q.preSmooth = q.postSmooth = 2
+        setattr(q, field, value)
+        with pytest.raises(saras_gb300.SarasError) as e:
+            saras_gb300.Solver(q)
+        assert e.value.status == _abi.BAD_CONFIG, field
+    text = open(os.path.join(HERE, "golden", "configs", "tgv_65_gs.yaml")).read().replace('"Mesh Type": "UUU"', '"Mesh Type": "UDS"')
+    path = tmp_path / "stretched.yaml"
+    path.write_text(text)
+    q = saras_gb300.parser(str(path))
+    assert (q.xGrid, q.yGrid, q.zGrid) == (0, 2, 1)

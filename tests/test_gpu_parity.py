@@ -1,5 +1,9 @@
 """GPU parity: every hot-path operator of the C ABI against the CPU oracle.
 
+Every case runs on a uniform mesh and, for the "_d" kinds, on a mesh with
+double-sided tangent-hyperbolic stretching (grid.cc:442-519), where every
+stencil reads the metric arrays at its point (xixx terms included).
+
 The CUDA path runs the reference arithmetic in the reference order (no FMA
 contraction), so agreement is expected to the last bit for all local
 operators; reductions whose summation order differs (the padded-array mean of
@@ -32,21 +36,26 @@ def assert_close(a, b, what, tol=TOL):
 
 FIELDS = {"ldc": [F.FIELD_VX, F.FIELD_VY, F.FIELD_VZ], "tgv": [F.FIELD_VX, F.FIELD_VY, F.FIELD_VZ],
           "rbc": [F.FIELD_VX, F.FIELD_VY, F.FIELD_VZ, F.FIELD_T]}
+KINDS = ["ldc", "tgv", "rbc"] + C.STRETCHED
 
 
-@pytest.mark.parametrize("kind", ["ldc", "tgv", "rbc"])
+def fields_of(kind):
+    return FIELDS[C.base_kind(kind)]
+
+
+@pytest.mark.parametrize("kind", KINDS)
 def test_initial_bc_state(kind):
     p, g, o = pair(kind)
-    for f in FIELDS[kind] + [F.FIELD_P]:
+    for f in fields_of(kind) + [F.FIELD_P]:
         assert np.array_equal(g.get(f), o.get(f)), F.FIELD_NAMES[f]
 
 
-@pytest.mark.parametrize("kind", ["ldc", "tgv", "rbc"])
+@pytest.mark.parametrize("kind", KINDS)
 def test_boundary_fill_random(kind):
     """imposeU/V/W/TBCs on random data: syncData + wall objects, bit-exact."""
     p, g, o = pair(kind)
     rng = np.random.default_rng(7)
-    for f in FIELDS[kind]:
+    for f in fields_of(kind):
         a = rng.standard_normal(g.dims(f))
         g.set(f, a); o.set(f, a)
         g.apply_bc(f); o.apply_bc(f)
@@ -57,12 +66,12 @@ def test_boundary_fill_random(kind):
     assert np.array_equal(g.get(F.FIELD_PP), o.get(F.FIELD_PP))
 
 
-@pytest.mark.parametrize("kind", ["ldc", "tgv", "rbc"])
+@pytest.mark.parametrize("kind", KINDS)
 def test_field_operators(kind):
     """computeDiff, computeNLin, gradient, divergence (and T's) on random fields."""
     p, g, o = pair(kind)
     rng = np.random.default_rng(11)
-    for f in FIELDS[kind]:
+    for f in fields_of(kind):
         a = rng.standard_normal(g.dims(f))
         g.set(f, a); o.set(f, a)
         g.apply_bc(f); o.apply_bc(f)
@@ -83,19 +92,19 @@ def test_field_operators(kind):
             assert np.array_equal(g.get(f), o.get(f)), "gradient " + F.FIELD_NAMES[f]
     g.vfield_divergence(); o.vfield_divergence()
     assert np.array_equal(g.get(F.FIELD_MGRHS), o.get(F.FIELD_MGRHS))
-    if kind == "rbc":
+    if C.base_kind(kind) == "rbc":
         z = np.zeros(g.dims(F.FIELD_TRHS)); g.set(F.FIELD_TRHS, z); o.set(F.FIELD_TRHS, z)
         g.tfield_compute_diff(); o.tfield_compute_diff()
         g.tfield_compute_nlin(); o.tfield_compute_nlin()
         assert np.array_equal(g.get(F.FIELD_TRHS), o.get(F.FIELD_TRHS))
 
 
-@pytest.mark.parametrize("kind", ["ldc", "tgv", "rbc"])
+@pytest.mark.parametrize("kind", KINDS)
 def test_cn_solve(kind):
     """solveVx/Vy/Vz (and solveT): iterations equal, fields to 1e-10."""
     p, g, o = pair(kind)
     rng = np.random.default_rng(5)
-    comps = [0, 1, 2] + ([3] if kind == "rbc" else [])
+    comps = [0, 1, 2] + ([3] if C.base_kind(kind) == "rbc" else [])
     for c in comps:
         f = F.FIELD_T if c == 3 else F.FIELD_VX + c
         r = F.FIELD_TRHS if c == 3 else F.FIELD_NSE_X + c
@@ -109,7 +118,8 @@ def test_cn_solve(kind):
         assert_close(g.get(f), o.get(f), "CN " + F.FIELD_NAMES[f])
 
 
-LEVEL_CASES = [(k, 4, 0) for k in ("ldc", "tgv", "rbc")] + [(k, ind, 1) for k in ("ldc", "tgv", "rbc") for ind in (4, 5)]
+LEVEL_CASES = ([(k, 4, 0) for k in ("ldc", "tgv", "rbc")] + [(k, ind, 1) for k in ("ldc", "tgv", "rbc") for ind in (4, 5)] +
+               [(k, 4, gs) for k in C.STRETCHED for gs in (0, 1)] + [(k, 5, 1) for k in C.STRETCHED])
 
 
 @pytest.mark.parametrize("kind,ind,gs", LEVEL_CASES)
@@ -122,7 +132,7 @@ def test_multigrid_level_operators(kind, ind, gs):
     Gauss-Seidel smoothing (poisson_d3.cc:137-150), bit for bit; at ind 5 the
     finest level (35^3 padded) runs the multi-CTA wavefront kernel, the others
     the shared-memory one."""
-    kw = dict(ind=(ind, ind, ind - 1) if kind == "rbc" else ind, depth=2)
+    kw = dict(ind=(ind, ind, ind - 1) if C.base_kind(kind) == "rbc" else ind, depth=2)
     p = C.CASES[kind](**kw)
     p.gsSmooth = gs
     g, o = Solver(p), Oracle(p)
@@ -160,11 +170,11 @@ def test_multigrid_level_operators(kind, ind, gs):
         assert eg == eo, (norm, eg, eo)
 
 
-@pytest.mark.parametrize("kind,ind,gs", [(k, 4, 0) for k in ("ldc", "tgv", "rbc")] + [(k, 5, 1) for k in ("ldc", "tgv", "rbc")])
+@pytest.mark.parametrize("kind,ind,gs", [(k, 4, 0) for k in KINDS] + [(k, 5, 1) for k in KINDS])
 def test_mg_solve(kind, ind, gs):
     """poisson::mgSolve on the divergence of a random velocity field (gs = 1:
     Gauss-Seidel smoothing on every level, as the reference's shipped input)."""
-    p = C.CASES[kind](ind=(ind, ind, ind - 1) if kind == "rbc" else ind, depth=2 if ind == 4 else 3)
+    p = C.CASES[kind](ind=(ind, ind, ind - 1) if C.base_kind(kind) == "rbc" else ind, depth=2 if ind == 4 else 3)
     p.gsSmooth = gs
     g, o = Solver(p), Oracle(p)
     C.initialise(g, p, kind)
@@ -183,7 +193,8 @@ def test_mg_solve(kind, ind, gs):
 
 
 @pytest.mark.parametrize("kind,steps,gs", [("ldc", 10, 0), ("tgv", 10, 0), ("rbc", 10, 0), ("ldc", 5, 1), ("tgv", 5, 1),
-                                           ("rbc", 5, 1)])
+                                           ("rbc", 5, 1), ("ldc_d", 10, 0), ("tgv_d", 10, 0), ("rbc_d", 10, 0), ("ldc_d", 5, 1),
+                                           ("rbc_d", 5, 1)])
 def test_time_advance(kind, steps, gs):
     """hydro_d3 / scalar_d3 timeAdvance: equal iteration counts every step and
     V, P (and T) within 1e-10 after the run (gs = 1: Gauss-Seidel smoothing)."""
@@ -192,7 +203,7 @@ def test_time_advance(kind, steps, gs):
     g, o = Solver(p), Oracle(p)
     C.initialise(g, p, kind)
     C.initialise(o, p, kind)
-    fields = [F.FIELD_VX, F.FIELD_VY, F.FIELD_VZ, F.FIELD_P, F.FIELD_PP] + ([F.FIELD_T] if kind == "rbc" else [])
+    fields = [F.FIELD_VX, F.FIELD_VY, F.FIELD_VZ, F.FIELD_P, F.FIELD_PP] + ([F.FIELD_T] if C.base_kind(kind) == "rbc" else [])
     for step in range(steps):
         sg, stg = g.time_advance()
         so, sto = o.time_advance()

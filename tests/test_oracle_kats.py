@@ -132,6 +132,43 @@ def test_gradient_converges_at_second_order():
     assert min(_orders(errs)) >= 1.9, (errs, _orders(errs))
 
 
+def _stretched_ldc(ind):
+    p = C.CASES["ldc_d"](ind=ind, depth=2)
+    p.iScheme = 2   # full second derivatives (no Crank-Nicolson halving)
+    return p
+
+
+def test_stretched_mesh_derivatives_second_order():
+    """On a mesh stretched along every axis (Mesh Type "DDD", beta 1.3:
+    grid.cc:442-519 coordinates and metrics), computeDiff of
+    u = cos(pi x) cos(pi y) cos(pi z) approximates -3 pi^2 u through the chain
+    rule xix2 u_xi,xi + xixx u_xi (derivative.cc:178-243), and the divergence of
+    (u, 0, 0) the metric-scaled difference xi_x u_xi (vfield.cc:299-320); on the
+    interior (away from the ghosts, which keep uniform coordinates) both errors
+    fall by 4 per halving of the transformed spacing (measured order >= 1.8)."""
+    import saras_gb300 as S
+    e2, e1 = [], []
+    for ind in (4, 5, 6):
+        p = _stretched_ldc(ind)
+        o = Oracle(p)
+        (xs, xc), (ys, yc), (zs, zc) = S.grid_coords(p)
+        u = np.cos(np.pi * xc)[:, None, None] * np.cos(np.pi * ys)[None, :, None] * np.cos(np.pi * zs)[None, None, :]
+        o.set(F.FIELD_VX, u)
+        for f in (F.FIELD_VY, F.FIELD_VZ):
+            o.set(f, np.zeros(o.dims(f)))
+        for f in (F.FIELD_NSE_X, F.FIELD_NSE_Y, F.FIELD_NSE_Z):
+            o.set(f, np.zeros(o.dims(f)))
+        o.vfield_compute_diff()
+        H = o.get(F.FIELD_NSE_X)
+        e2.append(np.max(np.abs(H + 3.0 * np.pi ** 2 * u)[3:-3, 3:-3, 3:-3]))
+        o.vfield_divergence()
+        D = o.get(F.FIELD_MGRHS)
+        du = -np.pi * np.sin(np.pi * xs)[:, None, None] * np.cos(np.pi * ys)[None, :, None] * np.cos(np.pi * zs)[None, None, :]
+        e1.append(np.max(np.abs(D - du)[3:-3, 3:-3, 3:-3]))
+    assert min(_orders(e2)) >= 1.8, (e2, _orders(e2))
+    assert min(_orders(e1)) >= 1.8, (e1, _orders(e1))
+
+
 def test_crank_nicolson_half_factor():
     """calcDerivative2xx applies 0.5 * central22n / h^2 when iScheme = 1
     (derivative.cc:185-189): computeDiff of u = x^2 (and v = y^2, w = z^2, with
