@@ -1331,7 +1331,13 @@ int fields_setup(Ctx &c) {
         SARAS_CUDA_TRY(cudaMalloc(&c.scratch[q], bytes));
         SARAS_CUDA_TRY(cudaMemsetAsync(c.scratch[q], 0, bytes, c.stream));
     }
-    c.redCap = 1 << 16;
+    // per-block partials of the reductions: one per column block and segment of
+    // the finest level (k_tgt_stats), one per 4096-point chunk of a padded level
+    {
+        const long cols = (long)c.Ns[1] * c.Ns[2], pts = (long)(c.Ns[0] + 2) * (c.Ns[1] + 2) * (c.Ns[2] + 2);
+        const long need = std::max((cols + 255) / 256 * ((c.Ns[0] + 3) / 4 + 1), pts / 4096 + 1);
+        c.redCap = (int)std::max<long>(1 << 16, need);
+    }
     SARAS_CUDA_TRY(cudaMalloc(&c.red, sizeof(double) * c.redCap * 3));
     SARAS_CUDA_TRY(cudaMalloc(&c.dscal, sizeof(double) * 64));
     SARAS_CUDA_TRY(cudaMalloc(&c.dflag, sizeof(int) * 16));
