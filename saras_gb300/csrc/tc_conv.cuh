@@ -232,4 +232,156 @@ __global__ void __launch_bounds__(128) k_conv3d_tc(ConvArgs a) {
     if (warp == 0) tmem_dealloc(taddr, NCOLS);
 }
 
+// ---- weight gradient on the tensor cores
+// dW[n][tap][c] = sum_v dY[v][n] X[v + off(tap)][c] as the GEMM
+//   D[m][n] = sum_k A[m][k] B[n][k],  m = tap * Cin + c (27 Cin rows in tiles
+//   of 128), n = output channel, k = voxel.
+// Both operands are staged MN-major, which is the order the channels-last
+// tensors already have: one 16-byte row of a core matrix is 8 consecutive
+// channels of one voxel (X at the shifted voxel for A, dY for B), so every row
+// is one 16-byte cp.async straight from global memory.  Core matrices adjacent
+// along M (or N) are 128 B apart (the leading byte offset), the two 8-voxel
+// halves of a K step of 16 voxels 16 x 128 B (A) or N / 8 x 128 B (B) apart
+// (the stride byte offset).  Each CTA reduces a chunk of voxels for one M tile
+// into its tensor-memory accumulator and adds it to the FP32 dW with atomics;
+// the CTAs of M tile 0 also add their chunk's sum of dY to db.
+struct DwArgs {
+    const __nv_bfloat16 *in0, *in1;   // X, channels-last, concatenated along C
+    int c0, c1;
+    const __nv_bfloat16 *dy;          // dY, channels-last, N channels
+    float *dw;                        // [N][27][c0 + c1]
+    float *db;                        // [N], or null
+    int D, H, W, nvox;
+    int chunk;                        // voxels a CTA reduces (a multiple of 16)
+    int *err;
+};
+
+constexpr int kDwStages = 4;
+constexpr int kDwTileA = 128 * 16 * 2;
+// Reserve: the ring is followed by 32 KB that no operand occupies, so that even
+// a descriptor read with its two byte offsets exchanged (15 x 2048 B past a
+// stage at most) stays inside the CTA's shared memory.
+constexpr int kDwReserve = 32768;
+template <int N>
+__host__ __device__ constexpr int dw_stage_bytes() { return kDwTileA + N * 32; }
+template <int N>
+__host__ __device__ constexpr int dw_smem_bytes() { return kDwStages * dw_stage_bytes<N>() + kDwReserve + 128; }
+
+template <int N>
+__global__ void __launch_bounds__(128) k_conv_dw_tc(DwArgs a) {
+    static_assert(N % 16 == 0 && N >= 16 && N <= 128, "N");
+    extern __shared__ __align__(128) uint8_t smem[];
+    constexpr int SB = dw_stage_bytes<N>();
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + kDwStages * SB + kDwReserve);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + kDwStages);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    constexpr uint32_t NCOLS = conv_tmem_cols<N>();
+    constexpr uint32_t IDESC = idesc_bf16(128, N) | (1u << 15) | (1u << 16);   // A and B MN-major
+    const int cin = a.c0 + a.c1, mtot = 27 * cin;
+    const int mt = blockIdx.y;
+    const long v0 = (long)blockIdx.x * a.chunk;
+    const long v1 = min(v0 + (long)a.chunk, (long)a.nvox);
+    const int nsteps = v1 > v0 ? (int)((v1 - v0 + 15) / 16) : 0;
+
+    if (warp == 0) { tmem_alloc(tslot, NCOLS); tmem_relinquish(); }
+    if (tid == 0) {
+        for (int s = 0; s < kDwStages; ++s) mbar_init(&mbar[s], 1);
+        fence_mbar_init();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t taddr = *tslot;
+
+    auto load_step = [&](int s, int st) {
+        const uint32_t base = su32(smem + st * SB);
+        const long vb = v0 + (long)s * 16;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {   // A: 16 M groups x 16 voxel rows, two rows a thread
+            const int cidx = tid + h * 128, mg = cidx >> 4, r = cidx & 15;
+            const int m0 = mt * 128 + mg * 8;
+            const long v = vb + r;
+            const __nv_bfloat16 *src = a.in0;
+            bool ok = m0 < mtot && v < v1;
+            if (ok) {
+                const int tap = m0 / cin, c = m0 - tap * cin;
+                const int x = (int)(v % a.W);
+                const long t = v / a.W;
+                const int y = (int)(t % a.H), z = (int)(t / a.H);
+                const int zz = z + tap / 9 - 1, yy = y + (tap / 3) % 3 - 1, xx = x + tap % 3 - 1;
+                ok = zz >= 0 && zz < a.D && yy >= 0 && yy < a.H && xx >= 0 && xx < a.W;
+                if (ok) {
+                    const long sv = ((long)zz * a.H + yy) * a.W + xx;
+                    src = c < a.c0 ? a.in0 + sv * a.c0 + c : a.in1 + sv * a.c1 + (c - a.c0);
+                }
+            }
+            cp_async16(base + mg * 128 + (r & 7) * 16 + (r >> 3) * 2048, src, ok ? 16 : 0);
+        }
+        for (int cidx = tid; cidx < N * 2; cidx += 128) {   // B: N / 8 groups x 16 voxel rows
+            const int ng = cidx >> 4, r = cidx & 15;
+            const long v = vb + r;
+            const bool ok = v < v1;
+            cp_async16(base + kDwTileA + ng * 128 + (r & 7) * 16 + (r >> 3) * (N / 8) * 128, ok ? a.dy + v * N + ng * 8 : a.dy,
+                       ok ? 16 : 0);
+        }
+    };
+
+    bool ok = true;
+#pragma unroll 1
+    for (int s = 0; s < kDwStages - 1; ++s) {
+        if (s < nsteps) load_step(s, s);
+        cp_async_commit();
+    }
+#pragma unroll 1
+    for (int s = 0; s < nsteps; ++s) {
+        const int st = s % kDwStages;
+        cp_async_wait<kDwStages - 2>();
+        __syncthreads();
+        fence_async_smem();
+        if (tid == 0 && ok) {
+            tc_fence_after();
+            const uint32_t aAddr = su32(smem + st * SB), bAddr = aAddr + kDwTileA;
+            tc_mma_bf16(taddr, smem_desc(aAddr, 128, 2048), smem_desc(bAddr, 128, (N / 8) * 128), IDESC, s > 0 ? 1u : 0u);
+            tc_commit(&mbar[st]);
+        }
+        const int ns = s + kDwStages - 1;
+        if (ns < nsteps) {
+            const int nst = ns % kDwStages;
+            // stage nst was last read by the MMA of step ns - kDwStages (= s - 1)
+            if (ns >= kDwStages && ok) ok = mbar_wait(&mbar[nst], (uint32_t)(((ns - kDwStages) / kDwStages) & 1), a.err);
+            if (ok) load_step(ns, nst);
+        }
+        cp_async_commit();
+    }
+    cp_async_wait<0>();
+    if (ok && nsteps > 0) {
+        const int last = nsteps - 1;
+        ok = mbar_wait(&mbar[last % kDwStages], (uint32_t)((last / kDwStages) & 1), a.err);
+    }
+    __syncthreads();
+    tc_fence_after();
+    if (ok && nsteps > 0) {
+        const int m = mt * 128 + tid;
+        const int tap = m / cin, c = m - tap * cin;
+        const uint32_t tw = taddr + ((uint32_t)(warp * 32) << 16);
+#pragma unroll
+        for (int q = 0; q < N / 16; ++q) {
+            float vals[16];
+            tc_ld16(tw + q * 16, vals);
+            if (m < mtot) {
+#pragma unroll
+                for (int e = 0; e < 16; ++e) atomicAdd(&a.dw[((long)(q * 16 + e) * 27 + tap) * cin + c], vals[e]);
+            }
+        }
+    }
+    if (a.db && mt == 0 && tid < N) {
+        float sum = 0.0f;
+        for (long v = v0; v < v1; ++v) sum += __bfloat162float(a.dy[v * N + tid]);
+        atomicAdd(&a.db[tid], sum);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(taddr, NCOLS);
+}
+
 }  // namespace saras

@@ -9,8 +9,9 @@
 // and the solver keeps the previous pressure instead whenever the guess has the
 // larger FP64 residual.  The network is trained on (input, solution) pairs that
 // the solver itself produces during the run's warm-up, with Adam on FP32
-// master weights; forward and input-gradient convolutions run on the tensor
-// cores (k_conv3d_tc), weight gradients reduce over voxels on the CUDA cores.
+// master weights; forward and input-gradient convolutions (k_conv3d_tc) and
+// the weight gradients (k_conv_dw_tc, a GEMM whose K runs over voxels) all run
+// on the tensor cores.
 
 #include <cmath>
 #include <cstring>
@@ -103,72 +104,6 @@ __global__ void k_pack_weights(const float *__restrict__ w, bf16 *__restrict__ p
     float val = transposed ? w[((long)kk * 27 + (26 - tap)) * cin + n] : w[((long)n * 27 + tap) * cin + kk];
     long byte = s * (long)N * 32 + (n >> 3) * 256 + (k >> 3) * 128 + (n & 7) * 16 + (k & 7) * 2;
     pk[byte / 2] = __float2bfloat16(val);
-}
-
-// Weight and bias gradients: dW[n][tap][c] += sum_v dY[v][n] X[v + off(tap)][c],
-// db[n] += sum_v dY[v][n].  blockIdx.y = tap; each block reduces a voxel chunk.
-constexpr int kDwChunk = 2048;
-constexpr int kDwSub = 32;
-__global__ void __launch_bounds__(256) k_conv_dw(const bf16 *x0, const bf16 *x1, int c0, int c1, const bf16 *dy, int cout, Grid3 g,
-                                                  float *dw, float *db) {
-    extern __shared__ float sh[];
-    int cin = c0 + c1;
-    float *sx = sh;                   // kDwSub x cin
-    float *sy = sh + kDwSub * cin;    // kDwSub x cout
-    int tap = blockIdx.y;
-    int dz = tap / 9 - 1, dyy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
-    long v0 = (long)blockIdx.x * kDwChunk;
-    long nv = g.n();
-    int pairs = cin * cout;
-    constexpr int MAXP = 24;
-    float acc[MAXP];
-    float bacc = 0.0f;
-#pragma unroll
-    for (int q = 0; q < MAXP; ++q) acc[q] = 0.0f;
-    for (long vb = v0; vb < min(v0 + kDwChunk, nv); vb += kDwSub) {
-        __syncthreads();
-        for (int t = threadIdx.x; t < kDwSub * cin; t += blockDim.x) {
-            int r = t / cin, cc = t % cin;
-            long v = vb + r;
-            float val = 0.0f;
-            if (v < nv) {
-                int x = (int)(v % g.W), y = (int)((v / g.W) % g.H), z = (int)(v / ((long)g.W * g.H));
-                int zz = z + dz, yy = y + dyy, xx = x + dx;
-                if (zz >= 0 && zz < g.D && yy >= 0 && yy < g.H && xx >= 0 && xx < g.W) {
-                    long sv = ((long)zz * g.H + yy) * g.W + xx;
-                    val = cc < c0 ? __bfloat162float(x0[sv * c0 + cc]) : __bfloat162float(x1[sv * c1 + (cc - c0)]);
-                }
-            }
-            sx[t] = val;
-        }
-        for (int t = threadIdx.x; t < kDwSub * cout; t += blockDim.x) {
-            int r = t / cout, n = t % cout;
-            long v = vb + r;
-            sy[t] = v < nv ? __bfloat162float(dy[v * cout + n]) : 0.0f;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int q = 0; q < MAXP; ++q) {
-            int pr = threadIdx.x + q * blockDim.x;
-            if (pr < pairs) {
-                int n = pr / cin, cc = pr % cin;
-                float a = acc[q];
-                for (int r = 0; r < kDwSub; ++r) a = fmaf(sy[r * cout + n], sx[r * cin + cc], a);
-                acc[q] = a;
-            }
-        }
-        if (tap == 13 && (int)threadIdx.x < cout)
-            for (int r = 0; r < kDwSub; ++r) bacc += sy[r * cout + threadIdx.x];
-    }
-#pragma unroll
-    for (int q = 0; q < MAXP; ++q) {
-        int pr = threadIdx.x + q * blockDim.x;
-        if (pr < pairs) {
-            int n = pr / cin, cc = pr % cin;
-            atomicAdd(&dw[((long)n * 27 + tap) * cin + cc], acc[q]);
-        }
-    }
-    if (tap == 13 && (int)threadIdx.x < cout) atomicAdd(&db[threadIdx.x], bacc);
 }
 
 // Adam on the flat FP32 parameter vector.
@@ -717,16 +652,53 @@ static int add_mask(Ctx &c, const bf16 *a, const bf16 *b, const bf16 *mask, bf16
     return ucheck(c, "add_mask");
 }
 
+// Weight and bias gradients of layer li on the tensor cores (k_conv_dw_tc):
+// voxel chunks sized for about four CTAs an SM over all M tiles.
+template <int N>
+static cudaError_t launch_dw_n(const DwArgs &a, int mtiles, cudaStream_t st) {
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_conv_dw_tc<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, dw_smem_bytes<N>());
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    const long nch = (a.nvox + a.chunk - 1) / a.chunk;
+    k_conv_dw_tc<N><<<dim3((unsigned)nch, (unsigned)mtiles), 128, dw_smem_bytes<N>(), st>>>(a);
+    return cudaGetLastError();
+}
+
+static int launch_dw(Ctx &c, int N, DwArgs a) {
+    const int cin = a.c0 + a.c1;
+    const int mtiles = (27 * cin + 127) / 128;
+    const long want = std::max(1L, 4L * 152 / mtiles);   // voxel chunks
+    a.chunk = (int)std::max(16L, (((long)a.nvox + want - 1) / want + 15) / 16 * 16);
+    cudaError_t e;
+    switch (N) {
+    case 16: e = launch_dw_n<16>(a, mtiles, c.stream); break;
+    case 32: e = launch_dw_n<32>(a, mtiles, c.stream); break;
+    case 48: e = launch_dw_n<48>(a, mtiles, c.stream); break;
+    case 64: e = launch_dw_n<64>(a, mtiles, c.stream); break;
+    case 96: e = launch_dw_n<96>(a, mtiles, c.stream); break;
+    default: c.err = "unsupported convolution width"; return SARAS_BAD_ARG;
+    }
+    count_launch(c);
+    if (e != cudaSuccess) { c.err = std::string("k_conv_dw_tc: ") + cudaGetErrorString(e); return SARAS_CUDA_ERROR; }
+    return SARAS_OK;
+}
+
 static int conv_dw(Ctx &c, int li, const bf16 *x0, const bf16 *x1, const bf16 *dy) {
     UNet *u = U(c);
     const ConvLayer &l = u->L[li];
     const Grid3 &g = u->g[l.level];
-    int cin = l.cin0 + l.cin1;
-    dim3 grid((unsigned)((g.n() + kDwChunk - 1) / kDwChunk), 27);
-    size_t sm = sizeof(float) * kDwSub * (cin + l.cout);
-    k_conv_dw<<<grid, 256, sm, c.stream>>>(x0, x1, l.cin0, l.cin1, dy, l.cout, g, u->grad + l.woff, u->grad + l.boff);
-    count_launch(c);
-    return ucheck(c, "conv_dw");
+    DwArgs a;
+    a.in0 = x0; a.in1 = x1; a.c0 = l.cin0; a.c1 = l.cin1;
+    a.dy = dy;
+    a.dw = u->grad + l.woff;
+    a.db = u->grad + l.boff;
+    a.D = g.D; a.H = g.H; a.W = g.W; a.nvox = (int)g.n();
+    a.chunk = 0;
+    a.err = u->err;
+    return launch_dw(c, l.cout, a);
 }
 
 // Input gradient of layer li: conv of dY with the mirrored, transposed weights.
@@ -1227,10 +1199,12 @@ int conv3d_check(int mode, int D, int H, int W, int cin, int cout, const unsigne
             if (!s && (e = cudaMemcpy(out, dout32, sizeof(float) * nv * cin, cudaMemcpyDeviceToHost))) fail(e);
         } else if (mode == 2) {
             cudaMemset(dgrad, 0, wbytes + sizeof(float) * cout);
-            Grid3 g{D, H, W};
-            dim3 grid((unsigned)((nv + kDwChunk - 1) / kDwChunk), 27);
-            k_conv_dw<<<grid, 256, sizeof(float) * kDwSub * (cin + cout)>>>(dx, nullptr, cin, 0, ddy, cout, g, dgrad, dgrad + 27L * cin * cout);
-            if ((e = cudaGetLastError()) || (e = cudaMemcpy(out, dgrad, wbytes + sizeof(float) * cout, cudaMemcpyDeviceToHost))) fail(e);
+            DwArgs da;
+            da.in0 = dx; da.in1 = nullptr; da.c0 = cin; da.c1 = 0;
+            da.dy = ddy; da.dw = dgrad; da.db = dgrad + 27L * cin * cout;
+            da.D = D; da.H = H; da.W = W; da.nvox = (int)nv; da.chunk = 0; da.err = derr;
+            s = launch_dw(c, cout, da);
+            if (!s && (e = cudaMemcpy(out, dgrad, wbytes + sizeof(float) * cout, cudaMemcpyDeviceToHost))) fail(e);
         } else {
             s = SARAS_BAD_ARG;
         }
