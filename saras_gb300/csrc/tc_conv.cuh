@@ -240,9 +240,11 @@ __global__ void __launch_bounds__(128) k_conv3d_tc(ConvArgs a) {
 // tensors already have: one 16-byte row of a core matrix is 8 consecutive
 // channels of one voxel (X at the shifted voxel for A, dY for B), so every row
 // is one 16-byte cp.async straight from global memory.  Core matrices adjacent
-// along M (or N) are 128 B apart (the leading byte offset), the two 8-voxel
-// halves of a K step of 16 voxels 16 x 128 B (A) or N / 8 x 128 B (B) apart
-// (the stride byte offset).  Each CTA reduces a chunk of voxels for one M tile
+// along M (or N) are 128 B apart (the stride byte offset of a no-swizzle
+// MN-major descriptor), the two 8-voxel halves of a K step of 16 voxels
+// 16 x 128 B (A) or N / 8 x 128 B (B) apart (its leading byte offset; a first
+// build with the two exchanged read past the tile, into the reserve below, and
+// produced wrong sums, not a fault).  Each CTA reduces a chunk of voxels for one M tile
 // into its tensor-memory accumulator and adds it to the FP32 dW with atomics;
 // the CTAs of M tile 0 also add their chunk's sum of dY to db.
 struct DwArgs {
@@ -341,7 +343,9 @@ __global__ void __launch_bounds__(128) k_conv_dw_tc(DwArgs a) {
         if (tid == 0 && ok) {
             tc_fence_after();
             const uint32_t aAddr = su32(smem + st * SB), bAddr = aAddr + kDwTileA;
-            tc_mma_bf16(taddr, smem_desc(aAddr, 128, 2048), smem_desc(bAddr, 128, (N / 8) * 128), IDESC, s > 0 ? 1u : 0u);
+            // no-swizzle MN-major: the stride byte offset steps between core
+            // matrices along M / N, the leading byte offset along K
+            tc_mma_bf16(taddr, smem_desc(aAddr, 2048, 128), smem_desc(bAddr, (N / 8) * 128, 128), IDESC, s > 0 ? 1u : 0u);
             tc_commit(&mbar[st]);
         }
         const int ns = s + kDwStages - 1;
