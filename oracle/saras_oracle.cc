@@ -97,18 +97,24 @@ struct Grid {
     A1 xStaggr, yStaggr, zStaggr, xColloc, yColloc, zColloc;
     A1 xi_xColloc, xixxColloc, xix2Colloc, et_yColloc, etyyColloc, ety2Colloc, zt_zColloc, ztzzColloc, ztz2Colloc;
     A1 xi_xStaggr, xixxStaggr, xix2Staggr, et_yStaggr, etyyStaggr, ety2Staggr, zt_zStaggr, ztzzStaggr, ztz2Staggr;
+    // the 2D (PLANAR) solver: "Y Index" 0 gives one y point, dEt = yLen = 1
+    // (grid.cc:88-92) and one collocated y point (grid.cc:232-234)
+    bool planar = false;
 
     void build(const saras_params &p) {
+        planar = p.yInd == 0;
         sizeIndex[0] = p.xInd; sizeIndex[1] = p.yInd; sizeIndex[2] = p.zInd;
         for (int d = 0; d < 3; ++d) globalSize[d] = (sizeIndex[d] == 0) ? 1 : (int(std::pow(2, sizeIndex[d])) + 1);
         xLen = p.Lx; yLen = p.Ly; zLen = p.Lz;
         dXi = 1.0 / double(globalSize[0] - 1);
         dEt = 1.0 / double(globalSize[1] - 1);
         dZt = 1.0 / double(globalSize[2] - 1);
+        if (planar) { yLen = 1.0; dEt = 1.0; }
         for (int d = 0; d < 3; ++d) {
             staggrCoreSize[d] = globalSize[d];           // grid.cc:182-188 at npX = npY = 1
             collocCoreSize[d] = staggrCoreSize[d] - 1;   // grid.cc:230
         }
+        if (planar) collocCoreSize[1] = 1;
         // grid.cc:333-352 (global transformed grid = local at np = 1)
         xi.resize(-1, globalSize[0]); et.resize(-1, globalSize[1]); zt.resize(-1, globalSize[2]);
         for (int i = -1; i < globalSize[0] + 1; i++) xi(i) = double(i) * dXi;
@@ -149,7 +155,7 @@ struct Grid {
         const A1 *tc[3] = {&xi, &et, &zt};
         A1 *sco[3] = {&xStaggr, &yStaggr, &zStaggr}, *cco[3] = {&xColloc, &yColloc, &zColloc};
         for (int d = 0; d < 3; ++d) {
-            if (gtype[d] != 2) continue;
+            if (gtype[d] != 2 || (planar && d == 1)) continue;
             const double b = beta[d], Ld = L[d];
             const A1 &t = *tc[d];
             auto metrics = [&](A1 *const m[3], int i, double x) {
@@ -185,6 +191,7 @@ struct Field {
             blb[d] = 0; bub[d] = cnt[d] - 1;
             if (stag[d] && !per[d]) { blb[d] += 1; bub[d] -= 1; }   // field.cc:206-219
         }
+        if (g.planar) { blb[1] = 0; bub[1] = 0; }   // field.cc:221-224
         F.resize(-1, -1, -1, cnt[0], cnt[1], cnt[2]);
     }
     int w0(int d) const { return blb[d] - 1; }   // field.cc:269-285
@@ -195,7 +202,7 @@ struct Field {
 // the core range of the other two axes, then the four x-y edge copies over the
 // core z range.  Edge neighbours are always periodic (parallel.cc:124-130) and
 // are never reset by hydro::checkPeriodic (hydro.cc:174-212).
-static void syncData(A3 &F, const Field &f, bool xPer, bool yPer) {
+static void syncData(A3 &F, const Field &f, bool xPer, bool yPer, bool planar = false) {
     int cx = f.cnt[0], cy = f.cnt[1], cz = f.cnt[2];
     int lsx = f.stag[0] ? 1 : 0, hsx = cx - 1 - (f.stag[0] ? 1 : 0);
     int lsy = f.stag[1] ? 1 : 0, hsy = cy - 1 - (f.stag[1] ? 1 : 0);
@@ -205,6 +212,8 @@ static void syncData(A3 &F, const Field &f, bool xPer, bool yPer) {
             F(cx, j, k) = F(lsx, j, k);
         }
     }
+    // 2D: no y neighbours and no edge neighbours (parallel.cc:118-130, hydro.cc:188-191)
+    if (planar) return;
     if (yPer) {
         for (int i = 0; i < cx; ++i) for (int k = 0; k < cz; ++k) {
             F(i, -1, k) = F(i, hsy, k);
@@ -278,6 +287,8 @@ struct Multigrid {
     std::vector<A3> pressureData, residualData, tmpDataArray, smoothedPres;
     std::vector<int> xEnd, yEnd, zEnd, strideValues;
     std::vector<double> hx, hy, hz, hxhy, hyhz, hzhx, hxhyhz;
+    std::vector<double> hx2, hz2;   // 2D (poisson.cc:406-409, 426-428)
+    bool planar = false;
     std::vector<A1> xixx, xix2, etyy, ety2, ztzz, ztz2;
     int vLevel = 0, maxCount = 0;
     bool zeroBC = false;
@@ -293,7 +304,9 @@ struct Multigrid {
             xEnd[i] = int(std::pow(2, g->sizeIndex[0] - i));
             yEnd[i] = int(std::pow(2, g->sizeIndex[1] - i));
             zEnd[i] = int(std::pow(2, g->sizeIndex[2] - i));
+            if (g->planar) yEnd[i] = 0;   // poisson.cc:339-340: one y point on every level
         }
+        planar = g->planar;
         maxCount = (xEnd[d] + 2) * (yEnd[d] + 2) * (zEnd[d] + 2);                    // poisson.cc:360-361
         hx.resize(d + 1); hy.resize(d + 1); hz.resize(d + 1);
         hxhy.resize(d + 1); hyhz.resize(d + 1); hzhx.resize(d + 1); hxhyhz.resize(d + 1);
@@ -305,6 +318,11 @@ struct Multigrid {
             hyhz[i] = std::pow(strideValues[i], 4.0) * std::pow(g->dEt, 2.0) * std::pow(g->dZt, 2.0);
             hzhx[i] = std::pow(strideValues[i], 4.0) * std::pow(g->dZt, 2.0) * std::pow(g->dXi, 2.0);
             hxhyhz[i] = std::pow(strideValues[i], 6.0) * std::pow(g->dXi, 2.0) * std::pow(g->dEt, 2.0) * std::pow(g->dZt, 2.0);
+        }
+        hx2.resize(d + 1); hz2.resize(d + 1);
+        for (int i = 0; i <= d; i++) {
+            hx2[i] = std::pow(strideValues[i] * g->dXi, 2.0);
+            hz2[i] = std::pow(strideValues[i] * g->dZt, 2.0);
         }
         xixx.resize(d + 1); xix2.resize(d + 1); etyy.resize(d + 1); ety2.resize(d + 1); ztzz.resize(d + 1); ztz2.resize(d + 1);
         for (int n = 0; n <= d; ++n) {                                               // poisson.cc:463-495
@@ -369,7 +387,7 @@ struct Multigrid {
             for (int j = -1; j <= Y + 1; ++j) for (int k = -1; k <= Z + 1; ++k) a(X + 1, j, k) = a(1, j, k);
             for (int j = -1; j <= Y + 1; ++j) for (int k = -1; k <= Z + 1; ++k) a(-1, j, k) = a(X - 1, j, k);
         }
-        if (p.yPer) {
+        if (p.yPer && !planar) {   // 2D: no y neighbours (poisson_d2.cc updatePads exchanges x only)
             for (int i = -1; i <= X + 1; ++i) for (int k = -1; k <= Z + 1; ++k) a(i, Y + 1, k) = a(i, 1, k);
             for (int i = -1; i <= X + 1; ++i) for (int k = -1; k <= Z + 1; ++k) a(i, -1, k) = a(i, Y - 1, k);
         }
@@ -391,7 +409,7 @@ struct Multigrid {
                 }
             }
         }
-        if (!p.yPer) {
+        if (!p.yPer && !planar) {   // 2D: no y walls (poisson_d2.cc:300-361)
             for (int i = -1; i <= X + 1; ++i) for (int k = -1; k <= Z + 1; ++k) {
                 if (p.testPoisson) {
                     if (zeroBC) { a(i, -1, k) = -a(i, 1, k); a(i, Y + 1, k) = -a(i, Y - 1, k); }
@@ -416,8 +434,14 @@ struct Multigrid {
         }
     }
 
-    // Laplacian at level l, the expression of poisson_d3.cc:99-105.
+    // Laplacian at level l, the expression of poisson_d3.cc:99-105
+    // (poisson_d2.cc:97-100 in 2D).
     inline double lap(const A3 &P, int l, int i, int j, int k) const {
+        if (planar)
+            return xix2[l](i) * (P(i + 1, j, k) - 2.0 * P(i, j, k) + P(i - 1, j, k)) / (hx[l] * hx[l]) +
+                   xixx[l](i) * (P(i + 1, j, k) - P(i - 1, j, k)) / (2.0 * hx[l]) +
+                   ztz2[l](k) * (P(i, j, k + 1) - 2.0 * P(i, j, k) + P(i, j, k - 1)) / (hz[l] * hz[l]) +
+                   ztzz[l](k) * (P(i, j, k + 1) - P(i, j, k - 1)) / (2.0 * hz[l]);
         return xix2[l](i) * (P(i + 1, j, k) - 2.0 * P(i, j, k) + P(i - 1, j, k)) / (hx[l] * hx[l]) +
                xixx[l](i) * (P(i + 1, j, k) - P(i - 1, j, k)) / (2.0 * hx[l]) +
                ety2[l](j) * (P(i, j + 1, k) - 2.0 * P(i, j, k) + P(i, j - 1, k)) / (hy[l] * hy[l]) +
@@ -426,8 +450,16 @@ struct Multigrid {
                ztzz[l](k) * (P(i, j, k + 1) - P(i, j, k - 1)) / (2.0 * hz[l]);
     }
 
-    // Gauss-Seidel / Jacobi update, the expression of poisson_d3.cc:140-147.
+    // Gauss-Seidel / Jacobi update, the expression of poisson_d3.cc:140-147
+    // (poisson_d2.cc:126-131 in 2D).
     inline double update(const A3 &P, const A3 &R, int l, int i, int j, int k) const {
+        if (planar)
+            return (hz2[l] * xix2[l](i) * (P(i + 1, j, k) + P(i - 1, j, k)) * 2.0 +
+                    hz2[l] * xixx[l](i) * (P(i + 1, j, k) - P(i - 1, j, k)) * hx[l] +
+                    hx2[l] * ztz2[l](k) * (P(i, j, k + 1) + P(i, j, k - 1)) * 2.0 +
+                    hx2[l] * ztzz[l](k) * (P(i, j, k + 1) - P(i, j, k - 1)) * hz[l] -
+                    2.0 * hzhx[l] * R(i, j, k)) /
+                   (4.0 * (hz2[l] * xix2[l](i) + hx2[l] * ztz2[l](k)));
         return (hyhz[l] * xix2[l](i) * (P(i + 1, j, k) + P(i - 1, j, k)) * 2.0 +
                 hyhz[l] * xixx[l](i) * (P(i + 1, j, k) - P(i - 1, j, k)) * hx[l] +
                 hzhx[l] * ety2[l](j) * (P(i, j + 1, k) + P(i, j - 1, k)) * 2.0 +
@@ -500,6 +532,18 @@ struct Multigrid {
         vLevel += 1;
         const A3 &T = tmpDataArray[pLevel];
         A3 &R = residualData[vLevel];
+        if (planar) {   // poisson_d2.cc:207-225: 9-point full weighting in the y = 0 plane
+            for (int i = 0; i <= xEnd[vLevel]; ++i) {
+                int i2 = i * 2;
+                for (int k = 0; k <= zEnd[vLevel]; ++k) {
+                    int k2 = k * 2;
+                    double facePoints = (T(i2 + 1, 0, k2) + T(i2 - 1, 0, k2) + T(i2, 0, k2 + 1) + T(i2, 0, k2 - 1)) * 0.125;
+                    double vertPoints = (T(i2 + 1, 0, k2 + 1) + T(i2 + 1, 0, k2 - 1) + T(i2 - 1, 0, k2 + 1) + T(i2 - 1, 0, k2 - 1)) * 0.0625;
+                    R(i, 0, k) = facePoints + vertPoints + T(i2, 0, k2) * 0.25;
+                }
+            }
+            return;
+        }
 #pragma omp parallel for schedule(static)
         for (int i = 0; i <= xEnd[vLevel]; ++i) {
             int i2 = i * 2;
@@ -796,6 +840,7 @@ struct Solver {
     bool isScalar = false;
     double inverseRe = 0, nu = 0, kappa = 0, Fb = 0;
     double hx, hy, hz, hz2hx2, hx2hy2, hy2hz2, hx2hy2hz2;
+    double hx2 = 0, hz2 = 0;   // 2D (hydro.cc:229-232)
     int maxIterations = 0;
     double dt = 0;
     double totalVol = 0;
@@ -837,6 +882,8 @@ struct Solver {
         hx2hy2 = std::pow(g.dXi, 2.0) * std::pow(g.dEt, 2.0);
         hy2hz2 = std::pow(g.dEt, 2.0) * std::pow(g.dZt, 2.0);
         hx2hy2hz2 = std::pow(g.dXi, 2.0) * std::pow(g.dEt, 2.0) * std::pow(g.dZt, 2.0);
+        hx2 = std::pow(g.dXi, 2.0);
+        hz2 = std::pow(g.dZt, 2.0);
         dt = p.tStp;
         initVBC();
         if (isScalar) initTBC();
@@ -844,7 +891,8 @@ struct Solver {
         // tseries.cc:72-108 (np = 1)
         totalVol = 0.0;
         for (int iX = 0; iX <= fp.cnt[0] - 1; iX++) for (int iY = 0; iY <= fp.cnt[1] - 1; iY++) for (int iZ = 0; iZ <= fp.cnt[2] - 1; iZ++)
-            totalVol += (g.dXi / g.xi_xColloc(iX)) * (g.dEt / g.et_yColloc(iY)) * (g.dZt / g.zt_zColloc(iZ));
+            totalVol += g.planar ? (g.dXi / g.xi_xColloc(iX)) * (g.dZt / g.zt_zColloc(iZ))   // tseries.cc:93-99
+                                 : (g.dXi / g.xi_xColloc(iX)) * (g.dEt / g.et_yColloc(iY)) * (g.dZt / g.zt_zColloc(iZ));
     }
 
     // hydro.cc:287-371 (wall order as used by imposeU/V/WBCs: Lft, Rgt, Frn, Bak, Top, Bot)
@@ -856,24 +904,27 @@ struct Solver {
             if (p.probType == 3) { u.push_back(mk(BC_DIR_FC, 0, 1.0)); u.push_back(mk(BC_NEU_FC, 1, 0.0)); }
             else { u.push_back(mk(BC_DIR_FC, 0, 0.0)); u.push_back(mk(BC_DIR_FC, 1, 0.0)); }
         }
-        if (!p.yPer) { u.push_back(mk(BC_DIR_CC, 2, 0.0)); u.push_back(mk(BC_DIR_CC, 3, 0.0)); }
+        // 2D: no front and back walls, no Vy boundary objects (hydro.cc:298-301, 320-353)
+        if (!p.yPer && !g.planar) { u.push_back(mk(BC_DIR_CC, 2, 0.0)); u.push_back(mk(BC_DIR_CC, 3, 0.0)); }
         if (p.zPer) { u.push_back(mk(BC_PER_CC, 5, 0)); u.push_back(mk(BC_PER_CC, 4, 0)); }
         else if (p.probType == 1) { u.push_back(mk(BC_DIR_CC, 5, 1.0)); u.push_back(mk(BC_DIR_CC, 4, 0.0)); }
         else { u.push_back(mk(BC_DIR_CC, 5, 0.0)); u.push_back(mk(BC_DIR_CC, 4, 0.0)); }
 
-        if (!p.xPer) {
+        if (!p.xPer && !g.planar) {
             if (p.probType == 3) { v.push_back(mk(BC_DIR_CC, 0, 0.0)); v.push_back(mk(BC_NEU_CC, 1, 0.0)); }
             else { v.push_back(mk(BC_DIR_CC, 0, 0.0)); v.push_back(mk(BC_DIR_CC, 1, 0.0)); }
         }
-        if (!p.yPer) { v.push_back(mk(BC_DIR_FC, 2, 0.0)); v.push_back(mk(BC_DIR_FC, 3, 0.0)); }
-        if (p.zPer) { v.push_back(mk(BC_PER_CC, 5, 0)); v.push_back(mk(BC_PER_CC, 4, 0)); }
-        else { v.push_back(mk(BC_DIR_CC, 5, 0.0)); v.push_back(mk(BC_DIR_CC, 4, 0.0)); }
+        if (!g.planar) {
+            if (!p.yPer) { v.push_back(mk(BC_DIR_FC, 2, 0.0)); v.push_back(mk(BC_DIR_FC, 3, 0.0)); }
+            if (p.zPer) { v.push_back(mk(BC_PER_CC, 5, 0)); v.push_back(mk(BC_PER_CC, 4, 0)); }
+            else { v.push_back(mk(BC_DIR_CC, 5, 0.0)); v.push_back(mk(BC_DIR_CC, 4, 0.0)); }
+        }
 
         if (!p.xPer) {
             if (p.probType == 3) { w.push_back(mk(BC_DIR_CC, 0, 0.0)); w.push_back(mk(BC_NEU_CC, 1, 0.0)); }
             else { w.push_back(mk(BC_DIR_CC, 0, 0.0)); w.push_back(mk(BC_DIR_CC, 1, 0.0)); }
         }
-        if (!p.yPer) { w.push_back(mk(BC_DIR_CC, 2, 0.0)); w.push_back(mk(BC_DIR_CC, 3, 0.0)); }
+        if (!p.yPer && !g.planar) { w.push_back(mk(BC_DIR_CC, 2, 0.0)); w.push_back(mk(BC_DIR_CC, 3, 0.0)); }
         if (p.zPer) { w.push_back(mk(BC_PER_FC, 5, 0)); w.push_back(mk(BC_PER_FC, 4, 0)); }
         else { w.push_back(mk(BC_DIR_FC, 5, 0.0)); w.push_back(mk(BC_DIR_FC, 4, 0.0)); }
     }
@@ -887,7 +938,7 @@ struct Solver {
             if (p.probType == 5 || p.probType == 6 || p.probType == 8) { t.push_back(mk(BC_NEU_CC, 0, 0.0)); t.push_back(mk(BC_NEU_CC, 1, 0.0)); }
             else if (p.probType == 7) { t.push_back(mk(BC_DIR_CC, 0, 1.0)); t.push_back(mk(BC_DIR_CC, 1, 0.0)); }
         }
-        if (!p.yPer) { t.push_back(mk(BC_NEU_CC, 2, 0.0)); t.push_back(mk(BC_NEU_CC, 3, 0.0)); }
+        if (!p.yPer && !g.planar) { t.push_back(mk(BC_NEU_CC, 2, 0.0)); t.push_back(mk(BC_NEU_CC, 3, 0.0)); }
         if (p.zPer) { t.push_back(mk(BC_PER_CC, 5, 0)); t.push_back(mk(BC_PER_CC, 4, 0)); }
         else if (p.probType == 5 || p.probType == 8) { t.push_back(mk(BC_DIR_CC, 5, 0.0)); t.push_back(mk(BC_DIR_CC, 4, 1.0)); }
         else if (p.probType == 6) { t.push_back(mk(BC_DIR_CC, 5, 1.0)); t.push_back(mk(BC_DIR_CC, 4, 0.0)); }
@@ -896,7 +947,7 @@ struct Solver {
     // hydro.cc:386-461, scalar.cc:240-255
     void imposeBCs(int c) {
         Field &f = fieldOf(c);
-        syncData(f.F, f, p.xPer, p.yPer);
+        syncData(f.F, f, p.xPer, p.yPer, g.planar);
         for (const BC &b : bcs[c]) {
             int dim = b.wall / 2;
             if (dim == 0 && p.xPer) continue;
@@ -986,6 +1037,7 @@ struct Solver {
     // vfield::computeDiff (vfield.cc:104-146) / sfield::computeDiff (sfield.cc:86-100)
     void computeDiff(const Field &f, A3 &H) {
         for (int d = 0; d < 3; ++d) {
+            if (g.planar && d == 1) continue;   // vfield.cc:109-113, sfield.cc:91-95
 #pragma omp parallel for schedule(static)
             for (int i = 0; i < f.cnt[0]; ++i) for (int j = 0; j < f.cnt[1]; ++j) for (int k = 0; k < f.cnt[2]; ++k)
                 H(i, j, k) += d2(f, d, i, j, k);
@@ -996,6 +1048,7 @@ struct Solver {
     void computeNLin(const Field &f, A3 &H) {
         const Field *vsrc[3] = {&fx, &fy, &fz};
         for (int d = 0; d < 3; ++d) {
+            if (g.planar && d == 1) continue;   // vfield.cc:174-190, sfield.cc:123-131
             int sh[4][3];
             int ns = slices(f, d, sh);
             const A3 &S = vsrc[d]->F;
@@ -1013,8 +1066,9 @@ struct Solver {
     void gradient(const A3 &S) {
         for (int i = 0; i < fx.cnt[0]; ++i) for (int j = 0; j < fx.cnt[1]; ++j) for (int k = 0; k < fx.cnt[2]; ++k)
             gradX(i, j, k) = g.xi_xColloc(i) * (S(i + 1, j, k) - S(i, j, k)) / g.dXi;
-        for (int i = 0; i < fy.cnt[0]; ++i) for (int j = 0; j < fy.cnt[1]; ++j) for (int k = 0; k < fy.cnt[2]; ++k)
-            gradY(i, j, k) = g.et_yColloc(j) * (S(i, j + 1, k) - S(i, j, k)) / g.dEt;
+        if (!g.planar)   // sfield.cc:167-169
+            for (int i = 0; i < fy.cnt[0]; ++i) for (int j = 0; j < fy.cnt[1]; ++j) for (int k = 0; k < fy.cnt[2]; ++k)
+                gradY(i, j, k) = g.et_yColloc(j) * (S(i, j + 1, k) - S(i, j, k)) / g.dEt;
         for (int i = 0; i < fz.cnt[0]; ++i) for (int j = 0; j < fz.cnt[1]; ++j) for (int k = 0; k < fz.cnt[2]; ++k)
             gradZ(i, j, k) = g.zt_zColloc(k) * (S(i, j, k + 1) - S(i, j, k)) / g.dZt;
     }
@@ -1023,10 +1077,15 @@ struct Solver {
     void divergence(A3 &divV) {
         divV.fill(0.0);
         const A3 &X = fx.F, &Y = fy.F, &Z = fz.F;
-        for (int i = 0; i < fp.cnt[0]; ++i) for (int j = 0; j < fp.cnt[1]; ++j) for (int k = 0; k < fp.cnt[2]; ++k)
-            divV(i, j, k) = g.xi_xStaggr(i) * (X(i, j, k) - X(i - 1, j, k)) / g.dXi +
-                            g.et_yStaggr(j) * (Y(i, j, k) - Y(i, j - 1, k)) / g.dEt +
-                            g.zt_zStaggr(k) * (Z(i, j, k) - Z(i, j, k - 1)) / g.dZt;
+        for (int i = 0; i < fp.cnt[0]; ++i) for (int j = 0; j < fp.cnt[1]; ++j) for (int k = 0; k < fp.cnt[2]; ++k) {
+            if (g.planar)   // vfield.cc:312-314
+                divV(i, j, k) = g.xi_xStaggr(i) * (X(i, j, k) - X(i - 1, j, k)) / g.dXi +
+                                g.zt_zStaggr(k) * (Z(i, j, k) - Z(i, j, k - 1)) / g.dZt;
+            else
+                divV(i, j, k) = g.xi_xStaggr(i) * (X(i, j, k) - X(i - 1, j, k)) / g.dXi +
+                                g.et_yStaggr(j) * (Y(i, j, k) - Y(i, j - 1, k)) / g.dEt +
+                                g.zt_zStaggr(k) * (Z(i, j, k) - Z(i, j, k - 1)) / g.dZt;
+        }
     }
 
     // buoyantForce::addForcing (buoyantForce.cc:59-68)
@@ -1064,6 +1123,16 @@ struct Solver {
         while (true) {
 #pragma omp parallel for schedule(static)
             for (int iX = f.blb[0]; iX <= f.bub[0]; iX++) for (int iY = f.blb[1]; iY <= f.bub[1]; iY++) for (int iZ = f.blb[2]; iZ <= f.bub[2]; iZ++) {
+                if (g.planar) {   // hydro_d2.cc:293-299, scalar_d2.cc:425-431
+                    double A = hz2 * (*mx)(iX) * (V(iX + 1, iY, iZ) + V(iX - 1, iY, iZ)) + hx2 * (*mz)(iZ) * (V(iX, iY, iZ + 1) + V(iX, iY, iZ - 1));
+                    if (!useNu)
+                        guess(iX, iY, iZ) = (A * dt / (hz2hx2 * 2.0 * p.Re) + rhs(iX, iY, iZ)) /
+                                            (1.0 + dt * ((hz2 * (*mx)(iX) + hx2 * (*mz)(iZ))) / (p.Re * hz2hx2));
+                    else
+                        guess(iX, iY, iZ) = (A * dt * coef / (hz2hx2 * 2.0) + rhs(iX, iY, iZ)) /
+                                            (1.0 + dt * coef * ((hz2 * (*mx)(iX) + hx2 * (*mz)(iZ))) / hz2hx2);
+                    continue;
+                }
                 double A = hy2hz2 * (*mx)(iX) * (V(iX + 1, iY, iZ) + V(iX - 1, iY, iZ)) +
                            hz2hx2 * (*my)(iY) * (V(iX, iY + 1, iZ) + V(iX, iY - 1, iZ)) +
                            hx2hy2 * (*mz)(iZ) * (V(iX, iY, iZ + 1) + V(iX, iY, iZ - 1));
@@ -1079,9 +1148,12 @@ struct Solver {
             imposeBCs(c);
 #pragma omp parallel for schedule(static)
             for (int iX = f.blb[0]; iX <= f.bub[0]; iX++) for (int iY = f.blb[1]; iY <= f.bub[1]; iY++) for (int iZ = f.blb[2]; iZ <= f.bub[2]; iZ++) {
-                double L = (*mx)(iX) * (V(iX + 1, iY, iZ) - 2.0 * V(iX, iY, iZ) + V(iX - 1, iY, iZ)) / (hx * hx) +
-                           (*my)(iY) * (V(iX, iY + 1, iZ) - 2.0 * V(iX, iY, iZ) + V(iX, iY - 1, iZ)) / (hy * hy) +
-                           (*mz)(iZ) * (V(iX, iY, iZ + 1) - 2.0 * V(iX, iY, iZ) + V(iX, iY, iZ - 1)) / (hz * hz);
+                double L = g.planar   // hydro_d2.cc:305-309
+                               ? (*mx)(iX) * (V(iX + 1, iY, iZ) - 2.0 * V(iX, iY, iZ) + V(iX - 1, iY, iZ)) / (hx2) +
+                                     (*mz)(iZ) * (V(iX, iY, iZ + 1) - 2.0 * V(iX, iY, iZ) + V(iX, iY, iZ - 1)) / (hz2)
+                               : (*mx)(iX) * (V(iX + 1, iY, iZ) - 2.0 * V(iX, iY, iZ) + V(iX - 1, iY, iZ)) / (hx * hx) +
+                                     (*my)(iY) * (V(iX, iY + 1, iZ) - 2.0 * V(iX, iY, iZ) + V(iX, iY - 1, iZ)) / (hy * hy) +
+                                     (*mz)(iZ) * (V(iX, iY, iZ + 1) - 2.0 * V(iX, iY, iZ) + V(iX, iY, iZ - 1)) / (hz * hz);
                 double val = useNu ? V(iX, iY, iZ) - L * 0.5 * dt * coef
                                    : V(iX, iY, iZ) - L * 0.5 * dt * inverseRe;
                 lapA(iX, iY, iZ) = std::fabs(val - rhs(iX, iY, iZ));
@@ -1149,8 +1221,9 @@ struct Solver {
         for (size_t n = 0; n < nseX.v.size(); ++n) nseX.v[n] += fx.F.v[n];
         for (size_t n = 0; n < nseY.v.size(); ++n) nseY.v[n] += fy.F.v[n];
         for (size_t n = 0; n < nseZ.v.size(); ++n) nseZ.v[n] += fz.F.v[n];
-        syncData(nseX, fx, p.xPer, p.yPer); syncData(nseY, fy, p.xPer, p.yPer); syncData(nseZ, fz, p.xPer, p.yPer);
+        syncData(nseX, fx, p.xPer, p.yPer, g.planar); syncData(nseY, fy, p.xPer, p.yPer, g.planar); syncData(nseZ, fz, p.xPer, p.yPer, g.planar);
         for (int c = 0; c < 3; ++c) {
+            if (g.planar && c == VY) continue;   // hydro_d2.cc:242-244: solveVx, solveVz
             int it = 0; double e = 0;
             int s = cnSolve(c, &it, &e);
             if (st) st->cn_iters[c] = it;
@@ -1163,7 +1236,7 @@ struct Solver {
         double res = 0;
         int cyc = mg.mgSolve(Pp, mgRHS, &res);
         if (st) { st->vcycles = cyc; st->mg_residual = res; st->coarse_iters = (int)(mg.coarseIters - ci0); }
-        syncData(Pp, fp, p.xPer, p.yPer);
+        syncData(Pp, fp, p.xPer, p.yPer, g.planar);
         if (p.testPoisson) fp.F.fill(0.0);
         for (size_t n = 0; n < fp.F.v.size(); ++n) fp.F.v[n] += Pp.v[n];
         gradient(Pp);
@@ -1179,13 +1252,15 @@ struct Solver {
             computeNLin(ft, tmpRHS);
             for (double &x : tmpRHS.v) x *= dt;
             for (size_t n = 0; n < tmpRHS.v.size(); ++n) tmpRHS.v[n] += ft.F.v[n];
-            syncData(tmpRHS, ft, p.xPer, p.yPer);
+            syncData(tmpRHS, ft, p.xPer, p.yPer, g.planar);
             int it = 0; double e = 0;
             int s = cnSolve(TF, &it, &e);
             if (st) st->cn_iters[3] = it;
             if (s != SARAS_OK) { if (st) st->status = s; return s; }
         }
-        imposeBCs(VX); imposeBCs(VY); imposeBCs(VZ);
+        imposeBCs(VX);
+        if (!g.planar) imposeBCs(VY);   // hydro_d2.cc:278-279: imposeUBCs, imposeWBCs
+        imposeBCs(VZ);
         if (isScalar) imposeBCs(TF);
         return SARAS_OK;
     }
@@ -1202,6 +1277,7 @@ struct Solver {
     void computeTStp(double &dtOut) const {
         double delx = g.dXi, dely = g.dEt, delz = g.dZt;
         double Umax = fieldMax(fx.F), Vmax = fieldMax(fy.F), Wmax = fieldMax(fz.F);
+        if (g.planar) { dely = 0.0; Vmax = 1.0; }   // vfield.cc:273-279
         dtOut = p.courantNumber * (delx / Umax + dely / Vmax + delz / Wmax);
     }
 
@@ -1214,6 +1290,15 @@ struct Solver {
         double localEnergy = 0.0, localUzT = 0.0;
         for (int iX = 0; iX <= fp.cnt[0] - 1; iX++) for (int iY = 0; iY <= fp.cnt[1] - 1; iY++) for (int iZ = 0; iZ <= fp.cnt[2] - 1; iZ++) {
             double dv = (g.dXi / g.xi_xColloc(iX)) * (g.dEt / g.et_yColloc(iY)) * (g.dZt / g.zt_zColloc(iZ));
+            if (g.planar) {   // tseries.cc:149-156, 210-219
+                localEnergy += (std::pow((fx.F(iX - 1, iY, iZ) + fx.F(iX, iY, iZ)) / 2.0, 2.0) +
+                                std::pow((fz.F(iX, iY, iZ - 1) + fz.F(iX, iY, iZ)) / 2.0, 2.0)) *
+                               (g.dXi / g.xi_xColloc(iX)) * (g.dZt / g.zt_zColloc(iZ));
+                if (isScalar)
+                    localUzT += ((fz.F(iX, iY, iZ) + fz.F(iX, iY, iZ - 1)) / 2.0) * ft.F(iX, iY, iZ) * (g.dXi / g.xi_xColloc(iX)) *
+                                (g.dZt / g.zt_zColloc(iZ));
+                continue;
+            }
             localEnergy += (std::pow((fx.F(iX - 1, iY, iZ) + fx.F(iX, iY, iZ)) / 2.0, 2.0) +
                             std::pow((fy.F(iX, iY - 1, iZ) + fy.F(iX, iY, iZ)) / 2.0, 2.0) +
                             std::pow((fz.F(iX, iY, iZ - 1) + fz.F(iX, iY, iZ)) / 2.0, 2.0)) *
@@ -1361,7 +1446,7 @@ int orc_sync_field(void *h, int field) {
     const Field *f = (field == SARAS_FIELD_VX || field == SARAS_FIELD_NSE_X || field == SARAS_FIELD_GRAD_X) ? &s.fx :
                      (field == SARAS_FIELD_VY || field == SARAS_FIELD_NSE_Y || field == SARAS_FIELD_GRAD_Y) ? &s.fy :
                      (field == SARAS_FIELD_VZ || field == SARAS_FIELD_NSE_Z || field == SARAS_FIELD_GRAD_Z) ? &s.fz : &s.fp;
-    syncData(*a, *f, s.p.xPer, s.p.yPer);
+    syncData(*a, *f, s.p.xPer, s.p.yPer, s.g.planar);
     return SARAS_OK;
 }
 int orc_vfield_compute_diff(void *h) {

@@ -405,13 +405,19 @@ def grid_coords(params):
     tangent-hyperbolic map of grid.cc:442-519 (numpy's tanh: these arrays build
     initial conditions; the solver's own coordinates are Solver.grid_coords)."""
     out = []
-    for ind, L, gt, beta in ((params.xInd, params.Lx, params.xGrid, params.betaX), (params.yInd, params.Ly, params.yGrid, params.betaY),
-                             (params.zInd, params.Lz, params.zGrid, params.betaZ)):
+    for axis, (ind, L, gt, beta) in enumerate(((params.xInd, params.Lx, params.xGrid, params.betaX),
+                                                (params.yInd, params.Ly, params.yGrid, params.betaY),
+                                                (params.zInd, params.Lz, params.zGrid, params.betaZ))):
         n = 2 ** ind
         d = 1.0 / n
         xi = np.arange(-1, n + 2, dtype=np.float64) * d
         xs = L * xi
         xc = L * (xi[:-1] + xi[1:]) / 2.0
+        if ind == 0 and axis == 1:
+            # the 2D solver's single y point: coordinates keep their default 1
+            # (grid.cc:300-320, createUniformGrid skips y under PLANAR)
+            out.append((np.ones(3), np.ones(3)))
+            continue
         if gt == 2:
             t = np.tanh(beta)
             xs[1:n + 2] = L * (1.0 - np.tanh(beta * (1.0 - 2.0 * xi[1:n + 2])) / t) / 2.0
@@ -499,6 +505,20 @@ def taylor_green_velocity(params):
     Vy = (-_cos_pi(vs[0], n[0])[:, None, None] * _sin_pi(fc[1], n[1])[None, :, None] *
           _cos_pi(vs[2], n[2])[None, None, :])
     return Vx, Vy
+
+
+def taylor_green_velocity_2d(params):
+    """taylorGreen::initializeField in 2D (taylorGreen.cc:57-79): on the y = 0
+    plane u = sin(2 pi x / Lx) cos(2 pi z / Lz), w = -cos(2 pi x / Lx) sin(2 pi z / Lz),
+    correctly rounded as in 3D; the y ghost planes stay 0.  Returns (Vx, Vz)."""
+    n = [2 ** params.xInd, 2 ** params.zInd]
+    vs = [2 * np.arange(-1, m + 2, dtype=np.int64) for m in n]
+    fc = [2 * np.arange(-1, m + 1, dtype=np.int64) + 1 for m in n]
+    Vx = np.zeros((n[0] + 2, 3, n[1] + 3))
+    Vz = np.zeros((n[0] + 3, 3, n[1] + 2))
+    Vx[:, 1, :] = _sin_pi(fc[0], n[0])[:, None] * _cos_pi(vs[1], n[1])[None, :]
+    Vz[:, 1, :] = -_cos_pi(vs[0], n[0])[:, None] * _sin_pi(fc[1], n[1])[None, :]
+    return Vx, Vz
 
 
 def taylor_green_pressure(params):

@@ -207,3 +207,35 @@ def test_dirichlet_r2_over_6():
     ana = (x[:, None, None] ** 2 + x[None, :, None] ** 2 + x[None, None, :] ** 2) / 6.0
     P = o.get(F.FIELD_PP)[1:-1, 1:-1, 1:-1]
     assert np.max(np.abs(P - ana)) < 1e-3
+
+
+def _planar_tgv(ind):
+    p = C.tgv(ind=ind, depth=2)
+    p.yInd = 0
+    return p
+
+
+def test_planar_divergence_and_diffusion():
+    """The 2D (PLANAR) solver: one y point, no y terms (vfield.cc:104-146,
+    299-320 under PLANAR).  For the 2D Taylor-Green field u = sin x cos z,
+    w = -cos x sin z: the staggered divergence vanishes to rounding, and
+    computeDiff with the Crank-Nicolson half approximates Laplacian(u) / 2 = -u
+    with an error falling by 4 per halving of h (measured order >= 1.9)."""
+    from saras_gb300 import taylor_green_velocity_2d
+    errs = []
+    for ind in (4, 5, 6):
+        p = _planar_tgv(ind)
+        o = Oracle(p)
+        Vx, Vz = taylor_green_velocity_2d(p)
+        assert o.dims(F.FIELD_VX) == Vx.shape and o.dims(F.FIELD_VZ) == Vz.shape and o.dims(F.FIELD_P)[1] == 3
+        o.set(F.FIELD_VX, Vx)
+        o.set(F.FIELD_VZ, Vz)
+        o.vfield_divergence()
+        assert np.max(np.abs(o.get(F.FIELD_MGRHS))) < 1e-12
+        for f in (F.FIELD_NSE_X, F.FIELD_NSE_Y, F.FIELD_NSE_Z):
+            o.set(f, np.zeros(o.dims(f)))
+        o.vfield_compute_diff()
+        H = o.get(F.FIELD_NSE_X)
+        errs.append(np.max(np.abs(H[1:-1, 1, 1:-1] + Vx[1:-1, 1, 1:-1])))
+        assert np.all(o.get(F.FIELD_NSE_Y) == 0.0)   # Vy takes no part in 2D
+    assert min(_orders(errs)) >= 1.9, (errs, _orders(errs))
