@@ -257,7 +257,7 @@ int saras_parse_yaml(const char *path, saras_params *p, char *err, int errlen) {
     for (auto &x : bools) if (kv.count(x.k) && !to_bool(kv[x.k], *x.v)) return fail(err, errlen, std::string("bad boolean for ") + x.k, SARAS_BAD_CONFIG);
     std::string domain = kv["Program/Domain Type"], mesh = kv["Mesh/Mesh Type"];
     // parser::checkData (parser.cc:250-352)
-    if (p->yInd == 0) return fail(err, errlen, "Y Index parameter of YAML file is 0 for 3D simulation", SARAS_BAD_CONFIG);
+    // "Y Index" 0 selects the 2D (PLANAR) solver at run time (parser.cc:252-262)
     if (p->npX < 1) p->npX = 1;
     if (p->npY < 1) p->npY = 1;
     if (domain.size() != 3) return fail(err, errlen, "Domain type string is not correct", SARAS_BAD_CONFIG);
@@ -271,23 +271,29 @@ int saras_parse_yaml(const char *path, saras_params *p, char *err, int errlen) {
     // One GPU runs the whole domain (np = 1 semantics); the decomposition check
     // uses the full grid.
     int coarsest = (int)std::pow(2, p->vcDepth + 1);
-    if ((int)std::pow(2, p->xInd) < coarsest || (int)std::pow(2, p->yInd) < coarsest || (int)std::pow(2, p->zInd) < coarsest)
+    if ((int)std::pow(2, p->xInd) < coarsest || (p->yInd != 0 && (int)std::pow(2, p->yInd) < coarsest) || (int)std::pow(2, p->zInd) < coarsest)
         return fail(err, errlen, "The grid size is too coarse to reach the V-Cycle depth specified", SARAS_BAD_CONFIG);
     return SARAS_OK;
 }
 
 static int validate(const saras_params *p, std::string &why) {
-    if (p->xInd < 2 || p->yInd < 2 || p->zInd < 2 || p->xInd > 11 || p->yInd > 11 || p->zInd > 11) { why = "grid index out of range (2..11)"; return SARAS_BAD_CONFIG; }
+    const bool planar = p->yInd == 0;   // the 2D solver
+    if (p->xInd < 2 || (p->yInd < 2 && !planar) || p->zInd < 2 || p->xInd > 11 || p->yInd > 11 || p->zInd > 11) { why = "grid index out of range (2..11; Y Index 0 for 2D)"; return SARAS_BAD_CONFIG; }
     if (p->vcDepth < 1) { why = "V-Cycle Depth must be >= 1"; return SARAS_BAD_CONFIG; }
     int coarsest = (int)std::pow(2, p->vcDepth + 1);
-    if ((1 << p->xInd) < coarsest || (1 << p->yInd) < coarsest || (1 << p->zInd) < coarsest) { why = "grid too coarse for the V-Cycle depth"; return SARAS_BAD_CONFIG; }
+    if ((1 << p->xInd) < coarsest || (!planar && (1 << p->yInd) < coarsest) || (1 << p->zInd) < coarsest) { why = "grid too coarse for the V-Cycle depth"; return SARAS_BAD_CONFIG; }
+    // 2D runs the drop-in form (the GB300 extensions are 3D)
+    if (planar && (p->mgMode != SARAS_MG_REFERENCE || p->fastKernels != 0 || p->guessMode != SARAS_GUESS_PREVIOUS || p->testPoisson)) {
+        why = "the 2D solver (Y Index 0) runs in the drop-in mode only: Multigrid Mode 0, Fast Kernels 0, Guess Mode 0, no Test Poisson";
+        return SARAS_BAD_CONFIG;
+    }
     if (p->xGrid < 0 || p->xGrid > 2 || p->yGrid < 0 || p->yGrid > 2 || p->zGrid < 0 || p->zGrid > 2) { why = "bad grid type"; return SARAS_BAD_CONFIG; }
     // Mesh Type 'D' (double-sided tangent-hyperbolic stretching, grid.cc:442-519)
     // runs in the drop-in mode: the reference's multigrid and FP64 kernels read
     // the metric arrays at every point; the GB300 extensions assume uniform
     // metrics.  ('S', single-sided, builds a uniform grid in the reference,
     // grid.cc:117-131, and does here.)
-    const bool stretched = p->xGrid == 2 || p->yGrid == 2 || p->zGrid == 2;
+    const bool stretched = p->xGrid == 2 || (p->yGrid == 2 && !planar) || p->zGrid == 2;
     if (stretched && (p->mgMode != SARAS_MG_REFERENCE || p->fastKernels != 0 || p->guessMode != SARAS_GUESS_PREVIOUS || p->testPoisson)) {
         why = "stretched meshes (Mesh Type 'D') run in the drop-in mode only: Multigrid Mode 0, Fast Kernels 0, Guess Mode 0, no Test Poisson";
         return SARAS_BAD_CONFIG;

@@ -65,6 +65,8 @@ struct Level {
     // stretched meshes: the level's staggered metrics xix2, xixx, ety2, etyy,
     // ztz2, ztzz (poisson.cc:463-495), device pointers at index 0
     double *metBlock = nullptr;
+    double hx2 = 0, hz2 = 0;         // 2D: pow(2^l dXi, 2), pow(2^l dZt, 2) (poisson.cc:426-428)
+    int planar = 0;
     const double *xix2 = nullptr, *xixx = nullptr, *ety2 = nullptr, *etyy = nullptr, *ztz2 = nullptr, *ztzz = nullptr;
     double *pa() const { return cur == 0 ? a : b; }
     double *pb() const { return cur == 0 ? b : a; }
@@ -98,6 +100,9 @@ struct Ctx {
     // on the core of a stretched axis.  Host arrays start at index -1; device
     // pointers point at index 0.
     bool stretched = false;        // some axis has Mesh Type 'D'
+    // the 2D (PLANAR) solver: "Y Index" 0, one y point (grid.cc:88-92, 232-234);
+    // every y term of the stencils is left out and Vy takes no part
+    bool planar = false;
     std::vector<double> hmet[3][2][3], hcoord[3][2];
     double *dmet = nullptr;
     const double *met[3][2][3] = {};

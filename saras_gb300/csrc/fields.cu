@@ -44,6 +44,7 @@ struct UC {                 // stencil constants of one field
     // divergence (vfield.cc:299-320)
     const double *m1p[3], *mxp[3], *m2p[3], *gcp[3], *gsp[3];
     int var, half;          // half: iScheme 1 (the 0.5 of calcDerivative2xx)
+    int planar;             // 2D: the y terms are left out (vfield.cc, sfield.cc under PLANAR)
 };
 
 static UC make_uc(const Ctx &c, int field) {
@@ -65,6 +66,7 @@ static UC make_uc(const Ctx &c, int field) {
     }
     u.var = c.stretched ? 1 : 0;
     u.half = c.p.iScheme == 1 ? 1 : 0;
+    u.planar = c.planar ? 1 : 0;
     return u;
 }
 
@@ -164,12 +166,13 @@ struct Vel {
 template <int T>
 __device__ __forceinline__ double nlin_update(double H, const View3<const double> &F, const Vel &V, int i, int j, int k, const UC &u) {
     H = H - (interp<T, 0>(V.v[0], i, j, k) * d1_at(F, 0, i, j, k, u)) * (1.0 / Slices<T, 0>::n);
-    H = H - (interp<T, 1>(V.v[1], i, j, k) * d1_at(F, 1, i, j, k, u)) * (1.0 / Slices<T, 1>::n);
+    if (!u.planar) H = H - (interp<T, 1>(V.v[1], i, j, k) * d1_at(F, 1, i, j, k, u)) * (1.0 / Slices<T, 1>::n);
     H = H - (interp<T, 2>(V.v[2], i, j, k) * d1_at(F, 2, i, j, k, u)) * (1.0 / Slices<T, 2>::n);
     return H;
 }
 
 __device__ __forceinline__ double diff_sum(const View3<const double> &F, int i, int j, int k, const UC &u) {
+    if (u.planar) return d2_at(F, 0, i, j, k, u) + d2_at(F, 2, i, j, k, u);
     return d2_at(F, 0, i, j, k, u) + d2_at(F, 1, i, j, k, u) + d2_at(F, 2, i, j, k, u);
 }
 
@@ -214,7 +217,7 @@ __global__ void k_op_diff(View3<double> H, View3<const double> F, Box b, UC u) {
     if (!box_point(b, i, j, k)) return;
     double h = H(i, j, k);
     h += d2_at(F, 0, i, j, k, u);
-    h += d2_at(F, 1, i, j, k, u);
+    if (!u.planar) h += d2_at(F, 1, i, j, k, u);
     h += d2_at(F, 2, i, j, k, u);
     H(i, j, k) = h;
 }
@@ -262,7 +265,7 @@ __global__ void k_divergence(View3<double> D, Vel V, Box full, UC u, double scal
         double tx = (div_m(u, 0, i, j, k) * dx) * u.ih[0];
         double ty = (div_m(u, 1, i, j, k) * dy) * u.ih[1];
         double tz = (div_m(u, 2, i, j, k) * dz) * u.ih[2];
-        out = tx + ty + tz;
+        out = u.planar ? tx + tz : tx + ty + tz;
     }
     if (do_scale) out = out * scale;
     D(i, j, k) = out;
@@ -633,6 +636,7 @@ struct CnArgs {
     const double *mx, *my, *mz;
     double hy2hz2, hz2hx2, hx2hy2, h3, Re, ihx2, ihy2, ihz2;
     int var;
+    int planar;   // 2D (hydro_d2.cc:293-309): no y term in the update and the residual
 };
 
 __device__ __forceinline__ double cn_guess(const CnArgs &a, int i, int j, int k) {
@@ -640,12 +644,13 @@ __device__ __forceinline__ double cn_guess(const CnArgs &a, int i, int j, int k)
     double c1 = a.c1, c2 = a.c2, c3 = a.c3, Dn = a.Dn;
     if (a.var) {
         c1 = a.hy2hz2 * a.mx[i];
-        c2 = a.hz2hx2 * a.my[j];
+        c2 = a.planar ? 0.0 : a.hz2hx2 * a.my[j];
         c3 = a.hx2hy2 * a.mz[k];
-        const double B = c1 + c2 + c3;
+        const double B = a.planar ? c1 + c3 : c1 + c2 + c3;
         Dn = a.scalarForm ? 1.0 + a.dt * a.coef * B / a.h3 : 1.0 + a.dt * B / (a.Re * a.h3);
     }
-    double A = c1 * (V(i + 1, j, k) + V(i - 1, j, k)) + c2 * (V(i, j + 1, k) + V(i, j - 1, k)) + c3 * (V(i, j, k + 1) + V(i, j, k - 1));
+    double A = a.planar ? c1 * (V(i + 1, j, k) + V(i - 1, j, k)) + c3 * (V(i, j, k + 1) + V(i, j, k - 1))
+                        : c1 * (V(i + 1, j, k) + V(i - 1, j, k)) + c2 * (V(i, j + 1, k) + V(i, j - 1, k)) + c3 * (V(i, j, k + 1) + V(i, j, k - 1));
     double num = a.scalarForm ? (A * a.dt) * a.coef / a.X : (A * a.dt) / a.X;
     return (num + a.rhs(i, j, k)) / Dn;
 }
@@ -661,7 +666,12 @@ __global__ void k_cn(CnArgs a) {
                 const View3<const double> &V = a.in;
                 double v0 = V(i, j, k);
                 double L;
-                if (a.var)
+                if (a.planar && a.var)
+                    L = (a.mx[i] * (V(i + 1, j, k) - 2.0 * v0 + V(i - 1, j, k))) * a.ihx2 +
+                        (a.mz[k] * (V(i, j, k + 1) - 2.0 * v0 + V(i, j, k - 1))) * a.ihz2;
+                else if (a.planar)
+                    L = (a.lx * (V(i + 1, j, k) - 2.0 * v0 + V(i - 1, j, k))) + (a.lz * (V(i, j, k + 1) - 2.0 * v0 + V(i, j, k - 1)));
+                else if (a.var)
                     L = (a.mx[i] * (V(i + 1, j, k) - 2.0 * v0 + V(i - 1, j, k))) * a.ihx2 +
                         (a.my[j] * (V(i, j + 1, k) - 2.0 * v0 + V(i, j - 1, k))) * a.ihy2 +
                         (a.mz[k] * (V(i, j, k + 1) - 2.0 * v0 + V(i, j, k - 1))) * a.ihz2;
@@ -1065,15 +1075,17 @@ __global__ void k_diag(Vel V, View3<const double> T, int has_t, int nP0, int nP1
         double a = (V.v[0](i - 1, j, k) + V.v[0](i, j, k)) / 2.0;
         double b = (V.v[1](i, j - 1, k) + V.v[1](i, j, k)) / 2.0;
         double c = (V.v[2](i, j, k - 1) + V.v[2](i, j, k)) / 2.0;
-        // tseries.cc:150-165: the cell volume from the collocated metrics
-        const double dvp = u.var ? (u.h[0] / u.gcp[0][i]) * (u.h[1] / u.gcp[1][j]) * (u.h[2] / u.gcp[2][k]) : dv;
-        e += (a * a + b * b + c * c) * dvp;
+        // tseries.cc:150-165: the cell volume from the collocated metrics (2D: x and z, tseries.cc:149-156)
+        const double dvp = u.planar ? (u.h[0] / u.gcp[0][i]) * (u.h[2] / u.gcp[2][k])
+                           : u.var  ? (u.h[0] / u.gcp[0][i]) * (u.h[1] / u.gcp[1][j]) * (u.h[2] / u.gcp[2][k])
+                                    : dv;
+        e += (u.planar ? a * a + c * c : a * a + b * b + c * c) * dvp;
         if (has_t) w += ((V.v[2](i, j, k) + V.v[2](i, j, k - 1)) / 2.0) * T(i, j, k) * dvp;
         if (i < nc0 && j < nc1 && k < nc2) {
             double tx = (div_m(u, 0, i, j, k) * (V.v[0](i, j, k) - V.v[0](i - 1, j, k))) * u.ih[0];
             double ty = (div_m(u, 1, i, j, k) * (V.v[1](i, j, k) - V.v[1](i, j - 1, k))) * u.ih[1];
             double tz = (div_m(u, 2, i, j, k) * (V.v[2](i, j, k) - V.v[2](i, j, k - 1))) * u.ih[2];
-            dmax = fmax(dmax, tx + ty + tz);
+            dmax = fmax(dmax, u.planar ? tx + tz : tx + ty + tz);
         }
     }
     e = warp_sum(e); w = warp_sum(w); dmax = warp_max(dmax);
@@ -1111,7 +1123,7 @@ static void add_op(BcProgram &pg, int kind, const int lo[3], const int hi[3], co
 
 // mpidata::syncData at np = 1 (mpidata.cc:82-306): periodic faces over the
 // core range of the other axes, then the four x-y edges over the core z range.
-static void add_sync_ops(BcProgram &pg, const FieldInfo &f, bool xPer, bool yPer) {
+static void add_sync_ops(BcProgram &pg, const FieldInfo &f, bool xPer, bool yPer, bool planar) {
     int cx = f.n[0], cy = f.n[1], cz = f.n[2];
     int lx = f.stag[0] ? 1 : 0, hx = cx - 1 - (f.stag[0] ? 1 : 0);
     int ly = f.stag[1] ? 1 : 0, hy = cy - 1 - (f.stag[1] ? 1 : 0);
@@ -1121,6 +1133,7 @@ static void add_sync_ops(BcProgram &pg, const FieldInfo &f, bool xPer, bool yPer
         int lo2[3] = {cx, 0, 0}, hi2[3] = {cx, cy - 1, cz - 1}, sh2[3] = {lx - cx, 0, 0};
         add_op(pg, OP_COPY, lo2, hi2, sh2, 0);
     }
+    if (planar) return;   // 2D: no y and no edge neighbours (parallel.cc:118-130, hydro.cc:188-191)
     if (yPer) {
         int lo[3] = {0, -1, 0}, hi[3] = {cx - 1, -1, cz - 1}, sh[3] = {0, hy + 1, 0};
         add_op(pg, OP_COPY, lo, hi, sh, 0);
@@ -1161,9 +1174,11 @@ static void add_wall_op(BcProgram &pg, const FieldInfo &f, const Wall &w) {
 
 // hydro::initVBC (hydro.cc:287-371) and scalar::initTBC (scalar.cc:185-227), in
 // the order imposeU/V/W/TBCs apply them: Lft, Rgt, Frn, Bak, Top, Bot.
-static std::vector<Wall> walls_for(const saras_params &p, int field) {
+static std::vector<Wall> walls_for(const saras_params &p, int field, bool planar) {
     std::vector<Wall> w;
-    auto add = [&](WallKind k, int wall, double v) { w.push_back(Wall{k, wall, v}); };
+    // 2D: no front and back walls, no Vy boundary objects (hydro.cc:298-301, 320-353, scalar.cc:197-200)
+    auto add = [&](WallKind k, int wall, double v) { if (!(planar && wall / 2 == 1)) w.push_back(Wall{k, wall, v}); };
+    if (planar && field == SARAS_FIELD_VY) return w;
     if (field == SARAS_FIELD_VX) {
         if (!p.xPer) { if (p.probType == 3) { add(W_DIR_FC, 0, 1.0); add(W_NEU, 1, 0.0); } else { add(W_DIR_FC, 0, 0.0); add(W_DIR_FC, 1, 0.0); } }
         if (!p.yPer) { add(W_DIR_CC, 2, 0.0); add(W_DIR_CC, 3, 0.0); }
@@ -1203,10 +1218,11 @@ static void set_field_info(Ctx &c, int field, bool xs, bool ys, bool zs) {
         f.blo[d] = 0; f.bhi[d] = f.n[d] - 1;
         if (st[d] && !per[d]) { f.blo[d] += 1; f.bhi[d] -= 1; }   // field.cc:206-219
     }
+    if (c.planar) { f.blo[1] = 0; f.bhi[1] = 0; }                  // field.cc:221-224
     f.full.nops = 0; f.sync.nops = 0;
-    add_sync_ops(f.sync, f, per[0], per[1]);
-    add_sync_ops(f.full, f, per[0], per[1]);
-    for (const Wall &w : walls_for(c.p, field)) add_wall_op(f.full, f, w);
+    add_sync_ops(f.sync, f, per[0], per[1], c.planar);
+    add_sync_ops(f.full, f, per[0], per[1], c.planar);
+    for (const Wall &w : walls_for(c.p, field, c.planar)) add_wall_op(f.full, f, w);
     for (int d = 0; d < 3; ++d) {
         f.full.blo[d] = f.sync.blo[d] = f.blo[d];
         f.full.bhi[d] = f.sync.bhi[d] = f.bhi[d];
@@ -1239,6 +1255,10 @@ static int grid_metrics(Ctx &c) {
             for (int i = -1; i < n[st] + 1; ++i)
                 c.hcoord[d][st][i + 1] = st ? Ld * xi(i) : Ld * (xi(i) + xi(i + 1)) / 2.0;
             total += 3 * (size_t)len;
+        }
+        if (c.planar && d == 1) {   // grid.cc:300-320: y coordinates keep their default 1
+            for (int st = 0; st < 2; ++st) std::fill(c.hcoord[1][st].begin(), c.hcoord[1][st].end(), 1.0);
+            continue;
         }
         if (gtype[d] != 2) continue;
         c.stretched = true;
@@ -1273,10 +1293,13 @@ int fields_setup(Ctx &c) {
     const saras_params &p = c.p;
     int ind[3] = {p.xInd, p.yInd, p.zInd};
     double L[3] = {p.Lx, p.Ly, p.Lz};
+    c.planar = p.yInd == 0;
+    if (c.planar) L[1] = 1.0;                                   // grid.cc:88-92: yLen = dEt = 1
     for (int d = 0; d < 3; ++d) {
         c.Ns[d] = int(std::pow(2, ind[d])) + 1;                 // grid.cc:155-164
         c.Nc[d] = c.Ns[d] - 1;
         c.dXi[d] = 1.0 / double(c.Ns[d] - 1);                   // grid.cc:84-86
+        if (c.planar && d == 1) { c.Ns[1] = 1; c.Nc[1] = 1; c.dXi[1] = 1.0; }   // grid.cc:183-188, 232-234
         c.ih[d] = 1.0 / c.dXi[d];                               // derivative.cc:67-69
         c.ih2[d] = std::pow(c.ih[d], 2.0);
         c.L[d] = L[d];
@@ -1302,7 +1325,8 @@ int fields_setup(Ctx &c) {
     c.totalVol = 0.0;                                                 // tseries.cc:90-108
     const double *wx = c.hmet[0][0][0].data() + 1, *wy = c.hmet[1][0][0].data() + 1, *wz = c.hmet[2][0][0].data() + 1;
     for (int iX = 0; iX < c.Ns[0]; iX++) for (int iY = 0; iY < c.Ns[1]; iY++) for (int iZ = 0; iZ < c.Ns[2]; iZ++)
-        c.totalVol += (c.dXi[0] / wx[iX]) * (c.dXi[1] / wy[iY]) * (c.dXi[2] / wz[iZ]);
+        c.totalVol += c.planar ? (c.dXi[0] / wx[iX]) * (c.dXi[2] / wz[iZ])   // tseries.cc:93-99
+                               : (c.dXi[0] / wx[iX]) * (c.dXi[1] / wy[iY]) * (c.dXi[2] / wz[iZ]);
 
     set_field_info(c, SARAS_FIELD_VX, false, true, true);
     set_field_info(c, SARAS_FIELD_VY, true, false, true);
@@ -1399,6 +1423,7 @@ static Vel make_vel(const Ctx &c) {
 
 int vfield_compute_diff(Ctx &c) {
     for (int q = 0; q < 3; ++q) {
+        if (c.planar && q == 1) continue;   // 2D: Vy takes no part (vfield.cc:119-131)
         UC u = make_uc(c, SARAS_FIELD_VX + q);
         Box b = core_box(c.info[SARAS_FIELD_VX + q]);
         dim3 g, bl; box_launch_dims(b, g, bl);
@@ -1411,6 +1436,7 @@ int vfield_compute_diff(Ctx &c) {
 int vfield_compute_nlin(Ctx &c) {
     Vel V = make_vel(c);
     for (int q = 0; q < 3; ++q) {
+        if (c.planar && q == 1) continue;
         UC u = make_uc(c, SARAS_FIELD_VX + q);
         Box b = core_box(c.info[SARAS_FIELD_VX + q]);
         dim3 g, bl; box_launch_dims(b, g, bl);
@@ -1446,6 +1472,7 @@ int sfield_gradient(Ctx &c, int sf) {
     if (sf != SARAS_FIELD_P && sf != SARAS_FIELD_PP) return SARAS_BAD_ARG;
     UC u = make_uc(c, SARAS_FIELD_P);
     for (int q = 0; q < 3; ++q) {
+        if (c.planar && q == 1) continue;   // sfield.cc:167-169
         Box b = core_box(c.info[SARAS_FIELD_VX + q]);
         dim3 g, bl; box_launch_dims(b, g, bl);
         View3<double> G = mview(c, SARAS_FIELD_GRAD_X + q);
@@ -1503,11 +1530,13 @@ static void cn_setup(Ctx &c, int comp, CnArgs &a, CnFast &fa) {
     a.full = full_box(f);
     // Metrics: every component's xix2/ety2/ztz2 equal pow(1/L,2) on uniform grids
     // (the T solve's ztz2Colloc of scalar_d3.cc:551,570 has the same value).
+    // In 2D (dEt = 1) hy2hz2, hx2hy2 and hx2hy2hz2 equal the 2D coefficients hz2,
+    // hx2 and hz2hx2 exactly (hydro.cc:225-232); the y term is left out.
     double xix2 = c.m2[0], ety2 = c.m2[1], ztz2 = c.m2[2];
     a.c1 = c.hy2hz2 * xix2;
-    a.c2 = c.hz2hx2 * ety2;
+    a.c2 = c.planar ? 0.0 : c.hz2hx2 * ety2;
     a.c3 = c.hx2hy2 * ztz2;
-    double B = (c.hy2hz2 * xix2 + c.hz2hx2 * ety2) + c.hx2hy2 * ztz2;
+    double B = c.planar ? c.hy2hz2 * xix2 + c.hx2hy2 * ztz2 : (c.hy2hz2 * xix2 + c.hz2hx2 * ety2) + c.hx2hy2 * ztz2;
     a.dt = c.dt;
     if (!c.scalar) {
         a.scalarForm = 0;
@@ -1538,6 +1567,7 @@ static void cn_setup(Ctx &c, int comp, CnArgs &a, CnFast &fa) {
     a.Re = c.p.Re;
     a.ihx2 = 1.0 / (c.dXi[0] * c.dXi[0]); a.ihy2 = 1.0 / (c.dXi[1] * c.dXi[1]); a.ihz2 = 1.0 / (c.dXi[2] * c.dXi[2]);
     a.var = c.stretched ? 1 : 0;
+    a.planar = c.planar ? 1 : 0;
     fa.rhs = a.rhs; fa.prog = a.prog; fa.full = a.full;
     fa.c1 = a.c1; fa.c2 = a.c2; fa.c3 = a.c3;
     fa.k1 = a.scalarForm ? (a.dt * a.coef) / a.X : a.dt / a.X;
@@ -1576,6 +1606,7 @@ int compute_rhs(Ctx &c) {
     bool fast = c.p.fastKernels != 0;
     Rhs3Args a3;   // fastKernels = 2: one k_rhs_df3 launch for the three components
     for (int q = 0; q < 3; ++q) {
+        if (c.planar && q == 1) continue;   // hydro_d2.cc:222-240: Vx and Vz only
         a.H = mview(c, SARAS_FIELD_NSE_X + q);
         a.F = cview(c, SARAS_FIELD_VX + q);
         a.u = make_uc(c, SARAS_FIELD_VX + q);
@@ -1807,6 +1838,7 @@ static int cn_solve_delta(Ctx &c, int comp, int field, const CnFast &fa, double 
 int cn_solve(Ctx &c, int comp, int *iters, double *maxerr) {
     if (comp < 0 || comp > 3) return SARAS_BAD_ARG;
     if (comp == 3 && !c.scalar) return SARAS_BAD_ARG;
+    if (comp == 1 && c.planar) { c.err = "the 2D solver has no Vy equation"; return SARAS_BAD_ARG; }
     int field = comp == 3 ? SARAS_FIELD_T : SARAS_FIELD_VX + comp;
     const FieldInfo &f = c.info[field];
     CnArgs a;
@@ -1887,6 +1919,7 @@ int project(Ctx &c, bool with_bc) {
     prof_begin(c, PK_PROJECT, 0);
     double bytes = 0;
     for (int q = 0; q < 3; ++q) {
+        if (c.planar && q == 1) continue;   // 2D: the y gradient is 0, Vy unchanged
         int field = SARAS_FIELD_VX + q;
         const FieldInfo &f = c.info[field];
         Box fb = full_box(f);
@@ -1979,8 +2012,9 @@ int compute_tstp(Ctx &c, double *dt) {
     SARAS_CUDA_TRY(cudaStreamSynchronize(c.stream));
     int s = check_launch(c, "computeTStp");
     if (s) return s;
-    const double Umax = c.hscal[48], Vmax = c.hscal[49], Wmax = c.hscal[50];
-    *dt = c.p.courantNumber * (c.dXi[0] / Umax + c.dXi[1] / Vmax + c.dXi[2] / Wmax);
+    const double Umax = c.hscal[48], Vmax = c.planar ? 1.0 : c.hscal[49], Wmax = c.hscal[50];
+    const double dely = c.planar ? 0.0 : c.dXi[1];   // vfield.cc:273-279
+    *dt = c.p.courantNumber * (c.dXi[0] / Umax + dely / Vmax + c.dXi[2] / Wmax);
     return SARAS_OK;
 }
 
@@ -2084,6 +2118,7 @@ int time_advance(Ctx &c, saras_step_stats *st) {
     int s = compute_rhs(c);
     if (s) { for (int &q : c.n0Fresh) q = 0; return s; }
     for (int q = 0; q < 3; ++q) {
+        if (c.planar && q == 1) continue;   // hydro_d2.cc:242-244: solveVx, solveVz
         int it = 0; double e = 0;
         s = cn_solve(c, q, &it, &e);
         local.cn_iters[q] = it;
@@ -2107,7 +2142,11 @@ int time_advance(Ctx &c, saras_step_stats *st) {
         s = cn_solve(c, 3, &it, &e);
         local.cn_iters[3] = it;
         if (s) { local.status = s; if (st) *st = local; return s; }
-        for (int q = 0; q < 3; ++q) { s = apply_bc(c, SARAS_FIELD_VX + q); if (s) return s; }
+        for (int q = 0; q < 3; ++q) {
+            if (c.planar && q == 1) continue;   // scalar_d2.cc:309-311: imposeUBCs, imposeWBCs, imposeTBCs
+            s = apply_bc(c, SARAS_FIELD_VX + q);
+            if (s) return s;
+        }
         s = apply_bc(c, SARAS_FIELD_T);
         if (s) return s;
     }
@@ -2241,7 +2280,7 @@ extern "C" int saras_cn_solve_noalloc(const saras_params *p, int component, doub
         return SARAS_TOO_LARGE;
     }
     f.full.nops = 0;
-    add_sync_ops(f.full, f, per[0], per[1]);
+    add_sync_ops(f.full, f, per[0], per[1], false);   // 3D only (yInd >= 2 checked above)
     Wall walls[6];
     int nw = walls_fixed(*p, field, walls);
     for (int q = 0; q < nw; ++q) add_wall_op(f.full, f, walls[q]);
@@ -2255,7 +2294,8 @@ extern "C" int saras_cn_solve_noalloc(const saras_params *p, int component, doub
         else { nu = std::sqrt(p->Pr / p->Ra); kappa = 1.0 / std::sqrt(p->Pr * p->Ra); }
     }
     CnArgs a;
-    a.var = 0;   // uniform meshes only (checked above)
+    a.var = 0;   // uniform 3D meshes only (checked above)
+    a.planar = 0;
     a.mx = a.my = a.mz = nullptr;
     {
         View3<double> w = make_view<double>(const_cast<double *>(rhs), f.n[0], f.n[1], f.n[2]);

@@ -75,6 +75,7 @@ struct MgBC {
     int dirichlet;      // Dirichlet check (TEST_POISSON)
     int zeroBC;         // homogeneous Dirichlet (levels > 0)
     int tgtPads;        // residual pads: 0 = reference (z ghost 0, non-periodic 0), 1 = mirror/periodic
+    int planar;         // 2D: one y point, y never periodic (poisson_d2.cc)
 };
 
 struct MgK {            // level stencil constants
@@ -85,7 +86,9 @@ struct MgK {            // level stencil constants
     // (poisson.cc:463-495) and spacings, read at each point
     const double *xix2, *xixx, *ety2, *etyy, *ztz2, *ztzz;
     double hx, hy, hz, hxhy, hyhz, hzhx, hxhyhz, ihx2, ihy2, ihz2, i2hx, i2hy, i2hz;
+    double hx2, hz2;   // 2D (poisson.cc:406-409, 426-428)
     int var;
+    int planar;        // 2D: the x-z stencils of poisson_d2.cc (with var set, metrics from the arrays)
 };
 
 static MgK make_k(const Level &L) {
@@ -98,7 +101,9 @@ static MgK make_k(const Level &L) {
     k.hx = L.hx; k.hy = L.hy; k.hz = L.hz; k.hxhy = L.hxhy; k.hyhz = L.hyhz; k.hzhx = L.hzhx; k.hxhyhz = L.hxhyhz;
     k.ihx2 = L.ihx2; k.ihy2 = L.ihy2; k.ihz2 = L.ihz2;
     k.i2hx = 1.0 / (2.0 * L.hx); k.i2hy = 1.0 / (2.0 * L.hy); k.i2hz = 1.0 / (2.0 * L.hz);   // exact: powers of two
+    k.hx2 = L.hx2; k.hz2 = L.hz2;
     k.var = L.xix2 != nullptr;
+    k.planar = L.planar;
     return k;
 }
 
@@ -132,6 +137,10 @@ template <typename T>
 __device__ __forceinline__ T mg_update(T E, T W, T N, T S, T U, T D, T r, const MgK &k, int x, int y, int z) {
     using K = KSel<T>;
     if constexpr (sizeof(T) == 8) {
+        if (k.planar)   // poisson_d2.cc:126-131
+            return (k.hz2 * k.xix2[x] * (E + W) * 2.0 + k.hz2 * k.xixx[x] * (E - W) * k.hx + k.hx2 * k.ztz2[z] * (U + D) * 2.0 +
+                    k.hx2 * k.ztzz[z] * (U - D) * k.hz - 2.0 * k.hzhx * r) /
+                   (4.0 * (k.hz2 * k.xix2[x] + k.hx2 * k.ztz2[z]));
         if (k.var)
             return (k.hyhz * k.xix2[x] * (E + W) * 2.0 + k.hyhz * k.xixx[x] * (E - W) * k.hx + k.hzhx * k.ety2[y] * (N + S) * 2.0 +
                     k.hzhx * k.etyy[y] * (N - S) * k.hy + k.hxhy * k.ztz2[z] * (U + D) * 2.0 + k.hxhy * k.ztzz[z] * (U - D) * k.hz -
@@ -146,6 +155,9 @@ template <typename T>
 __device__ __forceinline__ T mg_lap(T E, T W, T N, T S, T U, T D, T C, const MgK &k, int x, int y, int z) {
     using K = KSel<T>;
     if constexpr (sizeof(T) == 8) {
+        if (k.planar)   // poisson_d2.cc:97-100
+            return k.xix2[x] * (E - 2.0 * C + W) * k.ihx2 + k.xixx[x] * (E - W) * k.i2hx + k.ztz2[z] * (U - 2.0 * C + D) * k.ihz2 +
+                   k.ztzz[z] * (U - D) * k.i2hz;
         if (k.var)
             return k.xix2[x] * (E - 2.0 * C + W) * k.ihx2 + k.xixx[x] * (E - W) * k.i2hx + k.ety2[y] * (N - 2.0 * C + S) * k.ihy2 +
                    k.etyy[y] * (N - S) * k.i2hy + k.ztz2[z] * (U - 2.0 * C + D) * k.ihz2 + k.ztzz[z] * (U - D) * k.i2hz;
@@ -243,6 +255,14 @@ __global__ void k_mg_restrict(View3<T> rc, View3<const T> t, MgBC bcf, MgBC bcc)
     int i, j, k;
     if (!core_pt(bcc.E, i, j, k)) return;
     int i2 = 2 * i, j2 = 2 * j, k2 = 2 * k;
+    if (bcf.planar) {   // poisson_d2.cc:207-225: 9-point full weighting in the y = 0 plane
+        const bool in2 = i2 > 0 && k2 > 0 && i2 < bcf.E[0] && k2 < bcf.E[2];
+        auto Q = [&](int a, int c) -> T { return in2 ? t(a, 0, c) : pad_val(t, a, 0, c, bcf); };
+        T facePoints = (Q(i2 + 1, k2) + Q(i2 - 1, k2) + Q(i2, k2 + 1) + Q(i2, k2 - 1)) * (T)0.125;
+        T vertPoints = (Q(i2 + 1, k2 + 1) + Q(i2 + 1, k2 - 1) + Q(i2 - 1, k2 + 1) + Q(i2 - 1, k2 - 1)) * (T)0.0625;
+        rc(i, 0, k) = facePoints + vertPoints + t(i2, 0, k2) * (T)0.25;
+        return;
+    }
     bool interior = i2 > 0 && j2 > 0 && k2 > 0 && i2 < bcf.E[0] && j2 < bcf.E[1] && k2 < bcf.E[2];
     auto T_ = [&](int a, int b, int c) -> T { return interior ? t(a, b, c) : pad_val(t, a, b, c, bcf); };
     T facePoints = (T_(i2 + 1, j2, k2) + T_(i2 - 1, j2, k2) + T_(i2, j2 + 1, k2) + T_(i2, j2 - 1, k2) +
@@ -1836,8 +1856,9 @@ __global__ void __launch_bounds__(kTailThreads) k_mg_tail(TailArgs<T> a) {
 // ------------------------------------------------------------------ host
 static MgBC level_bc(const Ctx &c, int l, bool tgt) {
     MgBC b;
-    b.per[0] = c.p.xPer; b.per[1] = c.p.yPer; b.per[2] = c.p.zPer;
+    b.per[0] = c.p.xPer; b.per[1] = c.planar ? 0 : c.p.yPer; b.per[2] = c.p.zPer;
     for (int d = 0; d < 3; ++d) b.E[d] = c.lv[l].n[d];
+    b.planar = c.planar ? 1 : 0;
     b.dirichlet = c.p.testPoisson && !tgt;
     b.zeroBC = (l != 0);
     b.tgtPads = tgt ? 1 : 0;
@@ -2064,6 +2085,7 @@ int mg_setup(Ctx &c) {
     for (int l = 0; l <= c.depth; ++l) {
         Level &L = c.lv[l];
         for (int d = 0; d < 3; ++d) L.n[d] = int(std::pow(2, ind[d] - l));          // poisson.cc:336-357
+        if (c.planar) L.n[1] = 0;                                                      // poisson.cc:339-340: one y point
         L.count = (long)(L.n[0] + 3) * (L.n[1] + 3) * (L.n[2] + 3);
         double s = std::pow(2, l);
         double dXi = c.dXi[0], dEt = c.dXi[1], dZt = c.dXi[2];
@@ -2078,7 +2100,9 @@ int mg_setup(Ctx &c) {
         L.den = 4.0 * (L.hyhz * xix2 + L.hzhx * ety2 + L.hxhy * ztz2);
         L.ihx2 = 1.0 / (L.hx * L.hx); L.ihy2 = 1.0 / (L.hy * L.hy); L.ihz2 = 1.0 / (L.hz * L.hz);
         L.lx = xix2 * L.ihx2; L.ly = ety2 * L.ihy2; L.lz = ztz2 * L.ihz2;
-        if (c.stretched) {
+        L.hx2 = std::pow(s * dXi, 2.0); L.hz2 = std::pow(s * dZt, 2.0);
+        L.planar = c.planar ? 1 : 0;
+        if (c.stretched || c.planar) {   // the stencils read the metrics at each point
             // poisson.cc:463-495: the staggered metrics of the finest grid at every
             // 2^l-th point on the level's core, 0 at its two ghost indices
             const int s2 = 1 << l;
@@ -2117,7 +2141,7 @@ int mg_setup(Ctx &c) {
     SARAS_CUDA_TRY(cudaFuncSetAttribute(k_mg_gs_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGsBlockSmem));
     SARAS_CUDA_TRY(cudaMemsetAsync(c.dflag, 0, 3 * sizeof(int), c.stream));
     if (int e = plane_setup(c)) return e;
-    c.tailLt = tail_level(c);
+    c.tailLt = c.planar ? 0 : tail_level(c);   // target modes only (3D)
     if (c.tailLt > 0) {
         SARAS_CUDA_TRY(cudaFuncSetAttribute(k_mg_tail<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         SARAS_CUDA_TRY(cudaFuncSetAttribute(k_mg_tail<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));

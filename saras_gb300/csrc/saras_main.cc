@@ -69,6 +69,19 @@ void taylor_green(saras_ctx *ctx, const saras_params &p) {
     std::vector<double> xs = coords(ctx, 0, 1), xc = coords(ctx, 0, 0), ys = coords(ctx, 1, 1), yc = coords(ctx, 1, 0),
                         zs = coords(ctx, 2, 1);
     Field vx = host_field(ctx, SARAS_FIELD_VX), vy = host_field(ctx, SARAS_FIELD_VY);
+    if (p.yInd == 0) {   // 2D (taylorGreen.cc:57-79): u and w on the y = 0 plane
+        std::vector<double> zc = coords(ctx, 2, 0);
+        Field vz = host_field(ctx, SARAS_FIELD_VZ);
+        for (int i = -1; i < vx.dims[0] - 1; ++i)
+            for (int k = -1; k < vx.dims[2] - 1; ++k)
+                vx.at(i, 0, k) = std::sin(2.0 * M_PI * xc[i + 1] / L[0]) * std::cos(2.0 * M_PI * zs[k + 1] / L[2]);
+        for (int i = -1; i < vz.dims[0] - 1; ++i)
+            for (int k = -1; k < vz.dims[2] - 1; ++k)
+                vz.at(i, 0, k) = -std::cos(2.0 * M_PI * xs[i + 1] / L[0]) * std::sin(2.0 * M_PI * zc[k + 1] / L[2]);
+        check(saras_upload(ctx, SARAS_FIELD_VX, vx.v.data()), ctx, "upload Vx");
+        check(saras_upload(ctx, SARAS_FIELD_VZ, vz.v.data()), ctx, "upload Vz");
+        return;
+    }
     for (int i = -1; i < vx.dims[0] - 1; ++i)
         for (int j = -1; j < vx.dims[1] - 1; ++j)
             for (int k = -1; k < vx.dims[2] - 1; ++k)
