@@ -21,7 +21,7 @@ def load(name):
     return np.load(path)
 
 
-@pytest.mark.parametrize("name,steps", [("ldc33", 3), ("rbc65", 1), ("tgv65gs", 2), ("tgv129", 0)])
+@pytest.mark.parametrize("name,steps", [("ldc33", 3), ("rbc65", 1), ("tgv65gs", 2), ("tgv129", 1)])
 def test_fixture_replays_on_the_oracle(name, steps):
     ref = load(name)
     p, kind, total = M.case_params(name)
