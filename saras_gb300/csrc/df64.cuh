@@ -21,41 +21,24 @@
 namespace saras {
 
 __device__ __forceinline__ void dsplit(double x, float &hi, float &lo) {
-    unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    unsigned h = (unsigned)(b >> 32), l = (unsigned)b;
-    unsigned sign = h & 0x80000000u;
-    int e = (int)((h >> 20) & 0x7ffu);
-    int fe = e - 896;   // float biased exponent of hi (1023 - 127 = 896)
-    unsigned fr = ((h & 0xfffffu) << 3) | (l >> 29);
-    unsigned hb;
-    if (fe >= 1 && fe <= 254) hb = sign | ((unsigned)fe << 23) | fr;
-    else if (e == 2047) hb = ((h & 0xfffffu) | l) ? 0x7fc00000u : (sign | 0x7f800000u);
-    else if (fe > 254) hb = sign | 0x7f800000u;
-    else hb = sign;
-    hi = __uint_as_float(hb);
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned h = (unsigned)(b >> 32), l = (unsigned)b;
+    const unsigned sign = h & 0x80000000u;
+    const unsigned e = (h >> 20) & 0x7ffu;
+    // hi for 897 <= e <= 1150: float exponent e - 896 above the top 23 fraction
+    // bits.  (h:l) << 3 holds e mod 512 in bits 31..23 above those bits, and
+    // 896 = 384 mod 512, so one subtraction rebases the exponent.
+    unsigned hb = (__funnelshift_l(l, h, 3) - (384u << 23)) & 0x7fffffffu;
+    if (e < 897u) hb = 0u;
+    else if (e > 1150u) hb = (e == 2047u && ((h & 0xfffffu) | l)) ? 0x7fc00000u : 0x7f800000u;
+    hi = __uint_as_float(hb | sign);
     // lo = (l mod 2^29) 2^(e-1075): its top 23 bits m as a float by the
     // magic-number conversion (2^(E-127) (1 + m 2^-23) - 2^(E-127) = m 2^(E-150),
-    // exact), with E - 150 = e - 1069, i.e. E = e - 919.
-    int me = e - 919;
-    unsigned m23 = (l & 0x1fffffffu) >> 6;
-    float mag = 0.0f;
-    if (me >= 1 && me <= 254) mag = __uint_as_float(((unsigned)me << 23) | m23) - __uint_as_float((unsigned)me << 23);
-    lo = sign ? -mag : mag;
-}
-
-// The high part of dsplit alone (x truncated to a float).
-__device__ __forceinline__ float dhi(double x) {
-    unsigned h = (unsigned)((unsigned long long)__double_as_longlong(x) >> 32);
-    unsigned sign = h & 0x80000000u;
-    int e = (int)((h >> 20) & 0x7ffu);
-    int fe = e - 896;
-    unsigned fr = ((h & 0xfffffu) << 3) | ((unsigned)__double_as_longlong(x) >> 29);
-    unsigned hb;
-    if (fe >= 1 && fe <= 254) hb = sign | ((unsigned)fe << 23) | fr;
-    else if (e == 2047) hb = 0x7fc00000u | sign;
-    else if (fe > 254) hb = sign | 0x7f800000u;
-    else hb = sign;
-    return __uint_as_float(hb);
+    // exact), with E - 150 = e - 1069, i.e. E = e - 919; 0 outside 1 <= E <= 254.
+    const unsigned me = e - 919u, base = me << 23;
+    float mag = __uint_as_float(base | ((l & 0x1fffffffu) >> 6)) - __uint_as_float(base);
+    if (me - 1u >= 254u) mag = 0.0f;
+    lo = __uint_as_float(__float_as_uint(mag) | sign);
 }
 
 __device__ __forceinline__ double f2d(float f) {
@@ -113,6 +96,25 @@ __device__ __forceinline__ fpair fp_fma(fpair a, fpair b, fpair c) {
     two_sum(p, c.h, s, t);
     t += e + fmaf(a.h, b.l, fmaf(a.l, b.h, c.l));
     return fp_norm(s, t);
+}
+
+// Unnormalised forms for accumulation chains: the second float carries the
+// rounding errors and cross terms without the final FastTwoSum, so it may be a
+// few ulps of the first.  Products and TwoSums of such pairs keep about 2^-44
+// of the result (the cross terms a.h b.l are formed in float from a b.l a few
+// ulps of a.h b.h); a chain ends in one fp_norm.
+__device__ __forceinline__ fpair fp_mul_u(fpair a, fpair b) {
+    float p = a.h * b.h;
+    float e = fmaf(a.h, b.h, -p);
+    return fpair{p, fmaf(a.h, b.l, fmaf(a.l, b.h, e))};
+}
+
+__device__ __forceinline__ fpair fp_fma_u(fpair a, fpair b, fpair c) {
+    float p = a.h * b.h;
+    float e = fmaf(a.h, b.h, -p);
+    float s, t;
+    two_sum(p, c.h, s, t);
+    return fpair{s, t + (e + fmaf(a.h, b.l, fmaf(a.l, b.h, c.l)))};
 }
 
 __device__ __forceinline__ fpair fp_of(double x) {

@@ -455,18 +455,30 @@ __device__ __forceinline__ fpair sum4_pair(fpair a, fpair b, fpair c, fpair d) {
     return fpair{s, (e1 + e2 + e3) + ((a.l + b.l) + (c.l + d.l))};
 }
 
-template <int C>
-__device__ __forceinline__ void rhs3_point(const Rhs3Args &a, const float2 (*sm)[4][kR3N], int i, int j, int k, int c0) {
+// a + b + c as an unnormalised pair.
+__device__ __forceinline__ fpair sum3_pair(fpair a, fpair b, fpair c) {
+    float s1, e1, s, e2;
+    two_sum(a.h, b.h, s1, e1);
+    two_sum(s1, c.h, s, e2);
+    return fpair{s, (e1 + e2) + ((a.l + b.l) + c.l)};
+}
+
+__device__ __forceinline__ fpair fp_scale(fpair a, float f) { return fpair{a.h * f, a.l * f}; }
+
+// ISO: equal spacing and metrics on the three axes, where KL_0 = KL_1 = KL_2 and
+// the advection constants are KN_C along the component's own axis and KN_C / 4
+// (exactly: the same FP64 value divided by 4 before the split) for the two
+// four-point averages, so the three Laplacians take one product and the three
+// advection terms one more.  The sums are accumulated unnormalised and
+// normalised once.
+// G(f, di, dj, dk): field f at (i + di, j + dj, k + dk) as a float pair.
+template <int C, bool ISO, class Get>
+__device__ __forceinline__ void rhs3_point(const Rhs3Args &a, const Get &G, int i, int j, int k) {
     if (i >= a.n[C][0] || j >= a.n[C][1] || k >= a.n[C][2]) return;
-    auto G = [&](int f, int di, int dj, int dk) -> fpair {
-        float2 v = sm[(i + di) & 3][f][c0 + dj * kR3K + dk];
-        return fpair{v.x, v.y};
-    };
     const long o = (long)(i + 1) * a.sx[C] + (long)(j + 1) * a.sy[C] + (k + 1);
     const Rhs3K &q = a.q[C];
     fpair c = G(C, 0, 0, 0), ex = G(C, 1, 0, 0), wx = G(C, -1, 0, 0);
     fpair ey = G(C, 0, 1, 0), wy = G(C, 0, -1, 0), ez = G(C, 0, 0, 1), wz = G(C, 0, 0, -1);
-    fpair acc = fp_fma(q.kl[0], lap_pair(ex, wx, c), fp_fma(q.kl[1], lap_pair(ey, wy, c), fp_mul(q.kl[2], lap_pair(ez, wz, c))));
     fpair s0, s1, s2, dp;
     if (C == 0) {
         s0 = c;
@@ -484,18 +496,32 @@ __device__ __forceinline__ void rhs3_point(const Rhs3Args &a, const float2 (*sm)
         s2 = c;
         dp = sub_pair(G(3, 0, 0, 1), G(3, 0, 0, 0));
     }
-    acc = fp_fma(fp_neg(q.kn[0]), fp_mul(s0, sub_pair(ex, wx)), acc);
-    acc = fp_fma(fp_neg(q.kn[1]), fp_mul(s1, sub_pair(ey, wy)), acc);
-    acc = fp_fma(fp_neg(q.kn[2]), fp_mul(s2, sub_pair(ez, wz)), acc);
+    const fpair d0 = sub_pair(ex, wx), d1 = sub_pair(ey, wy), d2 = sub_pair(ez, wz);
+    fpair acc;
+    if (ISO) {
+        acc = fp_mul_u(q.kl[0], sum3_pair(lap_pair(ex, wx, c), lap_pair(ey, wy, c), lap_pair(ez, wz, c)));
+        fpair adv;
+        if (C == 0) adv = fp_fma_u(s0, d0, fp_scale(fp_fma_u(s1, d1, fp_mul_u(s2, d2)), 0.25f));
+        else if (C == 1) adv = fp_fma_u(s1, d1, fp_scale(fp_fma_u(s0, d0, fp_mul_u(s2, d2)), 0.25f));
+        else adv = fp_fma_u(s2, d2, fp_scale(fp_fma_u(s0, d0, fp_mul_u(s1, d1)), 0.25f));
+        acc = fp_fma_u(fp_neg(q.kn[C]), adv, acc);
+    } else {
+        acc = fp_fma_u(q.kl[0], lap_pair(ex, wx, c), fp_fma_u(q.kl[1], lap_pair(ey, wy, c), fp_mul_u(q.kl[2], lap_pair(ez, wz, c))));
+        acc = fp_fma_u(fp_neg(q.kn[0]), fp_mul_u(s0, d0), acc);
+        acc = fp_fma_u(fp_neg(q.kn[1]), fp_mul_u(s1, d1), acc);
+        acc = fp_fma_u(fp_neg(q.kn[2]), fp_mul_u(s2, d2), acc);
+    }
     if (C == 2 && a.buoyancy) {
         long ot = (long)(i + 1) * a.sx[3] + (long)(j + 1) * a.sy[3] + (k + 1);
-        acc = fp_fma(q.kb, fp_add(fp_of(a.T[ot]), fp_of(a.T[ot + 1])), acc);
+        acc = fp_fma_u(q.kb, fp_add(fp_of(a.T[ot]), fp_of(a.T[ot + 1])), acc);
     }
-    acc = fp_fma(fp_neg(q.kg), dp, acc);
+    acc = fp_fma_u(fp_neg(q.kg), dp, acc);
+    acc = fp_norm(acc.h, acc.l);
     a.n0h[C][o] = acc.h;
     a.n0l[C][o] = acc.l;
 }
 
+template <bool ISO>
 __global__ void __launch_bounds__(256, 5) k_rhs_df3(Rhs3Args a) {
     __shared__ float2 sm[4][4][kR3N];
     const int tid = threadIdx.y * 32 + threadIdx.x;
@@ -532,10 +558,28 @@ __global__ void __launch_bounds__(256, 5) k_rhs_df3(Rhs3Args a) {
     for (int i = i0; i < iend; ++i) {
         load_plane(i + 1);
         __syncthreads();
-        rhs3_point<0>(a, sm, i, j, k, c0);
-        rhs3_point<1>(a, sm, i, j, k, c0);
-        rhs3_point<2>(a, sm, i, j, k, c0);
+        auto G = [&](int f, int di, int dj, int dk) -> fpair {
+            float2 v = sm[(i + di) & 3][f][c0 + dj * kR3K + dk];
+            return fpair{v.x, v.y};
+        };
+        rhs3_point<0, ISO>(a, G, i, j, k);
+        rhs3_point<1, ISO>(a, G, i, j, k);
+        rhs3_point<2, ISO>(a, G, i, j, k);
     }
+}
+
+// The constants of every component have the isotropic form rhs3_point's ISO
+// path assumes (bitwise: the same pairs, and a quarter of the own axis's
+// advection constant on the other two).
+static bool rhs3_iso(const Rhs3Args &a) {
+    auto same = [](fpair x, fpair y) { return x.h == y.h && x.l == y.l; };
+    for (int q = 0; q < 3; ++q) {
+        const Rhs3K &k = a.q[q];
+        if (!same(k.kl[0], k.kl[1]) || !same(k.kl[0], k.kl[2])) return false;
+        for (int d = 0; d < 3; ++d)
+            if (d != q && !same(k.kn[d], fpair{k.kn[q].h * 0.25f, k.kn[q].l * 0.25f})) return false;
+    }
+    return true;
 }
 
 static RhsFast make_rhs_fast(const Ctx &c, double visc) {
@@ -894,7 +938,7 @@ constexpr int kCnMarch = 8;
 constexpr bool kCnColumns = true;
 
 template <bool FINAL>
-__global__ void __launch_bounds__(256, 5) k_cn_delta(CnDelta a) {
+__global__ void __launch_bounds__(256, 4) k_cn_delta(CnDelta a) {
     int k, j, i0;
     bool on;
     if (kCnColumns) {
@@ -915,18 +959,29 @@ __global__ void __launch_bounds__(256, 5) k_cn_delta(CnDelta a) {
         bool bulkJK = j >= a.prog.blo[1] && j <= a.prog.bhi[1] && k >= a.prog.blo[2] && k <= a.prog.bhi[2];
         if (bulkJK && iend == i0 + kCnMarch && i0 >= a.prog.blo[0] && iend - 1 <= a.prog.bhi[0]) {
             // a whole segment of bulk points: branch-free, the column's own i-1 / i / i+1
-            // high parts carried in registers, every load of the segment in flight together
-            long o = a.off(i0, j, k);
+            // values carried in registers, and every store after the segment's last
+            // load (the output arrays may alias the inputs as far as the compiler
+            // can tell, so a store between loads would hold the later loads back)
+            const long o = a.off(i0, j, k);
             fpair dm = cn_d(a, o - a.sx), dc = cn_d(a, o);
+            fpair out[kCnMarch];
+            double v[kCnMarch];
 #pragma unroll
-            for (int q = 0; q < kCnMarch; ++q, o += a.sx) {
-                fpair dp = cn_d(a, o + a.sx);
+            for (int q = 0; q < kCnMarch; ++q) {
+                const long oq = o + q * a.sx;
+                fpair dp = cn_d(a, oq + a.sx);
                 fpair corr;
-                fpair out = cn_delta_update(a, o, dc, dp, dm, cn_d(a, o + a.sy), cn_d(a, o - a.sy), cn_d(a, o + 1), cn_d(a, o - 1), corr);
+                out[q] = cn_delta_update(a, oq, dc, dp, dm, cn_d(a, oq + a.sy), cn_d(a, oq - a.sy), cn_d(a, oq + 1), cn_d(a, oq - 1), corr);
+                if (FINAL) v[q] = (a.C0[oq] + f2d(out[q].h)) + f2d(out[q].l);
                 m = max(m, __float_as_uint(corr.h) & 0x7fffffffu);
-                cn_delta_store<FINAL>(a, o, out);
                 dm = dc;
                 dc = dp;
+            }
+#pragma unroll
+            for (int q = 0; q < kCnMarch; ++q) {
+                const long oq = o + q * a.sx;
+                if (FINAL) a.vout[oq] = v[q];
+                else { a.oh[oq] = out[q].h; a.ol[oq] = out[q].l; }
             }
             iend = i0;   // segment done (the generic loop below runs no iteration)
         }
@@ -1647,7 +1702,8 @@ int compute_rhs(Ctx &c) {
                 for (int d = 0; d < 3; ++d) a3.nu[d] = std::max(std::max(a3.n[0][d], a3.n[1][d]), std::max(a3.n[2][d], a3.n[3][d]));
                 a3.buoyancy = a.buoyancy;
                 dim3 gr((a3.nu[2] + 31) / 32, (a3.nu[1] + 7) / 8, (a3.nu[0] + kRhs3March - 1) / kRhs3March);
-                k_rhs_df3<<<gr, dim3(32, 8, 1), 0, c.stream>>>(a3);
+                if (rhs3_iso(a3)) k_rhs_df3<true><<<gr, dim3(32, 8, 1), 0, c.stream>>>(a3);
+                else k_rhs_df3<false><<<gr, dim3(32, 8, 1), 0, c.stream>>>(a3);
                 count_launch(c);
                 break;
             }
