@@ -426,6 +426,7 @@ struct Rhs3Args {
     const double *T;           // buoyancy: T, in P's layout
     float *n0h[3], *n0l[3];    // A of each component, component layouts
     int nu[3];                 // union of the cores
+    int edgeK;                 // nu[2] - 1 when it is a multiple of 32 (the tiles then end below it), else -1
     int buoyancy;
     Rhs3K q[3];
 };
@@ -525,6 +526,21 @@ template <bool ISO>
 __global__ void __launch_bounds__(256, 5) k_rhs_df3(Rhs3Args a) {
     __shared__ float2 sm[4][4][kR3N];
     const int tid = threadIdx.y * 32 + threadIdx.x;
+    if (a.edgeK >= 0 && blockIdx.x == gridDim.x - 1) {
+        // the last column k = edgeK, (i, j) numbered j fastest, one point a thread
+        // with its operands read from global memory (a 32-wide tile there would run
+        // every warp's instructions for one active lane)
+        const long t = ((long)blockIdx.z * gridDim.y + blockIdx.y) * 256 + tid;
+        if (t >= (long)a.nu[0] * a.nu[1]) return;
+        const int i = (int)(t / a.nu[1]), j = (int)(t - (long)i * a.nu[1]), k = a.edgeK;
+        auto G = [&](int f, int di, int dj, int dk) -> fpair {
+            return fp_of(a.f[f][(long)(i + di + 1) * a.sx[f] + (long)(j + dj + 1) * a.sy[f] + (k + dk + 1)]);
+        };
+        rhs3_point<0, ISO>(a, G, i, j, k);
+        rhs3_point<1, ISO>(a, G, i, j, k);
+        rhs3_point<2, ISO>(a, G, i, j, k);
+        return;
+    }
     const int k0 = blockIdx.x * 32, j0 = blockIdx.y * 8, i0 = blockIdx.z * kRhs3March;
     const int iend = min(i0 + kRhs3March, a.nu[0]);
     int js[2], ks[2];
@@ -1701,7 +1717,10 @@ int compute_rhs(Ctx &c) {
                 }
                 for (int d = 0; d < 3; ++d) a3.nu[d] = std::max(std::max(a3.n[0][d], a3.n[1][d]), std::max(a3.n[2][d], a3.n[3][d]));
                 a3.buoyancy = a.buoyancy;
-                dim3 gr((a3.nu[2] + 31) / 32, (a3.nu[1] + 7) / 8, (a3.nu[0] + kRhs3March - 1) / kRhs3March);
+                // rows of 32 m + 1 points: m tiles of 32 and one block column for the last point
+                a3.edgeK = (a3.nu[2] > 32 && (a3.nu[2] - 1) % 32 == 0) ? a3.nu[2] - 1 : -1;
+                dim3 gr(a3.edgeK >= 0 ? a3.edgeK / 32 + 1 : (a3.nu[2] + 31) / 32, (a3.nu[1] + 7) / 8,
+                        (a3.nu[0] + kRhs3March - 1) / kRhs3March);
                 if (rhs3_iso(a3)) k_rhs_df3<true><<<gr, dim3(32, 8, 1), 0, c.stream>>>(a3);
                 else k_rhs_df3<false><<<gr, dim3(32, 8, 1), 0, c.stream>>>(a3);
                 count_launch(c);
