@@ -441,6 +441,8 @@ def run_ours(args, dist):
         achieved = (b_k / n_k) / (avg_ms * 1e-3) / 1e9 if avg_ms > 0 else 0.0
         pc = per_cycle.get(names[k])
         n_all = pc * sum(vc) if pc else n_k
+        if pc and names[k] == "mg_smooth_fp32":
+            n_all -= sum(rs)   # each refinement step's first cycle starts from zero: its first two sweeps are one launch
         roofs.append({"kernel": names[k], "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                       "frac": round(achieved / peak, 4), "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
                       "traffic": ncu_traffic(names[k]), "traffic_source": "ncu capture, profiles/ncu_traffic.md",

@@ -999,6 +999,53 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 6 : 5) k_tgt_sweep(T *__
     }
 }
 
+// The zero start and the sweep after it in one launch (FP32 levels).  The
+// first sweep from 0 is pointwise, s1 = ar1 r (k_tgt_sweep<T, true>), so the
+// second reads s1 at its stencil points as ar1 r there: the same FP32 products
+// the first launch would have stored, in the same order, so the result is the
+// two launches' bits, for 8 bytes a point (r in, iterate out) instead of 20.
+template <typename T>
+__global__ void __launch_bounds__(256, 6) k_tgt_sweep2z(T *__restrict__ out, const T *__restrict__ r, int sx, int sy, MgBC bc,
+                                                       TgK<T> c1, TgK<T> c2) {
+    int j, k, seg;
+    if (!col_of<sizeof(T) == 8>(bc, j, k, seg)) return;
+    const int i0 = seg * kIch;
+    const int n = min(kIch, bc.E[0] - i0 + 1);
+    const NbrJK nb = nbr_jk(j, k, sy, bc);
+    const long o0 = (long)(i0 + 1) * sx + (long)(j + 1) * sy + (k + 1);
+    const T a1 = c1.ar;
+    T cm = a1 * r[o0 + nbr_x(i0, -1, sx, bc)];
+    if (n == kIch && i0 + kIch <= bc.E[0]) {   // a full column segment: every load before the first store
+        T nc[kIch + 1], ns[kIch], ud[kIch], rr[kIch];
+#pragma unroll
+        for (int q = 0; q < kIch; ++q) {
+            long o = o0 + (long)q * sx;
+            nc[q + 1] = a1 * r[o + sx];
+            ns[q] = a1 * r[o + nb.yp] + a1 * r[o + nb.ym];
+            ud[q] = a1 * r[o + nb.zp] + a1 * r[o + nb.zm];
+            rr[q] = r[o];
+        }
+        nc[0] = a1 * rr[0];
+#pragma unroll
+        for (int q = 0; q < kIch; ++q) {
+            T v = fma(c2.ax, cm + nc[q + 1], fma(c2.ay, ns[q], fma(c2.az, ud[q], fma(c2.ar, rr[q], c2.om1 * nc[q]))));
+            cm = nc[q];
+            out[o0 + (long)q * sx] = v;
+        }
+        return;
+    }
+    T cc = a1 * r[o0];
+    for (int q = 0; q < n; ++q) {
+        long o = o0 + (long)q * sx;
+        T cp = a1 * r[o + nbr_x(i0 + q, 1, sx, bc)];
+        T ns = a1 * r[o + nb.yp] + a1 * r[o + nb.ym], ud = a1 * r[o + nb.zp] + a1 * r[o + nb.zm];
+        T v = fma(c2.ax, cm + cp, fma(c2.ay, ns, fma(c2.az, ud, fma(c2.ar, r[o], c2.om1 * cc))));
+        cm = cc;
+        cc = cp;
+        out[o] = v;
+    }
+}
+
 // Target-mode prolongation + add (vertex-centred trilinear) on the core (the
 // target-mode kernels read face neighbours at their images, so no ghost layer
 // is written).  A thread owns a fine (j, k)
@@ -2295,6 +2342,18 @@ static int smooth(Ctx &c, int l, int count, bool zero_first, bool tgt) {
         prof_begin(c, pk, l);
         const double lb = (n == 0 && zero_first) ? bytes * 2.0 / 3.0 : bytes;   // a zero start reads no iterate
         if (tgt) {
+            if constexpr (sizeof(T) == 4) {
+                if (n == 0 && zero_first && count >= 2 && !(l == 0 && c.planeOk)) {
+                    // sweeps 0 and 1 in one launch, written where the second would leave
+                    // the iterate (the current buffer: two flips), so no flip
+                    TgK<T> tk2 = make_tgk<T>(L, smooth_weight(c, 1, count));
+                    k_tgt_sweep2z<T><<<gm, bm, 0, c.stream>>>(A_<T>(L), R_<T>(L), sx, sy, bc, tk, tk2);
+                    count_launch(c);
+                    prof_end(c, pk, l, lb);
+                    ++n;
+                    continue;
+                }
+            }
             if (n == 0 && zero_first) k_tgt_sweep<T, true><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
             else if constexpr (sizeof(T) == 4) {
                 if (l == 0 && c.planeOk) plane_launch(c, 0, B_<T>(L), A_<T>(L), R_<T>(L), bc, tk);
