@@ -950,11 +950,14 @@ __device__ __forceinline__ fpair cn_delta_boundary(const CnDelta &a, int i, int 
 // (blockIdx.y the segment), else 32 x 8 tiles (blockIdx.z the segment), which
 // leave the last tile of each 259-point row with three active lanes a warp
 // (the final sweep: 189 us in columns against 192 in tiles at 257^3).
-constexpr int kCnMarch = 8;
+// Segment length and blocks an SM, measured on the final sweep at 257^3: 4
+// points with six blocks (40 registers) 159 us, 4 with five 163, 8 with four
+// 171, 16 with three 197.
+constexpr int kCnMarch = 4;
 constexpr bool kCnColumns = true;
 
 template <bool FINAL>
-__global__ void __launch_bounds__(256, 4) k_cn_delta(CnDelta a) {
+__global__ void __launch_bounds__(256, 6) k_cn_delta(CnDelta a) {
     int k, j, i0;
     bool on;
     if (kCnColumns) {
