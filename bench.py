@@ -704,6 +704,81 @@ def study_tgv513(args):
             "data": "synthetic (Taylor-Green initial condition)"}
 
 
+def ldc33_params():
+    """The plain method's own configuration: lid-driven cavity in the unit cube,
+    33^3 points, 4 multigrid levels, Re 1000, lid Vx = 1 on z = 1, no-slip
+    elsewhere, zero initial state (P = 1), dt 1e-3, Crank-Nicolson and damped
+    Jacobi V(3,3) cycles to 1e-8: the reference's algorithm (the drop-in mode)."""
+    from saras_gb300 import _abi
+    p = _abi.default_params()
+    p.probType, p.icType = 1, 0
+    p.xPer = p.yPer = p.zPer = 0
+    p.Lx = p.Ly = p.Lz = 1.0
+    p.xInd = p.yInd = p.zInd = 5
+    p.vcDepth = 3
+    p.Re = 1000.0
+    p.tStp = 1.0e-3
+    p.cnTolerance = 1.0e-8
+    p.mgTolerance = 1.0e-8
+    p.preSmooth = p.postSmooth = 3
+    p.gsSmooth = 0
+    p.vcCount = 200
+    p.resType = 1
+    return p
+
+
+def study_ldc33(args):
+    """The drop-in (reference algorithm, FP64 throughout) on the cavity at 33^3
+    for 200 steps on the GPU, and the same steps of the reference's algorithm on
+    the host cores (the oracle, OpenMP) for a bounded sample: steps/s, V-cycles
+    and Jacobi iterations per step on both."""
+    import numpy as np
+    import saras_gb300 as S
+    from saras_gb300 import _abi as F
+    steps = args.study_steps or 200
+
+    def init(x, p):
+        x.set(F.FIELD_P, np.ones(x.dims(F.FIELD_P)))
+        for f in (F.FIELD_VX, F.FIELD_VY, F.FIELD_VZ):
+            x.apply_bc(f)
+
+    p = ldc33_params()
+    g = S.Solver(p)
+    init(g, p)
+    g.synchronize()
+    vc, cn = [], []
+    t0 = time.perf_counter()
+    for k in range(steps):
+        s, st = g.time_advance()
+        if s != 0:
+            raise RuntimeError("drop-in step failed: %d" % s)
+        vc.append(st.vcycles)
+        cn.append(sum(st.cn_iters))
+    g.synchronize()
+    gpu_s = time.perf_counter() - t0
+    launches = g.launch_count()
+    g.close()
+    out = {"study": "plain method, lid-driven cavity 33^3 (the drop-in)", "workload":
+           "LDC 33^3, unit cube, Re 1000, dt 1e-3, %d steps, CN Jacobi to 1e-8, Jacobi V(3,3) to 1e-8, FP64 throughout" % steps,
+           "gpu": {"steps": steps, "seconds": round(gpu_s, 3), "steps_per_s": round(steps / gpu_s, 3),
+                   "vcycles_per_step": round(sum(vc) / steps, 2), "ms_per_vcycle": round(1e3 * gpu_s / max(1, sum(vc)), 4),
+                   "cn_iterations_per_step": round(sum(cn) / steps, 2), "launches": launches}}
+    if not args.no_cpu:
+        from oracle.oracle import Oracle
+        o = Oracle(ldc33_params())
+        init(o, p)
+        n, vco, t0 = 0, [], time.perf_counter()
+        while n < steps and time.perf_counter() - t0 < args.cpu_seconds:
+            s, st = o.time_advance()
+            vco.append(st.vcycles)
+            n += 1
+        cpu_s = time.perf_counter() - t0
+        out["cpu_oracle"] = {"steps": n, "seconds": round(cpu_s, 3), "steps_per_s": round(n / cpu_s, 3),
+                             "vcycles_per_step": round(sum(vco) / max(1, n), 2), "cores": os.cpu_count(),
+                             "kind": "port", "same_counts_as_gpu": vco == vc[:n]}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -721,15 +796,15 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=30.0)
-    ap.add_argument("--workload", default="tgv257", choices=["tgv257", "rbc_learned", "tgv513"],
-                    help="tgv257: the headline line; rbc_learned, tgv513: the learned and at-scale studies")
+    ap.add_argument("--workload", default="tgv257", choices=["tgv257", "rbc_learned", "tgv513", "ldc33"],
+                    help="tgv257: the headline line; rbc_learned, tgv513, ldc33: the learned, at-scale and drop-in studies")
     ap.add_argument("--study-steps", type=int, default=0, help="total steps of a study (0: its configured count)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     args.learned = args.guess == "learned"
     if args.workload != "tgv257":
-        study = study_rbc_learned if args.workload == "rbc_learned" else study_tgv513
+        study = {"rbc_learned": study_rbc_learned, "tgv513": study_tgv513, "ldc33": study_ldc33}[args.workload]
         print(json.dumps(study(args)), flush=True)
         return
     dist = Dist()

@@ -80,6 +80,7 @@ struct MgBC {
 
 struct MgK {            // level stencil constants
     double cx, cy, cz, c7, den;
+    double iden;       // RN(1 / den), for div_rn
     double lx, ly, lz;
     float fcx, fcy, fcz, fc7, fden, flx, fly, flz;
     // stretched meshes (var != 0, reference mode): the level's metric arrays
@@ -94,6 +95,7 @@ struct MgK {            // level stencil constants
 static MgK make_k(const Level &L) {
     MgK k;
     k.cx = L.cx; k.cy = L.cy; k.cz = L.cz; k.c7 = L.c7; k.den = L.den;
+    k.iden = 1.0 / L.den;
     k.lx = L.lx; k.ly = L.ly; k.lz = L.lz;
     k.fcx = (float)L.cx; k.fcy = (float)L.cy; k.fcz = (float)L.cz; k.fc7 = (float)L.c7; k.fden = (float)L.den;
     k.flx = (float)L.lx; k.fly = (float)L.ly; k.flz = (float)L.lz;
@@ -129,6 +131,19 @@ template <> struct KSel<float> {
     static __device__ __forceinline__ float lz(const MgK &k) { return k.flz; }
 };
 
+// x / d correctly rounded for a divisor d whose reciprocal y = RN(1/d) is
+// known: Markstein's correction step (P. Markstein, IBM J. Res. Develop. 34(1),
+// 1990): q = RN(x y), r = x - q d exactly by an FMA, then RN(q + r y) = RN(x / d)
+// for x and x / d in the normal range (checked against IEEE division on 10^8
+// random pairs, all-ones and power-of-two significands included).  Three FP64
+// operations in place of a division subroutine, on a part whose FP64 pipe bounds
+// every reference-form kernel.  A zero x gives +0 where the division gives -0
+// for negative x: zeros compare and add alike.
+__device__ __forceinline__ double div_rn(double x, double d, double y) {
+    const double q = x * y;
+    return fma(fma(-q, d, x), y, q);
+}
+
 // Smoother update, the expression of poisson_d3.cc:156-163 at point (x, y, z).
 // Uniform grid: the xixx, etyy, ztzz terms are exactly zero and omitted, the
 // metric products are level constants.  Stretched mesh (FP64 only): every
@@ -147,7 +162,9 @@ __device__ __forceinline__ T mg_update(T E, T W, T N, T S, T U, T D, T r, const 
                     2.0 * k.hxhyhz * r) /
                    (4.0 * (k.hyhz * k.xix2[x] + k.hzhx * k.ety2[y] + k.hxhy * k.ztz2[z]));
     }
-    return ((K::cx(k) * (E + W)) * (T)2.0 + (K::cy(k) * (N + S)) * (T)2.0 + (K::cz(k) * (U + D)) * (T)2.0 - K::c7(k) * r) / K::den(k);
+    const T num = (K::cx(k) * (E + W)) * (T)2.0 + (K::cy(k) * (N + S)) * (T)2.0 + (K::cz(k) * (U + D)) * (T)2.0 - K::c7(k) * r;
+    if constexpr (sizeof(T) == 8) return div_rn(num, k.den, k.iden);
+    return num / K::den(k);
 }
 // Laplacian, the expression of poisson_d3.cc:99-105 at point (x, y, z); the
 // divisions by (hx*hx) and (2*hx) are multiplications by exact reciprocals.
@@ -2370,6 +2387,14 @@ static int smooth(Ctx &c, int l, int count, bool zero_first, bool tgt) {
     return chk(c, "mg smooth");
 }
 
+// Threads of the single-CTA coarsest Gauss-Seidel solve.  Its wavefront stages
+// hold at most (X + 1)(Y + 1) points (25 on a 5^3 level, one warp); the residual
+// check after each sweep takes the whole level.  Measured on the 33^3 cavity
+// (217 sweeps a V-cycle on the 5^3 level): 2.91 ms a V-cycle with 128 threads,
+// 2.98 with 64, 3.03 with 256, 3.26 with 32; dealing a stage's points across
+// the warps instead of packing them into one was slower (3.04).
+constexpr int kCoarseThreads = 128;
+
 template <typename T>
 static int coarse_solve(Ctx &c, bool tgt) {
     Level &L = c.lv[c.depth];
@@ -2380,7 +2405,7 @@ static int coarse_solve(Ctx &c, bool tgt) {
     // V-cycle's own error reduction (about 0.1), so 1e-3 of the initial residual
     T tol = tgt ? (T)1.0e-3 : (T)c.p.mgTolerance;
     int maxc = tgt ? 500 : c.maxCount;
-    k_mg_coarse<T><<<1, 256, smem, c.stream>>>(lview<T>(L, A_<T>(L)), lcview<T>(L, R_<T>(L)), kk, bc, tol, maxc, tgt ? 1 : 0,
+    k_mg_coarse<T><<<1, kCoarseThreads, smem, c.stream>>>(lview<T>(L, A_<T>(L)), lcview<T>(L, R_<T>(L)), kk, bc, tol, maxc, tgt ? 1 : 0,
                                                (long long *)(c.dscal + 40));
     count_launch(c);
     return chk(c, "mg coarse");
