@@ -685,6 +685,7 @@ struct CnArgs {
     Box full;
     double c1, c2, c3;       // hy2hz2*xix2, hz2hx2*ety2, hx2hy2*ztz2
     double dt, X, coef, Dn;  // hydro: X = hx2hy2hz2*2*Re, Dn = 1 + dt*B/(Re*hx2hy2hz2)
+    double iX, iDn;          // RN(1/X), RN(1/Dn): the divisions as div_rn
     int scalarForm;          // scalar_d3: ((A*dt)*coef)/X + rhs, Dn = 1 + (dt*coef)*B/h
     double lx, ly, lz;       // residual: metric * 1/(h*h)
     double resCoef;          // inverseRe (hydro) or nu / kappa (scalar)
@@ -711,8 +712,8 @@ __device__ __forceinline__ double cn_guess(const CnArgs &a, int i, int j, int k)
     }
     double A = a.planar ? c1 * (V(i + 1, j, k) + V(i - 1, j, k)) + c3 * (V(i, j, k + 1) + V(i, j, k - 1))
                         : c1 * (V(i + 1, j, k) + V(i - 1, j, k)) + c2 * (V(i, j + 1, k) + V(i, j - 1, k)) + c3 * (V(i, j, k + 1) + V(i, j, k - 1));
-    double num = a.scalarForm ? (A * a.dt) * a.coef / a.X : (A * a.dt) / a.X;
-    return (num + a.rhs(i, j, k)) / Dn;
+    double num = div_rn(a.scalarForm ? (A * a.dt) * a.coef : A * a.dt, a.X, a.iX);
+    return a.var ? (num + a.rhs(i, j, k)) / Dn : div_rn(num + a.rhs(i, j, k), Dn, a.iDn);
 }
 
 __global__ void k_cn(CnArgs a) {
@@ -1617,6 +1618,8 @@ static void cn_setup(Ctx &c, int comp, CnArgs &a, CnFast &fa) {
         a.coef = 0;
         a.X = c.hx2hy2hz2 * 2.0 * c.p.Re;
         a.Dn = 1.0 + c.dt * B / (c.p.Re * c.hx2hy2hz2);
+        a.iX = 1.0 / a.X;
+        a.iDn = 1.0 / a.Dn;
         a.resCoef = c.inverseRe;
     } else {
         double coef = comp == 3 ? c.kappa : c.nu;
@@ -1624,6 +1627,8 @@ static void cn_setup(Ctx &c, int comp, CnArgs &a, CnFast &fa) {
         a.coef = coef;
         a.X = c.hx2hy2hz2 * 2.0;
         a.Dn = 1.0 + c.dt * coef * B / c.hx2hy2hz2;
+        a.iX = 1.0 / a.X;
+        a.iDn = 1.0 / a.Dn;
         a.resCoef = coef;
     }
     // residual: metric*(...)/(h*h); h*h is a power of two, so /(h*h) == *(1/(h*h))
@@ -2389,12 +2394,16 @@ extern "C" int saras_cn_solve_noalloc(const saras_params *p, int component, doub
         a.scalarForm = 0; a.coef = 0;
         a.X = hx2hy2hz2 * 2.0 * p->Re;
         a.Dn = 1.0 + p->tStp * B / (p->Re * hx2hy2hz2);
+        a.iX = 1.0 / a.X;
+        a.iDn = 1.0 / a.Dn;
         a.resCoef = 1.0 / p->Re;
     } else {
         double coef = component == 3 ? kappa : nu;
         a.scalarForm = 1; a.coef = coef;
         a.X = hx2hy2hz2 * 2.0;
         a.Dn = 1.0 + p->tStp * coef * B / hx2hy2hz2;
+        a.iX = 1.0 / a.X;
+        a.iDn = 1.0 / a.Dn;
         a.resCoef = coef;
     }
     a.lx = m2[0] * (1.0 / (dXi[0] * dXi[0]));

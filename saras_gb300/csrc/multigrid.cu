@@ -131,19 +131,6 @@ template <> struct KSel<float> {
     static __device__ __forceinline__ float lz(const MgK &k) { return k.flz; }
 };
 
-// x / d correctly rounded for a divisor d whose reciprocal y = RN(1/d) is
-// known: Markstein's correction step (P. Markstein, IBM J. Res. Develop. 34(1),
-// 1990): q = RN(x y), r = x - q d exactly by an FMA, then RN(q + r y) = RN(x / d)
-// for x and x / d in the normal range (checked against IEEE division on 10^8
-// random pairs, all-ones and power-of-two significands included).  Three FP64
-// operations in place of a division subroutine, on a part whose FP64 pipe bounds
-// every reference-form kernel.  A zero x gives +0 where the division gives -0
-// for negative x: zeros compare and add alike.
-__device__ __forceinline__ double div_rn(double x, double d, double y) {
-    const double q = x * y;
-    return fma(fma(-q, d, x), y, q);
-}
-
 // Smoother update, the expression of poisson_d3.cc:156-163 at point (x, y, z).
 // Uniform grid: the xixx, etyy, ztzz terms are exactly zero and omitted, the
 // metric products are level constants.  Stretched mesh (FP64 only): every
@@ -2391,8 +2378,10 @@ static int smooth(Ctx &c, int l, int count, bool zero_first, bool tgt) {
 // hold at most (X + 1)(Y + 1) points (25 on a 5^3 level, one warp); the residual
 // check after each sweep takes the whole level.  Measured on the 33^3 cavity
 // (217 sweeps a V-cycle on the 5^3 level): 2.91 ms a V-cycle with 128 threads,
-// 2.98 with 64, 3.03 with 256, 3.26 with 32; dealing a stage's points across
-// the warps instead of packing them into one was slower (3.04).
+// 2.98 with 64, 3.03 with 256, 3.26 with 32.  Slower, and not kept: a stage's
+// points dealt across the warps instead of packed into one (3.04); the residual
+// check formed inside the sweep, plane s - 2 by the block's second half during
+// stage s (3.20: the two halves share the SM's FP64 pipe).
 constexpr int kCoarseThreads = 128;
 
 template <typename T>
