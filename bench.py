@@ -779,6 +779,72 @@ def study_ldc33(args):
     return out
 
 
+def ldc2d_params(ind=6):
+    """The reference's 2D cavity check (its tests/ldcTest input): Re 1000, unit
+    square in x-z ("Y Index" 0), lid Vx = 1 on z = 1, Gauss-Seidel V(2,2) cycles
+    on five levels, at most 7 a step, multigrid and Jacobi tolerances 1e-6, the
+    CFL time step (Courant number 0.1) capped at 1e-3, to t = 50; here on 65 x 65
+    points (X and Z Index 6) where the check uses 129 x 129."""
+    from saras_gb300 import _abi
+    p = _abi.default_params()
+    p.probType, p.icType = 1, 0
+    p.xPer = p.yPer = p.zPer = 0
+    p.Lx = p.Ly = p.Lz = 1.0
+    p.xInd, p.yInd, p.zInd = ind, 0, ind
+    p.vcDepth = 4
+    p.Re = 1000.0
+    p.tStp, p.tMax = 1.0e-3, 50.0
+    p.useCFL, p.courantNumber = 1, 0.1
+    p.cnTolerance = p.mgTolerance = 1.0e-6
+    p.gsSmooth, p.preSmooth, p.postSmooth = 1, 2, 2
+    p.vcCount = 7
+    p.resType = 1
+    p.ioCnt = 1000
+    return p
+
+
+def study_ldc2d_ghia(args):
+    """The 2D cavity at Re 1000 to t = 50 (the drop-in's 2D solver), then its
+    centre-line profiles -- u along x = 0.5 against the height, w along z = 0.5
+    against x -- against Ghia, Ghia and Shin (1982) as the reference ships them
+    (tests/golden/ghia_re1000.npz, made by tests/golden/make_ghia.py)."""
+    import numpy as np
+    import saras_gb300 as S
+    from saras_gb300 import _abi as F
+    p = ldc2d_params(args.grid_index)
+    if args.study_steps:
+        p.tMax = args.study_steps * p.tStp
+    h = S.hydro_d3(p)
+    g = h.solver
+    vc = []
+    t0 = time.perf_counter()
+    series = h.solvePDE(on_step=lambda hh, st: vc.append(st.vcycles))
+    secs = time.perf_counter() - t0
+    ghia = np.load(os.path.join(ROOT, "tests", "golden", "ghia_re1000.npz"))
+    xc, xs = g.grid_coords(0, False), g.grid_coords(0, True)
+    zc, zs = g.grid_coords(2, False), g.grid_coords(2, True)
+    Vx, Vz = g.get(F.FIELD_VX)[:, 1, :], g.get(F.FIELD_VZ)[:, 1, :]
+    # Vx: cell centres along x, vertices along z; Vz: vertices along x, cell centres along z
+    u_line = np.array([np.interp(0.5, xc, Vx[:, k]) for k in range(Vx.shape[1])])
+    w_line = np.array([np.interp(0.5, zc, Vz[i, :]) for i in range(Vz.shape[0])])
+    u = np.interp(ghia["z"], zs, u_line)
+    w = np.interp(ghia["x"], xs, w_line)
+    du, dw = u - ghia["u"], w - ghia["w"]
+    return {"study": "2D lid-driven cavity against Ghia et al. (the reference's ldcTest check)",
+            "workload": "2D LDC Re 1000, %d x %d, Gauss-Seidel V(2,2) <= 7 cycles a step, tolerances 1e-6, CFL 0.1 capped "
+                        "at dt 1e-3, to t = %g" % (2 ** p.xInd + 1, 2 ** p.zInd + 1, p.tMax),
+            "steps": h.timeStepCount, "time": round(h.time, 6), "seconds": round(secs, 2),
+            "steps_per_s": round(h.timeStepCount / secs, 1), "vcycles_per_step": round(sum(vc) / max(1, len(vc)), 2),
+            "energy_last": series[-1][1], "max_divergence_last": series[-1][2],
+            "u_centre_line": {"max_abs_dev": round(float(np.max(np.abs(du))), 4), "rms_dev": round(float(np.sqrt(np.mean(du ** 2))), 4),
+                              "min_u": round(float(u_line.min()), 4), "ghia_min_u": float(ghia["u"].min())},
+            "w_centre_line": {"max_abs_dev": round(float(np.max(np.abs(dw))), 4), "rms_dev": round(float(np.sqrt(np.mean(dw ** 2))), 4),
+                              "max_w": round(float(w_line.max()), 4), "min_w": round(float(w_line.min()), 4),
+                              "ghia_max_w": float(ghia["w"].max()), "ghia_min_w": float(ghia["w"].min())},
+            "profiles": {"z": ghia["z"].tolist(), "u": [round(float(a), 5) for a in u],
+                         "x": ghia["x"].tolist(), "w": [round(float(a), 5) for a in w]}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -796,15 +862,18 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=30.0)
-    ap.add_argument("--workload", default="tgv257", choices=["tgv257", "rbc_learned", "tgv513", "ldc33"],
-                    help="tgv257: the headline line; rbc_learned, tgv513, ldc33: the learned, at-scale and drop-in studies")
+    ap.add_argument("--workload", default="tgv257", choices=["tgv257", "rbc_learned", "tgv513", "ldc33", "ldc2d_ghia"],
+                    help="tgv257: the headline line; rbc_learned, tgv513, ldc33, ldc2d_ghia: the learned, at-scale, "
+                         "drop-in and 2D validation studies")
     ap.add_argument("--study-steps", type=int, default=0, help="total steps of a study (0: its configured count)")
+    ap.add_argument("--grid-index", type=int, default=6, help="ldc2d_ghia: X and Z Index (6: 65 x 65, 5: 33 x 33)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     args.learned = args.guess == "learned"
     if args.workload != "tgv257":
-        study = {"rbc_learned": study_rbc_learned, "tgv513": study_tgv513, "ldc33": study_ldc33}[args.workload]
+        study = {"rbc_learned": study_rbc_learned, "tgv513": study_tgv513, "ldc33": study_ldc33,
+                 "ldc2d_ghia": study_ldc2d_ghia}[args.workload]
         print(json.dumps(study(args)), flush=True)
         return
     dist = Dist()
