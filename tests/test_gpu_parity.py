@@ -8,7 +8,7 @@ The CUDA path runs the reference arithmetic in the reference order (no FMA
 contraction), so agreement is expected to the last bit for all local
 operators; reductions whose summation order differs (the padded-array mean of
 the multigrid RHS, the energy sum) agree to rounding.  The bar written in every
-assertion is the benchmark spec's tolerance: 1e-10 relative to the field's maximum.
+assertion is the drop-in's parity tolerance: 1e-10 relative to the field's maximum.
 """
 import numpy as np
 import pytest
