@@ -560,9 +560,10 @@ def run_reference(args, dist):
 
 
 # ------------------------------------------------------------------ studies
-# Two further workloads, run on request (--workload); each prints one JSON
-# line of its own.  They are the learned-warm-start and at-scale studies of
-# the same time step, not the headline metric.
+# Further workloads, run on request (--workload); each prints one JSON line of
+# its own: the learned-warm-start and at-scale studies of the same time step,
+# the plain method's drop-in configuration, and the 2D validation.  None is the
+# headline metric.
 def rbc_params(guess, ind=(8, 8, 7), depth=6, dt=5.0e-4):
     """Rayleigh-Benard convection: 257 x 257 x 129 on a 2:2:1 box, periodic
     sides, no-slip top and bottom (T = 1 bottom, 0 top), Ra 1e7, Pr 1; the
