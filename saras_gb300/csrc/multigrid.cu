@@ -32,6 +32,7 @@
 
 #include "context.cuh"
 #include "df64.cuh"
+#include <utility>
 #include "tma.cuh"
 
 #include <cudaTypedefs.h>
@@ -865,6 +866,30 @@ __device__ __noinline__ void scatter_slow(T *P, int sx, int sy, int i, int j, in
     put_scatter(V, i, j, k, v, bc);
 }
 
+// Programmatic dependent launch.  The target-mode level kernels run back to
+// back, each a few tens of microseconds at 257^3 and less below; launched with
+// programmatic stream serialisation (launch_pdl), the next kernel is launched
+// once every block of the previous one has exited, ahead of the grid's
+// completion, and waits in pdl_wait, before its first global access, until that
+// grid has completed and its writes are visible.  Launched the ordinary way,
+// pdl_wait returns at once.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... P, typename... A>
+static cudaError_t launch_pdl(void (*k)(P...), dim3 g, dim3 b, size_t smem, cudaStream_t st, A &&...args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = g;
+    cfg.blockDim = b;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k, std::forward<A>(args)...);
+}
+
 // The target-mode kernels march along x: a (32 k) x (8 j) thread tile walks
 // kIch consecutive x planes, keeping the x-1 / x / x+1 values of its column in
 // registers, so each point costs one new x-neighbour load plus the four
@@ -954,6 +979,7 @@ __device__ __forceinline__ long nbr_x(int i, int d, int sx, const MgBC &bc) {
 template <typename T, bool ZERO>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 6 : 5) k_tgt_sweep(T *__restrict__ out, const T *__restrict__ in, const T *__restrict__ r,
                                                    int sx, int sy, MgBC bc, TgK<T> c) {
+    pdl_wait();
     int j, k, seg;
     if (!col_of<sizeof(T) == 8>(bc, j, k, seg)) return;
     const int i0 = seg * kIch;
@@ -1011,6 +1037,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 6 : 5) k_tgt_sweep(T *__
 template <typename T>
 __global__ void __launch_bounds__(256, 6) k_tgt_sweep2z(T *__restrict__ out, const T *__restrict__ r, int sx, int sy, MgBC bc,
                                                        TgK<T> c1, TgK<T> c2) {
+    pdl_wait();
     int j, k, seg;
     if (!col_of<sizeof(T) == 8>(bc, j, k, seg)) return;
     const int i0 = seg * kIch;
@@ -1058,6 +1085,7 @@ __global__ void __launch_bounds__(256, 6) k_tgt_sweep2z(T *__restrict__ out, con
 template <typename T>
 __global__ void __launch_bounds__(256) k_tgt_prolong_add(T *__restrict__ pf, const T *__restrict__ pc, int sxf, int syf, int sxc, int syc,
                                                          MgBC bc) {
+    pdl_wait();
     int j, k, seg;
     if (!col_of<sizeof(T) == 8>(bc, j, k, seg)) return;
     const int i0 = seg * kIch;   // kIch is even
@@ -1099,6 +1127,7 @@ __global__ void __launch_bounds__(256) k_tgt_prolong_add(T *__restrict__ pf, con
 template <typename T, typename OT, bool MAXRED>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 6 : 5) k_tgt_residual(OT *__restrict__ out, const T *__restrict__ p, const T *__restrict__ b,
                                                       int sx, int sy, MgBC bc, TgK<T> c, double *maxres) {
+    pdl_wait();
     int j, k, seg;
     const bool on = col_of<sizeof(T) == 8>(bc, j, k, seg);
     const int i0 = seg * kIch;
@@ -1341,6 +1370,7 @@ constexpr int rr_ch() { return sizeof(T) == 8 ? 4 : 8; }
 template <typename T>
 __global__ void __launch_bounds__(256, 4) k_tgt_restrict(T *__restrict__ rc, const T *__restrict__ r, int sx, int sy, int csx, int csy,
                                                        MgBC bcf) {
+    pdl_wait();
     const int E0 = bcf.E[0], E1 = bcf.E[1], E2 = bcf.E[2];
     const int W = E2 / 2 + 1, t = blockIdx.x * blockDim.x + threadIdx.x;
     const int J = t / W, K = t - J * W, I0 = blockIdx.y * rr_ch<T>();
@@ -1762,6 +1792,7 @@ __device__ void tail_sweep(T *out, const T *in, const T *r, const MgBC &bc, cons
 
 template <typename T>
 __global__ void __launch_bounds__(kTailThreads) k_mg_tail(TailArgs<T> a) {
+    pdl_wait();
     extern __shared__ unsigned char smraw[];
     T *base = reinterpret_cast<T *>(smraw);
     T *P[kTailMaxLevels], *Q[kTailMaxLevels], *R[kTailMaxLevels];
@@ -2351,18 +2382,18 @@ static int smooth(Ctx &c, int l, int count, bool zero_first, bool tgt) {
                     // sweeps 0 and 1 in one launch, written where the second would leave
                     // the iterate (the current buffer: two flips), so no flip
                     TgK<T> tk2 = make_tgk<T>(L, smooth_weight(c, 1, count));
-                    k_tgt_sweep2z<T><<<gm, bm, 0, c.stream>>>(A_<T>(L), R_<T>(L), sx, sy, bc, tk, tk2);
+                    SARAS_CUDA_TRY(launch_pdl(k_tgt_sweep2z<T>, gm, bm, 0, c.stream, A_<T>(L), R_<T>(L), sx, sy, bc, tk, tk2));
                     count_launch(c);
                     prof_end(c, pk, l, lb);
                     ++n;
                     continue;
                 }
             }
-            if (n == 0 && zero_first) k_tgt_sweep<T, true><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
+            if (n == 0 && zero_first) SARAS_CUDA_TRY(launch_pdl(k_tgt_sweep<T, true>, gm, bm, 0, c.stream, B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk));
             else if constexpr (sizeof(T) == 4) {
                 if (l == 0 && c.planeOk) plane_launch(c, 0, B_<T>(L), A_<T>(L), R_<T>(L), bc, tk);
-                else k_tgt_sweep<T, false><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
-            } else k_tgt_sweep<T, false><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk);
+                else SARAS_CUDA_TRY(launch_pdl(k_tgt_sweep<T, false>, gm, bm, 0, c.stream, B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk));
+            } else SARAS_CUDA_TRY(launch_pdl(k_tgt_sweep<T, false>, gm, bm, 0, c.stream, B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bc, tk));
         } else if (n == 0 && zero_first)
             k_mg_sweep<T, true><<<g, b, 0, c.stream>>>(lview<T>(L, B_<T>(L)), lcview<T>(L, A_<T>(L)), lcview<T>(L, R_<T>(L)), kk, bc, omega);
         else
@@ -2420,7 +2451,8 @@ static int restrict_level(Ctx &c, int l, bool tgt) {
             }
         }
         if (!planed)
-            k_tgt_residual<T, T, false><<<gm, bm, 0, c.stream>>>(B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bcf, make_tgk<T>(L, 1.0), nullptr);
+            SARAS_CUDA_TRY(launch_pdl(k_tgt_residual<T, T, false>, gm, bm, 0, c.stream, B_<T>(L), A_<T>(L), R_<T>(L), sx, sy, bcf,
+                                      make_tgk<T>(L, 1.0), (double *)nullptr));
         count_launch(c);
         prof_end(c, pk, l, 3.0 * sizeof(T) * pts);
         pk = sizeof(T) == 8 ? PK_MG_RESTRICT64 : PK_MG_RESTRICT32;
@@ -2428,7 +2460,7 @@ static int restrict_level(Ctx &c, int l, bool tgt) {
         int csx = (C.n[1] + 3) * (C.n[2] + 3), csy = C.n[2] + 3;
         long ccols = (long)(C.n[1] + 1) * (C.n[2] + 1);
         dim3 gr((unsigned)((ccols + 255) / 256), (C.n[0] + 1 + rr_ch<T>() - 1) / rr_ch<T>(), 1);
-        k_tgt_restrict<T><<<gr, dim3(256, 1, 1), 0, c.stream>>>(R_<T>(C), B_<T>(L), sx, sy, csx, csy, bcf);
+        SARAS_CUDA_TRY(launch_pdl(k_tgt_restrict<T>, gr, dim3(256, 1, 1), 0, c.stream, R_<T>(C), B_<T>(L), sx, sy, csx, csy, bcf));
         count_launch(c);
         prof_end(c, pk, l, sizeof(T) * pts * (1.0 + 1.0 / 8.0));
         return chk(c, "mg restrict");
@@ -2456,7 +2488,8 @@ static int prolong_level(Ctx &c, int l, bool tgt, bool add) {
     if (tgt && add) {   // the core only: target-mode kernels read face neighbours at their images
         dim3 gm, bm; level_dims<T>(L, gm, bm);
         int sx = (L.n[1] + 3) * (L.n[2] + 3), sy = L.n[2] + 3;
-        k_tgt_prolong_add<T><<<gm, bm, 0, c.stream>>>(A_<T>(L), A_<T>(C), sx, sy, (C.n[1] + 3) * (C.n[2] + 3), C.n[2] + 3, bc);
+        SARAS_CUDA_TRY(launch_pdl(k_tgt_prolong_add<T>, gm, bm, 0, c.stream, A_<T>(L), A_<T>(C), sx, sy, (C.n[1] + 3) * (C.n[2] + 3),
+                                  C.n[2] + 3, bc));
     } else {
         k_mg_prolong_add<T><<<g, b, 0, c.stream>>>(lview<T>(L, A_<T>(L)), lcview<T>(C, A_<T>(C)), bc, add ? 1 : 0);
     }
@@ -2500,7 +2533,7 @@ static int tail_run(Ctx &c, int Lt) {
     a.rin = R_<T>(c.lv[Lt]);
     a.pout = A_<T>(c.lv[Lt]);
     a.iters = (long long *)(c.dscal + 40);
-    k_mg_tail<T><<<1, kTailThreads, smem, c.stream>>>(a);
+    SARAS_CUDA_TRY(launch_pdl(k_mg_tail<T>, dim3(1), dim3(kTailThreads), smem, c.stream, a));
     count_launch(c);
     return chk(c, "mg tail");
 }
