@@ -1485,7 +1485,7 @@ __global__ void __launch_bounds__(256) k_fx_refine(const long long *__restrict__
 // planes outside the core are read at their images, and the column's own
 // i - 1 / i + 1 values stay in registers.  flag: a value outside the
 // fixed-point range.
-__global__ void __launch_bounds__(256) k_fx_update(long long *__restrict__ pout, const long long *__restrict__ pin,
+__global__ void __launch_bounds__(256, 8) k_fx_update(long long *__restrict__ pout, const long long *__restrict__ pin,
                                                    const float *__restrict__ e, const long long *__restrict__ bfx,
                                                    float *__restrict__ r32, int sx, int sy, MgBC bc, int s, float rscale,
                                                    unsigned long long *maxr, int *flag, double *__restrict__ dst, double inv2s) {
@@ -1515,10 +1515,38 @@ __global__ void __launch_bounds__(256) k_fx_update(long long *__restrict__ pout,
             if (t < 340) (&tile[buf][0][0])[t] = lv[q] ? val(base + lo[q]) : 0;
         }
     };
+    unsigned long long m = 0;
+    if ((bc.E[2] & 31) == 0 && bc.E[2] >= 32 && blockIdx.x == gridDim.x - 1) {
+        // the tiles of rows of 32 m + 1 points leave their last column (k = E2) to
+        // a tile of one live lane; here it is dealt densely, a (j, segment) column
+        // a thread over the last block column, operands read at their images from
+        // global memory (integer sums: the tiles' values)
+        const long t = ((long)blockIdx.z * gridDim.y + blockIdx.y) * 256 + tid;
+        const int W = bc.E[1] + 1;
+        if (t < (long)W * gridDim.z) {
+            const int je = (int)(t % W), ie0 = (int)(t / W) * kIch, ke = bc.E[2];
+            const int ie1 = min(ie0 + kIch - 1, bc.E[0]);
+            const NbrJK nb = nbr_jk(je, ke, sy, bc);
+            long oe = (long)(ie0 + 1) * sx + (long)(je + 1) * sy + (ke + 1);
+            long long em = val(oe + nbr_x(ie0, -1, sx, bc));
+            for (int i = ie0; i <= ie1; ++i, oe += sx) {
+                const long long cc = val(oe), cp = val(oe + nbr_x(i, 1, sx, bc));
+                const long long nsum = (em + cp) + (val(oe + nb.ym) + val(oe + nb.yp)) + (val(oe + nb.zm) + val(oe + nb.zp));
+                const long long r = bfx[oe] - (nsum - 6 * cc);
+                r32[oe] = fx2f(r) * rscale;
+                const unsigned long long a = (unsigned long long)(r < 0 ? -r : r);
+                m = a > m ? a : m;
+                pout[oe] = cc;
+                if (dst) dst[oe] = __ll2double_rn(cc) * inv2s;
+                const unsigned long long ac = (unsigned long long)(cc < 0 ? -cc : cc);
+                if (ac > (1ull << 59)) bad = true;
+                em = cc;
+            }
+        }
+    } else {
     const bool active = j <= bc.E[1] && k <= bc.E[2];
     long o = (long)(i0 + 1) * sx + (long)(j + 1) * sy + (k + 1);
     long long cm = active ? val(o + nbr_x(i0, -1, sx, bc)) : 0;
-    unsigned long long m = 0;
     load_plane(i0, 0);
     for (int i = i0; i <= iend; ++i, o += sx) {
         const int b = (i - i0) % 3, bn = (i - i0 + 1) % 3;
@@ -1537,6 +1565,7 @@ __global__ void __launch_bounds__(256) k_fx_update(long long *__restrict__ pout,
             if (ac > (1ull << 59)) bad = true;
             cm = cc;
         }
+    }
     }
 #pragma unroll
     for (int off = 16; off; off >>= 1) {
