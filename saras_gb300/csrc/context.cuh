@@ -220,7 +220,6 @@ int mg_get_level(Ctx &c, int level, int which, double *host);
 int mg_test_prolong(Ctx &c, double *err);
 int mg_test_transfer(Ctx &c, double *err);
 int mg_test_periodic(Ctx &c, double *err);
-int mg_fine_residual(Ctx &c, const double *p, double *maxres, double *maxb);
 
 // ---- learned warm start (unet.cu)
 int unet_create(Ctx &c);

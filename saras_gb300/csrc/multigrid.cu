@@ -2815,12 +2815,6 @@ static int mg_solve_reference(Ctx &c, int *cycles, double *residual) {
     return SARAS_OK;
 }
 
-// FP64 max|b - A p| / max|b| of the level-0 iterate (target modes).
-int mg_fine_residual(Ctx &c, const double *pp, double *maxres, double *maxb) {
-    (void)pp; (void)maxres; (void)maxb;
-    return SARAS_OK;
-}
-
 // SARAS_MG_MIXED on an isotropic level 0: FP32 V-cycles inside the exact
 // fixed-point refinement (k_fx_refine).  On entry L0.r holds b, L0.pa() the
 // previous Pp with its face ghosts.  On return with done = true, L0.pa() holds
