@@ -67,3 +67,14 @@ def test_planar_solver_is_the_drop_in_only():
             q.gsSmooth = 0
             q.preSmooth = q.postSmooth = 3
         assert status_of(q) == _abi.BAD_CONFIG, field
+
+
+def test_2d_cavity_parameters_file_is_the_study():
+    """tests/golden/configs/ldc2d_65.yaml, the reference's 2D cavity check on 65 x 65
+    points as a parameters file, parses to the configuration of the ldc2d_ghia study."""
+    p = saras_gb300.parser(os.path.join(ROOT, "tests", "golden", "configs", "ldc2d_65.yaml"))
+    q = bench.ldc2d_params(6)
+    for k in ("probType", "xInd", "yInd", "zInd", "vcDepth", "vcCount", "gsSmooth", "preSmooth", "postSmooth", "resType",
+              "mgTolerance", "cnTolerance", "useCFL", "courantNumber", "tStp", "tMax", "Re", "xPer", "yPer", "zPer"):
+        assert getattr(p, k) == getattr(q, k), k
+    assert status_of(p) == _abi.NO_DEVICE
